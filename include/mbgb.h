@@ -1,0 +1,274 @@
+/*
+ * mbgb.h — C ABI of the GB300-native distance-estimated ray-march renderer.
+ *
+ * This library replaces one seam of Mandelbulber 1.21: the per-pixel render
+ *   void Render(sParamRender param, cImage *image, GtkWidget *outputDarea)
+ *   (src/Render3D.cpp:709), whose CPU branch (src/Render3D.cpp:719-1158) spawns
+ *   MainThread workers (src/Render3D.cpp:203) that call RayMarching
+ *   (src/Render3D.cpp:79) and the shaders (src/shaders.cpp:21-757), and whose
+ *   OpenCL branch (src/Render3D.cpp:1160-1252, CclSupport::Render
+ *   src/cl_support.cpp:527) is the existing precedent for a device drop-in.
+ *
+ * Everything crossing this boundary is plain C: POD structs, pointers, sizes.
+ * The scene struct mirrors the reference's sParamRender / sFractal / sImageAdjustments
+ * (src/fractparams.h:18-146, src/fractal.h:104-293, src/cimage.hpp:43-80) after the
+ * -nogui fix-ups (src/interface.cpp:690-729) and clamps (src/interface.cpp:3587-3602).
+ * Output layers have the element types and row-major order of cImage
+ * (src/cimage.hpp:155-162): x + y * width.
+ */
+#ifndef MBGB_H_
+#define MBGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MBGB_VERSION_MAJOR 0
+#define MBGB_VERSION_MINOR 1
+#define MBGB_VERSION_PATCH 0
+
+/* Status codes. The reference's Render() returns void and prints errors
+ * (src/cl_support.cpp:109 checkErr); every call here returns a status instead and never aborts. */
+typedef enum mbgb_status {
+  MBGB_OK = 0,
+  MBGB_ERR_BAD_PARAM = 1,   /* NULL pointer, size out of range, malformed settings */
+  MBGB_ERR_OOM = 2,         /* device or host allocation failed */
+  MBGB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  MBGB_ERR_TIMEOUT = 4,     /* a kernel hit its device-side deadline and stopped early */
+  MBGB_ERR_UNSUPPORTED = 5, /* the scene uses a feature this build does not render */
+  MBGB_ERR_IO = 6,          /* settings file could not be read / image could not be written */
+  MBGB_ERR_NO_DEVICE = 7    /* no CUDA device visible */
+} mbgb_status;
+
+/* enumFractalFormula (src/fractal.h:25-64), values that this build evaluates on the device. */
+enum {
+  MBGB_FORMULA_TRIG_DE = 1,
+  MBGB_FORMULA_TRIG_OPTIM = 2,   /* Mandelbulb, src/fractal.cpp:211-225 */
+  MBGB_FORMULA_TGLAD = 8         /* Mandelbox, src/fractal.cpp:409-529 */
+};
+
+/* enumPerspectiveType (src/common_math.h:39-42) */
+enum { MBGB_PERSP_THREE_POINT = 0, MBGB_PERSP_FISH_EYE = 1, MBGB_PERSP_EQUIRECT = 2, MBGB_PERSP_FISH_EYE_CUT = 3 };
+
+typedef struct mbgb_rgb { int32_t R, G, B; } mbgb_rgb;   /* sRGB, src/cimage.hpp:37-42 */
+
+/* One frame's render parameters: the fields of sParamRender that the settings
+ * reader fills (LoadOneSetting, src/settings.cpp:700-1183) plus the values the
+ * -nogui path derives from them. Angles are radians, as stored by the reference. */
+typedef struct mbgb_scene {
+  /* ---- sParamRenderD (src/fractparams.h:18-65) ---- */
+  double zoom, DE_factor, resolution, persp, quality, smoothness;
+  double alpha, beta, gamma;
+  double DOFFocus, DOFRadius;
+  double mainLightAlpha, mainLightBeta;
+  double auxLightIntensity, auxLightMaxDist, auxLightDistributionRadius, auxLightVisibility;
+  double auxLightPreIntensity[4];
+  double stereoEyeDistance;
+  double viewDistanceMin, viewDistanceMax;
+  double volumetricLightIntensity[5];
+  double fogDensity, fogColour1Distance, fogColour2Distance, fogDistanceFactor;
+  double colourSaturation, fastAoTune, iterFogOpacity, iterFogOpacityTrim;
+  double fakeLightsIntensity, fakeLightsVisibility, fakeLightsVisibilitySize;
+  double shadowConeAngle;
+  double primitivePlaneReflect, primitiveBoxReflect, primitiveInvertedBoxReflect;
+  double primitiveSphereReflect, primitiveInvertedSphereReflect, primitiveWaterReflect;
+  /* sImageAdjustments (src/cimage.hpp:43-59) */
+  double shading, directLight, ambient, specular, reflect, globalIlum, brightness;
+  double glow_intensity, fogVisibility, coloring_speed, imageGamma, paletteOffset;
+  double mainLightIntensity, contrast;
+  double vp[3];
+  double auxLightPre[4][3];
+  double auxLightRandomCenter[3];
+
+  /* ---- sFractalD (src/fractal.h:233-253) ---- */
+  double N;                     /* stored as double, truncated to int by Compute (src/fractal.cpp:53) */
+  double amin, amax, bmin, bmax, cmin, cmax;
+  double constantFactor, FoldingIntPowZfactor, FoldingIntPowFoldFactor;
+  double foldingLimit, foldingValue, foldingSphericalMin, foldingSphericalFixed;
+  double power, cadd;
+  double hybridPower[5];
+  double julia[3];
+  double fakeLightsOrbitTrap[3];
+  /* sFractalPrimitivesD (src/fractal.h:195-211) */
+  double planeCentre[3], planeNormal[3], boxCentre[3], boxSize[3];
+  double invertedBoxCentre[3], invertedBoxSize[3], sphereCentre[3];
+  double sphereRadius;
+  double invertedSphereCentre[3];
+  double invertedSphereRadius, waterHeight, waterAmplitude, waterLength, waterRotation, waterAnimSpeed;
+
+  /* ---- sFractalMandelboxD (src/fractal.h:160-180) ---- */
+  double mboxRotationMain[3];        /* radians */
+  double mboxRotation[2][3][3];      /* [fold][axis][component], radians */
+  double mboxColorFactorX, mboxColorFactorY, mboxColorFactorZ, mboxColorFactorR;
+  double mboxColorFactorSp1, mboxColorFactorSp2;
+  double mboxScale, mboxFoldingLimit, mboxFoldingValue;
+  double mboxFoldingSphericalMin, mboxFoldingSphericalFixed;
+  double mboxSharpness, mboxSolid, mboxMelt;
+  double mboxOffset[3];
+  double mboxVaryFold, mboxVaryMinR, mboxVaryScaleVary, mboxVaryWadd, mboxVaryRPower;
+  /* Derived by RecalculateIFSParams (src/callbacks.cpp:1549-1556): row-major 3x3
+   * CRotationMatrix contents and its `zero` (identity short-cut) flag. */
+  double mboxMainRot[9];
+  double mboxRot[2][3][9];
+  double mboxRotInv[2][3][9];
+  int32_t mboxMainRotZero;
+  int32_t mboxRotZero[2][3];
+
+  /* ---- sFractalIFSD (src/fractal.h:104-118), parsed for completeness ---- */
+  double ifsRotationGamma, ifsRotationAlfa, ifsRotationBeta, ifsScale;
+  double ifsDistance[9], ifsAlfa[9], ifsBeta[9], ifsGamma[9], ifsIntensity[9];
+  double ifsOffset[3];
+  double ifsDirection[9][3];
+  double ifsEdge[3];
+
+  /* ---- integers ---- */
+  int32_t image_width, image_height;
+  int32_t globalIlumQuality, reflectionsMax, coloring_seed, auxLightRandomSeed, auxLightNumber;
+  int32_t SSAOQuality, startFrame, endFrame, framesPerKeyframe, imageFormat;
+  int32_t noOfTiles, tileCount;
+  int32_t perspectiveType;
+  int32_t formula, minN, frameNo;
+  int32_t fakeLightsMinIter, fakeLightsMaxIter;
+  int32_t hybridIters[5], hybridFormula[5];
+  int32_t genFoldBoxType, waterIterations;
+
+  /* ---- booleans (0/1) ---- */
+  uint8_t shadow, global_ilumination, fastGlobalIllumination, slowShading;
+  uint8_t texturedBackground, background_as_fulldome, SSAOEnabled, DOFEnabled;
+  uint8_t auxLightPreEnabled[4], volumetricLightEnabled[5];
+  uint8_t penetratingLights, stereoEnabled, fishEyeCut, fakeLightsEnabled;
+  /* sImageSwitches (src/cimage.hpp:69-77) */
+  uint8_t coloringEnabled, fogEnabled, raytracedReflections, volumetricLightEnabledAny;
+  uint8_t iterFogEnabled, hdrEnabled;
+  /* sFractal switches (src/fractal.h:259-272) */
+  uint8_t limits_enabled, iterThresh, analitycDE, juliaMode, tgladFoldingMode;
+  uint8_t sphericalFoldingMode, interiorMode, hybridCyclic, linearDEmode, constantDEThreshold;
+  uint8_t mboxRotationsEnabled;
+  uint8_t ifsFoldingMode, ifsAbsX, ifsAbsY, ifsAbsZ, ifsMengerSpongeMode;
+  uint8_t ifsEnabled[9];
+  /* sFractalPrimitives (src/fractal.h:213-222) */
+  uint8_t planeEnable, boxEnable, invertedBoxEnable, sphereEnable, invertedSphereEnable;
+  uint8_t waterEnable, onlyPlane;
+  uint8_t paletteLoaded;        /* palette came from the file (not generated from coloring_seed) */
+  uint8_t pad_[2];
+
+  /* ---- colours (sRGB, 16-bit range unless noted) ---- */
+  mbgb_rgb background_color1, background_color2, background_color3;
+  mbgb_rgb auxLightPreColour[4];
+  mbgb_rgb fogColour1, fogColour2, fogColour3;
+  mbgb_rgb primitivePlaneColour, primitiveBoxColour, primitiveInvertedBoxColour;
+  mbgb_rgb primitiveSphereColour, primitiveInvertedSphereColour, primitiveWaterColour;
+  mbgb_rgb glow_color1, glow_color2, fogColor, mainLightColour;   /* sEffectColours */
+  mbgb_rgb palette[256];        /* 8-bit range */
+
+  double settingsVersion;
+} mbgb_scene;
+
+/* Output buffers: the cImage layers (src/cimage.hpp:155-162) the render writes.
+ * Any pointer may be NULL (layer not wanted). Pointers are host memory for
+ * mbgb_render_host and device memory for mbgb_render_device. Row-major, x + y * width. */
+typedef struct mbgb_image {
+  int32_t width, height;
+  float *image_float;          /* sRGBfloat, 3 floats per pixel (PutPixelImage) */
+  float *zbuffer;              /* float depth, 1e20 for background (PutPixelZBuffer) */
+  uint16_t *alpha;             /* PutPixelAlpha */
+  uint16_t *opacity;           /* PutPixelOpacity */
+  uint8_t *colour;             /* sRGB8, 3 bytes per pixel (PutPixelColour) */
+  /* debug / parity layers (no reference counterpart) */
+  uint8_t *hit;                /* 1 where the primary ray found the surface */
+  int32_t *iters;              /* orbit iterations of the last DE at the hit (itersOut) */
+  double *depth;               /* primary-ray depth (scan) as double, 1e20 for background */
+} mbgb_image;
+
+/* Precision policies of the device march. */
+enum {
+  MBGB_PREC_FP64 = 0,          /* every DE evaluation and every march in double */
+  MBGB_PREC_FP32_FIX = 1,      /* FP32 march/orbit with FP64 camera origin and FP64 hit refinement */
+  MBGB_PREC_AUTO = 2           /* FP32_FIX unless the pixel footprint is below ~1e-5 of scene scale, then FP64 */
+};
+
+typedef struct mbgb_opts {
+  int32_t precision;           /* MBGB_PREC_* */
+  int32_t jitter;              /* 0: deterministic march (parity mode); 1: per-step counter-hash jitter */
+  uint32_t jitter_seed;
+  int32_t row_begin, row_end;  /* render only rows [row_begin, row_end); 0,0 = all rows */
+  int32_t ctas_per_sm;         /* 0 = autotuned */
+  int32_t threads_per_cta;     /* 0 = autotuned */
+  int32_t deadline_ms;         /* device-side deadline; 0 = none */
+  void *stream;                /* cudaStream_t; NULL = the context's stream */
+} mbgb_opts;
+
+/* Per-render counters (the reference's N_counter, DE_counter, Pixel_counter,
+ * Missed_DE_counter globals, src/Render3D.cpp:51-57), kept per context here. */
+typedef struct mbgb_stats {
+  uint64_t orbit_iterations;   /* N_counter: sum over DE calls of (L + 1) */
+  uint64_t de_calls;           /* Loop_counter: Compute<> calls */
+  uint64_t primary_steps;      /* DE_counter */
+  uint64_t pixels;             /* Pixel_counter */
+  uint64_t missed_de;          /* Missed_DE_counter */
+  double kernel_ms;            /* device time of the last render */
+} mbgb_stats;
+
+typedef struct mbgb_context mbgb_context;
+
+/* ---- version / errors ---- */
+const char *mbgb_version(void);
+/* Thread-local text of the last error raised on this thread. */
+const char *mbgb_last_error(void);
+
+/* ---- settings (host only; no GPU needed) ----
+ * Replaces LoadSettings / LoadSettings2 / LoadOneSetting / LoadSettingsPost
+ * (src/settings.cpp:611-698, 700-1183, 1185-1195) plus the -nogui fix-ups of
+ * ReadInterface (src/interface.cpp:690-729), CheckPrameters (src/interface.cpp:3587)
+ * and RecalculateIFSParams (src/callbacks.cpp:1538-1556).
+ * `defaults_path` may be NULL (then the scene starts zeroed, as the reference's
+ * static noGUIdata does). `overrides` are "key=value" strings like the -o switch
+ * (src/interface.cpp:3512-3519, src/settings.cpp:660-676). */
+mbgb_status mbgb_scene_from_settings(const char *defaults_path, const char *path,
+                                     const char *const *overrides, int n_overrides,
+                                     mbgb_scene *out);
+/* Apply one "key value" pair (LoadOneSetting). Returns MBGB_ERR_BAD_PARAM for an unknown key. */
+mbgb_status mbgb_scene_set(mbgb_scene *scene, const char *key, const char *value);
+/* Re-derive the dependent fields (analytic-DE flag, resolution, matrices, clamps) after edits. */
+mbgb_status mbgb_scene_finalize(mbgb_scene *scene);
+/* Palette of NewPalette (src/image.cpp:28-55) seeded like LoadSettingsPost (src/settings.cpp:1185-1195). */
+void mbgb_palette_from_seed(int32_t seed, double saturation, mbgb_rgb palette[256]);
+/* Report whether the device kernels can render this scene (MBGB_OK) or why not. */
+mbgb_status mbgb_scene_supported(const mbgb_scene *scene);
+
+/* ---- context ---- */
+mbgb_status mbgb_context_create(int device, mbgb_context **out);
+void mbgb_context_destroy(mbgb_context *ctx);
+mbgb_status mbgb_get_stats(const mbgb_context *ctx, mbgb_stats *out);
+
+/* ---- render ----
+ * One frame; the drop-in for Render() (src/Render3D.cpp:709) writing the cImage
+ * layers the way MainThread does (src/Render3D.cpp:569-589). `opts` may be NULL.
+ * mbgb_render_device: `out` holds device pointers; the call is asynchronous on
+ * the stream unless the stream is NULL (then it synchronises).
+ * mbgb_render_host: `out` holds host pointers; copies in and out are part of the call. */
+mbgb_status mbgb_render_device(mbgb_context *ctx, const mbgb_scene *scene,
+                               const mbgb_image *out, const mbgb_opts *opts);
+mbgb_status mbgb_render_host(mbgb_context *ctx, const mbgb_scene *scene,
+                             const mbgb_image *out, const mbgb_opts *opts);
+
+/* Distance estimate at points (CalculateDistance, src/fractal.cpp:1245-1448) with
+ * detailSize = detail[i]; writes dist[i], iters[i] (itersOut) and max_iter[i].
+ * All pointers are device pointers. precision: MBGB_PREC_FP64 or MBGB_PREC_FP32_FIX (float orbit). */
+mbgb_status mbgb_distance_device(mbgb_context *ctx, const mbgb_scene *scene, int precision,
+                                 const double *points, const double *detail, int64_t n,
+                                 double *dist, int32_t *iters, uint8_t *max_iter);
+
+/* ---- image compile (src/cimage.cpp:132-214) ----
+ * Gamma/brightness/contrast/HDR of CalculatePixel + CompileImage into RGB16, host pointers. */
+mbgb_status mbgb_compile_image16(const mbgb_scene *scene, const float *image_float,
+                                 int32_t width, int32_t height, uint16_t *image16);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MBGB_H_ */

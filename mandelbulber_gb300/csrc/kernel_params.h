@@ -1,0 +1,107 @@
+// Host/device parameter blocks of the ray-march kernels.
+//
+// The host derives these once per frame from an mbgb_scene (capi.cpp) the way
+// MainThread prepares its locals (src/Render3D.cpp:213-344): camera rotation,
+// ray start, light vector, the ambient-occlusion direction table. They travel as
+// a by-value kernel parameter, so they live in the constant bank and graph
+// captures carry them. ParamsT<float> is the pre-converted copy for the FP32
+// kernels, so no kernel converts doubles on its hot path.
+#pragma once
+
+#include <cstdint>
+
+namespace mbgb {
+
+constexpr int kMaxMarchSteps = 10000;   // RayMarching loop bound (src/Render3D.cpp:94)
+constexpr int kStepSlots = 10002;       // sStep buffer length per ray (src/Render3D.cpp:267)
+constexpr int kMaxAOVectors = 10000;    // sVectorsAround table (src/Render3D.cpp:272)
+constexpr int kTileW = 8, kTileH = 4;   // one warp renders an 8x4 pixel tile
+
+// Fractal / distance-estimator parameters (sFractal, src/fractal.h:255-293).
+template <typename T>
+struct FractalT {
+  int formula;
+  int N;            // (int)doubles.N
+  int N5;           // (int)(doubles.N * 5): CalculateNormals (src/shaders.cpp:687)
+  int N10;          // (int)(doubles.N * 10): SurfaceColour (src/shaders.cpp:855)
+  int minN;
+  int juliaMode, tgladFoldingMode, sphericalFoldingMode;
+  int limits, iterThresh, interiorMode;
+  int mbRotEnabled, mbMainRotZero;
+  int mbRotZero[2][3];
+  T power, constantFactor;
+  T julia[3];
+  T foldingLimit, foldingValue, sphFixed, sphMin;
+  T mbScale, mbFoldLimit, mbFoldValue, mbMinR, mbFixedR;
+  T mbOffset[3];
+  T mbColX, mbColY, mbColZ, mbColR, mbColSp1, mbColSp2;
+  T mbMainRot[9];
+  T mbRot[2][3][9];
+  T mbRotInv[2][3][9];
+  T amin, amax, bmin, bmax, cmin, cmax;
+};
+
+// Everything MainThread and the shaders read (sParamRender, src/fractparams.h:67-146).
+template <typename T>
+struct ParamsT {
+  FractalT<T> f;
+  // camera (src/Render3D.cpp:237-333, 389-438)
+  int width, height, tiles, perspType, fishEyeCut;
+  int row_begin, row_end;
+  double tileXOffset, tileYOffset, aspect, fov;
+  double rot[9];
+  int rot_zero;
+  double start[3];
+  // march (src/Render3D.cpp:79-199)
+  T viewDistanceMin, viewDistanceMax, resolution, persp, quality, DE_factor, smoothness;
+  double resolution_d, persp_d, quality_d;   // FP64 hit refinement
+  int constantDEThreshold, interiorMode, slowShading;
+  int jitter;
+  uint32_t jitter_seed;
+  // shading (src/shaders.cpp:21-112, 480-926)
+  T lightVect[3];
+  T mainLight[3];
+  T directLight, shading, specular, globalIlum;
+  int shadow, penetrating, softShadow;
+  T softRange;
+  int ao, fastAO, aoQuality, aoCount;
+  T fastAoTune;
+  const T *aoVec;    // aoCount x 3, device memory
+  T aoWeight[3];     // lightmap colour of each direction (white default texture: 255)
+  int coloring;
+  T coloringSpeed, paletteOffset;
+  int palette[256][3];
+  int bg1[3], bg2[3], bg3[3];
+  // volumetric pass (src/shaders.cpp:185-478)
+  int needVolumetric;
+  T glowIntensity;
+  int glow1[3], glow2[3];
+  int postFog;
+  T fogVisibility;   // pow(10, post_fog_visibility / 10 - 16), computed on the host
+  int fogColor[3];
+  T fogDensity, fogC1Dist, fogC2Dist, fogDistFactor;
+  int fogCol1[3], fogCol2[3], fogCol3[3];
+};
+
+// Output and scratch pointers of one launch (device memory).
+struct FrameIO {
+  float *image_float;
+  float *zbuffer;
+  uint16_t *alpha;
+  uint16_t *opacity;
+  uint8_t *colour;
+  uint8_t *hit;
+  int32_t *iters;
+  double *depth;
+  // Scratch: per resident thread, the primary ray's step records (sStep,
+  // src/Render3D.h:32-39): step, distance and threshold, each [kStepSlots][slots].
+  void *step_step, *step_dist, *step_thr;
+  int64_t slots;
+  unsigned int *tile_counter;     // zeroed before the launch
+  unsigned long long *counters;   // [0] orbit iterations, [1] DE calls, [2] primary steps, [3] missed DE
+  int *error_flag;                // set to 1 when the device deadline expires
+  unsigned long long *start_ns;   // %globaltimer at the first tile claim (zeroed before the launch)
+  unsigned long long budget_ns;   // device-side time budget, 0 = none
+};
+
+}  // namespace mbgb

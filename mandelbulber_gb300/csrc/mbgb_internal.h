@@ -1,0 +1,30 @@
+// Internal declarations shared by the host-side translation units of libmbgb.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include "mbgb.h"
+
+namespace mbgb {
+
+// Records `msg` as this thread's last error and returns `st` (see mbgb_last_error).
+mbgb_status set_error(mbgb_status st, const std::string &msg);
+
+// The C library's srand()/rand() sequence (glibc additive feedback generator),
+// restated so palettes generated from coloring_random_seed are identical on every host.
+class GlibcRand {
+ public:
+  explicit GlibcRand(uint32_t seed);
+  int rand();
+  int random(int max);
+
+ private:
+  uint32_t next_raw();
+  uint32_t ring_[34];
+  uint64_t idx_;
+};
+
+bool scene_set(mbgb_scene *sc, const char *key, const char *value, bool *palette_loaded);
+
+}  // namespace mbgb

@@ -1,0 +1,879 @@
+// Device side of the per-pixel distance-estimated ray march.
+//
+// One template body serves both precision policies:
+//   * T = double, compiled with --fmad=false: every DE, march and shader runs in
+//     IEEE double with the reference's operation order, so the formulas built from
+//     + - * / sqrt (Mandelbox) reproduce the CPU results bit for bit.
+//   * T = float: the march, the orbit iteration and the shaders run in FP32 with
+//     FMA; the camera ray is formed in FP64 and the final binary hit refinement
+//     runs in FP64 (FractalT<double>).
+// The reference functions each part follows are cited at the function.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernel_params.h"
+
+namespace mbgb {
+namespace dev {
+
+// ---------------------------------------------------------------------------
+// small vector type and precision-overloaded math
+// ---------------------------------------------------------------------------
+template <typename T>
+struct V3 {
+  T x, y, z;
+};
+template <typename T>
+__device__ __forceinline__ V3<T> operator+(const V3<T> a, const V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator-(const V3<T> a, const V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator*(const V3<T> a, const T s) { return {a.x * s, a.y * s, a.z * s}; }
+// CVector3::Dot / Length (src/algebra.hpp:89-96): ((x*x + y*y) + z*z)
+template <typename T>
+__device__ __forceinline__ T dot3(const V3<T> a, const V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_fabs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_fabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double m_asin(double x) { return asin(x); }
+__device__ __forceinline__ float m_asin(float x) { return asinf(x); }
+__device__ __forceinline__ double m_atan2(double y, double x) { return atan2(y, x); }
+__device__ __forceinline__ float m_atan2(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double m_pow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float m_pow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double m_log(double x) { return log(x); }
+__device__ __forceinline__ float m_log(float x) { return logf(x); }
+__device__ __forceinline__ double m_floor(double x) { return floor(x); }
+__device__ __forceinline__ float m_floor(float x) { return floorf(x); }
+__device__ __forceinline__ void m_sincos(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ void m_sincos(float x, float *s, float *c) { sincosf(x, s, c); }
+
+template <typename T>
+__device__ __forceinline__ T length3(const V3<T> a) { return m_sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+// CVector3::Normalize (src/algebra.hpp:105-112): multiply by 1/length.
+template <typename T>
+__device__ __forceinline__ V3<T> normalize3(const V3<T> a) {
+  const T norm = T(1) / length3(a);
+  return {a.x * norm, a.y * norm, a.z * norm};
+}
+
+// Conversions with the results the reference gets from x86-64 code
+// (cvttsd2si to a 32-bit register, out-of-range -> INT_MIN, then truncation of
+// the register to the narrower type).
+__device__ __forceinline__ int to_i32_x86(double v) {
+  return (v >= -2147483648.0 && v < 2147483648.0) ? (int)v : (int)0x80000000;
+}
+__device__ __forceinline__ unsigned short to_u16_x86(double v) { return (unsigned short)to_i32_x86(v); }
+__device__ __forceinline__ unsigned char to_u8_x86(double v) { return (unsigned char)to_i32_x86(v); }
+
+// CRotationMatrix::RotateVector with its identity short-cut (src/algebra.cpp:163-174).
+template <typename T>
+__device__ __forceinline__ V3<T> rotate(const T *m, int zero, const V3<T> v) {
+  if (zero) return v;
+  return {m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+          m[6] * v.x + m[7] * v.y + m[8] * v.z};
+}
+
+// Device-side deadline: true once the launch has run longer than io.budget_ns.
+// The first caller stamps the launch start; every wait loop here is bounded, the
+// deadline only shortens a frame that would take too long.
+__device__ __forceinline__ bool deadline_passed(const FrameIO &io) {
+  if (!io.budget_ns) return false;
+  unsigned long long now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  unsigned long long st = atomicCAS(io.start_ns, 0ull, now);
+  if (st == 0ull) st = now;
+  return now - st > io.budget_ns;
+}
+
+struct Counters {
+  unsigned long long orbit;   // N_counter: sum of (L + 1)
+  unsigned long long calls;   // Loop_counter
+  unsigned long long steps;   // DE_counter (primary march + refinement)
+  unsigned long long missed;  // Missed_DE_counter
+};
+
+// ---------------------------------------------------------------------------
+// Compute<Mode> (src/fractal.cpp:40-1241) for the formulas this build carries.
+// MODE 0 = normal (returns the distance estimate), MODE 1 = colouring.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA, int MODE>
+__device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N, int &Lout, Counters &cnt) {
+  T distance = T(0);
+  T r_dz = T(1);
+  const T p = f.power;
+  const T fR2 = f.mbFixedR * f.mbFixedR;
+  const T mR2 = f.mbMinR * f.mbMinR;
+  const T tglad_factor1 = fR2 / mR2;
+  T tgladDE = T(1);
+  T tgladColor = T(1);
+  const T scale = f.mbScale;
+  V3<T> constant;
+  if (f.juliaMode) {
+    constant = {f.julia[0], f.julia[1], f.julia[2]};
+  } else {
+    constant = z * f.constantFactor;
+  }
+  T r = length3(z);
+  T minv = (sizeof(T) == 8) ? T(1e200) : T(__int_as_float(0x7f800000));
+  int L;
+  for (L = 0; L < N; L++) {
+    if (f.tgladFoldingMode) {  // src/fractal.cpp:124-156
+      if (z.x > f.foldingLimit) { z.x = f.foldingValue - z.x; tgladColor *= T(0.9); }
+      else if (z.x < -f.foldingLimit) { z.x = -f.foldingValue - z.x; tgladColor *= T(0.9); }
+      if (z.y > f.foldingLimit) { z.y = f.foldingValue - z.y; tgladColor *= T(0.9); }
+      else if (z.y < -f.foldingLimit) { z.y = -f.foldingValue - z.y; tgladColor *= T(0.9); }
+      if (z.z > f.foldingLimit) { z.z = f.foldingValue - z.z; tgladColor *= T(0.9); }
+      else if (z.z < -f.foldingLimit) { z.z = -f.foldingValue - z.z; tgladColor *= T(0.9); }
+      r = length3(z);
+    }
+    if (f.sphericalFoldingMode) {  // src/fractal.cpp:158-179
+      const T fR2_2 = f.sphFixed * f.sphFixed;
+      const T mR2_2 = f.sphMin * f.sphMin;
+      const T r2_2 = r * r;
+      const T tf1 = fR2_2 / mR2_2;
+      if (r2_2 < mR2_2) {
+        z = z * tf1; tgladDE *= tf1; tgladColor += T(1);
+      } else if (r2_2 < fR2_2) {
+        const T tf2 = fR2_2 / r2_2;
+        z = z * tf2; tgladDE *= tf2; tgladColor += T(10);
+      }
+      r = length3(z);
+    }
+    if (FORMULA == 2) {
+      // trig_optim Mandelbulb (src/fractal.cpp:211-225)
+      const T th0 = m_asin(z.z / r);
+      const T ph0 = m_atan2(z.y, z.x);
+      T rp = m_pow(r, p - T(1));
+      const T th = th0 * p;
+      const T ph = ph0 * p;
+      T sth, cth, sph, cph;
+      m_sincos(th, &sth, &cth);
+      m_sincos(ph, &sph, &cph);
+      r_dz = rp * r_dz * p + T(1);
+      rp *= r;
+      z = V3<T>{cth * cph, cth * sph, sth} * rp + constant;
+      r = length3(z);
+    } else if (FORMULA == 8) {
+      // tglad Mandelbox (src/fractal.cpp:409-529)
+      if (f.mbRotEnabled) {
+        bool lockout = false;
+        z = rotate(f.mbRot[0][0], f.mbRotZero[0][0], z);
+        if (z.x > f.mbFoldLimit) { z.x = f.mbFoldValue - z.x; tgladColor += f.mbColX; lockout = true; }
+        z = rotate(f.mbRotInv[0][0], 0, z);
+        z = rotate(f.mbRot[1][0], f.mbRotZero[1][0], z);
+        if (!lockout && z.x < -f.mbFoldLimit) { z.x = -f.mbFoldValue - z.x; tgladColor += f.mbColX; }
+        z = rotate(f.mbRotInv[1][0], 0, z);
+        lockout = false;
+        z = rotate(f.mbRot[0][1], f.mbRotZero[0][1], z);
+        if (z.y > f.mbFoldLimit) { z.y = f.mbFoldValue - z.y; tgladColor += f.mbColY; lockout = true; }
+        z = rotate(f.mbRotInv[0][1], 0, z);
+        z = rotate(f.mbRot[1][1], f.mbRotZero[1][1], z);
+        if (!lockout && z.y < -f.mbFoldLimit) { z.y = -f.mbFoldValue - z.y; tgladColor += f.mbColY; }
+        z = rotate(f.mbRotInv[1][1], 0, z);
+        lockout = false;
+        z = rotate(f.mbRot[0][2], f.mbRotZero[0][2], z);
+        if (z.z > f.mbFoldLimit) { z.z = f.mbFoldValue - z.z; tgladColor += f.mbColZ; lockout = true; }
+        z = rotate(f.mbRotInv[0][2], 0, z);
+        z = rotate(f.mbRot[1][2], f.mbRotZero[1][2], z);
+        if (!lockout && z.z < -f.mbFoldLimit) { z.z = -f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
+        z = rotate(f.mbRotInv[1][2], 0, z);
+      } else {
+        if (z.x > f.mbFoldLimit) { z.x = f.mbFoldValue - z.x; tgladColor += f.mbColX; }
+        else if (z.x < -f.mbFoldLimit) { z.x = -f.mbFoldValue - z.x; tgladColor += f.mbColX; }
+        if (z.y > f.mbFoldLimit) { z.y = f.mbFoldValue - z.y; tgladColor += f.mbColY; }
+        else if (z.y < -f.mbFoldLimit) { z.y = -f.mbFoldValue - z.y; tgladColor += f.mbColY; }
+        if (z.z > f.mbFoldLimit) { z.z = f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
+        else if (z.z < -f.mbFoldLimit) { z.z = -f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
+      }
+      r = length3(z);
+      const T r2 = r * r;
+      z = z + V3<T>{f.mbOffset[0], f.mbOffset[1], f.mbOffset[2]};
+      if (r2 < mR2) {
+        z = z * tglad_factor1; tgladDE *= tglad_factor1; tgladColor += f.mbColSp1;
+      } else if (r2 < fR2) {
+        const T tglad_factor2 = fR2 / r2;
+        z = z * tglad_factor2; tgladDE *= tglad_factor2; tgladColor += f.mbColSp2;
+      }
+      z = z - V3<T>{f.mbOffset[0], f.mbOffset[1], f.mbOffset[2]};
+      z = rotate(f.mbMainRot, f.mbMainRotZero, z);
+      z = z * scale + constant;
+      tgladDE = tgladDE * m_fabs(scale) + T(1);
+      r = length3(z);
+    }
+    // iteration terminate conditions (src/fractal.cpp:1133-1190)
+    if (FORMULA == 8) {
+      if (r > T(1024)) { distance = r / m_fabs(tgladDE); break; }
+    } else {
+      if (MODE == 0) {
+        if (r > T(100)) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
+      } else {
+        distance = length3(z);
+        if (distance < minv) minv = distance;
+        if (distance > T(1e15)) { distance = minv; break; }
+      }
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (MODE == 0) {
+    if (L == N) distance = T(0);
+    return distance;
+  } else {
+    if (FORMULA == 8) return tgladColor * T(100) + length3(z) * f.mbColR;
+    return distance * T(5000);
+  }
+}
+
+// CalculateDistance, analytic branch (src/fractal.cpp:1245-1300, 1436-1445).
+// `L` (itersOut) is left untouched when the limits box returns early, as in the reference.
+template <typename T, int FORMULA>
+__device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> point, const T detailSize, const int N,
+                                           const int minN, const bool normalMode, int &L, bool &maxIter,
+                                           Counters &cnt) {
+  T limitBoxDist = T(0);
+  if (f.limits) {
+    // MAX(a, b) = a > b ? a : b (gtk MAX macro)
+    const T ax = point.x - f.amax, bx = -(point.x - f.amin);
+    const T ay = point.y - f.bmax, by = -(point.y - f.bmin);
+    const T az = point.z - f.cmax, bz = -(point.z - f.cmin);
+    const T da = ax > bx ? ax : bx;
+    const T db = ay > by ? ay : by;
+    const T dc = az > bz ? az : bz;
+    // dMax (src/common_math.cpp:34-43)
+    limitBoxDist = (da > db) ? ((da > dc) ? da : dc) : ((db > dc) ? db : dc);
+    if (limitBoxDist > detailSize) {
+      maxIter = false;
+      return limitBoxDist;
+    }
+  }
+  int Li;
+  T distance = compute<T, FORMULA, 0>(f, point, N, Li, cnt);
+  maxIter = (Li == N);
+  L = Li;
+  if (distance < T(0)) distance = T(0);
+  if (Li < minN && distance < detailSize) distance = detailSize;
+  if (f.interiorMode && !normalMode) {
+    if (distance < T(0.5) * detailSize || Li == N) { distance = detailSize; maxIter = false; }
+  } else if (f.interiorMode && normalMode) {
+    if (distance < T(0.9) * detailSize) { distance = detailSize - distance; maxIter = false; }
+  }
+  if (f.iterThresh && Li < N) {
+    if (distance < detailSize) distance = detailSize * T(1.01);
+  }
+  if (f.limits) {
+    if (limitBoxDist < detailSize) distance = (distance > limitBoxDist) ? distance : limitBoxDist;
+  }
+  return distance;
+}
+
+// Counter-hash stand-in for the march jitter Random(1000) (src/Render3D.cpp:129-133):
+// a value in [0, 1000] from (seed, pixel, step) instead of a shared rand() stream.
+__device__ __forceinline__ int jitter1000(uint32_t seed, uint32_t pixel, uint32_t step) {
+  uint32_t h = seed ^ (pixel * 0x9E3779B1u) ^ (step * 0x85EBCA77u);
+  h ^= h >> 16; h *= 0x7FEB352Du; h ^= h >> 15; h *= 0x846CA68Bu; h ^= h >> 16;
+  return (int)(h % 1001u);
+}
+
+// Step-buffer view of one thread's scratch slot: record i at [i * slots + slot].
+template <typename T>
+struct StepBuf {
+  T *step, *dist, *thr;
+  int64_t slots, slot;
+  __device__ __forceinline__ int64_t at(int i) const { return (int64_t)i * slots + slot; }
+};
+
+// Per-pixel march state handed from the march to the shaders.
+struct RayState {
+  bool found;
+  int buffCount;
+  int iters;
+  double scan, step, dist, distThresh, detail;
+  double point[3];
+};
+
+constexpr double kPI = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// RayMarching march loop (src/Render3D.cpp:79-143) in precision T.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA>
+__device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, const V3<T> dir, const uint32_t pixel,
+                                      const StepBuf<T> &sb, RayState &rs, Counters &cnt) {
+  T scan = p.viewDistanceMin;
+  T distThresh = T(0);  // *distThreshOut is 0.0 for the primary ray (src/Render3D.cpp:443)
+  const T distThreshInit = T(0);
+  T dist = T(0);
+  T step = p.viewDistanceMin;
+  int buffCount = 0;
+  bool found = false;
+  int iters = 0;
+  int counter = 0;
+  const bool useSB = p.needVolumetric;
+  const T thrScale = p.resolution * p.persp / p.quality;
+  const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
+  for (int i = 0; i < kMaxMarchSteps; i++) {
+    counter++;
+    const V3<T> point = start + dir * scan;
+    if (p.constantDEThreshold) {
+      distThresh = p.quality;
+    } else if (sizeof(T) == 8) {
+      distThresh = scan * p.resolution * p.persp / p.quality + distThreshInit;
+    } else {
+      distThresh = scan * thrScale + distThreshInit;
+    }
+    if (p.perspType == 1 || p.perspType == 2) distThresh *= T(kPI);
+    bool mi;
+    dist = calc_distance<T, FORMULA>(p.f, point, distThresh, p.f.N, p.f.minN, false, iters, mi, cnt);
+    if (useSB) {
+      sb.dist[sb.at(i)] = dist;
+      sb.thr[sb.at(i)] = distThresh;
+    }
+    if (dist > T(3)) dist = T(3);
+    if (dist < distThresh) {
+      if (dist < T(0.1) * distThresh) cnt.missed++;
+      found = true;
+      break;
+    }
+    if (useSB) sb.step[sb.at(i)] = step;
+    step = (dist - stepFrac * distThresh) * p.DE_factor;
+    if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, pixel, (uint32_t)i)) / T(10000));
+    buffCount++;
+    scan += step;
+    if (scan > p.viewDistanceMax) break;
+  }
+  cnt.steps += (unsigned long long)counter;
+  rs.found = found;
+  rs.buffCount = buffCount;
+  rs.iters = iters;
+  rs.scan = (double)scan;
+  rs.step = (double)step;
+  rs.dist = (double)dist;
+  rs.distThresh = (double)distThresh;
+  rs.detail = (double)distThresh;
+  const V3<T> pt = start + dir * scan;
+  rs.point[0] = (double)pt.x;
+  rs.point[1] = (double)pt.y;
+  rs.point[2] = (double)pt.z;
+}
+
+// Binary hit refinement (src/Render3D.cpp:145-183), always in FP64.
+// detailSize keeps the value of the last march step, as in the reference.
+template <typename TP, int FORMULA>
+__device__ __forceinline__ void refine(const ParamsT<TP> &p, const FractalT<double> &fd, const V3<double> start,
+                                       const V3<double> dir, RayState &rs, Counters &cnt) {
+  const double search_accuracy = 0.01 * p.quality_d;
+  const double search_limit = 1.0 - search_accuracy;
+  double scan = rs.scan;
+  double step = rs.step * 0.5;
+  double dist = rs.dist;
+  double distThresh = rs.distThresh;
+  const double distThreshInit = 0.0;
+  V3<double> point{rs.point[0], rs.point[1], rs.point[2]};
+  int iters = rs.iters;
+  for (int i = 0; i < 20; i++) {
+    cnt.steps++;
+    if (dist < distThresh && dist > distThresh * search_limit) {
+      break;
+    } else {
+      if (dist > distThresh) {
+        scan += step;
+        point = start + dir * scan;
+      } else if (dist < distThresh * search_limit) {
+        scan -= step;
+        point = start + dir * scan;
+      }
+    }
+    if (p.constantDEThreshold) {
+      distThresh = p.quality_d;
+    } else {
+      distThresh = scan * p.resolution_d * p.persp_d / p.quality_d + distThreshInit;
+    }
+    bool mi;
+    dist = calc_distance<double, FORMULA>(fd, point, rs.detail, fd.N, fd.minN, false, iters, mi, cnt);
+    step *= 0.5;
+  }
+  rs.scan = scan;
+  rs.dist = dist;
+  rs.distThresh = distThresh;
+  rs.iters = iters;
+  rs.point[0] = point.x;
+  rs.point[1] = point.y;
+  rs.point[2] = point.z;
+}
+
+// ---------------------------------------------------------------------------
+// Shaders in precision T (src/shaders.cpp)
+// ---------------------------------------------------------------------------
+
+// CalculateNormals, fast branch (src/shaders.cpp:675-711, 745-757)
+template <typename T, int FORMULA>
+__device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> point, const T delta, const T dist_thresh,
+                                             const T detail, Counters &cnt) {
+  T dn = delta * p.smoothness;
+  if (p.f.interiorMode) dn = dist_thresh * p.quality * T(0.2) * p.smoothness;
+  int L;
+  bool mi;
+  const int N5 = p.f.N5;
+  const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt);
+  const T s2 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
+                                         true, L, mi, cnt);
+  const T s3 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
+                                         true, L, mi, cnt);
+  const T s4 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
+                                         true, L, mi, cnt);
+  V3<T> n{s2 - s1, s3 - s1, s4 - s1};
+  if (n.x == T(0) && n.y == T(0) && n.z == T(0)) {
+    n.x = T(1);
+  } else {
+    n = normalize3(n);
+  }
+  return n;
+}
+
+// MainShadow (src/shaders.cpp:480-570), without iteration fog / volumetric lights.
+// `detail` is the shared detailSize state; the reference leaves it at the float-rounded threshold.
+template <typename T, int FORMULA>
+__device__ __forceinline__ T main_shadow(const ParamsT<T> &p, const V3<T> point, const T dist_thresh, const T delta,
+                                         T &detail, const FrameIO &io, Counters &cnt) {
+  T factor = delta / p.resolution;
+  if (!p.penetrating) factor = p.viewDistanceMax;
+  T dist = dist_thresh;
+  detail = dist_thresh;
+  const T DE_factor = p.DE_factor;
+  T start = dist_thresh;
+  if (p.f.interiorMode) start = dist_thresh * DE_factor;
+  T shadowTemp = T(1);
+  const T softRange = p.softRange;
+  T maxSoft = T(0);
+  const bool bSoft = p.softShadow != 0;
+  const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
+  // the reference stores the threshold in a float (src/shaders.cpp:515)
+  const float thr_f = (float)dist_thresh;
+  const T thr = (T)thr_f;
+  int guard = 0;
+  for (T i = start; i < factor; i += dist * DE_factor) {
+    const V3<T> point2 = point + lv * i;
+    detail = thr;
+    int L;
+    bool mi;
+    dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+    if (bSoft) {
+      T angle = (dist - thr) / i;
+      if (angle < T(0)) angle = T(0);
+      if (dist < thr) angle = T(0);
+      T softShadow = (T(1) - angle / softRange);
+      if (p.penetrating) softShadow *= (factor - i) / factor;
+      if (softShadow < T(0)) softShadow = T(0);
+      if (softShadow > maxSoft) maxSoft = softShadow;
+    }
+    if (dist < thr || shadowTemp < T(0)) {
+      shadowTemp -= (factor - i) / factor;
+      if (!p.penetrating) shadowTemp = T(0);
+      if (shadowTemp < T(0)) shadowTemp = T(0);
+      break;
+    }
+    if ((++guard & 1023) == 0 && deadline_passed(io)) {
+      atomicExch(io.error_flag, 1);
+      break;
+    }
+  }
+  return bSoft ? (T(1) - maxSoft) : shadowTemp;
+}
+
+// FastAmbientOcclusion2 (src/shaders.cpp:585-605)
+template <typename T, int FORMULA>
+__device__ __forceinline__ T fast_ao(const ParamsT<T> &p, const V3<T> point, const V3<T> normal, const T dist_thresh,
+                                     const T detail, Counters &cnt) {
+  const T delta = dist_thresh;
+  T aoTemp = T(0);
+  const int q2 = p.aoQuality * p.aoQuality;
+  for (int i = 1; i < q2; i++) {
+    const T scan = T(i * i) * delta;
+    const V3<T> pt = point + normal * scan;
+    int L;
+    bool mi;
+    const T dist = calc_distance<T, FORMULA>(p.f, pt, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+    // 1.0 / pow(2.0, i) is exact for integral i
+    aoTemp += T(1) / T(ldexp(1.0, i)) * (scan - p.fastAoTune * dist) / dist_thresh;
+  }
+  T ao = T(1) - T(0.2) * aoTemp;
+  if (ao < T(0)) ao = T(0);
+  return ao;
+}
+
+// AmbientOcclusion, ray-traced (src/shaders.cpp:607-673), white light map:
+// every direction weighs (255, 255, 255).
+template <typename T, int FORMULA>
+__device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, const T delta, const T dist_thresh,
+                                        const T lastDist, const T detail, Counters &cnt) {
+  const T start_dist = delta;
+  const T end_dist = delta / p.resolution;
+  const float thr_f = (float)dist_thresh;
+  const T thr = (T)thr_f;
+  V3<T> AO{T(0), T(0), T(0)};
+  for (int v = 0; v < p.aoCount; v++) {
+    const V3<T> dir{__ldg(&p.aoVec[3 * v + 0]), __ldg(&p.aoVec[3 * v + 1]), __ldg(&p.aoVec[3 * v + 2])};
+    T dist = lastDist;
+    T shadowTemp = T(1);
+    for (T r = start_dist; r < end_dist; r += dist * T(2)) {
+      const V3<T> point2 = point + dir * r;
+      int L;
+      bool mi;
+      dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+      if (dist < thr || mi || shadowTemp < T(0)) {
+        shadowTemp -= (end_dist - r) / end_dist;
+        if (shadowTemp < T(0)) shadowTemp = T(0);
+        break;
+      }
+    }
+    AO.x += shadowTemp * p.aoWeight[0];
+    AO.y += shadowTemp * p.aoWeight[1];
+    AO.z += shadowTemp * p.aoWeight[2];
+  }
+  const T div = T(p.aoCount) * T(256);
+  AO.x /= div;
+  AO.y /= div;
+  AO.z /= div;
+  return AO;
+}
+
+// IndexToColour (src/shaders.cpp:1273-1305) -> sRGB in 8-bit range
+template <typename T>
+__device__ __forceinline__ void index_to_colour(const ParamsT<T> &p, int index, int rgb[3]) {
+  if (index < 0) {
+    rgb[0] = p.palette[255][0]; rgb[1] = p.palette[255][1]; rgb[2] = p.palette[255][2];
+    return;
+  }
+  index = index % (255 * 256);
+  const int kol = index / 256;
+  rgb[0] = rgb[1] = rgb[2] = 255;
+  if (kol < 255) {
+    const int delta = index % 256;
+    for (int c = 0; c < 3; c++) {
+      const double c1 = p.palette[kol][c];
+      const double c2 = p.palette[kol + 1][c];
+      const double k = (c2 - c1) / 256.0;
+      rgb[c] = (int)(c1 + (k * delta));
+    }
+  }
+}
+
+// SurfaceColour for the fractal object (src/shaders.cpp:850-879)
+template <typename T, int FORMULA>
+__device__ __forceinline__ V3<T> surface_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt) {
+  int L;
+  const T c = compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt);
+  int nrCol = to_i32_x86((double)m_floor(c));
+  // abs(nrCol) % (248 * 256) with the magnitude taken as unsigned, as the reference
+  // binary computes it: an out-of-range conversion (INT_MIN) gives 2^31 % 63488 = 2048.
+  const unsigned mag = nrCol < 0 ? 0u - (unsigned)nrCol : (unsigned)nrCol;
+  nrCol = (int)(mag % (248u * 256u));
+  int rgb[3] = {256, 256, 256};
+  if (p.coloring) {
+    int color_number;
+    if (nrCol >= 248 * 256) {
+      color_number = nrCol;
+    } else {
+      color_number = to_i32_x86((double)((T)nrCol * p.coloringSpeed + T(256) * p.paletteOffset)) % 65536;
+    }
+    index_to_colour(p, color_number, rgb);
+  }
+  return V3<T>{T(rgb[0]) / T(256), T(rgb[1]) / T(256), T(rgb[2]) / T(256)};
+}
+
+// BackgroundShader, gradient branch (src/shaders.cpp:154-182)
+template <typename T>
+__device__ __forceinline__ V3<T> background(const ParamsT<T> &p, const V3<T> view) {
+  const V3<T> vec{T(0), T(0), T(-1)};
+  T grad = (dot3(view, vec) + T(1));
+  int px[3];
+  if (grad < T(1)) {
+    const T Ngrad = T(1) - grad;
+    for (int c = 0; c < 3; c++) px[c] = to_u16_x86((double)(T(p.bg3[c]) * Ngrad + T(p.bg2[c]) * grad));
+  } else {
+    grad = grad - T(1);
+    const T Ngrad = T(1) - grad;
+    for (int c = 0; c < 3; c++) px[c] = to_u16_x86((double)(T(p.bg2[c]) * Ngrad + T(p.bg1[c]) * grad));
+  }
+  return V3<T>{T(px[0]) / T(65536), T(px[1]) / T(65536), T(px[2]) / T(65536)};
+}
+
+// VolumetricShader (src/shaders.cpp:185-478): glow, post fog and volumetric fog over
+// the primary step buffer, far to near, merging steps shorter than distThresh * quality.
+template <typename T>
+__device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
+                                           const T depth, T out[4], float &totalOpacityOut, bool &opacitySet) {
+  float totalOpacity = 0.0f;
+  const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
+  T glowN = T(1) - glow;
+  if (glowN < T(0)) glowN = T(0);
+  const T glowR = (T(p.glow1[0]) * glowN + T(p.glow2[0]) * glow) / T(65536);
+  const T glowG = (T(p.glow1[1]) * glowN + T(p.glow2[1]) * glow) / T(65536);
+  const T glowB = (T(p.glow1[2]) * glowN + T(p.glow2[2]) * glow) / T(65536);
+  const T colourThresh = p.fogC1Dist;
+  const T colourThresh2 = p.fogC2Dist;
+  const T fogReduce = p.fogDistFactor;
+  const T fogIntensity = p.fogDensity;
+  T totalStep = T(0);
+  for (int index = stepCount - 1; index > 0; index--) {
+    T step = sb.step[sb.at(index)];
+    const T distance = sb.dist[sb.at(index)];
+    const T dist_thresh = sb.thr[sb.at(index)];
+    totalStep += step;
+    if (totalStep < dist_thresh * p.quality) continue;
+    step = totalStep;
+    totalStep = T(0);
+    // glow
+    const T glowOpacity = glow * step / depth;
+    out[0] = glowOpacity * glowR + (T(1) - glowOpacity) * out[0];
+    out[1] = glowOpacity * glowG + (T(1) - glowOpacity) * out[1];
+    out[2] = glowOpacity * glowB + (T(1) - glowOpacity) * out[2];
+    out[3] += glowOpacity;
+    // basic fog
+    if (p.postFog) {
+      T fogDensity = step / p.fogVisibility;
+      if (fogDensity > T(1)) fogDensity = T(1);
+      out[0] = fogDensity * T(p.fogColor[0]) / T(65536) + (T(1) - fogDensity) * out[0];
+      out[1] = fogDensity * T(p.fogColor[1]) / T(65536) + (T(1) - fogDensity) * out[1];
+      out[2] = fogDensity * T(p.fogColor[2]) / T(65536) + (T(1) - fogDensity) * out[2];
+      totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
+      out[3] = fogDensity + (T(1) - fogDensity) * out[3];
+    }
+    // volumetric fog
+    if (fogIntensity > T(0)) {
+      const T densityTemp = (step * fogReduce) / (distance * distance + fogReduce * fogReduce);
+      T k = distance / colourThresh;
+      if (k > T(1)) k = T(1);
+      T kn = T(1) - k;
+      T fr = (T(p.fogCol1[0]) * kn + T(p.fogCol2[0]) * k);
+      T fg = (T(p.fogCol1[1]) * kn + T(p.fogCol2[1]) * k);
+      T fb = (T(p.fogCol1[2]) * kn + T(p.fogCol2[2]) * k);
+      T k2 = distance / colourThresh2 * k;
+      if (k2 > T(1)) k2 = T(1);
+      kn = T(1) - k2;
+      fr = (fr * kn + T(p.fogCol3[0]) * k2);
+      fg = (fg * kn + T(p.fogCol3[1]) * k2);
+      fb = (fb * kn + T(p.fogCol3[2]) * k2);
+      T fogDensity = T(0.3) * fogIntensity * densityTemp / (T(1) + fogIntensity * densityTemp);
+      if (fogDensity > T(1)) fogDensity = T(1);
+      out[0] = fogDensity * fr / T(65536) + (T(1) - fogDensity) * out[0];
+      out[1] = fogDensity * fg / T(65536) + (T(1) - fogDensity) * out[1];
+      out[2] = fogDensity * fb / T(65536) + (T(1) - fogDensity) * out[2];
+      totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
+      out[3] = fogDensity + (T(1) - fogDensity) * out[3];
+    }
+    if (totalOpacity > 1.0f) totalOpacity = 1.0f;
+    if (out[3] > T(1)) out[3] = T(1);
+    totalOpacityOut = totalOpacity;
+    opacitySet = true;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One pixel: MainThread pixel body (src/Render3D.cpp:389-589), reflections off.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA>
+__device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT<double> &fd, const FrameIO &io,
+                                             const int x, const int y, const StepBuf<T> &sb, Counters &cnt) {
+  const int64_t pix = (int64_t)y * p.width + x;
+  // view vector (src/Render3D.cpp:389-438)
+  const double x2 = ((double)x / p.width / p.tiles - 0.5 + p.tileXOffset / p.tiles) * p.aspect;
+  const double z2 = ((double)y / p.height / p.tiles - 0.5 + p.tileYOffset / p.tiles);
+  bool hemisphereCut = false;
+  V3<double> vv;
+  if (p.perspType == 1) {
+    if (p.fishEyeCut && sqrt(x2 * x2 + z2 * z2) > 0.5 / p.fov) hemisphereCut = true;
+    const double x3 = x2 * kPI;
+    const double z3 = z2 * kPI;
+    const double r = sqrt(x3 * x3 + z3 * z3);
+    if (r == 0) {
+      vv = {0.0, 1.0, 0.0};
+    } else {
+      vv.x = x3 / r * sin(r * p.fov);
+      vv.z = z3 / r * sin(r * p.fov);
+      vv.y = cos(r * p.fov);
+    }
+    vv = normalize3(vv);
+  } else if (p.perspType == 2) {
+    const double x3 = x2 * kPI;
+    const double z3 = z2 * kPI;
+    vv.x = sin(p.fov * x3) * cos(p.fov * z3);
+    vv.z = sin(p.fov * z3);
+    vv.y = cos(p.fov * x3) * cos(p.fov * z3);
+    vv = normalize3(vv);
+  } else {
+    vv = {x2 * p.fov, 1.0, z2 * p.fov};
+  }
+  const V3<double> view = rotate(p.rot, p.rot_zero, vv);
+  const V3<double> startD{p.start[0], p.start[1], p.start[2]};
+  const V3<T> viewT{(T)view.x, (T)view.y, (T)view.z};
+  const V3<T> startT{(T)startD.x, (T)startD.y, (T)startD.z};
+
+  RayState rs;
+  rs.found = false;
+  rs.buffCount = 0;
+  rs.iters = 0;
+  rs.distThresh = 0.0;
+  rs.dist = 0.0;
+  rs.scan = 0.0;
+  rs.point[0] = rs.point[1] = rs.point[2] = 0.0;
+  if (!hemisphereCut) {
+    march<T, FORMULA>(p, startT, viewT, (uint32_t)pix, sb, rs, cnt);
+    if (rs.found) refine<T, FORMULA>(p, fd, startD, view, rs, cnt);
+  }
+
+  T result[4] = {T(0), T(0), T(0), T(0)};
+  V3<T> objColour{T(0), T(0), T(0)};
+  double depth = rs.scan;
+  const T dist_thresh = (T)rs.distThresh;
+  T detail = (T)rs.distThresh;
+  if (rs.found) {
+    // ObjectShader (src/shaders.cpp:21-112), no aux/fake lights, no env mapping
+    const V3<T> point{(T)rs.point[0], (T)rs.point[1], (T)rs.point[2]};
+    T delta;
+    if (p.constantDEThreshold) delta = (T)rs.scan * p.resolution * p.persp;
+    else delta = dist_thresh * p.quality;
+    const V3<T> n = calc_normal<T, FORMULA>(p, point, delta, dist_thresh, detail, cnt);
+    const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
+    T shade = dot3(n, lv);
+    if (shade < T(0)) shade = T(0);
+    const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
+    T shadow = T(1);
+    if (p.shadow) shadow = main_shadow<T, FORMULA>(p, point, dist_thresh, delta, detail, io, cnt);
+    // MainSpecular (src/shaders.cpp:770-783)
+    V3<T> half = normalize3(lv - viewT);
+    T shade2 = dot3(n, half);
+    if (shade2 < T(0)) shade2 = T(0);
+    shade2 = m_pow(shade2, T(30)) * T(1);
+    if (shade2 > T(15)) shade2 = T(15);
+    const T spec = shade2 * p.specular;
+    const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt);
+    objColour = colour;
+    V3<T> ambient{T(0), T(0), T(0)};
+    if (p.ao) {
+      if (p.fastAO) {
+        const T a = fast_ao<T, FORMULA>(p, point, n, dist_thresh, detail, cnt);
+        ambient = {a, a, a};
+      } else {
+        ambient = ray_ao<T, FORMULA>(p, point, delta, dist_thresh, (T)rs.dist, detail, cnt);
+      }
+    }
+    const V3<T> ambient2{ambient.x * p.globalIlum, ambient.y * p.globalIlum, ambient.z * p.globalIlum};
+    const T objR = T(0) + (ambient2.x + p.mainLight[0] * shadeV * shadow) * colour.x;
+    const T objG = T(0) + (ambient2.y + p.mainLight[1] * shadeV * shadow) * colour.y;
+    const T objB = T(0) + (ambient2.z + p.mainLight[2] * shadeV * shadow) * colour.z;
+    const T specR = T(0) + p.mainLight[0] * spec * shadow;
+    const T specG = T(0) + p.mainLight[1] * spec * shadow;
+    const T specB = T(0) + p.mainLight[2] * spec * shadow;
+    result[0] = objR + T(0) + specR;
+    result[1] = objG + T(0) + specG;
+    result[2] = objB + T(0) + specB;
+    result[3] = T(1) + T(0);
+  } else {
+    const V3<T> bg = background(p, viewT);
+    result[0] = T(0) + bg.x + T(0);
+    result[1] = T(0) + bg.y + T(0);
+    result[2] = T(0) + bg.z + T(0);
+    result[3] = T(0);
+    depth = 1e20;
+  }
+  float totalOpacity = 0.0f;
+  bool opacitySet = false;
+  // the volumetric pass sees the march depth even for background pixels: the
+  // shader input is filled before the depth becomes 1e20 (src/Render3D.cpp:518-541)
+  if (p.needVolumetric) volumetric<T>(p, sb, rs.buffCount, (T)rs.scan, result, totalOpacity, opacitySet);
+
+  // buffer writes (src/Render3D.cpp:569-589)
+  if (io.opacity) io.opacity[pix] = to_u16_x86((double)totalOpacity * 65535.0);
+  if (io.alpha) io.alpha[pix] = to_u16_x86((double)result[3] * 65535.0);
+  if (io.image_float) {
+    io.image_float[3 * pix + 0] = (float)result[0];
+    io.image_float[3 * pix + 1] = (float)result[1];
+    io.image_float[3 * pix + 2] = (float)result[2];
+  }
+  if (io.colour) {
+    io.colour[3 * pix + 0] = to_u8_x86((double)(objColour.x * T(255)));
+    io.colour[3 * pix + 1] = to_u8_x86((double)(objColour.y * T(255)));
+    io.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
+  }
+  if (io.zbuffer) io.zbuffer[pix] = (float)depth;
+  if (io.hit) io.hit[pix] = rs.found ? 1 : 0;
+  if (io.iters) io.iters[pix] = rs.iters;
+  if (io.depth) io.depth[pix] = depth;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent kernel: each warp claims 8x4 pixel tiles from a global counter
+// until the frame is done, replacing the row claiming of MainThread
+// (src/Render3D.cpp:352-366) and the thread spawn of Render (src/Render3D.cpp:815-849).
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA>
+__global__ void __launch_bounds__(128) render_kernel(const ParamsT<T> p, const FractalT<double> fd, const FrameIO io) {
+  const int lane = threadIdx.x & 31;
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, io.slots, slot};
+  Counters cnt{0, 0, 0, 0};
+  const int tilesX = (p.width + kTileW - 1) / kTileW;
+  const int rowTiles = (p.row_end - p.row_begin + kTileH - 1) / kTileH;
+  const unsigned int nTiles = (unsigned int)(tilesX * rowTiles);
+  for (;;) {
+    unsigned int t = 0;
+    int stop = 0;
+    if (lane == 0) {
+      t = atomicAdd(io.tile_counter, 1u);
+      if (deadline_passed(io)) { atomicExch(io.error_flag, 1); stop = 1; }
+      if (*(volatile int *)io.error_flag) stop = 1;
+    }
+    t = __shfl_sync(0xffffffffu, t, 0);
+    stop = __shfl_sync(0xffffffffu, stop, 0);
+    if (stop || t >= nTiles) break;
+    const int tx = (int)(t % (unsigned int)tilesX);
+    const int ty = (int)(t / (unsigned int)tilesX);
+    const int x = tx * kTileW + (lane % kTileW);
+    const int y = p.row_begin + ty * kTileH + (lane / kTileW);
+    if (x < p.width && y < p.row_end) render_pixel<T, FORMULA>(p, fd, io, x, y, sb, cnt);
+  }
+  // one atomic per warp for the counters
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+    cnt.steps += __shfl_down_sync(0xffffffffu, cnt.steps, off);
+    cnt.missed += __shfl_down_sync(0xffffffffu, cnt.missed, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+    atomicAdd(&io.counters[2], cnt.steps);
+    atomicAdd(&io.counters[3], cnt.missed);
+  }
+}
+
+// CalculateDistance at arbitrary points (unit tests of the distance estimator).
+template <typename T, int FORMULA>
+__global__ void distance_kernel(const FractalT<T> f, const double *points, const double *detail, int64_t n,
+                                double *dist, int32_t *iters, uint8_t *max_iter, unsigned long long *counters) {
+  Counters cnt{0, 0, 0, 0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const V3<T> pt{(T)points[3 * i], (T)points[3 * i + 1], (T)points[3 * i + 2]};
+    int L = 0;
+    bool mi = false;
+    const T d = calc_distance<T, FORMULA>(f, pt, (T)detail[i], f.N, f.minN, false, L, mi, cnt);
+    dist[i] = (double)d;
+    iters[i] = L;
+    max_iter[i] = mi ? 1 : 0;
+  }
+  if (counters) {
+    atomicAdd(&counters[0], cnt.orbit);
+    atomicAdd(&counters[1], cnt.calls);
+  }
+}
+
+}  // namespace dev
+}  // namespace mbgb

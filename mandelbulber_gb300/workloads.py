@@ -1,0 +1,124 @@
+"""Scenes of the benchmark workloads, built from settings keys.
+
+Each workload is a dictionary of .fract keys (the names LoadOneSetting reads,
+src/settings.cpp:700-1183) applied to a zeroed scene, followed by the palette
+rule of LoadSettingsPost (src/settings.cpp:1185-1195) and the -nogui fix-ups.
+The values not named by a workload are the hot-path entries of the
+reference's default parameter set.
+
+  mandelbulb_640x480    Mandelbulb power 8 (trig_optim, formula 2), N 250, 640x480,
+                        camera (0,-3.5,0) looking +y, 53 deg horizontal FOV, DE factor 1,
+                        threshold = 1 pixel footprint, light at 45/45 deg, hard shadows,
+                        no AO / fog / glow.
+  mandelbox_1080p       Mandelbox scale 2 (tglad, formula 8), fold limit 1 / value 2,
+                        sphere fold 0.5 / 1.0, N 15 (bailout 1024), 1920x1080, camera
+                        (0,-20,0) looking +y (the scale-2 box spans |y| <= 6, so a camera
+                        at distance 6 would sit on its face), 53 deg FOV, hard shadows,
+                        ray-traced AO (quality 2:
+                        29 directions), volumetric fog density 0.5 over the primary
+                        step buffer, glow on.
+"""
+from __future__ import annotations
+
+import math
+
+from . import finalize, mbgb_scene, palette_from_seed, scene_set
+
+# hot-path entries of the reference's default parameter set
+BASE = {
+    "image_width": 800, "image_height": 600, "tiles": 1,
+    "x_min": -10, "x_max": 10, "y_min": -10, "y_max": 10, "z_min": -10, "z_max": 10,
+    "view_point_x": 0, "view_point_y": 0, "view_point_z": 0,
+    "angle_alfa": 0, "angle_beta": 0, "angle_gamma": 0,
+    "zoom": 1e-15, "perspective": 0.5, "formula": 2, "power": 8, "N": 250, "minN": 1,
+    "fractal_constant_factor": 1, "quality": 1, "smoothness": 1,
+    "julia_mode": 0, "tglad_folding_mode": 0, "folding_limit": 1, "folding_value": 2,
+    "spherical_folding_mode": 0, "spherical_folding_fixed": 1, "spherical_folding_min": 0.5,
+    "IFS_folding_mode": 0, "iteration_threshold_mode": 0, "analityc_DE_mode": 1, "DE_factor": 1,
+    "brightness": 1, "contrast": 1, "gamma": 1, "ambient": 0, "reflect": 0, "shadows_intensity": 0.7,
+    "ambient_occlusion": 1, "ambient_occlusion_quality": 4, "ambient_occlusion_fast_tune": 1,
+    "shading": 1, "specular": 1, "glow_intensity": 1,
+    "glow_color_1_R": 40984, "glow_color_1_G": 44713, "glow_color_1_B": 49490,
+    "glow_color_2_R": 57192, "glow_color_2_G": 60888, "glow_color_2_B": 62408,
+    "background_color_1_R": 0, "background_color_1_G": 38306, "background_color_1_B": 65535,
+    "background_color_2_R": 65535, "background_color_2_G": 65535, "background_color_2_B": 65535,
+    "background_color_3_R": 0, "background_color_3_G": 10000, "background_color_3_B": 500,
+    "fog_colour_1_R": 0, "fog_colour_1_G": 0, "fog_colour_1_B": 0,
+    "fog_colour_2_R": 0, "fog_colour_2_G": 30000, "fog_colour_2_B": 65535,
+    "fog_colour_3_R": 65535, "fog_colour_3_G": 65535, "fog_colour_3_B": 65535,
+    "textured_background": 0, "shadows_enabled": 1, "ambient_occlusion_enabled": 0,
+    "fast_ambient_occlusion_mode": 0, "fractal_color": 1, "coloring_random_seed": 123456,
+    "coloring_saturation": 1, "coloring_speed": 1, "coloring_palette_offset": 0, "slow_shading": 0,
+    "limits_enabled": 0, "post_fog_enabled": 0, "post_fog_visibility": 20,
+    "post_fog_color_R": 59399, "post_fog_color_G": 61202, "post_fog_color_B": 65535,
+    "post_SSAO_enabled": 0, "post_SSAO_quality": 20, "post_DOF_enabled": 0,
+    "main_light_intensity": 1, "main_light_alfa": -0.78539816339744828, "main_light_beta": 0.78539816339744828,
+    "main_light_colour_R": 65535, "main_light_colour_G": 65535, "main_light_colour_B": 65535,
+    "aux_light_number": 0, "aux_light_visibility": 1,
+    "mandelbox_scale": 2, "mandelbox_folding_limit": 1, "mandelbox_folding_value": 2,
+    "mandelbox_folding_min_radius": 0.5, "mandelbox_folding_fixed_radius": 1,
+    "mandelbox_color_R": 0, "mandelbox_color_X": 0.03, "mandelbox_color_Y": 0.05, "mandelbox_color_Z": 0.07,
+    "mandelbox_color_Sp1": 0.2, "mandelbox_color_Sp2": 0.2, "mandelbox_rotation_enabled": 0,
+    "view_distance_max": 50, "view_distance_min": 1e-15, "interior_mode": 0, "linear_DE_mode": 0,
+    "constant_DE_threshold": 0, "penetrating_lights": 1, "raytraced_reflections": 0, "reflections_max": 5,
+    "volumetric_fog_density": 0, "volumetric_fog_colour_1_distance": 1, "volumetric_fog_colour_2_distance": 2,
+    "volumetric_fog_distance_factor": 1, "iteration_fog_enable": 0, "fish_eye": 0,
+}
+
+
+def fov_persp(width: int, height: int, fov_deg: float = 53.0) -> float:
+    """The reference's perspective factor for a horizontal field of view.
+
+    The view vector is (x2 * persp, 1, z2 * persp) with x2 in [-aspect/2, aspect/2)
+    (src/Render3D.cpp:391-438), so tan(fov/2) = persp * aspect / 2.
+    """
+    return 2.0 * math.tan(math.radians(fov_deg / 2.0)) / (width / height)
+
+
+MANDELBULB_640x480 = {
+    "image_width": 640, "image_height": 480, "formula": 2, "power": 8, "N": 250,
+    "view_point_x": 0, "view_point_y": -3.5, "view_point_z": 0,
+    "perspective": fov_persp(640, 480), "DE_factor": 1, "quality": 1,
+    "main_light_alfa": math.radians(45.0), "main_light_beta": math.radians(45.0),
+    "shadows_enabled": 1, "shadows_cone_angle": 0, "penetrating_lights": 0,
+    "ambient_occlusion_enabled": 0, "volumetric_fog_density": 0, "glow_intensity": 0,
+    "post_SSAO_enabled": 0, "fractal_color": 1,
+}
+
+MANDELBOX_1080P = {
+    "image_width": 1920, "image_height": 1080, "formula": 8, "N": 15,
+    "mandelbox_scale": 2.0, "mandelbox_folding_limit": 1.0, "mandelbox_folding_value": 2.0,
+    "mandelbox_folding_min_radius": 0.5, "mandelbox_folding_fixed_radius": 1.0,
+    "view_point_x": 0, "view_point_y": -20.0, "view_point_z": 0,
+    "perspective": fov_persp(1920, 1080), "DE_factor": 1, "quality": 1,
+    "main_light_alfa": math.radians(45.0), "main_light_beta": math.radians(45.0),
+    "shadows_enabled": 1, "shadows_cone_angle": 0, "penetrating_lights": 0,
+    "ambient_occlusion_enabled": 1, "fast_ambient_occlusion_mode": 0, "ambient_occlusion_quality": 2,
+    "volumetric_fog_density": 0.5, "glow_intensity": 1, "post_SSAO_enabled": 0, "fractal_color": 1,
+}
+
+WORKLOADS = {"mandelbulb_640x480": MANDELBULB_640x480, "mandelbox_1080p": MANDELBOX_1080P}
+
+
+def make_scene(overrides: dict, base: dict | None = None) -> mbgb_scene:
+    """A finalized scene from BASE updated with `overrides` (keys as in .fract files)."""
+    keys = dict(BASE if base is None else base)
+    keys.update(overrides)
+    s = mbgb_scene()
+    for k, v in keys.items():
+        scene_set(s, k, repr(float(v)) if isinstance(v, float) else v)
+    pal = palette_from_seed(int(keys["coloring_random_seed"]), float(keys["coloring_saturation"]))
+    for i in range(256):
+        s.palette[i].R, s.palette[i].G, s.palette[i].B = (int(c) for c in pal[i])
+    s.paletteLoaded = 0
+    return finalize(s)
+
+
+def workload(name: str, width: int | None = None, height: int | None = None, **extra) -> mbgb_scene:
+    """A named workload, optionally at another resolution (FOV kept) or with extra keys."""
+    keys = dict(WORKLOADS[name])
+    if width and height:
+        keys["image_width"], keys["image_height"] = width, height
+        keys["perspective"] = fov_persp(width, height)
+    keys.update(extra)
+    return make_scene(keys)

@@ -1,0 +1,701 @@
+// ORACLE — test infrastructure, not product code.
+//
+// A plain double-precision CPU restatement of Mandelbulber 1.21's per-pixel
+// distance-estimated ray march, used (1) by the GPU parity tests as the checker
+// and (2) by bench.py as the timed CPU baseline. It shares no code with the
+// CUDA renderer. Parity of this restatement with the reference itself is pinned
+// by tests/test_oracle_golden.py against golden vectors that
+// tests/golden/make_golden.py produced by running the reference's own compiled
+// fractal.cpp / shaders.cpp (oracle/_ref).
+//
+// Function-by-function sources (reference paths):
+//   compute_normal / compute_colour   Compute<normal|colouring>  src/fractal.cpp:40-1241
+//   calculate_distance                CalculateDistance          src/fractal.cpp:1245-1448
+//   ray_marching                      RayMarching                src/Render3D.cpp:79-199
+//   calculate_normals                 CalculateNormals           src/shaders.cpp:675-757
+//   main_shadow                       MainShadow                 src/shaders.cpp:480-570
+//   fast_ao / ray_ao                  FastAmbientOcclusion2 / AmbientOcclusion src/shaders.cpp:585-673
+//   surface_colour, index_to_colour   SurfaceColour / IndexToColour src/shaders.cpp:813-879, 1273-1305
+//   background                        BackgroundShader           src/shaders.cpp:114-183
+//   volumetric                        VolumetricShader           src/shaders.cpp:185-478
+//   render_rows                       MainThread pixel body      src/Render3D.cpp:213-344, 389-589
+// Build: oracle/Makefile, -O2 -ffp-contract=off (parity) and -O3 -ffast-math (timing).
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../include/mbgb.h"
+
+namespace {
+
+struct Vec {
+  double x, y, z;
+};
+inline Vec add(Vec a, Vec b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline Vec sub(Vec a, Vec b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline Vec mul(Vec a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline double dot(Vec a, Vec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double len(Vec a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline Vec normalize(Vec a) {
+  double n = 1.0 / len(a);
+  return {a.x * n, a.y * n, a.z * n};
+}
+inline Vec rot(const double *m, int zero, Vec v) {
+  if (zero) return v;
+  return {m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z, m[6] * v.x + m[7] * v.y + m[8] * v.z};
+}
+// x86-64 conversion results (cvttsd2si into a 32-bit register)
+inline int to_i32(double v) { return (v >= -2147483648.0 && v < 2147483648.0) ? (int)v : (int)0x80000000u; }
+inline unsigned short to_u16(double v) { return (unsigned short)to_i32(v); }
+inline unsigned char to_u8(double v) { return (unsigned char)to_i32(v); }
+
+struct Cnt {
+  uint64_t orbit = 0, calls = 0, steps = 0;
+};
+
+// Mutable DE state that the reference keeps in its sFractal copy.
+struct Calc {
+  const mbgb_scene *s;
+  int N;            // (int)doubles.N, changed by normals (x5) and colouring (x10)
+  int minN;
+  bool normalMode;
+  double detail;    // doubles.detailSize
+  int itersOut;
+  Cnt *cnt;
+};
+
+// Compute<Mode>; colour = false -> normal mode.
+double compute(const Calc &c, Vec z, bool colour, int *Lout) {
+  const mbgb_scene &s = *c.s;
+  const int N = c.N;
+  double distance = 0;
+  double r_dz = 1;
+  const double p = s.power;
+  const double fR2 = s.mboxFoldingSphericalFixed * s.mboxFoldingSphericalFixed;
+  const double mR2 = s.mboxFoldingSphericalMin * s.mboxFoldingSphericalMin;
+  const double f1 = fR2 / mR2;
+  double tDE = 1.0, tCol = 1.0;
+  const double scale = s.mboxScale;
+  const bool box = s.formula == MBGB_FORMULA_TGLAD;
+  Vec cst = s.juliaMode ? Vec{s.julia[0], s.julia[1], s.julia[2]} : mul(z, s.constantFactor);
+  double r = len(z);
+  double minv = 1e200;
+  int L;
+  for (L = 0; L < N; L++) {
+    if (s.tgladFoldingMode) {
+      const double fl = s.foldingLimit, fv = s.foldingValue;
+      if (z.x > fl) { z.x = fv - z.x; tCol *= 0.9; } else if (z.x < -fl) { z.x = -fv - z.x; tCol *= 0.9; }
+      if (z.y > fl) { z.y = fv - z.y; tCol *= 0.9; } else if (z.y < -fl) { z.y = -fv - z.y; tCol *= 0.9; }
+      if (z.z > fl) { z.z = fv - z.z; tCol *= 0.9; } else if (z.z < -fl) { z.z = -fv - z.z; tCol *= 0.9; }
+      r = len(z);
+    }
+    if (s.sphericalFoldingMode) {
+      const double a = s.foldingSphericalFixed * s.foldingSphericalFixed;
+      const double b = s.foldingSphericalMin * s.foldingSphericalMin;
+      const double r2 = r * r;
+      const double k1 = a / b;
+      if (r2 < b) { z = mul(z, k1); tDE *= k1; tCol += 1; }
+      else if (r2 < a) { const double k2 = a / r2; z = mul(z, k2); tDE *= k2; tCol += 10; }
+      r = len(z);
+    }
+    if (s.formula == MBGB_FORMULA_TRIG_OPTIM) {
+      const double th0 = asin(z.z / r);
+      const double ph0 = atan2(z.y, z.x);
+      double rp = pow(r, p - 1.0);
+      const double th = th0 * p, ph = ph0 * p;
+      const double cth = cos(th);
+      r_dz = rp * r_dz * p + 1.0;
+      rp *= r;
+      z = add(mul(Vec{cth * cos(ph), cth * sin(ph), sin(th)}, rp), cst);
+      r = len(z);
+    } else if (box) {
+      const double fl = s.mboxFoldingLimit, fv = s.mboxFoldingValue;
+      if (s.mboxRotationsEnabled) {
+        bool lock = false;
+        z = rot(s.mboxRot[0][0], s.mboxRotZero[0][0], z);
+        if (z.x > fl) { z.x = fv - z.x; tCol += s.mboxColorFactorX; lock = true; }
+        z = rot(s.mboxRotInv[0][0], 0, z);
+        z = rot(s.mboxRot[1][0], s.mboxRotZero[1][0], z);
+        if (!lock && z.x < -fl) { z.x = -fv - z.x; tCol += s.mboxColorFactorX; }
+        z = rot(s.mboxRotInv[1][0], 0, z);
+        lock = false;
+        z = rot(s.mboxRot[0][1], s.mboxRotZero[0][1], z);
+        if (z.y > fl) { z.y = fv - z.y; tCol += s.mboxColorFactorY; lock = true; }
+        z = rot(s.mboxRotInv[0][1], 0, z);
+        z = rot(s.mboxRot[1][1], s.mboxRotZero[1][1], z);
+        if (!lock && z.y < -fl) { z.y = -fv - z.y; tCol += s.mboxColorFactorY; }
+        z = rot(s.mboxRotInv[1][1], 0, z);
+        lock = false;
+        z = rot(s.mboxRot[0][2], s.mboxRotZero[0][2], z);
+        if (z.z > fl) { z.z = fv - z.z; tCol += s.mboxColorFactorZ; lock = true; }
+        z = rot(s.mboxRotInv[0][2], 0, z);
+        z = rot(s.mboxRot[1][2], s.mboxRotZero[1][2], z);
+        if (!lock && z.z < -fl) { z.z = -fv - z.z; tCol += s.mboxColorFactorZ; }
+        z = rot(s.mboxRotInv[1][2], 0, z);
+      } else {
+        if (z.x > fl) { z.x = fv - z.x; tCol += s.mboxColorFactorX; } else if (z.x < -fl) { z.x = -fv - z.x; tCol += s.mboxColorFactorX; }
+        if (z.y > fl) { z.y = fv - z.y; tCol += s.mboxColorFactorY; } else if (z.y < -fl) { z.y = -fv - z.y; tCol += s.mboxColorFactorY; }
+        if (z.z > fl) { z.z = fv - z.z; tCol += s.mboxColorFactorZ; } else if (z.z < -fl) { z.z = -fv - z.z; tCol += s.mboxColorFactorZ; }
+      }
+      r = len(z);
+      const double r2 = r * r;
+      const Vec off{s.mboxOffset[0], s.mboxOffset[1], s.mboxOffset[2]};
+      z = add(z, off);
+      if (r2 < mR2) { z = mul(z, f1); tDE *= f1; tCol += s.mboxColorFactorSp1; }
+      else if (r2 < fR2) { const double f2 = fR2 / r2; z = mul(z, f2); tDE *= f2; tCol += s.mboxColorFactorSp2; }
+      z = sub(z, off);
+      z = rot(s.mboxMainRot, s.mboxMainRotZero, z);
+      z = add(mul(z, scale), cst);
+      tDE = tDE * fabs(scale) + 1.0;
+      r = len(z);
+    }
+    if (box) {
+      if (r > 1024) { distance = r / fabs(tDE); break; }
+    } else if (!colour) {
+      if (r > 1e2) { distance = 0.5 * r * log(r) / r_dz; break; }
+    } else {
+      distance = len(z);
+      if (distance < minv) minv = distance;
+      if (distance > 1e15) { distance = minv; break; }
+    }
+  }
+  c.cnt->orbit += (uint64_t)(L + 1);
+  c.cnt->calls++;
+  if (Lout) *Lout = L;
+  if (!colour) {
+    if (L == N) distance = 0;
+    return distance;
+  }
+  if (box) return tCol * 100.0 + len(z) * s.mboxColorFactorR;
+  return distance * 5000.0;
+}
+
+double calculate_distance(Calc &c, Vec p, bool *max_iter) {
+  const mbgb_scene &s = *c.s;
+  double limit = 0.0;
+  if (s.limits_enabled) {
+    auto mx = [](double a, double b) { return a > b ? a : b; };
+    const double da = mx(p.x - s.amax, -(p.x - s.amin));
+    const double db = mx(p.y - s.bmax, -(p.y - s.bmin));
+    const double dc = mx(p.z - s.cmax, -(p.z - s.cmin));
+    limit = (da > db) ? ((da > dc) ? da : dc) : ((db > dc) ? db : dc);
+    if (limit > c.detail) {
+      if (max_iter) *max_iter = false;
+      return limit;
+    }
+  }
+  int L;
+  double d = compute(c, p, false, &L);
+  if (max_iter) *max_iter = (L == c.N);
+  c.itersOut = L;
+  if (d < 0) d = 0;
+  if (L < c.minN && d < c.detail) d = c.detail;
+  if (s.interiorMode && !c.normalMode) {
+    if (d < 0.5 * c.detail || L == c.N) {
+      d = c.detail;
+      if (max_iter) *max_iter = false;
+    }
+  } else if (s.interiorMode && c.normalMode) {
+    if (d < 0.9 * c.detail) {
+      d = c.detail - d;
+      if (max_iter) *max_iter = false;
+    }
+  }
+  if (s.iterThresh && L < c.N) {
+    if (d < c.detail) d = c.detail * 1.01;
+  }
+  if (s.limits_enabled && limit < c.detail) d = d > limit ? d : limit;
+  return d;
+}
+
+struct Step {
+  double dist, step, thr;
+};
+
+struct Ray {
+  bool found;
+  int count;
+  double thr, lastDist, depth;
+  Vec point;
+};
+
+Ray ray_marching(const mbgb_scene &s, Calc &c, Vec start, Vec dir, std::vector<Step> &buf, bool jitter, Cnt &cnt) {
+  Ray out{};
+  Vec point{0, 0, 0};
+  bool found = false;
+  double scan = s.viewDistanceMin;
+  double thr = 0.0;
+  const double thrInit = 0.0;
+  double dist = 0;
+  const double limit = 1.0 - 0.01 * s.quality;
+  double step = s.viewDistanceMin;
+  int count = 0;
+  for (int i = 0; i < 10000; i++) {
+    cnt.steps++;
+    point = add(start, mul(dir, scan));
+    bool mi = false;
+    if (s.constantDEThreshold) thr = s.quality;
+    else thr = scan * s.resolution * s.persp / s.quality + thrInit;
+    if (s.perspectiveType == MBGB_PERSP_EQUIRECT || s.perspectiveType == MBGB_PERSP_FISH_EYE) thr *= M_PI;
+    c.detail = thr;
+    dist = calculate_distance(c, point, &mi);
+    buf[i].dist = dist;
+    buf[i].thr = thr;
+    if (dist > 3.0) dist = 3.0;
+    if (dist < thr) {
+      found = true;
+      break;
+    }
+    buf[i].step = step;
+    const double j = jitter ? (1.0 - (rand() % 1001) / 10000.0) : 1.0;
+    step = (dist - (s.interiorMode ? 0.8 : 0.5) * thr) * s.DE_factor * j;
+    count++;
+    scan += step;
+    if (scan > s.viewDistanceMax) break;
+  }
+  if (found) {
+    step *= 0.5;
+    for (int i = 0; i < 20; i++) {
+      cnt.steps++;
+      if (dist < thr && dist > thr * limit) break;
+      if (dist > thr) {
+        scan += step;
+        point = add(start, mul(dir, scan));
+      } else if (dist < thr * limit) {
+        scan -= step;
+        point = add(start, mul(dir, scan));
+      }
+      if (s.constantDEThreshold) thr = s.quality;
+      else thr = scan * s.resolution * s.persp / s.quality + thrInit;
+      bool mi = false;
+      dist = calculate_distance(c, point, &mi);
+      step *= 0.5;
+    }
+  }
+  out.found = found;
+  out.count = count;
+  out.thr = thr;
+  out.lastDist = dist;
+  out.depth = scan;
+  out.point = point;
+  return out;
+}
+
+Vec calculate_normals(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr) {
+  double d = delta * s.smoothness;
+  if (s.interiorMode) d = thr * s.quality * 0.2 * s.smoothness;
+  const int N0 = c.N, minN0 = c.minN;
+  c.N = (int)(s.N * 5);
+  c.minN = 0;
+  c.normalMode = true;
+  bool mi;
+  const double s1 = calculate_distance(c, p, &mi);
+  const double s2 = calculate_distance(c, Vec{p.x + d, p.y + 0.0, p.z + 0.0}, &mi);
+  const double s3 = calculate_distance(c, Vec{p.x + 0.0, p.y + d, p.z + 0.0}, &mi);
+  const double s4 = calculate_distance(c, Vec{p.x + 0.0, p.y + 0.0, p.z + d}, &mi);
+  Vec n{s2 - s1, s3 - s1, s4 - s1};
+  c.N = N0;
+  c.minN = minN0;
+  c.normalMode = false;
+  if (n.x == 0 && n.y == 0 && n.z == 0) n.x = 1;
+  else n = normalize(n);
+  return n;
+}
+
+double main_shadow(const mbgb_scene &s, Calc &c, Vec p, Vec light, double thr, double delta) {
+  double factor = delta / s.resolution;
+  if (!s.penetratingLights) factor = s.viewDistanceMax;
+  double dist = thr;
+  c.detail = thr;
+  const double DE_factor = s.DE_factor;
+  double start = thr;
+  if (s.interiorMode) start = thr * DE_factor;
+  double shadowTemp = 1.0;
+  const double softRange = tan(s.shadowConeAngle / 180.0 * M_PI);
+  double maxSoft = 0.0;
+  const bool bSoft = (!s.iterFogEnabled && !s.limits_enabled && !s.iterThresh) && softRange > 0.0;
+  for (double i = start; i < factor; i += dist * DE_factor) {
+    const Vec p2 = add(p, mul(light, i));
+    const float thr_f = (float)thr;  // the reference's float threshold
+    c.detail = thr_f;
+    bool mi;
+    dist = calculate_distance(c, p2, &mi);
+    if (bSoft) {
+      double angle = (dist - thr_f) / i;
+      if (angle < 0) angle = 0;
+      if (dist < thr_f) angle = 0;
+      double soft = (1.0 - angle / softRange);
+      if (s.penetratingLights) soft *= (factor - i) / factor;
+      if (soft < 0) soft = 0;
+      if (soft > maxSoft) maxSoft = soft;
+    }
+    if (dist < thr_f || shadowTemp < 0.0) {
+      shadowTemp -= (factor - i) / factor;
+      if (!s.penetratingLights) shadowTemp = 0.0;
+      if (shadowTemp < 0.0) shadowTemp = 0.0;
+      break;
+    }
+  }
+  return bSoft ? 1.0 - maxSoft : shadowTemp;
+}
+
+double fast_ao(const mbgb_scene &s, Calc &c, Vec p, Vec n, double thr) {
+  double ao = 0;
+  const double q = s.globalIlumQuality;
+  for (int i = 1; i < q * q; i++) {
+    const double scan = i * i * thr;
+    bool mi;
+    const double dist = calculate_distance(c, add(p, mul(n, scan)), &mi);
+    ao += 1.0 / (pow(2.0, i)) * (scan - s.fastAoTune * dist) / thr;
+  }
+  double r = 1.0 - 0.2 * ao;
+  return r < 0 ? 0 : r;
+}
+
+double ray_ao(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr, double lastDist,
+              const std::vector<Vec> &dirs) {
+  const double end = delta / s.resolution;
+  double AO = 0;
+  for (const Vec &v : dirs) {
+    double dist = lastDist;
+    double sh = 1.0;
+    for (double r = delta; r < end; r += dist * 2.0) {
+      bool mi;
+      dist = calculate_distance(c, add(p, mul(v, r)), &mi);
+      const float thr_f = (float)thr;
+      if (dist < thr_f || mi || sh < 0.0) {
+        sh -= (end - r) / end;
+        if (sh < 0.0) sh = 0.0;
+        break;
+      }
+    }
+    AO += sh * 255;
+  }
+  return AO / (dirs.size() * 256.0);
+}
+
+void index_to_colour(const mbgb_scene &s, int index, int out[3]) {
+  if (index < 0) {
+    out[0] = s.palette[255].R; out[1] = s.palette[255].G; out[2] = s.palette[255].B;
+    return;
+  }
+  out[0] = out[1] = out[2] = 255;
+  index = index % (255 * 256);
+  const int kol = index / 256;
+  if (kol < 255) {
+    const int delta = index % 256;
+    const int a[3] = {s.palette[kol].R, s.palette[kol].G, s.palette[kol].B};
+    const int b[3] = {s.palette[kol + 1].R, s.palette[kol + 1].G, s.palette[kol + 1].B};
+    for (int k = 0; k < 3; k++) {
+      const double R1 = a[k], R2 = b[k];
+      const double RK = (R2 - R1) / 256.0;
+      out[k] = (int)(R1 + (RK * delta));
+    }
+  }
+}
+
+Vec surface_colour(const mbgb_scene &s, Calc &c, Vec p) {
+  const int N0 = c.N;
+  c.N = (int)(s.N * 10);
+  int nr = to_i32(floor(compute(c, p, true, nullptr)));
+  c.N = N0;
+  // abs(nrCol) % (248 * 256): the reference binary takes the magnitude as unsigned,
+  // so an out-of-range conversion (INT_MIN) yields 2^31 % 63488 = 2048.
+  const unsigned mag = nr < 0 ? 0u - (unsigned)nr : (unsigned)nr;
+  nr = (int)(mag % (248u * 256u));
+  int col[3] = {256, 256, 256};
+  if (s.coloringEnabled) {
+    int num;
+    if (nr >= 248 * 256) num = nr;
+    else num = to_i32(nr * s.coloring_speed + 256 * s.paletteOffset) % 65536;
+    index_to_colour(s, num, col);
+  }
+  return {col[0] / 256.0, col[1] / 256.0, col[2] / 256.0};
+}
+
+Vec background(const mbgb_scene &s, Vec view) {
+  const Vec v = normalize(Vec{0.0, 0.0, -1.0});
+  double grad = (dot(view, v) + 1.0);
+  const int c1[3] = {s.background_color1.R, s.background_color1.G, s.background_color1.B};
+  const int c2[3] = {s.background_color2.R, s.background_color2.G, s.background_color2.B};
+  const int c3[3] = {s.background_color3.R, s.background_color3.G, s.background_color3.B};
+  unsigned short px[3];
+  if (grad < 1) {
+    const double ng = 1.0 - grad;
+    for (int k = 0; k < 3; k++) px[k] = to_u16(c3[k] * ng + c2[k] * grad);
+  } else {
+    grad = grad - 1;
+    const double ng = 1.0 - grad;
+    for (int k = 0; k < 3; k++) px[k] = to_u16(c2[k] * ng + c1[k] * grad);
+  }
+  return {px[0] / 65536.0, px[1] / 65536.0, px[2] / 65536.0};
+}
+
+void volumetric(const mbgb_scene &s, const std::vector<Step> &buf, int count, double depth, double out[4],
+                float *opacity) {
+  float total = 0.0f;
+  const double glow = count * s.glow_intensity / 512.0 * s.DE_factor;
+  double glowN = 1.0 - glow;
+  if (glowN < 0.0) glowN = 0.0;
+  const double gR = (s.glow_color1.R * glowN + s.glow_color2.R * glow) / 65536.0;
+  const double gG = (s.glow_color1.G * glowN + s.glow_color2.G * glow) / 65536.0;
+  const double gB = (s.glow_color1.B * glowN + s.glow_color2.B * glow) / 65536.0;
+  const double fogVis = pow(10.0, s.fogVisibility / 10 - 16.0);
+  const double ct1 = s.fogColour1Distance, ct2 = s.fogColour2Distance, red = s.fogDistanceFactor, I = s.fogDensity;
+  double acc = 0.0;
+  for (int k = count - 1; k > 0; k--) {
+    double step = buf[k].step;
+    const double d = buf[k].dist;
+    acc += step;
+    if (acc < buf[k].thr * s.quality) continue;
+    step = acc;
+    acc = 0.0;
+    const double go = glow * step / depth;
+    out[0] = go * gR + (1.0 - go) * out[0];
+    out[1] = go * gG + (1.0 - go) * out[1];
+    out[2] = go * gB + (1.0 - go) * out[2];
+    out[3] += go;
+    if (s.fogEnabled) {
+      double fd = step / fogVis;
+      if (fd > 1.0) fd = 1.0;
+      out[0] = fd * s.fogColor.R / 65536.0 + (1.0 - fd) * out[0];
+      out[1] = fd * s.fogColor.G / 65536.0 + (1.0 - fd) * out[1];
+      out[2] = fd * s.fogColor.B / 65536.0 + (1.0 - fd) * out[2];
+      total = fd + (1.0 - fd) * total;
+      out[3] = fd + (1.0 - fd) * out[3];
+    }
+    if (I > 0.0) {
+      const double dt = (step * red) / (d * d + red * red);
+      double kk = d / ct1;
+      if (kk > 1) kk = 1.0;
+      double kn = 1.0 - kk;
+      double fr = (s.fogColour1.R * kn + s.fogColour2.R * kk);
+      double fg = (s.fogColour1.G * kn + s.fogColour2.G * kk);
+      double fb = (s.fogColour1.B * kn + s.fogColour2.B * kk);
+      double k2 = d / ct2 * kk;
+      if (k2 > 1) k2 = 1.0;
+      kn = 1.0 - k2;
+      fr = (fr * kn + s.fogColour3.R * k2);
+      fg = (fg * kn + s.fogColour3.G * k2);
+      fb = (fb * kn + s.fogColour3.B * k2);
+      double fd = 0.3 * I * dt / (1.0 + I * dt);
+      if (fd > 1) fd = 1.0;
+      out[0] = fd * fr / 65536.0 + (1.0 - fd) * out[0];
+      out[1] = fd * fg / 65536.0 + (1.0 - fd) * out[1];
+      out[2] = fd * fb / 65536.0 + (1.0 - fd) * out[2];
+      total = fd + (1.0 - fd) * total;
+      out[3] = fd + (1.0 - fd) * out[3];
+    }
+    if (total > 1.0) total = 1.0;
+    if (out[3] > 1.0) out[3] = 1.0;
+    *opacity = total;
+  }
+}
+
+struct Frame {
+  const mbgb_scene *s;
+  double rm[9];
+  int rzero;
+  Vec start, light;
+  std::vector<Vec> aoDirs;
+};
+
+void setup_frame(const mbgb_scene &s, Frame &f) {
+  f.s = &s;
+  // RotateZ(alpha) * RotateX(beta) * RotateY(gamma), identity short-cut when all zero
+  double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  int zero = 1;
+  auto mulm = [&](const double r[9]) {
+    double o[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) o[3 * i + j] = m[3 * i] * r[j] + m[3 * i + 1] * r[3 + j] + m[3 * i + 2] * r[6 + j];
+    memcpy(m, o, sizeof(o));
+    zero = 0;
+  };
+  if (s.alpha != 0.0) { const double sn = sin(s.alpha), cs = cos(s.alpha); const double r[9] = {cs, -sn, 0, sn, cs, 0, 0, 0, 1}; mulm(r); }
+  if (s.beta != 0.0) { const double sn = sin(s.beta), cs = cos(s.beta); const double r[9] = {1, 0, 0, 0, cs, -sn, 0, sn, cs}; mulm(r); }
+  if (s.gamma != 0.0) { const double sn = sin(s.gamma), cs = cos(s.gamma); const double r[9] = {cs, 0, sn, 0, 1, 0, -sn, 0, cs}; mulm(r); }
+  memcpy(f.rm, m, sizeof(m));
+  f.rzero = zero;
+  const Vec baseY = rot(f.rm, f.rzero, Vec{0.0, 1.0, 0.0});
+  const Vec vp{s.vp[0], s.vp[1], s.vp[2]};
+  if (s.perspectiveType == MBGB_PERSP_FISH_EYE || s.perspectiveType == MBGB_PERSP_EQUIRECT) f.start = vp;
+  else f.start = sub(vp, mul(baseY, 1.0 / s.persp * s.zoom));
+  const Vec lv{cos(s.mainLightAlpha - 0.5 * M_PI) * cos(-s.mainLightBeta),
+               sin(s.mainLightAlpha - 0.5 * M_PI) * cos(-s.mainLightBeta), sin(-s.mainLightBeta)};
+  f.light = rot(f.rm, f.rzero, lv);
+  const int q = s.globalIlumQuality;
+  for (double b = -0.49 * M_PI; b < 0.49 * M_PI; b += 1.0 / q) {
+    for (double a = 0.0; a < 2.0 * M_PI; a += ((2.0 / q) / cos(b))) {
+      f.aoDirs.push_back(Vec{cos(a + b) * cos(b), sin(a + b) * cos(b), sin(b)});
+      if (f.aoDirs.size() >= 10000) break;
+    }
+    if (f.aoDirs.size() >= 10000) break;
+  }
+}
+
+void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jitter, const mbgb_image *img, Cnt &cnt) {
+  const mbgb_scene &s = *f.s;
+  const int W = img->width, H = img->height;
+  const int tiles = s.noOfTiles;
+  const double tx = (s.tileCount % tiles), ty = (s.tileCount / tiles);
+  const double aspect = (double)W / H;
+  const double fov = s.persp;
+  const double x2 = ((double)x / W / tiles - 0.5 + tx / tiles) * aspect;
+  const double z2 = ((double)y / H / tiles - 0.5 + ty / tiles);
+  bool cut = false;
+  Vec v;
+  if (s.perspectiveType == MBGB_PERSP_FISH_EYE) {
+    if (s.fishEyeCut && sqrt(x2 * x2 + z2 * z2) > 0.5 / fov) cut = true;
+    const double x3 = x2 * M_PI, z3 = z2 * M_PI;
+    const double r = sqrt(x3 * x3 + z3 * z3);
+    if (r == 0) v = {0.0, 1.0, 0.0};
+    else v = {x3 / r * sin(r * fov), cos(r * fov), z3 / r * sin(r * fov)};
+    v = normalize(v);
+  } else if (s.perspectiveType == MBGB_PERSP_EQUIRECT) {
+    const double x3 = x2 * M_PI, z3 = z2 * M_PI;
+    v = {sin(fov * x3) * cos(fov * z3), cos(fov * x3) * cos(fov * z3), sin(fov * z3)};
+    v = normalize(v);
+  } else {
+    v = {x2 * fov, 1.0, z2 * fov};
+  }
+  const Vec view = rot(f.rm, f.rzero, v);
+  Calc c{&s, (int)s.N, s.minN, false, 0.0, 0, &cnt};
+  Ray ray{};
+  if (!cut) ray = ray_marching(s, c, f.start, view, buf, jitter, cnt);
+  const int iters = c.itersOut;
+  double out[4] = {0, 0, 0, 0};
+  Vec objColour{0, 0, 0};
+  double depthZ = ray.depth;
+  if (ray.found) {
+    const double thr = ray.thr;
+    c.detail = thr;
+    const double delta = s.constantDEThreshold ? ray.depth * s.resolution * s.persp : thr * s.quality;
+    const Vec n = calculate_normals(s, c, ray.point, delta, thr);
+    double shade = dot(n, f.light);
+    if (shade < 0) shade = 0;
+    const double shadeV = s.directLight * ((1.0 - s.shading) + s.shading * shade);
+    double shadow = 1.0;
+    if (s.shadow) shadow = main_shadow(s, c, ray.point, f.light, thr, delta);
+    Vec half = normalize(sub(f.light, view));
+    double sp = dot(n, half);
+    if (sp < 0.0) sp = 0.0;
+    sp = pow(sp, 30.0) * 1.0;
+    if (sp > 15.0) sp = 15.0;
+    sp *= s.specular;
+    const Vec col = surface_colour(s, c, ray.point);
+    objColour = col;
+    double amb = 0.0;
+    if (s.global_ilumination) {
+      if (s.fastGlobalIllumination) amb = fast_ao(s, c, ray.point, n, thr);
+      else amb = ray_ao(s, c, ray.point, delta, thr, ray.lastDist, f.aoDirs);
+    }
+    const double a2 = amb * s.globalIlum;
+    const double ml[3] = {s.mainLightIntensity * s.mainLightColour.R / 65536.0,
+                          s.mainLightIntensity * s.mainLightColour.G / 65536.0,
+                          s.mainLightIntensity * s.mainLightColour.B / 65536.0};
+    const double cc[3] = {col.x, col.y, col.z};
+    for (int k = 0; k < 3; k++) {
+      const double obj = 0.0 + (a2 + ml[k] * shadeV * shadow) * cc[k];
+      const double spec = 0.0 + ml[k] * sp * shadow;
+      out[k] = obj + 0.0 + spec;
+    }
+    out[3] = 1.0 + 0.0;
+  } else {
+    const Vec bg = background(s, view);
+    out[0] = 0.0 + bg.x + 0.0;
+    out[1] = 0.0 + bg.y + 0.0;
+    out[2] = 0.0 + bg.z + 0.0;
+    out[3] = 0.0;
+    depthZ = 1e20;
+  }
+  float opacity = 0.0f;
+  volumetric(s, buf, ray.count, ray.depth, out, &opacity);
+  const int64_t pix = (int64_t)y * W + x;
+  if (img->opacity) img->opacity[pix] = to_u16((double)opacity * 65535.0);
+  if (img->alpha) img->alpha[pix] = to_u16(out[3] * 65535.0);
+  if (img->image_float) {
+    img->image_float[3 * pix + 0] = (float)out[0];
+    img->image_float[3 * pix + 1] = (float)out[1];
+    img->image_float[3 * pix + 2] = (float)out[2];
+  }
+  if (img->colour) {
+    img->colour[3 * pix + 0] = to_u8(objColour.x * 255);
+    img->colour[3 * pix + 1] = to_u8(objColour.y * 255);
+    img->colour[3 * pix + 2] = to_u8(objColour.z * 255);
+  }
+  if (img->zbuffer) img->zbuffer[pix] = (float)depthZ;
+  if (img->hit) img->hit[pix] = ray.found ? 1 : 0;
+  if (img->iters) img->iters[pix] = iters;
+  if (img->depth) img->depth[pix] = depthZ;
+}
+
+}  // namespace
+
+extern "C" {
+
+// CalculateDistance at points with detailSize = detail[i] (normal DE mode).
+void oracle_distance(const mbgb_scene *s, const double *pts, const double *detail, long n, double *dist, int *iters,
+                     unsigned char *max_iter) {
+  Cnt cnt;
+  Calc c{s, (int)s->N, s->minN, false, 0.0, -1, &cnt};
+  for (long i = 0; i < n; i++) {
+    c.detail = detail[i];
+    c.itersOut = -1;
+    bool mi = false;
+    dist[i] = calculate_distance(c, Vec{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]}, &mi);
+    iters[i] = c.itersOut;
+    max_iter[i] = mi ? 1 : 0;
+  }
+}
+
+// Compute<colouring> with N x 10, as SurfaceColour calls it.
+void oracle_colour_value(const mbgb_scene *s, const double *pts, long n, double *out) {
+  Cnt cnt;
+  Calc c{s, (int)(s->N * 10), s->minN, false, 0.0, 0, &cnt};
+  for (long i = 0; i < n; i++) out[i] = compute(c, Vec{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]}, true, nullptr);
+}
+
+// Renders rows [row0, row1) with `threads` workers pulling rows from a shared
+// counter (the reference's one-worker-per-core row claiming). jitter != 0 uses
+// the C library's shared rand() stream, as the reference does.
+// counters (may be NULL): [0] orbit iterations, [1] DE calls, [2] march steps.
+int oracle_render(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
+                  unsigned long long *counters) {
+  if (!s || !img || row0 < 0 || row1 > img->height || row0 > row1) return 1;
+  Frame f;
+  setup_frame(*s, f);
+  if (threads < 1) threads = 1;
+  std::atomic<int> next(row0);
+  std::vector<Cnt> cnts(threads);
+  auto worker = [&](int t) {
+    std::vector<Step> buf(10002);
+    for (;;) {
+      const int y = next.fetch_add(1);
+      if (y >= row1) break;
+      for (int x = 0; x < img->width; x++) render_pixel(f, x, y, buf, jitter != 0, img, cnts[t]);
+    }
+  };
+  if (threads == 1) {
+    worker(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++) pool.emplace_back(worker, t);
+    for (auto &th : pool) th.join();
+  }
+  if (counters) {
+    counters[0] = counters[1] = counters[2] = 0;
+    for (const Cnt &c : cnts) {
+      counters[0] += c.orbit;
+      counters[1] += c.calls;
+      counters[2] += c.steps;
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+"""Generates the golden vectors under tests/golden/ from the reference's OWN code.
+
+Runs in a container that has the reference tree: builds oracle/_ref/libmbref.so
+(the reference's src/fractal.cpp, src/shaders.cpp, src/algebra.cpp,
+src/common_math.cpp, src/primitives.cpp compiled in place, plus
+oracle/ref_harness.cpp) and records, for seeded inputs:
+  * de_<formula>.npz      CalculateDistance (distance, itersOut, max_iter) and the
+                          Compute<colouring> value SurfaceColour uses, at seeded points;
+  * render_<case>.npz     every cImage layer of the MainThread pixel body (jitter off)
+                          for small frames covering the shading features.
+Each file also stores the scene as raw mbgb_scene bytes and its settings keys, so
+the tests rebuild the exact input without the reference tree.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import mandelbulber_gb300 as mb  # noqa: E402
+from mandelbulber_gb300 import workloads as W  # noqa: E402
+
+# Small frames covering the hot-path features; the keys are applied on top of a workload.
+CASES = {
+    "mandelbulb_64x48": ("mandelbulb_640x480", 64, 48, {}),
+    "mandelbox_96x54": ("mandelbox_1080p", 96, 54, {}),
+    "mandelbulb_soft_penetrating": ("mandelbulb_640x480", 40, 32,
+                                    {"shadows_cone_angle": 1.0, "penetrating_lights": 1, "glow_intensity": 1}),
+    "mandelbulb_fastao_postfog": ("mandelbulb_640x480", 40, 32,
+                                  {"ambient_occlusion_enabled": 1, "fast_ambient_occlusion_mode": 1,
+                                   "ambient_occlusion_quality": 4, "post_fog_enabled": 1,
+                                   "post_fog_visibility": 160}),
+    "mandelbulb_rayao_q1": ("mandelbulb_640x480", 32, 32,
+                            {"ambient_occlusion_enabled": 1, "fast_ambient_occlusion_mode": 0,
+                             "ambient_occlusion_quality": 1}),
+    "mandelbulb_julia_limits": ("mandelbulb_640x480", 40, 32,
+                                {"julia_mode": 1, "julia_a": 0.2, "julia_b": -0.4, "julia_c": 0.1,
+                                 "limits_enabled": 1, "z_max": 0.4}),
+    "mandelbulb_power6_rotated": ("mandelbulb_640x480", 40, 32,
+                                  {"power": 6, "angle_alfa": 30, "angle_beta": 19, "angle_gamma": 10,
+                                   "view_point_x": 1.75, "view_point_y": -3.0, "view_point_z": -1.2}),
+    "mandelbox_rotated_interior": ("mandelbox_1080p", 56, 32,
+                                   {"mandelbox_rotation_enabled": 1, "mandelbox_rotation_X1_alfa": 10,
+                                    "mandelbox_rotation_Y2_beta": -15, "mandelbox_rotation_main_gamma": 5,
+                                    "ambient_occlusion_enabled": 0, "interior_mode": 0}),
+    "mandelbulb_interior": ("mandelbulb_640x480", 32, 32,
+                            {"interior_mode": 1, "view_point_y": -1.0, "N": 40, "glow_intensity": 1}),
+    "mandelbox_fog_colours": ("mandelbox_1080p", 56, 32,
+                              {"volumetric_fog_density": 2.0, "volumetric_fog_colour_1_distance": 0.3,
+                               "volumetric_fog_colour_2_distance": 0.8, "volumetric_fog_distance_factor": 0.5,
+                               "ambient_occlusion_enabled": 0}),
+    "mandelbox_constant_threshold_minN": ("mandelbox_1080p", 48, 32,
+                                          {"constant_DE_threshold": 1, "quality": 0.002, "minN": 3,
+                                           "ambient_occlusion_enabled": 1, "fast_ambient_occlusion_mode": 1,
+                                           "ambient_occlusion_quality": 3}),
+    "mandelbulb_tiles_equirect": ("mandelbulb_640x480", 32, 32,
+                                  {"tiles": 2, "tile_no": 3, "fish_eye": 2, "perspective": 0.8}),
+    "mandelbulb_fisheye_cut": ("mandelbulb_640x480", 32, 32,
+                               {"fish_eye": 1, "fish_eye_180cut": 1, "perspective": 1.2}),
+    "mandelbulb_prefolds_iterthresh": ("mandelbulb_640x480", 32, 32,
+                                       {"tglad_folding_mode": 1, "spherical_folding_mode": 1,
+                                        "iteration_threshold_mode": 1, "N": 60}),
+}
+
+
+def build_ref() -> ctypes.CDLL:
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libmbref.so"))
+    return lib
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def de_points(formula: str, rng: np.random.Generator):
+    """Seeded points: a uniform cube plus points near the surface along camera rays."""
+    if formula == "mandelbulb":
+        cube = rng.uniform(-1.6, 1.6, (2000, 3))
+    else:
+        cube = rng.uniform(-7.0, 7.0, (2000, 3))
+    return cube
+
+
+def main():
+    lib = build_ref()
+    manifest = {}
+    for formula, wl in (("mandelbulb", "mandelbulb_640x480"), ("mandelbox", "mandelbox_1080p")):
+        rng = np.random.default_rng(1234 if formula == "mandelbulb" else 5678)
+        sc = W.workload(wl, 64, 48)
+        pts = np.ascontiguousarray(de_points(formula, rng))
+        n = len(pts)
+        detail = np.ascontiguousarray(10.0 ** rng.uniform(-6, -2, n))
+        dist = np.zeros(n)
+        iters = np.zeros(n, np.int32)
+        mi = np.zeros(n, np.uint8)
+        lib.ref_distance(ctypes.byref(sc), ptr(pts), ptr(detail), ctypes.c_long(n), ptr(dist), ptr(iters), ptr(mi))
+        colour = np.zeros(n)
+        lib.ref_colour_value(ctypes.byref(sc), ptr(pts), ctypes.c_long(n), ptr(colour))
+        out = os.path.join(HERE, f"de_{formula}.npz")
+        np.savez_compressed(out, scene=np.frombuffer(mb.scene_bytes(sc), np.uint8), points=pts, detail=detail,
+                            dist=dist, iters=iters, max_iter=mi, colour=colour)
+        manifest[os.path.basename(out)] = {"workload": wl, "points": n}
+    for case, (wl, w, h, extra) in CASES.items():
+        keys = dict(W.WORKLOADS[wl])
+        keys["image_width"], keys["image_height"] = w, h
+        keys["perspective"] = W.fov_persp(w, h)
+        keys.update(extra)
+        sc = W.make_scene(keys)
+        img = mb.CImage.empty(w, h)
+        lib.ref_render(ctypes.byref(sc), 0, h, 0, ctypes.byref(img.as_c()))
+        out = os.path.join(HERE, f"render_{case}.npz")
+        np.savez_compressed(out, scene=np.frombuffer(mb.scene_bytes(sc), np.uint8),
+                            keys=np.array(json.dumps(keys)), image_float=img.image_float, zbuffer=img.zbuffer,
+                            alpha=img.alpha, opacity=img.opacity, colour=img.colour, hit=img.hit, iters=img.iters,
+                            depth=img.depth)
+        manifest[os.path.basename(out)] = {"workload": wl, "size": [w, h], "keys": extra,
+                                           "hit_fraction": float(img.hit.mean())}
+        print(case, "hit", img.hit.mean())
+    with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

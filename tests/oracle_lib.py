@@ -1,0 +1,68 @@
+"""Loads the CPU oracle (oracle/mb_oracle.cpp) for the tests — test infrastructure only."""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+_cache = {}
+
+
+def load(fast: bool = False) -> ctypes.CDLL:
+    key = "fast" if fast else "strict"
+    if key in _cache:
+        return _cache[key]
+    name = "libmboracle_fast.so" if fast else "libmboracle.so"
+    path = os.path.join(ORACLE_DIR, "_build", name)
+    subprocess.check_call(["make", "-s", "-C", ORACLE_DIR, "all"])
+    lib = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    lib.oracle_distance.argtypes = [vp, vp, vp, ctypes.c_long, vp, vp, vp]
+    lib.oracle_distance.restype = None
+    lib.oracle_colour_value.argtypes = [vp, vp, ctypes.c_long, vp]
+    lib.oracle_colour_value.restype = None
+    lib.oracle_render.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
+    lib.oracle_render.restype = ctypes.c_int
+    _cache[key] = lib
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def distance(lib, scene, points: np.ndarray, detail: np.ndarray):
+    pts = np.ascontiguousarray(points, np.float64)
+    det = np.ascontiguousarray(detail, np.float64)
+    n = len(pts)
+    d = np.zeros(n)
+    it = np.zeros(n, np.int32)
+    mi = np.zeros(n, np.uint8)
+    lib.oracle_distance(ctypes.addressof(scene), _p(pts), _p(det), n, _p(d), _p(it), _p(mi))
+    return d, it, mi
+
+
+def colour_value(lib, scene, points: np.ndarray):
+    pts = np.ascontiguousarray(points, np.float64)
+    out = np.zeros(len(pts))
+    lib.oracle_colour_value(ctypes.addressof(scene), _p(pts), len(pts), _p(out))
+    return out
+
+
+def render(lib, scene, rows=None, jitter=False, threads=None):
+    """Renders the scene on the CPU; returns (CImage, counters)."""
+    import mandelbulber_gb300 as mb
+    w, h = scene.image_width, scene.image_height
+    img = mb.CImage.empty(w, h)
+    r0, r1 = rows if rows else (0, h)
+    cnt = np.zeros(3, np.uint64)
+    c = img.as_c()
+    rc = lib.oracle_render(ctypes.addressof(scene), r0, r1, int(jitter), threads or os.cpu_count() or 1,
+                           ctypes.addressof(c), _p(cnt))
+    if rc != 0:
+        raise RuntimeError("oracle_render rejected its arguments")
+    return img, cnt
