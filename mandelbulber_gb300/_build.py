@@ -19,6 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libmbgb.so")
+PEAK_LIB = os.path.join(PKG, "libmbgb_peak.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -83,6 +84,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # ALU peak microbenchmark (bench.py's roofline denominator), a separate tool library
+    peak = [os.path.join(cuda, "bin", "nvcc"), "-std=c++17", "-O3", *ARCH, "-shared", "-Xcompiler", "-fPIC",
+            "-o", PEAK_LIB, os.path.join(CSRC, "peak.cu"), "-cudart", "static"]
+    r = subprocess.run(peak, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"peak tool build failed: {' '.join(peak)}\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -299,6 +299,9 @@ struct RayState {
 };
 
 constexpr double kPI = 3.14159265358979323846;
+// Upper bound of one shadow or AO march; the reference's loops have none, but a
+// float accumulator can stop advancing, and every device loop here must end.
+constexpr int kMaxSecondarySteps = 1 << 20;
 
 // ---------------------------------------------------------------------------
 // RayMarching march loop (src/Render3D.cpp:79-143) in precision T.
@@ -479,7 +482,9 @@ __device__ __forceinline__ T main_shadow(const ParamsT<T> &p, const V3<T> point,
       if (shadowTemp < T(0)) shadowTemp = T(0);
       break;
     }
-    if ((++guard & 1023) == 0 && deadline_passed(io)) {
+    // hard bound: in FP32 `i += dist` could stop advancing when dist falls below ulp(i)
+    if (++guard >= kMaxSecondarySteps) break;
+    if ((guard & 1023) == 0 && deadline_passed(io)) {
       atomicExch(io.error_flag, 1);
       break;
     }
@@ -522,7 +527,8 @@ __device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, 
     const V3<T> dir{__ldg(&p.aoVec[3 * v + 0]), __ldg(&p.aoVec[3 * v + 1]), __ldg(&p.aoVec[3 * v + 2])};
     T dist = lastDist;
     T shadowTemp = T(1);
-    for (T r = start_dist; r < end_dist; r += dist * T(2)) {
+    int guard = 0;
+    for (T r = start_dist; r < end_dist && guard < kMaxSecondarySteps; r += dist * T(2), guard++) {
       const V3<T> point2 = point + dir * r;
       int L;
       bool mi;

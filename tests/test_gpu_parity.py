@@ -1,0 +1,174 @@
+"""Device kernels against the oracle and the golden vectors (needs a GPU).
+
+Tolerances (stated per test):
+  * FP64 policy, Mandelbox: only + - * / sqrt on the orbit and the march, the
+    kernel is built with --fmad=false, so hit mask, depth, iterations, z-buffer,
+    alpha, opacity and colour are bit-exact; the float image differs from the
+    CPU only through pow() in the specular term (|diff| <= 1e-6).
+  * FP64 policy, Mandelbulb: asin/atan2/pow/sincos/log come from CUDA's libm,
+    which may round differently from the CPU's in the last ulp, and the orbit is
+    chaotic, so a few pixels may flip: hit mismatch <= 0.5 %, iteration agreement
+    >= 90 % and PSNR >= 35 dB on the 32x32 .. 64x48 golden frames (one flipped
+    pixel of a 32x32 frame alone costs several dB).
+  * FP32 + FP64-refinement policy: hit/miss mismatch <= 0.1 % and PSNR >= 45 dB
+    of the float image against the FP64 oracle (the spec bar), at sizes the
+    oracle finishes in seconds.
+"""
+import ctypes
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import mandelbulber_gb300 as mb
+from mandelbulber_gb300 import workloads as W
+from tests import metrics, oracle_lib
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+RENDERS = sorted(os.path.basename(p)[7:-4] for p in glob.glob(os.path.join(GOLDEN, "render_*.npz")))
+LAYERS = ["image_float", "zbuffer", "alpha", "opacity", "colour", "hit", "iters", "depth"]
+
+
+def _golden_image(z, w, h):
+    img = mb.CImage.empty(w, h)
+    for k in LAYERS:
+        setattr(img, k, z[k])
+    return img
+
+
+def _device_distance(ctx, scene, pts, detail, precision):
+    import torch
+    n = len(pts)
+    p = torch.tensor(pts, dtype=torch.float64, device="cuda")
+    d = torch.tensor(detail, dtype=torch.float64, device="cuda")
+    dist = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it = torch.zeros(n, dtype=torch.int32, device="cuda")
+    mi = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    ctx.distance(scene, p.data_ptr(), d.data_ptr(), n, dist.data_ptr(), it.data_ptr(), mi.data_ptr(), precision)
+    torch.cuda.synchronize()
+    return dist.cpu().numpy(), it.cpu().numpy(), mi.cpu().numpy()
+
+
+def test_distance_fp64_mandelbox_bit_exact(gpu_ctx):
+    z = np.load(os.path.join(GOLDEN, "de_mandelbox.npz"))
+    sc = mb.scene_from_bytes(z["scene"].tobytes())
+    d, it, mi = _device_distance(gpu_ctx, sc, z["points"], z["detail"], mb.PREC_FP64)
+    np.testing.assert_array_equal(d, z["dist"])
+    np.testing.assert_array_equal(it, z["iters"])
+    np.testing.assert_array_equal(mi, z["max_iter"])
+
+
+def test_distance_fp64_mandelbulb_close(gpu_ctx):
+    z = np.load(os.path.join(GOLDEN, "de_mandelbulb.npz"))
+    sc = mb.scene_from_bytes(z["scene"].tobytes())
+    d, it, mi = _device_distance(gpu_ctx, sc, z["points"], z["detail"], mb.PREC_FP64)
+    agree = it == z["iters"]
+    assert agree.mean() >= 0.98, agree.mean()
+    rel = np.abs(d[agree] - z["dist"][agree]) / np.maximum(np.abs(z["dist"][agree]), 1e-300)
+    assert np.percentile(rel, 99) < 1e-9, np.percentile(rel, 99)
+
+
+@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox"])
+def test_distance_fp32_close(gpu_ctx, formula):
+    z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
+    sc = mb.scene_from_bytes(z["scene"].tobytes())
+    d, it, mi = _device_distance(gpu_ctx, sc, z["points"], z["detail"], mb.PREC_FP32_FIX)
+    agree = it == z["iters"]
+    assert agree.mean() >= 0.9, agree.mean()
+    far = agree & (z["dist"] > 1e-3)
+    rel = np.abs(d[far] - z["dist"][far]) / z["dist"][far]
+    assert np.median(rel) < 1e-4, np.median(rel)
+
+
+@pytest.mark.parametrize("case", RENDERS)
+def test_render_fp64_against_reference_golden(gpu_ctx, case):
+    """FP64 device render vs the reference's own output (golden vectors)."""
+    z = np.load(os.path.join(GOLDEN, f"render_{case}.npz"))
+    sc = mb.scene_from_bytes(z["scene"].tobytes())
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    ref = _golden_image(z, sc.image_width, sc.image_height)
+    m = metrics.compare(img, ref)
+    if sc.formula == 8 and sc.perspectiveType == 0:
+        for k in ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]:
+            np.testing.assert_array_equal(getattr(img, k), z[k], err_msg=f"{case}: {k}")
+        np.testing.assert_allclose(img.image_float, z["image_float"], rtol=0, atol=1e-6)
+    else:
+        assert m["hit_mismatch"] <= 0.005, m
+        if "iters_agree" in m:
+            assert m["iters_agree"] >= 0.90, m
+        assert m["psnr_float"] >= 35.0, m
+
+
+@pytest.mark.parametrize("name,size", [("mandelbulb_640x480", (320, 240)), ("mandelbox_1080p", (480, 270))])
+def test_render_fp32_fix_against_oracle(gpu_ctx, oracle, name, size):
+    """FP32 march + FP64 refinement vs the FP64 oracle: <= 0.1 % hit mismatch, >= 45 dB."""
+    sc = W.workload(name, *size)
+    ref, _ = oracle_lib.render(oracle, sc)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    m = metrics.compare(img, ref)
+    print(name, m)
+    assert m["hit_mismatch"] <= 0.001, m
+    assert m["psnr_float"] >= 45.0, m
+
+
+def test_full_size_fp32_fix_against_fp64(gpu_ctx):
+    """At the full 1080p size: FP32+fix vs the FP64 device path (the oracle is too slow there)."""
+    sc = W.workload("mandelbox_1080p")
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    b = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    m = metrics.compare(a, b)
+    print(m)
+    assert m["hit_mismatch"] <= 0.001, m
+    assert m["psnr_float"] >= 45.0, m
+
+
+def test_render_is_deterministic_and_row_ranges_compose(gpu_ctx):
+    sc = W.workload("mandelbox_1080p", 320, 180)
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    b = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    for k in LAYERS:
+        np.testing.assert_array_equal(getattr(a, k), getattr(b, k))
+    c = mb.CImage.empty(320, 180)
+    gpu_ctx.render(sc, c, precision=mb.PREC_FP32_FIX, rows=(0, 77))
+    gpu_ctx.render(sc, c, precision=mb.PREC_FP32_FIX, rows=(77, 180))
+    np.testing.assert_array_equal(c.image_float, a.image_float)
+
+
+def test_jitter_changes_steps_but_not_the_picture(gpu_ctx):
+    """Step jitter (the reference's Random(1000) factor) perturbs the march only slightly."""
+    sc = W.workload("mandelbox_1080p", 320, 180)
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    b = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, jitter=True, jitter_seed=7)
+    m = metrics.compare(b, a)
+    assert m["hit_mismatch"] <= 0.01 and m["psnr_float"] >= 30.0, m
+    assert not np.array_equal(a.depth, b.depth)
+
+
+def test_errors_are_status_codes(gpu_ctx):
+    sc = W.workload("mandelbulb_640x480", 64, 48, formula=7)
+    with pytest.raises(mb.MbgbError) as e:
+        gpu_ctx.render(sc)
+    assert e.value.status == 5
+    sc = W.workload("mandelbulb_640x480", 64, 48)
+    with pytest.raises(mb.MbgbError) as e:
+        gpu_ctx.render(sc, mb.CImage.empty(32, 32))
+    assert e.value.status == 1
+    with pytest.raises(mb.MbgbError) as e:
+        gpu_ctx.render(sc, rows=(40, 10))
+    assert e.value.status == 1
+    with pytest.raises(mb.MbgbError) as e:
+        gpu_ctx.render(sc, precision=9)
+    assert e.value.status == 1
+
+
+def test_device_deadline_returns_timeout_and_context_survives(gpu_ctx):
+    """A 1 ms device budget on a full frame stops the kernel early with MBGB_ERR_TIMEOUT."""
+    sc = W.workload("mandelbox_1080p")
+    with pytest.raises(mb.MbgbError) as e:
+        gpu_ctx.render(sc, precision=mb.PREC_FP64, deadline_ms=1)
+    assert e.value.status == 4
+    small = W.workload("mandelbox_1080p", 64, 36)
+    img = gpu_ctx.render(small, precision=mb.PREC_FP32_FIX)
+    assert img.hit.mean() > 0.5
