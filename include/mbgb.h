@@ -209,6 +209,7 @@ typedef struct mbgb_stats {
   uint64_t primary_steps;      /* DE_counter */
   uint64_t pixels;             /* Pixel_counter */
   uint64_t missed_de;          /* Missed_DE_counter */
+  uint64_t long_rays;          /* primary rays longer than the main pass's step records (re-rendered) */
   double kernel_ms;            /* device time of the last render */
 } mbgb_stats;
 

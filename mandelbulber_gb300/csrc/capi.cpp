@@ -276,7 +276,9 @@ struct mbgb_context {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;
-  DeviceBuf step[2][3];          // [precision][step, dist, thr]
+  DeviceBuf step[2][3];          // [precision][step, dist, thr], kStepCap records per slot
+  DeviceBuf ovstep[2][3];        // overflow pass: kStepSlots records per slot, kOverflowThreads slots
+  DeviceBuf ovlist;              // overflow pixel list
   DeviceBuf control;              // tile counter, error flag, counters
   DeviceBuf ao64, ao32;
   int ao_quality = -1;
@@ -350,6 +352,9 @@ extern "C" void mbgb_context_destroy(mbgb_context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto &a : c->step)
     for (auto &b : a) b.release();
+  for (auto &a : c->ovstep)
+    for (auto &b : a) b.release();
+  c->ovlist.release();
   c->control.release();
   c->ao64.release();
   c->ao32.release();
@@ -417,18 +422,27 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   io.iters = img->iters;
   io.depth = img->depth;
   io.slots = slots;
+  io.step_cap = kStepCap;
+  io.overflow_pass = 0;
   const bool needVol = (scene->glow_intensity != 0.0) || scene->fogEnabled || (scene->fogDensity > 0.0);
+  const size_t esz = prec == 0 ? sizeof(double) : sizeof(float);
   if (needVol) {
-    const size_t esz = prec == 0 ? sizeof(double) : sizeof(float);
-    const size_t bytes = (size_t)kStepSlots * (size_t)slots * esz;
-    for (int k = 0; k < 3; k++) MBGB_CUDA(c->step[prec][k].ensure(bytes));
+    const size_t bytes = (size_t)kStepCap * (size_t)slots * esz;
+    const size_t obytes = (size_t)kStepSlots * (size_t)kOverflowThreads * esz;
+    for (int k = 0; k < 3; k++) {
+      MBGB_CUDA(c->step[prec][k].ensure(bytes));
+      MBGB_CUDA(c->ovstep[prec][k].ensure(obytes));
+    }
+    MBGB_CUDA(c->ovlist.ensure((size_t)scene->image_width * scene->image_height * sizeof(unsigned int)));
     io.step_step = c->step[prec][0].ptr;
     io.step_dist = c->step[prec][1].ptr;
     io.step_thr = c->step[prec][2].ptr;
+    io.overflow_list = (unsigned int *)c->ovlist.ptr;
   }
   MBGB_CUDA(c->control.ensure(256));
   char *ctl = (char *)c->control.ptr;
   io.tile_counter = (unsigned int *)(ctl + 0);
+  io.overflow_count = (unsigned int *)(ctl + 4);
   io.error_flag = (int *)(ctl + 16);
   io.counters = (unsigned long long *)(ctl + 64);
   io.start_ns = (unsigned long long *)(ctl + 32);
@@ -438,14 +452,25 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   fill_fractal<double>(*scene, fd);
   MBGB_CUDA(cudaEventRecord(c->ev0, s));
   cudaError_t e;
+  // main pass, then (when the step buffer is in use) the overflow pass for rays longer than kStepCap
+  FrameIO ov = io;
+  ov.overflow_pass = 1;
+  ov.step_cap = kStepSlots;
+  ov.slots = kOverflowThreads;
+  ov.step_step = c->ovstep[prec][0].ptr;
+  ov.step_dist = c->ovstep[prec][1].ptr;
+  ov.step_thr = c->ovstep[prec][2].ptr;
+  const int ovBlocks = kOverflowThreads / block > 0 ? kOverflowThreads / block : 1;
   if (prec == 0) {
     ParamsT<double> p;
     fill_params<double>(*scene, p, o, (const double *)c->ao64.ptr, c->ao_count);
     e = launch_render_f64(scene->formula, p, fd, io, grid, block, s);
+    if (e == cudaSuccess && needVol) e = launch_render_f64(scene->formula, p, fd, ov, ovBlocks, block, s);
   } else {
     ParamsT<float> p;
     fill_params<float>(*scene, p, o, (const float *)c->ao32.ptr, c->ao_count);
     e = launch_render_f32(scene->formula, p, fd, io, grid, block, s);
+    if (e == cudaSuccess && needVol) e = launch_render_f32(scene->formula, p, fd, ov, ovBlocks, block, s);
   }
   if (e != cudaSuccess) return cuda_error(e, "render kernel launch");
   MBGB_CUDA(cudaEventRecord(c->ev1, s));
@@ -453,8 +478,11 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
     MBGB_CUDA(cudaStreamSynchronize(s));
     unsigned long long cnt[4];
     int flag = 0;
+    unsigned int nover = 0;
     MBGB_CUDA(cudaMemcpy(cnt, ctl + 64, sizeof(cnt), cudaMemcpyDeviceToHost));
     MBGB_CUDA(cudaMemcpy(&flag, ctl + 16, sizeof(flag), cudaMemcpyDeviceToHost));
+    MBGB_CUDA(cudaMemcpy(&nover, ctl + 4, sizeof(nover), cudaMemcpyDeviceToHost));
+    c->stats.long_rays = nover;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.orbit_iterations = cnt[0];

@@ -14,6 +14,8 @@ namespace mbgb {
 
 constexpr int kMaxMarchSteps = 10000;   // RayMarching loop bound (src/Render3D.cpp:94)
 constexpr int kStepSlots = 10002;       // sStep buffer length per ray (src/Render3D.cpp:267)
+constexpr int kStepCap = 1024;          // step records per thread slot in the main pass
+constexpr int kOverflowThreads = 128;   // threads of the pass that re-renders rays longer than kStepCap
 constexpr int kMaxAOVectors = 10000;    // sVectorsAround table (src/Render3D.cpp:272)
 constexpr int kTileW = 8, kTileH = 4;   // one warp renders an 8x4 pixel tile
 
@@ -94,9 +96,16 @@ struct FrameIO {
   int32_t *iters;
   double *depth;
   // Scratch: per resident thread, the primary ray's step records (sStep,
-  // src/Render3D.h:32-39): step, distance and threshold, each [kStepSlots][slots].
+  // src/Render3D.h:32-39): step, distance and threshold, each [step_cap][slots].
+  // A ray that needs more than step_cap records is appended to the overflow
+  // list; the overflow pass (overflow_pass = 1) re-renders those pixels with
+  // step_cap = kStepSlots and its own, smaller slot set.
   void *step_step, *step_dist, *step_thr;
   int64_t slots;
+  int step_cap;
+  int overflow_pass;
+  unsigned int *overflow_count;   // zeroed before the main pass
+  unsigned int *overflow_list;    // pixel indices, capacity = pixels of the frame
   unsigned int *tile_counter;     // zeroed before the launch
   unsigned long long *counters;   // [0] orbit iterations, [1] DE calls, [2] primary steps, [3] missed DE
   int *error_flag;                // set to 1 when the device deadline expires

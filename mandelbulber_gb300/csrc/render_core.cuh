@@ -292,6 +292,7 @@ struct StepBuf {
 // Per-pixel march state handed from the march to the shaders.
 struct RayState {
   bool found;
+  bool overflow;   // the march needed more step records than the slot holds
   int buffCount;
   int iters;
   double scan, step, dist, distThresh, detail;
@@ -308,7 +309,7 @@ constexpr int kMaxSecondarySteps = 1 << 20;
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA>
 __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, const V3<T> dir, const uint32_t pixel,
-                                      const StepBuf<T> &sb, RayState &rs, Counters &cnt) {
+                                      const StepBuf<T> &sb, const int stepCap, RayState &rs, Counters &cnt) {
   T scan = p.viewDistanceMin;
   T distThresh = T(0);  // *distThreshOut is 0.0 for the primary ray (src/Render3D.cpp:443)
   const T distThreshInit = T(0);
@@ -321,7 +322,12 @@ __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, co
   const bool useSB = p.needVolumetric;
   const T thrScale = p.resolution * p.persp / p.quality;
   const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
+  rs.overflow = false;
   for (int i = 0; i < kMaxMarchSteps; i++) {
+    if (useSB && i >= stepCap) {
+      rs.overflow = true;  // re-rendered by the overflow pass with full-length records
+      return;
+    }
     counter++;
     const V3<T> point = start + dir * scan;
     if (p.constantDEThreshold) {
@@ -687,7 +693,8 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA>
 __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT<double> &fd, const FrameIO &io,
-                                             const int x, const int y, const StepBuf<T> &sb, Counters &cnt) {
+                                             const int x, const int y, const StepBuf<T> &sb, const int stepCap,
+                                             Counters &cnt) {
   const int64_t pix = (int64_t)y * p.width + x;
   // view vector (src/Render3D.cpp:389-438)
   const double x2 = ((double)x / p.width / p.tiles - 0.5 + p.tileXOffset / p.tiles) * p.aspect;
@@ -724,6 +731,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
 
   RayState rs;
   rs.found = false;
+  rs.overflow = false;
   rs.buffCount = 0;
   rs.iters = 0;
   rs.distThresh = 0.0;
@@ -731,7 +739,12 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
   rs.scan = 0.0;
   rs.point[0] = rs.point[1] = rs.point[2] = 0.0;
   if (!hemisphereCut) {
-    march<T, FORMULA>(p, startT, viewT, (uint32_t)pix, sb, rs, cnt);
+    march<T, FORMULA>(p, startT, viewT, (uint32_t)pix, sb, stepCap, rs, cnt);
+    if (rs.overflow) {
+      const unsigned int k = atomicAdd(io.overflow_count, 1u);
+      io.overflow_list[k] = (unsigned int)pix;
+      return;
+    }
     if (rs.found) refine<T, FORMULA>(p, fd, startD, view, rs, cnt);
   }
 
@@ -829,6 +842,15 @@ __global__ void __launch_bounds__(128) render_kernel(const ParamsT<T> p, const F
   const int tilesX = (p.width + kTileW - 1) / kTileW;
   const int rowTiles = (p.row_end - p.row_begin + kTileH - 1) / kTileH;
   const unsigned int nTiles = (unsigned int)(tilesX * rowTiles);
+  if (io.overflow_pass) {
+    // rays longer than the main pass's step_cap, one pixel per thread, full-length records
+    const unsigned int n = *io.overflow_count;
+    for (unsigned int k = (unsigned int)slot; k < n; k += (unsigned int)(gridDim.x * blockDim.x)) {
+      const unsigned int pix = io.overflow_list[k];
+      render_pixel<T, FORMULA>(p, fd, io, (int)(pix % (unsigned int)p.width), (int)(pix / (unsigned int)p.width), sb,
+                               kStepSlots, cnt);
+    }
+  } else
   for (;;) {
     unsigned int t = 0;
     int stop = 0;
@@ -844,7 +866,7 @@ __global__ void __launch_bounds__(128) render_kernel(const ParamsT<T> p, const F
     const int ty = (int)(t / (unsigned int)tilesX);
     const int x = tx * kTileW + (lane % kTileW);
     const int y = p.row_begin + ty * kTileH + (lane / kTileW);
-    if (x < p.width && y < p.row_end) render_pixel<T, FORMULA>(p, fd, io, x, y, sb, cnt);
+    if (x < p.width && y < p.row_end) render_pixel<T, FORMULA>(p, fd, io, x, y, sb, io.step_cap, cnt);
   }
   // one atomic per warp for the counters
   for (int off = 16; off > 0; off >>= 1) {

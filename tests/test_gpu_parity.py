@@ -124,6 +124,17 @@ def test_full_size_fp32_fix_against_fp64(gpu_ctx):
     assert m["psnr_float"] >= 45.0, m
 
 
+def test_long_rays_take_the_overflow_pass(gpu_ctx, oracle):
+    """Rays longer than the main pass's step records are re-rendered with full-length records."""
+    sc = W.workload("mandelbox_1080p", 96, 54, DE_factor=0.01)
+    ref, _ = oracle_lib.render(oracle, sc)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    assert gpu_ctx.stats().long_rays > 0
+    for k in ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]:
+        np.testing.assert_array_equal(getattr(img, k), getattr(ref, k), err_msg=k)
+    np.testing.assert_allclose(img.image_float, ref.image_float, rtol=0, atol=1e-6)
+
+
 def test_render_is_deterministic_and_row_ranges_compose(gpu_ctx):
     sc = W.workload("mandelbox_1080p", 320, 180)
     a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
