@@ -256,6 +256,23 @@ mbgb_status mbgb_render_device(mbgb_context *ctx, const mbgb_scene *scene,
 mbgb_status mbgb_render_host(mbgb_context *ctx, const mbgb_scene *scene,
                              const mbgb_image *out, const mbgb_opts *opts);
 
+/* Allocation-free render (no counterpart in the reference): the FP32_FIX render of
+ * mbgb_render_device for callers that cannot allocate device memory while they
+ * render — an application whose memory manager has already reserved the GPU for its
+ * own pool, a plugin inside such a host, or a frame loop that must not call
+ * cudaMalloc/cudaFree because they synchronise the device. It needs no context and
+ * calls no allocator: its scratch is a set of static device arrays (79.4 MB in total)
+ * that every GPU loading this library holds until the process exits. `out` holds
+ * device pointers; the render runs on the current device and on opts->stream
+ * (NULL = the legacy default stream, and the call then waits for the frame and
+ * reports a device-deadline timeout). Limits: precision MBGB_PREC_FP32_FIX (or
+ * MBGB_PREC_AUTO) only; at most 4194304 pixels (e.g. 2048 x 2048), larger frames are
+ * rejected with MBGB_ERR_BAD_PARAM. The first call on a device resolves the arrays'
+ * device addresses, so make that first call before any stream capture. All calls
+ * share the arrays: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
+mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const mbgb_image *out, const mbgb_opts *opts);
+
 /* Distance estimate at points (CalculateDistance, src/fractal.cpp:1245-1448) with
  * detailSize = detail[i]; writes dist[i], iters[i] (itersOut) and max_iter[i].
  * All pointers are device pointers. precision: MBGB_PREC_FP64 or MBGB_PREC_FP32_FIX (float orbit). */

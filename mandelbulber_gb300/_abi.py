@@ -103,6 +103,7 @@ FUNCTIONS = {
     "mbgb_get_stats": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_stats)]),
     "mbgb_render_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), _P(mbgb_opts)]),
     "mbgb_render_host": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), _P(mbgb_opts)]),
+    "mbgb_render_device_noalloc": (ctypes.c_int, [_P(mbgb_scene), _P(mbgb_image), _P(mbgb_opts)]),
     "mbgb_distance_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p]),

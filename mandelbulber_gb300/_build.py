@@ -41,6 +41,7 @@ def _units(cuda: str):
                   "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(cuda, "include")]
     yield "render_f64.cu", common_cu + ["--fmad=false"]
     yield "render_f32.cu", common_cu
+    yield "noalloc.cu", common_cu
     yield "capi.cpp", common_cpp
     yield "settings.cpp", common_cpp
 

@@ -268,6 +268,33 @@ struct DeviceBuf {
   }
 };
 
+// Parameter blocks of the FP32 render kernel for one frame, written into caller
+// storage (used by the allocation-free entry point; no heap or device allocation).
+mbgb_status prepare_frame_f32(const mbgb_scene &scene, const mbgb_opts &o, const float *aoVec, int aoCount,
+                              ParamsT<float> *p, FractalT<double> *fd) {
+  fill_params<float>(scene, *p, o, aoVec, aoCount);
+  fill_fractal<double>(scene, *fd);
+  return MBGB_OK;
+}
+
+// The ray-traced AO direction table (src/Render3D.cpp:272-313) written into caller
+// storage of `max_vectors` x 3 floats; returns the number of directions.
+int ao_vectors_into(int quality, float *out, int max_vectors) {
+  int counter = 0;
+  for (double b = -0.49 * M_PI; b < 0.49 * M_PI; b += 1.0 / quality) {
+    for (double a = 0.0; a < 2.0 * M_PI; a += ((2.0 / quality) / cos(b))) {
+      if (counter >= max_vectors) return counter;
+      out[3 * counter + 0] = (float)(cos(a + b) * cos(b));
+      out[3 * counter + 1] = (float)(sin(a + b) * cos(b));
+      out[3 * counter + 2] = (float)sin(b);
+      counter++;
+      if (counter >= kMaxAOVectors) break;
+    }
+    if (counter >= kMaxAOVectors) break;
+  }
+  return counter;
+}
+
 }  // namespace mbgb
 
 using namespace mbgb;

@@ -27,4 +27,12 @@ class GlibcRand {
 
 bool scene_set(mbgb_scene *sc, const char *key, const char *value, bool *palette_loaded);
 
+template <typename T>
+struct ParamsT;
+template <typename T>
+struct FractalT;
+mbgb_status prepare_frame_f32(const mbgb_scene &scene, const mbgb_opts &o, const float *aoVec, int aoCount,
+                              ParamsT<float> *p, FractalT<double> *fd);
+int ao_vectors_into(int quality, float *out, int max_vectors);
+
 }  // namespace mbgb

@@ -1,0 +1,88 @@
+"""The allocation-free render entry point (mbgb_render_device_noalloc), through the C ABI.
+
+Callers that cannot allocate device memory while they render (an application whose
+memory manager has reserved the GPU for its own pool, a plugin inside such a host, a
+frame loop that must not call cudaMalloc/cudaFree because they synchronise the
+device) use this entry point; its scratch is static device memory shared by all
+calls. The test renders through it twice in a row — first a scene whose long rays
+go through the overflow pass, then the benchmark scene — and checks each frame
+against mbgb_render_device on the same scene with the FP32 parity tolerance used
+by the other tests (<= 0.1 % hit mismatch, >= 45 dB PSNR of the float image).
+The two entry points run the same FP32 kernel, but the allocation-free one keeps
+fewer step records per thread, so more rays take the overflow pass; that pass's
+inlined copy of the pixel code may contract multiply-adds differently, which moves
+some float results by a few ulps — hence a tolerance, not bit equality.
+This file is collected last so a failure here comes after every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import mandelbulber_gb300 as mb
+from mandelbulber_gb300 import workloads as W
+from tests import metrics
+
+pytestmark = pytest.mark.gpu
+LAYERS = [("image_float", 12, np.float32, (3,)), ("zbuffer", 4, np.float32, ()), ("alpha", 2, np.uint16, ()),
+          ("opacity", 2, np.uint16, ()), ("colour", 3, np.uint8, (3,)), ("hit", 1, np.uint8, ()),
+          ("iters", 4, np.int32, ()), ("depth", 8, np.float64, ())]
+
+
+def _device_layers(w, h, fill):
+    import torch
+    return {name: torch.full((w * h * nbytes,), fill, dtype=torch.uint8, device="cuda")
+            for name, nbytes, _, _ in LAYERS}
+
+
+def _to_image(layers, w, h):
+    img = mb.CImage.empty(w, h)
+    for name, _, dt, extra in LAYERS:
+        setattr(img, name, layers[name].cpu().numpy().view(dt).reshape((h, w) + extra))
+    return img
+
+
+def _c_image(layers, w, h):
+    return mb.mbgb_image(w, h, *[ctypes.c_void_p(layers[name].data_ptr()) for name, _, _, _ in LAYERS])
+
+
+def test_noalloc_matches_render_device_on_two_calls(mblib):
+    import torch
+    lib = mb.library()
+    scenes = [W.workload("mandelbox_1080p", 192, 108, DE_factor=0.02),   # long rays: overflow pass
+              W.workload("mandelbox_1080p", 480, 270)]
+    refs = []
+    with mb.Context(0) as ctx:
+        for sc in scenes:
+            w, h = sc.image_width, sc.image_height
+            layers = _device_layers(w, h, 0)
+            ctx.render_device(sc, {k: v.data_ptr() for k, v in layers.items()}, precision=mb.PREC_FP32_FIX)
+            torch.cuda.synchronize()
+            refs.append(_to_image(layers, w, h))
+    opts = mb.make_opts(precision=mb.PREC_FP32_FIX)
+    for sc, ref in zip(scenes, refs):       # two calls in a row share the static scratch
+        w, h = sc.image_width, sc.image_height
+        layers = _device_layers(w, h, 0xA5)  # garbage: every pixel must be written
+        img_c = _c_image(layers, w, h)
+        rc = lib.mbgb_render_device_noalloc(ctypes.byref(sc), ctypes.byref(img_c), ctypes.byref(opts))
+        assert rc == 0, lib.mbgb_last_error()
+        torch.cuda.synchronize()
+        got = _to_image(layers, w, h)
+        m = metrics.compare(got, ref)
+        assert m["hit_mismatch"] <= 0.001 and m["psnr_float"] >= 45.0, m
+        # every pixel was written (the output started as 0xA5 garbage)
+        assert np.isfinite(got.image_float).all()
+        assert np.all((got.hit == 0) | (got.hit == 1))
+
+
+def test_noalloc_rejects_what_its_scratch_cannot_hold(mblib):
+    lib = mb.library()
+    big = W.workload("mandelbox_1080p", 4096, 2160)
+    img = mb.mbgb_image(4096, 2160, *([None] * 8))
+    assert lib.mbgb_render_device_noalloc(ctypes.byref(big), ctypes.byref(img), None) == 1
+    assert b"4194304 pixels" in lib.mbgb_last_error()
+    small = W.workload("mandelbox_1080p", 64, 36)
+    img = mb.mbgb_image(64, 36, *([None] * 8))
+    opts = mb.make_opts(precision=mb.PREC_FP64)
+    assert lib.mbgb_render_device_noalloc(ctypes.byref(small), ctypes.byref(img), ctypes.byref(opts)) == 1
+    assert b"FP32_FIX" in lib.mbgb_last_error()
