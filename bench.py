@@ -296,18 +296,34 @@ def main() -> int:
     e2e_value = world * npx * len(e2e_t) / sum(e2e_t) / 1e6
     d2h = npx * (12 + 4 + 2 + 2 + 3)
 
-    # roofline of the dominant kernel: ALU bound
+    # roofline of the dominant kernel: ALU bound. The library records CUDA events between
+    # its stage launches on the launching stream (profile_stages); each stage's algorithmic
+    # work comes from its own orbit/DE counters.
     peak_lib = ctypes.CDLL(os.path.join(ROOT, "mandelbulber_gb300", "libmbgb_peak.so"))
     peak_lib.mbgb_peak_tflops.restype = ctypes.c_double
     peak32 = peak_lib.mbgb_peak_tflops(0, dev)
     peak64 = peak_lib.mbgb_peak_tflops(1, dev)
     f = scene.formula
+    stage_names = ["primary_kernel", "polish_kernel", "secondary_kernel", "compose_kernel"]
+
+    def stage_profile(precision, frames):
+        acc = np.zeros(4)
+        for _ in range(frames):
+            ctx.render_device(scene, ptrs, precision=precision, profile_stages=True)
+            st = ctx.stats()
+            acc += np.array(list(st.stage_ms))
+        acc /= frames
+        work = [st.stage_orbit[k] * FLOPS_PER_ITER[f] + st.stage_de[k] * FLOPS_PER_DE[f] for k in range(4)]
+        stages = {stage_names[k]: {"ms": float(acc[k]), "flops": int(work[k]), "orbit_iterations": int(st.stage_orbit[k]),
+                                   "de_evaluations": int(st.stage_de[k])} for k in range(4)}
+        top = max(range(4), key=lambda k: acc[k])
+        return stages, stage_names[top], work[top], acc[top] / 1e3
+
+    stages32, top32, work32, sec32 = stage_profile(mb.PREC_FP32_FIX, args.steps)
+    stages64, top64, work64, sec64 = stage_profile(mb.PREC_FP64, 1)
     flops32 = st32.orbit_iterations * FLOPS_PER_ITER[f] + st32.de_calls * FLOPS_PER_DE[f]
-    flops64 = st64.orbit_iterations * FLOPS_PER_ITER[f] + st64.de_calls * FLOPS_PER_DE[f]
-    per_launch_s32 = total32 / args.steps
-    per_launch_s64 = total64 / args.fp64_steps
-    ach32 = flops32 / per_launch_s32 / 1e12
-    ach64 = flops64 / per_launch_s64 / 1e12
+    ach32 = work32 / sec32 / 1e12
+    ach64 = work64 / sec64 / 1e12
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     traffic = None
     if os.path.exists(prof):
@@ -333,21 +349,23 @@ def main() -> int:
                             "ray AO q2 (29 dirs), volumetric fog 0.5, glow",
                    "precision": "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement",
                    "l2": "flushed between timed frames (512 MiB write)", "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "fp32_alu", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
+        "roofline": {"kernel": top32, "bound": "fp32_alu", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
                      "frac": ach32 / peak32 if peak32 > 0 else None, "traffic": traffic,
                      "peak_source": "measured live: FP32 FMA-chain microbenchmark (libmbgb_peak.so)",
-                     "flops_per_launch": flops32,
-                     "work": f"{st32.orbit_iterations} orbit iterations x {FLOPS_PER_ITER[f]} + "
-                             f"{st32.de_calls} DE evaluations x {FLOPS_PER_DE[f]}"},
+                     "flops_per_launch": int(work32),
+                     "frame_flops": int(flops32),
+                     "frame_achieved": flops32 / (total32 / args.steps) / 1e12,
+                     "work": f"{FLOPS_PER_ITER[f]} FP ops per orbit iteration + {FLOPS_PER_DE[f]} per DE evaluation"},
+        "stages": stages32,
         "fp64_plain": {"value": value64, "unit": "Mpix/s", "ms_per_step": 1e3 * total64 / args.fp64_steps,
-                       "steps": args.fp64_steps,
-                       "roofline": {"bound": "fp64_alu", "achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
-                                    "frac": ach64 / peak64 if peak64 > 0 else None}},
+                       "steps": args.fp64_steps, "stages": stages64,
+                       "roofline": {"kernel": top64, "bound": "fp64_alu", "achieved": ach64, "peak": peak64,
+                                    "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 > 0 else None}},
         "ratio_vs_fp64": value / value64,
         "parity_vs_fp64": parity,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": ctypes.sizeof(mb.mbgb_scene),
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (5 if scene.glow_intensity or scene.fogDensity > 0 or scene.fogEnabled else 4),
         "clocks": clocks,
         "cpu_baseline": cpu,
         "wall_s_timed_region": wall32,

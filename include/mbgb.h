@@ -199,7 +199,15 @@ typedef struct mbgb_opts {
   int32_t threads_per_cta;     /* 0 = autotuned */
   int32_t deadline_ms;         /* device-side deadline; 0 = none */
   void *stream;                /* cudaStream_t; NULL = the context's stream */
+  int32_t engine;              /* MBGB_ENGINE_*; 0 = wavefront stages */
+  int32_t profile_stages;      /* 1: record CUDA events between stages (synchronous calls fill stage_ms) */
 } mbgb_opts;
+
+/* Render engines (same results within the precision policy's tolerance). */
+enum {
+  MBGB_ENGINE_WAVEFRONT = 0,   /* ray-granular stages with lane refill (default) */
+  MBGB_ENGINE_PER_PIXEL = 1    /* one thread renders a whole pixel; smallest scratch */
+};
 
 /* Per-render counters (the reference's N_counter, DE_counter, Pixel_counter,
  * Missed_DE_counter globals, src/Render3D.cpp:51-57), kept per context here. */
@@ -211,6 +219,11 @@ typedef struct mbgb_stats {
   uint64_t missed_de;          /* Missed_DE_counter */
   uint64_t long_rays;          /* primary rays longer than the main pass's step records (re-rendered) */
   double kernel_ms;            /* device time of the last render */
+  /* per stage: [0] primary rays (wavefront) or the per-pixel kernel, [1] FP64 hit polish,
+   * [2] shadow and AO rays, [3] composition */
+  uint64_t stage_orbit[4];     /* orbit iterations */
+  uint64_t stage_de[4];        /* DE evaluations */
+  double stage_ms[4];          /* device time between the stage's CUDA events (profile_stages = 1) */
 } mbgb_stats;
 
 typedef struct mbgb_context mbgb_context;
@@ -235,6 +248,14 @@ mbgb_status mbgb_scene_from_settings(const char *defaults_path, const char *path
 mbgb_status mbgb_scene_set(mbgb_scene *scene, const char *key, const char *value);
 /* Re-derive the dependent fields (analytic-DE flag, resolution, matrices, clamps) after edits. */
 mbgb_status mbgb_scene_finalize(mbgb_scene *scene);
+/* Scene of animation frame `frame` from `n_keys` keyframes, `frames_per_key` frames apart:
+ * CMorph::CatmullRom (src/morph.cpp:49-109) over every interpolated double, as MainRender
+ * applies it in keyframe mode (src/Render3D.cpp:2280-2291). The non-interpolated fields
+ * come from `base` (NULL = keys[0]); derived fields are rebuilt (mbgb_scene_finalize). */
+mbgb_status mbgb_scene_interpolate(const mbgb_scene *keys, int n_keys, int frames_per_key, int frame,
+                                   const mbgb_scene *base, mbgb_scene *out);
+/* The same spline on plain rows: keys[n_keys][size] -> out[size] for one frame. */
+mbgb_status mbgb_catmull_rom(const double *keys, int n_keys, int size, int frames_per_key, int frame, double *out);
 /* Palette of NewPalette (src/image.cpp:28-55) seeded like LoadSettingsPost (src/settings.cpp:1185-1195). */
 void mbgb_palette_from_seed(int32_t seed, double saturation, mbgb_rgb palette[256]);
 /* Report whether the device kernels can render this scene (MBGB_OK) or why not. */

@@ -96,6 +96,10 @@ FUNCTIONS = {
                                                 _P(mbgb_scene)]),
     "mbgb_scene_set": (ctypes.c_int, [_P(mbgb_scene), ctypes.c_char_p, ctypes.c_char_p]),
     "mbgb_scene_finalize": (ctypes.c_int, [_P(mbgb_scene)]),
+    "mbgb_catmull_rom": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p]),
+    "mbgb_scene_interpolate": (ctypes.c_int, [_P(mbgb_scene), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              _P(mbgb_scene), _P(mbgb_scene)]),
     "mbgb_palette_from_seed": (None, [ctypes.c_int32, ctypes.c_double, _P(mbgb_rgb)]),
     "mbgb_scene_supported": (ctypes.c_int, [_P(mbgb_scene)]),
     "mbgb_context_create": (ctypes.c_int, [ctypes.c_int, _P(ctypes.c_void_p)]),

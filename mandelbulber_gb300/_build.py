@@ -42,8 +42,11 @@ def _units(cuda: str):
     yield "render_f64.cu", common_cu + ["--fmad=false"]
     yield "render_f32.cu", common_cu
     yield "noalloc.cu", common_cu
+    yield "wave_f64.cu", common_cu + ["--fmad=false"]
+    yield "wave_f32.cu", common_cu
     yield "capi.cpp", common_cpp
     yield "settings.cpp", common_cpp
+    yield "keyframes.cpp", common_cpp
 
 
 def _sources_newer(target: str) -> bool:

@@ -15,6 +15,22 @@
 #include "launch.h"
 #include "mbgb.h"
 #include "mbgb_internal.h"
+#include "wave_launch.h"
+
+namespace mbgb {
+// WaveBufs layout (must match wave_core.cuh)
+template <typename T>
+struct WaveBufs {
+  uint8_t *flags;
+  T *scan, *dist, *thr, *step, *detail;
+  int32_t *bis_left;
+  double *point;
+  int32_t *iters, *count;
+  T *vol, *shadow, *ao;
+  uint32_t *hit_list, *ctl, *overflow_list;
+  int64_t npix;
+};
+}  // namespace mbgb
 
 namespace mbgb {
 
@@ -311,7 +327,9 @@ struct mbgb_context {
   int ao_quality = -1;
   int ao_count = 0;
   DeviceBuf out[8];               // device staging for mbgb_render_host
+  DeviceBuf wave[2];              // wavefront per-pixel buffers, per precision
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t sev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // stage events
   mbgb_stats stats{};
   std::mutex mu;
 };
@@ -365,7 +383,10 @@ extern "C" mbgb_status mbgb_context_create(int device, mbgb_context **out) {
   }
   c->sms = prop.multiProcessorCount;
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
+      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
+      (e = cudaEventCreate(&c->sev[0])) != cudaSuccess || (e = cudaEventCreate(&c->sev[1])) != cudaSuccess ||
+      (e = cudaEventCreate(&c->sev[2])) != cudaSuccess || (e = cudaEventCreate(&c->sev[3])) != cudaSuccess ||
+      (e = cudaEventCreate(&c->sev[4])) != cudaSuccess) {
     delete c;
     return cuda_error(e, "context stream/event creation");
   }
@@ -382,10 +403,13 @@ extern "C" void mbgb_context_destroy(mbgb_context *c) {
   for (auto &a : c->ovstep)
     for (auto &b : a) b.release();
   c->ovlist.release();
+  for (auto &b : c->wave) b.release();
   c->control.release();
   c->ao64.release();
   c->ao32.release();
   for (auto &b : c->out) b.release();
+  for (auto &ev : c->sev)
+    if (ev) cudaEventDestroy(ev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -409,6 +433,120 @@ static mbgb_status ensure_ao(mbgb_context *c, int quality, cudaStream_t s) {
   MBGB_CUDA(cudaStreamSynchronize(s));
   c->ao_quality = quality;
   c->ao_count = (int)(v.size() / 3);
+  return MBGB_OK;
+}
+
+// The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
+// julia, limits, iteration threshold or interior mode, and fold value = 2 x fold limit.
+static bool fast_mandelbox(const mbgb_scene &s) {
+  return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
+         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
+         s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
+         s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit;
+}
+
+// The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,
+// no pre-folds, limits, iteration threshold or interior mode).
+static bool fast_mandelbulb(const mbgb_scene &s) {
+  return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
+         !s.limits_enabled && !s.iterThresh && !s.interiorMode;
+}
+
+// Wavefront stages (wave_core.cuh): primary rays, FP64 polish (FP32 policy), shadow/AO
+// rays, composition. All launches are enqueued on `s` without host round trips.
+template <typename T>
+static mbgb_status render_wave(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *img, const mbgb_opts &o,
+                               cudaStream_t s, const int prec, FrameIO io, bool needVol, uint32_t **long_rays_ctl) {
+  const int64_t npix = (int64_t)scene->image_width * scene->image_height;
+  const int block = 128;
+  const bool rayAO = scene->global_ilumination && !scene->fastGlobalIllumination;
+  const int aoN = rayAO ? c->ao_count : 0;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return at;
+  };
+  const size_t ts = sizeof(T);
+  const size_t o_flags = take(npix), o_scan = take(npix * ts), o_dist = take(npix * ts), o_thr = take(npix * ts);
+  const size_t o_step = take(npix * ts), o_detail = take(npix * ts), o_bis = take(npix * 4);
+  const size_t o_point = take(3 * npix * 8), o_iters = take(npix * 4), o_count = take(npix * 4);
+  const size_t o_vol = take(6 * npix * ts), o_shadow = take(npix * ts), o_ao = take((size_t)aoN * npix * ts);
+  const size_t o_hit = take(npix * 4), o_ovl = take(npix * 4), o_ctl = take(64);
+  MBGB_CUDA(c->wave[prec].ensure(off));
+  char *base = (char *)c->wave[prec].ptr;
+  WaveLaunch<T> L;
+  WaveBufs<T> &wb = L.wb;
+  wb.flags = (uint8_t *)(base + o_flags);
+  wb.scan = (T *)(base + o_scan);
+  wb.dist = (T *)(base + o_dist);
+  wb.thr = (T *)(base + o_thr);
+  wb.step = (T *)(base + o_step);
+  wb.detail = (T *)(base + o_detail);
+  wb.bis_left = (int32_t *)(base + o_bis);
+  wb.point = (double *)(base + o_point);
+  wb.iters = (int32_t *)(base + o_iters);
+  wb.count = (int32_t *)(base + o_count);
+  wb.vol = (T *)(base + o_vol);
+  wb.shadow = (T *)(base + o_shadow);
+  wb.ao = (T *)(base + o_ao);
+  wb.hit_list = (uint32_t *)(base + o_hit);
+  wb.overflow_list = (uint32_t *)(base + o_ovl);
+  wb.ctl = (uint32_t *)(base + o_ctl);
+  wb.npix = npix;
+  MBGB_CUDA(cudaMemsetAsync(wb.ctl, 0, 64, s));
+
+  int occ1 = (sizeof(T) == 8) ? occupancy_wave_f64(scene->formula, block, 0) : occupancy_wave_f32(scene->formula, block, 0);
+  int occ2 = (sizeof(T) == 8) ? occupancy_wave_f64(scene->formula, block, 1) : occupancy_wave_f32(scene->formula, block, 1);
+  if (occ1 < 1) occ1 = 1;
+  if (occ2 < 1) occ2 = 1;
+  if (o.ctas_per_sm > 0) {
+    occ1 = std::min(occ1, o.ctas_per_sm);
+    occ2 = std::min(occ2, o.ctas_per_sm);
+  }
+  L.grid = c->sms * occ1;
+  L.grid2 = c->sms * occ2;
+  L.block = block;
+  L.ov_grid = kOverflowThreads / block > 0 ? kOverflowThreads / block : 1;
+  L.polish_grid = c->sms * 8;
+  const int64_t nrow = (int64_t)(o.row_end - o.row_begin) * scene->image_width;
+  L.compose_grid = (int)std::min<int64_t>((nrow + block - 1) / block, (int64_t)c->sms * 32);
+  if (L.compose_grid < 1) L.compose_grid = 1;
+  const int64_t slots = (int64_t)L.grid * block;
+  io.slots = slots;
+  io.step_cap = kStepCap;
+  io.overflow_pass = 0;
+  const size_t esz = sizeof(T);
+  if (needVol) {
+    const size_t bytes = (size_t)kStepCap * (size_t)slots * esz;
+    const size_t obytes = (size_t)kStepSlots * (size_t)kOverflowThreads * esz;
+    for (int k = 0; k < 3; k++) {
+      MBGB_CUDA(c->step[prec][k].ensure(bytes));
+      MBGB_CUDA(c->ovstep[prec][k].ensure(obytes));
+    }
+    io.step_step = c->step[prec][0].ptr;
+    io.step_dist = c->step[prec][1].ptr;
+    io.step_thr = c->step[prec][2].ptr;
+  }
+  L.io = io;
+  L.ov = io;
+  L.ov.overflow_pass = 1;
+  L.ov.step_cap = kStepSlots;
+  L.ov.slots = kOverflowThreads;
+  L.ov.step_step = c->ovstep[prec][0].ptr;
+  L.ov.step_dist = c->ovstep[prec][1].ptr;
+  L.ov.step_thr = c->ovstep[prec][2].ptr;
+  L.overflow = needVol;
+  for (int k = 0; k < 5; k++) L.ev[k] = o.profile_stages ? c->sev[k] : nullptr;
+  L.fast = fast_mandelbox(*scene) || fast_mandelbulb(*scene);
+  fill_fractal<double>(*scene, L.fd);
+  fill_params<T>(*scene, L.p, o, (const T *)(sizeof(T) == 8 ? c->ao64.ptr : c->ao32.ptr), c->ao_count);
+  cudaError_t e;
+  if constexpr (sizeof(T) == 8) e = launch_wave_f64(L, s);
+  else e = launch_wave_f32(L, s);
+  if (e != cudaSuccess) return cuda_error(e, "wavefront launch");
+  *long_rays_ctl = wb.ctl + 3;
+  (void)img;
   return MBGB_OK;
 }
 
@@ -453,7 +591,10 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   io.overflow_pass = 0;
   const bool needVol = (scene->glow_intensity != 0.0) || scene->fogEnabled || (scene->fogDensity > 0.0);
   const size_t esz = prec == 0 ? sizeof(double) : sizeof(float);
-  if (needVol) {
+  const bool rayAOjobs = scene->global_ilumination && !scene->fastGlobalIllumination;
+  const double jobs = (double)scene->image_width * scene->image_height * (1.0 + (rayAOjobs ? c->ao_count : 0));
+  const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && jobs < 4.0e9;
+  if (needVol && !wave) {
     const size_t bytes = (size_t)kStepCap * (size_t)slots * esz;
     const size_t obytes = (size_t)kStepSlots * (size_t)kOverflowThreads * esz;
     for (int k = 0; k < 3; k++) {
@@ -479,7 +620,13 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   fill_fractal<double>(*scene, fd);
   MBGB_CUDA(cudaEventRecord(c->ev0, s));
   cudaError_t e;
-  // main pass, then (when the step buffer is in use) the overflow pass for rays longer than kStepCap
+  uint32_t *longRays = (uint32_t *)(ctl + 4);
+  if (wave) {
+    mbgb_status ws = prec == 0 ? render_wave<double>(c, scene, img, o, s, 0, io, needVol, &longRays)
+                               : render_wave<float>(c, scene, img, o, s, 1, io, needVol, &longRays);
+    if (ws != MBGB_OK) return ws;
+  }
+  // per-pixel engine: main pass, then (when the step buffer is in use) the overflow pass
   FrameIO ov = io;
   ov.overflow_pass = 1;
   ov.step_cap = kStepSlots;
@@ -488,7 +635,9 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   ov.step_dist = c->ovstep[prec][1].ptr;
   ov.step_thr = c->ovstep[prec][2].ptr;
   const int ovBlocks = kOverflowThreads / block > 0 ? kOverflowThreads / block : 1;
-  if (prec == 0) {
+  if (wave) {
+    e = cudaSuccess;
+  } else if (prec == 0) {
     ParamsT<double> p;
     fill_params<double>(*scene, p, o, (const double *)c->ao64.ptr, c->ao_count);
     e = launch_render_f64(scene->formula, p, fd, io, grid, block, s);
@@ -503,12 +652,27 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   MBGB_CUDA(cudaEventRecord(c->ev1, s));
   if (!o.stream) {
     MBGB_CUDA(cudaStreamSynchronize(s));
-    unsigned long long cnt[4];
+    unsigned long long cnt[16];
     int flag = 0;
     unsigned int nover = 0;
     MBGB_CUDA(cudaMemcpy(cnt, ctl + 64, sizeof(cnt), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 4; k++) {
+      c->stats.stage_orbit[k] = cnt[4 * k + 0];
+      c->stats.stage_de[k] = cnt[4 * k + 1];
+      c->stats.stage_ms[k] = 0.0;
+      if (wave && o.profile_stages) {
+        float sm = 0;
+        if (cudaEventElapsedTime(&sm, c->sev[k], c->sev[k + 1]) == cudaSuccess) c->stats.stage_ms[k] = sm;
+      }
+    }
+    for (int k = 1; k < 4; k++) {
+      cnt[0] += cnt[4 * k + 0];
+      cnt[1] += cnt[4 * k + 1];
+      cnt[2] += cnt[4 * k + 2];
+      cnt[3] += cnt[4 * k + 3];
+    }
     MBGB_CUDA(cudaMemcpy(&flag, ctl + 16, sizeof(flag), cudaMemcpyDeviceToHost));
-    MBGB_CUDA(cudaMemcpy(&nover, ctl + 4, sizeof(nover), cudaMemcpyDeviceToHost));
+    MBGB_CUDA(cudaMemcpy(&nover, longRays, sizeof(nover), cudaMemcpyDeviceToHost));
     c->stats.long_rays = nover;
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);

@@ -1,0 +1,820 @@
+// Wavefront renderer: the per-pixel pipeline of MainThread (src/Render3D.cpp:389-589)
+// split into ray-granular stages so that SIMT lanes stay busy.
+//
+//   primary_kernel   one primary ray per job: RayMarching's march and binary refinement
+//                    (src/Render3D.cpp:79-199); at the end of each ray the lane folds
+//                    the ray's step records into the volumetric pass's affine map and
+//                    takes the next pixel (lane refill).
+//   polish_kernel    FP32 policy: the last bisection steps in FP64 at every hit.
+//   secondary_kernel one shadow ray (MainShadow, src/shaders.cpp:480-570) or one AO
+//                    direction (AmbientOcclusion, src/shaders.cpp:607-673) per job,
+//                    with lane refill; results go to per-pixel slots.
+//   compose_kernel   normals, colour, specular, fast AO, background, the volumetric
+//                    map and the cImage writes (ObjectShader / BackgroundShader /
+//                    VolumetricShader, src/shaders.cpp:21-478).
+//
+// The volumetric pass is affine in the pixel colour it starts from: every glow, post-fog
+// and volumetric-fog group computes out = a*C + (1 - a)*out, so the whole pass is
+// out = A*base + B with one A for the three channels; alpha and opacity do not depend on
+// the base colour (its alpha is 1 for a hit and 0 otherwise, known when the march ends).
+// Lane refill: each warp keeps 32 rays in flight; when rays end, one atomicAdd on the
+// job counter hands the free lanes their next jobs (popc of the ballot).
+#pragma once
+
+#include "render_core.cuh"
+
+namespace mbgb {
+
+// Per-frame SoA buffers of the wavefront stages (device memory).
+template <typename T>
+struct WaveBufs {
+  uint8_t *flags;        // [npix] bit0: hit, bit1: hemisphere cut / not marched
+  T *scan;               // [npix] depth of the primary ray
+  T *dist;               // [npix] last distance (lastDist)
+  T *thr;                // [npix] distThresh at the hit
+  T *step;               // [npix] FP32 policy: bisection step left for the FP64 polish
+  T *detail;             // [npix] detailSize of the march's last step (src/Render3D.cpp:110)
+  int32_t *bis_left;     // [npix] FP32 policy: bisection iterations left
+  double *point;         // [3][npix] hit point
+  int32_t *iters;        // [npix] itersOut at the end of the march
+  int32_t *count;        // [npix] buffCount
+  T *vol;                // [6][npix] A, B.r, B.g, B.b, alpha, opacity
+  T *shadow;             // [npix]
+  T *ao;                 // [aoCount][npix] per-direction shadowTemp
+  uint32_t *hit_list;    // [npix]
+  uint32_t *ctl;         // [0] primary jobs taken, [1] hits, [2] secondary jobs taken, [3] overflow
+                         // count, [4] overflow-pass jobs taken (zeroed before the frame)
+  uint32_t *overflow_list;
+  int64_t npix;
+};
+
+namespace dev {
+
+// Mandelbox orbit (formula 8, normal mode) for the common case: no rotation, no offset,
+// no pre-folds, julia off, fold value = 2 x fold limit. Squared radius throughout: the
+// bailout r > 1024 becomes r^2 > 1024^2 and the sphere fold tests r^2 directly, so the
+// loop has no square root; the fold is clamp(x)*2 - x, identical to fv - x / -fv - x.
+__device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const float px, const float py,
+                                                const float pz, const int N, int &Lout, Counters &cnt) {
+  const float fl = f.mbFoldLimit;
+  const float mR2 = f.mbMinR * f.mbMinR;
+  const float fR2 = f.mbFixedR * f.mbFixedR;
+  const float k1 = fR2 / mR2;
+  const float s = f.mbScale;
+  const float as = fabsf(s);
+  const float cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
+  float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
+  int L;
+  for (L = 0; L < N; L++) {
+    x = fminf(fmaxf(x, -fl), fl) * 2.0f - x;
+    y = fminf(fmaxf(y, -fl), fl) * 2.0f - y;
+    z = fminf(fmaxf(z, -fl), fl) * 2.0f - z;
+    float r2 = x * x + y * y + z * z;
+    const float k = (r2 < mR2) ? k1 : ((r2 < fR2) ? __fdividef(fR2, r2) : 1.0f);
+    const float ks = k * s;
+    x = fmaf(x, ks, cx);
+    y = fmaf(y, ks, cy);
+    z = fmaf(z, ks, cz);
+    dr = fmaf(dr, k * as, 1.0f);
+    r2 = x * x + y * y + z * z;
+    if (r2 > 1048576.0f) {
+      dist = sqrtf(r2) / fabsf(dr);
+      break;
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (L == N) dist = 0.0f;
+  return dist;
+}
+
+// Mandelbulb power 8 (trig_optim, src/fractal.cpp:211-225) without transcendentals:
+// theta = asin(z/r) in [-pi/2, pi/2] has cos = rho/r >= 0 and sin = z/r; phi = atan2(y, x)
+// has cos = x/rho, sin = y/rho (phi = 0 when rho = 0, as atan2(0, 0)). Three angle
+// doublings (c, s) -> (c^2 - s^2, 2cs) give 8*theta and 8*phi; r^8 and r^7 come from r^2.
+// MODE 0 returns the distance estimate 0.5*r*ln(r)/dr at the bailout r > 100;
+// MODE 1 returns the colouring value (min |z| until |z| > 1e15, times 5000).
+template <int MODE>
+__device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, const float px, const float py,
+                                                  const float pz, const int N, int &Lout, Counters &cnt) {
+  float cx, cy, cz;
+  if (f.juliaMode) {
+    cx = f.julia[0]; cy = f.julia[1]; cz = f.julia[2];
+  } else {
+    cx = px * f.constantFactor; cy = py * f.constantFactor; cz = pz * f.constantFactor;
+  }
+  float x = px, y = py, z = pz, r_dz = 1.0f, dist = 0.0f;
+  float r2 = x * x + y * y + z * z;
+  float minr2 = __int_as_float(0x7f800000);
+  int L;
+  for (L = 0; L < N; L++) {
+    const float rho2 = x * x + y * y;
+    const float inv_r = rsqrtf(r2);
+    const bool axis = rho2 == 0.0f;
+    const float inv_rho = axis ? 0.0f : rsqrtf(rho2);
+    float ct = rho2 * inv_rho * inv_r, st = z * inv_r;
+    float cp = axis ? 1.0f : x * inv_rho, sp = axis ? 0.0f : y * inv_rho;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const float ct2 = ct * ct - st * st, st2 = 2.0f * st * ct;
+      const float cp2 = cp * cp - sp * sp, sp2 = 2.0f * sp * cp;
+      ct = ct2; st = st2; cp = cp2; sp = sp2;
+    }
+    const float r4 = r2 * r2;
+    const float r8 = r4 * r4;
+    r_dz = fmaf(8.0f * r8 * inv_r, r_dz, 1.0f);   // p * r^(p-1) * r_dz + 1
+    const float t = ct * r8;
+    x = fmaf(t, cp, cx);
+    y = fmaf(t, sp, cy);
+    z = fmaf(st, r8, cz);
+    r2 = x * x + y * y + z * z;
+    if (MODE == 0) {
+      if (r2 > 1.0e4f) {
+        const float r = sqrtf(r2);
+        dist = 0.5f * r * __logf(r) / r_dz;
+        break;
+      }
+    } else {
+      if (r2 < minr2) minr2 = r2;
+      if (r2 > 1.0e30f) break;
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (MODE == 0) {
+    if (L == N) dist = 0.0f;
+    return dist;
+  }
+  // colouring: min |z| after a bailout, else the last |z|
+  return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
+}
+
+// CalculateDistance with the orbit chosen at compile time: FAST selects mandelbox_fast
+// (formula 8) or mandelbulb8_fast (formula 2, power 8).
+template <typename T, int FORMULA, bool FAST>
+__device__ __forceinline__ T wave_distance(const FractalT<T> &f, const V3<T> p, const T detail, const int N,
+                                           const int minN, const bool normalMode, int &L, bool &maxIter,
+                                           Counters &cnt) {
+  if constexpr (FAST && sizeof(T) == 4) {
+    int Li;
+    T distance;
+    if constexpr (FORMULA == 8) distance = mandelbox_fast(f, p.x, p.y, p.z, N, Li, cnt);
+    else distance = mandelbulb8_fast<0>(f, p.x, p.y, p.z, N, Li, cnt);
+    maxIter = (Li == N);
+    L = Li;
+    if (distance < T(0)) distance = T(0);
+    if (Li < minN && distance < detail) distance = detail;
+    return distance;
+  } else {
+    return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt);
+  }
+}
+
+// SurfaceColour (src/shaders.cpp:850-879) with the fast power-8 colouring orbit when it applies.
+template <typename T, int FORMULA, bool FAST>
+__device__ __forceinline__ V3<T> wave_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt) {
+  if constexpr (FAST && FORMULA == 2 && sizeof(T) == 4) {
+    int L;
+    const float c = mandelbulb8_fast<1>(p.f, point.x, point.y, point.z, p.f.N10, L, cnt);
+    int nrCol = to_i32_x86((double)floorf(c));
+    const unsigned mag = nrCol < 0 ? 0u - (unsigned)nrCol : (unsigned)nrCol;
+    nrCol = (int)(mag % (248u * 256u));
+    int rgb[3] = {256, 256, 256};
+    if (p.coloring) {
+      const int color_number = to_i32_x86((double)((T)nrCol * p.coloringSpeed + T(256) * p.paletteOffset)) % 65536;
+      index_to_colour(p, color_number, rgb);
+    }
+    return V3<T>{T(rgb[0]) / T(256), T(rgb[1]) / T(256), T(rgb[2]) / T(256)};
+  } else {
+    return surface_colour<T, FORMULA>(p, point, cnt);
+  }
+}
+
+// Warp-level job hand-out: lanes with need == true receive consecutive job indices.
+__device__ __forceinline__ unsigned int claim_jobs(unsigned int *counter, const bool need) {
+  const unsigned int lane = threadIdx.x & 31u;
+  const unsigned int mask = __ballot_sync(0xffffffffu, need);
+  unsigned int base = 0;
+  if (lane == (unsigned int)(__ffs(mask) - 1) && mask) base = atomicAdd(counter, (unsigned int)__popc(mask));
+  base = __shfl_sync(0xffffffffu, base, mask ? (__ffs(mask) - 1) : 0);
+  return base + (unsigned int)__popc(mask & ((1u << lane) - 1u));
+}
+
+// Job index -> pixel: 8x4 tiles in row-major tile order, so a warp's first 32 jobs are one tile.
+__device__ __forceinline__ void job_pixel(const int width, const int row_begin, const unsigned int job, int &x,
+                                          int &y) {
+  const int tilesX = (width + kTileW - 1) / kTileW;
+  const unsigned int tile = job / (kTileW * kTileH);
+  const unsigned int inTile = job % (kTileW * kTileH);
+  x = (int)(tile % (unsigned int)tilesX) * kTileW + (int)(inTile % kTileW);
+  y = row_begin + (int)(tile / (unsigned int)tilesX) * kTileH + (int)(inTile / kTileW);
+}
+
+// Camera ray of a pixel (src/Render3D.cpp:389-438); returns false for a fisheye-cut pixel.
+template <typename T>
+__device__ __forceinline__ bool camera_ray(const ParamsT<T> &p, const int x, const int y, V3<double> &view) {
+  const double x2 = ((double)x / p.width / p.tiles - 0.5 + p.tileXOffset / p.tiles) * p.aspect;
+  const double z2 = ((double)y / p.height / p.tiles - 0.5 + p.tileYOffset / p.tiles);
+  bool cut = false;
+  V3<double> vv;
+  if (p.perspType == 1) {
+    if (p.fishEyeCut && sqrt(x2 * x2 + z2 * z2) > 0.5 / p.fov) cut = true;
+    const double x3 = x2 * kPI, z3 = z2 * kPI;
+    const double r = sqrt(x3 * x3 + z3 * z3);
+    if (r == 0) {
+      vv = {0.0, 1.0, 0.0};
+    } else {
+      vv.x = x3 / r * sin(r * p.fov);
+      vv.z = z3 / r * sin(r * p.fov);
+      vv.y = cos(r * p.fov);
+    }
+    vv = normalize3(vv);
+  } else if (p.perspType == 2) {
+    const double x3 = x2 * kPI, z3 = z2 * kPI;
+    vv.x = sin(p.fov * x3) * cos(p.fov * z3);
+    vv.z = sin(p.fov * z3);
+    vv.y = cos(p.fov * x3) * cos(p.fov * z3);
+    vv = normalize3(vv);
+  } else {
+    vv = {x2 * p.fov, 1.0, z2 * p.fov};
+  }
+  view = rotate(p.rot, p.rot_zero, vv);
+  return !cut;
+}
+
+// The volumetric pass over one ray's records (VolumetricShader's glow, post fog and
+// volumetric fog, src/shaders.cpp:185-478) as the affine map out = A*base + B, plus
+// the alpha and opacity it leaves for a base alpha of `alpha0`.
+template <typename T>
+__device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
+                                                  const T depth, const T alpha0, T vol[6]) {
+  T A = T(1), B0 = T(0), B1 = T(0), B2 = T(0), alpha = alpha0;
+  float totalOpacity = 0.0f, opacityOut = 0.0f;
+  const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
+  T glowN = T(1) - glow;
+  if (glowN < T(0)) glowN = T(0);
+  const T gR = (T(p.glow1[0]) * glowN + T(p.glow2[0]) * glow) / T(65536);
+  const T gG = (T(p.glow1[1]) * glowN + T(p.glow2[1]) * glow) / T(65536);
+  const T gB = (T(p.glow1[2]) * glowN + T(p.glow2[2]) * glow) / T(65536);
+  T totalStep = T(0);
+  for (int index = stepCount - 1; index > 0; index--) {
+    T step = sb.step[sb.at(index)];
+    const T distance = sb.dist[sb.at(index)];
+    const T dist_thresh = sb.thr[sb.at(index)];
+    totalStep += step;
+    if (totalStep < dist_thresh * p.quality) continue;
+    step = totalStep;
+    totalStep = T(0);
+    const T go = glow * step / depth;
+    A = (T(1) - go) * A;
+    B0 = go * gR + (T(1) - go) * B0;
+    B1 = go * gG + (T(1) - go) * B1;
+    B2 = go * gB + (T(1) - go) * B2;
+    alpha += go;
+    if (p.postFog) {
+      T fd = step / p.fogVisibility;
+      if (fd > T(1)) fd = T(1);
+      A = (T(1) - fd) * A;
+      B0 = fd * T(p.fogColor[0]) / T(65536) + (T(1) - fd) * B0;
+      B1 = fd * T(p.fogColor[1]) / T(65536) + (T(1) - fd) * B1;
+      B2 = fd * T(p.fogColor[2]) / T(65536) + (T(1) - fd) * B2;
+      totalOpacity = (float)(fd + (T(1) - fd) * (T)totalOpacity);
+      alpha = fd + (T(1) - fd) * alpha;
+    }
+    if (p.fogDensity > T(0)) {
+      const T red = p.fogDistFactor;
+      const T dt = (step * red) / (distance * distance + red * red);
+      T k = distance / p.fogC1Dist;
+      if (k > T(1)) k = T(1);
+      T kn = T(1) - k;
+      T fr = (T(p.fogCol1[0]) * kn + T(p.fogCol2[0]) * k);
+      T fg = (T(p.fogCol1[1]) * kn + T(p.fogCol2[1]) * k);
+      T fb = (T(p.fogCol1[2]) * kn + T(p.fogCol2[2]) * k);
+      T k2 = distance / p.fogC2Dist * k;
+      if (k2 > T(1)) k2 = T(1);
+      kn = T(1) - k2;
+      fr = (fr * kn + T(p.fogCol3[0]) * k2);
+      fg = (fg * kn + T(p.fogCol3[1]) * k2);
+      fb = (fb * kn + T(p.fogCol3[2]) * k2);
+      T fd = T(0.3) * p.fogDensity * dt / (T(1) + p.fogDensity * dt);
+      if (fd > T(1)) fd = T(1);
+      A = (T(1) - fd) * A;
+      B0 = fd * fr / T(65536) + (T(1) - fd) * B0;
+      B1 = fd * fg / T(65536) + (T(1) - fd) * B1;
+      B2 = fd * fb / T(65536) + (T(1) - fd) * B2;
+      totalOpacity = (float)(fd + (T(1) - fd) * (T)totalOpacity);
+      alpha = fd + (T(1) - fd) * alpha;
+    }
+    if (totalOpacity > 1.0f) totalOpacity = 1.0f;
+    if (alpha > T(1)) alpha = T(1);
+    opacityOut = totalOpacity;
+  }
+  vol[0] = A;
+  vol[1] = B0;
+  vol[2] = B1;
+  vol[3] = B2;
+  vol[4] = alpha;
+  vol[5] = (T)opacityOut;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1: primary rays with lane refill.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA, bool FAST>
+__global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const FractalT<double> fd,
+                                                      const FrameIO io, const WaveBufs<T> wb) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, io.slots, slot};
+  const bool useSB = p.needVolumetric;
+  const bool f64 = sizeof(T) == 8;
+  const V3<T> start{(T)p.start[0], (T)p.start[1], (T)p.start[2]};
+  const T thrScale = p.resolution * p.persp / p.quality;
+  const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
+  const T search_limit = T(1) - T(0.01) * p.quality;
+  const int stepCap = io.overflow_pass ? kStepSlots : io.step_cap;
+  // jobs: 8x4 tiles of the row range (partial tiles included), or the overflow list
+  const int tilesX = (p.width + kTileW - 1) / kTileW;
+  const unsigned int nTileJobs =
+      io.overflow_pass ? *(volatile unsigned int *)&wb.ctl[3]
+                       : (unsigned int)(tilesX * ((p.row_end - p.row_begin + kTileH - 1) / kTileH) * kTileW * kTileH);
+  Counters cnt{0, 0, 0, 0};
+  unsigned int *jobCounter = io.overflow_pass ? (wb.ctl + 4) : (wb.ctl + 0);
+
+  // per-lane ray state
+  bool active = false, exhausted = false;
+  int pix = 0, phase = 0, i = 0, buffCount = 0, iters = 0, bis = 0;
+  V3<T> dir{T(0), T(0), T(0)};
+  T scan = T(0), step = T(0), thr = T(0), dist = T(0), detail = T(0);  // detail: detailSize of the march
+  int guardSteps = 0;
+  for (;;) {
+    // hand out jobs to idle lanes
+    const bool need = !active && !exhausted;
+    if (__any_sync(0xffffffffu, need)) {
+      if (io.budget_ns && (threadIdx.x & 31) == 0 && deadline_passed(io)) atomicExch(io.error_flag, 1);
+      const bool stop = *(volatile int *)io.error_flag != 0;
+      const unsigned int job = claim_jobs(jobCounter, need);
+      if (need) {
+        if (stop || job >= nTileJobs) {
+          exhausted = true;
+        } else {
+          int x, y;
+          if (io.overflow_pass) {
+            pix = (int)wb.overflow_list[job];
+            x = pix % p.width;
+            y = pix / p.width;
+          } else {
+            job_pixel(p.width, p.row_begin, job, x, y);
+            pix = y * p.width + x;
+          }
+          if (x < p.width && y < p.row_end) {
+            V3<double> view;
+            const bool marched = camera_ray(p, x, y, view);
+            dir = {(T)view.x, (T)view.y, (T)view.z};
+            scan = p.viewDistanceMin;
+            step = p.viewDistanceMin;
+            thr = T(0);
+            dist = T(0);
+            i = 0;
+            buffCount = 0;
+            iters = 0;
+            phase = 0;
+            bis = 0;
+            active = true;
+            if (!marched) {
+              // fisheye cut: no march, background with an empty step buffer
+              wb.flags[pix] = 2;
+              wb.scan[pix] = T(0);
+              wb.count[pix] = 0;
+              wb.iters[pix] = 0;
+              T* v = wb.vol;
+              v[0 * wb.npix + pix] = T(1);
+              for (int c = 1; c < 6; c++) v[c * wb.npix + pix] = T(0);
+              active = false;
+            }
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) {
+      if (__all_sync(0xffffffffu, exhausted || !active) && __all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    if (active) {
+      // one DE evaluation of the ray's current phase (0: march, 1: bisection)
+      const V3<T> point = start + dir * scan;
+      if (phase == 0) {
+        if (p.constantDEThreshold) thr = p.quality;
+        else if (f64) thr = scan * p.resolution * p.persp / p.quality;
+        else thr = scan * thrScale;
+        if (p.perspType == 1 || p.perspType == 2) thr *= T(kPI);
+        detail = thr;
+      }
+      bool mi;
+      dist = wave_distance<T, FORMULA, FAST>(p.f, point, detail, p.f.N, p.f.minN, false, iters, mi, cnt);
+      cnt.steps++;
+      bool done = false;
+      if (phase == 0) {
+        if (useSB && i >= stepCap) {
+          // more records than this slot holds: re-marched by the overflow pass
+          const unsigned int k = atomicAdd(wb.ctl + 3, 1u);
+          wb.overflow_list[k] = (unsigned int)pix;
+          active = false;
+          continue;
+        }
+        if (useSB) {
+          sb.dist[sb.at(i)] = dist;
+          sb.thr[sb.at(i)] = thr;
+        }
+        if (dist > T(3)) dist = T(3);
+        if (dist < thr) {
+          if (dist < T(0.1) * thr) cnt.missed++;
+          phase = 1;
+          step *= T(0.5);
+          bis = 0;
+          // FP64 policy and FP32 policy both continue with the bisection here; the FP32
+          // policy finishes it in FP64 in polish_kernel
+          if (dist < thr && dist > thr * search_limit) done = true;
+        } else {
+          if (useSB) sb.step[sb.at(i)] = step;
+          step = (dist - stepFrac * thr) * p.DE_factor;
+          if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)pix, (uint32_t)i)) / T(10000));
+          buffCount++;
+          scan += step;
+          i++;
+          if (scan > p.viewDistanceMax || i >= kMaxMarchSteps) done = true;
+        }
+        if (!done && phase == 1) {
+          // first bisection move (src/Render3D.cpp:151-167)
+          if (dist > thr) scan += step;
+          else if (dist < thr * search_limit) scan -= step;
+          if (p.constantDEThreshold) thr = p.quality;
+          else if (f64) thr = scan * p.resolution * p.persp / p.quality;
+          else thr = scan * thrScale;
+          bis = 1;
+        }
+      } else {
+        // bisection iteration `bis` evaluated; next check/move
+        step *= T(0.5);
+        if (bis >= 20 || (dist < thr && dist > thr * search_limit)) {
+          done = true;
+        } else {
+          if (dist > thr) scan += step;
+          else if (dist < thr * search_limit) scan -= step;
+          if (p.constantDEThreshold) thr = p.quality;
+          else if (f64) thr = scan * p.resolution * p.persp / p.quality;
+          else thr = scan * thrScale;
+          bis++;
+        }
+      }
+      if (++guardSteps > (1 << 24)) done = true;
+      if (done) {
+        const bool found = phase == 1;
+        T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
+        if (useSB) volumetric_affine<T>(p, sb, buffCount, scan, found ? T(1) : T(0), vol);
+        for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + pix] = vol[c];
+        wb.flags[pix] = found ? 1 : 0;
+        wb.scan[pix] = scan;
+        wb.dist[pix] = dist;
+        wb.thr[pix] = thr;
+        wb.step[pix] = step;
+        wb.detail[pix] = detail;
+        wb.bis_left[pix] = 20 - bis;
+        wb.count[pix] = buffCount;
+        wb.iters[pix] = iters;
+        const V3<T> hp = start + dir * scan;
+        wb.point[0 * wb.npix + pix] = (double)hp.x;
+        wb.point[1 * wb.npix + pix] = (double)hp.y;
+        wb.point[2 * wb.npix + pix] = (double)hp.z;
+        if (found) {
+          const unsigned int k = atomicAdd(wb.ctl + 1, 1u);
+          wb.hit_list[k] = (unsigned int)pix;
+        }
+        active = false;
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+    cnt.steps += __shfl_down_sync(0xffffffffu, cnt.steps, off);
+    cnt.missed += __shfl_down_sync(0xffffffffu, cnt.missed, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+    atomicAdd(&io.counters[2], cnt.steps);
+    atomicAdd(&io.counters[3], cnt.missed);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2 (FP32 policy): finish the binary refinement of every hit in FP64
+// (src/Render3D.cpp:145-183): the distance is re-evaluated in FP64 at the FP32
+// result and the bisection continues with the iterations it has left.
+// ---------------------------------------------------------------------------
+template <int FORMULA>
+__global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, const FractalT<double> fd,
+                                                     const FrameIO io, const WaveBufs<float> wb) {
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  Counters cnt{0, 0, 0, 0};
+  const double search_limit = 1.0 - 0.01 * p.quality_d;
+  const V3<double> start{p.start[0], p.start[1], p.start[2]};
+  for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += gridDim.x * blockDim.x) {
+    const unsigned int pix = wb.hit_list[k];
+    const int x = (int)(pix % (unsigned int)p.width), y = (int)(pix / (unsigned int)p.width);
+    V3<double> dir;
+    camera_ray(p, x, y, dir);
+    double scan = (double)wb.scan[pix];
+    double step = (double)wb.step[pix];
+    const double detail = (double)wb.detail[pix];
+    int left = wb.bis_left[pix];
+    auto thr_of = [&](double sc) {
+      return p.constantDEThreshold ? p.quality_d : sc * p.resolution_d * p.persp_d / p.quality_d;
+    };
+    double thr = thr_of(scan);
+    V3<double> point = start + dir * scan;
+    int iters = 0;
+    bool mi;
+    double dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt);
+    cnt.steps++;
+    for (int it = 0; it < left; it++) {
+      if (dist < thr && dist > thr * search_limit) break;
+      if (dist > thr) scan += step;
+      else if (dist < thr * search_limit) scan -= step;
+      point = start + dir * scan;
+      thr = thr_of(scan);
+      dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt);
+      cnt.steps++;
+      step *= 0.5;
+    }
+    wb.scan[pix] = (float)scan;
+    wb.dist[pix] = (float)dist;
+    wb.thr[pix] = (float)thr;
+    wb.iters[pix] = iters;
+    wb.point[0 * wb.npix + pix] = point.x;
+    wb.point[1 * wb.npix + pix] = point.y;
+    wb.point[2 * wb.npix + pix] = point.z;
+  }
+  atomicAdd(&io.counters[0], cnt.orbit);
+  atomicAdd(&io.counters[1], cnt.calls);
+  atomicAdd(&io.counters[2], cnt.steps);
+}
+
+// Shading-stage quantities of a hit pixel shared by the secondary and compose stages.
+template <typename T>
+struct HitInfo {
+  V3<T> point;
+  T thr, delta, scan;
+};
+
+template <typename T>
+__device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const WaveBufs<T> &wb, const unsigned int pix) {
+  HitInfo<T> h;
+  h.point = {(T)wb.point[0 * wb.npix + pix], (T)wb.point[1 * wb.npix + pix], (T)wb.point[2 * wb.npix + pix]};
+  h.thr = wb.thr[pix];
+  h.scan = wb.scan[pix];
+  h.delta = p.constantDEThreshold ? h.scan * p.resolution * p.persp : h.thr * p.quality;
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 3: shadow rays and ray-traced AO directions of all hits, lane refill.
+// Jobs [0, nShadow): one shadow ray per hit; then aoCount x hits AO rays,
+// direction-major so a warp's initial 32 rays share a direction.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA, bool FAST>
+__global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb) {
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  const unsigned int nShadow = p.shadow ? nh : 0u;
+  const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
+  const unsigned int njobs = nShadow + nAO;
+  Counters cnt{0, 0, 0, 0};
+  const V3<T> light{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
+  bool active = false, exhausted = false;
+  int kind = 0;
+  unsigned int pix = 0, j = 0;
+  V3<T> point{T(0), T(0), T(0)}, dir{T(0), T(0), T(0)};
+  T r = T(0), end = T(0), dist = T(0), sh = T(1), thr = T(0), detail = T(0), maxSoft = T(0), stepMul = T(0);
+  int guard = 0;
+  for (;;) {
+    const bool need = !active && !exhausted;
+    if (__any_sync(0xffffffffu, need)) {
+      if (io.budget_ns && (threadIdx.x & 31) == 0 && deadline_passed(io)) atomicExch(io.error_flag, 1);
+      const bool stop = *(volatile int *)io.error_flag != 0;
+      const unsigned int job = claim_jobs(wb.ctl + 2, need);
+      if (need) {
+        if (stop || job >= njobs) {
+          exhausted = true;
+        } else {
+          kind = job < nShadow ? 0 : 1;
+          if (kind == 0) {
+            pix = wb.hit_list[job];
+          } else {
+            const unsigned int q = job - nShadow;
+            j = q / nh;
+            pix = wb.hit_list[q % nh];
+          }
+          const HitInfo<T> h = hit_info(p, wb, pix);
+          point = h.point;
+          // MainShadow and AmbientOcclusion compare with the threshold stored in a float
+          thr = (T)(float)h.thr;
+          sh = T(1);
+          maxSoft = T(0);
+          guard = 0;
+          T factor = p.penetrating ? h.delta / p.resolution : p.viewDistanceMax;
+          const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
+          if (kind == 0) {
+            dir = light;
+            end = factor;
+            r = shadowStart;
+            dist = h.thr;
+            detail = thr;
+            stepMul = p.DE_factor;
+          } else {
+            dir = {__ldg(&p.aoVec[3 * j + 0]), __ldg(&p.aoVec[3 * j + 1]), __ldg(&p.aoVec[3 * j + 2])};
+            end = h.delta / p.resolution;
+            r = h.delta;
+            dist = wb.dist[pix];
+            // detailSize after MainShadow: the float threshold if its loop ran at least once
+            detail = (p.shadow && shadowStart < factor) ? thr : h.thr;
+            stepMul = T(2);
+          }
+          active = true;
+          if (!(r < end)) {  // loop body never runs
+            if (kind == 0) wb.shadow[pix] = p.softShadow ? T(1) : sh;
+            else wb.ao[(int64_t)j * wb.npix + pix] = sh;
+            active = false;
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    if (active) {
+      const V3<T> point2 = point + dir * r;
+      int L;
+      bool mi;
+      dist = wave_distance<T, FORMULA, FAST>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+      bool done = false;
+      if (kind == 0) {
+        if (p.softShadow) {
+          T angle = (dist - thr) / r;
+          if (angle < T(0)) angle = T(0);
+          if (dist < thr) angle = T(0);
+          T soft = (T(1) - angle / p.softRange);
+          if (p.penetrating) soft *= (end - r) / end;
+          if (soft < T(0)) soft = T(0);
+          if (soft > maxSoft) maxSoft = soft;
+        }
+        if (dist < thr || sh < T(0)) {
+          sh -= (end - r) / end;
+          if (!p.penetrating) sh = T(0);
+          if (sh < T(0)) sh = T(0);
+          done = true;
+        }
+      } else {
+        if (dist < thr || mi || sh < T(0)) {
+          sh -= (end - r) / end;
+          if (sh < T(0)) sh = T(0);
+          done = true;
+        }
+      }
+      if (!done) {
+        r += dist * stepMul;
+        if (!(r < end) || ++guard >= kMaxSecondarySteps) done = true;
+      }
+      if (done) {
+        if (kind == 0) wb.shadow[pix] = p.softShadow ? (T(1) - maxSoft) : sh;
+        else wb.ao[(int64_t)j * wb.npix + pix] = sh;
+        active = false;
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589).
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA, bool FAST>
+__global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb) {
+  Counters cnt{0, 0, 0, 0};
+  const int64_t first = (int64_t)p.row_begin * p.width;
+  const int64_t n = (int64_t)(p.row_end - p.row_begin) * p.width;
+  const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pix = first + k;
+    const int x = (int)(pix % p.width), y = (int)(pix / p.width);
+    const uint8_t flags = wb.flags[pix];
+    const bool hit = (flags & 1) != 0;
+    V3<double> view;
+    camera_ray(p, x, y, view);
+    const V3<T> viewT{(T)view.x, (T)view.y, (T)view.z};
+    T base[3];
+    V3<T> objColour{T(0), T(0), T(0)};
+    if (hit) {
+      const HitInfo<T> h = hit_info(p, wb, (unsigned int)pix);
+      // CalculateNormals (src/shaders.cpp:675-711): 4 DEs at N x 5, minN 0
+      T dn = h.delta * p.smoothness;
+      if (p.f.interiorMode) dn = h.thr * p.quality * T(0.2) * p.smoothness;
+      int L;
+      bool mi;
+      const int N5 = p.f.N5;
+      const T s1 = wave_distance<T, FORMULA, FAST>(p.f, h.point, h.thr, N5, 0, true, L, mi, cnt);
+      const T s2 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + dn, h.point.y + T(0), h.point.z + T(0)},
+                                                   h.thr, N5, 0, true, L, mi, cnt);
+      const T s3 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + T(0), h.point.y + dn, h.point.z + T(0)},
+                                                   h.thr, N5, 0, true, L, mi, cnt);
+      const T s4 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + T(0), h.point.y + T(0), h.point.z + dn},
+                                                   h.thr, N5, 0, true, L, mi, cnt);
+      V3<T> nrm{s2 - s1, s3 - s1, s4 - s1};
+      if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
+      else nrm = normalize3(nrm);
+      T shade = dot3(nrm, lv);
+      if (shade < T(0)) shade = T(0);
+      const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
+      const T shadow = p.shadow ? wb.shadow[pix] : T(1);
+      V3<T> half = normalize3(lv - viewT);
+      T shade2 = dot3(nrm, half);
+      if (shade2 < T(0)) shade2 = T(0);
+      shade2 = m_pow(shade2, T(30)) * T(1);
+      if (shade2 > T(15)) shade2 = T(15);
+      const T spec = shade2 * p.specular;
+      const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt);
+      objColour = colour;
+      V3<T> ambient{T(0), T(0), T(0)};
+      if (p.ao) {
+        if (p.fastAO) {
+          // detailSize after MainShadow: the float threshold if its loop ran
+          const T factor = p.penetrating ? h.delta / p.resolution : p.viewDistanceMax;
+          const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
+          const T detail = (p.shadow && shadowStart < factor) ? (T)(float)h.thr : h.thr;
+          const T a = fast_ao<T, FORMULA>(p, h.point, nrm, h.thr, detail, cnt);
+          ambient = {a, a, a};
+        } else {
+          T acc = T(0);
+          for (int jj = 0; jj < p.aoCount; jj++) acc += wb.ao[(int64_t)jj * wb.npix + pix] * p.aoWeight[0];
+          const T div = T(p.aoCount) * T(256);
+          ambient = {acc / div, acc / div, acc / div};
+        }
+      }
+      const T a2x = ambient.x * p.globalIlum, a2y = ambient.y * p.globalIlum, a2z = ambient.z * p.globalIlum;
+      const T objR = T(0) + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
+      const T objG = T(0) + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
+      const T objB = T(0) + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
+      base[0] = objR + T(0) + (T(0) + p.mainLight[0] * spec * shadow);
+      base[1] = objG + T(0) + (T(0) + p.mainLight[1] * spec * shadow);
+      base[2] = objB + T(0) + (T(0) + p.mainLight[2] * spec * shadow);
+    } else {
+      const V3<T> bg = background(p, viewT);
+      base[0] = T(0) + bg.x + T(0);
+      base[1] = T(0) + bg.y + T(0);
+      base[2] = T(0) + bg.z + T(0);
+    }
+    const T A = wb.vol[0 * wb.npix + pix];
+    const T out0 = A * base[0] + wb.vol[1 * wb.npix + pix];
+    const T out1 = A * base[1] + wb.vol[2 * wb.npix + pix];
+    const T out2 = A * base[2] + wb.vol[3 * wb.npix + pix];
+    const T alpha = wb.vol[4 * wb.npix + pix];
+    const T opacity = wb.vol[5 * wb.npix + pix];
+    const double depth = hit ? (double)wb.scan[pix] : 1e20;
+    if (io.opacity) io.opacity[pix] = to_u16_x86((double)opacity * 65535.0);
+    if (io.alpha) io.alpha[pix] = to_u16_x86((double)alpha * 65535.0);
+    if (io.image_float) {
+      io.image_float[3 * pix + 0] = (float)out0;
+      io.image_float[3 * pix + 1] = (float)out1;
+      io.image_float[3 * pix + 2] = (float)out2;
+    }
+    if (io.colour) {
+      io.colour[3 * pix + 0] = to_u8_x86((double)(objColour.x * T(255)));
+      io.colour[3 * pix + 1] = to_u8_x86((double)(objColour.y * T(255)));
+      io.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
+    }
+    if (io.zbuffer) io.zbuffer[pix] = (float)depth;
+    if (io.hit) io.hit[pix] = hit ? 1 : 0;
+    if (io.iters) io.iters[pix] = wb.iters[pix];
+    if (io.depth) io.depth[pix] = depth;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+  }
+}
+
+}  // namespace dev
+}  // namespace mbgb

@@ -1,0 +1,41 @@
+// Instantiation of the wavefront kernels for T = float.
+#include "wave_core.cuh"
+#include "wave_launch.h"
+
+namespace mbgb {
+
+template <int F, bool FAST>
+static cudaError_t run_stages_f32(const WaveLaunch<float> &L, cudaStream_t s) {
+  if (L.ev[0]) cudaEventRecord(L.ev[0], s);
+  dev::primary_kernel<float, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb);
+  if (L.overflow)
+    dev::primary_kernel<float, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb);
+  if (L.ev[0]) cudaEventRecord(L.ev[1], s);
+  dev::polish_kernel<F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), L.wb);
+  if (L.ev[0]) cudaEventRecord(L.ev[2], s);
+  dev::secondary_kernel<float, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb);
+  if (L.ev[0]) cudaEventRecord(L.ev[3], s);
+  dev::compose_kernel<float, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb);
+  if (L.ev[0]) cudaEventRecord(L.ev[4], s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wave_f32(const WaveLaunch<float> &L, cudaStream_t s) {
+  if (L.p.f.formula == 2) return L.fast ? run_stages_f32<2, true>(L, s) : run_stages_f32<2, false>(L, s);
+  if (L.p.f.formula == 8) return L.fast ? run_stages_f32<8, true>(L, s) : run_stages_f32<8, false>(L, s);
+  return cudaErrorInvalidValue;
+}
+
+int occupancy_wave_f32(int formula, int block, int which) {
+  int n = 0;
+  if (which == 0) {
+    if (formula == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<float, 2, true>, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<float, 8, true>, block, 0);
+  } else {
+    if (formula == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<float, 2, true>, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<float, 8, true>, block, 0);
+  }
+  return n;
+}
+
+}  // namespace mbgb

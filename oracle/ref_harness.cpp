@@ -24,6 +24,7 @@
 #include "fractal.h"
 #include "mbgb.h"
 #include "shaders.h"
+#include "morph.hpp"
 
 guint64 N_counter = 0;
 guint64 Loop_counter = 0;
@@ -407,5 +408,13 @@ int ref_render(const mbgb_scene *s, int row0, int row1, int jitter, const mbgb_i
 }
 
 unsigned long long ref_orbit_counter(void) { return N_counter; }
+
+// CMorph::CatmullRom (src/morph.cpp) over keys[n_keys][size] for frames [0, n_frames).
+void ref_catmull_rom(const double *keys, int n_keys, int size, int frames_per_key, int n_frames, double *out) {
+  CMorph m(n_keys, size);
+  m.SetFramesPerKey(frames_per_key);
+  for (int k = 0; k < n_keys; k++) m.AddData(k, const_cast<double *>(keys + (size_t)k * size));
+  for (int f = 0; f < n_frames; f++) m.CatmullRom(f, out + (size_t)f * size);
+}
 
 }  // extern "C"

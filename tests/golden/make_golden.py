@@ -127,6 +127,24 @@ def main():
         manifest[os.path.basename(out)] = {"workload": wl, "size": [w, h], "keys": extra,
                                            "hit_fraction": float(img.hit.mean())}
         print(case, "hit", img.hit.mean())
+    # CMorph::CatmullRom (src/morph.cpp:49-109) on seeded rows covering its branches:
+    # same-sign rows with large variation (logarithmic mode), negative rows, mixed signs,
+    # near-constant rows, rows crossing +-1e20 and values below 1e-20
+    rng = np.random.default_rng(4242)
+    n_keys, size, fpk = 8, 64, 8
+    keys = np.empty((n_keys, size))
+    keys[:, 0:12] = rng.uniform(0.1, 10.0, (n_keys, 12))
+    keys[:, 12:24] = -rng.uniform(0.1, 10.0, (n_keys, 12))
+    keys[:, 24:36] = rng.uniform(-3.0, 3.0, (n_keys, 12))
+    keys[:, 36:44] = 5.0 + rng.uniform(-0.01, 0.01, (n_keys, 8))
+    keys[:, 44:50] = rng.uniform(1e19, 9e20, (n_keys, 6)) * np.where(rng.random((n_keys, 6)) < 0.5, -1, 1)
+    keys[:, 50:56] = rng.uniform(-1e-19, 1e-19, (n_keys, 6))
+    keys[:, 56:64] = np.cumsum(rng.normal(0, 1, (n_keys, 8)), axis=0)
+    keys = np.ascontiguousarray(keys)
+    out = np.zeros((n_keys * fpk, size))
+    lib.ref_catmull_rom(ptr(keys), n_keys, size, fpk, n_keys * fpk, ptr(out))
+    np.savez_compressed(os.path.join(HERE, "catmull_rom.npz"), keys=keys, frames_per_key=fpk, out=out)
+    manifest["catmull_rom.npz"] = {"keys": [n_keys, size], "frames_per_key": fpk}
     with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 

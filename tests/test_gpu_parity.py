@@ -82,12 +82,16 @@ def test_distance_fp32_close(gpu_ctx, formula):
     assert np.median(rel) < 1e-4, np.median(rel)
 
 
+ENGINES = [mb.ENGINE_WAVEFRONT, mb.ENGINE_PER_PIXEL]
+
+
+@pytest.mark.parametrize("engine", ENGINES, ids=["wavefront", "per_pixel"])
 @pytest.mark.parametrize("case", RENDERS)
-def test_render_fp64_against_reference_golden(gpu_ctx, case):
+def test_render_fp64_against_reference_golden(gpu_ctx, case, engine):
     """FP64 device render vs the reference's own output (golden vectors)."""
     z = np.load(os.path.join(GOLDEN, f"render_{case}.npz"))
     sc = mb.scene_from_bytes(z["scene"].tobytes())
-    img = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=engine)
     ref = _golden_image(z, sc.image_width, sc.image_height)
     m = metrics.compare(img, ref)
     if sc.formula == 8 and sc.perspectiveType == 0:
@@ -101,12 +105,13 @@ def test_render_fp64_against_reference_golden(gpu_ctx, case):
         assert m["psnr_float"] >= 35.0, m
 
 
+@pytest.mark.parametrize("engine", ENGINES, ids=["wavefront", "per_pixel"])
 @pytest.mark.parametrize("name,size", [("mandelbulb_640x480", (320, 240)), ("mandelbox_1080p", (480, 270))])
-def test_render_fp32_fix_against_oracle(gpu_ctx, oracle, name, size):
+def test_render_fp32_fix_against_oracle(gpu_ctx, oracle, name, size, engine):
     """FP32 march + FP64 refinement vs the FP64 oracle: <= 0.1 % hit mismatch, >= 45 dB."""
     sc = W.workload(name, *size)
     ref, _ = oracle_lib.render(oracle, sc)
-    img = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, engine=engine)
     m = metrics.compare(img, ref)
     print(name, m)
     assert m["hit_mismatch"] <= 0.001, m
@@ -119,16 +124,21 @@ def test_full_size_fp32_fix_against_fp64(gpu_ctx):
     a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
     b = gpu_ctx.render(sc, precision=mb.PREC_FP64)
     m = metrics.compare(a, b)
+    c = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=mb.ENGINE_PER_PIXEL)
+    # the two engines agree exactly in FP64 on hits and depth
+    np.testing.assert_array_equal(b.hit, c.hit)
+    np.testing.assert_array_equal(b.depth, c.depth)
     print(m)
     assert m["hit_mismatch"] <= 0.001, m
     assert m["psnr_float"] >= 45.0, m
 
 
-def test_long_rays_take_the_overflow_pass(gpu_ctx, oracle):
+@pytest.mark.parametrize("engine", ENGINES, ids=["wavefront", "per_pixel"])
+def test_long_rays_take_the_overflow_pass(gpu_ctx, oracle, engine):
     """Rays longer than the main pass's step records are re-rendered with full-length records."""
     sc = W.workload("mandelbox_1080p", 96, 54, DE_factor=0.01)
     ref, _ = oracle_lib.render(oracle, sc)
-    img = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=engine)
     assert gpu_ctx.stats().long_rays > 0
     for k in ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]:
         np.testing.assert_array_equal(getattr(img, k), getattr(ref, k), err_msg=k)
