@@ -187,7 +187,9 @@ typedef struct mbgb_image {
 enum {
   MBGB_PREC_FP64 = 0,          /* every DE evaluation and every march in double */
   MBGB_PREC_FP32_FIX = 1,      /* FP32 march/orbit with FP64 camera origin and FP64 hit refinement */
-  MBGB_PREC_AUTO = 2           /* FP32_FIX unless the pixel footprint is below ~1e-5 of scene scale, then FP64 */
+  MBGB_PREC_AUTO = 2           /* FP32_FIX unless the pixel footprint at the nearest surface (FP64 distance
+                                * estimate at the ray origin x resolution x persp / quality) is below 1e-5 of
+                                * the scene scale, then FP64 for the whole frame; the probe synchronises */
 };
 
 typedef struct mbgb_opts {
@@ -201,6 +203,8 @@ typedef struct mbgb_opts {
   void *stream;                /* cudaStream_t; NULL = the context's stream */
   int32_t engine;              /* MBGB_ENGINE_*; 0 = wavefront stages */
   int32_t profile_stages;      /* 1: record CUDA events between stages (synchronous calls fill stage_ms) */
+  int32_t polish_all;          /* FP32_FIX: 1 = re-run the end of every hit's bisection in FP64; 0 = only the
+                                * hits whose FP32 window decision is within 1e-4 of an edge */
 } mbgb_opts;
 
 /* Render engines (same results within the precision policy's tolerance). */
@@ -218,6 +222,8 @@ typedef struct mbgb_stats {
   uint64_t pixels;             /* Pixel_counter */
   uint64_t missed_de;          /* Missed_DE_counter */
   uint64_t long_rays;          /* primary rays longer than the main pass's step records (re-rendered) */
+  uint64_t fp64_polished;      /* FP32_FIX, wavefront: hits whose bisection was finished in FP64 */
+  uint64_t auto_fp64;          /* MBGB_PREC_AUTO: 1 if the last frame was rendered in FP64 */
   double kernel_ms;            /* device time of the last render */
   /* per stage: [0] primary rays (wavefront) or the per-pixel kernel, [1] FP64 hit polish,
    * [2] shadow and AO rays, [3] composition */

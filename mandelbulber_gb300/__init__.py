@@ -146,11 +146,12 @@ ENGINE_WAVEFRONT, ENGINE_PER_PIXEL = 0, 1
 
 def make_opts(precision: int = PREC_FP32_FIX, jitter: bool = False, jitter_seed: int = 0, rows=None,
               ctas_per_sm: int = 0, threads_per_cta: int = 0, deadline_ms: int = 0, stream: int = 0,
-              engine: int = ENGINE_WAVEFRONT, profile_stages: bool = False) -> mbgb_opts:
+              engine: int = ENGINE_WAVEFRONT, profile_stages: bool = False, polish_all: bool = False) -> mbgb_opts:
     r0, r1 = rows if rows else (0, 0)
     return mbgb_opts(precision=precision, jitter=int(jitter), jitter_seed=jitter_seed, row_begin=r0, row_end=r1,
                      ctas_per_sm=ctas_per_sm, threads_per_cta=threads_per_cta, deadline_ms=deadline_ms,
-                     stream=stream if stream else None, engine=engine, profile_stages=int(profile_stages))
+                     stream=stream if stream else None, engine=engine, profile_stages=int(profile_stages),
+                     polish_all=int(polish_all))
 
 
 class Context:

@@ -24,12 +24,18 @@ struct WaveBufs {
   uint8_t *flags;
   T *scan, *dist, *thr, *step, *detail;
   int32_t *bis_left;
-  double *point;
+  T *point;
   int32_t *iters, *count;
   T *vol, *shadow, *ao;
-  uint32_t *hit_list, *ctl, *overflow_list;
+  uint32_t *hit_list, *polish_list, *ctl, *overflow_list;
+  T *pool_step, *pool_dist, *pool_thr;
+  int32_t *pool_prev, *last_chunk;
+  uint32_t pool_cap;
+  int polish_all;
   int64_t npix;
 };
+constexpr int kChunk = 32;
+constexpr int kPoolChunksPerPixel = 4;
 }  // namespace mbgb
 
 namespace mbgb {
@@ -187,6 +193,7 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   rot.rotX(s.beta);
   rot.rotY(s.gamma);
   memcpy(p.rot, rot.m, sizeof(p.rot));
+  for (int i = 0; i < 9; i++) p.rotf[i] = (float)rot.m[i];
   p.rot_zero = rot.zero;
   const double by[3] = {0.0, 1.0, 0.0};
   double baseY[3];
@@ -328,6 +335,7 @@ struct mbgb_context {
   int ao_count = 0;
   DeviceBuf out[8];               // device staging for mbgb_render_host
   DeviceBuf wave[2];              // wavefront per-pixel buffers, per precision
+  DeviceBuf probe;                // MBGB_PREC_AUTO: one-point distance probe
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t sev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // stage events
   mbgb_stats stats{};
@@ -404,6 +412,7 @@ extern "C" void mbgb_context_destroy(mbgb_context *c) {
     for (auto &b : a) b.release();
   c->ovlist.release();
   for (auto &b : c->wave) b.release();
+  c->probe.release();
   c->control.release();
   c->ao64.release();
   c->ao32.release();
@@ -470,9 +479,13 @@ static mbgb_status render_wave(mbgb_context *c, const mbgb_scene *scene, const m
   const size_t ts = sizeof(T);
   const size_t o_flags = take(npix), o_scan = take(npix * ts), o_dist = take(npix * ts), o_thr = take(npix * ts);
   const size_t o_step = take(npix * ts), o_detail = take(npix * ts), o_bis = take(npix * 4);
-  const size_t o_point = take(3 * npix * 8), o_iters = take(npix * 4), o_count = take(npix * 4);
+  const size_t o_point = take(3 * npix * ts), o_iters = take(npix * 4), o_count = take(npix * 4);
   const size_t o_vol = take(6 * npix * ts), o_shadow = take(npix * ts), o_ao = take((size_t)aoN * npix * ts);
-  const size_t o_hit = take(npix * 4), o_ovl = take(npix * 4), o_ctl = take(64);
+  const size_t o_hit = take(npix * 4), o_pol = take(npix * 4), o_ovl = take(npix * 4), o_ctl = take(64);
+  const size_t o_last = take(npix * 4);
+  const uint32_t poolCap = needVol ? (uint32_t)std::min<int64_t>(npix * kPoolChunksPerPixel, 0x7fffffff) : 1u;
+  const size_t o_pstep = take((size_t)poolCap * kChunk * ts), o_pdist = take((size_t)poolCap * kChunk * ts);
+  const size_t o_pthr = take((size_t)poolCap * kChunk * ts), o_pprev = take((size_t)poolCap * 4);
   MBGB_CUDA(c->wave[prec].ensure(off));
   char *base = (char *)c->wave[prec].ptr;
   WaveLaunch<T> L;
@@ -484,15 +497,23 @@ static mbgb_status render_wave(mbgb_context *c, const mbgb_scene *scene, const m
   wb.step = (T *)(base + o_step);
   wb.detail = (T *)(base + o_detail);
   wb.bis_left = (int32_t *)(base + o_bis);
-  wb.point = (double *)(base + o_point);
+  wb.point = (T *)(base + o_point);
   wb.iters = (int32_t *)(base + o_iters);
   wb.count = (int32_t *)(base + o_count);
   wb.vol = (T *)(base + o_vol);
   wb.shadow = (T *)(base + o_shadow);
   wb.ao = (T *)(base + o_ao);
   wb.hit_list = (uint32_t *)(base + o_hit);
+  wb.polish_list = (uint32_t *)(base + o_pol);
   wb.overflow_list = (uint32_t *)(base + o_ovl);
   wb.ctl = (uint32_t *)(base + o_ctl);
+  wb.last_chunk = (int32_t *)(base + o_last);
+  wb.pool_step = (T *)(base + o_pstep);
+  wb.pool_dist = (T *)(base + o_pdist);
+  wb.pool_thr = (T *)(base + o_pthr);
+  wb.pool_prev = (int32_t *)(base + o_pprev);
+  wb.pool_cap = poolCap;
+  wb.polish_all = o.polish_all;
   wb.npix = npix;
   MBGB_CUDA(cudaMemsetAsync(wb.ctl, 0, 64, s));
 
@@ -565,7 +586,32 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
     return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
   MBGB_CUDA(cudaSetDevice(c->device));
   cudaStream_t s = o.stream ? (cudaStream_t)o.stream : c->stream;
-  const int prec = (o.precision == MBGB_PREC_FP64) ? 0 : 1;
+  int prec = (o.precision == MBGB_PREC_FP64) ? 0 : 1;
+  if (o.precision == MBGB_PREC_AUTO) {
+    // Deep-zoom rule: FP64 for the whole frame when the pixel footprint at the nearest
+    // surface, d * resolution * persp / quality with d the FP64 distance estimate at the
+    // ray origin, is below 1e-5 of the scene scale (max(1, |origin|)).
+    ParamsT<double> pp;
+    fill_params<double>(*scene, pp, o, nullptr, 0);
+    double host[5] = {pp.start[0], pp.start[1], pp.start[2], 0.0, 0.0};
+    host[3] = 1e-300;
+    MBGB_CUDA(c->probe.ensure(128));
+    char *pb = (char *)c->probe.ptr;
+    MBGB_CUDA(cudaMemcpyAsync(pb, host, 4 * sizeof(double), cudaMemcpyHostToDevice, s));
+    FractalT<double> fp;
+    fill_fractal<double>(*scene, fp);
+    cudaError_t pe = launch_distance_f64(scene->formula, fp, (const double *)pb, (const double *)(pb + 24), 1,
+                                         (double *)(pb + 32), (int *)(pb + 40), (unsigned char *)(pb + 44), nullptr, s);
+    if (pe != cudaSuccess) return cuda_error(pe, "precision probe");
+    double d = 0.0;
+    MBGB_CUDA(cudaMemcpyAsync(&d, pb + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MBGB_CUDA(cudaStreamSynchronize(s));
+    const double scale = std::max(1.0, sqrt(host[0] * host[0] + host[1] * host[1] + host[2] * host[2]));
+    const double footprint = scene->constantDEThreshold ? scene->quality
+                                                        : d * scene->resolution * scene->persp / scene->quality;
+    prec = footprint < 1e-5 * scale ? 0 : 1;
+    c->stats.auto_fp64 = prec == 0;
+  }
   st = ensure_ao(c, scene->globalIlumQuality, s);
   if (st != MBGB_OK) return st;
 
@@ -674,6 +720,12 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
     MBGB_CUDA(cudaMemcpy(&flag, ctl + 16, sizeof(flag), cudaMemcpyDeviceToHost));
     MBGB_CUDA(cudaMemcpy(&nover, longRays, sizeof(nover), cudaMemcpyDeviceToHost));
     c->stats.long_rays = nover;
+    c->stats.fp64_polished = 0;
+    if (wave && prec == 1) {
+      uint32_t npol = 0;
+      MBGB_CUDA(cudaMemcpy(&npol, longRays + 3, sizeof(npol), cudaMemcpyDeviceToHost));
+      c->stats.fp64_polished = npol;
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     c->stats.orbit_iterations = cnt[0];

@@ -52,6 +52,7 @@ struct ParamsT {
   int row_begin, row_end;
   double tileXOffset, tileYOffset, aspect, fov;
   double rot[9];
+  float rotf[9];     // FP32 copy for the FP32 policy's camera rays
   int rot_zero;
   double start[3];
   // march (src/Render3D.cpp:79-199)

@@ -35,18 +35,29 @@ struct WaveBufs {
   T *step;               // [npix] FP32 policy: bisection step left for the FP64 polish
   T *detail;             // [npix] detailSize of the march's last step (src/Render3D.cpp:110)
   int32_t *bis_left;     // [npix] FP32 policy: bisection iterations left
-  double *point;         // [3][npix] hit point
+  T *point;              // [3][npix] hit point in the march precision
   int32_t *iters;        // [npix] itersOut at the end of the march
   int32_t *count;        // [npix] buffCount
-  T *vol;                // [6][npix] A, B.r, B.g, B.b, alpha, opacity
+  T *vol;                // [6][npix] overflow pass only: A, B.r, B.g, B.b, alpha, opacity
   T *shadow;             // [npix]
   T *ao;                 // [aoCount][npix] per-direction shadowTemp
-  uint32_t *hit_list;    // [npix]
-  uint32_t *ctl;         // [0] primary jobs taken, [1] hits, [2] secondary jobs taken, [3] overflow
-                         // count, [4] overflow-pass jobs taken (zeroed before the frame)
+  uint32_t *hit_list;    // [npix] hits (secondary rays)
+  uint32_t *polish_list; // [npix] hits the FP64 polish re-evaluates
+  uint32_t *ctl;         // [0] primary jobs, [1] hits, [2] secondary jobs, [3] overflow count,
+                         // [4] overflow-pass jobs, [5] pool chunks, [6] polish count (zeroed per frame)
   uint32_t *overflow_list;
+  // Step records of the primary rays: chunks of kChunk records linked backwards
+  // (prev), allocated by bump counter; the pixel keeps its last chunk.
+  T *pool_step, *pool_dist, *pool_thr;   // [chunk * kChunk + r]
+  int32_t *pool_prev;                    // [chunk]
+  int32_t *last_chunk;                   // [npix], -1 = no records
+  uint32_t pool_cap;                     // chunks
+  int polish_all;                        // 1: every hit takes the FP64 polish
   int64_t npix;
 };
+
+constexpr int kChunk = 32;       // step records per pool chunk
+constexpr int kPoolChunksPerPixel = 4;   // pool budget; rays beyond it take the overflow pass
 
 namespace dev {
 
@@ -244,6 +255,33 @@ __device__ __forceinline__ bool camera_ray(const ParamsT<T> &p, const int x, con
   return !cut;
 }
 
+// Camera ray in the march precision: the FP32 policy forms the three-point-perspective
+// direction in FP32 (the per-frame ray origin stays the FP64 value from the host); the
+// FP64 policy and the fisheye/equirectangular projections use camera_ray below.
+template <typename T>
+__device__ __forceinline__ bool camera_dir(const ParamsT<T> &p, const int x, const int y, V3<T> &dir) {
+  if (sizeof(T) == 4 && p.perspType != 1 && p.perspType != 2) {
+    const float x2 = ((float)x / (float)p.width / (float)p.tiles - 0.5f + (float)p.tileXOffset / (float)p.tiles) *
+                     (float)p.aspect;
+    const float z2 = ((float)y / (float)p.height / (float)p.tiles - 0.5f + (float)p.tileYOffset / (float)p.tiles);
+    const float fov = (float)p.fov;
+    const V3<float> vv{x2 * fov, 1.0f, z2 * fov};
+    if (p.rot_zero) {
+      dir = {(T)vv.x, (T)vv.y, (T)vv.z};
+    } else {
+      dir = {(T)(p.rotf[0] * vv.x + p.rotf[1] * vv.y + p.rotf[2] * vv.z),
+             (T)(p.rotf[3] * vv.x + p.rotf[4] * vv.y + p.rotf[5] * vv.z),
+             (T)(p.rotf[6] * vv.x + p.rotf[7] * vv.y + p.rotf[8] * vv.z)};
+    }
+    return true;
+  }
+  V3<double> view;
+  const bool ok = camera_ray(p, x, y, view);
+  dir = {(T)view.x, (T)view.y, (T)view.z};
+  return ok;
+}
+
+
 // The volumetric pass over one ray's records (VolumetricShader's glow, post fog and
 // volumetric fog, src/shaders.cpp:185-478) as the affine map out = A*base + B, plus
 // the alpha and opacity it leaves for a base alpha of `alpha0`.
@@ -345,6 +383,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
   // per-lane ray state
   bool active = false, exhausted = false;
   int pix = 0, phase = 0, i = 0, buffCount = 0, iters = 0, bis = 0;
+  int chunk = -1;   // current pool chunk of the ray's step records (main pass)
   V3<T> dir{T(0), T(0), T(0)};
   T scan = T(0), step = T(0), thr = T(0), dist = T(0), detail = T(0);  // detail: detailSize of the march
   int guardSteps = 0;
@@ -369,9 +408,8 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
             pix = y * p.width + x;
           }
           if (x < p.width && y < p.row_end) {
-            V3<double> view;
-            const bool marched = camera_ray(p, x, y, view);
-            dir = {(T)view.x, (T)view.y, (T)view.z};
+            const bool marched = camera_dir(p, x, y, dir);
+            chunk = -1;
             scan = p.viewDistanceMin;
             step = p.viewDistanceMin;
             thr = T(0);
@@ -388,9 +426,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
               wb.scan[pix] = T(0);
               wb.count[pix] = 0;
               wb.iters[pix] = 0;
-              T* v = wb.vol;
-              v[0 * wb.npix + pix] = T(1);
-              for (int c = 1; c < 6; c++) v[c * wb.npix + pix] = T(0);
+              wb.last_chunk[pix] = -1;
               active = false;
             }
           }
@@ -416,16 +452,34 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
       cnt.steps++;
       bool done = false;
       if (phase == 0) {
-        if (useSB && i >= stepCap) {
-          // more records than this slot holds: re-marched by the overflow pass
-          const unsigned int k = atomicAdd(wb.ctl + 3, 1u);
-          wb.overflow_list[k] = (unsigned int)pix;
-          active = false;
-          continue;
-        }
+        int64_t rec = 0;
         if (useSB) {
-          sb.dist[sb.at(i)] = dist;
-          sb.thr[sb.at(i)] = thr;
+          if (io.overflow_pass) {
+            sb.dist[sb.at(i)] = dist;
+            sb.thr[sb.at(i)] = thr;
+          } else {
+            // main pass: records go to the frame's pool in chunks of kChunk
+            bool full = false;
+            if ((i % kChunk) == 0) {
+              const unsigned int c = atomicAdd(wb.ctl + 5, 1u);
+              if (c >= wb.pool_cap) {
+                full = true;
+              } else {
+                wb.pool_prev[c] = chunk;
+                chunk = (int)c;
+              }
+            }
+            if (full) {
+              // the pool is spent: re-marched by the overflow pass with slot records
+              const unsigned int k = atomicAdd(wb.ctl + 3, 1u);
+              wb.overflow_list[k] = (unsigned int)pix;
+              active = false;
+              continue;
+            }
+            rec = (int64_t)chunk * kChunk + (i % kChunk);
+            wb.pool_dist[rec] = dist;
+            wb.pool_thr[rec] = thr;
+          }
         }
         if (dist > T(3)) dist = T(3);
         if (dist < thr) {
@@ -437,7 +491,10 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
           // policy finishes it in FP64 in polish_kernel
           if (dist < thr && dist > thr * search_limit) done = true;
         } else {
-          if (useSB) sb.step[sb.at(i)] = step;
+          if (useSB) {
+            if (io.overflow_pass) sb.step[sb.at(i)] = step;
+            else wb.pool_step[rec] = step;
+          }
           step = (dist - stepFrac * thr) * p.DE_factor;
           if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)pix, (uint32_t)i)) / T(10000));
           buffCount++;
@@ -471,10 +528,16 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
       if (++guardSteps > (1 << 24)) done = true;
       if (done) {
         const bool found = phase == 1;
-        T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
-        if (useSB) volumetric_affine<T>(p, sb, buffCount, scan, found ? T(1) : T(0), vol);
-        for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + pix] = vol[c];
-        wb.flags[pix] = found ? 1 : 0;
+        uint8_t flags = found ? 1 : 0;
+        if (io.overflow_pass && useSB) {
+          // rare long rays: fold the records now (the slot is reused); compose applies the map
+          T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
+          volumetric_affine<T>(p, sb, buffCount, scan, found ? T(1) : T(0), vol);
+          for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + pix] = vol[c];
+          flags |= 4;
+        }
+        wb.flags[pix] = flags;
+        wb.last_chunk[pix] = chunk;
         wb.scan[pix] = scan;
         wb.dist[pix] = dist;
         wb.thr[pix] = thr;
@@ -484,12 +547,22 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
         wb.count[pix] = buffCount;
         wb.iters[pix] = iters;
         const V3<T> hp = start + dir * scan;
-        wb.point[0 * wb.npix + pix] = (double)hp.x;
-        wb.point[1 * wb.npix + pix] = (double)hp.y;
-        wb.point[2 * wb.npix + pix] = (double)hp.z;
+        wb.point[0 * wb.npix + pix] = hp.x;
+        wb.point[1 * wb.npix + pix] = hp.y;
+        wb.point[2 * wb.npix + pix] = hp.z;
         if (found) {
           const unsigned int k = atomicAdd(wb.ctl + 1, 1u);
           wb.hit_list[k] = (unsigned int)pix;
+          // FP32 policy: the FP64 polish re-checks every hit whose FP32 bisection did not end
+          // clearly inside the window (dist/thr within 1e-4 of an edge, or 20 steps used)
+          if (!f64) {
+            const T q = dist / thr;
+            const bool clear = (q > search_limit + T(1e-4)) && (q < T(1) - T(1e-4));
+            if (wb.polish_all || !clear) {
+              const unsigned int m = atomicAdd(wb.ctl + 6, 1u);
+              wb.polish_list[m] = (unsigned int)pix;
+            }
+          }
         }
         active = false;
       }
@@ -517,12 +590,12 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
 template <int FORMULA>
 __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, const FractalT<double> fd,
                                                      const FrameIO io, const WaveBufs<float> wb) {
-  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[6];
   Counters cnt{0, 0, 0, 0};
   const double search_limit = 1.0 - 0.01 * p.quality_d;
   const V3<double> start{p.start[0], p.start[1], p.start[2]};
   for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += gridDim.x * blockDim.x) {
-    const unsigned int pix = wb.hit_list[k];
+    const unsigned int pix = wb.polish_list[k];
     const int x = (int)(pix % (unsigned int)p.width), y = (int)(pix / (unsigned int)p.width);
     V3<double> dir;
     camera_ray(p, x, y, dir);
@@ -553,9 +626,9 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
     wb.dist[pix] = (float)dist;
     wb.thr[pix] = (float)thr;
     wb.iters[pix] = iters;
-    wb.point[0 * wb.npix + pix] = point.x;
-    wb.point[1 * wb.npix + pix] = point.y;
-    wb.point[2 * wb.npix + pix] = point.z;
+    wb.point[0 * wb.npix + pix] = (float)point.x;
+    wb.point[1 * wb.npix + pix] = (float)point.y;
+    wb.point[2 * wb.npix + pix] = (float)point.z;
   }
   atomicAdd(&io.counters[0], cnt.orbit);
   atomicAdd(&io.counters[1], cnt.calls);
@@ -572,7 +645,7 @@ struct HitInfo {
 template <typename T>
 __device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const WaveBufs<T> &wb, const unsigned int pix) {
   HitInfo<T> h;
-  h.point = {(T)wb.point[0 * wb.npix + pix], (T)wb.point[1 * wb.npix + pix], (T)wb.point[2 * wb.npix + pix]};
+  h.point = {wb.point[0 * wb.npix + pix], wb.point[1 * wb.npix + pix], wb.point[2 * wb.npix + pix]};
   h.thr = wb.thr[pix];
   h.scan = wb.scan[pix];
   h.delta = p.constantDEThreshold ? h.scan * p.resolution * p.persp : h.thr * p.quality;
@@ -704,6 +777,90 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
   }
 }
 
+// Backward walk over a ray's pooled records: record `index` of a chain whose last chunk
+// holds the records from kChunk * (nchunks - 1) on.
+template <typename T>
+struct PoolRecords {
+  const T *step, *dist, *thr;
+  const int32_t *prev;
+  int32_t last;      // chunk holding the last written record
+  int lastRec;       // index of the last written record: buffCount for a hit (its hit step
+                     // writes distance and threshold), buffCount - 1 otherwise
+};
+
+// VolumetricShader (src/shaders.cpp:185-478; glow, post fog, volumetric fog) reading the
+// pooled records far to near; same arithmetic as `volumetric` in render_core.cuh.
+template <typename T>
+__device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolRecords<T> &pr, const int stepCount,
+                                                const T depth, T out[4], float &totalOpacityOut, bool &opacitySet) {
+  float totalOpacity = 0.0f;
+  const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
+  T glowN = T(1) - glow;
+  if (glowN < T(0)) glowN = T(0);
+  const T glowR = (T(p.glow1[0]) * glowN + T(p.glow2[0]) * glow) / T(65536);
+  const T glowG = (T(p.glow1[1]) * glowN + T(p.glow2[1]) * glow) / T(65536);
+  const T glowB = (T(p.glow1[2]) * glowN + T(p.glow2[2]) * glow) / T(65536);
+  const T fogIntensity = p.fogDensity;
+  T totalStep = T(0);
+  int32_t chunk = pr.last;
+  int chunkBase = (pr.lastRec / kChunk) * kChunk;   // first record index of `chunk`
+  for (int index = stepCount - 1; index > 0; index--) {
+    while (index < chunkBase) {
+      chunk = pr.prev[chunk];
+      chunkBase -= kChunk;
+    }
+    const int64_t rec = (int64_t)chunk * kChunk + (index - chunkBase);
+    T step = pr.step[rec];
+    const T distance = pr.dist[rec];
+    const T dist_thresh = pr.thr[rec];
+    totalStep += step;
+    if (totalStep < dist_thresh * p.quality) continue;
+    step = totalStep;
+    totalStep = T(0);
+    const T glowOpacity = glow * step / depth;
+    out[0] = glowOpacity * glowR + (T(1) - glowOpacity) * out[0];
+    out[1] = glowOpacity * glowG + (T(1) - glowOpacity) * out[1];
+    out[2] = glowOpacity * glowB + (T(1) - glowOpacity) * out[2];
+    out[3] += glowOpacity;
+    if (p.postFog) {
+      T fogDensity = step / p.fogVisibility;
+      if (fogDensity > T(1)) fogDensity = T(1);
+      out[0] = fogDensity * T(p.fogColor[0]) / T(65536) + (T(1) - fogDensity) * out[0];
+      out[1] = fogDensity * T(p.fogColor[1]) / T(65536) + (T(1) - fogDensity) * out[1];
+      out[2] = fogDensity * T(p.fogColor[2]) / T(65536) + (T(1) - fogDensity) * out[2];
+      totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
+      out[3] = fogDensity + (T(1) - fogDensity) * out[3];
+    }
+    if (fogIntensity > T(0)) {
+      const T fogReduce = p.fogDistFactor;
+      const T densityTemp = (step * fogReduce) / (distance * distance + fogReduce * fogReduce);
+      T k = distance / p.fogC1Dist;
+      if (k > T(1)) k = T(1);
+      T kn = T(1) - k;
+      T fr = (T(p.fogCol1[0]) * kn + T(p.fogCol2[0]) * k);
+      T fg = (T(p.fogCol1[1]) * kn + T(p.fogCol2[1]) * k);
+      T fb = (T(p.fogCol1[2]) * kn + T(p.fogCol2[2]) * k);
+      T k2 = distance / p.fogC2Dist * k;
+      if (k2 > T(1)) k2 = T(1);
+      kn = T(1) - k2;
+      fr = (fr * kn + T(p.fogCol3[0]) * k2);
+      fg = (fg * kn + T(p.fogCol3[1]) * k2);
+      fb = (fb * kn + T(p.fogCol3[2]) * k2);
+      T fogDensity = T(0.3) * fogIntensity * densityTemp / (T(1) + fogIntensity * densityTemp);
+      if (fogDensity > T(1)) fogDensity = T(1);
+      out[0] = fogDensity * fr / T(65536) + (T(1) - fogDensity) * out[0];
+      out[1] = fogDensity * fg / T(65536) + (T(1) - fogDensity) * out[1];
+      out[2] = fogDensity * fb / T(65536) + (T(1) - fogDensity) * out[2];
+      totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
+      out[3] = fogDensity + (T(1) - fogDensity) * out[3];
+    }
+    if (totalOpacity > 1.0f) totalOpacity = 1.0f;
+    if (out[3] > T(1)) out[3] = T(1);
+    totalOpacityOut = totalOpacity;
+    opacitySet = true;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589).
 // ---------------------------------------------------------------------------
@@ -718,9 +875,8 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
     const int x = (int)(pix % p.width), y = (int)(pix / p.width);
     const uint8_t flags = wb.flags[pix];
     const bool hit = (flags & 1) != 0;
-    V3<double> view;
-    camera_ray(p, x, y, view);
-    const V3<T> viewT{(T)view.x, (T)view.y, (T)view.z};
+    V3<T> viewT;
+    camera_dir(p, x, y, viewT);
     T base[3];
     V3<T> objColour{T(0), T(0), T(0)};
     if (hit) {
@@ -782,12 +938,32 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       base[1] = T(0) + bg.y + T(0);
       base[2] = T(0) + bg.z + T(0);
     }
-    const T A = wb.vol[0 * wb.npix + pix];
-    const T out0 = A * base[0] + wb.vol[1 * wb.npix + pix];
-    const T out1 = A * base[1] + wb.vol[2 * wb.npix + pix];
-    const T out2 = A * base[2] + wb.vol[3 * wb.npix + pix];
-    const T alpha = wb.vol[4 * wb.npix + pix];
-    const T opacity = wb.vol[5 * wb.npix + pix];
+    T out0, out1, out2, alpha, opacity;
+    if (flags & 4) {
+      // a long ray of the overflow pass: its volumetric pass was folded into an affine map
+      const T A = wb.vol[0 * wb.npix + pix];
+      out0 = A * base[0] + wb.vol[1 * wb.npix + pix];
+      out1 = A * base[1] + wb.vol[2 * wb.npix + pix];
+      out2 = A * base[2] + wb.vol[3 * wb.npix + pix];
+      alpha = wb.vol[4 * wb.npix + pix];
+      opacity = wb.vol[5 * wb.npix + pix];
+    } else {
+      // VolumetricShader over the ray's pooled step records, far to near, on this base colour
+      T res[4] = {base[0], base[1], base[2], hit ? T(1) + T(0) : T(0)};
+      float totalOpacity = 0.0f;
+      bool set = false;
+      if (p.needVolumetric) {
+        const int count = wb.count[pix];
+        const PoolRecords<T> pr{wb.pool_step, wb.pool_dist, wb.pool_thr, wb.pool_prev, wb.last_chunk[pix],
+                                hit ? count : count - 1};
+        volumetric_pool<T>(p, pr, wb.count[pix], wb.scan[pix], res, totalOpacity, set);
+      }
+      out0 = res[0];
+      out1 = res[1];
+      out2 = res[2];
+      alpha = res[3];
+      opacity = (T)totalOpacity;
+    }
     const double depth = hit ? (double)wb.scan[pix] : 1e20;
     if (io.opacity) io.opacity[pix] = to_u16_x86((double)opacity * 65535.0);
     if (io.alpha) io.alpha[pix] = to_u16_x86((double)alpha * 65535.0);

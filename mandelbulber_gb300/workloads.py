@@ -100,6 +100,65 @@ MANDELBOX_1080P = {
 WORKLOADS = {"mandelbulb_640x480": MANDELBULB_640x480, "mandelbox_1080p": MANDELBOX_1080P}
 
 
+def look_angles(d) -> tuple[float, float]:
+    """Camera angles (degrees) that look along direction d.
+
+    MainThread's view vector for the centre pixel is RotZ(alpha) RotX(beta) (0, 1, 0)
+    = (-sin a cos b, cos a cos b, sin b) (src/Render3D.cpp:237-240, src/algebra.cpp:94-143).
+    """
+    import numpy as np
+    d = np.asarray(d, float) / np.linalg.norm(d)
+    return math.degrees(math.atan2(-d[0], d[1])), math.degrees(math.asin(d[2]))
+
+
+def deep_zoom(ctx, size: int = 1024, seed: int = 5, N: int = 1000, **extra) -> mbgb_scene:
+    """Deep-zoom Mandelbulb (power 8, N 1000): the camera sits 1e-6 before a surface point.
+
+    A seeded direction from (0,-3.5,0) (within 15 deg of the bulb's centre) is sphere-traced
+    with the device's FP64 distance estimate until the distance is below 1e-12; the camera
+    is placed 1e-6 back along the ray, looking at the point, and the perspective factor is
+    chosen so that the footprint scan * persp / width at scan = 1e-6 is 10**U(-9, -7).
+    """
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(seed)
+    origin = np.array([0.0, -3.5, 0.0])
+    base = make_scene({**MANDELBULB_640x480, "N": N, "image_width": size, "image_height": size})
+    pts = torch.zeros(3, dtype=torch.float64, device="cuda")
+    det = torch.full((1,), 1e-13, dtype=torch.float64, device="cuda")
+    dist = torch.zeros(1, dtype=torch.float64, device="cuda")
+    it = torch.zeros(1, dtype=torch.int32, device="cuda")
+    mi = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    from . import PREC_FP64
+    while True:
+        d = np.array([0.0, 1.0, 0.0]) + rng.normal(0.0, 0.15, 3)
+        d /= np.linalg.norm(d)
+        t, hit = 0.0, False
+        for _ in range(20000):
+            p = origin + d * t
+            pts.copy_(torch.tensor(p, dtype=torch.float64))
+            ctx.distance(base, pts.data_ptr(), det.data_ptr(), 1, dist.data_ptr(), it.data_ptr(), mi.data_ptr(),
+                         PREC_FP64)
+            de = float(dist.item())
+            if de < 1e-12:
+                hit = True
+                break
+            t += de
+            if t > 10.0:
+                break
+        if hit:
+            break
+    footprint = 10.0 ** rng.uniform(-9.0, -7.0)
+    cam = origin + d * (t - 1e-6)
+    a, b = look_angles(d)
+    keys = {**MANDELBULB_640x480, "N": N, "image_width": size, "image_height": size,
+            "view_point_x": cam[0], "view_point_y": cam[1], "view_point_z": cam[2],
+            "angle_alfa": a, "angle_beta": b, "perspective": footprint * size / 1e-6,
+            "view_distance_min": 1e-15, "zoom": 1e-15}
+    keys.update(extra)
+    return make_scene(keys)
+
+
 def make_scene(overrides: dict, base: dict | None = None) -> mbgb_scene:
     """A finalized scene from BASE updated with `overrides` (keys as in .fract files)."""
     keys = dict(BASE if base is None else base)

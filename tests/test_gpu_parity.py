@@ -118,6 +118,19 @@ def test_render_fp32_fix_against_oracle(gpu_ctx, oracle, name, size, engine):
     assert m["psnr_float"] >= 45.0, m
 
 
+def test_fp32_fix_with_full_fp64_polish(gpu_ctx, oracle):
+    """polish_all: every hit finishes its bisection in FP64; same parity bar, more polished hits."""
+    sc = W.workload("mandelbox_1080p", 320, 180)
+    ref, _ = oracle_lib.render(oracle, sc)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, polish_all=True)
+    all_polished = gpu_ctx.stats().fp64_polished
+    m = metrics.compare(img, ref)
+    assert m["hit_mismatch"] <= 0.001 and m["psnr_float"] >= 45.0, m
+    assert all_polished == int(ref.hit.sum()) or abs(all_polished - int(img.hit.sum())) == 0
+    gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    assert gpu_ctx.stats().fp64_polished < all_polished
+
+
 def test_full_size_fp32_fix_against_fp64(gpu_ctx):
     """At the full 1080p size: FP32+fix vs the FP64 device path (the oracle is too slow there)."""
     sc = W.workload("mandelbox_1080p")
