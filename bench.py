@@ -156,6 +156,71 @@ def run_reference(args, rank: int, world: int) -> int:
     return 0
 
 
+def batch_section(ctx, torch, dev, stream, flush, args, world, dist) -> dict:
+    """The 64-frame flight animation (Mandelbulb power 8, per-frame resolutions 320x240 ..
+    1920x1080, hard shadows + fast AO q4, FP32 with FP64 refinement) as one batch: the
+    launch configuration comes from the autotuner and the launches are captured once in a
+    CUDA graph and replayed. One step = one batch of 64 frames."""
+    import mandelbulber_gb300 as mb
+    from mandelbulber_gb300 import workloads as W
+    frames = W.flight()
+    npx = sum(f.image_width * f.image_height for f in frames)
+    bufs, layers = [], []
+    for f in frames:
+        n = f.image_width * f.image_height
+        b = {"image_float": torch.empty(n * 3, dtype=torch.float32, device=dev),
+             "zbuffer": torch.empty(n, dtype=torch.float32, device=dev),
+             "alpha": torch.empty(n, dtype=torch.int16, device=dev),
+             "opacity": torch.empty(n, dtype=torch.int16, device=dev),
+             "colour": torch.empty(n * 3, dtype=torch.uint8, device=dev)}
+        bufs.append(b)
+        layers.append({k: v.data_ptr() for k, v in b.items()})
+    big = max(frames, key=lambda f: f.image_width * f.image_height)
+    tuning = ctx.autotune(big)
+
+    def run(steps, warmup, **opts):
+        for _ in range(warmup):
+            ctx.render_batch_device(frames, layers, stream=stream.cuda_stream, **opts)
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        for e0, e1 in evs:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0.record(stream)
+            ctx.render_batch_device(frames, layers, stream=stream.cuda_stream, **opts)
+            e1.record(stream)
+        stream.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        if dist:
+            t = torch.tensor([total], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t.item())
+        return total
+
+    steps = max(1, args.batch_steps)
+    t_graph = run(steps, 3, autotune=True, use_graph=True)
+    # counters of one batch (synchronous call)
+    ctx.render_batch_device(frames, layers, autotune=True, use_graph=True)
+    st = ctx.stats()
+    t_plain = run(1, 1)
+    return {"workload": "flight_64", "frames": len(frames), "pixels_per_batch": npx, "steps": steps,
+            "value": world * npx * steps / t_graph / 1e6, "unit": "Mpix/s",
+            "ms_per_batch": 1e3 * t_graph / steps,
+            "untuned_ungraphed_ms_per_batch": 1e3 * t_plain,
+            "graph_replayed": int(st.graph_replayed), "launches_per_batch": int(st.launches),
+            "de_evaluations_per_s": world * st.de_calls * steps / t_graph,
+            "tuning": {"tile": [tuning.tile_w, tuning.tile_h], "threads_per_cta": tuning.threads_per_cta,
+                       "ctas_per_sm": tuning.ctas_per_sm, "refill_min": tuning.refill_min,
+                       "tuned_ms": tuning.ms, "default_ms": tuning.ms_default, "trials": tuning.trials,
+                       "tuning_frame": [big.image_width, big.image_height]},
+            "scene": "Mandelbulb power 8, N 250, flight through 8 seeded keyframes (shell r 2-4, looking at "
+                     "the origin), Catmull-Rom, 8 frames per key, seeded resolutions, hard shadows, fast AO q4",
+            "precision": "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement"}
+
+
 def run_once(args) -> int:
     """One frame of the workload at a small size (plus `--warmup` frames): the ncu profiling case."""
     import mandelbulber_gb300 as mb
@@ -183,6 +248,8 @@ def main() -> int:
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-frame flight batch")
+    ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
     ap.add_argument("--precision", default="fp32_fix", choices=["fp32_fix", "fp64"])
@@ -332,6 +399,12 @@ def main() -> int:
         except (OSError, ValueError):
             traffic = None
 
+    # launches of one timed frame (the library counts the kernels it enqueues)
+    ctx.render_device(scene, ptrs, precision=mb.PREC_FP32_FIX)
+    launches_per_frame = int(ctx.stats().launches)
+
+    batch = None if args.no_batch else batch_section(ctx, torch, dev, stream, flush, args, world, dist)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, desc = cpu_sample(scene, args.cpu_seconds)
@@ -365,7 +438,8 @@ def main() -> int:
         "parity_vs_fp64": parity,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": ctypes.sizeof(mb.mbgb_scene),
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps * (5 if scene.glow_intensity or scene.fogDensity > 0 or scene.fogEnabled else 4),
+        "gpu_launches": args.steps * launches_per_frame,
+        "batch": batch,
         "clocks": clocks,
         "cpu_baseline": cpu,
         "wall_s_timed_region": wall32,

@@ -205,7 +205,28 @@ typedef struct mbgb_opts {
   int32_t profile_stages;      /* 1: record CUDA events between stages (synchronous calls fill stage_ms) */
   int32_t polish_all;          /* FP32_FIX: 1 = re-run the end of every hit's bisection in FP64; 0 = only the
                                 * hits whose FP32 window decision is within 1e-4 of an edge */
+  int32_t tile_w, tile_h;      /* wavefront: pixel tile of a warp's first 32 primary rays (tile_w * tile_h
+                                * = 32); 0,0 = autotuned or 8 x 4 */
+  int32_t refill_min;          /* wavefront: idle lanes of a warp before it claims new rays; 0 = tuned or 1 */
+  int32_t autotune;            /* 1: tile shape, threads per CTA, CTAs per SM and refill_min that are 0
+                                * come from mbgb_autotune, run once per scene class and context */
+  int32_t use_graph;           /* 1: the launches are captured once in a CUDA graph and replayed while
+                                * the frames, outputs and options stay the same */
+  int32_t exact_hit;           /* wavefront: 1 = after the binary refinement every hit is moved in FP64
+                                * (Newton steps) onto the level set DE(P) = thr, the surface the
+                                * differentiable render differentiates; 0 = the reference's window */
 } mbgb_opts;
+
+/* Launch configuration picked by mbgb_autotune. */
+typedef struct mbgb_tuning {
+  int32_t tile_w, tile_h;      /* primary-ray pixel tile */
+  int32_t threads_per_cta;     /* 64 or 128 */
+  int32_t ctas_per_sm;         /* resident CTAs per SM of the ray stages */
+  int32_t refill_min;          /* idle lanes before a warp refills */
+  double ms;                   /* device time of the picked configuration on the tuning frame */
+  double ms_default;           /* device time of the default configuration (8 x 4, 128, max, 1) */
+  int32_t trials;              /* configurations timed */
+} mbgb_tuning;
 
 /* Render engines (same results within the precision policy's tolerance). */
 enum {
@@ -223,13 +244,19 @@ typedef struct mbgb_stats {
   uint64_t missed_de;          /* Missed_DE_counter */
   uint64_t long_rays;          /* primary rays longer than the main pass's step records (re-rendered) */
   uint64_t fp64_polished;      /* FP32_FIX, wavefront: hits whose bisection was finished in FP64 */
-  uint64_t auto_fp64;          /* MBGB_PREC_AUTO: 1 if the last frame was rendered in FP64 */
+  uint64_t auto_fp64;          /* 1 if any frame of the last call was rendered in FP64 (MBGB_PREC_AUTO picks per frame) */
   double kernel_ms;            /* device time of the last render */
   /* per stage: [0] primary rays (wavefront) or the per-pixel kernel, [1] FP64 hit polish,
    * [2] shadow and AO rays, [3] composition */
   uint64_t stage_orbit[4];     /* orbit iterations */
   uint64_t stage_de[4];        /* DE evaluations */
   double stage_ms[4];          /* device time between the stage's CUDA events (profile_stages = 1) */
+  uint64_t frames;             /* frames of the last call */
+  uint64_t launches;           /* kernels the last call launched (graph replays included) */
+  uint64_t graph_replayed;     /* 1 if the last call replayed a captured CUDA graph */
+  uint64_t level_set_missed;   /* exact_hit: hits whose Newton refinement did not reach the level set */
+  uint64_t grad_pixels;        /* mbgb_render_grad: hit pixels differentiated */
+  uint64_t grad_skipped;       /* mbgb_render_grad: hit pixels left out (level set missed, grazing ray) */
 } mbgb_stats;
 
 typedef struct mbgb_context mbgb_context;
@@ -282,6 +309,49 @@ mbgb_status mbgb_render_device(mbgb_context *ctx, const mbgb_scene *scene,
                                const mbgb_image *out, const mbgb_opts *opts);
 mbgb_status mbgb_render_host(mbgb_context *ctx, const mbgb_scene *scene,
                              const mbgb_image *out, const mbgb_opts *opts);
+
+/* Batch of `n` frames (MainRender's keyframe / flight loops, src/Render3D.cpp:2144-2350,
+ * each frame a Render() call at :2410/:2417) in one sequence of wavefront launches: frames
+ * with the same fractal, shading and fog parameters share the launches, so cameras and
+ * resolutions may differ from frame to frame. frames[i] renders into outs[i].
+ * mbgb_render_batch: device pointers, asynchronous on opts->stream unless it is NULL.
+ * mbgb_render_batch_host: host pointers, device staging and copies are part of the call.
+ * A row range in opts applies to every frame. The per-pixel engine renders the frames one
+ * by one. */
+mbgb_status mbgb_render_batch(mbgb_context *ctx, const mbgb_scene *frames, int32_t n,
+                              const mbgb_image *outs, const mbgb_opts *opts);
+mbgb_status mbgb_render_batch_host(mbgb_context *ctx, const mbgb_scene *frames, int32_t n,
+                                   const mbgb_image *outs, const mbgb_opts *opts);
+
+/* Differentiable render (no counterpart in the reference; the reference's parameters
+ * are only ever set by hand or by the keyframe splines). theta of a frame has
+ * MBGB_GRAD_PARAMS entries: [0] the fractal parameter (power of formula 2, Mandelbox scale
+ * of formula 8), [1..3] the camera position vp, [4] main light alpha, [5] main light
+ * beta (radians). frames[i] is rendered into outs[i] (device layers) with every hit moved
+ * onto the level set DE(P) = thr (opts->exact_hit is implied), and differentiated at
+ * that point: implicit differentiation of the hit distance, forward-mode derivatives of
+ * every distance estimate (the orbits are recomputed, not stored), the reference's
+ * forward-difference normal, Lambert and specular shading. Hard shadows and the palette
+ * colour are piecewise constant and contribute nothing.
+ * dL_dimage: NULL or n device pointers to [height][width][3] floats (dL / d image_float);
+ * jacobian: NULL or n device pointers to [height][width][3][MBGB_GRAD_PARAMS] floats;
+ * dL_dtheta: NULL or host [n][MBGB_GRAD_PARAMS] doubles, the sums over pixels and channels
+ * of dL/dI dI/dtheta. Precision MBGB_PREC_FP64 or MBGB_PREC_FP32_FIX. Scenes: formula 2, or
+ * formula 8 without rotations, offset or pre-folds; no AO, glow, fog, interior mode,
+ * limits, iteration threshold, soft or penetrating shadows (MBGB_ERR_UNSUPPORTED
+ * otherwise). Synchronous. */
+#define MBGB_GRAD_PARAMS 6
+mbgb_status mbgb_render_grad(mbgb_context *ctx, const mbgb_scene *frames, int32_t n, const mbgb_image *outs,
+                             const float *const *dL_dimage, float *const *jacobian, double *dL_dtheta,
+                             const mbgb_opts *opts);
+
+/* Autotuner of the wavefront launch configuration: times the candidate tile shapes,
+ * threads per CTA, CTAs per SM and refill thresholds on `scene` (a representative frame,
+ * rendered into context scratch) and returns the fastest. The result is cached in the
+ * context for the scene's class (formula, orbit, precision, shadow / AO / volumetric
+ * switches), where renders with opts->autotune = 1 pick it up. Synchronous. */
+mbgb_status mbgb_autotune(mbgb_context *ctx, const mbgb_scene *scene, const mbgb_opts *opts,
+                          mbgb_tuning *out);
 
 /* Allocation-free render (no counterpart in the reference): the FP32_FIX render of
  * mbgb_render_device for callers that cannot allocate device memory while they

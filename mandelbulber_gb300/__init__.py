@@ -10,6 +10,8 @@ path:
 * ``Context.render(scene)`` is Render(sParamRender, cImage*) (src/Render3D.cpp:709)
   and returns a ``CImage`` holding the layers MainThread writes
   (src/Render3D.cpp:569-589): image_float, zbuffer, alpha, opacity, colour.
+* ``Context.render_batch(scenes)`` renders the frames of MainRender's keyframe /
+  flight loops (src/Render3D.cpp:2144-2350) in one launch sequence.
 
 There is no CPU fallback: every render call runs the CUDA kernels and raises
 ``MbgbError`` when the library or a GPU is missing.
@@ -23,7 +25,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import PREC_AUTO, PREC_FP32_FIX, PREC_FP64, mbgb_image, mbgb_opts, mbgb_rgb, mbgb_scene, mbgb_stats
+from ._abi import (PREC_AUTO, PREC_FP32_FIX, PREC_FP64, mbgb_image, mbgb_opts, mbgb_rgb, mbgb_scene, mbgb_stats,
+                   mbgb_tuning)
 
 __all__ = [
     "MbgbError", "load_settings", "scene_set", "finalize", "supported", "palette_from_seed", "Context", "CImage",
@@ -100,6 +103,17 @@ def palette_from_seed(seed: int, saturation: float) -> np.ndarray:
     return np.array([[c.R, c.G, c.B] for c in pal], dtype=np.int32)
 
 
+def interpolate(keys, frames_per_key: int, frame: int, base: mbgb_scene | None = None) -> mbgb_scene:
+    """Scene of animation frame ``frame`` from keyframes (CMorph::CatmullRom over every
+    interpolated double, src/morph.cpp:49-109, as MainRender applies it)."""
+    n = len(keys)
+    arr = (mbgb_scene * n)(*keys)
+    out = mbgb_scene()
+    _check(library().mbgb_scene_interpolate(arr, n, frames_per_key, frame,
+                                            ctypes.byref(base) if base is not None else None, ctypes.byref(out)))
+    return out
+
+
 def scene_bytes(scene: mbgb_scene) -> bytes:
     return ctypes.string_at(ctypes.addressof(scene), ctypes.sizeof(scene))
 
@@ -146,12 +160,23 @@ ENGINE_WAVEFRONT, ENGINE_PER_PIXEL = 0, 1
 
 def make_opts(precision: int = PREC_FP32_FIX, jitter: bool = False, jitter_seed: int = 0, rows=None,
               ctas_per_sm: int = 0, threads_per_cta: int = 0, deadline_ms: int = 0, stream: int = 0,
-              engine: int = ENGINE_WAVEFRONT, profile_stages: bool = False, polish_all: bool = False) -> mbgb_opts:
+              engine: int = ENGINE_WAVEFRONT, profile_stages: bool = False, polish_all: bool = False,
+              tile=None, refill_min: int = 0, autotune: bool = False, use_graph: bool = False) -> mbgb_opts:
     r0, r1 = rows if rows else (0, 0)
+    tw, th = tile if tile else (0, 0)
     return mbgb_opts(precision=precision, jitter=int(jitter), jitter_seed=jitter_seed, row_begin=r0, row_end=r1,
                      ctas_per_sm=ctas_per_sm, threads_per_cta=threads_per_cta, deadline_ms=deadline_ms,
                      stream=stream if stream else None, engine=engine, profile_stages=int(profile_stages),
-                     polish_all=int(polish_all))
+                     polish_all=int(polish_all), tile_w=tw, tile_h=th, refill_min=refill_min,
+                     autotune=int(autotune), use_graph=int(use_graph))
+
+
+_LAYERS = ["image_float", "zbuffer", "alpha", "opacity", "colour", "hit", "iters", "depth"]
+
+
+def _device_image(scene: mbgb_scene, layers: dict) -> mbgb_image:
+    return mbgb_image(scene.image_width, scene.image_height,
+                      *[ctypes.c_void_p(layers.get(n) or 0) if layers.get(n) else None for n in _LAYERS])
 
 
 class Context:
@@ -191,11 +216,36 @@ class Context:
 
     def render_device(self, scene: mbgb_scene, layers: dict, **opts) -> None:
         """Renders into device buffers; ``layers`` maps layer names to device pointers (ints)."""
-        names = ["image_float", "zbuffer", "alpha", "opacity", "colour", "hit", "iters", "depth"]
-        img = mbgb_image(scene.image_width, scene.image_height,
-                         *[ctypes.c_void_p(layers.get(n) or 0) if layers.get(n) else None for n in names])
+        img = _device_image(scene, layers)
         o = make_opts(**opts)
         _check(self._lib.mbgb_render_device(self._h, ctypes.byref(scene), ctypes.byref(img), ctypes.byref(o)))
+
+    def render_batch(self, scenes, images=None, **opts) -> list:
+        """Renders the frames of an animation in one launch sequence into host layers
+        (mbgb_render_batch_host); returns the CImages."""
+        n = len(scenes)
+        if images is None:
+            images = [CImage.empty(sc.image_width, sc.image_height) for sc in scenes]
+        arr = (mbgb_scene * n)(*scenes)
+        imgs = (mbgb_image * n)(*[im.as_c() for im in images])
+        o = make_opts(**opts)
+        _check(self._lib.mbgb_render_batch_host(self._h, arr, n, imgs, ctypes.byref(o)))
+        return images
+
+    def render_batch_device(self, scenes, layers: list, **opts) -> None:
+        """mbgb_render_batch: frame i renders into the device pointers of ``layers[i]``."""
+        n = len(scenes)
+        arr = (mbgb_scene * n)(*scenes)
+        imgs = (mbgb_image * n)(*[_device_image(sc, ly) for sc, ly in zip(scenes, layers)])
+        o = make_opts(**opts)
+        _check(self._lib.mbgb_render_batch(self._h, arr, n, imgs, ctypes.byref(o)))
+
+    def autotune(self, scene: mbgb_scene, **opts) -> mbgb_tuning:
+        """mbgb_autotune: times the launch configurations on this frame and caches the best."""
+        t = mbgb_tuning()
+        o = make_opts(**opts)
+        _check(self._lib.mbgb_autotune(self._h, ctypes.byref(scene), ctypes.byref(o), ctypes.byref(t)))
+        return t
 
     def distance(self, scene: mbgb_scene, points_dev: int, detail_dev: int, n: int, dist_dev: int, iters_dev: int,
                  maxiter_dev: int, precision: int = PREC_FP64) -> None:

@@ -74,6 +74,10 @@ class mbgb_stats(ctypes.Structure):
     _fields_ = _struct_fields("mbgb_stats")
 
 
+class mbgb_tuning(ctypes.Structure):
+    _fields_ = _struct_fields("mbgb_tuning")
+
+
 MBGB_STATUS = {
     0: "MBGB_OK",
     1: "MBGB_ERR_BAD_PARAM",
@@ -108,6 +112,11 @@ FUNCTIONS = {
     "mbgb_render_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), _P(mbgb_opts)]),
     "mbgb_render_host": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), _P(mbgb_opts)]),
     "mbgb_render_device_noalloc": (ctypes.c_int, [_P(mbgb_scene), _P(mbgb_image), _P(mbgb_opts)]),
+    "mbgb_render_batch": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int32, _P(mbgb_image),
+                                         _P(mbgb_opts)]),
+    "mbgb_render_batch_host": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int32, _P(mbgb_image),
+                                              _P(mbgb_opts)]),
+    "mbgb_autotune": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_opts), _P(mbgb_tuning)]),
     "mbgb_distance_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p]),

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,26 +18,6 @@
 #include "mbgb_internal.h"
 #include "wave_launch.h"
 
-namespace mbgb {
-// WaveBufs layout (must match wave_core.cuh)
-template <typename T>
-struct WaveBufs {
-  uint8_t *flags;
-  T *scan, *dist, *thr, *step, *detail;
-  int32_t *bis_left;
-  T *point;
-  int32_t *iters, *count;
-  T *vol, *shadow, *ao;
-  uint32_t *hit_list, *polish_list, *ctl, *overflow_list;
-  T *pool_step, *pool_dist, *pool_thr;
-  int32_t *pool_prev, *last_chunk;
-  uint32_t pool_cap;
-  int polish_all;
-  int64_t npix;
-};
-constexpr int kChunk = 32;
-constexpr int kPoolChunksPerPixel = 4;
-}  // namespace mbgb
 
 namespace mbgb {
 
@@ -322,24 +303,85 @@ int ao_vectors_into(int quality, float *out, int max_vectors) {
 
 using namespace mbgb;
 
+// Launch configuration of the wavefront stages (mbgb_tuning without the timings).
+struct LaunchCfg {
+  int tileW = kTileW, tileH = kTileH;   // primary-ray pixel tile of a warp
+  int block = 128;                      // threads per CTA
+  int ctasPerSm = 0;                    // 0 = the occupancy limit
+  int refill = 1;                       // idle lanes before a warp refills
+};
+
+// Scene class an autotuned configuration applies to.
+using TuneKey = std::array<int, 10>;
+
+// One launch sequence of a render call: frames sharing every non-camera parameter and
+// the precision policy (wavefront), or one frame of the per-pixel engine.
+struct Group {
+  int prec = 1;                  // 0: FP64, 1: FP32 with FP64 refinement
+  bool wave = true;
+  std::vector<int> frames;       // indices into the call's frames
+  int64_t npix = 0;              // full-frame pixels of the group's frames
+  int64_t jobs = 0;              // primary jobs (tile-padded pixels in the row range)
+  size_t cams_off = 0;           // byte offset of the group's frame table in the context's table buffer
+  size_t grad_off = 0;           // differentiable render: byte offset of the group's gradient table
+  LaunchCfg cfg;
+};
+
+// Device pointers of a differentiable render call (mbgb_render_grad), one per frame.
+struct GradRequest {
+  const float *const *dL_dimage;   // null or n pointers to [h][w][3]
+  float *const *jacobian;          // null or n pointers to [h][w][3][kGradParams]
+};
+
+// What a render call enqueued; read back after the stream is synchronised.
+struct CallPlan {
+  std::vector<Group> groups;
+  uint64_t pixels = 0;
+  uint64_t frames = 0;
+  uint64_t launches = 0;
+  bool profile = false;
+  bool grad = false;             // the gradient stage runs after composition
+};
+
 struct mbgb_context {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;
-  DeviceBuf step[2][3];          // [precision][step, dist, thr], kStepCap records per slot
+  DeviceBuf step[2][3];          // per-pixel engine: [precision][step, dist, thr], kStepCap records per slot
   DeviceBuf ovstep[2][3];        // overflow pass: kStepSlots records per slot, kOverflowThreads slots
-  DeviceBuf ovlist;              // overflow pixel list
-  DeviceBuf control;              // tile counter, error flag, counters
+  DeviceBuf ovlist;              // overflow pixel list (per-pixel engine)
+  DeviceBuf control;             // error flag, start time, stage counters
+  DeviceBuf fctl;                // per group: wavefront stage counters / per-pixel tile counter (64 B each)
+  DeviceBuf cams;                // frame tables of the wavefront groups
   DeviceBuf ao64, ao32;
   int ao_quality = -1;
   int ao_count = 0;
-  DeviceBuf out[8];               // device staging for mbgb_render_host
-  DeviceBuf wave[2];              // wavefront per-pixel buffers, per precision
-  DeviceBuf probe;                // MBGB_PREC_AUTO: one-point distance probe
+  DeviceBuf out[8];              // device staging for mbgb_render_host / mbgb_render_batch_host
+  DeviceBuf wave[2];             // wavefront per-pixel buffers, per precision
+  DeviceBuf probe;               // MBGB_PREC_AUTO: distance probes at the ray origins
+  DeviceBuf tune_out;            // autotuner output layers
+  DeviceBuf gradacc;             // differentiable render: per-frame dL/dtheta sums
+  uint64_t gen = 0;              // bumped whenever a scratch buffer is reallocated
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t sev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // stage events
+  std::vector<cudaEvent_t> gev;  // stage events, 5 per group (profile_stages)
+  std::map<TuneKey, mbgb_tuning> tunings;
+  CallPlan plan;                 // the last call's launches
+  // use_graph: the captured launches of the last such call and what they depend on
+  std::vector<char> graph_key;
+  uint64_t graph_gen = 0;
+  cudaGraphExec_t graph = nullptr;
+  CallPlan graph_plan;
+  std::vector<char> graph_cams;  // host copy of the frame tables the graph reads
+  bool cams_hold_graph = false;  // the table buffer holds graph_cams
   mbgb_stats stats{};
   std::mutex mu;
+
+  cudaError_t ensure(DeviceBuf &b, size_t want) {
+    void *old = b.ptr;
+    cudaError_t e = b.ensure(want);
+    if (b.ptr != old) gen++;
+    return e;
+  }
 };
 
 extern "C" const char *mbgb_version(void) { return "mbgb 0.1.0 (sm_103a)"; }
@@ -391,10 +433,7 @@ extern "C" mbgb_status mbgb_context_create(int device, mbgb_context **out) {
   }
   c->sms = prop.multiProcessorCount;
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess ||
-      (e = cudaEventCreate(&c->sev[0])) != cudaSuccess || (e = cudaEventCreate(&c->sev[1])) != cudaSuccess ||
-      (e = cudaEventCreate(&c->sev[2])) != cudaSuccess || (e = cudaEventCreate(&c->sev[3])) != cudaSuccess ||
-      (e = cudaEventCreate(&c->sev[4])) != cudaSuccess) {
+      (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
     delete c;
     return cuda_error(e, "context stream/event creation");
   }
@@ -413,12 +452,17 @@ extern "C" void mbgb_context_destroy(mbgb_context *c) {
   c->ovlist.release();
   for (auto &b : c->wave) b.release();
   c->probe.release();
+  c->tune_out.release();
+  c->gradacc.release();
   c->control.release();
+  c->fctl.release();
+  c->cams.release();
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (auto ev : c->gev)
+    if (ev) cudaEventDestroy(ev);
   c->ao64.release();
   c->ao32.release();
   for (auto &b : c->out) b.release();
-  for (auto &ev : c->sev)
-    if (ev) cudaEventDestroy(ev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -435,8 +479,8 @@ static mbgb_status ensure_ao(mbgb_context *c, int quality, cudaStream_t s) {
   if (c->ao_quality == quality) return MBGB_OK;
   std::vector<double> v = ao_vectors(quality);
   std::vector<float> vf(v.begin(), v.end());
-  MBGB_CUDA(c->ao64.ensure(std::max<size_t>(v.size() * sizeof(double), 16)));
-  MBGB_CUDA(c->ao32.ensure(std::max<size_t>(vf.size() * sizeof(float), 16)));
+  MBGB_CUDA(c->ensure(c->ao64, std::max<size_t>(v.size() * sizeof(double), 16)));
+  MBGB_CUDA(c->ensure(c->ao32, std::max<size_t>(vf.size() * sizeof(float), 16)));
   MBGB_CUDA(cudaMemcpyAsync(c->ao64.ptr, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
   MBGB_CUDA(cudaMemcpyAsync(c->ao32.ptr, vf.data(), vf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
   MBGB_CUDA(cudaStreamSynchronize(s));
@@ -461,94 +505,298 @@ static bool fast_mandelbulb(const mbgb_scene &s) {
          !s.limits_enabled && !s.iterThresh && !s.interiorMode;
 }
 
-// Wavefront stages (wave_core.cuh): primary rays, FP64 polish (FP32 policy), shadow/AO
-// rays, composition. All launches are enqueued on `s` without host round trips.
+// Per-frame fields of ParamsT (camera, size, rows, light direction) cleared, so that
+// two frames compare equal exactly when one launch sequence can render both.
 template <typename T>
-static mbgb_status render_wave(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *img, const mbgb_opts &o,
-                               cudaStream_t s, const int prec, FrameIO io, bool needVol, uint32_t **long_rays_ctl) {
-  const int64_t npix = (int64_t)scene->image_width * scene->image_height;
-  const int block = 128;
-  const bool rayAO = scene->global_ilumination && !scene->fastGlobalIllumination;
-  const int aoN = rayAO ? c->ao_count : 0;
+static void strip_camera(ParamsT<T> &p) {
+  p.width = p.height = p.tiles = p.row_begin = p.row_end = 0;
+  p.tileXOffset = p.tileYOffset = p.aspect = p.fov = 0.0;
+  memset(p.rot, 0, sizeof(p.rot));
+  memset(p.rotf, 0, sizeof(p.rotf));
+  p.rot_zero = 0;
+  memset(p.start, 0, sizeof(p.start));
+  p.resolution = p.persp = T(0);
+  p.resolution_d = p.persp_d = 0.0;
+  for (int k = 0; k < 3; k++) p.lightVect[k] = T(0);
+  p.aoVec = nullptr;
+}
+
+// Fractal fields the scene's formula never reads cleared. Keyframe splines leave
+// last-bit differences in parameters that stay constant over an animation
+// (2 v - 5 v + 4 v - v is not exactly 0 in doubles), and those in unused fields
+// must not split a batch.
+template <typename T>
+static void clear_unused(FractalT<T> &f) {
+  if (f.formula == MBGB_FORMULA_TRIG_OPTIM) {
+    f.mbRotEnabled = f.mbMainRotZero = 0;
+    memset(f.mbRotZero, 0, sizeof(f.mbRotZero));
+    f.mbScale = f.mbFoldLimit = f.mbFoldValue = f.mbMinR = f.mbFixedR = T(0);
+    f.mbColX = f.mbColY = f.mbColZ = f.mbColR = f.mbColSp1 = f.mbColSp2 = T(0);
+    for (int k = 0; k < 3; k++) f.mbOffset[k] = T(0);
+    memset(f.mbMainRot, 0, sizeof(f.mbMainRot));
+    memset(f.mbRot, 0, sizeof(f.mbRot));
+    memset(f.mbRotInv, 0, sizeof(f.mbRotInv));
+  } else if (f.formula == MBGB_FORMULA_TGLAD) {
+    f.power = T(0);
+  }
+}
+
+// Whether frames a and b can share one launch sequence in precision T: every
+// parameter the kernels read, other than the per-frame camera, is equal in the
+// form the kernels receive it.
+template <typename T>
+static bool same_shared(const mbgb_scene &a, const mbgb_scene &b, const mbgb_opts &o) {
+  ParamsT<T> pa, pb;
+  fill_params<T>(a, pa, o, nullptr, 0);
+  fill_params<T>(b, pb, o, nullptr, 0);
+  strip_camera(pa);
+  strip_camera(pb);
+  clear_unused(pa.f);
+  clear_unused(pb.f);
+  if (memcmp(&pa, &pb, sizeof(pa)) != 0) return false;
+  FractalT<double> fa, fb;
+  fill_fractal<double>(a, fa);
+  fill_fractal<double>(b, fb);
+  clear_unused(fa);
+  clear_unused(fb);
+  return memcmp(&fa, &fb, sizeof(fa)) == 0;
+}
+
+// Camera, size, rows and output layers of one frame (MainThread's per-frame set-up,
+// src/Render3D.cpp:213-344).
+template <typename T>
+static void fill_cam(const mbgb_scene &s, const mbgb_image &img, const mbgb_opts &o, const LaunchCfg &cfg,
+                     FrameCam<T> &cam) {
+  ParamsT<T> p;
+  fill_params<T>(s, p, o, nullptr, 0);
+  memset(&cam, 0, sizeof(cam));
+  cam.width = p.width;
+  cam.height = p.height;
+  cam.tiles = p.tiles;
+  cam.row_begin = p.row_begin;
+  cam.row_end = p.row_end;
+  cam.rot_zero = p.rot_zero;
+  cam.tileW = cfg.tileW;
+  cam.tileH = cfg.tileH;
+  cam.tileXOffset = p.tileXOffset;
+  cam.tileYOffset = p.tileYOffset;
+  cam.aspect = p.aspect;
+  cam.fov = p.fov;
+  memcpy(cam.rot, p.rot, sizeof(cam.rot));
+  memcpy(cam.rotf, p.rotf, sizeof(cam.rotf));
+  memcpy(cam.start, p.start, sizeof(cam.start));
+  cam.resolution = p.resolution;
+  cam.persp = p.persp;
+  cam.resolution_d = p.resolution_d;
+  cam.persp_d = p.persp_d;
+  for (int k = 0; k < 3; k++) cam.lightVect[k] = p.lightVect[k];
+  cam.image_float = img.image_float;
+  cam.zbuffer = img.zbuffer;
+  cam.alpha = img.alpha;
+  cam.opacity = img.opacity;
+  cam.colour = img.colour;
+  cam.hit = img.hit;
+  cam.iters = img.iters;
+  cam.depth = img.depth;
+}
+
+static bool need_volumetric(const mbgb_scene &s) {
+  return (s.glow_intensity != 0.0) || s.fogEnabled || (s.fogDensity > 0.0);
+}
+
+// Scenes whose distance estimate the dual-number orbit (exact hits, gradients) covers:
+// formula 2, or formula 8 without rotations, offset or pre-folds, and the analytic
+// estimate without limits, iteration threshold or interior mode.
+static mbgb_status level_set_supported(const mbgb_scene &s) {
+  if (s.tgladFoldingMode || s.sphericalFoldingMode)
+    return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: pre-folds");
+  if (s.formula == MBGB_FORMULA_TGLAD &&
+      (s.mboxRotationsEnabled || !s.mboxMainRotZero || s.mboxOffset[0] != 0.0 || s.mboxOffset[1] != 0.0 ||
+       s.mboxOffset[2] != 0.0))
+    return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: Mandelbox rotations or offset");
+  if (s.limits_enabled || s.iterThresh || s.interiorMode)
+    return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: limits, iteration threshold or interior mode");
+  return MBGB_OK;
+}
+
+// Shading terms the gradient stage differentiates: Lambert, specular, hard shadows.
+static mbgb_status grad_supported(const mbgb_scene &s) {
+  if (s.global_ilumination) return set_error(MBGB_ERR_UNSUPPORTED, "gradients: ambient occlusion");
+  if (need_volumetric(s)) return set_error(MBGB_ERR_UNSUPPORTED, "gradients: glow or fog");
+  if (s.shadow && (s.penetratingLights || tan(s.shadowConeAngle / 180.0 * M_PI) > 0.0))
+    return set_error(MBGB_ERR_UNSUPPORTED, "gradients: soft or penetrating shadows");
+  return MBGB_OK;
+}
+
+// Gradient-stage inputs of frame i: its loss derivative and Jacobian buffers, its slot of
+// the dL/dtheta sums, and the derivatives of the camera-relative light vector
+// rot (cos(a) cos(b), sin(a) cos(b), sin(b)), a = alpha - pi/2, b = -beta
+// (src/Render3D.cpp:252-256) by alpha and beta.
+template <typename T>
+static void fill_grad_cam(const mbgb_scene &s, const GradRequest &g, int i, double *acc, GradCam<T> &gc) {
+  memset(&gc, 0, sizeof(gc));
+  gc.dL_dimage = g.dL_dimage ? g.dL_dimage[i] : nullptr;
+  gc.jacobian = g.jacobian ? g.jacobian[i] : nullptr;
+  gc.dtheta = acc + (size_t)kGradParams * i;
+  static_assert(kGradParams == MBGB_GRAD_PARAMS, "gradient parameter count");
+  HostRot rot;
+  rot.rotZ(s.alpha);
+  rot.rotX(s.beta);
+  rot.rotY(s.gamma);
+  const double a = s.mainLightAlpha - 0.5 * M_PI, b = -s.mainLightBeta;
+  const double da[3] = {-sin(a) * cos(b), cos(a) * cos(b), 0.0};
+  const double db[3] = {cos(a) * sin(b), sin(a) * sin(b), -cos(b)};
+  double ra[3], rb[3];
+  rot.apply(da, ra);
+  rot.apply(db, rb);
+  for (int k = 0; k < 3; k++) {
+    gc.dLight[0][k] = (T)ra[k];
+    gc.dLight[1][k] = (T)rb[k];
+  }
+}
+
+static TuneKey tune_key(const mbgb_scene &s, int prec) {
+  return TuneKey{s.formula, (int)(fast_mandelbox(s) || fast_mandelbulb(s)), prec, (int)need_volumetric(s),
+                 s.shadow, s.global_ilumination, s.fastGlobalIllumination, s.globalIlumQuality, s.perspectiveType,
+                 s.interiorMode};
+}
+
+// Launch configuration of a group: explicit options first, then the cached autotuning
+// (opts.autotune), then the defaults.
+static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mbgb_scene &s, int prec) {
+  LaunchCfg cfg;
+  if (o.autotune) {
+    auto it = c->tunings.find(tune_key(s, prec));
+    if (it != c->tunings.end()) {
+      cfg.tileW = it->second.tile_w;
+      cfg.tileH = it->second.tile_h;
+      cfg.block = it->second.threads_per_cta;
+      cfg.ctasPerSm = it->second.ctas_per_sm;
+      cfg.refill = it->second.refill_min;
+    }
+  }
+  if (o.tile_w > 0 && o.tile_h > 0) {
+    cfg.tileW = o.tile_w;
+    cfg.tileH = o.tile_h;
+  }
+  if (o.threads_per_cta > 0) cfg.block = o.threads_per_cta;
+  if (o.ctas_per_sm > 0) cfg.ctasPerSm = o.ctas_per_sm;
+  if (o.refill_min > 0) cfg.refill = o.refill_min;
+  return cfg;
+}
+
+// Byte layout of the wavefront buffers for `npix` pixels (256-byte aligned pieces).
+struct WaveLayout {
+  size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
+  size_t pstep, pdist, pthr, pprev;
+  uint32_t poolCap;
+  size_t total;
+};
+
+static WaveLayout wave_layout(int64_t npix, size_t ts, int aoN, bool needVol) {
+  WaveLayout w{};
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t at = off;
     off += (bytes + 255) & ~(size_t)255;
     return at;
   };
-  const size_t ts = sizeof(T);
-  const size_t o_flags = take(npix), o_scan = take(npix * ts), o_dist = take(npix * ts), o_thr = take(npix * ts);
-  const size_t o_step = take(npix * ts), o_detail = take(npix * ts), o_bis = take(npix * 4);
-  const size_t o_point = take(3 * npix * ts), o_iters = take(npix * 4), o_count = take(npix * 4);
-  const size_t o_vol = take(6 * npix * ts), o_shadow = take(npix * ts), o_ao = take((size_t)aoN * npix * ts);
-  const size_t o_hit = take(npix * 4), o_pol = take(npix * 4), o_ovl = take(npix * 4), o_ctl = take(64);
-  const size_t o_last = take(npix * 4);
-  const uint32_t poolCap = needVol ? (uint32_t)std::min<int64_t>(npix * kPoolChunksPerPixel, 0x7fffffff) : 1u;
-  const size_t o_pstep = take((size_t)poolCap * kChunk * ts), o_pdist = take((size_t)poolCap * kChunk * ts);
-  const size_t o_pthr = take((size_t)poolCap * kChunk * ts), o_pprev = take((size_t)poolCap * 4);
-  MBGB_CUDA(c->wave[prec].ensure(off));
+  w.flags = take(npix);
+  w.scan = take(npix * ts);
+  w.dist = take(npix * ts);
+  w.thr = take(npix * ts);
+  w.step = take(npix * ts);
+  w.detail = take(npix * ts);
+  w.bis = take(npix * 4);
+  w.point = take(3 * npix * ts);
+  w.iters = take(npix * 4);
+  w.count = take(npix * 4);
+  w.vol = take((needVol ? 6 : 1) * npix * ts);
+  w.shadow = take(npix * ts);
+  w.ao = take((size_t)aoN * npix * ts);
+  w.hit = take(npix * 4);
+  w.pol = take(npix * 4);
+  w.ovl = take(npix * 4);
+  w.last = take(npix * 4);
+  w.poolCap = needVol ? (uint32_t)std::min<int64_t>(npix * kPoolChunksPerPixel, 0x7fffffff) : 1u;
+  w.pstep = take((size_t)w.poolCap * kChunk * ts);
+  w.pdist = take((size_t)w.poolCap * kChunk * ts);
+  w.pthr = take((size_t)w.poolCap * kChunk * ts);
+  w.pprev = take((size_t)w.poolCap * 4);
+  w.total = off;
+  return w;
+}
+
+template <typename T>
+static int wave_occupancy(int formula, int block, int which) {
+  if constexpr (sizeof(T) == 8) return occupancy_wave_f64(formula, block, which);
+  else return occupancy_wave_f32(formula, block, which);
+}
+
+// Enqueue the wavefront stages (wave_core.cuh) of one group: primary rays, FP64 polish
+// (FP32 policy), shadow/AO rays, composition. No host round trips.
+template <typename T>
+static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const Group &g, const mbgb_opts &o,
+                                cudaStream_t s, FrameIO io, uint32_t *ctl, cudaEvent_t *ev, bool grad,
+                                uint64_t *launches) {
+  const mbgb_scene &scene = scenes[g.frames[0]];
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  const bool needVol = need_volumetric(scene);
+  const bool rayAO = scene.global_ilumination && !scene.fastGlobalIllumination;
+  const int aoN = rayAO ? c->ao_count : 0;
+  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol);
   char *base = (char *)c->wave[prec].ptr;
   WaveLaunch<T> L;
   WaveBufs<T> &wb = L.wb;
-  wb.flags = (uint8_t *)(base + o_flags);
-  wb.scan = (T *)(base + o_scan);
-  wb.dist = (T *)(base + o_dist);
-  wb.thr = (T *)(base + o_thr);
-  wb.step = (T *)(base + o_step);
-  wb.detail = (T *)(base + o_detail);
-  wb.bis_left = (int32_t *)(base + o_bis);
-  wb.point = (T *)(base + o_point);
-  wb.iters = (int32_t *)(base + o_iters);
-  wb.count = (int32_t *)(base + o_count);
-  wb.vol = (T *)(base + o_vol);
-  wb.shadow = (T *)(base + o_shadow);
-  wb.ao = (T *)(base + o_ao);
-  wb.hit_list = (uint32_t *)(base + o_hit);
-  wb.polish_list = (uint32_t *)(base + o_pol);
-  wb.overflow_list = (uint32_t *)(base + o_ovl);
-  wb.ctl = (uint32_t *)(base + o_ctl);
-  wb.last_chunk = (int32_t *)(base + o_last);
-  wb.pool_step = (T *)(base + o_pstep);
-  wb.pool_dist = (T *)(base + o_pdist);
-  wb.pool_thr = (T *)(base + o_pthr);
-  wb.pool_prev = (int32_t *)(base + o_pprev);
-  wb.pool_cap = poolCap;
+  wb.flags = (uint8_t *)(base + w.flags);
+  wb.scan = (T *)(base + w.scan);
+  wb.dist = (T *)(base + w.dist);
+  wb.thr = (T *)(base + w.thr);
+  wb.step = (T *)(base + w.step);
+  wb.detail = (T *)(base + w.detail);
+  wb.bis_left = (int32_t *)(base + w.bis);
+  wb.point = (T *)(base + w.point);
+  wb.iters = (int32_t *)(base + w.iters);
+  wb.count = (int32_t *)(base + w.count);
+  wb.vol = (T *)(base + w.vol);
+  wb.shadow = (T *)(base + w.shadow);
+  wb.ao = (T *)(base + w.ao);
+  wb.hit_list = (uint32_t *)(base + w.hit);
+  wb.polish_list = (uint32_t *)(base + w.pol);
+  wb.overflow_list = (uint32_t *)(base + w.ovl);
+  wb.ctl = ctl;
+  wb.last_chunk = (int32_t *)(base + w.last);
+  wb.pool_step = (T *)(base + w.pstep);
+  wb.pool_dist = (T *)(base + w.pdist);
+  wb.pool_thr = (T *)(base + w.pthr);
+  wb.pool_prev = (int32_t *)(base + w.pprev);
+  wb.pool_cap = w.poolCap;
   wb.polish_all = o.polish_all;
-  wb.npix = npix;
-  MBGB_CUDA(cudaMemsetAsync(wb.ctl, 0, 64, s));
+  wb.refill_min = g.cfg.refill;
+  wb.exact_hit = o.exact_hit ? 1 : 0;
+  wb.npix = g.npix;
+  MBGB_CUDA(cudaMemsetAsync(ctl, 0, 64, s));
 
-  int occ1 = (sizeof(T) == 8) ? occupancy_wave_f64(scene->formula, block, 0) : occupancy_wave_f32(scene->formula, block, 0);
-  int occ2 = (sizeof(T) == 8) ? occupancy_wave_f64(scene->formula, block, 1) : occupancy_wave_f32(scene->formula, block, 1);
-  if (occ1 < 1) occ1 = 1;
-  if (occ2 < 1) occ2 = 1;
-  if (o.ctas_per_sm > 0) {
-    occ1 = std::min(occ1, o.ctas_per_sm);
-    occ2 = std::min(occ2, o.ctas_per_sm);
+  const int block = g.cfg.block;
+  int occ1 = std::max(1, wave_occupancy<T>(scene.formula, block, 0));
+  int occ2 = std::max(1, wave_occupancy<T>(scene.formula, block, 1));
+  if (g.cfg.ctasPerSm > 0) {
+    occ1 = std::min(occ1, g.cfg.ctasPerSm);
+    occ2 = std::min(occ2, g.cfg.ctasPerSm);
   }
   L.grid = c->sms * occ1;
   L.grid2 = c->sms * occ2;
   L.block = block;
-  L.ov_grid = kOverflowThreads / block > 0 ? kOverflowThreads / block : 1;
+  L.ov_grid = std::max(1, kOverflowThreads / block);
   L.polish_grid = c->sms * 8;
-  const int64_t nrow = (int64_t)(o.row_end - o.row_begin) * scene->image_width;
-  L.compose_grid = (int)std::min<int64_t>((nrow + block - 1) / block, (int64_t)c->sms * 32);
-  if (L.compose_grid < 1) L.compose_grid = 1;
-  const int64_t slots = (int64_t)L.grid * block;
-  io.slots = slots;
+  L.compose_grid = (int)std::max<int64_t>(1, std::min<int64_t>((g.npix + block - 1) / block, (int64_t)c->sms * 32));
+  L.cams = (const FrameCam<T> *)((char *)c->cams.ptr + g.cams_off);
+  L.gcams = grad ? (const GradCam<T> *)((char *)c->cams.ptr + g.grad_off) : nullptr;
+  L.grad_grid = L.compose_grid;
+  L.ncams = (int)g.frames.size();
+  io.slots = (int64_t)L.grid * block;
   io.step_cap = kStepCap;
   io.overflow_pass = 0;
-  const size_t esz = sizeof(T);
-  if (needVol) {
-    const size_t bytes = (size_t)kStepCap * (size_t)slots * esz;
-    const size_t obytes = (size_t)kStepSlots * (size_t)kOverflowThreads * esz;
-    for (int k = 0; k < 3; k++) {
-      MBGB_CUDA(c->step[prec][k].ensure(bytes));
-      MBGB_CUDA(c->ovstep[prec][k].ensure(obytes));
-    }
-    io.step_step = c->step[prec][0].ptr;
-    io.step_dist = c->step[prec][1].ptr;
-    io.step_thr = c->step[prec][2].ptr;
-  }
   L.io = io;
   L.ov = io;
   L.ov.overflow_pass = 1;
@@ -558,121 +806,49 @@ static mbgb_status render_wave(mbgb_context *c, const mbgb_scene *scene, const m
   L.ov.step_dist = c->ovstep[prec][1].ptr;
   L.ov.step_thr = c->ovstep[prec][2].ptr;
   L.overflow = needVol;
-  for (int k = 0; k < 5; k++) L.ev[k] = o.profile_stages ? c->sev[k] : nullptr;
-  L.fast = fast_mandelbox(*scene) || fast_mandelbulb(*scene);
-  fill_fractal<double>(*scene, L.fd);
-  fill_params<T>(*scene, L.p, o, (const T *)(sizeof(T) == 8 ? c->ao64.ptr : c->ao32.ptr), c->ao_count);
+  for (int k = 0; k < 5; k++) L.ev[k] = ev ? ev[k] : nullptr;
+  L.fast = fast_mandelbox(scene) || fast_mandelbulb(scene);
+  fill_fractal<double>(scene, L.fd);
+  fill_params<T>(scene, L.p, o, (const T *)(prec == 0 ? c->ao64.ptr : c->ao32.ptr), c->ao_count);
   cudaError_t e;
   if constexpr (sizeof(T) == 8) e = launch_wave_f64(L, s);
   else e = launch_wave_f32(L, s);
   if (e != cudaSuccess) return cuda_error(e, "wavefront launch");
-  *long_rays_ctl = wb.ctl + 3;
-  (void)img;
+  *launches += 3 + (needVol ? 1 : 0) + (prec == 1 ? 1 : 0) + (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
   return MBGB_OK;
 }
 
-static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *img,
-                                      const mbgb_opts *opts_in) {
-  if (!c || !scene || !img) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
-  mbgb_status st = mbgb_scene_supported(scene);
-  if (st != MBGB_OK) return st;
-  if (img->width != scene->image_width || img->height != scene->image_height)
-    return set_error(MBGB_ERR_BAD_PARAM, "image size does not match the scene");
-  mbgb_opts o{};
-  if (opts_in) o = *opts_in;
-  if (o.precision < 0 || o.precision > 2) return set_error(MBGB_ERR_BAD_PARAM, "unknown precision policy");
-  if (o.row_end == 0) o.row_end = scene->image_height;
-  if (o.row_begin < 0 || o.row_end > scene->image_height || o.row_begin >= o.row_end)
-    return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
-  MBGB_CUDA(cudaSetDevice(c->device));
-  cudaStream_t s = o.stream ? (cudaStream_t)o.stream : c->stream;
-  int prec = (o.precision == MBGB_PREC_FP64) ? 0 : 1;
-  if (o.precision == MBGB_PREC_AUTO) {
-    // Deep-zoom rule: FP64 for the whole frame when the pixel footprint at the nearest
-    // surface, d * resolution * persp / quality with d the FP64 distance estimate at the
-    // ray origin, is below 1e-5 of the scene scale (max(1, |origin|)).
-    ParamsT<double> pp;
-    fill_params<double>(*scene, pp, o, nullptr, 0);
-    double host[5] = {pp.start[0], pp.start[1], pp.start[2], 0.0, 0.0};
-    host[3] = 1e-300;
-    MBGB_CUDA(c->probe.ensure(128));
-    char *pb = (char *)c->probe.ptr;
-    MBGB_CUDA(cudaMemcpyAsync(pb, host, 4 * sizeof(double), cudaMemcpyHostToDevice, s));
-    FractalT<double> fp;
-    fill_fractal<double>(*scene, fp);
-    cudaError_t pe = launch_distance_f64(scene->formula, fp, (const double *)pb, (const double *)(pb + 24), 1,
-                                         (double *)(pb + 32), (int *)(pb + 40), (unsigned char *)(pb + 44), nullptr, s);
-    if (pe != cudaSuccess) return cuda_error(pe, "precision probe");
-    double d = 0.0;
-    MBGB_CUDA(cudaMemcpyAsync(&d, pb + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
-    MBGB_CUDA(cudaStreamSynchronize(s));
-    const double scale = std::max(1.0, sqrt(host[0] * host[0] + host[1] * host[1] + host[2] * host[2]));
-    const double footprint = scene->constantDEThreshold ? scene->quality
-                                                        : d * scene->resolution * scene->persp / scene->quality;
-    prec = footprint < 1e-5 * scale ? 0 : 1;
-    c->stats.auto_fp64 = prec == 0;
-  }
-  st = ensure_ao(c, scene->globalIlumQuality, s);
-  if (st != MBGB_OK) return st;
-
-  const int block = o.threads_per_cta > 0 ? o.threads_per_cta : 128;
-  if (block % 32 != 0 || block > 128) return set_error(MBGB_ERR_BAD_PARAM, "threads_per_cta must be a multiple of 32, <= 128");
-  int per_sm = occupancy_render(prec, scene->formula, block);
-  if (per_sm < 1) per_sm = 1;
-  if (o.ctas_per_sm > 0) per_sm = std::min(per_sm, o.ctas_per_sm);
+// Enqueue the per-pixel engine (render_core.cuh) for one frame: main pass, then (when
+// the step buffer is in use) the overflow pass.
+static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, const mbgb_image &img,
+                                     const Group &g, const mbgb_opts &o, cudaStream_t s, FrameIO io, char *fctl,
+                                     uint64_t *launches) {
+  const int prec = g.prec;
+  const int block = g.cfg.block;
+  int per_sm = std::max(1, occupancy_render(prec, scene.formula, block));
+  if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
   const int grid = c->sms * per_sm;
-  const int64_t slots = (int64_t)grid * block;
-
-  FrameIO io{};
-  io.image_float = img->image_float;
-  io.zbuffer = img->zbuffer;
-  io.alpha = img->alpha;
-  io.opacity = img->opacity;
-  io.colour = img->colour;
-  io.hit = img->hit;
-  io.iters = img->iters;
-  io.depth = img->depth;
-  io.slots = slots;
+  io.image_float = img.image_float;
+  io.zbuffer = img.zbuffer;
+  io.alpha = img.alpha;
+  io.opacity = img.opacity;
+  io.colour = img.colour;
+  io.hit = img.hit;
+  io.iters = img.iters;
+  io.depth = img.depth;
+  io.slots = (int64_t)grid * block;
   io.step_cap = kStepCap;
   io.overflow_pass = 0;
-  const bool needVol = (scene->glow_intensity != 0.0) || scene->fogEnabled || (scene->fogDensity > 0.0);
-  const size_t esz = prec == 0 ? sizeof(double) : sizeof(float);
-  const bool rayAOjobs = scene->global_ilumination && !scene->fastGlobalIllumination;
-  const double jobs = (double)scene->image_width * scene->image_height * (1.0 + (rayAOjobs ? c->ao_count : 0));
-  const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && jobs < 4.0e9;
-  if (needVol && !wave) {
-    const size_t bytes = (size_t)kStepCap * (size_t)slots * esz;
-    const size_t obytes = (size_t)kStepSlots * (size_t)kOverflowThreads * esz;
-    for (int k = 0; k < 3; k++) {
-      MBGB_CUDA(c->step[prec][k].ensure(bytes));
-      MBGB_CUDA(c->ovstep[prec][k].ensure(obytes));
-    }
-    MBGB_CUDA(c->ovlist.ensure((size_t)scene->image_width * scene->image_height * sizeof(unsigned int)));
+  io.tile_counter = (unsigned int *)(fctl + 0);
+  io.overflow_count = (unsigned int *)(fctl + 4);
+  const bool needVol = need_volumetric(scene);
+  if (needVol) {
     io.step_step = c->step[prec][0].ptr;
     io.step_dist = c->step[prec][1].ptr;
     io.step_thr = c->step[prec][2].ptr;
     io.overflow_list = (unsigned int *)c->ovlist.ptr;
   }
-  MBGB_CUDA(c->control.ensure(256));
-  char *ctl = (char *)c->control.ptr;
-  io.tile_counter = (unsigned int *)(ctl + 0);
-  io.overflow_count = (unsigned int *)(ctl + 4);
-  io.error_flag = (int *)(ctl + 16);
-  io.counters = (unsigned long long *)(ctl + 64);
-  io.start_ns = (unsigned long long *)(ctl + 32);
-  io.budget_ns = o.deadline_ms > 0 ? (unsigned long long)o.deadline_ms * 1000000ull : 0ull;
-  MBGB_CUDA(cudaMemsetAsync(ctl, 0, 256, s));
-  FractalT<double> fd;
-  fill_fractal<double>(*scene, fd);
-  MBGB_CUDA(cudaEventRecord(c->ev0, s));
-  cudaError_t e;
-  uint32_t *longRays = (uint32_t *)(ctl + 4);
-  if (wave) {
-    mbgb_status ws = prec == 0 ? render_wave<double>(c, scene, img, o, s, 0, io, needVol, &longRays)
-                               : render_wave<float>(c, scene, img, o, s, 1, io, needVol, &longRays);
-    if (ws != MBGB_OK) return ws;
-  }
-  // per-pixel engine: main pass, then (when the step buffer is in use) the overflow pass
+  MBGB_CUDA(cudaMemsetAsync(fctl, 0, 64, s));
   FrameIO ov = io;
   ov.overflow_pass = 1;
   ov.step_cap = kStepSlots;
@@ -680,62 +856,557 @@ static mbgb_status render_device_impl(mbgb_context *c, const mbgb_scene *scene, 
   ov.step_step = c->ovstep[prec][0].ptr;
   ov.step_dist = c->ovstep[prec][1].ptr;
   ov.step_thr = c->ovstep[prec][2].ptr;
-  const int ovBlocks = kOverflowThreads / block > 0 ? kOverflowThreads / block : 1;
-  if (wave) {
-    e = cudaSuccess;
-  } else if (prec == 0) {
+  const int ovBlocks = std::max(1, kOverflowThreads / block);
+  FractalT<double> fd;
+  fill_fractal<double>(scene, fd);
+  cudaError_t e;
+  if (prec == 0) {
     ParamsT<double> p;
-    fill_params<double>(*scene, p, o, (const double *)c->ao64.ptr, c->ao_count);
-    e = launch_render_f64(scene->formula, p, fd, io, grid, block, s);
-    if (e == cudaSuccess && needVol) e = launch_render_f64(scene->formula, p, fd, ov, ovBlocks, block, s);
+    fill_params<double>(scene, p, o, (const double *)c->ao64.ptr, c->ao_count);
+    e = launch_render_f64(scene.formula, p, fd, io, grid, block, s);
+    if (e == cudaSuccess && needVol) e = launch_render_f64(scene.formula, p, fd, ov, ovBlocks, block, s);
   } else {
     ParamsT<float> p;
-    fill_params<float>(*scene, p, o, (const float *)c->ao32.ptr, c->ao_count);
-    e = launch_render_f32(scene->formula, p, fd, io, grid, block, s);
-    if (e == cudaSuccess && needVol) e = launch_render_f32(scene->formula, p, fd, ov, ovBlocks, block, s);
+    fill_params<float>(scene, p, o, (const float *)c->ao32.ptr, c->ao_count);
+    e = launch_render_f32(scene.formula, p, fd, io, grid, block, s);
+    if (e == cudaSuccess && needVol) e = launch_render_f32(scene.formula, p, fd, ov, ovBlocks, block, s);
   }
   if (e != cudaSuccess) return cuda_error(e, "render kernel launch");
-  MBGB_CUDA(cudaEventRecord(c->ev1, s));
-  if (!o.stream) {
-    MBGB_CUDA(cudaStreamSynchronize(s));
-    unsigned long long cnt[16];
-    int flag = 0;
-    unsigned int nover = 0;
-    MBGB_CUDA(cudaMemcpy(cnt, ctl + 64, sizeof(cnt), cudaMemcpyDeviceToHost));
-    for (int k = 0; k < 4; k++) {
-      c->stats.stage_orbit[k] = cnt[4 * k + 0];
-      c->stats.stage_de[k] = cnt[4 * k + 1];
-      c->stats.stage_ms[k] = 0.0;
-      if (wave && o.profile_stages) {
-        float sm = 0;
-        if (cudaEventElapsedTime(&sm, c->sev[k], c->sev[k + 1]) == cudaSuccess) c->stats.stage_ms[k] = sm;
+  *launches += 1 + (needVol ? 1 : 0);
+  return MBGB_OK;
+}
+
+// MBGB_PREC_AUTO, deep-zoom rule: FP64 for the whole frame when the pixel footprint at the
+// nearest surface, d * resolution * persp / quality with d the FP64 distance estimate at
+// the ray origin, is below 1e-5 of the scene scale (max(1, |origin|)). One probe launch
+// covers every frame of the call.
+static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int n, const mbgb_opts &o,
+                                  cudaStream_t s, std::vector<int> &prec) {
+  std::vector<double> pts(3 * (size_t)n), det((size_t)n, 1e-300);
+  for (int i = 0; i < n; i++) {
+    ParamsT<double> pp;
+    fill_params<double>(scenes[i], pp, o, nullptr, 0);
+    for (int k = 0; k < 3; k++) pts[3 * i + k] = pp.start[k];
+  }
+  const size_t nb = (size_t)n;
+  const size_t o_pts = 0, o_det = o_pts + 24 * nb, o_d = o_det + 8 * nb, o_it = o_d + 8 * nb, o_mi = o_it + 4 * nb;
+  MBGB_CUDA(c->ensure(c->probe, o_mi + nb + 16));
+  char *pb = (char *)c->probe.ptr;
+  MBGB_CUDA(cudaMemcpyAsync(pb + o_pts, pts.data(), 24 * nb, cudaMemcpyHostToDevice, s));
+  MBGB_CUDA(cudaMemcpyAsync(pb + o_det, det.data(), 8 * nb, cudaMemcpyHostToDevice, s));
+  std::vector<double> d((size_t)n, 0.0);
+  // frames of one call may differ in fractal parameters: one probe per distinct fractal
+  for (int i = 0; i < n; i++) {
+    FractalT<double> fp;
+    fill_fractal<double>(scenes[i], fp);
+    cudaError_t pe = launch_distance_f64(scenes[i].formula, fp, (const double *)(pb + o_pts) + 3 * i,
+                                         (const double *)(pb + o_det) + i, 1, (double *)(pb + o_d) + i,
+                                         (int *)(pb + o_it) + i, (unsigned char *)(pb + o_mi) + i, nullptr, s);
+    if (pe != cudaSuccess) return cuda_error(pe, "precision probe");
+  }
+  MBGB_CUDA(cudaMemcpyAsync(d.data(), pb + o_d, 8 * nb, cudaMemcpyDeviceToHost, s));
+  MBGB_CUDA(cudaStreamSynchronize(s));
+  prec.assign((size_t)n, 1);
+  for (int i = 0; i < n; i++) {
+    const double *st = &pts[3 * i];
+    const double scale = std::max(1.0, sqrt(st[0] * st[0] + st[1] * st[1] + st[2] * st[2]));
+    const double footprint = scenes[i].constantDEThreshold
+                                 ? scenes[i].quality
+                                 : d[i] * scenes[i].resolution * scenes[i].persp / scenes[i].quality;
+    prec[i] = footprint < 1e-5 * scale ? 0 : 1;
+  }
+  return MBGB_OK;
+}
+
+static mbgb_status check_opts(const mbgb_opts &o) {
+  if (o.precision < 0 || o.precision > 2) return set_error(MBGB_ERR_BAD_PARAM, "unknown precision policy");
+  if (o.threads_per_cta != 0 && (o.threads_per_cta % 32 != 0 || o.threads_per_cta < 32 || o.threads_per_cta > 128))
+    return set_error(MBGB_ERR_BAD_PARAM, "threads_per_cta must be a multiple of 32, <= 128");
+  if ((o.tile_w != 0 || o.tile_h != 0) && (o.tile_w <= 0 || o.tile_h <= 0 || o.tile_w * o.tile_h != 32))
+    return set_error(MBGB_ERR_BAD_PARAM, "tile_w x tile_h must be 32");
+  if (o.refill_min < 0 || o.refill_min > 32) return set_error(MBGB_ERR_BAD_PARAM, "refill_min must be in [0, 32]");
+  if (o.ctas_per_sm < 0) return set_error(MBGB_ERR_BAD_PARAM, "negative ctas_per_sm");
+  if (o.row_begin < 0 || o.row_end < 0) return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
+  return MBGB_OK;
+}
+
+// Largest number of pixels x (1 + ray-AO directions) one wavefront group indexes with
+// 32-bit pixel and job numbers.
+constexpr double kMaxGroupJobs = 4.0e9;
+
+static void key_append(std::vector<char> &k, const void *p, size_t n) {
+  k.insert(k.end(), (const char *)p, (const char *)p + n);
+}
+
+// The ray-traced AO direction table of a call: a context holds one table, so the frames
+// that trace AO rays must share its quality (fast AO and frames without AO read none).
+static mbgb_status ensure_call_ao(mbgb_context *c, const mbgb_scene *scenes, int n, cudaStream_t s) {
+  int q = -1;
+  for (int i = 0; i < n; i++) {
+    if (!scenes[i].global_ilumination || scenes[i].fastGlobalIllumination) continue;
+    if (q < 0) q = scenes[i].globalIlumQuality;
+    else if (scenes[i].globalIlumQuality != q)
+      return set_error(MBGB_ERR_BAD_PARAM, "frames of one call that trace AO rays must share the AO quality");
+  }
+  if (q < 0) q = scenes[0].globalIlumQuality;
+  return ensure_ao(c, q, s);
+}
+
+static mbgb_status read_back(mbgb_context *c, const CallPlan &plan, int replayed);
+static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const mbgb_opts &o, cudaStream_t s,
+                                 mbgb_tuning *out);
+
+// Every render call: validate, plan the groups, prepare scratch and frame tables, enqueue
+// (or capture once and replay), and, for calls without a caller stream, wait and read the
+// counters back.
+static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int n, const mbgb_image *imgs,
+                                 const mbgb_opts *opts_in, const GradRequest *grad = nullptr) {
+  if (!c || !scenes || !imgs) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
+  if (n < 1) return set_error(MBGB_ERR_BAD_PARAM, "no frames");
+  mbgb_opts o{};
+  if (opts_in) o = *opts_in;
+  if (grad) {
+    o.exact_hit = 1;
+    o.engine = MBGB_ENGINE_WAVEFRONT;
+    o.use_graph = 0;
+  }
+  mbgb_status st = check_opts(o);
+  if (st != MBGB_OK) return st;
+  for (int i = 0; i < n; i++) {
+    st = mbgb_scene_supported(&scenes[i]);
+    if (st == MBGB_OK && o.exact_hit) st = level_set_supported(scenes[i]);
+    if (st == MBGB_OK && grad) st = grad_supported(scenes[i]);
+    if (st != MBGB_OK) return n > 1 ? set_error(st, "frame " + std::to_string(i) + ": " + mbgb_last_error()) : st;
+    if (imgs[i].width != scenes[i].image_width || imgs[i].height != scenes[i].image_height)
+      return set_error(MBGB_ERR_BAD_PARAM, "image size does not match the scene");
+    const int r1 = o.row_end == 0 ? scenes[i].image_height : o.row_end;
+    if (o.row_begin >= r1 || r1 > scenes[i].image_height)
+      return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
+  }
+  MBGB_CUDA(cudaSetDevice(c->device));
+  cudaStream_t s = o.stream ? (cudaStream_t)o.stream : c->stream;
+  const bool sync = o.stream == nullptr;
+
+  // a captured graph of the same frames, outputs and options is replayed as it is
+  std::vector<char> key;
+  if (o.use_graph) {
+    mbgb_opts ko = o;
+    ko.stream = nullptr;
+    key_append(key, &n, sizeof(n));
+    key_append(key, scenes, sizeof(mbgb_scene) * (size_t)n);
+    key_append(key, imgs, sizeof(mbgb_image) * (size_t)n);
+    key_append(key, &ko, sizeof(ko));
+    if (c->graph && key == c->graph_key) {
+      st = ensure_call_ao(c, scenes, n, s);
+      if (st != MBGB_OK) return st;
+      if (c->gen == c->graph_gen) {
+        if (!c->cams_hold_graph && !c->graph_cams.empty()) {
+          MBGB_CUDA(cudaMemcpyAsync(c->cams.ptr, c->graph_cams.data(), c->graph_cams.size(), cudaMemcpyHostToDevice,
+                                    s));
+          c->cams_hold_graph = true;
+        }
+        MBGB_CUDA(cudaEventRecord(c->ev0, s));
+        MBGB_CUDA(cudaGraphLaunch(c->graph, s));
+        MBGB_CUDA(cudaEventRecord(c->ev1, s));
+        c->plan = c->graph_plan;
+        return sync ? read_back(c, c->plan, 1) : MBGB_OK;
       }
     }
-    for (int k = 1; k < 4; k++) {
-      cnt[0] += cnt[4 * k + 0];
-      cnt[1] += cnt[4 * k + 1];
-      cnt[2] += cnt[4 * k + 2];
-      cnt[3] += cnt[4 * k + 3];
-    }
-    MBGB_CUDA(cudaMemcpy(&flag, ctl + 16, sizeof(flag), cudaMemcpyDeviceToHost));
-    MBGB_CUDA(cudaMemcpy(&nover, longRays, sizeof(nover), cudaMemcpyDeviceToHost));
-    c->stats.long_rays = nover;
-    c->stats.fp64_polished = 0;
-    if (wave && prec == 1) {
-      uint32_t npol = 0;
-      MBGB_CUDA(cudaMemcpy(&npol, longRays + 3, sizeof(npol), cudaMemcpyDeviceToHost));
-      c->stats.fp64_polished = npol;
-    }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    c->stats.orbit_iterations = cnt[0];
-    c->stats.de_calls = cnt[1];
-    c->stats.primary_steps = cnt[2];
-    c->stats.missed_de = cnt[3];
-    c->stats.pixels = (uint64_t)(o.row_end - o.row_begin) * (uint64_t)scene->image_width;
-    c->stats.kernel_ms = ms;
-    if (flag) return set_error(MBGB_ERR_TIMEOUT, "render stopped at its device deadline");
   }
+
+  // precision per frame
+  std::vector<int> prec((size_t)n, o.precision == MBGB_PREC_FP64 ? 0 : 1);
+  if (o.precision == MBGB_PREC_AUTO) {
+    st = auto_precision(c, scenes, n, o, s, prec);
+    if (st != MBGB_OK) return st;
+  }
+  st = ensure_call_ao(c, scenes, n, s);
+  if (st != MBGB_OK) return st;
+  if (o.autotune) {
+    // tune once per scene class, on the call's largest frame of that class
+    for (int i = 0; i < n; i++) {
+      if (c->tunings.count(tune_key(scenes[i], prec[i]))) continue;
+      int best = i;
+      for (int j = i + 1; j < n; j++)
+        if (tune_key(scenes[j], prec[j]) == tune_key(scenes[i], prec[i]) &&
+            (int64_t)scenes[j].image_width * scenes[j].image_height >
+                (int64_t)scenes[best].image_width * scenes[best].image_height)
+          best = j;
+      mbgb_opts to = o;
+      to.precision = prec[best] == 0 ? MBGB_PREC_FP64 : MBGB_PREC_FP32_FIX;
+      to.use_graph = 0;
+      mbgb_tuning t;
+      st = autotune_impl(c, &scenes[best], to, s, &t);
+      if (st != MBGB_OK) return st;
+    }
+  }
+
+  // groups: frames with equal shared parameters and precision render in one launch sequence
+  CallPlan plan;
+  plan.frames = (uint64_t)n;
+  plan.profile = o.profile_stages && !o.use_graph;
+  plan.grad = grad != nullptr;
+  for (int i = 0; i < n; i++) {
+    const mbgb_scene &sc = scenes[i];
+    const int r0 = o.row_begin, r1 = o.row_end == 0 ? sc.image_height : o.row_end;
+    plan.pixels += (uint64_t)(r1 - r0) * (uint64_t)sc.image_width;
+    const LaunchCfg cfg = resolve_cfg(c, o, sc, prec[i]);
+    const int64_t fpix = (int64_t)sc.image_width * sc.image_height;
+    const int64_t fjobs = (int64_t)((sc.image_width + cfg.tileW - 1) / cfg.tileW) *
+                          ((r1 - r0 + cfg.tileH - 1) / cfg.tileH) * 32;
+    const bool rayAO = sc.global_ilumination && !sc.fastGlobalIllumination;
+    const double perPix = 1.0 + (rayAO ? c->ao_count : 0);
+    const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && (double)std::max(fpix, fjobs) * perPix < kMaxGroupJobs;
+    if (!wave && (grad || o.exact_hit))
+      return set_error(MBGB_ERR_BAD_PARAM, "exact hits and gradients need the wavefront engine and frames below 4e9 rays");
+    Group *g = nullptr;
+    if (wave) {
+      for (auto &h : plan.groups) {
+        if (!h.wave || h.prec != prec[i]) continue;
+        if ((double)std::max(h.npix + fpix, h.jobs + fjobs) * perPix >= kMaxGroupJobs) continue;
+        const mbgb_scene &rep = scenes[h.frames[0]];
+        const bool same = prec[i] == 0 ? same_shared<double>(rep, sc, o) : same_shared<float>(rep, sc, o);
+        if (!same) continue;
+        const LaunchCfg &hc = h.cfg;
+        if (hc.tileW != cfg.tileW || hc.tileH != cfg.tileH || hc.block != cfg.block ||
+            hc.ctasPerSm != cfg.ctasPerSm || hc.refill != cfg.refill)
+          continue;
+        g = &h;
+        break;
+      }
+    }
+    if (!g) {
+      plan.groups.emplace_back();
+      g = &plan.groups.back();
+      g->prec = prec[i];
+      g->wave = wave;
+      g->cfg = cfg;
+    }
+    g->frames.push_back(i);
+    g->npix += fpix;
+    g->jobs += fjobs;
+  }
+
+  // scratch for the largest group of each kind, frame tables of all groups
+  size_t wave_bytes[2] = {0, 0};
+  bool volPrec[2] = {false, false};
+  int64_t maxPixPerPixel = 0;
+  int64_t maxSlots[2] = {0, 0};
+  size_t camsBytes = 0;
+  for (auto &g : plan.groups) {
+    const mbgb_scene &rep = scenes[g.frames[0]];
+    const bool needVol = need_volumetric(rep);
+    if (needVol) volPrec[g.prec] = true;
+    if (g.wave) {
+      const bool rayAO = rep.global_ilumination && !rep.fastGlobalIllumination;
+      const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
+      wave_bytes[g.prec] = std::max(wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol).total);
+      g.cams_off = camsBytes;
+      const size_t cs = g.prec == 0 ? sizeof(FrameCam<double>) : sizeof(FrameCam<float>);
+      camsBytes += (cs * g.frames.size() + 255) & ~(size_t)255;
+      if (grad) {
+        g.grad_off = camsBytes;
+        const size_t gs = g.prec == 0 ? sizeof(GradCam<double>) : sizeof(GradCam<float>);
+        camsBytes += (gs * g.frames.size() + 255) & ~(size_t)255;
+      }
+    } else if (needVol) {
+      maxPixPerPixel = std::max(maxPixPerPixel, g.npix);
+      int per_sm = std::max(1, occupancy_render(g.prec, rep.formula, g.cfg.block));
+      if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
+      maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_sm * g.cfg.block);
+    }
+  }
+  for (int p = 0; p < 2; p++) {
+    if (wave_bytes[p]) MBGB_CUDA(c->ensure(c->wave[p], wave_bytes[p]));
+    const size_t esz = p == 0 ? sizeof(double) : sizeof(float);
+    if (volPrec[p])
+      for (int k = 0; k < 3; k++)
+        MBGB_CUDA(c->ensure(c->ovstep[p][k], (size_t)kStepSlots * (size_t)kOverflowThreads * esz));
+    if (maxSlots[p])
+      for (int k = 0; k < 3; k++) MBGB_CUDA(c->ensure(c->step[p][k], (size_t)kStepCap * (size_t)maxSlots[p] * esz));
+  }
+  if (maxPixPerPixel) MBGB_CUDA(c->ensure(c->ovlist, (size_t)maxPixPerPixel * sizeof(unsigned int)));
+  MBGB_CUDA(c->ensure(c->control, 256));
+  MBGB_CUDA(c->ensure(c->fctl, 64 * plan.groups.size()));
+  if (grad) MBGB_CUDA(c->ensure(c->gradacc, sizeof(double) * kGradParams * (size_t)n));
+  std::vector<char> camsHost(camsBytes);
+  for (auto &g : plan.groups) {
+    if (!g.wave) continue;
+    int64_t pixBase = 0;
+    uint32_t jobBase = 0;
+    for (size_t k = 0; k < g.frames.size(); k++) {
+      const int i = g.frames[k];
+      const mbgb_scene &sc = scenes[i];
+      const int r0 = o.row_begin, r1 = o.row_end == 0 ? sc.image_height : o.row_end;
+      const uint32_t jobs = (uint32_t)(((sc.image_width + g.cfg.tileW - 1) / g.cfg.tileW) *
+                                       ((r1 - r0 + g.cfg.tileH - 1) / g.cfg.tileH) * 32);
+      if (g.prec == 0) {
+        FrameCam<double> cam;
+        fill_cam<double>(sc, imgs[i], o, g.cfg, cam);
+        cam.pixBase = pixBase;
+        cam.jobBase = jobBase;
+        cam.jobCount = jobs;
+        memcpy(camsHost.data() + g.cams_off + k * sizeof(cam), &cam, sizeof(cam));
+        if (grad) {
+          GradCam<double> gc;
+          fill_grad_cam<double>(sc, *grad, i, (double *)c->gradacc.ptr, gc);
+          memcpy(camsHost.data() + g.grad_off + k * sizeof(gc), &gc, sizeof(gc));
+        }
+      } else {
+        FrameCam<float> cam;
+        fill_cam<float>(sc, imgs[i], o, g.cfg, cam);
+        cam.pixBase = pixBase;
+        cam.jobBase = jobBase;
+        cam.jobCount = jobs;
+        memcpy(camsHost.data() + g.cams_off + k * sizeof(cam), &cam, sizeof(cam));
+        if (grad) {
+          GradCam<float> gc;
+          fill_grad_cam<float>(sc, *grad, i, (double *)c->gradacc.ptr, gc);
+          memcpy(camsHost.data() + g.grad_off + k * sizeof(gc), &gc, sizeof(gc));
+        }
+      }
+      pixBase += (int64_t)sc.image_width * sc.image_height;
+      jobBase += jobs;
+    }
+  }
+  if (camsBytes) {
+    MBGB_CUDA(c->ensure(c->cams, camsBytes));
+    MBGB_CUDA(cudaMemcpyAsync(c->cams.ptr, camsHost.data(), camsBytes, cudaMemcpyHostToDevice, s));
+    c->cams_hold_graph = false;
+  }
+  if (plan.profile) {
+    const size_t want = 5 * plan.groups.size();
+    while (c->gev.size() < want) {
+      cudaEvent_t ev;
+      MBGB_CUDA(cudaEventCreate(&ev));
+      c->gev.push_back(ev);
+    }
+  }
+
+  // enqueue (inside a capture when use_graph)
+  char *ctl = (char *)c->control.ptr;
+  FrameIO io{};
+  io.error_flag = (int *)(ctl + 16);
+  io.start_ns = (unsigned long long *)(ctl + 32);
+  io.counters = (unsigned long long *)(ctl + 64);
+  io.budget_ns = o.deadline_ms > 0 ? (unsigned long long)o.deadline_ms * 1000000ull : 0ull;
+  auto enqueue = [&]() -> mbgb_status {
+    MBGB_CUDA(cudaMemsetAsync(ctl, 0, 256, s));
+    if (grad) MBGB_CUDA(cudaMemsetAsync(c->gradacc.ptr, 0, sizeof(double) * kGradParams * (size_t)n, s));
+    for (size_t gi = 0; gi < plan.groups.size(); gi++) {
+      const Group &g = plan.groups[gi];
+      char *gctl = (char *)c->fctl.ptr + 64 * gi;
+      cudaEvent_t *ev = plan.profile ? &c->gev[5 * gi] : nullptr;
+      mbgb_status r;
+      if (!g.wave) {
+        r = enqueue_per_pixel(c, scenes[g.frames[0]], imgs[g.frames[0]], g, o, s, io, gctl, &plan.launches);
+      } else if (g.prec == 0) {
+        r = enqueue_wave<double>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches);
+      } else {
+        r = enqueue_wave<float>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches);
+      }
+      if (r != MBGB_OK) return r;
+    }
+    return MBGB_OK;
+  };
+  if (o.use_graph) {
+    if (c->graph) {
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+      c->graph_key.clear();
+    }
+    MBGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    st = enqueue();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    if (st != MBGB_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    if (ec != cudaSuccess) return cuda_error(ec, "cudaStreamEndCapture");
+    const cudaError_t ei = cudaGraphInstantiate(&c->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      c->graph = nullptr;
+      return cuda_error(ei, "cudaGraphInstantiate");
+    }
+    c->graph_key = key;
+    c->graph_gen = c->gen;
+    c->graph_plan = plan;
+    c->graph_cams = camsHost;
+    c->cams_hold_graph = true;
+    MBGB_CUDA(cudaEventRecord(c->ev0, s));
+    MBGB_CUDA(cudaGraphLaunch(c->graph, s));
+    MBGB_CUDA(cudaEventRecord(c->ev1, s));
+  } else {
+    MBGB_CUDA(cudaEventRecord(c->ev0, s));
+    st = enqueue();
+    if (st != MBGB_OK) return st;
+    MBGB_CUDA(cudaEventRecord(c->ev1, s));
+  }
+  c->plan = plan;
+  return sync ? read_back(c, plan, 0) : MBGB_OK;
+}
+
+// Wait for the call's stream and fill the context's counters (the reference's globals,
+// src/Render3D.cpp:51-57) from the device.
+static mbgb_status read_back(mbgb_context *c, const CallPlan &plan, int replayed) {
+  MBGB_CUDA(cudaStreamSynchronize(c->stream));
+  MBGB_CUDA(cudaEventSynchronize(c->ev1));
+  char *ctl = (char *)c->control.ptr;
+  unsigned long long cnt[20];
+  int flag = 0;
+  MBGB_CUDA(cudaMemcpy(cnt, ctl + 64, sizeof(cnt), cudaMemcpyDeviceToHost));
+  MBGB_CUDA(cudaMemcpy(&flag, ctl + 16, sizeof(flag), cudaMemcpyDeviceToHost));
+  std::vector<uint32_t> gctl(16 * plan.groups.size());
+  if (!gctl.empty())
+    MBGB_CUDA(cudaMemcpy(gctl.data(), c->fctl.ptr, 64 * plan.groups.size(), cudaMemcpyDeviceToHost));
+  mbgb_stats &S = c->stats;
+  S = mbgb_stats{};
+  for (int k = 0; k < 4; k++) {
+    S.stage_orbit[k] = cnt[4 * k + 0];
+    S.stage_de[k] = cnt[4 * k + 1];
+  }
+  for (size_t gi = 0; gi < plan.groups.size(); gi++) {
+    const Group &g = plan.groups[gi];
+    const uint32_t *q = &gctl[16 * gi];
+    if (g.wave) {
+      S.long_rays += q[3];
+      if (g.prec == 1) S.fp64_polished += q[6];
+      S.level_set_missed += q[7];
+    } else {
+      S.long_rays += q[1];
+    }
+    if (plan.profile) {
+      for (int k = 0; k < 4; k++) {
+        float sm = 0;
+        if (g.wave && cudaEventElapsedTime(&sm, c->gev[5 * gi + k], c->gev[5 * gi + k + 1]) == cudaSuccess)
+          S.stage_ms[k] += sm;
+      }
+    }
+  }
+  for (int k = 1; k < 4; k++) {
+    cnt[0] += cnt[4 * k + 0];
+    cnt[1] += cnt[4 * k + 1];
+    cnt[2] += cnt[4 * k + 2];
+    cnt[3] += cnt[4 * k + 3];
+  }
+  // the gradient stage's counters: orbit iterations, DE calls, pixels differentiated, skipped
+  cnt[0] += cnt[16];
+  cnt[1] += cnt[17];
+  S.grad_pixels = plan.grad ? cnt[18] : 0;
+  S.grad_skipped = plan.grad ? cnt[19] : 0;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  S.orbit_iterations = cnt[0];
+  S.de_calls = cnt[1];
+  S.primary_steps = cnt[2];
+  S.missed_de = cnt[3];
+  S.pixels = plan.pixels;
+  S.frames = plan.frames;
+  S.launches = plan.launches;
+  S.graph_replayed = (uint64_t)replayed;
+  S.kernel_ms = ms;
+  bool anyFp64 = false;
+  for (auto &g : plan.groups) anyFp64 = anyFp64 || g.prec == 0;
+  S.auto_fp64 = anyFp64;
+  if (flag) return set_error(MBGB_ERR_TIMEOUT, "render stopped at its device deadline");
+  return MBGB_OK;
+}
+
+// Autotuner: coordinate search over tile shape, threads per CTA, CTAs per SM and the
+// refill threshold, each candidate timed on the device (best of two after a warm-up).
+static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const mbgb_opts &o_in, cudaStream_t s,
+                                 mbgb_tuning *out) {
+  const int64_t npix = (int64_t)scene->image_width * scene->image_height;
+  MBGB_CUDA(c->ensure(c->tune_out, (size_t)npix * 24 + 1024));
+  char *b = (char *)c->tune_out.ptr;
+  mbgb_image img{};
+  img.width = scene->image_width;
+  img.height = scene->image_height;
+  img.image_float = (float *)b;
+  img.zbuffer = (float *)(b + ((npix * 12 + 255) & ~(int64_t)255));
+  img.alpha = (uint16_t *)((char *)img.zbuffer + ((npix * 4 + 255) & ~(int64_t)255));
+  img.opacity = (uint16_t *)((char *)img.alpha + ((npix * 2 + 255) & ~(int64_t)255));
+  mbgb_opts o = o_in;
+  o.autotune = 0;
+  o.use_graph = 0;
+  o.profile_stages = 0;
+  o.stream = nullptr;
+  o.engine = MBGB_ENGINE_WAVEFRONT;
+  MBGB_CUDA(cudaStreamSynchronize(s));   // earlier work of the caller's stream may use the scratch
+  int trials = 0;
+  auto time_cfg = [&](const LaunchCfg &cfg, double *ms) -> mbgb_status {
+    o.tile_w = cfg.tileW;
+    o.tile_h = cfg.tileH;
+    o.threads_per_cta = cfg.block;
+    o.ctas_per_sm = cfg.ctasPerSm;
+    o.refill_min = cfg.refill;
+    double best = 1e30;
+    for (int r = 0; r < 3; r++) {
+      mbgb_status st = render_frames(c, scene, 1, &img, &o);
+      if (st != MBGB_OK) return st;
+      if (r > 0) best = std::min(best, c->stats.kernel_ms);
+    }
+    trials++;
+    *ms = best;
+    return MBGB_OK;
+  };
+  const int prec = o.precision == MBGB_PREC_FP64 ? 0 : 1;
+  LaunchCfg cur;
+  double curMs = 0;
+  mbgb_status st = time_cfg(cur, &curMs);
+  if (st != MBGB_OK) return st;
+  const double defMs = curMs;
+  auto consider = [&](LaunchCfg cand) -> mbgb_status {
+    double ms = 0;
+    mbgb_status r = time_cfg(cand, &ms);
+    if (r != MBGB_OK) return r;
+    if (ms < curMs) {
+      cur = cand;
+      curMs = ms;
+    }
+    return MBGB_OK;
+  };
+  const int tiles[3][2] = {{16, 2}, {4, 8}, {32, 1}};
+  const LaunchCfg base = cur;
+  for (auto &t : tiles) {
+    LaunchCfg cand = base;
+    cand.tileW = t[0];
+    cand.tileH = t[1];
+    if ((st = consider(cand)) != MBGB_OK) return st;
+  }
+  {
+    LaunchCfg cand = cur;
+    cand.block = 64;
+    if ((st = consider(cand)) != MBGB_OK) return st;
+  }
+  {
+    const int occ = std::max(1, prec == 0 ? occupancy_wave_f64(scene->formula, cur.block, 0)
+                                          : occupancy_wave_f32(scene->formula, cur.block, 0));
+    if (occ >= 2) {
+      LaunchCfg cand = cur;
+      cand.ctasPerSm = occ / 2;
+      if ((st = consider(cand)) != MBGB_OK) return st;
+    }
+  }
+  const LaunchCfg before = cur;
+  for (int rf : {4, 8, 16}) {
+    LaunchCfg cand = before;
+    cand.refill = rf;
+    if ((st = consider(cand)) != MBGB_OK) return st;
+  }
+  mbgb_tuning t{};
+  t.tile_w = cur.tileW;
+  t.tile_h = cur.tileH;
+  t.threads_per_cta = cur.block;
+  t.ctas_per_sm = cur.ctasPerSm;
+  t.refill_min = cur.refill;
+  t.ms = curMs;
+  t.ms_default = defMs;
+  t.trials = trials;
+  c->tunings[tune_key(*scene, prec)] = t;
+  if (out) *out = t;
   return MBGB_OK;
 }
 
@@ -743,57 +1414,128 @@ extern "C" mbgb_status mbgb_render_device(mbgb_context *c, const mbgb_scene *sce
                                           const mbgb_opts *opts) {
   if (!c) return set_error(MBGB_ERR_BAD_PARAM, "NULL context");
   std::lock_guard<std::mutex> lk(c->mu);
-  return render_device_impl(c, scene, out, opts);
+  return render_frames(c, scene, 1, out, opts);
+}
+
+extern "C" mbgb_status mbgb_render_batch(mbgb_context *c, const mbgb_scene *frames, int32_t n,
+                                         const mbgb_image *outs, const mbgb_opts *opts) {
+  if (!c) return set_error(MBGB_ERR_BAD_PARAM, "NULL context");
+  std::lock_guard<std::mutex> lk(c->mu);
+  return render_frames(c, frames, n, outs, opts);
+}
+
+extern "C" mbgb_status mbgb_render_grad(mbgb_context *c, const mbgb_scene *frames, int32_t n,
+                                        const mbgb_image *outs, const float *const *dL_dimage,
+                                        float *const *jacobian, double *dL_dtheta, const mbgb_opts *opts) {
+  if (!c) return set_error(MBGB_ERR_BAD_PARAM, "NULL context");
+  std::lock_guard<std::mutex> lk(c->mu);
+  mbgb_opts o{};
+  if (opts) o = *opts;
+  o.stream = nullptr;   // synchronous: the sums are read back
+  GradRequest gr{dL_dimage, jacobian};
+  mbgb_status st = render_frames(c, frames, n, outs, &o, &gr);
+  if (st != MBGB_OK) return st;
+  if (dL_dtheta)
+    MBGB_CUDA(cudaMemcpy(dL_dtheta, c->gradacc.ptr, sizeof(double) * kGradParams * (size_t)n, cudaMemcpyDeviceToHost));
+  return MBGB_OK;
+}
+
+extern "C" mbgb_status mbgb_autotune(mbgb_context *c, const mbgb_scene *scene, const mbgb_opts *opts,
+                                     mbgb_tuning *out) {
+  if (!c || !scene) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  mbgb_opts o{};
+  if (opts) o = *opts;
+  if (o.precision == MBGB_PREC_AUTO) o.precision = MBGB_PREC_FP32_FIX;
+  o.row_begin = o.row_end = 0;
+  mbgb_status st = check_opts(o);
+  if (st != MBGB_OK) return st;
+  st = mbgb_scene_supported(scene);
+  if (st != MBGB_OK) return st;
+  MBGB_CUDA(cudaSetDevice(c->device));
+  return autotune_impl(c, scene, o, c->stream, out);
+}
+
+// Host-pointer variant of render_frames: device staging per frame and layer, copies in
+// the call (rows outside the row range are not copied back).
+static mbgb_status render_frames_host(mbgb_context *c, const mbgb_scene *scenes, int n, const mbgb_image *outs,
+                                      const mbgb_opts *opts) {
+  if (!c || !scenes || !outs) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
+  if (n < 1) return set_error(MBGB_ERR_BAD_PARAM, "no frames");
+  MBGB_CUDA(cudaSetDevice(c->device));
+  const size_t per_pix[8] = {12, 4, 2, 2, 3, 1, 4, 8};
+  auto layer_ptr = [](const mbgb_image &im, int k) -> void * {
+    switch (k) {
+      case 0: return im.image_float;
+      case 1: return im.zbuffer;
+      case 2: return im.alpha;
+      case 3: return im.opacity;
+      case 4: return im.colour;
+      case 5: return im.hit;
+      case 6: return im.iters;
+      default: return im.depth;
+    }
+  };
+  // staging layout: layer k of frame i at off[i][k]
+  std::vector<size_t> off((size_t)n * 8, 0);
+  size_t total = 0;
+  for (int i = 0; i < n; i++) {
+    if (outs[i].width != scenes[i].image_width || outs[i].height != scenes[i].image_height)
+      return set_error(MBGB_ERR_BAD_PARAM, "image size does not match the scene");
+    const size_t npix = (size_t)outs[i].width * outs[i].height;
+    for (int k = 0; k < 8; k++) {
+      if (!layer_ptr(outs[i], k)) continue;
+      off[8 * i + k] = total;
+      total += (npix * per_pix[k] + 255) & ~(size_t)255;
+    }
+  }
+  MBGB_CUDA(c->ensure(c->out[0], std::max<size_t>(total, 256)));
+  char *stage = (char *)c->out[0].ptr;
+  std::vector<mbgb_image> dev(outs, outs + n);
+  for (int i = 0; i < n; i++) {
+    void *p[8];
+    for (int k = 0; k < 8; k++) p[k] = layer_ptr(outs[i], k) ? stage + off[8 * i + k] : nullptr;
+    dev[i].image_float = (float *)p[0];
+    dev[i].zbuffer = (float *)p[1];
+    dev[i].alpha = (uint16_t *)p[2];
+    dev[i].opacity = (uint16_t *)p[3];
+    dev[i].colour = (uint8_t *)p[4];
+    dev[i].hit = (uint8_t *)p[5];
+    dev[i].iters = (int32_t *)p[6];
+    dev[i].depth = (double *)p[7];
+  }
+  mbgb_opts o{};
+  if (opts) o = *opts;
+  cudaStream_t s = o.stream ? (cudaStream_t)o.stream : c->stream;
+  mbgb_status st = render_frames(c, scenes, n, dev.data(), &o);
+  if (st != MBGB_OK) return st;
+  for (int i = 0; i < n; i++) {
+    const int r0 = o.row_begin, r1 = o.row_end > 0 ? o.row_end : outs[i].height;
+    const size_t rowpix = (size_t)outs[i].width;
+    for (int k = 0; k < 8; k++) {
+      void *h = layer_ptr(outs[i], k);
+      if (!h) continue;
+      const size_t o0 = (size_t)r0 * rowpix * per_pix[k];
+      const size_t len = (size_t)(r1 - r0) * rowpix * per_pix[k];
+      MBGB_CUDA(cudaMemcpyAsync((char *)h + o0, stage + off[8 * i + k] + o0, len, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  MBGB_CUDA(cudaStreamSynchronize(s));
+  return MBGB_OK;
 }
 
 extern "C" mbgb_status mbgb_render_host(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *out,
                                         const mbgb_opts *opts) {
-  if (!c || !scene || !out) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
+  if (!c) return set_error(MBGB_ERR_BAD_PARAM, "NULL context");
   std::lock_guard<std::mutex> lk(c->mu);
-  if (out->width != scene->image_width || out->height != scene->image_height)
-    return set_error(MBGB_ERR_BAD_PARAM, "image size does not match the scene");
-  MBGB_CUDA(cudaSetDevice(c->device));
-  const size_t npix = (size_t)out->width * out->height;
-  struct Layer {
-    void *host;
-    size_t bytes;
-  } layers[8] = {{out->image_float, npix * 12}, {out->zbuffer, npix * 4}, {out->alpha, npix * 2},
-                 {out->opacity, npix * 2},      {out->colour, npix * 3},  {out->hit, npix},
-                 {out->iters, npix * 4},        {out->depth, npix * 8}};
-  void *dev[8] = {nullptr};
-  for (int i = 0; i < 8; i++) {
-    if (!layers[i].host) continue;
-    MBGB_CUDA(c->out[i].ensure(layers[i].bytes));
-    dev[i] = c->out[i].ptr;
-  }
-  mbgb_image d = *out;
-  d.image_float = (float *)dev[0];
-  d.zbuffer = (float *)dev[1];
-  d.alpha = (uint16_t *)dev[2];
-  d.opacity = (uint16_t *)dev[3];
-  d.colour = (uint8_t *)dev[4];
-  d.hit = (uint8_t *)dev[5];
-  d.iters = (int32_t *)dev[6];
-  d.depth = (double *)dev[7];
-  mbgb_opts o{};
-  if (opts) o = *opts;
-  cudaStream_t s = o.stream ? (cudaStream_t)o.stream : c->stream;
-  o.stream = nullptr;  // synchronous render on the context stream
-  if (s != c->stream) o.stream = s;
-  mbgb_status st = render_device_impl(c, scene, &d, &o);
-  if (st != MBGB_OK) return st;
-  // rows outside [row_begin, row_end) are not copied back
-  const int r0 = o.row_begin, r1 = o.row_end > 0 ? o.row_end : out->height;
-  const size_t rowpix = (size_t)out->width;
-  const size_t per_pix[8] = {12, 4, 2, 2, 3, 1, 4, 8};
-  for (int i = 0; i < 8; i++) {
-    if (!layers[i].host) continue;
-    const size_t off = (size_t)r0 * rowpix * per_pix[i];
-    const size_t len = (size_t)(r1 - r0) * rowpix * per_pix[i];
-    MBGB_CUDA(cudaMemcpyAsync((char *)layers[i].host + off, (char *)dev[i] + off, len, cudaMemcpyDeviceToHost, s));
-  }
-  MBGB_CUDA(cudaStreamSynchronize(s));
-  return MBGB_OK;
+  return render_frames_host(c, scene, 1, out, opts);
+}
+
+extern "C" mbgb_status mbgb_render_batch_host(mbgb_context *c, const mbgb_scene *frames, int32_t n,
+                                              const mbgb_image *outs, const mbgb_opts *opts) {
+  if (!c) return set_error(MBGB_ERR_BAD_PARAM, "NULL context");
+  std::lock_guard<std::mutex> lk(c->mu);
+  return render_frames_host(c, frames, n, outs, opts);
 }
 
 extern "C" mbgb_status mbgb_distance_device(mbgb_context *c, const mbgb_scene *scene, int precision,

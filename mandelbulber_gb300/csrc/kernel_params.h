@@ -86,6 +86,32 @@ struct ParamsT {
   int fogCol1[3], fogCol2[3], fogCol3[3];
 };
 
+// Per-frame camera, resolution and output layers of a batch (device memory, one per
+// frame). Everything else of the scene is shared by the batch's frames (ParamsT).
+// Built like MainThread's per-frame set-up (src/Render3D.cpp:213-344).
+template <typename T>
+struct FrameCam {
+  int width, height, tiles, row_begin, row_end, rot_zero;
+  int tileW, tileH;             // pixel tile of one warp's first 32 jobs (autotuned)
+  int64_t pixBase;              // first pixel of the frame in the per-pixel buffers
+  uint32_t jobBase, jobCount;   // primary jobs of the frame: [jobBase, jobBase + jobCount)
+  double tileXOffset, tileYOffset, aspect, fov;
+  double rot[9];
+  float rotf[9];
+  double start[3];
+  T resolution, persp;
+  double resolution_d, persp_d;
+  T lightVect[3];
+  float *image_float;
+  float *zbuffer;
+  uint16_t *alpha;
+  uint16_t *opacity;
+  uint8_t *colour;
+  uint8_t *hit;
+  int32_t *iters;
+  double *depth;
+};
+
 // Output and scratch pointers of one launch (device memory).
 struct FrameIO {
   float *image_float;

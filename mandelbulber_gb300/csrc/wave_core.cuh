@@ -21,43 +21,11 @@
 // job counter hands the free lanes their next jobs (popc of the ballot).
 #pragma once
 
+#include "dual.cuh"
 #include "render_core.cuh"
+#include "wave_launch.h"
 
 namespace mbgb {
-
-// Per-frame SoA buffers of the wavefront stages (device memory).
-template <typename T>
-struct WaveBufs {
-  uint8_t *flags;        // [npix] bit0: hit, bit1: hemisphere cut / not marched
-  T *scan;               // [npix] depth of the primary ray
-  T *dist;               // [npix] last distance (lastDist)
-  T *thr;                // [npix] distThresh at the hit
-  T *step;               // [npix] FP32 policy: bisection step left for the FP64 polish
-  T *detail;             // [npix] detailSize of the march's last step (src/Render3D.cpp:110)
-  int32_t *bis_left;     // [npix] FP32 policy: bisection iterations left
-  T *point;              // [3][npix] hit point in the march precision
-  int32_t *iters;        // [npix] itersOut at the end of the march
-  int32_t *count;        // [npix] buffCount
-  T *vol;                // [6][npix] overflow pass only: A, B.r, B.g, B.b, alpha, opacity
-  T *shadow;             // [npix]
-  T *ao;                 // [aoCount][npix] per-direction shadowTemp
-  uint32_t *hit_list;    // [npix] hits (secondary rays)
-  uint32_t *polish_list; // [npix] hits the FP64 polish re-evaluates
-  uint32_t *ctl;         // [0] primary jobs, [1] hits, [2] secondary jobs, [3] overflow count,
-                         // [4] overflow-pass jobs, [5] pool chunks, [6] polish count (zeroed per frame)
-  uint32_t *overflow_list;
-  // Step records of the primary rays: chunks of kChunk records linked backwards
-  // (prev), allocated by bump counter; the pixel keeps its last chunk.
-  T *pool_step, *pool_dist, *pool_thr;   // [chunk * kChunk + r]
-  int32_t *pool_prev;                    // [chunk]
-  int32_t *last_chunk;                   // [npix], -1 = no records
-  uint32_t pool_cap;                     // chunks
-  int polish_all;                        // 1: every hit takes the FP64 polish
-  int64_t npix;
-};
-
-constexpr int kChunk = 32;       // step records per pool chunk
-constexpr int kPoolChunksPerPixel = 4;   // pool budget; rays beyond it take the overflow pass
 
 namespace dev {
 
@@ -76,12 +44,15 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
   const float cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
   float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
   int L;
+#pragma unroll 3
   for (L = 0; L < N; L++) {
     x = fminf(fmaxf(x, -fl), fl) * 2.0f - x;
     y = fminf(fmaxf(y, -fl), fl) * 2.0f - y;
     z = fminf(fmaxf(z, -fl), fl) * 2.0f - z;
     float r2 = x * x + y * y + z * z;
-    const float k = (r2 < mR2) ? k1 : ((r2 < fR2) ? __fdividef(fR2, r2) : 1.0f);
+    // sphere fold: fR2/mR2 inside mR2, fR2/r2 between mR2 and fR2, 1 outside; the same
+    // value as the clamp of fR2/r2 to [1, fR2/mR2]
+    const float k = fminf(fmaxf(__fdividef(fR2, r2), 1.0f), k1);
     const float ks = k * s;
     x = fmaf(x, ks, cx);
     y = fmaf(y, ks, cy);
@@ -213,74 +184,98 @@ __device__ __forceinline__ unsigned int claim_jobs(unsigned int *counter, const 
   return base + (unsigned int)__popc(mask & ((1u << lane) - 1u));
 }
 
-// Job index -> pixel: 8x4 tiles in row-major tile order, so a warp's first 32 jobs are one tile.
-__device__ __forceinline__ void job_pixel(const int width, const int row_begin, const unsigned int job, int &x,
-                                          int &y) {
-  const int tilesX = (width + kTileW - 1) / kTileW;
-  const unsigned int tile = job / (kTileW * kTileH);
-  const unsigned int inTile = job % (kTileW * kTileH);
-  x = (int)(tile % (unsigned int)tilesX) * kTileW + (int)(inTile % kTileW);
-  y = row_begin + (int)(tile / (unsigned int)tilesX) * kTileH + (int)(inTile / kTileW);
+// Frame of a primary job / of a pixel of the batch (binary search over the frame table).
+template <typename T>
+__device__ __forceinline__ int frame_of_job(const FrameCam<T> *__restrict__ cams, const int n, const unsigned int job) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cams[mid].jobBase <= job) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+template <typename T>
+__device__ __forceinline__ int frame_of_pixel(const FrameCam<T> *__restrict__ cams, const int n, const int64_t gp) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cams[mid].pixBase <= gp) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Job index within a frame -> pixel: tiles of tileW x tileH (32 pixels) in row-major
+// tile order, so a warp's first 32 jobs cover one tile.
+__device__ __forceinline__ void job_pixel(const int width, const int row_begin, const int tileW, const int tileH,
+                                          const unsigned int job, int &x, int &y) {
+  const int tilesX = (width + tileW - 1) / tileW;
+  const unsigned int tile = job / (unsigned int)(tileW * tileH);
+  const unsigned int inTile = job % (unsigned int)(tileW * tileH);
+  x = (int)(tile % (unsigned int)tilesX) * tileW + (int)(inTile % (unsigned int)tileW);
+  y = row_begin + (int)(tile / (unsigned int)tilesX) * tileH + (int)(inTile / (unsigned int)tileW);
 }
 
 // Camera ray of a pixel (src/Render3D.cpp:389-438); returns false for a fisheye-cut pixel.
 template <typename T>
-__device__ __forceinline__ bool camera_ray(const ParamsT<T> &p, const int x, const int y, V3<double> &view) {
-  const double x2 = ((double)x / p.width / p.tiles - 0.5 + p.tileXOffset / p.tiles) * p.aspect;
-  const double z2 = ((double)y / p.height / p.tiles - 0.5 + p.tileYOffset / p.tiles);
+__device__ __forceinline__ bool camera_ray(const ParamsT<T> &p, const FrameCam<T> &c, const int x, const int y,
+                                           V3<double> &view) {
+  const double x2 = ((double)x / c.width / c.tiles - 0.5 + c.tileXOffset / c.tiles) * c.aspect;
+  const double z2 = ((double)y / c.height / c.tiles - 0.5 + c.tileYOffset / c.tiles);
   bool cut = false;
   V3<double> vv;
   if (p.perspType == 1) {
-    if (p.fishEyeCut && sqrt(x2 * x2 + z2 * z2) > 0.5 / p.fov) cut = true;
+    if (p.fishEyeCut && sqrt(x2 * x2 + z2 * z2) > 0.5 / c.fov) cut = true;
     const double x3 = x2 * kPI, z3 = z2 * kPI;
     const double r = sqrt(x3 * x3 + z3 * z3);
     if (r == 0) {
       vv = {0.0, 1.0, 0.0};
     } else {
-      vv.x = x3 / r * sin(r * p.fov);
-      vv.z = z3 / r * sin(r * p.fov);
-      vv.y = cos(r * p.fov);
+      vv.x = x3 / r * sin(r * c.fov);
+      vv.z = z3 / r * sin(r * c.fov);
+      vv.y = cos(r * c.fov);
     }
     vv = normalize3(vv);
   } else if (p.perspType == 2) {
     const double x3 = x2 * kPI, z3 = z2 * kPI;
-    vv.x = sin(p.fov * x3) * cos(p.fov * z3);
-    vv.z = sin(p.fov * z3);
-    vv.y = cos(p.fov * x3) * cos(p.fov * z3);
+    vv.x = sin(c.fov * x3) * cos(c.fov * z3);
+    vv.z = sin(c.fov * z3);
+    vv.y = cos(c.fov * x3) * cos(c.fov * z3);
     vv = normalize3(vv);
   } else {
-    vv = {x2 * p.fov, 1.0, z2 * p.fov};
+    vv = {x2 * c.fov, 1.0, z2 * c.fov};
   }
-  view = rotate(p.rot, p.rot_zero, vv);
+  view = rotate(c.rot, c.rot_zero, vv);
   return !cut;
 }
 
 // Camera ray in the march precision: the FP32 policy forms the three-point-perspective
 // direction in FP32 (the per-frame ray origin stays the FP64 value from the host); the
-// FP64 policy and the fisheye/equirectangular projections use camera_ray below.
+// FP64 policy and the fisheye/equirectangular projections use camera_ray.
 template <typename T>
-__device__ __forceinline__ bool camera_dir(const ParamsT<T> &p, const int x, const int y, V3<T> &dir) {
+__device__ __forceinline__ bool camera_dir(const ParamsT<T> &p, const FrameCam<T> &c, const int x, const int y,
+                                           V3<T> &dir) {
   if (sizeof(T) == 4 && p.perspType != 1 && p.perspType != 2) {
-    const float x2 = ((float)x / (float)p.width / (float)p.tiles - 0.5f + (float)p.tileXOffset / (float)p.tiles) *
-                     (float)p.aspect;
-    const float z2 = ((float)y / (float)p.height / (float)p.tiles - 0.5f + (float)p.tileYOffset / (float)p.tiles);
-    const float fov = (float)p.fov;
+    const float x2 = ((float)x / (float)c.width / (float)c.tiles - 0.5f + (float)c.tileXOffset / (float)c.tiles) *
+                     (float)c.aspect;
+    const float z2 = ((float)y / (float)c.height / (float)c.tiles - 0.5f + (float)c.tileYOffset / (float)c.tiles);
+    const float fov = (float)c.fov;
     const V3<float> vv{x2 * fov, 1.0f, z2 * fov};
-    if (p.rot_zero) {
+    if (c.rot_zero) {
       dir = {(T)vv.x, (T)vv.y, (T)vv.z};
     } else {
-      dir = {(T)(p.rotf[0] * vv.x + p.rotf[1] * vv.y + p.rotf[2] * vv.z),
-             (T)(p.rotf[3] * vv.x + p.rotf[4] * vv.y + p.rotf[5] * vv.z),
-             (T)(p.rotf[6] * vv.x + p.rotf[7] * vv.y + p.rotf[8] * vv.z)};
+      dir = {(T)(c.rotf[0] * vv.x + c.rotf[1] * vv.y + c.rotf[2] * vv.z),
+             (T)(c.rotf[3] * vv.x + c.rotf[4] * vv.y + c.rotf[5] * vv.z),
+             (T)(c.rotf[6] * vv.x + c.rotf[7] * vv.y + c.rotf[8] * vv.z)};
     }
     return true;
   }
   V3<double> view;
-  const bool ok = camera_ray(p, x, y, view);
+  const bool ok = camera_ray(p, c, x, y, view);
   dir = {(T)view.x, (T)view.y, (T)view.z};
   return ok;
 }
-
 
 // The volumetric pass over one ray's records (VolumetricShader's glow, post fog and
 // volumetric fog, src/shaders.cpp:185-478) as the affine map out = A*base + B, plus
@@ -358,57 +353,67 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 }
 
 // ---------------------------------------------------------------------------
-// Stage 1: primary rays with lane refill.
+// Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
 __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const FractalT<double> fd,
-                                                      const FrameIO io, const WaveBufs<T> wb) {
+                                                      const FrameIO io, const WaveBufs<T> wb,
+                                                      const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, io.slots, slot};
   const bool useSB = p.needVolumetric;
   const bool f64 = sizeof(T) == 8;
-  const V3<T> start{(T)p.start[0], (T)p.start[1], (T)p.start[2]};
-  const T thrScale = p.resolution * p.persp / p.quality;
   const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
   const T search_limit = T(1) - T(0.01) * p.quality;
   const int stepCap = io.overflow_pass ? kStepSlots : io.step_cap;
-  // jobs: 8x4 tiles of the row range (partial tiles included), or the overflow list
-  const int tilesX = (p.width + kTileW - 1) / kTileW;
-  const unsigned int nTileJobs =
-      io.overflow_pass ? *(volatile unsigned int *)&wb.ctl[3]
-                       : (unsigned int)(tilesX * ((p.row_end - p.row_begin + kTileH - 1) / kTileH) * kTileW * kTileH);
+  // jobs: every frame's tiles (partial tiles included), or the overflow list
+  const unsigned int nJobs = io.overflow_pass ? *(volatile unsigned int *)&wb.ctl[3]
+                                              : cams[ncams - 1].jobBase + cams[ncams - 1].jobCount;
   Counters cnt{0, 0, 0, 0};
   unsigned int *jobCounter = io.overflow_pass ? (wb.ctl + 4) : (wb.ctl + 0);
 
   // per-lane ray state
   bool active = false, exhausted = false;
-  int pix = 0, phase = 0, i = 0, buffCount = 0, iters = 0, bis = 0;
+  int64_t gp = 0;   // pixel of the batch
+  int phase = 0, i = 0, buffCount = 0, iters = 0, bis = 0;
   int chunk = -1;   // current pool chunk of the ray's step records (main pass)
-  V3<T> dir{T(0), T(0), T(0)};
+  V3<T> dir{T(0), T(0), T(0)}, start{T(0), T(0), T(0)};
+  T res = T(0), persp = T(0), thrScale = T(0);
   T scan = T(0), step = T(0), thr = T(0), dist = T(0), detail = T(0);  // detail: detailSize of the march
   int guardSteps = 0;
   for (;;) {
     // hand out jobs to idle lanes
+    // a warp claims new jobs once refill_min of its lanes are idle, or when none is busy
     const bool need = !active && !exhausted;
-    if (__any_sync(0xffffffffu, need)) {
+    const unsigned int needMask = __ballot_sync(0xffffffffu, need);
+    if (needMask && (__popc(needMask) >= (unsigned int)wb.refill_min || !__any_sync(0xffffffffu, active))) {
       if (io.budget_ns && (threadIdx.x & 31) == 0 && deadline_passed(io)) atomicExch(io.error_flag, 1);
       const bool stop = *(volatile int *)io.error_flag != 0;
       const unsigned int job = claim_jobs(jobCounter, need);
       if (need) {
-        if (stop || job >= nTileJobs) {
+        if (stop || job >= nJobs) {
           exhausted = true;
         } else {
-          int x, y;
+          int x, y, fr;
           if (io.overflow_pass) {
-            pix = (int)wb.overflow_list[job];
-            x = pix % p.width;
-            y = pix / p.width;
+            gp = (int64_t)wb.overflow_list[job];
+            fr = frame_of_pixel(cams, ncams, gp);
+            const int64_t local = gp - cams[fr].pixBase;
+            x = (int)(local % cams[fr].width);
+            y = (int)(local / cams[fr].width);
           } else {
-            job_pixel(p.width, p.row_begin, job, x, y);
-            pix = y * p.width + x;
+            fr = frame_of_job(cams, ncams, job);
+            const FrameCam<T> &c = cams[fr];
+            job_pixel(c.width, c.row_begin, c.tileW, c.tileH, job - c.jobBase, x, y);
+            gp = c.pixBase + (int64_t)y * c.width + x;
           }
-          if (x < p.width && y < p.row_end) {
-            const bool marched = camera_dir(p, x, y, dir);
+          const FrameCam<T> &c = cams[fr];
+          if (x < c.width && y < c.row_end) {
+            const bool marched = camera_dir(p, c, x, y, dir);
+            start = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
+            res = c.resolution;
+            persp = c.persp;
+            thrScale = res * persp / p.quality;
             chunk = -1;
             scan = p.viewDistanceMin;
             step = p.viewDistanceMin;
@@ -422,11 +427,11 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
             active = true;
             if (!marched) {
               // fisheye cut: no march, background with an empty step buffer
-              wb.flags[pix] = 2;
-              wb.scan[pix] = T(0);
-              wb.count[pix] = 0;
-              wb.iters[pix] = 0;
-              wb.last_chunk[pix] = -1;
+              wb.flags[gp] = 2;
+              wb.scan[gp] = T(0);
+              wb.count[gp] = 0;
+              wb.iters[gp] = 0;
+              wb.last_chunk[gp] = -1;
               active = false;
             }
           }
@@ -434,7 +439,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
       }
     }
     if (!__any_sync(0xffffffffu, active)) {
-      if (__all_sync(0xffffffffu, exhausted || !active) && __all_sync(0xffffffffu, exhausted)) break;
+      if (__all_sync(0xffffffffu, exhausted)) break;
       continue;
     }
     if (active) {
@@ -442,7 +447,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
       const V3<T> point = start + dir * scan;
       if (phase == 0) {
         if (p.constantDEThreshold) thr = p.quality;
-        else if (f64) thr = scan * p.resolution * p.persp / p.quality;
+        else if (f64) thr = scan * res * persp / p.quality;
         else thr = scan * thrScale;
         if (p.perspType == 1 || p.perspType == 2) thr *= T(kPI);
         detail = thr;
@@ -458,21 +463,21 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
             sb.dist[sb.at(i)] = dist;
             sb.thr[sb.at(i)] = thr;
           } else {
-            // main pass: records go to the frame's pool in chunks of kChunk
+            // main pass: records go to the batch's pool in chunks of kChunk
             bool full = false;
             if ((i % kChunk) == 0) {
-              const unsigned int c = atomicAdd(wb.ctl + 5, 1u);
-              if (c >= wb.pool_cap) {
+              const unsigned int cc = atomicAdd(wb.ctl + 5, 1u);
+              if (cc >= wb.pool_cap) {
                 full = true;
               } else {
-                wb.pool_prev[c] = chunk;
-                chunk = (int)c;
+                wb.pool_prev[cc] = chunk;
+                chunk = (int)cc;
               }
             }
             if (full) {
               // the pool is spent: re-marched by the overflow pass with slot records
               const unsigned int k = atomicAdd(wb.ctl + 3, 1u);
-              wb.overflow_list[k] = (unsigned int)pix;
+              wb.overflow_list[k] = (unsigned int)gp;
               active = false;
               continue;
             }
@@ -487,8 +492,6 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
           phase = 1;
           step *= T(0.5);
           bis = 0;
-          // FP64 policy and FP32 policy both continue with the bisection here; the FP32
-          // policy finishes it in FP64 in polish_kernel
           if (dist < thr && dist > thr * search_limit) done = true;
         } else {
           if (useSB) {
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
             else wb.pool_step[rec] = step;
           }
           step = (dist - stepFrac * thr) * p.DE_factor;
-          if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)pix, (uint32_t)i)) / T(10000));
+          if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)gp, (uint32_t)i)) / T(10000));
           buffCount++;
           scan += step;
           i++;
@@ -507,7 +510,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
           if (dist > thr) scan += step;
           else if (dist < thr * search_limit) scan -= step;
           if (p.constantDEThreshold) thr = p.quality;
-          else if (f64) thr = scan * p.resolution * p.persp / p.quality;
+          else if (f64) thr = scan * res * persp / p.quality;
           else thr = scan * thrScale;
           bis = 1;
         }
@@ -520,7 +523,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
           if (dist > thr) scan += step;
           else if (dist < thr * search_limit) scan -= step;
           if (p.constantDEThreshold) thr = p.quality;
-          else if (f64) thr = scan * p.resolution * p.persp / p.quality;
+          else if (f64) thr = scan * res * persp / p.quality;
           else thr = scan * thrScale;
           bis++;
         }
@@ -533,34 +536,35 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
           // rare long rays: fold the records now (the slot is reused); compose applies the map
           T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
           volumetric_affine<T>(p, sb, buffCount, scan, found ? T(1) : T(0), vol);
-          for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + pix] = vol[c];
+          for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + gp] = vol[c];
           flags |= 4;
         }
-        wb.flags[pix] = flags;
-        wb.last_chunk[pix] = chunk;
-        wb.scan[pix] = scan;
-        wb.dist[pix] = dist;
-        wb.thr[pix] = thr;
-        wb.step[pix] = step;
-        wb.detail[pix] = detail;
-        wb.bis_left[pix] = 20 - bis;
-        wb.count[pix] = buffCount;
-        wb.iters[pix] = iters;
+        wb.flags[gp] = flags;
+        wb.last_chunk[gp] = chunk;
+        wb.scan[gp] = scan;
+        wb.dist[gp] = dist;
+        wb.thr[gp] = thr;
+        wb.step[gp] = step;
+        wb.detail[gp] = detail;
+        wb.bis_left[gp] = 20 - bis;
+        wb.count[gp] = buffCount;
+        wb.iters[gp] = iters;
         const V3<T> hp = start + dir * scan;
-        wb.point[0 * wb.npix + pix] = hp.x;
-        wb.point[1 * wb.npix + pix] = hp.y;
-        wb.point[2 * wb.npix + pix] = hp.z;
+        wb.point[0 * wb.npix + gp] = hp.x;
+        wb.point[1 * wb.npix + gp] = hp.y;
+        wb.point[2 * wb.npix + gp] = hp.z;
         if (found) {
           const unsigned int k = atomicAdd(wb.ctl + 1, 1u);
-          wb.hit_list[k] = (unsigned int)pix;
+          wb.hit_list[k] = (unsigned int)gp;
           // FP32 policy: the FP64 polish re-checks every hit whose FP32 bisection did not end
-          // clearly inside the window (dist/thr within 1e-4 of an edge, or 20 steps used)
-          if (!f64) {
+          // clearly inside the window (dist/thr within 1e-4 of an edge, or 20 steps used);
+          // exact_hit: every hit goes on to the level-set refinement
+          if (!f64 || wb.exact_hit) {
             const T q = dist / thr;
             const bool clear = (q > search_limit + T(1e-4)) && (q < T(1) - T(1e-4));
-            if (wb.polish_all || !clear) {
+            if (wb.polish_all || wb.exact_hit || !clear) {
               const unsigned int m = atomicAdd(wb.ctl + 6, 1u);
-              wb.polish_list[m] = (unsigned int)pix;
+              wb.polish_list[m] = (unsigned int)gp;
             }
           }
         }
@@ -583,28 +587,31 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
 }
 
 // ---------------------------------------------------------------------------
-// Stage 2 (FP32 policy): finish the binary refinement of every hit in FP64
-// (src/Render3D.cpp:145-183): the distance is re-evaluated in FP64 at the FP32
+// Stage 2 (FP32 policy): finish the binary refinement in FP64 (src/Render3D.cpp:145-183)
+// for the hits on the polish list: the distance is re-evaluated in FP64 at the FP32
 // result and the bisection continues with the iterations it has left.
 // ---------------------------------------------------------------------------
 template <int FORMULA>
 __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, const FractalT<double> fd,
-                                                     const FrameIO io, const WaveBufs<float> wb) {
+                                                     const FrameIO io, const WaveBufs<float> wb,
+                                                     const FrameCam<float> *__restrict__ cams, const int ncams) {
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[6];
   Counters cnt{0, 0, 0, 0};
   const double search_limit = 1.0 - 0.01 * p.quality_d;
-  const V3<double> start{p.start[0], p.start[1], p.start[2]};
   for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += gridDim.x * blockDim.x) {
-    const unsigned int pix = wb.polish_list[k];
-    const int x = (int)(pix % (unsigned int)p.width), y = (int)(pix / (unsigned int)p.width);
+    const int64_t gp = (int64_t)wb.polish_list[k];
+    const FrameCam<float> &c = cams[frame_of_pixel(cams, ncams, gp)];
+    const int64_t local = gp - c.pixBase;
+    const int x = (int)(local % c.width), y = (int)(local / c.width);
     V3<double> dir;
-    camera_ray(p, x, y, dir);
-    double scan = (double)wb.scan[pix];
-    double step = (double)wb.step[pix];
-    const double detail = (double)wb.detail[pix];
-    int left = wb.bis_left[pix];
+    camera_ray(p, c, x, y, dir);
+    const V3<double> start{c.start[0], c.start[1], c.start[2]};
+    double scan = (double)wb.scan[gp];
+    double step = (double)wb.step[gp];
+    const double detail = (double)wb.detail[gp];
+    const int left = wb.bis_left[gp];
     auto thr_of = [&](double sc) {
-      return p.constantDEThreshold ? p.quality_d : sc * p.resolution_d * p.persp_d / p.quality_d;
+      return p.constantDEThreshold ? p.quality_d : sc * c.resolution_d * c.persp_d / p.quality_d;
     };
     double thr = thr_of(scan);
     V3<double> point = start + dir * scan;
@@ -622,17 +629,79 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
       cnt.steps++;
       step *= 0.5;
     }
-    wb.scan[pix] = (float)scan;
-    wb.dist[pix] = (float)dist;
-    wb.thr[pix] = (float)thr;
-    wb.iters[pix] = iters;
-    wb.point[0 * wb.npix + pix] = (float)point.x;
-    wb.point[1 * wb.npix + pix] = (float)point.y;
-    wb.point[2 * wb.npix + pix] = (float)point.z;
+    wb.scan[gp] = (float)scan;
+    wb.dist[gp] = (float)dist;
+    wb.thr[gp] = (float)thr;
+    wb.iters[gp] = iters;
+    wb.point[0 * wb.npix + gp] = (float)point.x;
+    wb.point[1 * wb.npix + gp] = (float)point.y;
+    wb.point[2 * wb.npix + gp] = (float)point.z;
   }
   atomicAdd(&io.counters[0], cnt.orbit);
   atomicAdd(&io.counters[1], cnt.calls);
   atomicAdd(&io.counters[2], cnt.steps);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2b (exact_hit, both policies; the differentiable render's forward pass): after
+// the binary refinement, Newton steps in FP64 move every hit on the polish list onto the
+// level set DE = thr. A hit that does not get there keeps its bisection result and is
+// flagged (bit 3) so the gradient stage leaves it out.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA>
+__global__ void __launch_bounds__(128) level_set_kernel(const ParamsT<T> p, const FractalT<double> fd,
+                                                        const WaveBufs<T> wb, const FrameCam<T> *__restrict__ cams,
+                                                        const int ncams) {
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[6];
+  unsigned int missed = 0;
+  for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += gridDim.x * blockDim.x) {
+    const int64_t gp = (int64_t)wb.polish_list[k];
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
+    const int64_t local = gp - c.pixBase;
+    const int x = (int)(local % c.width), y = (int)(local / c.width);
+    V3<double> dir;
+    camera_ray(p, c, x, y, dir);
+    const V3<double> start{c.start[0], c.start[1], c.start[2]};
+    const double kd = p.constantDEThreshold ? 0.0 : c.resolution_d * c.persp_d / p.quality_d;
+    double t = (double)wb.scan[gp];
+    int li = wb.iters[gp];
+    if (level_set_hit<FORMULA>(fd, start, dir, kd, p.quality_d, t, li)) {
+      const V3<double> point = start + dir * t;
+      const double thr = p.constantDEThreshold ? p.quality_d : t * c.resolution_d * c.persp_d / p.quality_d;
+      wb.scan[gp] = (T)t;
+      wb.dist[gp] = (T)thr;
+      wb.thr[gp] = (T)thr;
+      wb.iters[gp] = li;
+      wb.point[0 * wb.npix + gp] = (T)point.x;
+      wb.point[1 * wb.npix + gp] = (T)point.y;
+      wb.point[2 * wb.npix + gp] = (T)point.z;
+    } else {
+      wb.flags[gp] |= 8;
+      missed++;
+    }
+  }
+  if (missed) atomicAdd(wb.ctl + 7, missed);
+}
+
+// FastAmbientOcclusion2 (src/shaders.cpp:585-605) on the stage's orbit: q^2 - 1 DE samples
+// along the normal at i^2 x the threshold, weighted 2^-i.
+template <typename T, int FORMULA, bool FAST>
+__device__ __forceinline__ T wave_fast_ao(const ParamsT<T> &p, const V3<T> point, const V3<T> normal,
+                                          const T dist_thresh, const T detail, Counters &cnt) {
+  T aoTemp = T(0);
+  const int q2 = p.aoQuality * p.aoQuality;
+  for (int i = 1; i < q2; i++) {
+    const T scan = T(i * i) * dist_thresh;
+    const V3<T> pt = point + normal * scan;
+    int L;
+    bool mi;
+    const T dist = wave_distance<T, FORMULA, FAST>(p.f, pt, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+    // 1.0 / pow(2.0, i) is exact for integral i
+    aoTemp += T(1) / T(ldexp(1.0, i)) * (scan - p.fastAoTune * dist) / dist_thresh;
+  }
+  T ao = T(1) - T(0.2) * aoTemp;
+  if (ao < T(0)) ao = T(0);
+  return ao;
 }
 
 // Shading-stage quantities of a hit pixel shared by the secondary and compose stages.
@@ -643,12 +712,13 @@ struct HitInfo {
 };
 
 template <typename T>
-__device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const WaveBufs<T> &wb, const unsigned int pix) {
+__device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const FrameCam<T> &c, const WaveBufs<T> &wb,
+                                               const int64_t gp) {
   HitInfo<T> h;
-  h.point = {wb.point[0 * wb.npix + pix], wb.point[1 * wb.npix + pix], wb.point[2 * wb.npix + pix]};
-  h.thr = wb.thr[pix];
-  h.scan = wb.scan[pix];
-  h.delta = p.constantDEThreshold ? h.scan * p.resolution * p.persp : h.thr * p.quality;
+  h.point = {wb.point[0 * wb.npix + gp], wb.point[1 * wb.npix + gp], wb.point[2 * wb.npix + gp]};
+  h.thr = wb.thr[gp];
+  h.scan = wb.scan[gp];
+  h.delta = p.constantDEThreshold ? h.scan * c.resolution * c.persp : h.thr * p.quality;
   return h;
 }
 
@@ -658,22 +728,25 @@ __device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const WaveBu
 // direction-major so a warp's initial 32 rays share a direction.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb) {
+__global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
+                                                        const FrameCam<T> *__restrict__ cams, const int ncams) {
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
   const unsigned int nShadow = p.shadow ? nh : 0u;
   const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
   const unsigned int njobs = nShadow + nAO;
   Counters cnt{0, 0, 0, 0};
-  const V3<T> light{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
   bool active = false, exhausted = false;
   int kind = 0;
-  unsigned int pix = 0, j = 0;
+  unsigned int j = 0;
+  int64_t gp = 0;
   V3<T> point{T(0), T(0), T(0)}, dir{T(0), T(0), T(0)};
   T r = T(0), end = T(0), dist = T(0), sh = T(1), thr = T(0), detail = T(0), maxSoft = T(0), stepMul = T(0);
   int guard = 0;
   for (;;) {
+    // a warp claims new jobs once refill_min of its lanes are idle, or when none is busy
     const bool need = !active && !exhausted;
-    if (__any_sync(0xffffffffu, need)) {
+    const unsigned int needMask = __ballot_sync(0xffffffffu, need);
+    if (needMask && (__popc(needMask) >= (unsigned int)wb.refill_min || !__any_sync(0xffffffffu, active))) {
       if (io.budget_ns && (threadIdx.x & 31) == 0 && deadline_passed(io)) atomicExch(io.error_flag, 1);
       const bool stop = *(volatile int *)io.error_flag != 0;
       const unsigned int job = claim_jobs(wb.ctl + 2, need);
@@ -683,23 +756,24 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
         } else {
           kind = job < nShadow ? 0 : 1;
           if (kind == 0) {
-            pix = wb.hit_list[job];
+            gp = (int64_t)wb.hit_list[job];
           } else {
             const unsigned int q = job - nShadow;
             j = q / nh;
-            pix = wb.hit_list[q % nh];
+            gp = (int64_t)wb.hit_list[q % nh];
           }
-          const HitInfo<T> h = hit_info(p, wb, pix);
+          const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
+          const HitInfo<T> h = hit_info(p, c, wb, gp);
           point = h.point;
           // MainShadow and AmbientOcclusion compare with the threshold stored in a float
           thr = (T)(float)h.thr;
           sh = T(1);
           maxSoft = T(0);
           guard = 0;
-          T factor = p.penetrating ? h.delta / p.resolution : p.viewDistanceMax;
+          const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
           const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
           if (kind == 0) {
-            dir = light;
+            dir = {c.lightVect[0], c.lightVect[1], c.lightVect[2]};
             end = factor;
             r = shadowStart;
             dist = h.thr;
@@ -707,17 +781,17 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
             stepMul = p.DE_factor;
           } else {
             dir = {__ldg(&p.aoVec[3 * j + 0]), __ldg(&p.aoVec[3 * j + 1]), __ldg(&p.aoVec[3 * j + 2])};
-            end = h.delta / p.resolution;
+            end = h.delta / c.resolution;
             r = h.delta;
-            dist = wb.dist[pix];
+            dist = wb.dist[gp];
             // detailSize after MainShadow: the float threshold if its loop ran at least once
             detail = (p.shadow && shadowStart < factor) ? thr : h.thr;
             stepMul = T(2);
           }
           active = true;
           if (!(r < end)) {  // loop body never runs
-            if (kind == 0) wb.shadow[pix] = p.softShadow ? T(1) : sh;
-            else wb.ao[(int64_t)j * wb.npix + pix] = sh;
+            if (kind == 0) wb.shadow[gp] = p.softShadow ? T(1) : sh;
+            else wb.ao[(int64_t)j * wb.npix + gp] = sh;
             active = false;
           }
         }
@@ -761,8 +835,8 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
         if (!(r < end) || ++guard >= kMaxSecondarySteps) done = true;
       }
       if (done) {
-        if (kind == 0) wb.shadow[pix] = p.softShadow ? (T(1) - maxSoft) : sh;
-        else wb.ao[(int64_t)j * wb.npix + pix] = sh;
+        if (kind == 0) wb.shadow[gp] = p.softShadow ? (T(1) - maxSoft) : sh;
+        else wb.ao[(int64_t)j * wb.npix + gp] = sh;
         active = false;
       }
     }
@@ -862,25 +936,29 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
 }
 
 // ---------------------------------------------------------------------------
-// Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589).
+// Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589),
+// over every pixel of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb) {
+__global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
+                                                      const FrameCam<T> *__restrict__ cams, const int ncams) {
   Counters cnt{0, 0, 0, 0};
-  const int64_t first = (int64_t)p.row_begin * p.width;
-  const int64_t n = (int64_t)(p.row_end - p.row_begin) * p.width;
-  const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pix = first + k;
-    const int x = (int)(pix % p.width), y = (int)(pix / p.width);
-    const uint8_t flags = wb.flags[pix];
+  const int64_t total = wb.npix;
+  for (int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gp < total;
+       gp += (int64_t)gridDim.x * blockDim.x) {
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
+    const int64_t pix = gp - c.pixBase;   // pixel within the frame's own layers
+    const int x = (int)(pix % c.width), y = (int)(pix / c.width);
+    if (y < c.row_begin || y >= c.row_end) continue;
+    const uint8_t flags = wb.flags[gp];
     const bool hit = (flags & 1) != 0;
     V3<T> viewT;
-    camera_dir(p, x, y, viewT);
+    camera_dir(p, c, x, y, viewT);
+    const V3<T> lv{c.lightVect[0], c.lightVect[1], c.lightVect[2]};
     T base[3];
     V3<T> objColour{T(0), T(0), T(0)};
     if (hit) {
-      const HitInfo<T> h = hit_info(p, wb, (unsigned int)pix);
+      const HitInfo<T> h = hit_info(p, c, wb, gp);
       // CalculateNormals (src/shaders.cpp:675-711): 4 DEs at N x 5, minN 0
       T dn = h.delta * p.smoothness;
       if (p.f.interiorMode) dn = h.thr * p.quality * T(0.2) * p.smoothness;
@@ -900,7 +978,7 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       T shade = dot3(nrm, lv);
       if (shade < T(0)) shade = T(0);
       const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
-      const T shadow = p.shadow ? wb.shadow[pix] : T(1);
+      const T shadow = p.shadow ? wb.shadow[gp] : T(1);
       V3<T> half = normalize3(lv - viewT);
       T shade2 = dot3(nrm, half);
       if (shade2 < T(0)) shade2 = T(0);
@@ -913,14 +991,14 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       if (p.ao) {
         if (p.fastAO) {
           // detailSize after MainShadow: the float threshold if its loop ran
-          const T factor = p.penetrating ? h.delta / p.resolution : p.viewDistanceMax;
+          const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
           const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
           const T detail = (p.shadow && shadowStart < factor) ? (T)(float)h.thr : h.thr;
-          const T a = fast_ao<T, FORMULA>(p, h.point, nrm, h.thr, detail, cnt);
+          const T a = wave_fast_ao<T, FORMULA, FAST>(p, h.point, nrm, h.thr, detail, cnt);
           ambient = {a, a, a};
         } else {
           T acc = T(0);
-          for (int jj = 0; jj < p.aoCount; jj++) acc += wb.ao[(int64_t)jj * wb.npix + pix] * p.aoWeight[0];
+          for (int jj = 0; jj < p.aoCount; jj++) acc += wb.ao[(int64_t)jj * wb.npix + gp] * p.aoWeight[0];
           const T div = T(p.aoCount) * T(256);
           ambient = {acc / div, acc / div, acc / div};
         }
@@ -941,22 +1019,22 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
     T out0, out1, out2, alpha, opacity;
     if (flags & 4) {
       // a long ray of the overflow pass: its volumetric pass was folded into an affine map
-      const T A = wb.vol[0 * wb.npix + pix];
-      out0 = A * base[0] + wb.vol[1 * wb.npix + pix];
-      out1 = A * base[1] + wb.vol[2 * wb.npix + pix];
-      out2 = A * base[2] + wb.vol[3 * wb.npix + pix];
-      alpha = wb.vol[4 * wb.npix + pix];
-      opacity = wb.vol[5 * wb.npix + pix];
+      const T A = wb.vol[0 * wb.npix + gp];
+      out0 = A * base[0] + wb.vol[1 * wb.npix + gp];
+      out1 = A * base[1] + wb.vol[2 * wb.npix + gp];
+      out2 = A * base[2] + wb.vol[3 * wb.npix + gp];
+      alpha = wb.vol[4 * wb.npix + gp];
+      opacity = wb.vol[5 * wb.npix + gp];
     } else {
       // VolumetricShader over the ray's pooled step records, far to near, on this base colour
       T res[4] = {base[0], base[1], base[2], hit ? T(1) + T(0) : T(0)};
       float totalOpacity = 0.0f;
       bool set = false;
       if (p.needVolumetric) {
-        const int count = wb.count[pix];
-        const PoolRecords<T> pr{wb.pool_step, wb.pool_dist, wb.pool_thr, wb.pool_prev, wb.last_chunk[pix],
+        const int count = wb.count[gp];
+        const PoolRecords<T> pr{wb.pool_step, wb.pool_dist, wb.pool_thr, wb.pool_prev, wb.last_chunk[gp],
                                 hit ? count : count - 1};
-        volumetric_pool<T>(p, pr, wb.count[pix], wb.scan[pix], res, totalOpacity, set);
+        volumetric_pool<T>(p, pr, count, wb.scan[gp], res, totalOpacity, set);
       }
       out0 = res[0];
       out1 = res[1];
@@ -964,23 +1042,23 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       alpha = res[3];
       opacity = (T)totalOpacity;
     }
-    const double depth = hit ? (double)wb.scan[pix] : 1e20;
-    if (io.opacity) io.opacity[pix] = to_u16_x86((double)opacity * 65535.0);
-    if (io.alpha) io.alpha[pix] = to_u16_x86((double)alpha * 65535.0);
-    if (io.image_float) {
-      io.image_float[3 * pix + 0] = (float)out0;
-      io.image_float[3 * pix + 1] = (float)out1;
-      io.image_float[3 * pix + 2] = (float)out2;
+    const double depth = hit ? (double)wb.scan[gp] : 1e20;
+    if (c.opacity) c.opacity[pix] = to_u16_x86((double)opacity * 65535.0);
+    if (c.alpha) c.alpha[pix] = to_u16_x86((double)alpha * 65535.0);
+    if (c.image_float) {
+      c.image_float[3 * pix + 0] = (float)out0;
+      c.image_float[3 * pix + 1] = (float)out1;
+      c.image_float[3 * pix + 2] = (float)out2;
     }
-    if (io.colour) {
-      io.colour[3 * pix + 0] = to_u8_x86((double)(objColour.x * T(255)));
-      io.colour[3 * pix + 1] = to_u8_x86((double)(objColour.y * T(255)));
-      io.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
+    if (c.colour) {
+      c.colour[3 * pix + 0] = to_u8_x86((double)(objColour.x * T(255)));
+      c.colour[3 * pix + 1] = to_u8_x86((double)(objColour.y * T(255)));
+      c.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
     }
-    if (io.zbuffer) io.zbuffer[pix] = (float)depth;
-    if (io.hit) io.hit[pix] = hit ? 1 : 0;
-    if (io.iters) io.iters[pix] = wb.iters[pix];
-    if (io.depth) io.depth[pix] = depth;
+    if (c.zbuffer) c.zbuffer[pix] = (float)depth;
+    if (c.hit) c.hit[pix] = hit ? 1 : 0;
+    if (c.iters) c.iters[pix] = wb.iters[gp];
+    if (c.depth) c.depth[pix] = depth;
   }
   for (int off = 16; off > 0; off >>= 1) {
     cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);

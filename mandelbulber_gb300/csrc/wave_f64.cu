@@ -1,4 +1,5 @@
 // Instantiation of the wavefront kernels for T = double.
+#include "grad_core.cuh"
 #include "wave_core.cuh"
 #include "wave_launch.h"
 
@@ -7,15 +8,20 @@ namespace mbgb {
 template <int F, bool FAST>
 static cudaError_t run_stages_f64(const WaveLaunch<double> &L, cudaStream_t s) {
   if (L.ev[0]) cudaEventRecord(L.ev[0], s);
-  dev::primary_kernel<double, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb);
+  dev::primary_kernel<double, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb, L.cams, L.ncams);
   if (L.overflow)
-    dev::primary_kernel<double, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb);
+    dev::primary_kernel<double, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb, L.cams, L.ncams);
   if (L.ev[0]) cudaEventRecord(L.ev[1], s);
+  if (L.wb.exact_hit)
+    dev::level_set_kernel<double, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
   if (L.ev[0]) cudaEventRecord(L.ev[2], s);
-  dev::secondary_kernel<double, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb);
+  dev::secondary_kernel<double, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
   if (L.ev[0]) cudaEventRecord(L.ev[3], s);
-  dev::compose_kernel<double, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb);
+  dev::compose_kernel<double, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
   if (L.ev[0]) cudaEventRecord(L.ev[4], s);
+  if (L.gcams)
+    dev::grad_kernel<double, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 4), L.wb, L.cams, L.gcams,
+                                                                   L.ncams);
   return cudaGetLastError();
 }
 

@@ -1,4 +1,5 @@
-// Launch description of the wavefront stages (wave_core.cuh) for one frame.
+// Launch description of the wavefront stages (wave_core.cuh) for a batch of frames
+// sharing one scene's fractal, shading and fog parameters.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -7,8 +8,55 @@
 
 namespace mbgb {
 
+// SoA buffers of the wavefront stages over all pixels of a batch (device memory).
 template <typename T>
-struct WaveBufs;
+struct WaveBufs {
+  uint8_t *flags;        // [npix] bit0: hit, bit1: hemisphere cut / not marched
+  T *scan;               // [npix] depth of the primary ray
+  T *dist;               // [npix] last distance (lastDist)
+  T *thr;                // [npix] distThresh at the hit
+  T *step;               // [npix] FP32 policy: bisection step left for the FP64 polish
+  T *detail;             // [npix] detailSize of the march's last step (src/Render3D.cpp:110)
+  int32_t *bis_left;     // [npix] FP32 policy: bisection iterations left
+  T *point;              // [3][npix] hit point in the march precision
+  int32_t *iters;        // [npix] itersOut at the end of the march
+  int32_t *count;        // [npix] buffCount
+  T *vol;                // [6][npix] overflow pass only: A, B.r, B.g, B.b, alpha, opacity
+  T *shadow;             // [npix]
+  T *ao;                 // [aoCount][npix] per-direction shadowTemp
+  uint32_t *hit_list;    // [npix] hits (secondary rays)
+  uint32_t *polish_list; // [npix] hits the FP64 polish re-evaluates
+  uint32_t *ctl;         // [0] primary jobs, [1] hits, [2] secondary jobs, [3] overflow count,
+                         // [4] overflow-pass jobs, [5] pool chunks, [6] polish count,
+                         // [7] exact_hit refinements that missed the level set (zeroed per group)
+  uint32_t *overflow_list;
+  // Step records of the primary rays: chunks of kChunk records linked backwards
+  // (prev), allocated by bump counter; the pixel keeps its last chunk.
+  T *pool_step, *pool_dist, *pool_thr;   // [chunk * kChunk + r]
+  int32_t *pool_prev;                    // [chunk]
+  int32_t *last_chunk;                   // [npix], -1 = no records
+  uint32_t pool_cap;                     // chunks
+  int polish_all;                        // 1: every hit takes the FP64 polish
+  int refill_min;                        // idle lanes of a warp before it claims new rays
+  int exact_hit;                         // 1: hits are refined in FP64 to the level set DE = thr
+  int64_t npix;
+};
+
+constexpr int kChunk = 32;       // step records per pool chunk
+constexpr int kPoolChunksPerPixel = 4;   // pool budget; rays beyond it take the overflow pass
+
+// Parameters of the differentiable render: [0] fractal parameter (power of formula 2,
+// scale of formula 8), [1..3] camera position, [4] main light alpha, [5] main light beta.
+constexpr int kGradParams = 6;
+
+// Per-frame inputs and outputs of the gradient stage (device table, one per frame).
+template <typename T>
+struct GradCam {
+  const float *dL_dimage;   // [height][width][3] or null: the loss's derivative by the float image
+  float *jacobian;          // [height][width][3][kGradParams] or null: dI/dtheta per pixel and channel
+  double *dtheta;           // [kGradParams]: sum over pixels of dL/dI dI/dtheta (zeroed by the host)
+  T dLight[2][3];           // d lightVect / d alpha, d lightVect / d beta (camera rotation applied)
+};
 
 template <typename T>
 struct WaveLaunch {
@@ -17,10 +65,14 @@ struct WaveLaunch {
   FrameIO io;        // main primary pass
   FrameIO ov;        // overflow primary pass (rays longer than io.step_cap records)
   WaveBufs<T> wb;
+  const FrameCam<T> *cams;  // device table of the batch's frames (camera, size, rows, outputs)
+  const GradCam<T> *gcams;  // differentiable render: per-frame gradient table (null = no gradient stage)
+  int ncams;
   int grid, block, ov_grid, polish_grid, grid2, compose_grid;
   bool overflow;     // the step buffer is in use, so the overflow pass is enqueued
   bool fast;         // the scene qualifies for a lean FP32 orbit (Mandelbox, power-8 Mandelbulb)
   cudaEvent_t ev[5]; // optional: recorded before stage 0 and after each of the 4 stages
+  int grad_grid;     // blocks of the gradient stage
 };
 
 // Stage k adds its counters at io.counters + 4 * k.
