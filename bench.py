@@ -221,6 +221,43 @@ def batch_section(ctx, torch, dev, stream, flush, args, world, dist) -> dict:
             "precision": "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement"}
 
 
+def grad_section(ctx, torch, dev, args) -> dict:
+    """The gradient workload: 32 Mandelbulb frames at 256x256 with seeded theta (power,
+    camera position, light angles), loss = L2 against targets rendered at theta + delta.
+    One step = the differentiable render of all 32 frames (forward stages with level-set
+    hits plus the gradient stage) and the read-back of dL/dtheta; FP32 policy."""
+    import mandelbulber_gb300 as mb
+    from mandelbulber_gb300 import diff as D
+    scenes, th, tg = D.grad_batch(32, 256)
+    RT = D.Renderer(ctx, scenes, mb.PREC_FP32_FIX)
+    RT.set_theta(tg)
+    T = RT.forward().clone()
+    R = D.Renderer(ctx, scenes, mb.PREC_FP32_FIX)
+    R.set_theta(th)
+    I = R.forward()
+    dL = (2 * (I - T)).contiguous()
+    for _ in range(3):
+        R.backward(dL)
+    steps = max(1, args.grad_steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    e0.record()
+    for _ in range(steps):
+        g = R.backward(dL)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    st = ctx.stats()
+    return {"workload": "grad_mandelbulb_32x256", "frames": len(scenes), "params_per_frame": D.GRAD_PARAMS,
+            "value": len(scenes) * steps / wall, "unit": "grads/s (theta-vectors/s)", "steps": steps,
+            "ms_per_batch": 1e3 * wall / steps, "device_ms_per_batch": e0.elapsed_time(e1) / steps,
+            "grad_pixels": int(st.grad_pixels), "grad_skipped": int(st.grad_skipped),
+            "launches_per_batch": int(st.launches), "finite": bool(np.isfinite(g).all()),
+            "precision": "fp32 forward with fp64 level-set hits; fp64 derivative arithmetic",
+            "check": "tests/test_gpu_grad.py: adjoint vs central differences (h = 1e-4, FP64) within 1e-3"}
+
+
 def run_once(args) -> int:
     """One frame of the workload at a small size (plus `--warmup` frames): the ncu profiling case."""
     import mandelbulber_gb300 as mb
@@ -250,6 +287,8 @@ def main() -> int:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-frame flight batch")
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--no-grad", action="store_true", help="skip the gradient workload")
+    ap.add_argument("--grad-steps", type=int, default=5)
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
     ap.add_argument("--precision", default="fp32_fix", choices=["fp32_fix", "fp64"])
@@ -404,6 +443,7 @@ def main() -> int:
     launches_per_frame = int(ctx.stats().launches)
 
     batch = None if args.no_batch else batch_section(ctx, torch, dev, stream, flush, args, world, dist)
+    grads = None if args.no_grad else grad_section(ctx, torch, dev, args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -440,6 +480,7 @@ def main() -> int:
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps * launches_per_frame,
         "batch": batch,
+        "grads": grads,
         "clocks": clocks,
         "cpu_baseline": cpu,
         "wall_s_timed_region": wall32,

@@ -178,7 +178,7 @@ typedef struct mbgb_image {
   uint16_t *opacity;           /* PutPixelOpacity */
   uint8_t *colour;             /* sRGB8, 3 bytes per pixel (PutPixelColour) */
   /* debug / parity layers (no reference counterpart) */
-  uint8_t *hit;                /* 1 where the primary ray found the surface */
+  uint8_t *hit;                /* 1 where the primary ray found the surface (3: exact_hit missed the level set) */
   int32_t *iters;              /* orbit iterations of the last DE at the hit (itersOut) */
   double *depth;               /* primary-ray depth (scan) as double, 1e20 for background */
 } mbgb_image;

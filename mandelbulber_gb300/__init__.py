@@ -161,14 +161,15 @@ ENGINE_WAVEFRONT, ENGINE_PER_PIXEL = 0, 1
 def make_opts(precision: int = PREC_FP32_FIX, jitter: bool = False, jitter_seed: int = 0, rows=None,
               ctas_per_sm: int = 0, threads_per_cta: int = 0, deadline_ms: int = 0, stream: int = 0,
               engine: int = ENGINE_WAVEFRONT, profile_stages: bool = False, polish_all: bool = False,
-              tile=None, refill_min: int = 0, autotune: bool = False, use_graph: bool = False) -> mbgb_opts:
+              tile=None, refill_min: int = 0, autotune: bool = False, use_graph: bool = False,
+              exact_hit: bool = False) -> mbgb_opts:
     r0, r1 = rows if rows else (0, 0)
     tw, th = tile if tile else (0, 0)
     return mbgb_opts(precision=precision, jitter=int(jitter), jitter_seed=jitter_seed, row_begin=r0, row_end=r1,
                      ctas_per_sm=ctas_per_sm, threads_per_cta=threads_per_cta, deadline_ms=deadline_ms,
                      stream=stream if stream else None, engine=engine, profile_stages=int(profile_stages),
                      polish_all=int(polish_all), tile_w=tw, tile_h=th, refill_min=refill_min,
-                     autotune=int(autotune), use_graph=int(use_graph))
+                     autotune=int(autotune), use_graph=int(use_graph), exact_hit=int(exact_hit))
 
 
 _LAYERS = ["image_float", "zbuffer", "alpha", "opacity", "colour", "hit", "iters", "depth"]
@@ -239,6 +240,22 @@ class Context:
         imgs = (mbgb_image * n)(*[_device_image(sc, ly) for sc, ly in zip(scenes, layers)])
         o = make_opts(**opts)
         _check(self._lib.mbgb_render_batch(self._h, arr, n, imgs, ctypes.byref(o)))
+
+    def render_grad(self, scenes, layers: list, dL_dimage=None, jacobian=None, **opts) -> np.ndarray:
+        """mbgb_render_grad: renders the frames into the device layers (hits on the level set)
+        and returns dL/dtheta [n, GRAD_PARAMS] for the device loss gradients ``dL_dimage``
+        (list of pointers to [h, w, 3] float32, or None); ``jacobian`` optionally receives
+        dI/dtheta per pixel (list of pointers to [h, w, 3, GRAD_PARAMS] float32)."""
+        n = len(scenes)
+        arr = (mbgb_scene * n)(*scenes)
+        imgs = (mbgb_image * n)(*[_device_image(sc, ly) for sc, ly in zip(scenes, layers)])
+        gin = (ctypes.c_void_p * n)(*dL_dimage) if dL_dimage is not None else None
+        jac = (ctypes.c_void_p * n)(*jacobian) if jacobian is not None else None
+        out = np.zeros((n, _abi.GRAD_PARAMS), np.float64)
+        o = make_opts(**opts)
+        _check(self._lib.mbgb_render_grad(self._h, arr, n, imgs, gin, jac,
+                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(o)))
+        return out
 
     def autotune(self, scene: mbgb_scene, **opts) -> mbgb_tuning:
         """mbgb_autotune: times the launch configurations on this frame and caches the best."""

@@ -90,6 +90,7 @@ MBGB_STATUS = {
 }
 
 PREC_FP64, PREC_FP32_FIX, PREC_AUTO = 0, 1, 2
+GRAD_PARAMS = 6   # MBGB_GRAD_PARAMS
 
 # every entry point include/mbgb.h declares: name -> (restype, argtypes)
 _P = ctypes.POINTER
@@ -117,6 +118,9 @@ FUNCTIONS = {
     "mbgb_render_batch_host": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int32, _P(mbgb_image),
                                               _P(mbgb_opts)]),
     "mbgb_autotune": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_opts), _P(mbgb_tuning)]),
+    "mbgb_render_grad": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int32, _P(mbgb_image),
+                                        _P(ctypes.c_void_p), _P(ctypes.c_void_p), _P(ctypes.c_double),
+                                        _P(mbgb_opts)]),
     "mbgb_distance_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p]),

@@ -1056,7 +1056,8 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       c.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
     }
     if (c.zbuffer) c.zbuffer[pix] = (float)depth;
-    if (c.hit) c.hit[pix] = hit ? 1 : 0;
+    // debug layer: 0 miss, 1 hit, 3 hit whose exact_hit refinement missed the level set
+    if (c.hit) c.hit[pix] = hit ? ((flags & 8) ? 3 : 1) : 0;
     if (c.iters) c.iters[pix] = wb.iters[gp];
     if (c.depth) c.depth[pix] = depth;
   }

@@ -20,7 +20,7 @@ static cudaError_t run_stages_f64(const WaveLaunch<double> &L, cudaStream_t s) {
   dev::compose_kernel<double, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
   if (L.ev[0]) cudaEventRecord(L.ev[4], s);
   if (L.gcams)
-    dev::grad_kernel<double, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 4), L.wb, L.cams, L.gcams,
+    dev::grad_kernel<double, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 4), L.wb, L.cams, L.gcams,
                                                                    L.ncams);
   return cudaGetLastError();
 }

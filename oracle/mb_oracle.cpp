@@ -19,6 +19,9 @@
 //   background                        BackgroundShader           src/shaders.cpp:114-183
 //   volumetric                        VolumetricShader           src/shaders.cpp:185-478
 //   render_rows                       MainThread pixel body      src/Render3D.cpp:213-344, 389-589
+//   level_set                         (not in the reference) Newton refinement of a hit onto
+//                                     DE(P) = thr, the surface the differentiable render's
+//                                     gradients are checked on; off unless oracle_render_exact
 // Build: oracle/Makefile, -O2 -ffp-contract=off (parity) and -O3 -ffast-math (timing).
 #include <atomic>
 #include <cmath>
@@ -285,6 +288,40 @@ Ray ray_marching(const mbgb_scene &s, Calc &c, Vec start, Vec dir, std::vector<S
   return out;
 }
 
+// After RayMarching's bisection (hit inside the window (0.99 thr, thr)): Newton steps on
+// F(t) = DE(start + t dir) - thr(t) with a central-difference derivative until
+// |F| <= 1e-13 thr. Returns false (ray unchanged) on a flat estimate, a grazing ray
+// (F' >= 0), a step longer than thr or no convergence in 16 steps.
+bool level_set(const mbgb_scene &s, Calc &c, Vec start, Vec dir, Ray &ray) {
+  const double k = s.constantDEThreshold ? 0.0 : s.resolution * s.persp / s.quality;
+  const double dlen = len(dir);
+  double t = ray.depth;
+  for (int it = 0; it < 16; it++) {
+    const double thr = s.constantDEThreshold ? s.quality : t * k;
+    c.detail = thr;
+    bool mi = false;
+    const double d0 = calculate_distance(c, add(start, mul(dir, t)), &mi);
+    if (mi || c.itersOut < c.minN) return false;
+    const double F = d0 - thr;
+    if (fabs(F) <= 1e-13 * thr) {
+      ray.depth = t;
+      ray.point = add(start, mul(dir, t));
+      ray.thr = thr;
+      ray.lastDist = d0;
+      return true;
+    }
+    const double eps = 1e-6 * thr / dlen;
+    const double dp = calculate_distance(c, add(start, mul(dir, t + eps)), &mi);
+    const double dm = calculate_distance(c, add(start, mul(dir, t - eps)), &mi);
+    const double Ft = (dp - dm) / (2.0 * eps) - k;
+    if (!(Ft < 0.0)) return false;
+    const double dt = -F / Ft;
+    if (fabs(dt) > thr / dlen) return false;
+    t += dt;
+  }
+  return false;
+}
+
 Vec calculate_normals(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr) {
   double d = delta * s.smoothness;
   if (s.interiorMode) d = thr * s.quality * 0.2 * s.smoothness;
@@ -502,6 +539,7 @@ struct Frame {
   int rzero;
   Vec start, light;
   std::vector<Vec> aoDirs;
+  bool exact = false;   // level-set refinement of hits (oracle_render_exact)
 };
 
 void setup_frame(const mbgb_scene &s, Frame &f) {
@@ -567,6 +605,8 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
   Calc c{&s, (int)s.N, s.minN, false, 0.0, 0, &cnt};
   Ray ray{};
   if (!cut) ray = ray_marching(s, c, f.start, view, buf, jitter, cnt);
+  bool levelMissed = false;
+  if (f.exact && ray.found) levelMissed = !level_set(s, c, f.start, view, ray);
   const int iters = c.itersOut;
   double out[4] = {0, 0, 0, 0};
   Vec objColour{0, 0, 0};
@@ -629,7 +669,7 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     img->colour[3 * pix + 2] = to_u8(objColour.z * 255);
   }
   if (img->zbuffer) img->zbuffer[pix] = (float)depthZ;
-  if (img->hit) img->hit[pix] = ray.found ? 1 : 0;
+  if (img->hit) img->hit[pix] = ray.found ? (levelMissed ? 3 : 1) : 0;
   if (img->iters) img->iters[pix] = iters;
   if (img->depth) img->depth[pix] = depthZ;
 }
@@ -664,11 +704,12 @@ void oracle_colour_value(const mbgb_scene *s, const double *pts, long n, double 
 // counter (the reference's one-worker-per-core row claiming). jitter != 0 uses
 // the C library's shared rand() stream, as the reference does.
 // counters (may be NULL): [0] orbit iterations, [1] DE calls, [2] march steps.
-int oracle_render(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
-                  unsigned long long *counters) {
+static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
+                       unsigned long long *counters, bool exact) {
   if (!s || !img || row0 < 0 || row1 > img->height || row0 > row1) return 1;
   Frame f;
   setup_frame(*s, f);
+  f.exact = exact;
   if (threads < 1) threads = 1;
   std::atomic<int> next(row0);
   std::vector<Cnt> cnts(threads);
@@ -696,6 +737,17 @@ int oracle_render(const mbgb_scene *s, int row0, int row1, int jitter, int threa
     }
   }
   return 0;
+}
+
+int oracle_render(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
+                  unsigned long long *counters) {
+  return render_rows(s, row0, row1, jitter, threads, img, counters, false);
+}
+
+// The same render with every hit moved onto the level set DE(P) = thr after the
+// bisection (hit layer 3 where that fails): the forward pass the gradient checks use.
+int oracle_render_exact(const mbgb_scene *s, int row0, int row1, int threads, const mbgb_image *img) {
+  return render_rows(s, row0, row1, 0, threads, img, nullptr, true);
 }
 
 }  // extern "C"

@@ -27,6 +27,8 @@ def load(fast: bool = False) -> ctypes.CDLL:
     lib.oracle_colour_value.restype = None
     lib.oracle_render.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
     lib.oracle_render.restype = ctypes.c_int
+    lib.oracle_render_exact.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+    lib.oracle_render_exact.restype = ctypes.c_int
     _cache[key] = lib
     return lib
 
@@ -66,3 +68,16 @@ def render(lib, scene, rows=None, jitter=False, threads=None):
     if rc != 0:
         raise RuntimeError("oracle_render rejected its arguments")
     return img, cnt
+
+
+def render_exact(lib, scene, threads=None):
+    """The oracle render with every hit moved onto the level set DE = thr (hit layer 3
+    where that fails): the forward pass of the gradient checks. Returns a CImage."""
+    import mandelbulber_gb300 as mb
+    img = mb.CImage.empty(scene.image_width, scene.image_height)
+    c = img.as_c()
+    rc = lib.oracle_render_exact(ctypes.addressof(scene), 0, scene.image_height, threads or os.cpu_count() or 1,
+                                 ctypes.addressof(c))
+    if rc != 0:
+        raise RuntimeError("oracle_render_exact rejected its arguments")
+    return img
