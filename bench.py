@@ -37,6 +37,10 @@ WORKLOAD = "mandelbox_1080p"
 # 3 fold add/sub + 5 for x^2+y^2+z^2 + 5 sphere fold (1 div) + 6 for z*scale+c + 2 for DE*|s|+1,
 # plus sqrt and divide of each DE evaluation
 FLOPS_PER_ITER = {8: 21, 2: 27}
+# dram__bytes_read.sum + dram__bytes_write.sum of secondary_kernel per 1080p launch: an ncu
+# --set full capture at 480x270 read 2.35 MB and wrote 0 B; the traffic is the per-hit
+# inputs and AO slots, so it scales with the pixel count (x16)
+DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 37.6e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
 
 
@@ -62,7 +66,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -238,6 +242,13 @@ def grad_section(ctx, torch, dev, args) -> dict:
     dL = (2 * (I - T)).contiguous()
     for _ in range(3):
         R.backward(dL)
+    # per-stage device times of one differentiable render of the batch
+    g = ctx.render_grad(R.scenes, R.layers(), dL_dimage=[dL[i].data_ptr() for i in range(len(scenes))],
+                        precision=mb.PREC_FP32_FIX, profile_stages=True)
+    st = ctx.stats()
+    names = ["primary_kernel", "polish_kernel", "secondary_kernel", "compose_kernel", "level_set_kernel",
+             "grad_kernel"]
+    stage_ms = {names[k]: float(st.stage_ms[k]) for k in range(6)}
     steps = max(1, args.grad_steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(dev)
@@ -253,7 +264,7 @@ def grad_section(ctx, torch, dev, args) -> dict:
             "value": len(scenes) * steps / wall, "unit": "grads/s (theta-vectors/s)", "steps": steps,
             "ms_per_batch": 1e3 * wall / steps, "device_ms_per_batch": e0.elapsed_time(e1) / steps,
             "grad_pixels": int(st.grad_pixels), "grad_skipped": int(st.grad_skipped),
-            "launches_per_batch": int(st.launches), "finite": bool(np.isfinite(g).all()),
+            "launches_per_batch": int(st.launches), "finite": bool(np.isfinite(g).all()), "stage_ms": stage_ms,
             "precision": "fp32 forward with fp64 level-set hits; fp64 derivative arithmetic",
             "check": "tests/test_gpu_grad.py: adjoint vs central differences (h = 1e-4, FP64) within 1e-3"}
 
@@ -278,7 +289,7 @@ def run_once(args) -> int:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
@@ -417,7 +428,7 @@ def main() -> int:
         for _ in range(frames):
             ctx.render_device(scene, ptrs, precision=precision, profile_stages=True)
             st = ctx.stats()
-            acc += np.array(list(st.stage_ms))
+            acc += np.array(list(st.stage_ms)[:4])
         acc /= frames
         work = [st.stage_orbit[k] * FLOPS_PER_ITER[f] + st.stage_de[k] * FLOPS_PER_DE[f] for k in range(4)]
         stages = {stage_names[k]: {"ms": float(acc[k]), "flops": int(work[k]), "orbit_iterations": int(st.stage_orbit[k]),
@@ -430,13 +441,7 @@ def main() -> int:
     flops32 = st32.orbit_iterations * FLOPS_PER_ITER[f] + st32.de_calls * FLOPS_PER_DE[f]
     ach32 = work32 / sec32 / 1e12
     ach64 = work64 / sec64 / 1e12
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    traffic = None
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get(args.workload, {}).get("dram_bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+    traffic = DRAM_BYTES_PER_LAUNCH.get(args.workload) if top32 == "secondary_kernel" else None
 
     # launches of one timed frame (the library counts the kernels it enqueues)
     ctx.render_device(scene, ptrs, precision=mb.PREC_FP32_FIX)

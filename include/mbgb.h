@@ -247,10 +247,11 @@ typedef struct mbgb_stats {
   uint64_t auto_fp64;          /* 1 if any frame of the last call was rendered in FP64 (MBGB_PREC_AUTO picks per frame) */
   double kernel_ms;            /* device time of the last render */
   /* per stage: [0] primary rays (wavefront) or the per-pixel kernel, [1] FP64 hit polish,
-   * [2] shadow and AO rays, [3] composition */
-  uint64_t stage_orbit[4];     /* orbit iterations */
-  uint64_t stage_de[4];        /* DE evaluations */
-  double stage_ms[4];          /* device time between the stage's CUDA events (profile_stages = 1) */
+   * [2] shadow and AO rays, [3] composition, [4] level-set refinement (exact_hit),
+   * [5] gradient stage (mbgb_render_grad) */
+  uint64_t stage_orbit[6];     /* orbit iterations (stages 0-3, 5) */
+  uint64_t stage_de[6];        /* DE evaluations (stages 0-3, 5) */
+  double stage_ms[6];          /* device time between the stage's CUDA events (profile_stages = 1) */
   uint64_t frames;             /* frames of the last call */
   uint64_t launches;           /* kernels the last call launched (graph replays included) */
   uint64_t graph_replayed;     /* 1 if the last call replayed a captured CUDA graph */

@@ -363,7 +363,7 @@ struct mbgb_context {
   DeviceBuf gradacc;             // differentiable render: per-frame dL/dtheta sums
   uint64_t gen = 0;              // bumped whenever a scratch buffer is reallocated
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::vector<cudaEvent_t> gev;  // stage events, 5 per group (profile_stages)
+  std::vector<cudaEvent_t> gev;  // stage events, kStageEvents per group (profile_stages)
   std::map<TuneKey, mbgb_tuning> tunings;
   CallPlan plan;                 // the last call's launches
   // use_graph: the captured launches of the last such call and what they depend on
@@ -541,6 +541,13 @@ static void clear_unused(FractalT<T> &f) {
   }
 }
 
+// The formula's main parameter (power / Mandelbox scale) travels per frame (FrameCam::fparam).
+template <typename T>
+static void clear_fparam(FractalT<T> &f) {
+  if (f.formula == MBGB_FORMULA_TGLAD) f.mbScale = T(0);
+  else f.power = T(0);
+}
+
 // Whether frames a and b can share one launch sequence in precision T: every
 // parameter the kernels read, other than the per-frame camera, is equal in the
 // form the kernels receive it.
@@ -553,13 +560,19 @@ static bool same_shared(const mbgb_scene &a, const mbgb_scene &b, const mbgb_opt
   strip_camera(pb);
   clear_unused(pa.f);
   clear_unused(pb.f);
+  clear_fparam(pa.f);
+  clear_fparam(pb.f);
   if (memcmp(&pa, &pb, sizeof(pa)) != 0) return false;
   FractalT<double> fa, fb;
   fill_fractal<double>(a, fa);
   fill_fractal<double>(b, fb);
   clear_unused(fa);
   clear_unused(fb);
-  return memcmp(&fa, &fb, sizeof(fa)) == 0;
+  clear_fparam(fa);
+  clear_fparam(fb);
+  // the lean orbits are chosen per launch sequence
+  const bool fastA = fast_mandelbox(a) || fast_mandelbulb(a), fastB = fast_mandelbox(b) || fast_mandelbulb(b);
+  return fastA == fastB && memcmp(&fa, &fb, sizeof(fa)) == 0;
 }
 
 // Camera, size, rows and output layers of one frame (MainThread's per-frame set-up,
@@ -590,6 +603,8 @@ static void fill_cam(const mbgb_scene &s, const mbgb_image &img, const mbgb_opts
   cam.resolution_d = p.resolution_d;
   cam.persp_d = p.persp_d;
   for (int k = 0; k < 3; k++) cam.lightVect[k] = p.lightVect[k];
+  cam.fparam = (T)(s.formula == MBGB_FORMULA_TGLAD ? s.mboxScale : s.power);
+  cam.fparam_d = s.formula == MBGB_FORMULA_TGLAD ? s.mboxScale : s.power;
   cam.image_float = img.image_float;
   cam.zbuffer = img.zbuffer;
   cam.alpha = img.alpha;
@@ -806,7 +821,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.ov.step_dist = c->ovstep[prec][1].ptr;
   L.ov.step_thr = c->ovstep[prec][2].ptr;
   L.overflow = needVol;
-  for (int k = 0; k < 5; k++) L.ev[k] = ev ? ev[k] : nullptr;
+  for (int k = 0; k < kStageEvents; k++) L.ev[k] = ev ? ev[k] : nullptr;
   L.fast = fast_mandelbox(scene) || fast_mandelbulb(scene);
   fill_fractal<double>(scene, L.fd);
   fill_params<T>(scene, L.p, o, (const T *)(prec == 0 ? c->ao64.ptr : c->ao32.ptr), c->ao_count);
@@ -1175,7 +1190,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     c->cams_hold_graph = false;
   }
   if (plan.profile) {
-    const size_t want = 5 * plan.groups.size();
+    const size_t want = kStageEvents * plan.groups.size();
     while (c->gev.size() < want) {
       cudaEvent_t ev;
       MBGB_CUDA(cudaEventCreate(&ev));
@@ -1196,7 +1211,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     for (size_t gi = 0; gi < plan.groups.size(); gi++) {
       const Group &g = plan.groups[gi];
       char *gctl = (char *)c->fctl.ptr + 64 * gi;
-      cudaEvent_t *ev = plan.profile ? &c->gev[5 * gi] : nullptr;
+      cudaEvent_t *ev = plan.profile ? &c->gev[kStageEvents * gi] : nullptr;
       mbgb_status r;
       if (!g.wave) {
         r = enqueue_per_pixel(c, scenes[g.frames[0]], imgs[g.frames[0]], g, o, s, io, gctl, &plan.launches);
@@ -1254,7 +1269,7 @@ static mbgb_status read_back(mbgb_context *c, const CallPlan &plan, int replayed
   MBGB_CUDA(cudaStreamSynchronize(c->stream));
   MBGB_CUDA(cudaEventSynchronize(c->ev1));
   char *ctl = (char *)c->control.ptr;
-  unsigned long long cnt[20];
+  unsigned long long cnt[4 * kStages];
   int flag = 0;
   MBGB_CUDA(cudaMemcpy(cnt, ctl + 64, sizeof(cnt), cudaMemcpyDeviceToHost));
   MBGB_CUDA(cudaMemcpy(&flag, ctl + 16, sizeof(flag), cudaMemcpyDeviceToHost));
@@ -1263,7 +1278,7 @@ static mbgb_status read_back(mbgb_context *c, const CallPlan &plan, int replayed
     MBGB_CUDA(cudaMemcpy(gctl.data(), c->fctl.ptr, 64 * plan.groups.size(), cudaMemcpyDeviceToHost));
   mbgb_stats &S = c->stats;
   S = mbgb_stats{};
-  for (int k = 0; k < 4; k++) {
+  for (int k = 0; k < kStages; k++) {
     S.stage_orbit[k] = cnt[4 * k + 0];
     S.stage_de[k] = cnt[4 * k + 1];
   }
@@ -1277,11 +1292,15 @@ static mbgb_status read_back(mbgb_context *c, const CallPlan &plan, int replayed
     } else {
       S.long_rays += q[1];
     }
-    if (plan.profile) {
-      for (int k = 0; k < 4; k++) {
+    if (plan.profile && g.wave) {
+      // events in launch order -> stats slots (primary 0, polish 1, level set 4, shadow/AO 2,
+      // compose 3, gradient 5)
+      const int slot[kStages] = {0, 1, 4, 2, 3, 5};
+      for (int k = 0; k < kStages; k++) {
         float sm = 0;
-        if (g.wave && cudaEventElapsedTime(&sm, c->gev[5 * gi + k], c->gev[5 * gi + k + 1]) == cudaSuccess)
-          S.stage_ms[k] += sm;
+        if (cudaEventElapsedTime(&sm, c->gev[kStageEvents * gi + k], c->gev[kStageEvents * gi + k + 1]) ==
+            cudaSuccess)
+          S.stage_ms[slot[k]] += sm;
       }
     }
   }
@@ -1292,10 +1311,10 @@ static mbgb_status read_back(mbgb_context *c, const CallPlan &plan, int replayed
     cnt[3] += cnt[4 * k + 3];
   }
   // the gradient stage's counters: orbit iterations, DE calls, pixels differentiated, skipped
-  cnt[0] += cnt[16];
-  cnt[1] += cnt[17];
-  S.grad_pixels = plan.grad ? cnt[18] : 0;
-  S.grad_skipped = plan.grad ? cnt[19] : 0;
+  cnt[0] += cnt[20];
+  cnt[1] += cnt[21];
+  S.grad_pixels = plan.grad ? cnt[22] : 0;
+  S.grad_skipped = plan.grad ? cnt[23] : 0;
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev0, c->ev1);
   S.orbit_iterations = cnt[0];

@@ -178,26 +178,27 @@ __device__ __forceinline__ Dual<T, K> dlength(const DV3<T, K> &v) {
 }
 
 // Compute<normal> of formula 2 (src/fractal.cpp:211-225) or formula 8 without rotations
-// and offset (src/fractal.cpp:467-528), with dual numbers: tangents 0..2 = the point,
-// tangent 3 = power (formula 2) or scale (formula 8). Returns the distance estimate
-// (0 with zero derivatives when the orbit does not escape) and the iteration count.
-template <typename T, int FORMULA>
-__device__ __forceinline__ Dual<T, 4> de_dual(const FractalT<T> &f, const V3<T> P, const int N, int &Lout) {
-  using D = Dual<T, 4>;
-  DV3<T, 4> z{dseed<T, 4>(P.x, 0), dseed<T, 4>(P.y, 1), dseed<T, 4>(P.z, 2)};
-  DV3<T, 4> c;
+// and offset (src/fractal.cpp:467-528) on dual numbers: `z` is the point with its K
+// tangents, `fp` the formula's parameter (power of formula 2, Mandelbox scale of formula
+// 8) with its tangents. Returns the distance estimate (0 with zero derivatives when the
+// orbit does not escape) and the iteration count.
+template <typename T, int FORMULA, int K>
+__device__ __forceinline__ Dual<T, K> de_dual_seeded(const FractalT<T> &f, DV3<T, K> z, const Dual<T, K> fp,
+                                                     const int N, int &Lout) {
+  using D = Dual<T, K>;
+  DV3<T, K> c;
   if (f.juliaMode) {
-    c = {dconst<T, 4>(f.julia[0]), dconst<T, 4>(f.julia[1]), dconst<T, 4>(f.julia[2])};
+    c = {dconst<T, K>(f.julia[0]), dconst<T, K>(f.julia[1]), dconst<T, K>(f.julia[2])};
   } else {
     c = {z.x * f.constantFactor, z.y * f.constantFactor, z.z * f.constantFactor};
   }
-  D dist = dconst<T, 4>(T(0));
+  D dist = dconst<T, K>(T(0));
   D r = dlength(z);
   int L;
   if (FORMULA == 2) {
-    const D p = dseed<T, 4>(f.power, 3);
+    const D p = fp;
     const D pm1 = p + T(-1);
-    D r_dz = dconst<T, 4>(T(1));
+    D r_dz = dconst<T, K>(T(1));
     for (L = 0; L < N; L++) {
       const D th0 = dasin(z.z / r);
       const D ph0 = datan2(z.y, z.x);
@@ -217,11 +218,11 @@ __device__ __forceinline__ Dual<T, 4> de_dual(const FractalT<T> &f, const V3<T> 
       }
     }
   } else {
-    const D scale = dseed<T, 4>(f.mbScale, 3);
+    const D scale = fp;
     const T fR2 = f.mbFixedR * f.mbFixedR;
     const T mR2 = f.mbMinR * f.mbMinR;
     const T factor1 = fR2 / mR2;
-    D tgladDE = dconst<T, 4>(T(1));
+    D tgladDE = dconst<T, K>(T(1));
     for (L = 0; L < N; L++) {
       if (z.x.v > f.mbFoldLimit) z.x = -z.x + f.mbFoldValue;
       else if (z.x.v < -f.mbFoldLimit) z.x = -z.x + (-f.mbFoldValue);
@@ -235,7 +236,7 @@ __device__ __forceinline__ Dual<T, 4> de_dual(const FractalT<T> &f, const V3<T> 
         z = {z.x * factor1, z.y * factor1, z.z * factor1};
         tgladDE = tgladDE * factor1;
       } else if (r2.v < fR2) {
-        const D f2 = dconst<T, 4>(fR2) / r2;
+        const D f2 = dconst<T, K>(fR2) / r2;
         z = {z.x * f2, z.y * f2, z.z * f2};
         tgladDE = tgladDE * f2;
       }
@@ -249,8 +250,28 @@ __device__ __forceinline__ Dual<T, 4> de_dual(const FractalT<T> &f, const V3<T> 
     }
   }
   Lout = L;
-  if (L == N || dist.v < T(0)) dist = dconst<T, 4>(T(0));
+  if (L == N || dist.v < T(0)) dist = dconst<T, K>(T(0));
   return dist;
+}
+
+// Distance estimate with derivatives by the point (tangents 0..2) and by the formula's
+// parameter (tangent 3).
+template <typename T, int FORMULA>
+__device__ __forceinline__ Dual<T, 4> de_dual(const FractalT<T> &f, const V3<T> P, const int N, int &Lout,
+                                              const T fparam) {
+  const DV3<T, 4> z{dseed<T, 4>(P.x, 0), dseed<T, 4>(P.y, 1), dseed<T, 4>(P.z, 2)};
+  return de_dual_seeded<T, FORMULA, 4>(f, z, dseed<T, 4>(fparam, 3), N, Lout);
+}
+
+// Distance estimate and its derivative along direction d (one tangent).
+template <typename T, int FORMULA>
+__device__ __forceinline__ Dual<T, 1> de_along(const FractalT<T> &f, const V3<T> P, const V3<T> d, const int N,
+                                               int &Lout, const T fparam) {
+  DV3<T, 1> z{dconst<T, 1>(P.x), dconst<T, 1>(P.y), dconst<T, 1>(P.z)};
+  z.x.d[0] = d.x;
+  z.y.d[0] = d.y;
+  z.z.d[0] = d.z;
+  return de_dual_seeded<T, FORMULA, 1>(f, z, dconst<T, 1>(fparam), N, Lout);
 }
 
 // Newton refinement of a hit to the level set DE(o + t d) = thr(t) in FP64 (after the
@@ -259,11 +280,12 @@ __device__ __forceinline__ Dual<T, 4> de_dual(const FractalT<T> &f, const V3<T> 
 // flat estimate (orbit not escaping, minN clamp), or no convergence in 16 steps.
 template <int FORMULA>
 __device__ __forceinline__ bool level_set_hit(const FractalT<double> &f, const V3<double> o, const V3<double> d,
-                                              const double k, const double thrConst, double &t, int &iters) {
+                                              const double k, const double thrConst, double &t, int &iters,
+                                              const double fparam) {
   double tt = t;
   for (int it = 0; it < 16; it++) {
     int L;
-    const Dual<double, 4> de = de_dual<double, FORMULA>(f, o + d * tt, f.N, L);
+    const Dual<double, 1> de = de_along<double, FORMULA>(f, o + d * tt, d, f.N, L, fparam);
     const double thr = k > 0.0 ? tt * k : thrConst;
     if (L == f.N || L < f.minN) return false;
     const double F = de.v - thr;
@@ -272,7 +294,7 @@ __device__ __forceinline__ bool level_set_hit(const FractalT<double> &f, const V
       iters = L;
       return true;
     }
-    const double Ft = de.d[0] * d.x + de.d[1] * d.y + de.d[2] * d.z - k;
+    const double Ft = de.d[0] - k;
     if (!(Ft < 0.0)) return false;
     double dt = -F / Ft;
     // the bisection window already brackets the root to a small fraction of thr

@@ -46,7 +46,7 @@ __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const Fracta
   const double k = p.constantDEThreshold ? 0.0 : c.resolution_d * c.persp_d / p.quality_d;
   int L;
   // implicit differentiation of the hit distance
-  const Dual<double, 4> de = de_dual<double, FORMULA>(fd, P, fd.N, L);
+  const Dual<double, 4> de = de_dual<double, FORMULA>(fd, P, fd.N, L, c.fparam_d);
   const double Ft = de.d[0] * d.x + de.d[1] * d.y + de.d[2] * d.z - k;
   if (!(Ft < 0.0)) return false;
   double dt[kGradParams];
@@ -69,10 +69,10 @@ __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const Fracta
   const V3<T> PT{wb.point[0 * wb.npix + gp], wb.point[1 * wb.npix + gp], wb.point[2 * wb.npix + gp]};
   const V3<T> PxT{PT.x + dnT, PT.y, PT.z}, PyT{PT.x, PT.y + dnT, PT.z}, PzT{PT.x, PT.y, PT.z + dnT};
   const int N5 = fd.N5;
-  const Dual<double, 4> s1 = de_dual<double, FORMULA>(fd, P, N5, L);
-  const Dual<double, 4> sx = de_dual<double, FORMULA>(fd, V3<double>{(double)PxT.x, P.y, P.z}, N5, L);
-  const Dual<double, 4> sy = de_dual<double, FORMULA>(fd, V3<double>{P.x, (double)PyT.y, P.z}, N5, L);
-  const Dual<double, 4> sz = de_dual<double, FORMULA>(fd, V3<double>{P.x, P.y, (double)PzT.z}, N5, L);
+  const Dual<double, 4> s1 = de_dual<double, FORMULA>(fd, P, N5, L, c.fparam_d);
+  const Dual<double, 4> sx = de_dual<double, FORMULA>(fd, V3<double>{(double)PxT.x, P.y, P.z}, N5, L, c.fparam_d);
+  const Dual<double, 4> sy = de_dual<double, FORMULA>(fd, V3<double>{P.x, (double)PyT.y, P.z}, N5, L, c.fparam_d);
+  const Dual<double, 4> sz = de_dual<double, FORMULA>(fd, V3<double>{P.x, P.y, (double)PzT.z}, N5, L, c.fparam_d);
   const V3<double> gv{sx.v - s1.v, sy.v - s1.v, sz.v - s1.v};
   const double glen = sqrt(gv.x * gv.x + gv.y * gv.y + gv.z * gv.z);
   V3<double> n{1.0, 0.0, 0.0};
@@ -124,7 +124,7 @@ __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const Fracta
     }
   }
   const double shadow = p.shadow ? (double)wb.shadow[gp] : 1.0;
-  const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, PT, cnt);
+  const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, PT, cnt, c.fparam);
   const double col[3] = {(double)colour.x, (double)colour.y, (double)colour.z};
   bool finite = true;
   for (int ch = 0; ch < 3; ch++) {

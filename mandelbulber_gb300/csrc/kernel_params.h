@@ -86,8 +86,9 @@ struct ParamsT {
   int fogCol1[3], fogCol2[3], fogCol3[3];
 };
 
-// Per-frame camera, resolution and output layers of a batch (device memory, one per
-// frame). Everything else of the scene is shared by the batch's frames (ParamsT).
+// Per-frame camera, resolution, fractal parameter and output layers of a batch (device
+// memory, one per frame). Everything else of the scene is shared by the batch's frames
+// (ParamsT).
 // Built like MainThread's per-frame set-up (src/Render3D.cpp:213-344).
 template <typename T>
 struct FrameCam {
@@ -102,6 +103,8 @@ struct FrameCam {
   T resolution, persp;
   double resolution_d, persp_d;
   T lightVect[3];
+  T fparam;                     // the formula's main parameter: power (2) or Mandelbox scale (8)
+  double fparam_d;
   float *image_float;
   float *zbuffer;
   uint16_t *alpha;

@@ -55,6 +55,23 @@ __device__ __forceinline__ void m_sincos(float x, float *s, float *c) { sincosf(
 template <typename T>
 __device__ __forceinline__ T length3(const V3<T> a) { return m_sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 
+// |z| of an orbit point. FP32: the squares overflow once a component passes 1.8e19, which
+// an orbit of power ~10 reaches at its escape step (r^p with r up to the bailout 100);
+// the length is then taken from the components scaled by the largest one. FP64 keeps the
+// reference's plain expression (its range is not reached before the bailout).
+template <typename T>
+__device__ __forceinline__ T orbit_length(const V3<T> a) {
+  const T r2 = a.x * a.x + a.y * a.y + a.z * a.z;
+  if (sizeof(T) == 4 && !(r2 <= T(3.0e38))) {
+    const T m = m_fabs(a.x) > m_fabs(a.y) ? (m_fabs(a.x) > m_fabs(a.z) ? m_fabs(a.x) : m_fabs(a.z))
+                                           : (m_fabs(a.y) > m_fabs(a.z) ? m_fabs(a.y) : m_fabs(a.z));
+    if (!(m <= T(3.0e38))) return m;   // a component already overflowed (inf) or is NaN
+    const T x = a.x / m, y = a.y / m, z = a.z / m;
+    return m * m_sqrt(x * x + y * y + z * z);
+  }
+  return m_sqrt(r2);
+}
+
 // CVector3::Normalize (src/algebra.hpp:105-112): multiply by 1/length.
 template <typename T>
 __device__ __forceinline__ V3<T> normalize3(const V3<T> a) {
@@ -98,28 +115,37 @@ struct Counters {
   unsigned long long missed;  // Missed_DE_counter
 };
 
+// The formula's main parameter: power (formula 2) or Mandelbox scale (formula 8).
+template <typename T>
+__host__ __device__ __forceinline__ T fparam_of(const FractalT<T> &f) {
+  return f.formula == 8 ? f.mbScale : f.power;
+}
+
 // ---------------------------------------------------------------------------
 // Compute<Mode> (src/fractal.cpp:40-1241) for the formulas this build carries.
 // MODE 0 = normal (returns the distance estimate), MODE 1 = colouring.
 // ---------------------------------------------------------------------------
+// `fparam` is the formula's main parameter: the power of formula 2, the Mandelbox scale
+// of formula 8 (a frame of a batch may carry its own; see fparam_of).
 template <typename T, int FORMULA, int MODE>
-__device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N, int &Lout, Counters &cnt) {
+__device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N, int &Lout, Counters &cnt,
+                                     const T fparam) {
   T distance = T(0);
   T r_dz = T(1);
-  const T p = f.power;
+  const T p = fparam;
   const T fR2 = f.mbFixedR * f.mbFixedR;
   const T mR2 = f.mbMinR * f.mbMinR;
   const T tglad_factor1 = fR2 / mR2;
   T tgladDE = T(1);
   T tgladColor = T(1);
-  const T scale = f.mbScale;
+  const T scale = fparam;
   V3<T> constant;
   if (f.juliaMode) {
     constant = {f.julia[0], f.julia[1], f.julia[2]};
   } else {
     constant = z * f.constantFactor;
   }
-  T r = length3(z);
+  T r = orbit_length(z);
   T minv = (sizeof(T) == 8) ? T(1e200) : T(__int_as_float(0x7f800000));
   int L;
   for (L = 0; L < N; L++) {
@@ -130,7 +156,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       else if (z.y < -f.foldingLimit) { z.y = -f.foldingValue - z.y; tgladColor *= T(0.9); }
       if (z.z > f.foldingLimit) { z.z = f.foldingValue - z.z; tgladColor *= T(0.9); }
       else if (z.z < -f.foldingLimit) { z.z = -f.foldingValue - z.z; tgladColor *= T(0.9); }
-      r = length3(z);
+      r = orbit_length(z);
     }
     if (f.sphericalFoldingMode) {  // src/fractal.cpp:158-179
       const T fR2_2 = f.sphFixed * f.sphFixed;
@@ -143,7 +169,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
         const T tf2 = fR2_2 / r2_2;
         z = z * tf2; tgladDE *= tf2; tgladColor += T(10);
       }
-      r = length3(z);
+      r = orbit_length(z);
     }
     if (FORMULA == 2) {
       // trig_optim Mandelbulb (src/fractal.cpp:211-225)
@@ -158,7 +184,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       r_dz = rp * r_dz * p + T(1);
       rp *= r;
       z = V3<T>{cth * cph, cth * sph, sth} * rp + constant;
-      r = length3(z);
+      r = orbit_length(z);
     } else if (FORMULA == 8) {
       // tglad Mandelbox (src/fractal.cpp:409-529)
       if (f.mbRotEnabled) {
@@ -191,7 +217,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
         if (z.z > f.mbFoldLimit) { z.z = f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
         else if (z.z < -f.mbFoldLimit) { z.z = -f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
       }
-      r = length3(z);
+      r = orbit_length(z);
       const T r2 = r * r;
       z = z + V3<T>{f.mbOffset[0], f.mbOffset[1], f.mbOffset[2]};
       if (r2 < mR2) {
@@ -204,7 +230,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       z = rotate(f.mbMainRot, f.mbMainRotZero, z);
       z = z * scale + constant;
       tgladDE = tgladDE * m_fabs(scale) + T(1);
-      r = length3(z);
+      r = orbit_length(z);
     }
     // iteration terminate conditions (src/fractal.cpp:1133-1190)
     if (FORMULA == 8) {
@@ -213,7 +239,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       if (MODE == 0) {
         if (r > T(100)) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
       } else {
-        distance = length3(z);
+        distance = orbit_length(z);
         if (distance < minv) minv = distance;
         if (distance > T(1e15)) { distance = minv; break; }
       }
@@ -226,7 +252,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
     if (L == N) distance = T(0);
     return distance;
   } else {
-    if (FORMULA == 8) return tgladColor * T(100) + length3(z) * f.mbColR;
+    if (FORMULA == 8) return tgladColor * T(100) + orbit_length(z) * f.mbColR;
     return distance * T(5000);
   }
 }
@@ -236,7 +262,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
 template <typename T, int FORMULA>
 __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> point, const T detailSize, const int N,
                                            const int minN, const bool normalMode, int &L, bool &maxIter,
-                                           Counters &cnt) {
+                                           Counters &cnt, const T fparam) {
   T limitBoxDist = T(0);
   if (f.limits) {
     // MAX(a, b) = a > b ? a : b (gtk MAX macro)
@@ -254,7 +280,7 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
     }
   }
   int Li;
-  T distance = compute<T, FORMULA, 0>(f, point, N, Li, cnt);
+  T distance = compute<T, FORMULA, 0>(f, point, N, Li, cnt, fparam);
   maxIter = (Li == N);
   L = Li;
   if (distance < T(0)) distance = T(0);
@@ -339,7 +365,7 @@ __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, co
     }
     if (p.perspType == 1 || p.perspType == 2) distThresh *= T(kPI);
     bool mi;
-    dist = calc_distance<T, FORMULA>(p.f, point, distThresh, p.f.N, p.f.minN, false, iters, mi, cnt);
+    dist = calc_distance<T, FORMULA>(p.f, point, distThresh, p.f.N, p.f.minN, false, iters, mi, cnt, fparam_of(p.f));
     if (useSB) {
       sb.dist[sb.at(i)] = dist;
       sb.thr[sb.at(i)] = distThresh;
@@ -405,7 +431,7 @@ __device__ __forceinline__ void refine(const ParamsT<TP> &p, const FractalT<doub
       distThresh = scan * p.resolution_d * p.persp_d / p.quality_d + distThreshInit;
     }
     bool mi;
-    dist = calc_distance<double, FORMULA>(fd, point, rs.detail, fd.N, fd.minN, false, iters, mi, cnt);
+    dist = calc_distance<double, FORMULA>(fd, point, rs.detail, fd.N, fd.minN, false, iters, mi, cnt, fparam_of(fd));
     step *= 0.5;
   }
   rs.scan = scan;
@@ -430,13 +456,13 @@ __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> po
   int L;
   bool mi;
   const int N5 = p.f.N5;
-  const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt);
+  const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam_of(p.f));
   const T s2 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
-                                         true, L, mi, cnt);
+                                         true, L, mi, cnt, fparam_of(p.f));
   const T s3 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
-                                         true, L, mi, cnt);
+                                         true, L, mi, cnt, fparam_of(p.f));
   const T s4 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
-                                         true, L, mi, cnt);
+                                         true, L, mi, cnt, fparam_of(p.f));
   V3<T> n{s2 - s1, s3 - s1, s4 - s1};
   if (n.x == T(0) && n.y == T(0) && n.z == T(0)) {
     n.x = T(1);
@@ -472,7 +498,7 @@ __device__ __forceinline__ T main_shadow(const ParamsT<T> &p, const V3<T> point,
     detail = thr;
     int L;
     bool mi;
-    dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+    dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt, fparam_of(p.f));
     if (bSoft) {
       T angle = (dist - thr) / i;
       if (angle < T(0)) angle = T(0);
@@ -510,7 +536,7 @@ __device__ __forceinline__ T fast_ao(const ParamsT<T> &p, const V3<T> point, con
     const V3<T> pt = point + normal * scan;
     int L;
     bool mi;
-    const T dist = calc_distance<T, FORMULA>(p.f, pt, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+    const T dist = calc_distance<T, FORMULA>(p.f, pt, detail, p.f.N, p.f.minN, false, L, mi, cnt, fparam_of(p.f));
     // 1.0 / pow(2.0, i) is exact for integral i
     aoTemp += T(1) / T(ldexp(1.0, i)) * (scan - p.fastAoTune * dist) / dist_thresh;
   }
@@ -538,7 +564,7 @@ __device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, 
       const V3<T> point2 = point + dir * r;
       int L;
       bool mi;
-      dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+      dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt, fparam_of(p.f));
       if (dist < thr || mi || shadowTemp < T(0)) {
         shadowTemp -= (end_dist - r) / end_dist;
         if (shadowTemp < T(0)) shadowTemp = T(0);
@@ -579,9 +605,10 @@ __device__ __forceinline__ void index_to_colour(const ParamsT<T> &p, int index, 
 
 // SurfaceColour for the fractal object (src/shaders.cpp:850-879)
 template <typename T, int FORMULA>
-__device__ __forceinline__ V3<T> surface_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt) {
+__device__ __forceinline__ V3<T> surface_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt,
+                                                const T fparam) {
   int L;
-  const T c = compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt);
+  const T c = compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt, fparam);
   int nrCol = to_i32_x86((double)m_floor(c));
   // abs(nrCol) % (248 * 256) with the magnitude taken as unsigned, as the reference
   // binary computes it: an out-of-range conversion (INT_MIN) gives 2^31 % 63488 = 2048.
@@ -773,7 +800,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
     shade2 = m_pow(shade2, T(30)) * T(1);
     if (shade2 > T(15)) shade2 = T(15);
     const T spec = shade2 * p.specular;
-    const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt);
+    const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt, fparam_of(p.f));
     objColour = colour;
     V3<T> ambient{T(0), T(0), T(0)};
     if (p.ao) {
@@ -892,7 +919,7 @@ __global__ void distance_kernel(const FractalT<T> f, const double *points, const
     const V3<T> pt{(T)points[3 * i], (T)points[3 * i + 1], (T)points[3 * i + 2]};
     int L = 0;
     bool mi = false;
-    const T d = calc_distance<T, FORMULA>(f, pt, (T)detail[i], f.N, f.minN, false, L, mi, cnt);
+    const T d = calc_distance<T, FORMULA>(f, pt, (T)detail[i], f.N, f.minN, false, L, mi, cnt, fparam_of(f));
     dist[i] = (double)d;
     iters[i] = L;
     max_iter[i] = mi ? 1 : 0;

@@ -34,12 +34,12 @@ namespace dev {
 // bailout r > 1024 becomes r^2 > 1024^2 and the sphere fold tests r^2 directly, so the
 // loop has no square root; the fold is clamp(x)*2 - x, identical to fv - x / -fv - x.
 __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const float px, const float py,
-                                                const float pz, const int N, int &Lout, Counters &cnt) {
+                                                const float pz, const int N, int &Lout, Counters &cnt,
+                                                const float s) {
   const float fl = f.mbFoldLimit;
   const float mR2 = f.mbMinR * f.mbMinR;
   const float fR2 = f.mbFixedR * f.mbFixedR;
   const float k1 = fR2 / mR2;
-  const float s = f.mbScale;
   const float as = fabsf(s);
   const float cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
   float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
@@ -138,11 +138,11 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
 template <typename T, int FORMULA, bool FAST>
 __device__ __forceinline__ T wave_distance(const FractalT<T> &f, const V3<T> p, const T detail, const int N,
                                            const int minN, const bool normalMode, int &L, bool &maxIter,
-                                           Counters &cnt) {
+                                           Counters &cnt, const T fparam) {
   if constexpr (FAST && sizeof(T) == 4) {
     int Li;
     T distance;
-    if constexpr (FORMULA == 8) distance = mandelbox_fast(f, p.x, p.y, p.z, N, Li, cnt);
+    if constexpr (FORMULA == 8) distance = mandelbox_fast(f, p.x, p.y, p.z, N, Li, cnt, fparam);
     else distance = mandelbulb8_fast<0>(f, p.x, p.y, p.z, N, Li, cnt);
     maxIter = (Li == N);
     L = Li;
@@ -150,13 +150,14 @@ __device__ __forceinline__ T wave_distance(const FractalT<T> &f, const V3<T> p, 
     if (Li < minN && distance < detail) distance = detail;
     return distance;
   } else {
-    return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt);
+    return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);
   }
 }
 
 // SurfaceColour (src/shaders.cpp:850-879) with the fast power-8 colouring orbit when it applies.
 template <typename T, int FORMULA, bool FAST>
-__device__ __forceinline__ V3<T> wave_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt) {
+__device__ __forceinline__ V3<T> wave_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt,
+                                             const T fparam) {
   if constexpr (FAST && FORMULA == 2 && sizeof(T) == 4) {
     int L;
     const float c = mandelbulb8_fast<1>(p.f, point.x, point.y, point.z, p.f.N10, L, cnt);
@@ -170,7 +171,7 @@ __device__ __forceinline__ V3<T> wave_colour(const ParamsT<T> &p, const V3<T> po
     }
     return V3<T>{T(rgb[0]) / T(256), T(rgb[1]) / T(256), T(rgb[2]) / T(256)};
   } else {
-    return surface_colour<T, FORMULA>(p, point, cnt);
+    return surface_colour<T, FORMULA>(p, point, cnt, fparam);
   }
 }
 
@@ -378,7 +379,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
   int phase = 0, i = 0, buffCount = 0, iters = 0, bis = 0;
   int chunk = -1;   // current pool chunk of the ray's step records (main pass)
   V3<T> dir{T(0), T(0), T(0)}, start{T(0), T(0), T(0)};
-  T res = T(0), persp = T(0), thrScale = T(0);
+  T res = T(0), persp = T(0), thrScale = T(0), fpar = T(0);
   T scan = T(0), step = T(0), thr = T(0), dist = T(0), detail = T(0);  // detail: detailSize of the march
   int guardSteps = 0;
   for (;;) {
@@ -413,6 +414,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
             start = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
             res = c.resolution;
             persp = c.persp;
+            fpar = c.fparam;
             thrScale = res * persp / p.quality;
             chunk = -1;
             scan = p.viewDistanceMin;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
         detail = thr;
       }
       bool mi;
-      dist = wave_distance<T, FORMULA, FAST>(p.f, point, detail, p.f.N, p.f.minN, false, iters, mi, cnt);
+      dist = wave_distance<T, FORMULA, FAST>(p.f, point, detail, p.f.N, p.f.minN, false, iters, mi, cnt, fpar);
       cnt.steps++;
       bool done = false;
       if (phase == 0) {
@@ -617,7 +619,7 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
     V3<double> point = start + dir * scan;
     int iters = 0;
     bool mi;
-    double dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt);
+    double dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt, c.fparam_d);
     cnt.steps++;
     for (int it = 0; it < left; it++) {
       if (dist < thr && dist > thr * search_limit) break;
@@ -625,7 +627,7 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
       else if (dist < thr * search_limit) scan -= step;
       point = start + dir * scan;
       thr = thr_of(scan);
-      dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt);
+      dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt, c.fparam_d);
       cnt.steps++;
       step *= 0.5;
     }
@@ -665,7 +667,7 @@ __global__ void __launch_bounds__(128) level_set_kernel(const ParamsT<T> p, cons
     const double kd = p.constantDEThreshold ? 0.0 : c.resolution_d * c.persp_d / p.quality_d;
     double t = (double)wb.scan[gp];
     int li = wb.iters[gp];
-    if (level_set_hit<FORMULA>(fd, start, dir, kd, p.quality_d, t, li)) {
+    if (level_set_hit<FORMULA>(fd, start, dir, kd, p.quality_d, t, li, c.fparam_d)) {
       const V3<double> point = start + dir * t;
       const double thr = p.constantDEThreshold ? p.quality_d : t * c.resolution_d * c.persp_d / p.quality_d;
       wb.scan[gp] = (T)t;
@@ -687,7 +689,7 @@ __global__ void __launch_bounds__(128) level_set_kernel(const ParamsT<T> p, cons
 // along the normal at i^2 x the threshold, weighted 2^-i.
 template <typename T, int FORMULA, bool FAST>
 __device__ __forceinline__ T wave_fast_ao(const ParamsT<T> &p, const V3<T> point, const V3<T> normal,
-                                          const T dist_thresh, const T detail, Counters &cnt) {
+                                          const T dist_thresh, const T detail, Counters &cnt, const T fparam) {
   T aoTemp = T(0);
   const int q2 = p.aoQuality * p.aoQuality;
   for (int i = 1; i < q2; i++) {
@@ -695,7 +697,7 @@ __device__ __forceinline__ T wave_fast_ao(const ParamsT<T> &p, const V3<T> point
     const V3<T> pt = point + normal * scan;
     int L;
     bool mi;
-    const T dist = wave_distance<T, FORMULA, FAST>(p.f, pt, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+    const T dist = wave_distance<T, FORMULA, FAST>(p.f, pt, detail, p.f.N, p.f.minN, false, L, mi, cnt, fparam);
     // 1.0 / pow(2.0, i) is exact for integral i
     aoTemp += T(1) / T(ldexp(1.0, i)) * (scan - p.fastAoTune * dist) / dist_thresh;
   }
@@ -741,6 +743,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
   int64_t gp = 0;
   V3<T> point{T(0), T(0), T(0)}, dir{T(0), T(0), T(0)};
   T r = T(0), end = T(0), dist = T(0), sh = T(1), thr = T(0), detail = T(0), maxSoft = T(0), stepMul = T(0);
+  T fpar = T(0);
   int guard = 0;
   for (;;) {
     // a warp claims new jobs once refill_min of its lanes are idle, or when none is busy
@@ -765,6 +768,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
           const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
           const HitInfo<T> h = hit_info(p, c, wb, gp);
           point = h.point;
+          fpar = c.fparam;
           // MainShadow and AmbientOcclusion compare with the threshold stored in a float
           thr = (T)(float)h.thr;
           sh = T(1);
@@ -805,7 +809,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, cons
       const V3<T> point2 = point + dir * r;
       int L;
       bool mi;
-      dist = wave_distance<T, FORMULA, FAST>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt);
+      dist = wave_distance<T, FORMULA, FAST>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt, fpar);
       bool done = false;
       if (kind == 0) {
         if (p.softShadow) {
@@ -965,13 +969,13 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       int L;
       bool mi;
       const int N5 = p.f.N5;
-      const T s1 = wave_distance<T, FORMULA, FAST>(p.f, h.point, h.thr, N5, 0, true, L, mi, cnt);
+      const T s1 = wave_distance<T, FORMULA, FAST>(p.f, h.point, h.thr, N5, 0, true, L, mi, cnt, c.fparam);
       const T s2 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + dn, h.point.y + T(0), h.point.z + T(0)},
-                                                   h.thr, N5, 0, true, L, mi, cnt);
+                                                   h.thr, N5, 0, true, L, mi, cnt, c.fparam);
       const T s3 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + T(0), h.point.y + dn, h.point.z + T(0)},
-                                                   h.thr, N5, 0, true, L, mi, cnt);
+                                                   h.thr, N5, 0, true, L, mi, cnt, c.fparam);
       const T s4 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + T(0), h.point.y + T(0), h.point.z + dn},
-                                                   h.thr, N5, 0, true, L, mi, cnt);
+                                                   h.thr, N5, 0, true, L, mi, cnt, c.fparam);
       V3<T> nrm{s2 - s1, s3 - s1, s4 - s1};
       if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
       else nrm = normalize3(nrm);
@@ -985,7 +989,7 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
       shade2 = m_pow(shade2, T(30)) * T(1);
       if (shade2 > T(15)) shade2 = T(15);
       const T spec = shade2 * p.specular;
-      const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt);
+      const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt, c.fparam);
       objColour = colour;
       V3<T> ambient{T(0), T(0), T(0)};
       if (p.ao) {
@@ -994,7 +998,7 @@ __global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const 
           const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
           const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
           const T detail = (p.shadow && shadowStart < factor) ? (T)(float)h.thr : h.thr;
-          const T a = wave_fast_ao<T, FORMULA, FAST>(p, h.point, nrm, h.thr, detail, cnt);
+          const T a = wave_fast_ao<T, FORMULA, FAST>(p, h.point, nrm, h.thr, detail, cnt, c.fparam);
           ambient = {a, a, a};
         } else {
           T acc = T(0);

@@ -7,21 +7,26 @@ namespace mbgb {
 
 template <int F, bool FAST>
 static cudaError_t run_stages_f64(const WaveLaunch<double> &L, cudaStream_t s) {
-  if (L.ev[0]) cudaEventRecord(L.ev[0], s);
+  auto mark = [&](int k) {
+    if (L.ev[0]) cudaEventRecord(L.ev[k], s);
+  };
+  mark(0);
   dev::primary_kernel<double, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb, L.cams, L.ncams);
   if (L.overflow)
     dev::primary_kernel<double, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb, L.cams, L.ncams);
-  if (L.ev[0]) cudaEventRecord(L.ev[1], s);
+  mark(1);
+  mark(2);
   if (L.wb.exact_hit)
     dev::level_set_kernel<double, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
-  if (L.ev[0]) cudaEventRecord(L.ev[2], s);
+  mark(3);
   dev::secondary_kernel<double, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
-  if (L.ev[0]) cudaEventRecord(L.ev[3], s);
+  mark(4);
   dev::compose_kernel<double, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
-  if (L.ev[0]) cudaEventRecord(L.ev[4], s);
+  mark(5);
   if (L.gcams)
-    dev::grad_kernel<double, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 4), L.wb, L.cams, L.gcams,
+    dev::grad_kernel<double, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 5), L.wb, L.cams, L.gcams,
                                                                    L.ncams);
+  mark(6);
   return cudaGetLastError();
 }
 

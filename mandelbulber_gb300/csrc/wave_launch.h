@@ -42,6 +42,11 @@ struct WaveBufs {
   int64_t npix;
 };
 
+// Stage events of one launch sequence (see WaveLaunch::ev) and the stats slot of each
+// stage: primary 0, polish 1, shadow/AO 2, compose 3, level set 4, gradient 5.
+constexpr int kStageEvents = 7;
+constexpr int kStages = 6;
+
 constexpr int kChunk = 32;       // step records per pool chunk
 constexpr int kPoolChunksPerPixel = 4;   // pool budget; rays beyond it take the overflow pass
 
@@ -71,7 +76,10 @@ struct WaveLaunch {
   int grid, block, ov_grid, polish_grid, grid2, compose_grid;
   bool overflow;     // the step buffer is in use, so the overflow pass is enqueued
   bool fast;         // the scene qualifies for a lean FP32 orbit (Mandelbox, power-8 Mandelbulb)
-  cudaEvent_t ev[5]; // optional: recorded before stage 0 and after each of the 4 stages
+  // optional stage events, in launch order: before the primary rays, after them, after the
+  // polish, after the level-set refinement, after the shadow/AO rays, after composition,
+  // after the gradient stage
+  cudaEvent_t ev[kStageEvents];
   int grad_grid;     // blocks of the gradient stage
 };
 

@@ -139,3 +139,21 @@ def test_flight_frames_against_oracle(gpu_ctx, oracle, frame):
     m = metrics.compare(got, ref)
     assert m["hit_mismatch"] <= 0.001, m
     assert m["psnr_float"] >= 45.0, m
+
+
+def test_per_frame_fractal_parameter(gpu_ctx):
+    # frames that differ only in power (formula 2) or scale (formula 8) share one launch
+    # sequence: the parameter travels in the frame table
+    bulbs = [W.workload("mandelbulb_640x480", 64, 48, power=pw) for pw in (6.5, 7.0, 9.25)]
+    batch = gpu_ctx.render_batch(bulbs)
+    assert gpu_ctx.stats().launches == 4
+    for i, f in enumerate(bulbs):
+        _same(batch[i], gpu_ctx.render(f), f"power frame {i}")
+    boxes = [W.workload("mandelbox_1080p", 96, 54, mandelbox_scale=sc) for sc in (2.0, 2.2, -1.5)]
+    batch = gpu_ctx.render_batch(boxes)
+    assert gpu_ctx.stats().launches == 5   # + the overflow pass of the volumetric records
+    for i, f in enumerate(boxes):
+        _same(batch[i], gpu_ctx.render(f), f"scale frame {i}")
+    batch = gpu_ctx.render_batch(boxes, precision=mb.PREC_FP64)
+    for i, f in enumerate(boxes):
+        _same(batch[i], gpu_ctx.render(f, precision=mb.PREC_FP64), f"FP64 scale frame {i}")
