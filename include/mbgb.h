@@ -278,6 +278,11 @@ const char *mbgb_last_error(void);
 mbgb_status mbgb_scene_from_settings(const char *defaults_path, const char *path,
                                      const char *const *overrides, int n_overrides,
                                      mbgb_scene *out);
+/* A string-valued setting (file_destination, file_keyframes, file_animation_path, ...) as
+ * LoadSettings reads the same files and overrides (the last occurrence wins) into `out`.
+ * MBGB_ERR_BAD_PARAM when the key occurs nowhere or `out_len` is too small. */
+mbgb_status mbgb_settings_string(const char *defaults_path, const char *path, const char *const *overrides,
+                                 int n_overrides, const char *key, char *out, int32_t out_len);
 /* Apply one "key value" pair (LoadOneSetting). Returns MBGB_ERR_BAD_PARAM for an unknown key. */
 mbgb_status mbgb_scene_set(mbgb_scene *scene, const char *key, const char *value);
 /* Re-derive the dependent fields (analytic-DE flag, resolution, matrices, clamps) after edits. */
@@ -382,6 +387,28 @@ mbgb_status mbgb_distance_device(mbgb_context *ctx, const mbgb_scene *scene, int
  * Gamma/brightness/contrast/HDR of CalculatePixel + CompileImage into RGB16, host pointers. */
 mbgb_status mbgb_compile_image16(const mbgb_scene *scene, const float *image_float,
                                  int32_t width, int32_t height, uint16_t *image16);
+
+/* SavePNG / SavePNG16 / SavePNG16Alpha (src/files.cpp:385-565): a PNG file of width x height
+ * pixels, `channels` 3 (RGB) or 4 (RGBA), `bit_depth` 8 (uint8_t samples) or 16 (uint16_t
+ * samples in host order; big-endian in the file), rows top to bottom. The pixel data are
+ * stored in uncompressed deflate blocks (no zlib needed); decoders read the same samples
+ * the reference's libpng files hold. Host pointers. */
+mbgb_status mbgb_write_png(const char *path, int32_t width, int32_t height, int32_t bit_depth, int32_t channels,
+                           const void *pixels);
+
+/* CompileImage (src/cimage.cpp:132-214, progressive factor 1) on the device: image_float
+ * (device, RGB float) -> image16 (device, RGB16) with the scene's brightness, contrast,
+ * gamma and HDR switch. Synchronous on the context's stream. */
+mbgb_status mbgb_compile_image16_device(mbgb_context *ctx, const mbgb_scene *scene, const float *image_float,
+                                        int32_t width, int32_t height, uint16_t *image16);
+
+/* PostRendering_SSAO (src/image.cpp:249-478) on the device, in place on image16 (device,
+ * RGB16 from CompileImage), reading the z-buffer, opacity and colour layers of `layers`
+ * (device pointers): scene->SSAOQuality directions x (quality - 1) samples per pixel,
+ * intensity scene->globalIlum, the scene's perspective type and persp. Arithmetic in
+ * double (the reference's) unless opts->precision is MBGB_PREC_FP32_FIX. Synchronous. */
+mbgb_status mbgb_ssao_device(mbgb_context *ctx, const mbgb_scene *scene, const mbgb_image *layers,
+                             uint16_t *image16, const mbgb_opts *opts);
 
 #ifdef __cplusplus
 }

@@ -100,6 +100,10 @@ FUNCTIONS = {
     "mbgb_scene_from_settings": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _P(ctypes.c_char_p), ctypes.c_int,
                                                 _P(mbgb_scene)]),
     "mbgb_scene_set": (ctypes.c_int, [_P(mbgb_scene), ctypes.c_char_p, ctypes.c_char_p]),
+    "mbgb_settings_string": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _P(ctypes.c_char_p), ctypes.c_int,
+                                            ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32]),
+    "mbgb_write_png": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_void_p]),
     "mbgb_scene_finalize": (ctypes.c_int, [_P(mbgb_scene)]),
     "mbgb_catmull_rom": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p]),
@@ -126,6 +130,10 @@ FUNCTIONS = {
                                             ctypes.c_void_p]),
     "mbgb_compile_image16": (ctypes.c_int, [_P(mbgb_scene), ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                             ctypes.c_void_p]),
+    "mbgb_compile_image16_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_void_p, ctypes.c_int32,
+                                                   ctypes.c_int32, ctypes.c_void_p]),
+    "mbgb_ssao_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), ctypes.c_void_p,
+                                        _P(mbgb_opts)]),
 }
 
 

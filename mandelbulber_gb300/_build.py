@@ -20,6 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libmbgb.so")
 PEAK_LIB = os.path.join(PKG, "libmbgb_peak.so")
+CLI = os.path.join(PKG, "mbgb_cli")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -44,9 +45,11 @@ def _units(cuda: str):
     yield "noalloc.cu", common_cu
     yield "wave_f64.cu", common_cu + ["--fmad=false"]
     yield "wave_f32.cu", common_cu
+    yield "post.cu", common_cu + ["--fmad=false"]
     yield "capi.cpp", common_cpp
     yield "settings.cpp", common_cpp
     yield "keyframes.cpp", common_cpp
+    yield "image_io.cpp", common_cpp
 
 
 def _sources_newer(target: str) -> bool:
@@ -94,6 +97,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     r = subprocess.run(peak, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"peak tool build failed: {' '.join(peak)}\n{r.stdout}\n{r.stderr}")
+    # the -nogui command-line renderer, linked against the library next to it
+    cli = [os.path.join(cuda, "bin", "nvcc"), "-std=c++17", "-O2", "-I", INCLUDE, "-o", CLI,
+           os.path.join(CSRC, "cli.cpp"), "-L", PKG, "-lmbgb", "-Xlinker", "-rpath,$ORIGIN", "-cudart", "static"]
+    r = subprocess.run(cli, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"mbgb_cli build failed: {' '.join(cli)}\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -361,6 +361,7 @@ struct mbgb_context {
   DeviceBuf probe;               // MBGB_PREC_AUTO: distance probes at the ray origins
   DeviceBuf tune_out;            // autotuner output layers
   DeviceBuf gradacc;             // differentiable render: per-frame dL/dtheta sums
+  DeviceBuf post;                // post-processing: gamma table and SSAO direction tables
   uint64_t gen = 0;              // bumped whenever a scratch buffer is reallocated
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> gev;  // stage events, kStageEvents per group (profile_stages)
@@ -454,6 +455,7 @@ extern "C" void mbgb_context_destroy(mbgb_context *c) {
   c->probe.release();
   c->tune_out.release();
   c->gradacc.release();
+  c->post.release();
   c->control.release();
   c->fctl.release();
   c->cams.release();
@@ -1581,6 +1583,32 @@ extern "C" mbgb_status mbgb_distance_device(mbgb_context *c, const mbgb_scene *s
   if (e != cudaSuccess) return cuda_error(e, "distance kernel launch");
   MBGB_CUDA(cudaStreamSynchronize(c->stream));
   return MBGB_OK;
+}
+
+extern "C" mbgb_status mbgb_compile_image16_device(mbgb_context *c, const mbgb_scene *scene,
+                                                   const float *image_float, int32_t width, int32_t height,
+                                                   uint16_t *image16) {
+  if (!c || !scene || !image_float || !image16 || width <= 0 || height <= 0)
+    return set_error(MBGB_ERR_BAD_PARAM, "bad argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  MBGB_CUDA(cudaSetDevice(c->device));
+  MBGB_CUDA(c->ensure(c->post, sizeof(int) * 65536));
+  return compile16_device(*scene, image_float, width, height, image16, (int *)c->post.ptr, c->stream);
+}
+
+extern "C" mbgb_status mbgb_ssao_device(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *layers,
+                                        uint16_t *image16, const mbgb_opts *opts) {
+  if (!c || !scene || !layers || !image16) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
+  if (!layers->zbuffer || !layers->opacity || !layers->colour)
+    return set_error(MBGB_ERR_BAD_PARAM, "SSAO needs the z-buffer, opacity and colour layers");
+  if (layers->width <= 0 || layers->height <= 0) return set_error(MBGB_ERR_BAD_PARAM, "bad image size");
+  if (scene->SSAOQuality > 1000) return set_error(MBGB_ERR_BAD_PARAM, "SSAO quality above 1000");
+  mbgb_opts o{};
+  if (opts) o = *opts;
+  std::lock_guard<std::mutex> lk(c->mu);
+  MBGB_CUDA(cudaSetDevice(c->device));
+  MBGB_CUDA(c->ensure(c->post, std::max<size_t>(sizeof(int) * 65536, 16 * (size_t)(scene->SSAOQuality + 1))));
+  return ssao_device(*scene, *layers, image16, o.precision != MBGB_PREC_FP32_FIX, c->post.ptr, c->stream);
 }
 
 // CompileImage / CalculatePixel / CalculateGammaTable (src/cimage.cpp:132-214), progressive factor 1.

@@ -538,7 +538,59 @@ mbgb_status load_file(const char *path, mbgb_scene *sc, const std::vector<std::s
   return MBGB_OK;
 }
 
+// The value of `key` in a settings file as LoadSettings2 reads it (the last line wins);
+// false when the key does not occur.
+bool find_string(const char *path, const char *key, std::string &value) {
+  FILE *fp = fopen(path, "r");
+  if (!fp) return false;
+  bool found = false;
+  std::vector<char> str1(100), str2(2000);
+  while (!feof(fp)) {
+    int c = fscanf(fp, "%99s", str1.data());
+    if (c > 0) {
+      str2[0] = 0;
+      c = fscanf(fp, "%1999[ ]", str2.data());
+      str2[0] = 0;
+      c = fscanf(fp, "%1999[^;]", str2.data());
+      if (c <= 0) str2[0] = 0;
+      if (strcmp(str1.data(), key) == 0) {
+        value = str2.data();
+        found = true;
+      }
+      c = fscanf(fp, "%1999[^\n]", str2.data());
+    }
+  }
+  fclose(fp);
+  return found;
+}
+
 }  // namespace
+
+extern "C" mbgb_status mbgb_settings_string(const char *defaults_path, const char *path,
+                                            const char *const *overrides, int n_overrides, const char *key,
+                                            char *out, int32_t out_len) {
+  if (!path || !key || !out || out_len < 1) return mbgb::set_error(MBGB_ERR_BAD_PARAM, "mbgb_settings_string: bad argument");
+  if (n_overrides < 0 || (n_overrides > 0 && !overrides))
+    return mbgb::set_error(MBGB_ERR_BAD_PARAM, "mbgb_settings_string: bad override list");
+  std::string value;
+  bool found = false;
+  if (defaults_path) found = find_string(defaults_path, key, value);
+  FILE *probe = fopen(path, "r");
+  if (!probe) return mbgb::set_error(MBGB_ERR_IO, std::string("cannot open settings file: ") + path);
+  fclose(probe);
+  found = find_string(path, key, value) || found;
+  for (int i = 0; i < n_overrides; i++) {
+    char k[100], v[2000];
+    if (overrides[i] && sscanf(overrides[i], "%99[^= \t]%*1[= ]%1999s", k, v) == 2 && strcmp(k, key) == 0) {
+      value = v;
+      found = true;
+    }
+  }
+  if (!found) return mbgb::set_error(MBGB_ERR_BAD_PARAM, std::string("setting not present: ") + key);
+  if ((int32_t)value.size() >= out_len) return mbgb::set_error(MBGB_ERR_BAD_PARAM, "output buffer too small");
+  memcpy(out, value.c_str(), value.size() + 1);
+  return MBGB_OK;
+}
 
 extern "C" mbgb_status mbgb_scene_from_settings(const char *defaults_path, const char *path,
                                                 const char *const *overrides, int n_overrides,

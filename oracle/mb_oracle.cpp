@@ -19,6 +19,8 @@
 //   background                        BackgroundShader           src/shaders.cpp:114-183
 //   volumetric                        VolumetricShader           src/shaders.cpp:185-478
 //   render_rows                       MainThread pixel body      src/Render3D.cpp:213-344, 389-589
+//   compile16                         CompileImage / CalculatePixel / CalculateGammaTable src/cimage.cpp:132-214
+//   ssao                              PostRendering_SSAO / ThreadSSAO src/image.cpp:249-478
 //   level_set                         (not in the reference) Newton refinement of a hit onto
 //                                     DE(P) = thr, the surface the differentiable render's
 //                                     gradients are checked on; off unless oracle_render_exact
@@ -737,6 +739,102 @@ static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int 
     }
   }
   return 0;
+}
+
+// CompileImage with progressive factor 1: brightness and contrast in double rounded to
+// float, optional float tanh, clamp to [0, 1], x 65535 truncated, gamma table.
+void oracle_compile16(int w, int h, const float *image_float, double brightness, double contrast, double gamma,
+                      int hdr, unsigned short *image16) {
+  std::vector<int> table(65536);
+  for (int i = 0; i < 65536; i++) table[i] = (int)(pow(i / 65536.0, 1.0 / gamma) * 65535);
+  const long n = 3L * w * h;
+  for (long i = 0; i < n; i++) {
+    float v = (float)(image_float[i] * brightness);
+    v = (float)((v - 0.5) * contrast + 0.5);
+    if (v < 0.0f) v = 0.0f;
+    if (hdr) v = tanhf(v);
+    if (v > 1.0f) v = 1.0f;
+    const unsigned short q = (unsigned short)(v * 65535.0);
+    image16[i] = (unsigned short)table[q];
+  }
+}
+
+// SSAO over an RGB16 image (in place). For each pixel on the object: `quality` directions
+// at angle i / quality * 2 pi; along each, samples at radius r^2 * width / (2 quality^2),
+// r = 1 .. quality - 1, skipping the pixel itself and samples off the image; the steepest
+// -dz / (lateral distance) gives the horizon, ambient += 0.5 - atan(slope) / pi. Lateral
+// positions follow the perspective type; the fish-eye centre skips its projection at
+// radius 0, its samples do not (they test the loop radius, which is never 0).
+void oracle_ssao(int w, int h, const float *zbuf, const unsigned short *opacity, const unsigned char *colour,
+                 double persp, int quality, int ptype, double intensity, unsigned short *image16) {
+  std::vector<double> ca(quality > 0 ? quality : 1), sa(quality > 0 ? quality : 1);
+  for (int i = 0; i < quality; i++) {
+    sa[i] = sin((double)i / quality * 2.0 * M_PI);
+    ca[i] = cos((double)i / quality * 2.0 * M_PI);
+  }
+  const double scale = (double)w / (quality * quality) / 2.0;
+  const double aspect = (double)w / h;
+  auto lateral = [&](double fx, double fy, double z, bool centre, double &ox, double &oy) {
+    if (ptype == MBGB_PERSP_FISH_EYE) {
+      const double x2 = M_PI * (fx / w - 0.5) * aspect;
+      const double y2 = M_PI * (fy / h - 0.5);
+      const double r = sqrt(x2 * x2 + y2 * y2);
+      ox = x2;
+      oy = y2;
+      if (!centre || r != 0.0) {
+        ox = x2 / r * sin(r * persp) * z;
+        oy = y2 / r * sin(r * persp) * z;
+      }
+    } else if (ptype == MBGB_PERSP_EQUIRECT) {
+      const double x2 = M_PI * (fx / w - 0.5) * aspect;
+      const double y2 = M_PI * (fy / h - 0.5);
+      ox = sin(persp * x2) * cos(persp * y2) * z;
+      oy = sin(persp * y2) * z;
+    } else if (centre) {
+      ox = (fx / w - 0.5) * aspect * z * persp;
+      oy = (fy / h - 0.5) * z * persp;
+    } else {
+      ox = (fx / w - 0.5) * aspect * (z * persp);
+      oy = (fy / h - 0.5) * (z * persp);
+    }
+  };
+  for (int y = 0; y < h; y++) {
+    for (int x = 0; x < w; x++) {
+      const long p = (long)y * w + x;
+      const double z = zbuf[p];
+      const double op = opacity[p] / 65535.0;
+      double total = 0.0;
+      if (z < 1e19) {
+        double x2, y2;
+        lateral(x, y, z, true, x2, y2);
+        double ambient = 0.0;
+        for (int a = 0; a < quality; a++) {
+          double best = -1e50;
+          for (double r = 1.0; r < quality; r += 1.0) {
+            const double rr = r * r * scale;
+            const double xx = x + rr * ca[a];
+            const double yy = y + rr * sa[a];
+            if ((int)xx == x && (int)yy == y) continue;
+            if (xx < 0 || xx > w - 1 || yy < 0 || yy > h - 1) continue;
+            const double z2 = zbuf[(long)(int)yy * w + (int)xx];
+            double xx2, yy2;
+            lateral(xx, yy, z2, false, xx2, yy2);
+            const double dx = xx2 - x2, dy = yy2 - y2, dz = z2 - z;
+            const double slope = -dz / sqrt(dx * dx + dy * dy);
+            if (slope > best) best = slope;
+          }
+          ambient += -atan(best) / M_PI + 0.5;
+        }
+        total = ambient / quality;
+        if (total < 0) total = 0;
+      }
+      for (int c = 0; c < 3; c++) {
+        double v = image16[3 * p + c] + 65535.0 * colour[3 * p + c] / 256.0 * total * intensity * (1.0 - op);
+        if (v > 65535) v = 65535;
+        image16[3 * p + c] = (unsigned short)v;
+      }
+    }
+  }
 }
 
 int oracle_render(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,

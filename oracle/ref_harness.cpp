@@ -28,7 +28,9 @@
 
 guint64 N_counter = 0;
 guint64 Loop_counter = 0;
+#ifndef MBGB_REF_POST   // the post-processing build takes it from src/image.cpp
 guint64 histogram[256];
+#endif
 
 // ---- cTexture: the default constructor's white bitmap ----
 cTexture::cTexture(void) {

@@ -7,11 +7,15 @@ oracle/ref_harness.cpp) and records, for seeded inputs:
   * de_<formula>.npz      CalculateDistance (distance, itersOut, max_iter) and the
                           Compute<colouring> value SurfaceColour uses, at seeded points;
   * render_<case>.npz     every cImage layer of the MainThread pixel body (jitter off)
-                          for small frames covering the shading features.
+                          for small frames covering the shading features;
+  * post_<case>.npz       CompileImage (src/cimage.cpp:183-214) and PostRendering_SSAO
+                          (src/image.cpp:249-478) of the reference (oracle/_ref/libmbref_post.so)
+                          applied to render fixtures, for several image adjustments.
 Each file also stores the scene as raw mbgb_scene bytes and its settings keys, so
 the tests rebuild the exact input without the reference tree.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # everything
+    python tests/golden/make_golden.py post     # the post-processing fixtures only
 """
 from __future__ import annotations
 
@@ -145,9 +149,53 @@ def main():
     lib.ref_catmull_rom(ptr(keys), n_keys, size, fpk, n_keys * fpk, ptr(out))
     np.savez_compressed(os.path.join(HERE, "catmull_rom.npz"), keys=keys, frames_per_key=fpk, out=out)
     manifest["catmull_rom.npz"] = {"keys": [n_keys, size], "frames_per_key": fpk}
+    post_goldens(manifest)
     with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
 
+# render fixtures used as post-processing inputs, with (brightness, contrast, gamma, hdr,
+# SSAO quality, global illumination intensity)
+POST_CASES = {
+    "mandelbulb_64x48": ("mandelbulb_64x48", 1.0, 1.0, 1.0, 0, 20, 1.0),
+    "mandelbox_96x54": ("mandelbox_96x54", 1.3, 1.1, 0.8, 0, 7, 0.8),
+    "fisheye": ("mandelbulb_fisheye_cut", 0.9, 1.4, 1.2, 1, 12, 1.0),
+    "equirect": ("mandelbulb_tiles_equirect", 1.0, 0.9, 1.0, 1, 5, 1.5),
+}
+
+
+def post_goldens(manifest: dict):
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libmbref_post.so"))
+    lib.ref_compile_image.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_ssao.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    for case, (render, bright, contrast, gamma, hdr, quality, ilum) in POST_CASES.items():
+        z = np.load(os.path.join(HERE, f"render_{render}.npz"))
+        sc = mb.scene_from_bytes(z["scene"].tobytes())
+        h, w = z["zbuffer"].shape
+        img_f = np.ascontiguousarray(z["image_float"], np.float32)
+        img16 = np.zeros((h, w, 3), np.uint16)
+        lib.ref_compile_image(w, h, ptr(img_f), bright, contrast, gamma, hdr, ptr(img16))
+        compiled = img16.copy()
+        lib.ref_ssao(w, h, ptr(np.ascontiguousarray(z["zbuffer"])), ptr(np.ascontiguousarray(z["opacity"])),
+                     ptr(np.ascontiguousarray(z["colour"])), sc.persp, quality, sc.perspectiveType, ilum, ptr(img16))
+        out = os.path.join(HERE, f"post_{case}.npz")
+        np.savez_compressed(out, render=np.array(render), brightness=bright, contrast=contrast, gamma=gamma,
+                            hdr=hdr, quality=quality, global_ilum=ilum, image16_compiled=compiled,
+                            image16_ssao=img16)
+        manifest[os.path.basename(out)] = {"render": render, "ssao_quality": quality,
+                                           "changed_by_ssao": float(np.mean(img16 != compiled))}
+        print(case, "ssao changed", np.mean(img16 != compiled))
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["post"]:
+        with open(os.path.join(HERE, "MANIFEST.json")) as f:
+            manifest = json.load(f)
+        post_goldens(manifest)
+        with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
+            json.dump(manifest, f, indent=1, sort_keys=True)
+    else:
+        main()

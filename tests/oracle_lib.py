@@ -28,6 +28,8 @@ def load(fast: bool = False) -> ctypes.CDLL:
     lib.oracle_render.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
     lib.oracle_render.restype = ctypes.c_int
     lib.oracle_render_exact.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+    lib.oracle_compile16.restype = None
+    lib.oracle_ssao.restype = None
     lib.oracle_render_exact.restype = ctypes.c_int
     _cache[key] = lib
     return lib
