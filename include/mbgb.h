@@ -405,10 +405,10 @@ mbgb_status mbgb_compile_image16_device(mbgb_context *ctx, const mbgb_scene *sce
 /* PostRendering_SSAO (src/image.cpp:249-478) on the device, in place on image16 (device,
  * RGB16 from CompileImage), reading the z-buffer, opacity and colour layers of `layers`
  * (device pointers): scene->SSAOQuality directions x (quality - 1) samples per pixel,
- * intensity scene->globalIlum, the scene's perspective type and persp. Arithmetic in
- * double (the reference's) unless opts->precision is MBGB_PREC_FP32_FIX. Synchronous. */
+ * intensity scene->globalIlum, the scene's perspective type and persp, in double (the
+ * reference's arithmetic). Synchronous. */
 mbgb_status mbgb_ssao_device(mbgb_context *ctx, const mbgb_scene *scene, const mbgb_image *layers,
-                             uint16_t *image16, const mbgb_opts *opts);
+                             uint16_t *image16);
 
 #ifdef __cplusplus
 }

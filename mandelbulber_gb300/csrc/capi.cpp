@@ -1597,18 +1597,16 @@ extern "C" mbgb_status mbgb_compile_image16_device(mbgb_context *c, const mbgb_s
 }
 
 extern "C" mbgb_status mbgb_ssao_device(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *layers,
-                                        uint16_t *image16, const mbgb_opts *opts) {
+                                        uint16_t *image16) {
   if (!c || !scene || !layers || !image16) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
   if (!layers->zbuffer || !layers->opacity || !layers->colour)
     return set_error(MBGB_ERR_BAD_PARAM, "SSAO needs the z-buffer, opacity and colour layers");
   if (layers->width <= 0 || layers->height <= 0) return set_error(MBGB_ERR_BAD_PARAM, "bad image size");
   if (scene->SSAOQuality > 1000) return set_error(MBGB_ERR_BAD_PARAM, "SSAO quality above 1000");
-  mbgb_opts o{};
-  if (opts) o = *opts;
   std::lock_guard<std::mutex> lk(c->mu);
   MBGB_CUDA(cudaSetDevice(c->device));
   MBGB_CUDA(c->ensure(c->post, std::max<size_t>(sizeof(int) * 65536, 16 * (size_t)(scene->SSAOQuality + 1))));
-  return ssao_device(*scene, *layers, image16, o.precision != MBGB_PREC_FP32_FIX, c->post.ptr, c->stream);
+  return ssao_device(*scene, *layers, image16, c->post.ptr, c->stream);
 }
 
 // CompileImage / CalculatePixel / CalculateGammaTable (src/cimage.cpp:132-214), progressive factor 1.

@@ -221,12 +221,7 @@ bool render_jobs(mbgb_context *ctx, const std::vector<Job> &jobs, const Args &a)
     const int w = sc.image_width, h = sc.image_height;
     const size_t px = (size_t)w * h;
     ok = mbgb_compile_image16_device(ctx, &sc, outs[i].image_float, w, h, img16[i]) == MBGB_OK;
-    if (ok && sc.SSAOEnabled) {
-      mbgb_opts po;
-      memset(&po, 0, sizeof(po));
-      po.precision = a.precision == MBGB_PREC_FP32_FIX ? MBGB_PREC_FP32_FIX : MBGB_PREC_FP64;
-      ok = mbgb_ssao_device(ctx, &sc, &outs[i], img16[i], &po) == MBGB_OK;
-    }
+    if (ok && sc.SSAOEnabled) ok = mbgb_ssao_device(ctx, &sc, &outs[i], img16[i]) == MBGB_OK;
     if (!ok) {
       fprintf(stderr, "mbgb_cli: post-processing: %s\n", mbgb_last_error());
       break;

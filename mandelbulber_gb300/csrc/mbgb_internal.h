@@ -40,7 +40,7 @@ int ao_vectors_into(int quality, float *out, int max_vectors);
 // Post-processing on the device (post.cu): CompileImage into RGB16 and the SSAO pass.
 mbgb_status compile16_device(const mbgb_scene &scene, const float *image_float, int width, int height,
                              uint16_t *image16, int *gamma_dev, cudaStream_t s);
-mbgb_status ssao_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, bool fp64,
-                        void *tables, cudaStream_t s);
+mbgb_status ssao_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, void *tables,
+                        cudaStream_t s);
 
 }  // namespace mbgb

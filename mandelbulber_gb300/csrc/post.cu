@@ -29,7 +29,7 @@ __global__ void compile16_kernel(const float *__restrict__ image_float, int64_t 
     float v = (float)((double)image_float[i] * brightness);
     v = (float)(((double)v - 0.5) * contrast + 0.5);
     if (v < 0.0f) v = 0.0f;
-    if (hdr) v = tanhf(v);
+    if (hdr) v = (float)tanh((double)v);   // the host's tanhf, to the float it rounds to
     if (v > 1.0f) v = 1.0f;
     const unsigned short q = (unsigned short)((double)v * 65535.0);
     image16[i] = (uint16_t)gamma[q];
@@ -93,8 +93,7 @@ __global__ void ssao_kernel(const float *__restrict__ zbuf, const uint16_t *__re
       T ambient = T(0);
       for (int a = 0; a < quality; a++) {
         const T ca = cs[a], sa = sn[a];
-        T maxDiff = T(-1e30);
-        if (sizeof(T) == 8) maxDiff = T(-1e50);
+        T maxDiff = T(-1e50);
         for (T r = T(1); r < (T)quality; r += T(1)) {
           const T rr = r * r * scale;
           const T xx = (T)x + rr * ca;
@@ -158,49 +157,28 @@ mbgb_status compile16_device(const mbgb_scene &scene, const float *image_float, 
   return MBGB_OK;
 }
 
-// PostRendering_SSAO on the device; `tables` holds 2 x quality values of precision T.
-mbgb_status ssao_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, bool fp64,
-                        void *tables, cudaStream_t s) {
+// PostRendering_SSAO on the device, in double (the reference's arithmetic): the sample
+// positions x + r^2 s cos(a) land on the neighbouring pixel or not depending on the last
+// bits of cos(a) near 0 (cos(pi / 2) = 6e-17), which float arithmetic does not keep.
+// `tables` receives cos and sin of the `quality` directions.
+mbgb_status ssao_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, void *tables,
+                        cudaStream_t s) {
   const int q = scene.SSAOQuality;
   if (q < 1) return MBGB_OK;   // the loops of ThreadSSAO run no direction: nothing changes
-  std::vector<double> cs(q), sn(q);
+  std::vector<double> t(2 * (size_t)q);
   for (int i = 0; i < q; i++) {
-    sn[i] = sin((double)i / q * 2.0 * kPi);
-    cs[i] = cos((double)i / q * 2.0 * kPi);
+    t[q + i] = sin((double)i / q * 2.0 * kPi);
+    t[i] = cos((double)i / q * 2.0 * kPi);
   }
   const int64_t n = (int64_t)layers.width * layers.height;
   const int block = 128;
-  const int grid = grid_for(n, block);
-  cudaError_t e;
-  if (fp64) {
-    std::vector<double> t(2 * (size_t)q);
-    for (int i = 0; i < q; i++) {
-      t[i] = cs[i];
-      t[q + i] = sn[i];
-    }
-    e = cudaMemcpyAsync(tables, t.data(), sizeof(double) * 2 * q, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-      ssao_kernel<double><<<grid, block, 0, s>>>(layers.zbuffer, layers.opacity, layers.colour, image16,
-                                                 layers.width, layers.height, scene.persp, q,
-                                                 scene.perspectiveType, scene.globalIlum, (const double *)tables,
-                                                 (const double *)tables + q);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  } else {
-    std::vector<float> t(2 * (size_t)q);
-    for (int i = 0; i < q; i++) {
-      t[i] = (float)cs[i];
-      t[q + i] = (float)sn[i];
-    }
-    e = cudaMemcpyAsync(tables, t.data(), sizeof(float) * 2 * q, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-      ssao_kernel<float><<<grid, block, 0, s>>>(layers.zbuffer, layers.opacity, layers.colour, image16,
-                                                layers.width, layers.height, (float)scene.persp, q,
-                                                scene.perspectiveType, (float)scene.globalIlum,
-                                                (const float *)tables, (const float *)tables + q);
-    if (e == cudaSuccess) e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  }
+  cudaError_t e = cudaMemcpyAsync(tables, t.data(), sizeof(double) * 2 * q, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    ssao_kernel<double><<<grid_for(n, block), block, 0, s>>>(
+        layers.zbuffer, layers.opacity, layers.colour, image16, layers.width, layers.height, scene.persp, q,
+        scene.perspectiveType, scene.globalIlum, (const double *)tables, (const double *)tables + q);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(MBGB_ERR_CUDA, std::string("SSAO kernel: ") + cudaGetErrorString(e));
   return MBGB_OK;
 }

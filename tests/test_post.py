@@ -5,7 +5,7 @@ tests/golden/post_*.npz hold CompileImage (src/cimage.cpp:132-214) and PostRende
 render fixtures with several brightness / contrast / gamma / HDR / SSAO-quality settings,
 for the three perspective types. The oracle's restatement and the library's host
 CompileImage must reproduce them exactly; the device kernels (GPU tests) exactly for the
-compile step without HDR and to +-1 of 65535 where CUDA's tanhf or atan round differently
+compile step without HDR and to +-1 of 65535 where CUDA's tanh or atan round differently
 from the host's libm (counted, at most 0.5 % of the values).
 """
 import ctypes
@@ -86,25 +86,19 @@ def test_device_compile_and_ssao_match_reference(gpu_ctx, name):
                                            img16.data_ptr()) == 0, lib.mbgb_last_error()
     got = img16.cpu().numpy().view(np.uint16)
     if sc.hdrEnabled:
-        _within_one(got, z["image16_compiled"], "compile (tanhf)")
+        _within_one(got, z["image16_compiled"], "compile (tanh)")
     else:
         np.testing.assert_array_equal(got, z["image16_compiled"])
-    # SSAO from the reference's compiled image
+    # SSAO from the reference's compiled image (the library runs on its own stream: wait
+    # for torch's copy first)
     img16.copy_(torch.tensor(z["image16_compiled"].view(np.int16), device="cuda"))
+    torch.cuda.synchronize()
     zb = torch.tensor(np.ascontiguousarray(r["zbuffer"]), device="cuda")
     op = torch.tensor(np.ascontiguousarray(r["opacity"]).view(np.int16), device="cuda")
     col = torch.tensor(np.ascontiguousarray(r["colour"]), device="cuda")
     layers = mb.mbgb_image(w, h, None, ctypes.c_void_p(zb.data_ptr()), None, ctypes.c_void_p(op.data_ptr()),
                            ctypes.c_void_p(col.data_ptr()), None, None, None)
-    opts = mb.make_opts(precision=mb.PREC_FP64)
-    assert lib.mbgb_ssao_device(gpu_ctx._h, ctypes.byref(sc), ctypes.byref(layers), img16.data_ptr(),
-                                ctypes.byref(opts)) == 0, lib.mbgb_last_error()
+    assert lib.mbgb_ssao_device(gpu_ctx._h, ctypes.byref(sc), ctypes.byref(layers), img16.data_ptr()) == 0, \
+        lib.mbgb_last_error()
     torch.cuda.synchronize()
-    _within_one(img16.cpu().numpy().view(np.uint16), z["image16_ssao"], "ssao fp64 (atan)")
-    # FP32 arithmetic: same bar on these fixtures
-    img16.copy_(torch.tensor(z["image16_compiled"].view(np.int16), device="cuda"))
-    opts = mb.make_opts(precision=mb.PREC_FP32_FIX)
-    assert lib.mbgb_ssao_device(gpu_ctx._h, ctypes.byref(sc), ctypes.byref(layers), img16.data_ptr(),
-                                ctypes.byref(opts)) == 0, lib.mbgb_last_error()
-    d = np.abs(img16.cpu().numpy().view(np.uint16).astype(np.int64) - z["image16_ssao"].astype(np.int64))
-    assert d.max() <= 64, ("ssao fp32", int(d.max()))
+    _within_one(img16.cpu().numpy().view(np.uint16), z["image16_ssao"], "ssao (atan)")
