@@ -204,7 +204,7 @@ typedef struct mbgb_opts {
   int32_t engine;              /* MBGB_ENGINE_*; 0 = wavefront stages */
   int32_t profile_stages;      /* 1: record CUDA events between stages (synchronous calls fill stage_ms) */
   int32_t polish_all;          /* FP32_FIX: 1 = re-run the end of every hit's bisection in FP64; 0 = only the
-                                * hits whose FP32 window decision is within 1e-4 of an edge */
+                                * hits whose FP32 bisection stopped early within 1e-4 of a window edge */
   int32_t tile_w, tile_h;      /* wavefront: pixel tile of a warp's first 32 primary rays (tile_w * tile_h
                                 * = 32); 0,0 = autotuned or 8 x 4 */
   int32_t refill_min;          /* wavefront: idle lanes of a warp before it claims new rays; 0 = tuned or 1 */

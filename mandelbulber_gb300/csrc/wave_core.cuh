@@ -40,7 +40,6 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
   const float mR2 = f.mbMinR * f.mbMinR;
   const float fR2 = f.mbFixedR * f.mbFixedR;
   const float k1 = fR2 / mR2;
-  const float as = fabsf(s);
   const float cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
   float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
   int L;
@@ -57,7 +56,7 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
     x = fmaf(x, ks, cx);
     y = fmaf(y, ks, cy);
     z = fmaf(z, ks, cz);
-    dr = fmaf(dr, k * as, 1.0f);
+    dr = fmaf(dr, fabsf(ks), 1.0f);   // |k s| = k |s| (k > 0), one instruction
     r2 = x * x + y * y + z * z;
     if (r2 > 1048576.0f) {
       dist = sqrtf(r2) / fabsf(dr);
@@ -131,6 +130,107 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
   }
   // colouring: min |z| after a bailout, else the last |z|
   return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
+}
+
+// FP64 versions of the lean orbits for the FP32 policy's FP64 polish, which needs FP64
+// accuracy but not the reference's operation order: the squared radius throughout (no
+// square root per iteration) and, for the Mandelbulb, no transcendentals.
+__device__ __forceinline__ double mandelbox_lean_d(const FractalT<double> &f, const double px, const double py,
+                                                   const double pz, const int N, int &Lout, Counters &cnt,
+                                                   const double s) {
+  const double fl = f.mbFoldLimit;
+  const double mR2 = f.mbMinR * f.mbMinR;
+  const double fR2 = f.mbFixedR * f.mbFixedR;
+  const double k1 = fR2 / mR2;
+  const double cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
+  double x = px, y = py, z = pz, dr = 1.0, dist = 0.0;
+  int L;
+  for (L = 0; L < N; L++) {
+    x = fmin(fmax(x, -fl), fl) * 2.0 - x;
+    y = fmin(fmax(y, -fl), fl) * 2.0 - y;
+    z = fmin(fmax(z, -fl), fl) * 2.0 - z;
+    double r2 = x * x + y * y + z * z;
+    const double k = fmin(fmax(fR2 / r2, 1.0), k1);
+    const double ks = k * s;
+    x = fma(x, ks, cx);
+    y = fma(y, ks, cy);
+    z = fma(z, ks, cz);
+    dr = fma(dr, fabs(ks), 1.0);
+    r2 = x * x + y * y + z * z;
+    if (r2 > 1048576.0) {
+      dist = sqrt(r2) / fabs(dr);
+      break;
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (L == N) dist = 0.0;
+  return dist;
+}
+
+__device__ __forceinline__ double mandelbulb8_lean_d(const FractalT<double> &f, const double px, const double py,
+                                                     const double pz, const int N, int &Lout, Counters &cnt) {
+  double cx, cy, cz;
+  if (f.juliaMode) {
+    cx = f.julia[0]; cy = f.julia[1]; cz = f.julia[2];
+  } else {
+    cx = px * f.constantFactor; cy = py * f.constantFactor; cz = pz * f.constantFactor;
+  }
+  double x = px, y = py, z = pz, r_dz = 1.0, dist = 0.0;
+  double r2 = x * x + y * y + z * z;
+  int L;
+  for (L = 0; L < N; L++) {
+    const double rho2 = x * x + y * y;
+    const double inv_r = rsqrt(r2);
+    const bool axis = rho2 == 0.0;
+    const double inv_rho = axis ? 0.0 : rsqrt(rho2);
+    double ct = rho2 * inv_rho * inv_r, st = z * inv_r;
+    double cp = axis ? 1.0 : x * inv_rho, sp = axis ? 0.0 : y * inv_rho;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double ct2 = ct * ct - st * st, st2 = 2.0 * st * ct;
+      const double cp2 = cp * cp - sp * sp, sp2 = 2.0 * sp * cp;
+      ct = ct2; st = st2; cp = cp2; sp = sp2;
+    }
+    const double r4 = r2 * r2;
+    const double r8 = r4 * r4;
+    r_dz = fma(8.0 * r8 * inv_r, r_dz, 1.0);
+    const double t = ct * r8;
+    x = fma(t, cp, cx);
+    y = fma(t, sp, cy);
+    z = fma(st, r8, cz);
+    r2 = x * x + y * y + z * z;
+    if (r2 > 1.0e4) {
+      const double r = sqrt(r2);
+      dist = 0.5 * r * log(r) / r_dz;
+      break;
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (L == N) dist = 0.0;
+  return dist;
+}
+
+// CalculateDistance in FP64 for the polish: the lean orbits when the scene qualifies.
+template <int FORMULA, bool FAST>
+__device__ __forceinline__ double polish_distance(const FractalT<double> &f, const V3<double> p, const double detail,
+                                                  int &L, bool &maxIter, Counters &cnt, const double fparam) {
+  if constexpr (FAST) {
+    int Li;
+    double distance;
+    if constexpr (FORMULA == 8) distance = mandelbox_lean_d(f, p.x, p.y, p.z, f.N, Li, cnt, fparam);
+    else distance = mandelbulb8_lean_d(f, p.x, p.y, p.z, f.N, Li, cnt);
+    maxIter = (Li == f.N);
+    L = Li;
+    if (distance < 0.0) distance = 0.0;
+    if (Li < f.minN && distance < detail) distance = detail;
+    return distance;
+  } else {
+    return calc_distance<double, FORMULA>(f, p, detail, f.N, f.minN, false, L, maxIter, cnt, fparam);
+  }
 }
 
 // CalculateDistance with the orbit chosen at compile time: FAST selects mandelbox_fast
@@ -357,7 +457,7 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 // Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const FractalT<double> fd,
+__global__ void __launch_bounds__(128, 6) primary_kernel(const ParamsT<T> p, const FractalT<double> fd,
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -558,13 +658,15 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
         if (found) {
           const unsigned int k = atomicAdd(wb.ctl + 1, 1u);
           wb.hit_list[k] = (unsigned int)gp;
-          // FP32 policy: the FP64 polish re-checks every hit whose FP32 bisection did not end
-          // clearly inside the window (dist/thr within 1e-4 of an edge, or 20 steps used);
-          // exact_hit: every hit goes on to the level-set refinement
+          // FP32 policy: the FP64 polish re-checks every hit whose FP32 bisection stopped
+          // early but not clearly inside the window (dist/thr within 1e-4 of an edge). A
+          // bisection that used all 20 steps has none left to continue, so FP64 would keep
+          // its depth: it is not re-evaluated. exact_hit: every hit goes on to the level-set
+          // refinement.
           if (!f64 || wb.exact_hit) {
             const T q = dist / thr;
             const bool clear = (q > search_limit + T(1e-4)) && (q < T(1) - T(1e-4));
-            if (wb.polish_all || wb.exact_hit || !clear) {
+            if (wb.polish_all || wb.exact_hit || (!clear && bis < 20)) {
               const unsigned int m = atomicAdd(wb.ctl + 6, 1u);
               wb.polish_list[m] = (unsigned int)gp;
             }
@@ -591,9 +693,10 @@ __global__ void __launch_bounds__(128) primary_kernel(const ParamsT<T> p, const 
 // ---------------------------------------------------------------------------
 // Stage 2 (FP32 policy): finish the binary refinement in FP64 (src/Render3D.cpp:145-183)
 // for the hits on the polish list: the distance is re-evaluated in FP64 at the FP32
-// result and the bisection continues with the iterations it has left.
+// result and the bisection continues with the iterations it has left. Scenes of the lean
+// orbit class use the FP64 lean orbits (polish_distance).
 // ---------------------------------------------------------------------------
-template <int FORMULA>
+template <int FORMULA, bool FAST>
 __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, const FractalT<double> fd,
                                                      const FrameIO io, const WaveBufs<float> wb,
                                                      const FrameCam<float> *__restrict__ cams, const int ncams) {
@@ -619,7 +722,7 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
     V3<double> point = start + dir * scan;
     int iters = 0;
     bool mi;
-    double dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt, c.fparam_d);
+    double dist = polish_distance<FORMULA, FAST>(fd, point, detail, iters, mi, cnt, c.fparam_d);
     cnt.steps++;
     for (int it = 0; it < left; it++) {
       if (dist < thr && dist > thr * search_limit) break;
@@ -627,7 +730,7 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
       else if (dist < thr * search_limit) scan -= step;
       point = start + dir * scan;
       thr = thr_of(scan);
-      dist = calc_distance<double, FORMULA>(fd, point, detail, fd.N, fd.minN, false, iters, mi, cnt, c.fparam_d);
+      dist = polish_distance<FORMULA, FAST>(fd, point, detail, iters, mi, cnt, c.fparam_d);
       cnt.steps++;
       step *= 0.5;
     }

@@ -15,7 +15,7 @@ static cudaError_t run_stages_f32(const WaveLaunch<float> &L, cudaStream_t s) {
   if (L.overflow)
     dev::primary_kernel<float, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb, L.cams, L.ncams);
   mark(1);
-  dev::polish_kernel<F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), L.wb, L.cams, L.ncams);
+  dev::polish_kernel<F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), L.wb, L.cams, L.ncams);
   mark(2);
   if (L.wb.exact_hit)
     dev::level_set_kernel<float, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
