@@ -492,12 +492,14 @@ static mbgb_status ensure_ao(mbgb_context *c, int quality, cudaStream_t s) {
 }
 
 // The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
-// julia, limits, iteration threshold or interior mode, and fold value = 2 x fold limit.
+// julia, limits, iteration threshold or interior mode, fold value = 2 x fold limit, and
+// min radius <= fixed radius (so that the sphere fold is a clamp).
 static bool fast_mandelbox(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
          !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
          s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
-         s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit;
+         s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
+         s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
 }
 
 // The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,

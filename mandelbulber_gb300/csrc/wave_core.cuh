@@ -39,7 +39,9 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
   const float fl = f.mbFoldLimit;
   const float mR2 = f.mbMinR * f.mbMinR;
   const float fR2 = f.mbFixedR * f.mbFixedR;
-  const float k1 = fR2 / mR2;
+  const float k1 = fR2 / mR2;   // >= 1 in the lean class (min radius <= fixed radius)
+  const float km1 = k1 - 1.0f;
+  const float sa = km1 > 0.0f ? fR2 / km1 : 0.0f, sb = km1 > 0.0f ? 1.0f / km1 : 0.0f;
   const float cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
   float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
   int L;
@@ -49,9 +51,10 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
     y = fminf(fmaxf(y, -fl), fl) * 2.0f - y;
     z = fminf(fmaxf(z, -fl), fl) * 2.0f - z;
     float r2 = x * x + y * y + z * z;
-    // sphere fold: fR2/mR2 inside mR2, fR2/r2 between mR2 and fR2, 1 outside; the same
-    // value as the clamp of fR2/r2 to [1, fR2/mR2]
-    const float k = fminf(fmaxf(__fdividef(fR2, r2), 1.0f), k1);
+    // sphere fold: fR2/mR2 inside mR2, fR2/r2 between mR2 and fR2, 1 outside; the clamp of
+    // fR2/r2 to [1, k1], written 1 + (k1 - 1) sat((fR2/r2 - 1) / (k1 - 1)) so that the
+    // clamp rides on the FMA pipe's saturation instead of two min/max instructions
+    const float k = fmaf(__saturatef(__fdividef(sa, r2) - sb), km1, 1.0f);
     const float ks = k * s;
     x = fmaf(x, ks, cx);
     y = fmaf(y, ks, cy);
