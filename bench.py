@@ -44,6 +44,23 @@ DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 37.6e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
 
 
+def max_over_ranks(seconds: float, dist, device) -> float:
+    """The slowest rank's timed region (every rank gets it); `dist` is torch.distributed or
+    None for one process. `device` holds the reduction tensor (a GPU for NCCL, "cpu" for gloo)."""
+    if not dist:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank_step: float, steps: int, seconds: float) -> float:
+    """Weak scaling: every rank processes the same units per step; the job's rate is all
+    ranks' units over the slowest rank's time."""
+    return world * units_per_rank_step * steps / seconds
+
+
 def env_int(name, default):
     try:
         return int(os.environ.get(name, default))
@@ -198,11 +215,7 @@ def batch_section(ctx, torch, dev, stream, flush, args, world, dist) -> dict:
             e1.record(stream)
         stream.synchronize()
         total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-        if dist:
-            t = torch.tensor([total], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total = float(t.item())
-        return total
+        return max_over_ranks(total, dist, dev)
 
     steps = max(1, args.batch_steps)
     t_graph = run(steps, 3, autotune=True, use_graph=True)
@@ -362,11 +375,7 @@ def main() -> int:
         wall = time.perf_counter() - t_wall
         ms = [a.elapsed_time(b) for a, b in evs]
         total = sum(ms) / 1e3
-        if dist:
-            t = torch.tensor([total], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total = float(t.item())
-        return total, ms, wall
+        return max_over_ranks(total, dist, dev), ms, wall
 
     # counters of one frame (deterministic: jitter off) for the roofline
     ctx.render_device(scene, ptrs, precision=mb.PREC_FP32_FIX)
@@ -378,8 +387,8 @@ def main() -> int:
     st64 = ctx.stats()
     total64, ms64, _ = timed_frames(mb.PREC_FP64, args.fp64_steps, 1)
 
-    value = world * npx * args.steps / total32 / 1e6
-    value64 = world * npx * args.fp64_steps / total64 / 1e6
+    value = whole_job_rate(world, npx, args.steps, total32) / 1e6
+    value64 = whole_job_rate(world, npx, args.fp64_steps, total64) / 1e6
 
     # parity of the two policies at full size (hit mask, PSNR of the float image)
     from tests import metrics
