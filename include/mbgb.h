@@ -45,9 +45,11 @@ typedef enum mbgb_status {
 
 /* enumFractalFormula (src/fractal.h:25-64), values that this build evaluates on the device. */
 enum {
-  MBGB_FORMULA_TRIG_DE = 1,
+  MBGB_FORMULA_TRIG_DE = 1,      /* Mandelbulb with a derivative vector, src/fractal.cpp:189-209 */
   MBGB_FORMULA_TRIG_OPTIM = 2,   /* Mandelbulb, src/fractal.cpp:211-225 */
-  MBGB_FORMULA_TGLAD = 8         /* Mandelbox, src/fractal.cpp:409-529 */
+  MBGB_FORMULA_MENGER = 7,       /* Menger sponge, src/fractal.cpp:369-407 */
+  MBGB_FORMULA_TGLAD = 8,        /* Mandelbox, src/fractal.cpp:409-529 */
+  MBGB_FORMULA_MBOX_VARY4D = 18  /* Mandelbox with varying scale, 4D, src/fractal.cpp:887-915 */
 };
 
 /* enumPerspectiveType (src/common_math.h:39-42) */

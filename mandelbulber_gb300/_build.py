@@ -45,6 +45,10 @@ def _units(cuda: str):
     yield "noalloc.cu", common_cu
     yield "wave_f64.cu", common_cu + ["--fmad=false"]
     yield "wave_f32.cu", common_cu
+    yield "wave_more_f64.cu", common_cu + ["--fmad=false"]
+    yield "wave_more_f32.cu", common_cu
+    yield "render_more_f64.cu", common_cu + ["--fmad=false"]
+    yield "render_more_f32.cu", common_cu
     yield "post.cu", common_cu + ["--fmad=false"]
     yield "capi.cpp", common_cpp
     yield "settings.cpp", common_cpp

@@ -151,6 +151,11 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   f.amin = (T)s.amin; f.amax = (T)s.amax;
   f.bmin = (T)s.bmin; f.bmax = (T)s.bmax;
   f.cmin = (T)s.cmin; f.cmax = (T)s.cmax;
+  f.mbVaryFold = (T)s.mboxVaryFold;
+  f.mbVaryMinR = (T)s.mboxVaryMinR;
+  f.mbVaryScaleVary = (T)s.mboxVaryScaleVary;
+  f.mbVaryWadd = (T)s.mboxVaryWadd;
+  f.mbVaryRPower = (T)s.mboxVaryRPower;
 }
 
 // MainThread's per-frame preparation (src/Render3D.cpp:213-344) into a kernel parameter block.
@@ -391,7 +396,7 @@ extern "C" const char *mbgb_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" mbgb_status mbgb_scene_supported(const mbgb_scene *s) {
   if (!s) return set_error(MBGB_ERR_BAD_PARAM, "NULL scene");
-  if (s->formula != MBGB_FORMULA_TRIG_OPTIM && s->formula != MBGB_FORMULA_TGLAD)
+  if (s->formula != MBGB_FORMULA_TRIG_OPTIM && s->formula != MBGB_FORMULA_TGLAD && !runtime_formula(s->formula))
     return set_error(MBGB_ERR_UNSUPPORTED, "formula " + std::to_string(s->formula) + " is not built on the device");
   if (!s->analitycDE) return set_error(MBGB_ERR_UNSUPPORTED, "delta-DE mode is not built on the device");
   if (s->ifsFoldingMode) return set_error(MBGB_ERR_UNSUPPORTED, "IFS folding mode");
@@ -525,6 +530,11 @@ static void strip_camera(ParamsT<T> &p) {
   p.aoVec = nullptr;
 }
 
+// Formulas whose main parameter is the Mandelbox scale (the device's scale_formula).
+static bool scale_formula_host(int formula) {
+  return formula == 8 || formula == 17 || formula == 18 || formula == 37;
+}
+
 // Fractal fields the scene's formula never reads cleared. Keyframe splines leave
 // last-bit differences in parameters that stay constant over an animation
 // (2 v - 5 v + 4 v - v is not exactly 0 in doubles), and those in unused fields
@@ -548,7 +558,7 @@ static void clear_unused(FractalT<T> &f) {
 // The formula's main parameter (power / Mandelbox scale) travels per frame (FrameCam::fparam).
 template <typename T>
 static void clear_fparam(FractalT<T> &f) {
-  if (f.formula == MBGB_FORMULA_TGLAD) f.mbScale = T(0);
+  if (scale_formula_host(f.formula)) f.mbScale = T(0);
   else f.power = T(0);
 }
 
@@ -607,8 +617,8 @@ static void fill_cam(const mbgb_scene &s, const mbgb_image &img, const mbgb_opts
   cam.resolution_d = p.resolution_d;
   cam.persp_d = p.persp_d;
   for (int k = 0; k < 3; k++) cam.lightVect[k] = p.lightVect[k];
-  cam.fparam = (T)(s.formula == MBGB_FORMULA_TGLAD ? s.mboxScale : s.power);
-  cam.fparam_d = s.formula == MBGB_FORMULA_TGLAD ? s.mboxScale : s.power;
+  cam.fparam = (T)(scale_formula_host(s.formula) ? s.mboxScale : s.power);
+  cam.fparam_d = scale_formula_host(s.formula) ? s.mboxScale : s.power;
   cam.image_float = img.image_float;
   cam.zbuffer = img.zbuffer;
   cam.alpha = img.alpha;
@@ -627,6 +637,8 @@ static bool need_volumetric(const mbgb_scene &s) {
 // formula 2, or formula 8 without rotations, offset or pre-folds, and the analytic
 // estimate without limits, iteration threshold or interior mode.
 static mbgb_status level_set_supported(const mbgb_scene &s) {
+  if (s.formula != MBGB_FORMULA_TRIG_OPTIM && s.formula != MBGB_FORMULA_TGLAD)
+    return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: formulas 2 and 8 only");
   if (s.tgladFoldingMode || s.sphericalFoldingMode)
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: pre-folds");
   if (s.formula == MBGB_FORMULA_TGLAD &&
@@ -1567,7 +1579,8 @@ extern "C" mbgb_status mbgb_distance_device(mbgb_context *c, const mbgb_scene *s
   if (!c || !scene || (n > 0 && (!points || !detail || !dist || !iters || !max_iter)))
     return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
   if (n < 0) return set_error(MBGB_ERR_BAD_PARAM, "negative point count");
-  if (scene->formula != MBGB_FORMULA_TRIG_OPTIM && scene->formula != MBGB_FORMULA_TGLAD)
+  if (scene->formula != MBGB_FORMULA_TRIG_OPTIM && scene->formula != MBGB_FORMULA_TGLAD &&
+      !runtime_formula(scene->formula))
     return set_error(MBGB_ERR_UNSUPPORTED, "formula not built on the device");
   if (n == 0) return MBGB_OK;
   std::lock_guard<std::mutex> lk(c->mu);

@@ -19,6 +19,10 @@ constexpr int kOverflowThreads = 128;   // threads of the pass that re-renders r
 constexpr int kMaxAOVectors = 10000;    // sVectorsAround table (src/Render3D.cpp:272)
 constexpr int kTileW = 8, kTileH = 4;   // one warp renders an 8x4 pixel tile
 
+// Formulas the kernels select at run time (FORMULA 0 of compute()): trig_DE, menger_sponge,
+// mandelboxVaryScale4D. trig_optim (2) and tglad (8) have instantiations of their own.
+inline bool runtime_formula(int formula) { return formula == 1 || formula == 7 || formula == 18; }
+
 // Fractal / distance-estimator parameters (sFractal, src/fractal.h:255-293).
 template <typename T>
 struct FractalT {
@@ -41,6 +45,7 @@ struct FractalT {
   T mbRot[2][3][9];
   T mbRotInv[2][3][9];
   T amin, amax, bmin, bmax, cmin, cmax;
+  T mbVaryFold, mbVaryMinR, mbVaryScaleVary, mbVaryWadd, mbVaryRPower;   // mandelboxVaryScale4D
 };
 
 // Everything MainThread and the shaders read (sParamRender, src/fractparams.h:67-146).

@@ -115,18 +115,27 @@ struct Counters {
   unsigned long long missed;  // Missed_DE_counter
 };
 
-// The formula's main parameter: power (formula 2) or Mandelbox scale (formula 8).
+// Formulas whose main parameter is the Mandelbox scale (tglad 8, smoothMandelbox 17,
+// mandelboxVaryScale4D 18, generalizedFoldBox 37); the others use the power.
+__host__ __device__ __forceinline__ bool scale_formula(const int formula) {
+  return formula == 8 || formula == 17 || formula == 18 || formula == 37;
+}
+
+// The formula's main parameter: the power or the Mandelbox scale.
 template <typename T>
 __host__ __device__ __forceinline__ T fparam_of(const FractalT<T> &f) {
-  return f.formula == 8 ? f.mbScale : f.power;
+  return scale_formula(f.formula) ? f.mbScale : f.power;
 }
 
 // ---------------------------------------------------------------------------
 // Compute<Mode> (src/fractal.cpp:40-1241) for the formulas this build carries.
 // MODE 0 = normal (returns the distance estimate), MODE 1 = colouring.
+// FORMULA 2 (trig_optim) and 8 (tglad) are compiled as such; FORMULA 0 selects the
+// formula at run time from f.formula: trig_DE (1), menger_sponge (7) and
+// mandelboxVaryScale4D (18).
 // ---------------------------------------------------------------------------
-// `fparam` is the formula's main parameter: the power of formula 2, the Mandelbox scale
-// of formula 8 (a frame of a batch may carry its own; see fparam_of).
+// `fparam` is the formula's main parameter: the power, or the Mandelbox scale of the
+// scale formulas (a frame of a batch may carry its own; see fparam_of).
 template <typename T, int FORMULA, int MODE>
 __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N, int &Lout, Counters &cnt,
                                      const T fparam) {
@@ -147,6 +156,11 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
   }
   T r = orbit_length(z);
   T minv = (sizeof(T) == 8) ? T(1e200) : T(__int_as_float(0x7f800000));
+  // state of the run-time formulas: trig_DE's derivative vector in polar form, the 4th
+  // coordinate and the varying scale of mandelboxVaryScale4D
+  const int form = FORMULA == 0 ? f.formula : FORMULA;
+  V3<T> dz{T(1), T(0), T(0)};
+  T th_dz = T(0), ph_dz = T(0), w = T(0), scaleV = scale;
   int L;
   for (L = 0; L < N; L++) {
     if (f.tgladFoldingMode) {  // src/fractal.cpp:124-156
@@ -231,9 +245,82 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       z = z * scale + constant;
       tgladDE = tgladDE * m_fabs(scale) + T(1);
       r = orbit_length(z);
+    } else if (FORMULA == 0) {
+      if (form == 1) {
+        // trig_DE (src/fractal.cpp:189-209): angles atan2(y, x) and -atan2(z, rho); in normal
+        // mode the derivative vector dz is carried in the same polar form
+        const T r1 = m_pow(r, p - T(1));
+        const T r2 = r1 * r;
+        const T th = m_atan2(z.y, z.x);
+        const T ph = -m_atan2(z.z, m_sqrt(z.x * z.x + z.y * z.y));
+        if (MODE == 0) {
+          const T p_r1_rdz = p * r1 * r_dz;
+          const T ph_phdz = (p - T(1)) * ph + ph_dz;
+          const T th_thdz = (p - T(1)) * th + th_dz;
+          T sb, cb, sa, ca;
+          m_sincos(ph_phdz, &sb, &cb);
+          m_sincos(th_thdz, &sa, &ca);
+          const V3<T> rot{cb * ca, cb * sa, sb};
+          dz = V3<T>{rot.x * p_r1_rdz + T(1), rot.y * p_r1_rdz + T(0), rot.z * p_r1_rdz + T(0)};
+          r_dz = length3(dz);
+          th_dz = m_atan2(dz.y, dz.x);
+          ph_dz = -m_atan2(dz.z, m_sqrt(dz.x * dz.x + dz.y * dz.y));
+        }
+        T sb, cb, sa, ca;
+        m_sincos(p * ph, &sb, &cb);
+        m_sincos(p * th, &sa, &ca);
+        z = V3<T>{cb * ca, cb * sa, sb} * r2 + constant;
+        r = orbit_length(z);
+      } else if (form == 7) {
+        // menger_sponge (src/fractal.cpp:369-407): fold into the first octant sorted x >= y >= z
+        z.x = m_fabs(z.x);
+        z.y = m_fabs(z.y);
+        z.z = m_fabs(z.z);
+        T t;
+        if (z.x - z.y < T(0)) { t = z.y; z.y = z.x; z.x = t; }
+        if (z.x - z.z < T(0)) { t = z.z; z.z = z.x; z.x = t; }
+        if (z.y - z.z < T(0)) { t = z.z; z.z = z.y; z.y = t; }
+        if (MODE == 1) {
+          const T len = orbit_length(z);
+          if (len < minv) minv = len;
+        }
+        z = z * T(3);
+        z.x -= T(2);
+        z.y -= T(2);
+        if (z.z > T(1)) z.z -= T(2);
+        r = orbit_length(z);
+        tgladDE *= T(3);
+      } else if (form == 18) {
+        // mandelboxVaryScale4D (src/fractal.cpp:887-915)
+        scaleV = scaleV + f.mbVaryScaleVary * (m_fabs(scaleV) - T(1));
+        const V3<T> oldz = z;
+        const T fo = f.mbVaryFold;
+        z.x = m_fabs(z.x + fo) - m_fabs(z.x - fo) - z.x;
+        z.y = m_fabs(z.y + fo) - m_fabs(z.y - fo) - z.y;
+        z.z = m_fabs(z.z + fo) - m_fabs(z.z - fo) - z.z;
+        w = m_fabs(w + fo) - m_fabs(w - fo) - w;
+        if (z.x != oldz.x) tgladColor += f.mbColX;
+        if (z.y != oldz.y) tgladColor += f.mbColY;
+        if (z.z != oldz.z) tgladColor += f.mbColZ;
+        const T rr = m_pow(z.x * z.x + z.y * z.y + z.z * z.z + w * w, f.mbVaryRPower);
+        T m = scaleV;
+        if (rr < f.mbVaryMinR * f.mbVaryMinR) {
+          m = scaleV / (f.mbVaryMinR * f.mbVaryMinR);
+          tgladColor += f.mbColSp1;
+        } else if (rr < T(1)) {
+          m = scaleV / rr;
+          tgladColor += f.mbColSp2;
+        }
+        z = z * m + constant;
+        w = w * m + f.mbVaryWadd;
+        tgladDE = tgladDE * m_fabs(m) + T(1);
+        r = m_sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
+      }
     }
     // iteration terminate conditions (src/fractal.cpp:1133-1190)
-    if (FORMULA == 8) {
+    if (form == 7) {
+      if (r > T(1000)) { distance = (r - T(2)) / tgladDE; break; }
+    } else if (FORMULA == 8 || form == 18) {
       if (r > T(1024)) { distance = r / m_fabs(tgladDE); break; }
     } else {
       if (MODE == 0) {
@@ -252,7 +339,8 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
     if (L == N) distance = T(0);
     return distance;
   } else {
-    if (FORMULA == 8) return tgladColor * T(100) + orbit_length(z) * f.mbColR;
+    if (FORMULA == 8 || form == 18) return tgladColor * T(100) + orbit_length(z) * f.mbColR;
+    if (form == 7) return minv * T(1000);
     return distance * T(5000);
   }
 }

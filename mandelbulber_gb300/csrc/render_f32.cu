@@ -9,7 +9,9 @@ cudaError_t launch_render_f32(int formula, const ParamsT<float> &p, const Fracta
   switch (formula) {
     case 2: dev::render_kernel<float, 2><<<grid, block, 0, s>>>(p, fd, io); break;
     case 8: dev::render_kernel<float, 8><<<grid, block, 0, s>>>(p, fd, io); break;
-    default: return cudaErrorInvalidValue;
+    default:
+      if (runtime_formula(formula)) return launch_render_f32_runtime(p, fd, io, grid, block, s);
+      return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
@@ -23,7 +25,9 @@ cudaError_t launch_distance_f32(int formula, const FractalT<float> &f, const dou
   switch (formula) {
     case 2: dev::distance_kernel<float, 2><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
     case 8: dev::distance_kernel<float, 8><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
-    default: return cudaErrorInvalidValue;
+    default:
+      if (runtime_formula(formula)) return launch_distance_f32_runtime(f, points, detail, n, dist, iters, max_iter, counters, s);
+      return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
@@ -31,7 +35,8 @@ cudaError_t launch_distance_f32(int formula, const FractalT<float> &f, const dou
 int occupancy_render_f32(int formula, int block) {
   int n = 0;
   if (formula == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::render_kernel<float, 2>, block, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::render_kernel<float, 8>, block, 0);
+  else if (formula == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::render_kernel<float, 8>, block, 0);
+  else n = occupancy_render_f32_runtime(block);
   return n;
 }
 

@@ -9,7 +9,9 @@ cudaError_t launch_render_f64(int formula, const ParamsT<double> &p, const Fract
   switch (formula) {
     case 2: dev::render_kernel<double, 2><<<grid, block, 0, s>>>(p, fd, io); break;
     case 8: dev::render_kernel<double, 8><<<grid, block, 0, s>>>(p, fd, io); break;
-    default: return cudaErrorInvalidValue;
+    default:
+      if (runtime_formula(formula)) return launch_render_f64_runtime(p, fd, io, grid, block, s);
+      return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
@@ -23,7 +25,9 @@ cudaError_t launch_distance_f64(int formula, const FractalT<double> &f, const do
   switch (formula) {
     case 2: dev::distance_kernel<double, 2><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
     case 8: dev::distance_kernel<double, 8><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
-    default: return cudaErrorInvalidValue;
+    default:
+      if (runtime_formula(formula)) return launch_distance_f64_runtime(f, points, detail, n, dist, iters, max_iter, counters, s);
+      return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
@@ -31,7 +35,8 @@ cudaError_t launch_distance_f64(int formula, const FractalT<double> &f, const do
 int occupancy_render_f64(int formula, int block) {
   int n = 0;
   if (formula == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::render_kernel<double, 2>, block, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::render_kernel<double, 8>, block, 0);
+  else if (formula == 8) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::render_kernel<double, 8>, block, 0);
+  else n = occupancy_render_f64_runtime(block);
   return n;
 }
 

@@ -1,51 +1,20 @@
-// Instantiation of the wavefront kernels for T = double.
-#include "grad_core.cuh"
-#include "wave_core.cuh"
-#include "wave_launch.h"
+// Instantiation of the wavefront kernels for T = double, formulas 2 and 8 (the other
+// formulas are in wave_more_f64.cu).
+#include "wave_stages.cuh"
 
 namespace mbgb {
 
-template <int F, bool FAST>
-static cudaError_t run_stages_f64(const WaveLaunch<double> &L, cudaStream_t s) {
-  auto mark = [&](int k) {
-    if (L.ev[0]) cudaEventRecord(L.ev[k], s);
-  };
-  mark(0);
-  dev::primary_kernel<double, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb, L.cams, L.ncams);
-  if (L.overflow)
-    dev::primary_kernel<double, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb, L.cams, L.ncams);
-  mark(1);
-  mark(2);
-  if (L.wb.exact_hit)
-    dev::level_set_kernel<double, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
-  mark(3);
-  dev::secondary_kernel<double, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
-  mark(4);
-  dev::compose_kernel<double, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
-  mark(5);
-  if (L.gcams)
-    dev::grad_kernel<double, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 5), L.wb, L.cams, L.gcams,
-                                                                   L.ncams);
-  mark(6);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_wave_f64(const WaveLaunch<double> &L, cudaStream_t s) {
-  if (L.p.f.formula == 2) return L.fast ? run_stages_f64<2, false>(L, s) : run_stages_f64<2, false>(L, s);
-  if (L.p.f.formula == 8) return L.fast ? run_stages_f64<8, false>(L, s) : run_stages_f64<8, false>(L, s);
+  if (L.p.f.formula == 2) return L.fast ? run_stages<double, 2, false>(L, s) : run_stages<double, 2, false>(L, s);
+  if (L.p.f.formula == 8) return L.fast ? run_stages<double, 8, false>(L, s) : run_stages<double, 8, false>(L, s);
+  if (runtime_formula(L.p.f.formula)) return launch_wave_f64_runtime(L, s);
   return cudaErrorInvalidValue;
 }
 
 int occupancy_wave_f64(int formula, int block, int which) {
-  int n = 0;
-  if (which == 0) {
-    if (formula == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<double, 2, false>, block, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<double, 8, false>, block, 0);
-  } else {
-    if (formula == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<double, 2, false>, block, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<double, 8, false>, block, 0);
-  }
-  return n;
+  if (formula == 2) return stage_occupancy<double, 2, false>(block, which);
+  if (formula == 8) return stage_occupancy<double, 8, false>(block, which);
+  return occupancy_wave_f64_runtime(block, which);
 }
 
 }  // namespace mbgb

@@ -94,5 +94,10 @@ cudaError_t launch_wave_f64(const WaveLaunch<double> &L, cudaStream_t s);
 cudaError_t launch_wave_f32(const WaveLaunch<float> &L, cudaStream_t s);
 int occupancy_wave_f64(int formula, int block, int which);
 int occupancy_wave_f32(int formula, int block, int which);
+// the formulas compute() selects at run time (runtime_formula)
+cudaError_t launch_wave_f64_runtime(const WaveLaunch<double> &L, cudaStream_t s);
+cudaError_t launch_wave_f32_runtime(const WaveLaunch<float> &L, cudaStream_t s);
+int occupancy_wave_f64_runtime(int block, int which);
+int occupancy_wave_f32_runtime(int block, int which);
 
 }  // namespace mbgb

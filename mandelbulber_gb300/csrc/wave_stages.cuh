@@ -1,0 +1,46 @@
+// The launch sequence of the wavefront stages (wave_core.cuh, grad_core.cuh) for one
+// launch group, shared by the translation units that instantiate it per formula.
+#pragma once
+
+#include "grad_core.cuh"
+#include "wave_core.cuh"
+#include "wave_launch.h"
+
+namespace mbgb {
+
+template <typename T, int F, bool FAST>
+cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
+  auto mark = [&](int k) {
+    if (L.ev[0]) cudaEventRecord(L.ev[k], s);
+  };
+  mark(0);
+  dev::primary_kernel<T, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb, L.cams, L.ncams);
+  if (L.overflow)
+    dev::primary_kernel<T, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb, L.cams, L.ncams);
+  mark(1);
+  if constexpr (sizeof(T) == 4)
+    dev::polish_kernel<F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), L.wb, L.cams, L.ncams);
+  mark(2);
+  if (L.wb.exact_hit)
+    dev::level_set_kernel<T, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
+  mark(3);
+  dev::secondary_kernel<T, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
+  mark(4);
+  dev::compose_kernel<T, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
+  mark(5);
+  if (L.gcams)
+    dev::grad_kernel<T, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 5), L.wb, L.cams, L.gcams,
+                                                              L.ncams);
+  mark(6);
+  return cudaGetLastError();
+}
+
+template <typename T, int F, bool FAST>
+int stage_occupancy(int block, int which) {
+  int n = 0;
+  if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<T, F, FAST>, block, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<T, F, FAST>, block, 0);
+  return n;
+}
+
+}  // namespace mbgb

@@ -102,6 +102,12 @@ MANDELBOX_1080P = {
 
 WORKLOADS = {"mandelbulb_640x480": MANDELBULB_640x480, "mandelbox_1080p": MANDELBOX_1080P}
 
+# mandelboxVaryScale4D's own parameters at the values of the reference's default settings
+# (src/settings.cpp:413-417); the
+# other formulas ignore them, so the base scenes keep them at zero
+VARY4D = {"formula": 18, "mandelbox_vary_scale_vary": 0.1, "mandelbox_vary_fold": 1,
+          "mandelbox_vary_minr": 0.5, "mandelbox_vary_rpower": 1, "mandelbox_vary_wadd": 0}
+
 
 def look_angles(d) -> tuple[float, float]:
     """Camera angles (degrees) that look along direction d.

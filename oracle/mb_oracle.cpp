@@ -9,7 +9,9 @@
 // fractal.cpp / shaders.cpp (oracle/_ref).
 //
 // Function-by-function sources (reference paths):
-//   compute_normal / compute_colour   Compute<normal|colouring>  src/fractal.cpp:40-1241
+//   compute_normal / compute_colour   Compute<normal|colouring>  src/fractal.cpp:40-1241 (formulas
+//                                     trig_DE 1, trig_optim 2, menger_sponge 7, tglad 8,
+//                                     mandelboxVaryScale4D 18)
 //   calculate_distance                CalculateDistance          src/fractal.cpp:1245-1448
 //   ray_marching                      RayMarching                src/Render3D.cpp:79-199
 //   calculate_normals                 CalculateNormals           src/shaders.cpp:675-757
@@ -31,6 +33,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../include/mbgb.h"
@@ -84,8 +87,12 @@ double compute(const Calc &c, Vec z, bool colour, int *Lout) {
   const double mR2 = s.mboxFoldingSphericalMin * s.mboxFoldingSphericalMin;
   const double f1 = fR2 / mR2;
   double tDE = 1.0, tCol = 1.0;
-  const double scale = s.mboxScale;
-  const bool box = s.formula == MBGB_FORMULA_TGLAD;
+  double scale = s.mboxScale;
+  const bool box = s.formula == MBGB_FORMULA_TGLAD || s.formula == MBGB_FORMULA_MBOX_VARY4D;
+  const bool menger = s.formula == MBGB_FORMULA_MENGER;
+  // trig_DE keeps its derivative as a vector in polar form; the 4D box keeps w
+  Vec dz{1.0, 0.0, 0.0};
+  double thdz = 0.0, phdz = 0.0, w = 0.0;
   Vec cst = s.juliaMode ? Vec{s.julia[0], s.julia[1], s.julia[2]} : mul(z, s.constantFactor);
   double r = len(z);
   double minv = 1e200;
@@ -117,6 +124,57 @@ double compute(const Calc &c, Vec z, bool colour, int *Lout) {
       rp *= r;
       z = add(mul(Vec{cth * cos(ph), cth * sin(ph), sin(th)}, rp), cst);
       r = len(z);
+    } else if (s.formula == MBGB_FORMULA_TRIG_DE) {
+      const double r1 = pow(r, p - 1.0);
+      const double r2 = r1 * r;
+      const double th = atan2(z.y, z.x);
+      const double ph = -atan2(z.z, sqrt(z.x * z.x + z.y * z.y));
+      if (!colour) {
+        const double k = p * r1 * r_dz;
+        const double a = (p - 1.0) * th + thdz;
+        const double b = (p - 1.0) * ph + phdz;
+        dz = Vec{cos(b) * cos(a) * k + 1.0, cos(b) * sin(a) * k + 0.0, sin(b) * k + 0.0};
+        r_dz = len(dz);
+        thdz = atan2(dz.y, dz.x);
+        phdz = -atan2(dz.z, sqrt(dz.x * dz.x + dz.y * dz.y));
+      }
+      z = add(mul(Vec{cos(p * ph) * cos(p * th), cos(p * ph) * sin(p * th), sin(p * ph)}, r2), cst);
+      r = len(z);
+    } else if (menger) {
+      z = Vec{fabs(z.x), fabs(z.y), fabs(z.z)};
+      if (z.x - z.y < 0) std::swap(z.x, z.y);
+      if (z.x - z.z < 0) std::swap(z.x, z.z);
+      if (z.y - z.z < 0) std::swap(z.y, z.z);
+      if (colour) {
+        const double l = len(z);
+        if (l < minv) minv = l;
+      }
+      z = mul(z, 3.0);
+      z.x -= 2.0;
+      z.y -= 2.0;
+      if (z.z > 1.0) z.z -= 2.0;
+      r = len(z);
+      tDE *= 3.0;
+    } else if (s.formula == MBGB_FORMULA_MBOX_VARY4D) {
+      scale = scale + s.mboxVaryScaleVary * (fabs(scale) - 1.0);
+      const Vec o = z;
+      const double fo = s.mboxVaryFold;
+      z.x = fabs(z.x + fo) - fabs(z.x - fo) - z.x;
+      z.y = fabs(z.y + fo) - fabs(z.y - fo) - z.y;
+      z.z = fabs(z.z + fo) - fabs(z.z - fo) - z.z;
+      w = fabs(w + fo) - fabs(w - fo) - w;
+      if (z.x != o.x) tCol += s.mboxColorFactorX;
+      if (z.y != o.y) tCol += s.mboxColorFactorY;
+      if (z.z != o.z) tCol += s.mboxColorFactorZ;
+      const double rr = pow(z.x * z.x + z.y * z.y + z.z * z.z + w * w, s.mboxVaryRPower);
+      const double mr2 = s.mboxVaryMinR * s.mboxVaryMinR;
+      double m = scale;
+      if (rr < mr2) { m = scale / mr2; tCol += s.mboxColorFactorSp1; }
+      else if (rr < 1.0) { m = scale / rr; tCol += s.mboxColorFactorSp2; }
+      z = add(mul(z, m), cst);
+      w = w * m + s.mboxVaryWadd;
+      tDE = tDE * fabs(m) + 1.0;
+      r = sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
     } else if (box) {
       const double fl = s.mboxFoldingLimit, fv = s.mboxFoldingValue;
       if (s.mboxRotationsEnabled) {
@@ -158,7 +216,9 @@ double compute(const Calc &c, Vec z, bool colour, int *Lout) {
       tDE = tDE * fabs(scale) + 1.0;
       r = len(z);
     }
-    if (box) {
+    if (menger) {
+      if (r > 1000) { distance = (r - 2.0) / tDE; break; }
+    } else if (box) {
       if (r > 1024) { distance = r / fabs(tDE); break; }
     } else if (!colour) {
       if (r > 1e2) { distance = 0.5 * r * log(r) / r_dz; break; }
@@ -176,6 +236,7 @@ double compute(const Calc &c, Vec z, bool colour, int *Lout) {
     return distance;
   }
   if (box) return tCol * 100.0 + len(z) * s.mboxColorFactorR;
+  if (menger) return minv * 1000.0;
   return distance * 5000.0;
 }
 

@@ -114,6 +114,8 @@ sParamRender *make_params(const mbgb_scene &s) {
   m.scale = s.mboxScale; m.foldingLimit = s.mboxFoldingLimit; m.foldingValue = s.mboxFoldingValue;
   m.foldingSphericalMin = s.mboxFoldingSphericalMin; m.foldingSphericalFixed = s.mboxFoldingSphericalFixed;
   m.offset = v3(s.mboxOffset);
+  m.vary4D.fold = s.mboxVaryFold; m.vary4D.minR = s.mboxVaryMinR; m.vary4D.scaleVary = s.mboxVaryScaleVary;
+  m.vary4D.wadd = s.mboxVaryWadd; m.vary4D.rPower = s.mboxVaryRPower;
   f.mandelbox.rotationsEnabled = s.mboxRotationsEnabled;
   // RecalculateIFSParams, Mandelbox part (src/callbacks.cpp:1549-1556)
   f.mandelbox.mainRot.SetRotation(m.rotationMain);

@@ -16,6 +16,7 @@ the tests rebuild the exact input without the reference tree.
 
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py post     # the post-processing fixtures only
+    python tests/golden/make_golden.py formulas # the run-time formulas' fixtures only
 """
 from __future__ import annotations
 
@@ -75,6 +76,29 @@ CASES = {
                                        {"tglad_folding_mode": 1, "spherical_folding_mode": 1,
                                         "iteration_threshold_mode": 1, "N": 60}),
 }
+
+# formulas selected at run time on the device: trig_DE (1), menger_sponge (7),
+# mandelboxVaryScale4D (18)
+FORMULA_CASES = {
+    "trigde_40x32": ("mandelbulb_640x480", 40, 32, {"formula": 1}),
+    "trigde_power6_rotated": ("mandelbulb_640x480", 40, 32,
+                              {"formula": 1, "power": 6, "angle_alfa": 30, "angle_beta": 19,
+                               "view_point_x": 1.75, "view_point_y": -3.0, "view_point_z": -1.2}),
+    "menger_48x32": ("mandelbulb_640x480", 48, 32, {"formula": 7, "N": 50, "view_point_x": 0.9,
+                                                    "view_point_z": 0.6, "angle_alfa": -14, "angle_beta": -9}),
+    "menger_glow_fastao": ("mandelbulb_640x480", 40, 32,
+                           {"formula": 7, "N": 50, "glow_intensity": 1, "ambient_occlusion_enabled": 1,
+                            "fast_ambient_occlusion_mode": 1, "ambient_occlusion_quality": 3}),
+    "vary4d_48x32": ("mandelbox_1080p", 48, 32, {**W.VARY4D, "ambient_occlusion_enabled": 0,
+                                                 "mandelbox_scale": 2.0}),
+    "vary4d_rpower_wadd": ("mandelbox_1080p", 48, 32,
+                           {**W.VARY4D, "ambient_occlusion_enabled": 0, "mandelbox_scale": 2.0,
+                            "view_point_y": -17.0, "angle_alfa": 20, "mandelbox_vary_rpower": 0.8, "mandelbox_vary_wadd": 0.3,
+                            "mandelbox_vary_scale_vary": 0.05, "volumetric_fog_density": 0}),
+}
+FORMULA_DE = (("trigde", "mandelbulb_640x480", {"formula": 1}, 1.6),
+              ("menger", "mandelbulb_640x480", {"formula": 7, "N": 50}, 1.5),
+              ("vary4d", "mandelbox_1080p", {**W.VARY4D, "mandelbox_scale": 2.0}, 4.0))
 
 
 def build_ref() -> ctypes.CDLL:
@@ -150,6 +174,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "catmull_rom.npz"), keys=keys, frames_per_key=fpk, out=out)
     manifest["catmull_rom.npz"] = {"keys": [n_keys, size], "frames_per_key": fpk}
     post_goldens(manifest)
+    formula_goldens(manifest)
     with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
@@ -190,11 +215,56 @@ def post_goldens(manifest: dict):
         print(case, "ssao changed", np.mean(img16 != compiled))
 
 
+def formula_goldens(manifest: dict):
+    """DE and render fixtures of the run-time formulas from the reference's own code."""
+    lib = build_ref()
+    for name, wl, extra, half in FORMULA_DE:
+        rng = np.random.default_rng({"trigde": 11, "menger": 12, "vary4d": 13}[name])
+        keys = dict(W.WORKLOADS[wl])
+        keys["image_width"], keys["image_height"] = 64, 48
+        keys["perspective"] = W.fov_persp(64, 48)
+        keys.update(extra)
+        sc = W.make_scene(keys)
+        pts = np.ascontiguousarray(rng.uniform(-half, half, (2000, 3)))
+        n = len(pts)
+        detail = np.ascontiguousarray(10.0 ** rng.uniform(-6, -2, n))
+        dist = np.zeros(n)
+        iters = np.zeros(n, np.int32)
+        mi = np.zeros(n, np.uint8)
+        lib.ref_distance(ctypes.byref(sc), ptr(pts), ptr(detail), ctypes.c_long(n), ptr(dist), ptr(iters), ptr(mi))
+        colour = np.zeros(n)
+        lib.ref_colour_value(ctypes.byref(sc), ptr(pts), ctypes.c_long(n), ptr(colour))
+        out = os.path.join(HERE, f"de_{name}.npz")
+        np.savez_compressed(out, scene=np.frombuffer(mb.scene_bytes(sc), np.uint8), points=pts, detail=detail,
+                            dist=dist, iters=iters, max_iter=mi, colour=colour)
+        manifest[os.path.basename(out)] = {"workload": wl, "points": n, "keys": extra}
+    render_cases(lib, FORMULA_CASES, manifest)
+
+
+def render_cases(lib, cases: dict, manifest: dict):
+    for case, (wl, w, h, extra) in cases.items():
+        keys = dict(W.WORKLOADS[wl])
+        keys["image_width"], keys["image_height"] = w, h
+        keys["perspective"] = W.fov_persp(w, h)
+        keys.update(extra)
+        sc = W.make_scene(keys)
+        img = mb.CImage.empty(w, h)
+        lib.ref_render(ctypes.byref(sc), 0, h, 0, ctypes.byref(img.as_c()))
+        out = os.path.join(HERE, f"render_{case}.npz")
+        np.savez_compressed(out, scene=np.frombuffer(mb.scene_bytes(sc), np.uint8),
+                            keys=np.array(json.dumps(keys)), image_float=img.image_float, zbuffer=img.zbuffer,
+                            alpha=img.alpha, opacity=img.opacity, colour=img.colour, hit=img.hit, iters=img.iters,
+                            depth=img.depth)
+        manifest[os.path.basename(out)] = {"workload": wl, "size": [w, h], "keys": extra,
+                                           "hit_fraction": float(img.hit.mean())}
+        print(case, "hit", img.hit.mean())
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["post"]:
+    if sys.argv[1:] in (["post"], ["formulas"]):
         with open(os.path.join(HERE, "MANIFEST.json")) as f:
             manifest = json.load(f)
-        post_goldens(manifest)
+        (post_goldens if sys.argv[1] == "post" else formula_goldens)(manifest)
         with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
             json.dump(manifest, f, indent=1, sort_keys=True)
     else:

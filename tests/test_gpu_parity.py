@@ -70,7 +70,22 @@ def test_distance_fp64_mandelbulb_close(gpu_ctx):
     assert np.percentile(rel, 99) < 1e-9, np.percentile(rel, 99)
 
 
-@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox"])
+@pytest.mark.parametrize("formula", ["trigde", "menger", "vary4d"])
+def test_distance_fp64_runtime_formulas(gpu_ctx, formula):
+    """trig_DE, menger_sponge and mandelboxVaryScale4D (formulas 1, 7, 18) against the
+    reference's own distances: the same iteration counts on >= 98 % of the points and
+    distances within 1e-9 relative (99th percentile) there."""
+    z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
+    sc = mb.scene_from_bytes(z["scene"].tobytes())
+    d, it, mi = _device_distance(gpu_ctx, sc, z["points"], z["detail"], mb.PREC_FP64)
+    agree = it == z["iters"]
+    assert agree.mean() >= 0.98, agree.mean()
+    rel = np.abs(d[agree] - z["dist"][agree]) / np.maximum(np.abs(z["dist"][agree]), 1e-300)
+    assert np.percentile(rel, 99) < 1e-9, np.percentile(rel, 99)
+    np.testing.assert_array_equal(mi[agree], z["max_iter"][agree])
+
+
+@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox", "trigde", "menger", "vary4d"])
 def test_distance_fp32_close(gpu_ctx, formula):
     z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
     sc = mb.scene_from_bytes(z["scene"].tobytes())
@@ -114,6 +129,30 @@ def test_render_fp32_fix_against_oracle(gpu_ctx, oracle, name, size, engine):
     img = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, engine=engine)
     m = metrics.compare(img, ref)
     print(name, m)
+    assert m["hit_mismatch"] <= 0.001, m
+    assert m["psnr_float"] >= 45.0, m
+
+
+RUNTIME_SCENES = {
+    "trigde": ("mandelbulb_640x480", (160, 120), {"formula": 1, "power": 6, "angle_alfa": 30, "angle_beta": 19,
+                                                 "view_point_x": 1.75, "view_point_y": -3.0, "view_point_z": -1.2}),
+    "menger": ("mandelbulb_640x480", (160, 120), {"formula": 7, "N": 50, "view_point_x": 0.9, "view_point_z": 0.6,
+                                                 "angle_alfa": -14, "angle_beta": -9}),
+    "vary4d": ("mandelbox_1080p", (192, 108), {**W.VARY4D, "mandelbox_scale": 2.0}),
+}
+
+
+@pytest.mark.parametrize("engine", ENGINES, ids=["wavefront", "per_pixel"])
+@pytest.mark.parametrize("formula", sorted(RUNTIME_SCENES))
+def test_render_fp32_fix_runtime_formulas(gpu_ctx, oracle, formula, engine):
+    """The FP32 policy on formulas 1, 7 and 18 against the FP64 oracle, with the same bar as
+    the headline scenes: <= 0.1 % hit mismatch, >= 45 dB float-image PSNR."""
+    name, size, extra = RUNTIME_SCENES[formula]
+    sc = W.workload(name, *size, **extra)
+    ref, _ = oracle_lib.render(oracle, sc)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, engine=engine)
+    m = metrics.compare(img, ref)
+    print(formula, m)
     assert m["hit_mismatch"] <= 0.001, m
     assert m["psnr_float"] >= 45.0, m
 

@@ -22,7 +22,7 @@ def _scene(z):
     return mb.scene_from_bytes(z["scene"].tobytes())
 
 
-@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox"])
+@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox", "trigde", "menger", "vary4d"])
 def test_distance_estimator_bit_exact(oracle, mblib, formula):
     z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
     sc = _scene(z)
@@ -32,7 +32,7 @@ def test_distance_estimator_bit_exact(oracle, mblib, formula):
     np.testing.assert_array_equal(mi, z["max_iter"])
 
 
-@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox"])
+@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox", "trigde", "menger", "vary4d"])
 def test_colouring_value_bit_exact(oracle, mblib, formula):
     z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
     sc = _scene(z)
