@@ -220,7 +220,7 @@ def test_jitter_changes_steps_but_not_the_picture(gpu_ctx):
 
 
 def test_errors_are_status_codes(gpu_ctx):
-    sc = W.workload("mandelbulb_640x480", 64, 48, formula=7)
+    sc = W.workload("mandelbulb_640x480", 64, 48, formula=10)   # kaleidoscopic IFS: not on the device
     with pytest.raises(mb.MbgbError) as e:
         gpu_ctx.render(sc)
     assert e.value.status == 5
