@@ -43,13 +43,32 @@ typedef enum mbgb_status {
   MBGB_ERR_NO_DEVICE = 7    /* no CUDA device visible */
 } mbgb_status;
 
-/* enumFractalFormula (src/fractal.h:25-64), values that this build evaluates on the device. */
+/* enumFractalFormula (src/fractal.h:25-64). The device evaluates every value from 1 to 37
+ * (Compute<Mode>, src/fractal.cpp:189-1107); `none` (0) and ocl_custom (38) are rejected.
+ * Formulas 1, 2, 7, 8, 10, 17, 18 and 37 have an analytic distance estimate; the others,
+ * and the hybrid (12), use the delta-DE branch of CalculateDistance
+ * (src/fractal.cpp:1308-1381) and render in FP64 under every precision policy. */
 enum {
-  MBGB_FORMULA_TRIG_DE = 1,      /* Mandelbulb with a derivative vector, src/fractal.cpp:189-209 */
-  MBGB_FORMULA_TRIG_OPTIM = 2,   /* Mandelbulb, src/fractal.cpp:211-225 */
-  MBGB_FORMULA_MENGER = 7,       /* Menger sponge, src/fractal.cpp:369-407 */
-  MBGB_FORMULA_TGLAD = 8,        /* Mandelbox, src/fractal.cpp:409-529 */
-  MBGB_FORMULA_MBOX_VARY4D = 18  /* Mandelbox with varying scale, 4D, src/fractal.cpp:887-915 */
+  MBGB_FORMULA_TRIG_DE = 1,         /* Mandelbulb with a derivative vector, src/fractal.cpp:189-209 */
+  MBGB_FORMULA_TRIG_OPTIM = 2,      /* Mandelbulb, src/fractal.cpp:211-225 */
+  MBGB_FORMULA_FAST_TRIG = 3,       /* power-2 Mandelbulb without trigonometry, :321-335 */
+  MBGB_FORMULA_HYPERCOMPLEX = 4,    /* :351-359 */
+  MBGB_FORMULA_QUATERNION = 5,      /* :360-368 */
+  MBGB_FORMULA_MINUS_FAST_TRIG = 6, /* :336-350 */
+  MBGB_FORMULA_MENGER = 7,          /* Menger sponge, :369-407 */
+  MBGB_FORMULA_TGLAD = 8,           /* Mandelbox, :409-529 */
+  MBGB_FORMULA_KALEIDOSCOPIC = 10,  /* kaleidoscopic IFS, :837-886 */
+  MBGB_FORMULA_XENODREAMBUIE = 11,  /* :300-320 */
+  MBGB_FORMULA_HYBRID = 12,         /* per-iteration formula sequence (CreateFormulaSequence) */
+  MBGB_FORMULA_MANDELBULB2 = 13,    /* :226-254 */
+  MBGB_FORMULA_MANDELBULB3 = 14,    /* :255-282 */
+  MBGB_FORMULA_MANDELBULB4 = 15,    /* :283-299 */
+  MBGB_FORMULA_FOLDING_INT_POW2 = 16, /* :794-836 */
+  MBGB_FORMULA_SMOOTH_MANDELBOX = 17, /* :751-793 */
+  MBGB_FORMULA_MBOX_VARY4D = 18,    /* Mandelbox with varying scale, 4D, :887-915 */
+  MBGB_FORMULA_AEXION = 19,         /* 19-36: aexion, benesi, bristorbrot, invert X/Y/Z/R, */
+  MBGB_FORMULA_ANGLE_MULTIPLY_Z = 36, /* sphericalFold, powXYZ, scale/offset X/Y/Z, angleMultiply X/Y/Z, :916-1100 */
+  MBGB_FORMULA_GENERALIZED_FOLD_BOX = 37 /* :531-750 */
 };
 
 /* enumPerspectiveType (src/common_math.h:39-42) */
@@ -246,7 +265,8 @@ typedef struct mbgb_stats {
   uint64_t missed_de;          /* Missed_DE_counter */
   uint64_t long_rays;          /* primary rays longer than the main pass's step records (re-rendered) */
   uint64_t fp64_polished;      /* FP32_FIX, wavefront: hits whose bisection was finished in FP64 */
-  uint64_t auto_fp64;          /* 1 if any frame of the last call was rendered in FP64 (MBGB_PREC_AUTO picks per frame) */
+  uint64_t auto_fp64;          /* 1 if any frame of the last call was rendered in FP64 (MBGB_PREC_FP64, MBGB_PREC_AUTO's
+                                  per-frame pick, or a delta-DE formula, which renders in FP64 under every policy) */
   double kernel_ms;            /* device time of the last render */
   /* per stage: [0] primary rays (wavefront) or the per-pixel kernel, [1] FP64 hit polish,
    * [2] shadow and AO rays, [3] composition, [4] level-set refinement (exact_hit),

@@ -102,6 +102,104 @@ static std::vector<double> ao_vectors(int quality) {
   return v;
 }
 
+// The hybrid formula's sequence (CreateFormulaSequence, src/callbacks.cpp:1666-1702) as runs
+// of (formula, iterations, power): slots 1-4 that are set and have iterations, then slot 5
+// for the rest of the orbit, or for its own iteration count when the sequence is cyclic;
+// the runs repeat until the orbit's N entries are filled. Returns the number of runs.
+static int hybrid_runs(const mbgb_scene &s, int form[5], int count[5], double power[5]) {
+  int n = 0;
+  for (int i = 0; i < 4; i++) {
+    if (s.hybridFormula[i] == 0 || s.hybridIters[i] <= 0) continue;
+    form[n] = s.hybridFormula[i];
+    count[n] = s.hybridIters[i];
+    power[n] = s.hybridPower[i];
+    n++;
+  }
+  if (s.hybridFormula[4] != 0) {
+    const int c = s.hybridCyclic ? s.hybridIters[4] : (int)s.N;
+    if (c > 0) {
+      form[n] = s.hybridFormula[4];
+      count[n] = c;
+      power[n] = s.hybridPower[4];
+      n++;
+    }
+  }
+  return n;
+}
+
+// Whether the orbit of scene s runs formula k: as its formula or as a run of the hybrid
+// sequence.
+static bool uses_formula(const mbgb_scene &s, int k) {
+  if (s.formula == k) return true;
+  if (s.formula != 12) return false;
+  int form[5], count[5];
+  double power[5];
+  const int n = hybrid_runs(s, form, count, power);
+  for (int i = 0; i < n; i++)
+    if (form[i] == k) return true;
+  return false;
+}
+
+// Face normals of the generalized fold box's polyhedra (RecalculateIFSParams,
+// src/callbacks.cpp:1557-1663): tetrahedron, cube, octahedron, dodecahedron, octahedron +
+// cube, icosahedron, hexagonal and pentagonal prisms; an unknown type folds like the
+// tetrahedron. The prisms use the reference's 3.14159 for pi.
+static int gfb_normals(int type, double nv[20][3]) {
+  const double si3 = 1.0 / sqrt(3.0);
+  const double oct[8][3] = {{si3, si3, -si3}, {si3, -si3, si3}, {-si3, si3, si3}, {-si3, -si3, -si3},
+                            {si3, si3, si3},  {-si3, -si3, si3}, {-si3, si3, -si3}, {si3, -si3, -si3}};
+  const double cube[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  int n = 0;
+  auto put = [&](double x, double y, double z) {
+    nv[n][0] = x; nv[n][1] = y; nv[n][2] = z;
+    n++;
+  };
+  switch (type) {
+    case 1:  // cube
+      for (auto &v : cube) put(v[0], v[1], v[2]);
+      break;
+    case 2:  // octahedron
+      for (auto &v : oct) put(v[0], v[1], v[2]);
+      break;
+    case 3: {  // dodecahedron
+      const double aa = (1.0 + sqrt(5.0)) / 2.0;
+      const double bb = 1.0 / sqrt(aa * aa + 1.0);
+      put(0, bb, aa * bb); put(0, bb, -aa * bb); put(0, -bb, aa * bb); put(0, -bb, -aa * bb);
+      put(bb, aa * bb, 0); put(bb, -aa * bb, 0); put(-bb, aa * bb, 0); put(-bb, -aa * bb, 0);
+      put(aa * bb, 0, bb); put(-aa * bb, 0, bb); put(aa * bb, 0, -bb); put(-aa * bb, 0, -bb);
+      break;
+    }
+    case 4:  // octahedron + cube
+      for (auto &v : oct) put(v[0], v[1], v[2]);
+      for (auto &v : cube) put(v[0], v[1], v[2]);
+      break;
+    case 5: {  // icosahedron
+      const double aa = (1.0 + sqrt(5.0)) / 2.0;
+      const double ff = sqrt(aa * aa + 1.0 / (aa * aa));
+      const double cc = aa / ff;
+      const double dd = 1.0 / aa / ff;
+      for (auto &v : oct) put(v[0], v[1], v[2]);
+      put(0, dd, cc); put(0, dd, -cc); put(0, -dd, cc); put(0, -dd, -cc);
+      put(cc, 0, dd); put(cc, 0, -dd); put(-cc, 0, dd); put(-cc, 0, -dd);
+      put(dd, cc, 0); put(dd, -cc, 0); put(-dd, cc, 0); put(-dd, -cc, 0);
+      break;
+    }
+    case 6:
+    case 7: {  // hexagonal / pentagonal prism
+      const int k = type == 6 ? 6 : 5;
+      const double tha = 3.14159 * 2.0 / (double)k;
+      put(0, 0, 1);
+      put(0, 0, -1);
+      for (int i = 0; i < k; i++) put(cos(tha * i), sin(tha * i), 0);
+      break;
+    }
+    default:  // tetrahedron
+      for (int i = 0; i < 4; i++) put(oct[i][0], oct[i][1], oct[i][2]);
+      break;
+  }
+  return n;
+}
+
 template <typename T>
 static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   memset(&f, 0, sizeof(f));
@@ -156,6 +254,60 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   f.mbVaryScaleVary = (T)s.mboxVaryScaleVary;
   f.mbVaryWadd = (T)s.mboxVaryWadd;
   f.mbVaryRPower = (T)s.mboxVaryRPower;
+  f.analytic = s.analitycDE;
+  f.linearDE = s.linearDEmode;
+  if (s.ifsFoldingMode || uses_formula(s, 10)) {
+    // RecalculateIFSParams, IFS part (src/callbacks.cpp:1538-1547): SetRotation(alfa, beta,
+    // gamma) = RotateZ(alfa) RotateY(beta) RotateX(gamma); the directions were normalised
+    // when the scene was finalised
+    f.ifsFolding = s.ifsFoldingMode;
+    f.ifsAbsX = s.ifsAbsX;
+    f.ifsAbsY = s.ifsAbsY;
+    f.ifsAbsZ = s.ifsAbsZ;
+    f.ifsMenger = s.ifsMengerSpongeMode;
+    HostRot mr;
+    mr.rotZ(s.ifsRotationAlfa);
+    mr.rotY(s.ifsRotationBeta);
+    mr.rotX(s.ifsRotationGamma);
+    for (int k = 0; k < 9; k++) f.ifsMainRot[k] = (T)mr.m[k];
+    f.ifsMainRotZero = mr.zero;
+    f.ifsScale = (T)s.ifsScale;
+    for (int c = 0; c < 3; c++) {
+      f.ifsOffset[c] = (T)s.ifsOffset[c];
+      f.ifsEdge[c] = (T)s.ifsEdge[c];
+    }
+    for (int i = 0; i < 9; i++) {
+      f.ifsEnabled[i] = s.ifsEnabled[i];
+      HostRot r;
+      r.rotZ(s.ifsAlfa[i]);
+      r.rotY(s.ifsBeta[i]);
+      r.rotX(s.ifsGamma[i]);
+      for (int k = 0; k < 9; k++) f.ifsRot[i][k] = (T)r.m[k];
+      f.ifsRotZero[i] = r.zero;
+      for (int c = 0; c < 3; c++) f.ifsDir[i][c] = (T)s.ifsDirection[i][c];
+      f.ifsDist[i] = (T)s.ifsDistance[i];
+      f.ifsIntensity[i] = (T)s.ifsIntensity[i];
+    }
+  }
+  if (uses_formula(s, 17)) f.mbSharpness = (T)s.mboxSharpness;
+  if (uses_formula(s, 37)) {
+    f.mbSolid = (T)s.mboxSolid;
+    f.mbMelt = (T)s.mboxMelt;
+    double nv[20][3];
+    f.gfbSides = gfb_normals(s.genFoldBoxType, nv);
+    for (int i = 0; i < f.gfbSides; i++)
+      for (int c = 0; c < 3; c++) f.gfbNv[i][c] = (T)nv[i][c];
+  }
+  if (uses_formula(s, 16)) {
+    f.intPowFold = (T)s.FoldingIntPowFoldFactor;
+    f.intPowZ = (T)s.FoldingIntPowZfactor;
+  }
+  if (uses_formula(s, 19)) f.cadd = (T)s.cadd;
+  if (s.formula == 12) {
+    double power[5];
+    f.hybridSegs = hybrid_runs(s, f.hybridForm, f.hybridCount, power);
+    for (int i = 0; i < f.hybridSegs; i++) f.hybridPower[i] = (T)power[i];
+  }
 }
 
 // MainThread's per-frame preparation (src/Render3D.cpp:213-344) into a kernel parameter block.
@@ -398,8 +550,16 @@ extern "C" mbgb_status mbgb_scene_supported(const mbgb_scene *s) {
   if (!s) return set_error(MBGB_ERR_BAD_PARAM, "NULL scene");
   if (s->formula != MBGB_FORMULA_TRIG_OPTIM && s->formula != MBGB_FORMULA_TGLAD && !runtime_formula(s->formula))
     return set_error(MBGB_ERR_UNSUPPORTED, "formula " + std::to_string(s->formula) + " is not built on the device");
-  if (!s->analitycDE) return set_error(MBGB_ERR_UNSUPPORTED, "delta-DE mode is not built on the device");
-  if (s->ifsFoldingMode) return set_error(MBGB_ERR_UNSUPPORTED, "IFS folding mode");
+  if (s->formula == 12) {
+    int form[5], count[5];
+    double power[5];
+    const int runs = hybrid_runs(*s, form, count, power);
+    if (runs == 0) return set_error(MBGB_ERR_UNSUPPORTED, "hybrid formula with an empty formula sequence");
+    for (int i = 0; i < runs; i++)
+      if (form[i] < 1 || form[i] > 37)
+        return set_error(MBGB_ERR_UNSUPPORTED, "hybrid sequence formula " + std::to_string(form[i]) +
+                                                   " is not built on the device");
+  }
   if (s->planeEnable || s->boxEnable || s->invertedBoxEnable || s->sphereEnable || s->invertedSphereEnable ||
       s->waterEnable || s->onlyPlane)
     return set_error(MBGB_ERR_UNSUPPORTED, "primitive objects");
@@ -501,7 +661,7 @@ static mbgb_status ensure_ao(mbgb_context *c, int quality, cudaStream_t s) {
 // min radius <= fixed radius (so that the sphere fold is a clamp).
 static bool fast_mandelbox(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
-         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
+         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
          s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
          s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
          s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
@@ -511,7 +671,7 @@ static bool fast_mandelbox(const mbgb_scene &s) {
 // no pre-folds, limits, iteration threshold or interior mode).
 static bool fast_mandelbulb(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
-         !s.limits_enabled && !s.iterThresh && !s.interiorMode;
+         !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode;
 }
 
 // Per-frame fields of ParamsT (camera, size, rows, light direction) cleared, so that
@@ -639,7 +799,7 @@ static bool need_volumetric(const mbgb_scene &s) {
 static mbgb_status level_set_supported(const mbgb_scene &s) {
   if (s.formula != MBGB_FORMULA_TRIG_OPTIM && s.formula != MBGB_FORMULA_TGLAD)
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: formulas 2 and 8 only");
-  if (s.tgladFoldingMode || s.sphericalFoldingMode)
+  if (s.tgladFoldingMode || s.sphericalFoldingMode || s.ifsFoldingMode)
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: pre-folds");
   if (s.formula == MBGB_FORMULA_TGLAD &&
       (s.mboxRotationsEnabled || !s.mboxMainRotZero || s.mboxOffset[0] != 0.0 || s.mboxOffset[1] != 0.0 ||
@@ -809,8 +969,9 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   MBGB_CUDA(cudaMemsetAsync(ctl, 0, 64, s));
 
   const int block = g.cfg.block;
-  int occ1 = std::max(1, wave_occupancy<T>(scene.formula, block, 0));
-  int occ2 = std::max(1, wave_occupancy<T>(scene.formula, block, 1));
+  const int kf = kernel_formula(scene.formula, scene.ifsFoldingMode);
+  int occ1 = std::max(1, wave_occupancy<T>(kf, block, 0));
+  int occ2 = std::max(1, wave_occupancy<T>(kf, block, 1));
   if (g.cfg.ctasPerSm > 0) {
     occ1 = std::min(occ1, g.cfg.ctasPerSm);
     occ2 = std::min(occ2, g.cfg.ctasPerSm);
@@ -856,7 +1017,8 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
                                      uint64_t *launches) {
   const int prec = g.prec;
   const int block = g.cfg.block;
-  int per_sm = std::max(1, occupancy_render(prec, scene.formula, block));
+  const int kf = kernel_formula(scene.formula, scene.ifsFoldingMode);
+  int per_sm = std::max(1, occupancy_render(prec, kf, block));
   if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
   const int grid = c->sms * per_sm;
   io.image_float = img.image_float;
@@ -894,13 +1056,13 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   if (prec == 0) {
     ParamsT<double> p;
     fill_params<double>(scene, p, o, (const double *)c->ao64.ptr, c->ao_count);
-    e = launch_render_f64(scene.formula, p, fd, io, grid, block, s);
-    if (e == cudaSuccess && needVol) e = launch_render_f64(scene.formula, p, fd, ov, ovBlocks, block, s);
+    e = launch_render_f64(kf, p, fd, io, grid, block, s);
+    if (e == cudaSuccess && needVol) e = launch_render_f64(kf, p, fd, ov, ovBlocks, block, s);
   } else {
     ParamsT<float> p;
     fill_params<float>(scene, p, o, (const float *)c->ao32.ptr, c->ao_count);
-    e = launch_render_f32(scene.formula, p, fd, io, grid, block, s);
-    if (e == cudaSuccess && needVol) e = launch_render_f32(scene.formula, p, fd, ov, ovBlocks, block, s);
+    e = launch_render_f32(kf, p, fd, io, grid, block, s);
+    if (e == cudaSuccess && needVol) e = launch_render_f32(kf, p, fd, ov, ovBlocks, block, s);
   }
   if (e != cudaSuccess) return cuda_error(e, "render kernel launch");
   *launches += 1 + (needVol ? 1 : 0);
@@ -930,7 +1092,7 @@ static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int
   for (int i = 0; i < n; i++) {
     FractalT<double> fp;
     fill_fractal<double>(scenes[i], fp);
-    cudaError_t pe = launch_distance_f64(scenes[i].formula, fp, (const double *)(pb + o_pts) + 3 * i,
+    cudaError_t pe = launch_distance_f64(kernel_formula(scenes[i].formula, scenes[i].ifsFoldingMode), fp, (const double *)(pb + o_pts) + 3 * i,
                                          (const double *)(pb + o_det) + i, 1, (double *)(pb + o_d) + i,
                                          (int *)(pb + o_it) + i, (unsigned char *)(pb + o_mi) + i, nullptr, s);
     if (pe != cudaSuccess) return cuda_error(pe, "precision probe");
@@ -1051,6 +1213,10 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     st = auto_precision(c, scenes, n, o, s, prec);
     if (st != MBGB_OK) return st;
   }
+  // delta-DE formulas difference orbits at a step of 1e-10 (src/fractal.cpp:1310), far
+  // below FP32 resolution: those frames render in FP64 under every policy
+  for (int i = 0; i < n; i++)
+    if (!scenes[i].analitycDE) prec[i] = 0;
   st = ensure_call_ao(c, scenes, n, s);
   if (st != MBGB_OK) return st;
   if (o.autotune) {
@@ -1142,7 +1308,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       }
     } else if (needVol) {
       maxPixPerPixel = std::max(maxPixPerPixel, g.npix);
-      int per_sm = std::max(1, occupancy_render(g.prec, rep.formula, g.cfg.block));
+      int per_sm = std::max(1, occupancy_render(g.prec, kernel_formula(rep.formula, rep.ifsFoldingMode), g.cfg.block));
       if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
       maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_sm * g.cfg.block);
     }
@@ -1417,8 +1583,8 @@ static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const
     if ((st = consider(cand)) != MBGB_OK) return st;
   }
   {
-    const int occ = std::max(1, prec == 0 ? occupancy_wave_f64(scene->formula, cur.block, 0)
-                                          : occupancy_wave_f32(scene->formula, cur.block, 0));
+    const int kf = kernel_formula(scene->formula, scene->ifsFoldingMode);
+    const int occ = std::max(1, prec == 0 ? occupancy_wave_f64(kf, cur.block, 0) : occupancy_wave_f32(kf, cur.block, 0));
     if (occ >= 2) {
       LaunchCfg cand = cur;
       cand.ctasPerSm = occ / 2;
@@ -1586,14 +1752,16 @@ extern "C" mbgb_status mbgb_distance_device(mbgb_context *c, const mbgb_scene *s
   std::lock_guard<std::mutex> lk(c->mu);
   MBGB_CUDA(cudaSetDevice(c->device));
   cudaError_t e;
-  if (precision == MBGB_PREC_FP64) {
+  if (precision == MBGB_PREC_FP64 || !scene->analitycDE) {  // delta-DE: FP64 under every policy
     FractalT<double> f;
     fill_fractal<double>(*scene, f);
-    e = launch_distance_f64(scene->formula, f, points, detail, n, dist, iters, max_iter, nullptr, c->stream);
+    e = launch_distance_f64(kernel_formula(scene->formula, scene->ifsFoldingMode), f, points, detail, n, dist, iters,
+                            max_iter, nullptr, c->stream);
   } else {
     FractalT<float> f;
     fill_fractal<float>(*scene, f);
-    e = launch_distance_f32(scene->formula, f, points, detail, n, dist, iters, max_iter, nullptr, c->stream);
+    e = launch_distance_f32(kernel_formula(scene->formula, scene->ifsFoldingMode), f, points, detail, n, dist, iters,
+                            max_iter, nullptr, c->stream);
   }
   if (e != cudaSuccess) return cuda_error(e, "distance kernel launch");
   MBGB_CUDA(cudaStreamSynchronize(c->stream));

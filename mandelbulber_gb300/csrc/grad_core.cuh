@@ -140,7 +140,7 @@ __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const Fracta
 // Stage 5 (differentiable render): per-pixel Jacobians and the per-frame sums
 // dL/dtheta = sum over pixels and channels of dL/dI dI/dtheta.
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) grad_kernel(const ParamsT<T> p, const FractalT<double> fd, const FrameIO io,
+__global__ void __launch_bounds__(128) grad_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd, const FrameIO io,
                                                    const WaveBufs<T> wb,
                                                    const FrameCam<T> *__restrict__ cams,
                                                    const GradCam<T> *__restrict__ gcams, const int ncams) {

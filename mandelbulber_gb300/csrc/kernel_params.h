@@ -19,9 +19,17 @@ constexpr int kOverflowThreads = 128;   // threads of the pass that re-renders r
 constexpr int kMaxAOVectors = 10000;    // sVectorsAround table (src/Render3D.cpp:272)
 constexpr int kTileW = 8, kTileH = 4;   // one warp renders an 8x4 pixel tile
 
-// Formulas the kernels select at run time (FORMULA 0 of compute()): trig_DE, menger_sponge,
-// mandelboxVaryScale4D. trig_optim (2) and tglad (8) have instantiations of their own.
-inline bool runtime_formula(int formula) { return formula == 1 || formula == 7 || formula == 18; }
+// Formulas the kernels select at run time (FORMULA 0 of compute(), formulas.cuh): every
+// formula of enumFractalFormula (src/fractal.h:25-65) from trig_DE (1) to generalizedFoldBox
+// (37) but trig_optim (2) and tglad (8), which have instantiations of their own. `none` (0)
+// and ocl_custom (38) are not rendered.
+inline bool runtime_formula(int formula) { return formula >= 1 && formula <= 37 && formula != 2 && formula != 8; }
+
+// The instantiation a scene runs: 2 or 8, or 0 for the run-time formula path (every other
+// formula, and 2 / 8 with the kaleidoscopic IFS pre-fold, which only that path carries).
+inline int kernel_formula(int formula, bool ifsFolding) {
+  return ((formula == 2 || formula == 8) && !ifsFolding) ? formula : 0;
+}
 
 // Fractal / distance-estimator parameters (sFractal, src/fractal.h:255-293).
 template <typename T>
@@ -46,6 +54,26 @@ struct FractalT {
   T mbRotInv[2][3][9];
   T amin, amax, bmin, bmax, cmin, cmax;
   T mbVaryFold, mbVaryMinR, mbVaryScaleVary, mbVaryWadd, mbVaryRPower;   // mandelboxVaryScale4D
+  // run-time formulas (formulas.cuh); each block is filled only when the formula (or a step
+  // of the hybrid sequence) reads it, so frames that differ only in unused fields still share
+  // a launch sequence
+  int analytic, linearDE;          // analitycDE, linearDEmode: delta-DE distance when analytic == 0
+  // kaleidoscopic IFS (sFractalIFS, src/fractal.h:138-148, prepared by RecalculateIFSParams)
+  int ifsFolding, ifsAbsX, ifsAbsY, ifsAbsZ, ifsMenger, ifsMainRotZero;
+  int ifsEnabled[9], ifsRotZero[9];
+  T ifsScale, ifsOffset[3], ifsEdge[3];
+  T ifsMainRot[9];
+  T ifsRot[9][9];
+  T ifsDir[9][3], ifsDist[9], ifsIntensity[9];
+  // smoothMandelbox / generalizedFoldBox (sFractalMandelboxD, sFractalGeneralizedFoldBox)
+  T mbSharpness, mbSolid, mbMelt;
+  int gfbSides;
+  T gfbNv[20][3];
+  T intPowFold, intPowZ, cadd;     // foldingIntPow2, aexion
+  // hybrid: the formula sequence as runs of (formula, iterations, power), repeated
+  int hybridSegs;
+  int hybridForm[5], hybridCount[5];
+  T hybridPower[5];
 };
 
 // Everything MainThread and the shaders read (sParamRender, src/fractparams.h:67-146).

@@ -106,6 +106,9 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   if (opts_in) o = *opts_in;
   if (o.precision != MBGB_PREC_FP32_FIX && o.precision != MBGB_PREC_AUTO)
     return mbgb::set_error(MBGB_ERR_BAD_PARAM, "the allocation-free entry point renders the FP32_FIX policy only");
+  if (!scene->analitycDE)
+    return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
+                           "delta-DE formulas render in FP64, which the allocation-free entry point does not carry");
   if (o.row_end == 0) o.row_end = scene->image_height;
   if (o.row_begin < 0 || o.row_end > scene->image_height || o.row_begin >= o.row_end)
     return mbgb::set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
@@ -170,8 +173,9 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   ov.step_thr = d->ovsteps + 2 * (size_t)kStepSlots * kOverflowThreads;
 
   const bool needVol = (scene->glow_intensity != 0.0) || scene->fogEnabled || (scene->fogDensity > 0.0);
-  e = mbgb::launch_render_f32(scene->formula, p, fd, io, grid, kNaThreads, s);
-  if (e == cudaSuccess && needVol) e = mbgb::launch_render_f32(scene->formula, p, fd, ov, 1, kOverflowThreads, s);
+  const int kf = mbgb::kernel_formula(scene->formula, scene->ifsFoldingMode);
+  e = mbgb::launch_render_f32(kf, p, fd, io, grid, kNaThreads, s);
+  if (e == cudaSuccess && needVol) e = mbgb::launch_render_f32(kf, p, fd, ov, 1, kOverflowThreads, s);
   if (e != cudaSuccess) return mbgb::set_error(MBGB_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));
   if (!o.stream) {
     e = cudaStreamSynchronize(s);

@@ -127,18 +127,33 @@ __host__ __device__ __forceinline__ T fparam_of(const FractalT<T> &f) {
   return scale_formula(f.formula) ? f.mbScale : f.power;
 }
 
+}  // namespace dev
+}  // namespace mbgb
+
+#include "formulas.cuh"
+
+namespace mbgb {
+namespace dev {
+
 // ---------------------------------------------------------------------------
-// Compute<Mode> (src/fractal.cpp:40-1241) for the formulas this build carries.
-// MODE 0 = normal (returns the distance estimate), MODE 1 = colouring.
-// FORMULA 2 (trig_optim) and 8 (tglad) are compiled as such; FORMULA 0 selects the
-// formula at run time from f.formula: trig_DE (1), menger_sponge (7) and
-// mandelboxVaryScale4D (18).
+// Compute<Mode> (src/fractal.cpp:40-1241). MODE 0 = normal (returns the distance
+// estimate), MODE 1 = colouring. FORMULA 2 (trig_optim) and 8 (tglad) are compiled as
+// such; FORMULA 0 runs the formula f.formula selects through the run-time formula path
+// (compute_runtime, formulas.cuh).
 // ---------------------------------------------------------------------------
 // `fparam` is the formula's main parameter: the power, or the Mandelbox scale of the
 // scale formulas (a frame of a batch may carry its own; see fparam_of).
 template <typename T, int FORMULA, int MODE>
 __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N, int &Lout, Counters &cnt,
                                      const T fparam) {
+  if (FORMULA == 0) {
+    int L;
+    const T d = compute_runtime<T, MODE>(&f, z, N, 0, &L, fparam);
+    cnt.orbit += (unsigned long long)(L + 1);
+    cnt.calls += 1;
+    Lout = L;
+    return d;
+  }
   T distance = T(0);
   T r_dz = T(1);
   const T p = fparam;
@@ -156,11 +171,6 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
   }
   T r = orbit_length(z);
   T minv = (sizeof(T) == 8) ? T(1e200) : T(__int_as_float(0x7f800000));
-  // state of the run-time formulas: trig_DE's derivative vector in polar form, the 4th
-  // coordinate and the varying scale of mandelboxVaryScale4D
-  const int form = FORMULA == 0 ? f.formula : FORMULA;
-  V3<T> dz{T(1), T(0), T(0)};
-  T th_dz = T(0), ph_dz = T(0), w = T(0), scaleV = scale;
   int L;
   for (L = 0; L < N; L++) {
     if (f.tgladFoldingMode) {  // src/fractal.cpp:124-156
@@ -186,141 +196,12 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       r = orbit_length(z);
     }
     if (FORMULA == 2) {
-      // trig_optim Mandelbulb (src/fractal.cpp:211-225)
-      const T th0 = m_asin(z.z / r);
-      const T ph0 = m_atan2(z.y, z.x);
-      T rp = m_pow(r, p - T(1));
-      const T th = th0 * p;
-      const T ph = ph0 * p;
-      T sth, cth, sph, cph;
-      m_sincos(th, &sth, &cth);
-      m_sincos(ph, &sph, &cph);
-      r_dz = rp * r_dz * p + T(1);
-      rp *= r;
-      z = V3<T>{cth * cph, cth * sph, sth} * rp + constant;
-      r = orbit_length(z);
+      trig_optim_step(z, r, r_dz, p, constant);
     } else if (FORMULA == 8) {
-      // tglad Mandelbox (src/fractal.cpp:409-529)
-      if (f.mbRotEnabled) {
-        bool lockout = false;
-        z = rotate(f.mbRot[0][0], f.mbRotZero[0][0], z);
-        if (z.x > f.mbFoldLimit) { z.x = f.mbFoldValue - z.x; tgladColor += f.mbColX; lockout = true; }
-        z = rotate(f.mbRotInv[0][0], 0, z);
-        z = rotate(f.mbRot[1][0], f.mbRotZero[1][0], z);
-        if (!lockout && z.x < -f.mbFoldLimit) { z.x = -f.mbFoldValue - z.x; tgladColor += f.mbColX; }
-        z = rotate(f.mbRotInv[1][0], 0, z);
-        lockout = false;
-        z = rotate(f.mbRot[0][1], f.mbRotZero[0][1], z);
-        if (z.y > f.mbFoldLimit) { z.y = f.mbFoldValue - z.y; tgladColor += f.mbColY; lockout = true; }
-        z = rotate(f.mbRotInv[0][1], 0, z);
-        z = rotate(f.mbRot[1][1], f.mbRotZero[1][1], z);
-        if (!lockout && z.y < -f.mbFoldLimit) { z.y = -f.mbFoldValue - z.y; tgladColor += f.mbColY; }
-        z = rotate(f.mbRotInv[1][1], 0, z);
-        lockout = false;
-        z = rotate(f.mbRot[0][2], f.mbRotZero[0][2], z);
-        if (z.z > f.mbFoldLimit) { z.z = f.mbFoldValue - z.z; tgladColor += f.mbColZ; lockout = true; }
-        z = rotate(f.mbRotInv[0][2], 0, z);
-        z = rotate(f.mbRot[1][2], f.mbRotZero[1][2], z);
-        if (!lockout && z.z < -f.mbFoldLimit) { z.z = -f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
-        z = rotate(f.mbRotInv[1][2], 0, z);
-      } else {
-        if (z.x > f.mbFoldLimit) { z.x = f.mbFoldValue - z.x; tgladColor += f.mbColX; }
-        else if (z.x < -f.mbFoldLimit) { z.x = -f.mbFoldValue - z.x; tgladColor += f.mbColX; }
-        if (z.y > f.mbFoldLimit) { z.y = f.mbFoldValue - z.y; tgladColor += f.mbColY; }
-        else if (z.y < -f.mbFoldLimit) { z.y = -f.mbFoldValue - z.y; tgladColor += f.mbColY; }
-        if (z.z > f.mbFoldLimit) { z.z = f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
-        else if (z.z < -f.mbFoldLimit) { z.z = -f.mbFoldValue - z.z; tgladColor += f.mbColZ; }
-      }
-      r = orbit_length(z);
-      const T r2 = r * r;
-      z = z + V3<T>{f.mbOffset[0], f.mbOffset[1], f.mbOffset[2]};
-      if (r2 < mR2) {
-        z = z * tglad_factor1; tgladDE *= tglad_factor1; tgladColor += f.mbColSp1;
-      } else if (r2 < fR2) {
-        const T tglad_factor2 = fR2 / r2;
-        z = z * tglad_factor2; tgladDE *= tglad_factor2; tgladColor += f.mbColSp2;
-      }
-      z = z - V3<T>{f.mbOffset[0], f.mbOffset[1], f.mbOffset[2]};
-      z = rotate(f.mbMainRot, f.mbMainRotZero, z);
-      z = z * scale + constant;
-      tgladDE = tgladDE * m_fabs(scale) + T(1);
-      r = orbit_length(z);
-    } else if (FORMULA == 0) {
-      if (form == 1) {
-        // trig_DE (src/fractal.cpp:189-209): angles atan2(y, x) and -atan2(z, rho); in normal
-        // mode the derivative vector dz is carried in the same polar form
-        const T r1 = m_pow(r, p - T(1));
-        const T r2 = r1 * r;
-        const T th = m_atan2(z.y, z.x);
-        const T ph = -m_atan2(z.z, m_sqrt(z.x * z.x + z.y * z.y));
-        if (MODE == 0) {
-          const T p_r1_rdz = p * r1 * r_dz;
-          const T ph_phdz = (p - T(1)) * ph + ph_dz;
-          const T th_thdz = (p - T(1)) * th + th_dz;
-          T sb, cb, sa, ca;
-          m_sincos(ph_phdz, &sb, &cb);
-          m_sincos(th_thdz, &sa, &ca);
-          const V3<T> rot{cb * ca, cb * sa, sb};
-          dz = V3<T>{rot.x * p_r1_rdz + T(1), rot.y * p_r1_rdz + T(0), rot.z * p_r1_rdz + T(0)};
-          r_dz = length3(dz);
-          th_dz = m_atan2(dz.y, dz.x);
-          ph_dz = -m_atan2(dz.z, m_sqrt(dz.x * dz.x + dz.y * dz.y));
-        }
-        T sb, cb, sa, ca;
-        m_sincos(p * ph, &sb, &cb);
-        m_sincos(p * th, &sa, &ca);
-        z = V3<T>{cb * ca, cb * sa, sb} * r2 + constant;
-        r = orbit_length(z);
-      } else if (form == 7) {
-        // menger_sponge (src/fractal.cpp:369-407): fold into the first octant sorted x >= y >= z
-        z.x = m_fabs(z.x);
-        z.y = m_fabs(z.y);
-        z.z = m_fabs(z.z);
-        T t;
-        if (z.x - z.y < T(0)) { t = z.y; z.y = z.x; z.x = t; }
-        if (z.x - z.z < T(0)) { t = z.z; z.z = z.x; z.x = t; }
-        if (z.y - z.z < T(0)) { t = z.z; z.z = z.y; z.y = t; }
-        if (MODE == 1) {
-          const T len = orbit_length(z);
-          if (len < minv) minv = len;
-        }
-        z = z * T(3);
-        z.x -= T(2);
-        z.y -= T(2);
-        if (z.z > T(1)) z.z -= T(2);
-        r = orbit_length(z);
-        tgladDE *= T(3);
-      } else if (form == 18) {
-        // mandelboxVaryScale4D (src/fractal.cpp:887-915)
-        scaleV = scaleV + f.mbVaryScaleVary * (m_fabs(scaleV) - T(1));
-        const V3<T> oldz = z;
-        const T fo = f.mbVaryFold;
-        z.x = m_fabs(z.x + fo) - m_fabs(z.x - fo) - z.x;
-        z.y = m_fabs(z.y + fo) - m_fabs(z.y - fo) - z.y;
-        z.z = m_fabs(z.z + fo) - m_fabs(z.z - fo) - z.z;
-        w = m_fabs(w + fo) - m_fabs(w - fo) - w;
-        if (z.x != oldz.x) tgladColor += f.mbColX;
-        if (z.y != oldz.y) tgladColor += f.mbColY;
-        if (z.z != oldz.z) tgladColor += f.mbColZ;
-        const T rr = m_pow(z.x * z.x + z.y * z.y + z.z * z.z + w * w, f.mbVaryRPower);
-        T m = scaleV;
-        if (rr < f.mbVaryMinR * f.mbVaryMinR) {
-          m = scaleV / (f.mbVaryMinR * f.mbVaryMinR);
-          tgladColor += f.mbColSp1;
-        } else if (rr < T(1)) {
-          m = scaleV / rr;
-          tgladColor += f.mbColSp2;
-        }
-        z = z * m + constant;
-        w = w * m + f.mbVaryWadd;
-        tgladDE = tgladDE * m_fabs(m) + T(1);
-        r = m_sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
-      }
+      tglad_step(f, z, r, tgladDE, tgladColor, scale, constant, fR2, mR2, tglad_factor1);
     }
     // iteration terminate conditions (src/fractal.cpp:1133-1190)
-    if (form == 7) {
-      if (r > T(1000)) { distance = (r - T(2)) / tgladDE; break; }
-    } else if (FORMULA == 8 || form == 18) {
+    if (FORMULA == 8) {
       if (r > T(1024)) { distance = r / m_fabs(tgladDE); break; }
     } else {
       if (MODE == 0) {
@@ -339,8 +220,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
     if (L == N) distance = T(0);
     return distance;
   } else {
-    if (FORMULA == 8 || form == 18) return tgladColor * T(100) + orbit_length(z) * f.mbColR;
-    if (form == 7) return minv * T(1000);
+    if (FORMULA == 8) return tgladColor * T(100) + orbit_length(z) * f.mbColR;
     return distance * T(5000);
   }
 }
@@ -351,6 +231,9 @@ template <typename T, int FORMULA>
 __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> point, const T detailSize, const int N,
                                            const int minN, const bool normalMode, int &L, bool &maxIter,
                                            Counters &cnt, const T fparam) {
+  if (FORMULA == 0)
+    return calc_distance_runtime<T>(&f, point, detailSize, N, minN, normalMode, &L, &maxIter, &cnt.orbit, &cnt.calls,
+                                    fparam);
   T limitBoxDist = T(0);
   if (f.limits) {
     // MAX(a, b) = a > b ? a : b (gtk MAX macro)
@@ -949,7 +832,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
 // (src/Render3D.cpp:352-366) and the thread spawn of Render (src/Render3D.cpp:815-849).
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA>
-__global__ void __launch_bounds__(128) render_kernel(const ParamsT<T> p, const FractalT<double> fd, const FrameIO io) {
+__global__ void __launch_bounds__(128) render_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd, const FrameIO io) {
   const int lane = threadIdx.x & 31;
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, io.slots, slot};
@@ -1000,7 +883,7 @@ __global__ void __launch_bounds__(128) render_kernel(const ParamsT<T> p, const F
 
 // CalculateDistance at arbitrary points (unit tests of the distance estimator).
 template <typename T, int FORMULA>
-__global__ void distance_kernel(const FractalT<T> f, const double *points, const double *detail, int64_t n,
+__global__ void distance_kernel(const __grid_constant__ FractalT<T> f, const double *points, const double *detail, int64_t n,
                                 double *dist, int32_t *iters, uint8_t *max_iter, unsigned long long *counters) {
   Counters cnt{0, 0, 0, 0};
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {

@@ -10,8 +10,7 @@ cudaError_t launch_render_f32(int formula, const ParamsT<float> &p, const Fracta
     case 2: dev::render_kernel<float, 2><<<grid, block, 0, s>>>(p, fd, io); break;
     case 8: dev::render_kernel<float, 8><<<grid, block, 0, s>>>(p, fd, io); break;
     default:
-      if (runtime_formula(formula)) return launch_render_f32_runtime(p, fd, io, grid, block, s);
-      return cudaErrorInvalidValue;
+      return launch_render_f32_runtime(p, fd, io, grid, block, s);
   }
   return cudaGetLastError();
 }
@@ -26,8 +25,7 @@ cudaError_t launch_distance_f32(int formula, const FractalT<float> &f, const dou
     case 2: dev::distance_kernel<float, 2><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
     case 8: dev::distance_kernel<float, 8><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
     default:
-      if (runtime_formula(formula)) return launch_distance_f32_runtime(f, points, detail, n, dist, iters, max_iter, counters, s);
-      return cudaErrorInvalidValue;
+      return launch_distance_f32_runtime(f, points, detail, n, dist, iters, max_iter, counters, s);
   }
   return cudaGetLastError();
 }

@@ -10,8 +10,7 @@ cudaError_t launch_render_f64(int formula, const ParamsT<double> &p, const Fract
     case 2: dev::render_kernel<double, 2><<<grid, block, 0, s>>>(p, fd, io); break;
     case 8: dev::render_kernel<double, 8><<<grid, block, 0, s>>>(p, fd, io); break;
     default:
-      if (runtime_formula(formula)) return launch_render_f64_runtime(p, fd, io, grid, block, s);
-      return cudaErrorInvalidValue;
+      return launch_render_f64_runtime(p, fd, io, grid, block, s);
   }
   return cudaGetLastError();
 }
@@ -26,8 +25,7 @@ cudaError_t launch_distance_f64(int formula, const FractalT<double> &f, const do
     case 2: dev::distance_kernel<double, 2><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
     case 8: dev::distance_kernel<double, 8><<<grid, block, 0, s>>>(f, points, detail, n, dist, iters, max_iter, counters); break;
     default:
-      if (runtime_formula(formula)) return launch_distance_f64_runtime(f, points, detail, n, dist, iters, max_iter, counters, s);
-      return cudaErrorInvalidValue;
+      return launch_distance_f64_runtime(f, points, detail, n, dist, iters, max_iter, counters, s);
   }
   return cudaGetLastError();
 }

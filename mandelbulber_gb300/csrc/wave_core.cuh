@@ -460,7 +460,7 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 // Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128, 6) primary_kernel(const ParamsT<T> p, const FractalT<double> fd,
+__global__ void __launch_bounds__(128, 6) primary_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -700,7 +700,7 @@ __global__ void __launch_bounds__(128, 6) primary_kernel(const ParamsT<T> p, con
 // orbit class use the FP64 lean orbits (polish_distance).
 // ---------------------------------------------------------------------------
 template <int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, const FractalT<double> fd,
+__global__ void __launch_bounds__(128) polish_kernel(const __grid_constant__ ParamsT<float> p, const __grid_constant__ FractalT<double> fd,
                                                      const FrameIO io, const WaveBufs<float> wb,
                                                      const FrameCam<float> *__restrict__ cams, const int ncams) {
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[6];
@@ -757,7 +757,7 @@ __global__ void __launch_bounds__(128) polish_kernel(const ParamsT<float> p, con
 // flagged (bit 3) so the gradient stage leaves it out.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA>
-__global__ void __launch_bounds__(128) level_set_kernel(const ParamsT<T> p, const FractalT<double> fd,
+__global__ void __launch_bounds__(128) level_set_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
                                                         const WaveBufs<T> wb, const FrameCam<T> *__restrict__ cams,
                                                         const int ncams) {
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[6];
@@ -836,7 +836,7 @@ __device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const FrameC
 // direction-major so a warp's initial 32 rays share a direction.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) secondary_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
+__global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                         const FrameCam<T> *__restrict__ cams, const int ncams) {
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
   const unsigned int nShadow = p.shadow ? nh : 0u;
@@ -1050,7 +1050,7 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
 // over every pixel of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) compose_kernel(const ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
+__global__ void __launch_bounds__(128) compose_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   Counters cnt{0, 0, 0, 0};
   const int64_t total = wb.npix;

@@ -5,10 +5,10 @@
 namespace mbgb {
 
 cudaError_t launch_wave_f64(const WaveLaunch<double> &L, cudaStream_t s) {
-  if (L.p.f.formula == 2) return L.fast ? run_stages<double, 2, false>(L, s) : run_stages<double, 2, false>(L, s);
-  if (L.p.f.formula == 8) return L.fast ? run_stages<double, 8, false>(L, s) : run_stages<double, 8, false>(L, s);
-  if (runtime_formula(L.p.f.formula)) return launch_wave_f64_runtime(L, s);
-  return cudaErrorInvalidValue;
+  const int kf = kernel_formula(L.p.f.formula, L.p.f.ifsFolding);
+  if (kf == 2) return L.fast ? run_stages<double, 2, false>(L, s) : run_stages<double, 2, false>(L, s);
+  if (kf == 8) return L.fast ? run_stages<double, 8, false>(L, s) : run_stages<double, 8, false>(L, s);
+  return launch_wave_f64_runtime(L, s);
 }
 
 int occupancy_wave_f64(int formula, int block, int which) {

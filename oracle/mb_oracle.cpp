@@ -9,10 +9,11 @@
 // fractal.cpp / shaders.cpp (oracle/_ref).
 //
 // Function-by-function sources (reference paths):
-//   compute_normal / compute_colour   Compute<normal|colouring>  src/fractal.cpp:40-1241 (formulas
-//                                     trig_DE 1, trig_optim 2, menger_sponge 7, tglad 8,
-//                                     mandelboxVaryScale4D 18)
-//   calculate_distance                CalculateDistance          src/fractal.cpp:1245-1448
+//   compute                           Compute<normal|colouring|deltaDE1|deltaDE2> src/fractal.cpp:40-1241
+//                                     (every formula from trig_DE 1 to generalizedFoldBox 37, the
+//                                     IFS / tglad / spherical pre-folds, the hybrid sequence)
+//   derive                            RecalculateIFSParams / CreateFormulaSequence src/callbacks.cpp:1538-1702
+//   calculate_distance                CalculateDistance, analytic and delta-DE src/fractal.cpp:1245-1448
 //   ray_marching                      RayMarching                src/Render3D.cpp:79-199
 //   calculate_normals                 CalculateNormals           src/shaders.cpp:675-757
 //   main_shadow                       MainShadow                 src/shaders.cpp:480-570
@@ -65,6 +66,105 @@ struct Cnt {
   uint64_t orbit = 0, calls = 0, steps = 0;
 };
 
+// What RecalculateIFSParams and CreateFormulaSequence (src/callbacks.cpp:1538-1702) prepare
+// for the orbit: the IFS rotation matrices, the generalized fold box's face normals and the
+// hybrid formula sequence.
+struct Derived {
+  double ifsMain[9];
+  int ifsMainZero;
+  double ifsRot[9][9];
+  int ifsRotZero[9];
+  int gfbSides = 0;
+  Vec gfb[20];
+  std::vector<int> seqFormula;
+  std::vector<double> seqPower;
+};
+
+// CRotationMatrix::SetRotation(alfa, beta, gamma): Z(alfa), then Y(beta), then X(gamma),
+// each skipped for a zero angle (src/algebra.cpp:94-159).
+void set_rotation(double a, double b, double g, double *m, int *zero) {
+  const double id[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  memcpy(m, id, sizeof(id));
+  *zero = 1;
+  auto mulm = [&](const double r[9]) {
+    double o[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) o[3 * i + j] = m[3 * i] * r[j] + m[3 * i + 1] * r[3 + j] + m[3 * i + 2] * r[6 + j];
+    memcpy(m, o, sizeof(o));
+    *zero = 0;
+  };
+  if (a != 0.0) { const double sn = sin(a), cs = cos(a); const double r[9] = {cs, -sn, 0, sn, cs, 0, 0, 0, 1}; mulm(r); }
+  if (b != 0.0) { const double sn = sin(b), cs = cos(b); const double r[9] = {cs, 0, sn, 0, 1, 0, -sn, 0, cs}; mulm(r); }
+  if (g != 0.0) { const double sn = sin(g), cs = cos(g); const double r[9] = {1, 0, 0, 0, cs, -sn, 0, sn, cs}; mulm(r); }
+}
+
+void derive(const mbgb_scene &s, Derived &d) {
+  set_rotation(s.ifsRotationAlfa, s.ifsRotationBeta, s.ifsRotationGamma, d.ifsMain, &d.ifsMainZero);
+  for (int i = 0; i < 9; i++) set_rotation(s.ifsAlfa[i], s.ifsBeta[i], s.ifsGamma[i], d.ifsRot[i], &d.ifsRotZero[i]);
+  // face normals (src/callbacks.cpp:1557-1663)
+  const double q = 1.0 / sqrt(3.0);
+  const Vec oct[8] = {{q, q, -q}, {q, -q, q}, {-q, q, q}, {-q, -q, -q}, {q, q, q}, {-q, -q, q}, {-q, q, -q}, {q, -q, -q}};
+  const Vec cube[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  const double aa = (1.0 + sqrt(5.0)) / 2.0;
+  const double bb = 1.0 / sqrt(aa * aa + 1.0);
+  const double ff = sqrt(aa * aa + 1.0 / (aa * aa));
+  const double cc = aa / ff, dd = 1.0 / aa / ff;
+  int n = 0;
+  auto put = [&](const Vec *v, int k) {
+    for (int i = 0; i < k; i++) d.gfb[n++] = v[i];
+  };
+  switch (s.genFoldBoxType) {
+    case 1: put(cube, 6); break;
+    case 2: put(oct, 8); break;
+    case 3: {
+      const Vec v[12] = {{0, bb, aa * bb}, {0, bb, -aa * bb}, {0, -bb, aa * bb}, {0, -bb, -aa * bb},
+                         {bb, aa * bb, 0}, {bb, -aa * bb, 0}, {-bb, aa * bb, 0}, {-bb, -aa * bb, 0},
+                         {aa * bb, 0, bb}, {-aa * bb, 0, bb}, {aa * bb, 0, -bb}, {-aa * bb, 0, -bb}};
+      put(v, 12);
+      break;
+    }
+    case 4: put(oct, 8); put(cube, 6); break;
+    case 5: {
+      const Vec v[12] = {{0, dd, cc}, {0, dd, -cc}, {0, -dd, cc}, {0, -dd, -cc}, {cc, 0, dd}, {cc, 0, -dd},
+                         {-cc, 0, dd}, {-cc, 0, -dd}, {dd, cc, 0}, {dd, -cc, 0}, {-dd, cc, 0}, {-dd, -cc, 0}};
+      put(oct, 8);
+      put(v, 12);
+      break;
+    }
+    case 6: case 7: {
+      const int k = s.genFoldBoxType == 6 ? 6 : 5;
+      const double th = 3.14159 * 2.0 / (k == 6 ? 6.0 : 5.0);
+      const Vec caps[2] = {{0, 0, 1}, {0, 0, -1}};
+      put(caps, 2);
+      for (int i = 0; i < k; i++) d.gfb[n++] = Vec{cos(th * i), sin(th * i), 0};
+      break;
+    }
+    default: put(oct, 4); break;
+  }
+  d.gfbSides = n;
+  // CreateFormulaSequence
+  const int N = (int)s.N;
+  d.seqFormula.assign(N > 0 ? N : 0, 0);
+  d.seqPower.assign(N > 0 ? N : 0, 0.0);
+  if (s.formula != MBGB_FORMULA_HYBRID || N <= 0) return;
+  int number = 0, guard = 0;
+  while (number < N && guard++ < 1000000) {
+    for (int h = 0; h < 4; h++) {
+      if (s.hybridFormula[h] == 0) continue;
+      for (int i = 0; i < s.hybridIters[h]; i++) {
+        if (number < N) { d.seqFormula[number] = s.hybridFormula[h]; d.seqPower[number] = s.hybridPower[h]; }
+        number++;
+      }
+    }
+    const int end = s.hybridCyclic ? s.hybridIters[4] : N;
+    if (s.hybridFormula[4] != 0)
+      for (int i = 0; i < end; i++) {
+        if (number < N) { d.seqFormula[number] = s.hybridFormula[4]; d.seqPower[number] = s.hybridPower[4]; }
+        number++;
+      }
+  }
+}
+
 // Mutable DE state that the reference keeps in its sFractal copy.
 struct Calc {
   const mbgb_scene *s;
@@ -74,30 +174,85 @@ struct Calc {
   double detail;    // doubles.detailSize
   int itersOut;
   Cnt *cnt;
+  const Derived *d;
 };
 
-// Compute<Mode>; colour = false -> normal mode.
-double compute(const Calc &c, Vec z, bool colour, int *Lout) {
+enum { kNormal = 0, kColour = 1, kDelta1 = 3, kDelta2 = 4 };
+
+bool box_like(int f) { return f == 8 || f == 17 || f == 18 || f == 37; }
+
+// the generalized fold box's search for the nearest cutting plane along y + a l
+int gfb_search(const Derived &d, double solid, Vec y, Vec l, int skip1, int skip2, bool origin, double &a) {
+  a = 1;
+  int side = -1;
+  for (int i = 0; i < d.gfbSides; i++) {
+    if (i == skip1 || i == skip2) continue;
+    const double b = origin ? solid : solid - dot(y, d.gfb[i]);
+    const double c = dot(l, d.gfb[i]);
+    if ((c > 0) && ((a * c) > b)) { side = i; a = b / c; }
+  }
+  return side;
+}
+
+bool gfb_push(Vec &z, Vec x, double melt) {
+  const Vec t = sub(x, z);
+  if (dot(t, t) > melt * melt) {
+    const double m = len(t);
+    z = add(z, mul(t, 2 * (m - melt) / (m + .00000001)));
+    return true;
+  }
+  return false;
+}
+
+// Compute<Mode> (src/fractal.cpp:40-1241); `count` is deltaDE2's iteration count.
+double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
   const mbgb_scene &s = *c.s;
+  const Derived &dv = *c.d;
   const int N = c.N;
+  const int Nseq = (int)s.N;
   double distance = 0;
+  double w = 0, cw = 0;
   double r_dz = 1;
-  const double p = s.power;
+  double p = s.power;
   const double fR2 = s.mboxFoldingSphericalFixed * s.mboxFoldingSphericalFixed;
   const double mR2 = s.mboxFoldingSphericalMin * s.mboxFoldingSphericalMin;
   const double f1 = fR2 / mR2;
   double tDE = 1.0, tCol = 1.0;
   double scale = s.mboxScale;
-  const bool box = s.formula == MBGB_FORMULA_TGLAD || s.formula == MBGB_FORMULA_MBOX_VARY4D;
-  const bool menger = s.formula == MBGB_FORMULA_MENGER;
-  // trig_DE keeps its derivative as a vector in polar form; the 4D box keeps w
+  int form = s.formula;
+  const bool hybrid = form == MBGB_FORMULA_HYBRID;
+  // trig_DE keeps its derivative as a vector in polar form
   Vec dz{1.0, 0.0, 0.0};
-  double thdz = 0.0, phdz = 0.0, w = 0.0;
+  double thdz = 0.0, phdz = 0.0;
   Vec cst = s.juliaMode ? Vec{s.julia[0], s.julia[1], s.julia[2]} : mul(z, s.constantFactor);
   double r = len(z);
   double minv = 1e200;
+  const Vec mbOff{s.mboxOffset[0], s.mboxOffset[1], s.mboxOffset[2]};
+  const Vec ifsOff{s.ifsOffset[0], s.ifsOffset[1], s.ifsOffset[2]};
   int L;
   for (L = 0; L < N; L++) {
+    if (hybrid) {
+      const int k = L < Nseq - 1 ? L : Nseq - 1;
+      form = dv.seqFormula[k];
+      p = dv.seqPower[k];
+      scale = p;
+    }
+    if (s.ifsFoldingMode) {
+      if (s.ifsAbsX) z.x = fabs(z.x);
+      if (s.ifsAbsY) z.y = fabs(z.y);
+      if (s.ifsAbsZ) z.z = fabs(z.z);
+      for (int i = 0; i < 9; i++) {
+        if (!s.ifsEnabled[i]) continue;
+        z = rot(dv.ifsRot[i], dv.ifsRotZero[i], z);
+        const Vec dir{s.ifsDirection[i][0], s.ifsDirection[i][1], s.ifsDirection[i][2]};
+        const double l = dot(z, dir);
+        if (l < s.ifsDistance[i]) z = sub(z, mul(mul(dir, 2.0), l - s.ifsDistance[i]));
+      }
+      z = add(rot(dv.ifsMain, dv.ifsMainZero, sub(z, ifsOff)), ifsOff);
+      z = mul(z, s.ifsScale);
+      z = sub(z, mul(ifsOff, s.ifsScale - 1.0));
+      r = len(z);
+    }
     if (s.tgladFoldingMode) {
       const double fl = s.foldingLimit, fv = s.foldingValue;
       if (z.x > fl) { z.x = fv - z.x; tCol *= 0.9; } else if (z.x < -fl) { z.x = -fv - z.x; tCol *= 0.9; }
@@ -114,115 +269,435 @@ double compute(const Calc &c, Vec z, bool colour, int *Lout) {
       else if (r2 < a) { const double k2 = a / r2; z = mul(z, k2); tDE *= k2; tCol += 10; }
       r = len(z);
     }
-    if (s.formula == MBGB_FORMULA_TRIG_OPTIM) {
-      const double th0 = asin(z.z / r);
-      const double ph0 = atan2(z.y, z.x);
-      double rp = pow(r, p - 1.0);
-      const double th = th0 * p, ph = ph0 * p;
-      const double cth = cos(th);
-      r_dz = rp * r_dz * p + 1.0;
-      rp *= r;
-      z = add(mul(Vec{cth * cos(ph), cth * sin(ph), sin(th)}, rp), cst);
-      r = len(z);
-    } else if (s.formula == MBGB_FORMULA_TRIG_DE) {
-      const double r1 = pow(r, p - 1.0);
-      const double r2 = r1 * r;
-      const double th = atan2(z.y, z.x);
-      const double ph = -atan2(z.z, sqrt(z.x * z.x + z.y * z.y));
-      if (!colour) {
-        const double k = p * r1 * r_dz;
-        const double a = (p - 1.0) * th + thdz;
-        const double b = (p - 1.0) * ph + phdz;
-        dz = Vec{cos(b) * cos(a) * k + 1.0, cos(b) * sin(a) * k + 0.0, sin(b) * k + 0.0};
-        r_dz = len(dz);
-        thdz = atan2(dz.y, dz.x);
-        phdz = -atan2(dz.z, sqrt(dz.x * dz.x + dz.y * dz.y));
+    switch (form) {
+      case 1: {  // trig_DE
+        const double r1 = pow(r, p - 1.0);
+        const double r2 = r1 * r;
+        const double th = atan2(z.y, z.x);
+        const double ph = -atan2(z.z, sqrt(z.x * z.x + z.y * z.y));
+        if (mode == kNormal) {
+          const double k = p * r1 * r_dz;
+          const double a = (p - 1.0) * th + thdz;
+          const double b = (p - 1.0) * ph + phdz;
+          dz = Vec{cos(b) * cos(a) * k + 1.0, cos(b) * sin(a) * k + 0.0, sin(b) * k + 0.0};
+          r_dz = len(dz);
+          thdz = atan2(dz.y, dz.x);
+          phdz = -atan2(dz.z, sqrt(dz.x * dz.x + dz.y * dz.y));
+        }
+        z = add(mul(Vec{cos(p * ph) * cos(p * th), cos(p * ph) * sin(p * th), sin(p * ph)}, r2), cst);
+        r = len(z);
+        break;
       }
-      z = add(mul(Vec{cos(p * ph) * cos(p * th), cos(p * ph) * sin(p * th), sin(p * ph)}, r2), cst);
-      r = len(z);
-    } else if (menger) {
-      z = Vec{fabs(z.x), fabs(z.y), fabs(z.z)};
-      if (z.x - z.y < 0) std::swap(z.x, z.y);
-      if (z.x - z.z < 0) std::swap(z.x, z.z);
-      if (z.y - z.z < 0) std::swap(z.y, z.z);
-      if (colour) {
-        const double l = len(z);
-        if (l < minv) minv = l;
+      case 2: {  // trig_optim
+        const double th0 = asin(z.z / r);
+        const double ph0 = atan2(z.y, z.x);
+        double rp = pow(r, p - 1.0);
+        const double th = th0 * p, ph = ph0 * p;
+        const double cth = cos(th);
+        r_dz = rp * r_dz * p + 1.0;
+        rp *= r;
+        z = add(mul(Vec{cth * cos(ph), cth * sin(ph), sin(th)}, rp), cst);
+        r = len(z);
+        break;
       }
-      z = mul(z, 3.0);
-      z.x -= 2.0;
-      z.y -= 2.0;
-      if (z.z > 1.0) z.z -= 2.0;
-      r = len(z);
-      tDE *= 3.0;
-    } else if (s.formula == MBGB_FORMULA_MBOX_VARY4D) {
-      scale = scale + s.mboxVaryScaleVary * (fabs(scale) - 1.0);
-      const Vec o = z;
-      const double fo = s.mboxVaryFold;
-      z.x = fabs(z.x + fo) - fabs(z.x - fo) - z.x;
-      z.y = fabs(z.y + fo) - fabs(z.y - fo) - z.y;
-      z.z = fabs(z.z + fo) - fabs(z.z - fo) - z.z;
-      w = fabs(w + fo) - fabs(w - fo) - w;
-      if (z.x != o.x) tCol += s.mboxColorFactorX;
-      if (z.y != o.y) tCol += s.mboxColorFactorY;
-      if (z.z != o.z) tCol += s.mboxColorFactorZ;
-      const double rr = pow(z.x * z.x + z.y * z.y + z.z * z.z + w * w, s.mboxVaryRPower);
-      const double mr2 = s.mboxVaryMinR * s.mboxVaryMinR;
-      double m = scale;
-      if (rr < mr2) { m = scale / mr2; tCol += s.mboxColorFactorSp1; }
-      else if (rr < 1.0) { m = scale / rr; tCol += s.mboxColorFactorSp2; }
-      z = add(mul(z, m), cst);
-      w = w * m + s.mboxVaryWadd;
-      tDE = tDE * fabs(m) + 1.0;
-      r = sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
-    } else if (box) {
-      const double fl = s.mboxFoldingLimit, fv = s.mboxFoldingValue;
-      if (s.mboxRotationsEnabled) {
-        bool lock = false;
-        z = rot(s.mboxRot[0][0], s.mboxRotZero[0][0], z);
-        if (z.x > fl) { z.x = fv - z.x; tCol += s.mboxColorFactorX; lock = true; }
-        z = rot(s.mboxRotInv[0][0], 0, z);
-        z = rot(s.mboxRot[1][0], s.mboxRotZero[1][0], z);
-        if (!lock && z.x < -fl) { z.x = -fv - z.x; tCol += s.mboxColorFactorX; }
-        z = rot(s.mboxRotInv[1][0], 0, z);
-        lock = false;
-        z = rot(s.mboxRot[0][1], s.mboxRotZero[0][1], z);
-        if (z.y > fl) { z.y = fv - z.y; tCol += s.mboxColorFactorY; lock = true; }
-        z = rot(s.mboxRotInv[0][1], 0, z);
-        z = rot(s.mboxRot[1][1], s.mboxRotZero[1][1], z);
-        if (!lock && z.y < -fl) { z.y = -fv - z.y; tCol += s.mboxColorFactorY; }
-        z = rot(s.mboxRotInv[1][1], 0, z);
-        lock = false;
-        z = rot(s.mboxRot[0][2], s.mboxRotZero[0][2], z);
-        if (z.z > fl) { z.z = fv - z.z; tCol += s.mboxColorFactorZ; lock = true; }
-        z = rot(s.mboxRotInv[0][2], 0, z);
-        z = rot(s.mboxRot[1][2], s.mboxRotZero[1][2], z);
-        if (!lock && z.z < -fl) { z.z = -fv - z.z; tCol += s.mboxColorFactorZ; }
-        z = rot(s.mboxRotInv[1][2], 0, z);
-      } else {
-        if (z.x > fl) { z.x = fv - z.x; tCol += s.mboxColorFactorX; } else if (z.x < -fl) { z.x = -fv - z.x; tCol += s.mboxColorFactorX; }
-        if (z.y > fl) { z.y = fv - z.y; tCol += s.mboxColorFactorY; } else if (z.y < -fl) { z.y = -fv - z.y; tCol += s.mboxColorFactorY; }
-        if (z.z > fl) { z.z = fv - z.z; tCol += s.mboxColorFactorZ; } else if (z.z < -fl) { z.z = -fv - z.z; tCol += s.mboxColorFactorZ; }
+      case 3: case 6: {  // fast_trig, minus_fast_trig
+        const double x2 = z.x * z.x, y2 = z.y * z.y, z2 = z.z * z.z;
+        const double t = 1.0 - z2 / (x2 + y2);
+        const double nx = (x2 - y2) * t;
+        const double ny = 2.0 * z.x * z.y * t;
+        const double nz = (form == 3 ? -2.0 : 2.0) * z.z * sqrt(x2 + y2);
+        z = Vec{nx + cst.x, ny + cst.y, nz + cst.z};
+        r = len(z);
+        break;
       }
-      r = len(z);
-      const double r2 = r * r;
-      const Vec off{s.mboxOffset[0], s.mboxOffset[1], s.mboxOffset[2]};
-      z = add(z, off);
-      if (r2 < mR2) { z = mul(z, f1); tDE *= f1; tCol += s.mboxColorFactorSp1; }
-      else if (r2 < fR2) { const double f2 = fR2 / r2; z = mul(z, f2); tDE *= f2; tCol += s.mboxColorFactorSp2; }
-      z = sub(z, off);
-      z = rot(s.mboxMainRot, s.mboxMainRotZero, z);
-      z = add(mul(z, scale), cst);
-      tDE = tDE * fabs(scale) + 1.0;
-      r = len(z);
+      case 4: {  // hypercomplex
+        const Vec nz{z.x * z.x - z.y * z.y - z.z * z.z - w * w, 2.0 * z.x * z.y - 2.0 * w * z.z, 2.0 * z.x * z.z - 2.0 * z.y * w};
+        const double nw = 2.0 * z.x * w - 2.0 * z.y * z.z;
+        z = add(nz, cst);
+        w = nw;
+        r = sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
+        break;
+      }
+      case 5: {  // quaternion
+        const Vec nz{z.x * z.x - z.y * z.y - z.z * z.z - w * w, 2.0 * z.x * z.y, 2.0 * z.x * z.z};
+        const double nw = 2.0 * z.x * w;
+        z = add(nz, cst);
+        w = nw;
+        r = sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
+        break;
+      }
+      case 7: {  // menger_sponge
+        z = Vec{fabs(z.x), fabs(z.y), fabs(z.z)};
+        if (z.x - z.y < 0) std::swap(z.x, z.y);
+        if (z.x - z.z < 0) std::swap(z.x, z.z);
+        if (z.y - z.z < 0) std::swap(z.y, z.z);
+        if (mode == kColour) {
+          const double l = len(z);
+          if (l < minv) minv = l;
+        }
+        z = mul(z, 3.0);
+        z.x -= 2.0;
+        z.y -= 2.0;
+        if (z.z > 1.0) z.z -= 2.0;
+        r = len(z);
+        tDE *= 3.0;
+        break;
+      }
+      case 8: {  // tglad
+        const double fl = s.mboxFoldingLimit, fv = s.mboxFoldingValue;
+        if (s.mboxRotationsEnabled) {
+          bool lock = false;
+          z = rot(s.mboxRot[0][0], s.mboxRotZero[0][0], z);
+          if (z.x > fl) { z.x = fv - z.x; tCol += s.mboxColorFactorX; lock = true; }
+          z = rot(s.mboxRotInv[0][0], 0, z);
+          z = rot(s.mboxRot[1][0], s.mboxRotZero[1][0], z);
+          if (!lock && z.x < -fl) { z.x = -fv - z.x; tCol += s.mboxColorFactorX; }
+          z = rot(s.mboxRotInv[1][0], 0, z);
+          lock = false;
+          z = rot(s.mboxRot[0][1], s.mboxRotZero[0][1], z);
+          if (z.y > fl) { z.y = fv - z.y; tCol += s.mboxColorFactorY; lock = true; }
+          z = rot(s.mboxRotInv[0][1], 0, z);
+          z = rot(s.mboxRot[1][1], s.mboxRotZero[1][1], z);
+          if (!lock && z.y < -fl) { z.y = -fv - z.y; tCol += s.mboxColorFactorY; }
+          z = rot(s.mboxRotInv[1][1], 0, z);
+          lock = false;
+          z = rot(s.mboxRot[0][2], s.mboxRotZero[0][2], z);
+          if (z.z > fl) { z.z = fv - z.z; tCol += s.mboxColorFactorZ; lock = true; }
+          z = rot(s.mboxRotInv[0][2], 0, z);
+          z = rot(s.mboxRot[1][2], s.mboxRotZero[1][2], z);
+          if (!lock && z.z < -fl) { z.z = -fv - z.z; tCol += s.mboxColorFactorZ; }
+          z = rot(s.mboxRotInv[1][2], 0, z);
+        } else {
+          if (z.x > fl) { z.x = fv - z.x; tCol += s.mboxColorFactorX; } else if (z.x < -fl) { z.x = -fv - z.x; tCol += s.mboxColorFactorX; }
+          if (z.y > fl) { z.y = fv - z.y; tCol += s.mboxColorFactorY; } else if (z.y < -fl) { z.y = -fv - z.y; tCol += s.mboxColorFactorY; }
+          if (z.z > fl) { z.z = fv - z.z; tCol += s.mboxColorFactorZ; } else if (z.z < -fl) { z.z = -fv - z.z; tCol += s.mboxColorFactorZ; }
+        }
+        r = len(z);
+        const double r2 = r * r;
+        z = add(z, mbOff);
+        if (r2 < mR2) { z = mul(z, f1); tDE *= f1; tCol += s.mboxColorFactorSp1; }
+        else if (r2 < fR2) { const double f2 = fR2 / r2; z = mul(z, f2); tDE *= f2; tCol += s.mboxColorFactorSp2; }
+        z = sub(z, mbOff);
+        z = rot(s.mboxMainRot, s.mboxMainRotZero, z);
+        z = add(mul(z, scale), cst);
+        tDE = tDE * fabs(scale) + 1.0;
+        r = len(z);
+        break;
+      }
+      case 10: {  // kaleidoscopic
+        if (s.ifsAbsX) z.x = fabs(z.x);
+        if (s.ifsAbsY) z.y = fabs(z.y);
+        if (s.ifsAbsZ) z.z = fabs(z.z);
+        for (int i = 0; i < 9; i++) {
+          if (!s.ifsEnabled[i]) continue;
+          z = rot(dv.ifsRot[i], dv.ifsRotZero[i], z);
+          const Vec dir{s.ifsDirection[i][0], s.ifsDirection[i][1], s.ifsDirection[i][2]};
+          const double l = dot(z, dir);
+          if (l < s.ifsDistance[i]) z = sub(z, mul(dir, 2.0 * (l - s.ifsDistance[i]) * s.ifsIntensity[i]));
+        }
+        z = add(rot(dv.ifsMain, dv.ifsMainZero, sub(z, ifsOff)), ifsOff);
+        if (s.ifsEdge[0] > 0) z.x = s.ifsEdge[0] - fabs(s.ifsEdge[0] - z.x);
+        if (s.ifsEdge[1] > 0) z.y = s.ifsEdge[1] - fabs(s.ifsEdge[1] - z.y);
+        if (s.ifsEdge[2] > 0) z.z = s.ifsEdge[2] - fabs(s.ifsEdge[2] - z.z);
+        if (mode == kColour) {
+          const double l2 = len(z);
+          if (l2 < minv) minv = l2;
+        }
+        z = mul(z, s.ifsScale);
+        if (s.ifsMengerSpongeMode) {
+          z.x -= s.ifsOffset[0] * (s.ifsScale - 1.0);
+          z.y -= s.ifsOffset[1] * (s.ifsScale - 1.0);
+          if (z.z > 0.5 * s.ifsOffset[2] * (s.ifsScale - 1.0)) z.z -= s.ifsOffset[2] * (s.ifsScale - 1.0);
+        } else {
+          z = sub(z, mul(ifsOff, s.ifsScale - 1.0));
+        }
+        tDE *= s.ifsScale;
+        r = len(z);
+        break;
+      }
+      case 11: {  // xenodreambuie
+        const double rp = pow(r, p);
+        const double th = atan2(z.y, z.x);
+        double ph = acos(z.z / r);
+        if (ph > 0.5 * M_PI) ph = M_PI - ph;
+        else if (ph < -0.5 * M_PI) ph = -M_PI - ph;
+        z = add(Vec{rp * cos(th * p) * sin(ph * p), rp * sin(th * p) * sin(ph * p), rp * cos(ph * p)}, cst);
+        r = len(z);
+        break;
+      }
+      case 13: case 14: {  // mandelbulb2, mandelbulb3
+        double t, tr;
+        double sg = 1.0, sg2 = 1.0;
+        if (form == 14 && z.x < 0) sg2 = -1.0;
+        tr = sqrt(z.x * z.x + z.y * z.y);
+        z = mul(z, 1.0 / tr);
+        t = z.x * z.x - z.y * z.y;
+        z.y = 2.0 * z.x * z.y;
+        z.x = t;
+        z = mul(z, tr);
+        if (form == 13) {
+          tr = sqrt(z.y * z.y + z.z * z.z);
+          z = mul(z, 1.0 / tr);
+          t = z.y * z.y - z.z * z.z;
+          z.z = 2.0 * z.y * z.z;
+          z.y = t;
+          z = mul(z, tr);
+          tr = sqrt(z.x * z.x + z.z * z.z);
+          z = mul(z, 1.0 / tr);
+          t = z.x * z.x - z.z * z.z;
+          z.z = 2.0 * z.x * z.z;
+          z.x = t;
+          z = mul(z, tr);
+        } else {
+          if (z.x < 0) sg = -1.0;
+          tr = sqrt(z.x * z.x + z.z * z.z);
+          z = mul(z, 1.0 / tr);
+          t = z.x * z.x - z.z * z.z;
+          z.z = 2.0 * z.x * z.z * sg2;
+          z.x = t * sg;
+          z = mul(z, tr);
+        }
+        z = mul(z, r);
+        z = add(z, cst);
+        r = len(z);
+        break;
+      }
+      case 15: {  // mandelbulb4: identity, then RotateX, RotateY, RotateZ by (p - 1) x the angles
+        const double rp = pow(r, p - 1);
+        const double az = atan2(z.y, z.x), ay = atan2(z.z, z.x), ax = atan2(z.z, z.y);
+        double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        int zero = 1;
+        auto mulm = [&](const double rr[9]) {
+          double o[9];
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) o[3 * i + j] = m[3 * i] * rr[j] + m[3 * i + 1] * rr[3 + j] + m[3 * i + 2] * rr[6 + j];
+          memcpy(m, o, sizeof(o));
+          zero = 0;
+        };
+        const double a = ax * (p - 1), b = ay * (p - 1), g = az * (p - 1);
+        if (a != 0.0) { const double sn = sin(a), cs = cos(a); const double rr[9] = {1, 0, 0, 0, cs, -sn, 0, sn, cs}; mulm(rr); }
+        if (b != 0.0) { const double sn = sin(b), cs = cos(b); const double rr[9] = {cs, 0, sn, 0, 1, 0, -sn, 0, cs}; mulm(rr); }
+        if (g != 0.0) { const double sn = sin(g), cs = cos(g); const double rr[9] = {cs, -sn, 0, sn, cs, 0, 0, 0, 1}; mulm(rr); }
+        z = add(mul(rot(m, zero, z), rp), cst);
+        r = len(z);
+        break;
+      }
+      case 16: {  // foldingIntPow2
+        const double F = s.FoldingIntPowFoldFactor;
+        if (z.x > F) z.x = F * 2.0 - z.x; else if (z.x < -F) z.x = -F * 2.0 - z.x;
+        if (z.y > F) z.y = F * 2.0 - z.y; else if (z.y < -F) z.y = -F * 2.0 - z.y;
+        if (z.z > F) z.z = F * 2.0 - z.z; else if (z.z < -F) z.z = -F * 2.0 - z.z;
+        r = len(z);
+        const double rr = r * r;
+        if (rr < 0.25) z = mul(z, 1.0 / 0.25);
+        else if (rr < 1.0) z = mul(z, 1.0 / rr);
+        z = mul(z, 2.0);
+        const double x2 = z.x * z.x, y2 = z.y * z.y, z2 = z.z * z.z;
+        const double t = 1.0 - z2 / (x2 + y2);
+        z = Vec{(x2 - y2) * t + cst.x, 2.0 * z.x * z.y * t + cst.y, -2.0 * z.z * sqrt(x2 + y2) + cst.z};
+        z.z *= s.FoldingIntPowZfactor;
+        r = len(z);
+        break;
+      }
+      case 17: {  // smoothMandelbox
+        const double sm = s.mboxSharpness, fl = s.mboxFoldingLimit, fv = s.mboxFoldingValue;
+        auto gt = [&](double a, double b) { return 1.0 / (1.0 + exp(sm * (b - a))); };
+        auto lt = [&](double a, double b) { return 1.0 / (1.0 + exp(sm * (a - b))); };
+        double *comp[3] = {&z.x, &z.y, &z.z};
+        const double cf[3] = {s.mboxColorFactorX, s.mboxColorFactorY, s.mboxColorFactorZ};
+        for (int k = 0; k < 3; k++) {
+          double &v = *comp[k];
+          const double k1 = gt(v, fl), k2 = lt(v, -fl);
+          v = v * (1.0 - k1) + (fv - v) * k1;
+          v = v * (1.0 - k2) + (-fv - v) * k2;
+          tCol += (k1 + k2) * cf[k];
+        }
+        r = len(z);
+        const double r2 = r * r;
+        const double f2 = fR2 / r2;
+        const double rk1 = lt(r2, mR2), rk2 = lt(r2, fR2);
+        const double rk21 = (1.0 - rk1) * rk2;
+        z = add(mul(z, 1.0 - rk1), mul(z, f1 * rk1));
+        z = add(mul(z, 1.0 - rk21), mul(z, f2 * rk21));
+        tDE = tDE * (1.0 - rk1) + tDE * (f1 * rk1);
+        tDE = tDE * (1.0 - rk21) + tDE * (f2 * rk21);
+        tCol += rk1 * s.mboxColorFactorSp1;
+        tCol += rk21 * s.mboxColorFactorSp2;
+        z = rot(s.mboxMainRot, s.mboxMainRotZero, z);
+        z = add(mul(z, scale), cst);
+        tDE = tDE * fabs(scale) + 1.0;
+        r = len(z);
+        break;
+      }
+      case 18: {  // mandelboxVaryScale4D
+        scale = scale + s.mboxVaryScaleVary * (fabs(scale) - 1.0);
+        const Vec o = z;
+        const double fo = s.mboxVaryFold;
+        z.x = fabs(z.x + fo) - fabs(z.x - fo) - z.x;
+        z.y = fabs(z.y + fo) - fabs(z.y - fo) - z.y;
+        z.z = fabs(z.z + fo) - fabs(z.z - fo) - z.z;
+        w = fabs(w + fo) - fabs(w - fo) - w;
+        if (z.x != o.x) tCol += s.mboxColorFactorX;
+        if (z.y != o.y) tCol += s.mboxColorFactorY;
+        if (z.z != o.z) tCol += s.mboxColorFactorZ;
+        const double rr = pow(z.x * z.x + z.y * z.y + z.z * z.z + w * w, s.mboxVaryRPower);
+        const double mr2 = s.mboxVaryMinR * s.mboxVaryMinR;
+        double m = scale;
+        if (rr < mr2) { m = scale / mr2; tCol += s.mboxColorFactorSp1; }
+        else if (rr < 1.0) { m = scale / rr; tCol += s.mboxColorFactorSp2; }
+        z = add(mul(z, m), cst);
+        w = w * m + s.mboxVaryWadd;
+        tDE = tDE * fabs(m) + 1.0;
+        r = sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
+        break;
+      }
+      case 19: {  // aexion
+        if (L == 0) {
+          const double a = s.cadd;
+          const Vec c0 = cst;
+          cst = Vec{fabs(c0.x + c0.y + c0.z) + a, fabs(-c0.x - c0.y + c0.z) + a, fabs(-c0.x + c0.y - c0.z) + a};
+          cw = fabs(c0.x - c0.y - c0.z) + a;
+          const Vec z0 = z;
+          z = Vec{fabs(z0.x + z0.y + z0.z) + a, fabs(-z0.x - z0.y + z0.z) + a, fabs(-z0.x + z0.y - z0.z) + a};
+          w = fabs(z0.x - z0.y - z0.z) + a;
+        }
+        const double tx = z.x * z.x - z.y * z.y + 2.0 * w * z.z + cst.x;
+        const double ty = z.y * z.y - z.x * z.x + 2.0 * w * z.z + cst.y;
+        const double tz = z.z * z.z - w * w + 2.0 * z.x * z.y + cst.z;
+        const double tw = w * w - z.z * z.z + 2.0 * z.x * z.y + cw;
+        z = Vec{tx, ty, tz};
+        w = tw;
+        r = sqrt(z.x * z.x + z.y * z.y + z.z * z.z + w * w);
+        break;
+      }
+      case 20: {  // benesi
+        double r1 = z.y * z.y + z.z * z.z;
+        const double nx = (cst.x < 0 || z.x < sqrt(r1)) ? z.x * z.x - r1 : -z.x * z.x + r1;
+        r1 = -1.0 / sqrt(r1) * 2.0 * fabs(z.x);
+        const double ny = r1 * (z.y * z.y - z.z * z.z);
+        const double nz = r1 * 2.0 * z.y * z.z;
+        z = Vec{nx + cst.x, ny + cst.y, nz + cst.z};
+        r = len(z);
+        break;
+      }
+      case 21: {  // bristorbrot
+        const double nx = z.x * z.x - z.y * z.y - z.z * z.z;
+        const double ny = z.y * (2.0 * z.x - z.z);
+        const double nz = z.z * (2.0 * z.x + z.y);
+        z = Vec{nx + cst.x, ny + cst.y, nz + cst.z};
+        r = len(z);
+        break;
+      }
+      case 22: case 23: case 24: {  // invertX, invertY, invertZ
+        double &v = form == 22 ? z.x : (form == 23 ? z.y : z.z);
+        v = v >= 0.0 ? v * v / (fabs(v) + p) : -v * v / (fabs(v) + p);
+        r = len(z);
+        break;
+      }
+      case 25: {  // invertR
+        const double ri = r * r / (r + p);
+        z = Vec{z.x / r * ri, z.y / r * ri, z.z / r * ri};
+        r = len(z);
+        break;
+      }
+      case 26: {  // sphericalFold
+        const double rr = r * r, pp = p * p;
+        if (rr < pp) z = Vec{1.0 / pp, 1.0 / pp, 1.0 / pp};
+        else if (rr < pp * 4.0) z = Vec{1.0 / rr, 1.0 / rr, 1.0 / rr};
+        r = len(z);
+        break;
+      }
+      case 27: {  // powXYZ
+        auto pw = [&](double v) { return v >= 0 ? pow(v, p) : -pow(-v, p); };
+        z = Vec{pw(z.x), pw(z.y), pw(z.z)};
+        r = len(z);
+        break;
+      }
+      case 28: z.x *= p; r = len(z); break;
+      case 29: z.y *= p; r = len(z); break;
+      case 30: z.z *= p; r = len(z); break;
+      case 31: z.x += p; r = len(z); break;
+      case 32: z.y += p; r = len(z); break;
+      case 33: z.z += p; r = len(z); break;
+      case 34: {  // angleMultiplyX
+        const double ang = atan2(z.z, z.y) * p;
+        const double tr = sqrt(z.z * z.z + z.y * z.y);
+        z.y = tr * cos(ang);
+        z.z = tr * sin(ang);
+        r = len(z);
+        break;
+      }
+      case 35: {  // angleMultiplyY
+        const double ang = atan2(z.z, z.x) * p;
+        const double tr = sqrt(z.z * z.z + z.x * z.x);
+        z.x = tr * cos(ang);
+        z.z = tr * sin(ang);
+        r = len(z);
+        break;
+      }
+      case 36: {  // angleMultiplyZ
+        const double ang = atan2(z.y, z.x) * p;
+        const double tr = sqrt(z.x * z.x + z.y * z.y);
+        z.x = tr * cos(ang);
+        z.y = tr * sin(ang);
+        r = len(z);
+        break;
+      }
+      case 37: {  // generalizedFoldBox
+        const double solid = s.mboxSolid, melt = s.mboxMelt;
+        double a;
+        const int sm = gfb_search(dv, solid, Vec{0, 0, 0}, z, -1, -1, true, a);
+        if (sm != -1) {
+          const Vec nm = dv.gfb[sm];
+          const Vec xm = sub(z, mul(nm, dot(z, nm) - solid));
+          Vec l = sub(xm, nm);
+          Vec y = nm;
+          const int sr = gfb_search(dv, solid, y, l, sm, -1, false, a);
+          if (sr != -1) {
+            const Vec xi = add(y, mul(l, a));
+            const Vec nr = dv.gfb[sr];
+            Vec lr{nm.y * nr.z - nm.z * nr.y, -nm.x * nr.z + nm.z * nr.x, nm.x * nr.y - nm.y * nr.x};
+            double ar = (dot(z, lr) - dot(xi, lr)) / dot(lr, lr);
+            if (ar < 0) { ar = -ar; lr = mul(lr, -1); }
+            const Vec xr = add(xi, mul(lr, ar));
+            l = sub(xr, xi);
+            y = xi;
+            const int si = gfb_search(dv, solid, y, l, sm, sr, false, a);
+            if (si != -1) {
+              if (gfb_push(z, add(y, mul(l, a)), melt)) tCol += s.mboxColorFactorZ;
+            } else if (gfb_push(z, xr, melt)) {
+              tCol += s.mboxColorFactorY;
+            }
+          } else if (gfb_push(z, xm, melt)) {
+            tCol += s.mboxColorFactorX;
+          }
+        }
+        r = len(z);
+        const double r2 = r * r;
+        z = add(z, mbOff);
+        if (r2 < mR2) { z = mul(z, f1); tDE *= f1; tCol += s.mboxColorFactorSp1; }
+        else if (r2 < fR2) { const double f2 = fR2 / r2; z = mul(z, f2); tDE *= f2; tCol += s.mboxColorFactorSp2; }
+        z = sub(z, mbOff);
+        z = rot(s.mboxMainRot, s.mboxMainRotZero, z);
+        z = add(mul(z, scale), cst);
+        tDE = tDE * fabs(scale) + 1.0;
+        r = len(z);
+        break;
+      }
+      default: break;
     }
-    if (menger) {
+    if (mode == kDelta1) {
+      if (r > 1e10) break;
+    } else if (mode == kDelta2) {
+      if (L == count) break;
+    }
+    if (form == 7 || form == 10) {
       if (r > 1000) { distance = (r - 2.0) / tDE; break; }
-    } else if (box) {
+    } else if (box_like(form)) {
       if (r > 1024) { distance = r / fabs(tDE); break; }
-    } else if (!colour) {
+    } else if (mode == kNormal) {
       if (r > 1e2) { distance = 0.5 * r * log(r) / r_dz; break; }
-    } else {
+    } else if (mode == kColour) {
       distance = len(z);
       if (distance < minv) minv = distance;
       if (distance > 1e15) { distance = minv; break; }
@@ -231,12 +706,19 @@ double compute(const Calc &c, Vec z, bool colour, int *Lout) {
   c.cnt->orbit += (uint64_t)(L + 1);
   c.cnt->calls++;
   if (Lout) *Lout = L;
-  if (!colour) {
+  if (mode == kNormal) {
     if (L == N) distance = 0;
     return distance;
   }
-  if (box) return tCol * 100.0 + len(z) * s.mboxColorFactorR;
-  if (menger) return minv * 1000.0;
+  if (mode == kDelta1 || mode == kDelta2) return r;
+  if (hybrid) {
+    if (minv > 100) minv = 100;
+    if (distance > 20) distance = 20;
+    if (tCol > 1000) tCol = 1000;
+    return distance * 5000.0 + tCol * 100.0 + minv * 1000.0;
+  }
+  if (box_like(form)) return tCol * 100.0 + len(z) * s.mboxColorFactorR;
+  if (form == 7 || form == 10) return minv * 1000.0;
   return distance * 5000.0;
 }
 
@@ -255,10 +737,36 @@ double calculate_distance(Calc &c, Vec p, bool *max_iter) {
     }
   }
   int L;
-  double d = compute(c, p, false, &L);
-  if (max_iter) *max_iter = (L == c.N);
-  c.itersOut = L;
-  if (d < 0) d = 0;
+  double d;
+  int retval;
+  if (s.analitycDE) {
+    d = compute(c, p, kNormal, 0, &L);
+    retval = L;
+    if (max_iter) *max_iter = (L == c.N);
+    c.itersOut = L;
+    if (d < 0) d = 0;
+  } else {
+    // delta-DE: forward differences of the escape radius (src/fractal.cpp:1308-1381)
+    const double h = 1e-10;
+    const double r = compute(c, p, kDelta1, 0, &L);
+    retval = L;
+    c.itersOut = L;
+    p.x += h; p.y += 0; p.z += 0;
+    const double d1 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
+    p.x -= h; p.y += h; p.z += 0;
+    const double d2 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
+    p.x += 0; p.y -= h; p.z += h;
+    const double d3 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
+    const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+    d = s.linearDEmode ? 0.5 * r / dr : 0.5 * r * log(r) / dr;
+    if (d < 0) d = 0;
+    if (retval == c.N) {
+      if (max_iter) *max_iter = true;
+      d = 0;
+    } else if (max_iter) {
+      *max_iter = false;
+    }
+  }
   if (L < c.minN && d < c.detail) d = c.detail;
   if (s.interiorMode && !c.normalMode) {
     if (d < 0.5 * c.detail || L == c.N) {
@@ -271,7 +779,7 @@ double calculate_distance(Calc &c, Vec p, bool *max_iter) {
       if (max_iter) *max_iter = false;
     }
   }
-  if (s.iterThresh && L < c.N) {
+  if (s.iterThresh && retval < c.N) {
     if (d < c.detail) d = c.detail * 1.01;
   }
   if (s.limits_enabled && limit < c.detail) d = d > limit ? d : limit;
@@ -501,7 +1009,7 @@ void index_to_colour(const mbgb_scene &s, int index, int out[3]) {
 Vec surface_colour(const mbgb_scene &s, Calc &c, Vec p) {
   const int N0 = c.N;
   c.N = (int)(s.N * 10);
-  int nr = to_i32(floor(compute(c, p, true, nullptr)));
+  int nr = to_i32(floor(compute(c, p, kColour, 0, nullptr)));
   c.N = N0;
   // abs(nrCol) % (248 * 256): the reference binary takes the magnitude as unsigned,
   // so an out-of-range conversion (INT_MIN) yields 2^31 % 63488 = 2048.
@@ -603,10 +1111,12 @@ struct Frame {
   Vec start, light;
   std::vector<Vec> aoDirs;
   bool exact = false;   // level-set refinement of hits (oracle_render_exact)
+  Derived d;
 };
 
 void setup_frame(const mbgb_scene &s, Frame &f) {
   f.s = &s;
+  derive(s, f.d);
   // RotateZ(alpha) * RotateX(beta) * RotateY(gamma), identity short-cut when all zero
   double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   int zero = 1;
@@ -665,7 +1175,7 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     v = {x2 * fov, 1.0, z2 * fov};
   }
   const Vec view = rot(f.rm, f.rzero, v);
-  Calc c{&s, (int)s.N, s.minN, false, 0.0, 0, &cnt};
+  Calc c{&s, (int)s.N, s.minN, false, 0.0, 0, &cnt, &f.d};
   Ray ray{};
   if (!cut) ray = ray_marching(s, c, f.start, view, buf, jitter, cnt);
   bool levelMissed = false;
@@ -745,7 +1255,9 @@ extern "C" {
 void oracle_distance(const mbgb_scene *s, const double *pts, const double *detail, long n, double *dist, int *iters,
                      unsigned char *max_iter) {
   Cnt cnt;
-  Calc c{s, (int)s->N, s->minN, false, 0.0, -1, &cnt};
+  Derived dv;
+  derive(*s, dv);
+  Calc c{s, (int)s->N, s->minN, false, 0.0, -1, &cnt, &dv};
   for (long i = 0; i < n; i++) {
     c.detail = detail[i];
     c.itersOut = -1;
@@ -759,8 +1271,10 @@ void oracle_distance(const mbgb_scene *s, const double *pts, const double *detai
 // Compute<colouring> with N x 10, as SurfaceColour calls it.
 void oracle_colour_value(const mbgb_scene *s, const double *pts, long n, double *out) {
   Cnt cnt;
-  Calc c{s, (int)(s->N * 10), s->minN, false, 0.0, 0, &cnt};
-  for (long i = 0; i < n; i++) out[i] = compute(c, Vec{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]}, true, nullptr);
+  Derived dv;
+  derive(*s, dv);
+  Calc c{s, (int)(s->N * 10), s->minN, false, 0.0, 0, &cnt, &dv};
+  for (long i = 0; i < n; i++) out[i] = compute(c, Vec{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]}, kColour, 0, nullptr);
 }
 
 // Renders rows [row0, row1) with `threads` workers pulling rows from a shared

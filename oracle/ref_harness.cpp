@@ -67,6 +67,85 @@ sRGB rgb(const mbgb_rgb &c) {
 }
 CVector3 v3(const double *d) { return CVector3(d[0], d[1], d[2]); }
 
+// RecalculateIFSParams' face-normal tables of the generalized fold box (restated: the
+// function lives in the GTK-bound src/callbacks.cpp). Only the table of the scene's type
+// is filled, with the sides count the formula reads for it.
+void set_fold_box(sFractalGeneralizedFoldBox &g, int type) {
+  g.type = (enumGeneralizedFoldBoxType)type;
+  const double q = 1.0 / sqrt(3.0);
+  const CVector3 oct[8] = {CVector3(q, q, -q), CVector3(q, -q, q), CVector3(-q, q, q), CVector3(-q, -q, -q),
+                           CVector3(q, q, q), CVector3(-q, -q, q), CVector3(-q, q, -q), CVector3(q, -q, -q)};
+  const CVector3 cube[6] = {CVector3(1, 0, 0), CVector3(-1, 0, 0), CVector3(0, 1, 0),
+                            CVector3(0, -1, 0), CVector3(0, 0, 1), CVector3(0, 0, -1)};
+  for (int i = 0; i < 4; i++) g.Nv_tet[i] = oct[i];
+  g.sides_tet = 4;
+  for (int i = 0; i < 6; i++) g.Nv_cube[i] = cube[i];
+  g.sides_cube = 6;
+  for (int i = 0; i < 8; i++) g.Nv_oct[i] = oct[i];
+  g.sides_oct = 8;
+  for (int i = 0; i < 8; i++) g.Nv_oct_cube[i] = oct[i];
+  for (int i = 0; i < 6; i++) g.Nv_oct_cube[8 + i] = cube[i];
+  g.sides_oct_cube = 14;
+  const double aa = ((1.0 + sqrt(5.0)) / 2.0);
+  const double bb = (1.0 / sqrt(aa * aa + 1.0));
+  const CVector3 dod[12] = {CVector3(0, bb, aa * bb), CVector3(0, bb, -aa * bb), CVector3(0, -bb, aa * bb),
+                            CVector3(0, -bb, -aa * bb), CVector3(bb, aa * bb, 0), CVector3(bb, -aa * bb, 0),
+                            CVector3(-bb, aa * bb, 0), CVector3(-bb, -aa * bb, 0), CVector3(aa * bb, 0, bb),
+                            CVector3(-aa * bb, 0, bb), CVector3(aa * bb, 0, -bb), CVector3(-aa * bb, 0, -bb)};
+  for (int i = 0; i < 12; i++) g.Nv_dodeca[i] = dod[i];
+  g.sides_dodeca = 12;
+  const double ff = sqrt(aa * aa + 1.0 / (aa * aa));
+  const double cc = aa / ff;
+  const double dd = 1.0 / aa / ff;
+  const CVector3 ico[12] = {CVector3(0, dd, cc), CVector3(0, dd, -cc), CVector3(0, -dd, cc), CVector3(0, -dd, -cc),
+                            CVector3(cc, 0, dd), CVector3(cc, 0, -dd), CVector3(-cc, 0, dd), CVector3(-cc, 0, -dd),
+                            CVector3(dd, cc, 0), CVector3(dd, -cc, 0), CVector3(-dd, cc, 0), CVector3(-dd, -cc, 0)};
+  for (int i = 0; i < 8; i++) g.Nv_icosa[i] = oct[i];
+  for (int i = 0; i < 12; i++) g.Nv_icosa[8 + i] = ico[i];
+  g.sides_icosa = 20;
+  const double tha = 3.14159 * 2.0 / 6.0;
+  g.Nv_box6[0] = CVector3(0, 0, 1);
+  g.Nv_box6[1] = CVector3(0, 0, -1);
+  for (int i = 0; i < 6; i++) g.Nv_box6[2 + i] = CVector3(cos(tha * i), sin(tha * i), 0);
+  g.sides_box6 = 8;
+  const double tha5 = 3.14159 * 2.0 / 5.0;
+  g.Nv_box5[0] = CVector3(0, 0, 1);
+  g.Nv_box5[1] = CVector3(0, 0, -1);
+  for (int i = 0; i < 5; i++) g.Nv_box5[2 + i] = CVector3(cos(tha5 * i), sin(tha5 * i), 0);
+  g.sides_box5 = 7;
+}
+
+// CreateFormulaSequence (restated from the GTK-bound src/callbacks.cpp:1666-1702; the loop
+// is bounded here, where the reference's would not end for a sequence without iterations).
+void make_formula_sequence(sFractal &f) {
+  const int N = (int)f.doubles.N;
+  f.formulaSequence.resize(N);
+  f.hybridPowerSequence.resize(N);
+  int number = 0, guard = 0;
+  while (number < N && guard++ < 1000000) {
+    for (int h = 0; h < HYBRID_COUNT - 1; ++h) {
+      if (f.hybridFormula[h] == none) continue;
+      for (int i = 0; i < f.hybridIters[h]; ++i) {
+        if (number < N) {
+          f.formulaSequence[number] = f.hybridFormula[h];
+          f.hybridPowerSequence[number] = f.doubles.hybridPower[h];
+        }
+        number++;
+      }
+    }
+    int end = N;
+    if (f.hybridCyclic) end = f.hybridIters[HYBRID_COUNT - 1];
+    if (f.hybridFormula[HYBRID_COUNT - 1] != none)
+      for (int i = 0; i < end; i++) {
+        if (number < N) {
+          f.formulaSequence[number] = f.hybridFormula[HYBRID_COUNT - 1];
+          f.hybridPowerSequence[number] = f.doubles.hybridPower[HYBRID_COUNT - 1];
+        }
+        number++;
+      }
+  }
+}
+
 // mbgb_scene -> sParamRender (only what the hot path reads is relevant).
 sParamRender *make_params(const mbgb_scene &s) {
   sParamRender *pp = new sParamRender();
@@ -104,6 +183,35 @@ sParamRender *make_params(const mbgb_scene &s) {
   f.interiorMode = s.interiorMode; f.linearDEmode = s.linearDEmode; f.constantDEThreshold = s.constantDEThreshold;
   f.normalCalculationMode = false; f.formula = (enumFractalFormula)s.formula; f.frameNo = s.frameNo;
   f.IFS.foldingMode = s.ifsFoldingMode;
+  // kaleidoscopic IFS (sFractalIFS, src/fractal.h:102-148)
+  sFractalIFS &ifs = f.IFS;
+  ifs.doubles.rotationAlfa = s.ifsRotationAlfa; ifs.doubles.rotationBeta = s.ifsRotationBeta;
+  ifs.doubles.rotationGamma = s.ifsRotationGamma; ifs.doubles.scale = s.ifsScale;
+  ifs.doubles.offset = v3(s.ifsOffset); ifs.doubles.edge = v3(s.ifsEdge);
+  ifs.absX = s.ifsAbsX; ifs.absY = s.ifsAbsY; ifs.absZ = s.ifsAbsZ; ifs.mengerSpongeMode = s.ifsMengerSpongeMode;
+  for (int i = 0; i < IFS_VECTOR_COUNT; i++) {
+    ifs.doubles.distance[i] = s.ifsDistance[i]; ifs.doubles.intensity[i] = s.ifsIntensity[i];
+    ifs.doubles.alfa[i] = s.ifsAlfa[i]; ifs.doubles.beta[i] = s.ifsBeta[i]; ifs.doubles.gamma[i] = s.ifsGamma[i];
+    // mbgb_scene_finalize already normalised the directions, as RecalculateIFSParams does once
+    ifs.doubles.direction[i] = v3(s.ifsDirection[i]);
+    ifs.enabled[i] = s.ifsEnabled[i];
+  }
+  // RecalculateIFSParams, IFS part (src/callbacks.cpp:1538-1547)
+  ifs.mainRot.SetRotation(ifs.doubles.rotationAlfa, ifs.doubles.rotationBeta, ifs.doubles.rotationGamma);
+  for (int i = 0; i < IFS_VECTOR_COUNT; i++)
+    ifs.rot[i].SetRotation(ifs.doubles.alfa[i], ifs.doubles.beta[i], ifs.doubles.gamma[i]);
+  // generalized fold box normals (src/callbacks.cpp:1557-1663)
+  set_fold_box(f.genFoldBox, s.genFoldBoxType);
+  f.doubles.FoldingIntPowZfactor = s.FoldingIntPowZfactor;
+  f.doubles.FoldingIntPowFoldFactor = s.FoldingIntPowFoldFactor;
+  // hybrid sequence (CreateFormulaSequence, src/callbacks.cpp:1666-1702)
+  for (int i = 0; i < HYBRID_COUNT; i++) {
+    f.hybridFormula[i] = (enumFractalFormula)s.hybridFormula[i];
+    f.hybridIters[i] = s.hybridIters[i];
+    f.doubles.hybridPower[i] = s.hybridPower[i];
+  }
+  f.hybridCyclic = s.hybridCyclic;
+  make_formula_sequence(f);
   sFractalMandelboxD &m = f.mandelbox.doubles;
   for (int c = 0; c < 3; c++) m.rotationMain[c] = s.mboxRotationMain[c];
   for (int a2 = 0; a2 < 2; a2++)
@@ -116,6 +224,7 @@ sParamRender *make_params(const mbgb_scene &s) {
   m.offset = v3(s.mboxOffset);
   m.vary4D.fold = s.mboxVaryFold; m.vary4D.minR = s.mboxVaryMinR; m.vary4D.scaleVary = s.mboxVaryScaleVary;
   m.vary4D.wadd = s.mboxVaryWadd; m.vary4D.rPower = s.mboxVaryRPower;
+  m.sharpness = s.mboxSharpness; m.solid = s.mboxSolid; m.melt = s.mboxMelt;
   f.mandelbox.rotationsEnabled = s.mboxRotationsEnabled;
   // RecalculateIFSParams, Mandelbox part (src/callbacks.cpp:1549-1556)
   f.mandelbox.mainRot.SetRotation(m.rotationMain);

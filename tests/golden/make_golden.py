@@ -16,7 +16,9 @@ the tests rebuild the exact input without the reference tree.
 
     python tests/golden/make_golden.py          # everything
     python tests/golden/make_golden.py post     # the post-processing fixtures only
-    python tests/golden/make_golden.py formulas # the run-time formulas' fixtures only
+    python tests/golden/make_golden.py formulas # the trig_DE / menger / vary4D fixtures only
+    python tests/golden/make_golden.py all_formulas # every other formula: DE fixtures, example
+                                                # scenes (share/examples) and synthetic scenes
 """
 from __future__ import annotations
 
@@ -99,6 +101,177 @@ FORMULA_CASES = {
 FORMULA_DE = (("trigde", "mandelbulb_640x480", {"formula": 1}, 1.6),
               ("menger", "mandelbulb_640x480", {"formula": 7, "N": 50}, 1.5),
               ("vary4d", "mandelbox_1080p", {**W.VARY4D, "mandelbox_scale": 2.0}, 4.0))
+
+
+# Example scenes of the reference (share/examples/*.fract, read through this build's settings
+# loader after share/defaults) at 48 x 32 with SSAO off; a few get one feature switched off
+# that this build does not render (the override is recorded in the fixture). The fixture
+# stores the loaded scene as bytes, so the tests need neither the reference tree nor the files.
+EXAMPLES = {
+    "ifs_sierpinski": ("IFS Sierpinski.fract", {}),
+    "ifs_icosahedron": ("IFS Icosahedron.fract", {}),
+    "ifs_dodecahedron": ("IFS Dodecahedron.fract", {}),
+    "ifs_trees": ("IFS Trees.fract", {}),
+    "hybrid_1": ("Hybrid 1.fract", {}),
+    "hybrid_3": ("Hybrid 3.fract", {}),
+    "hybrid_4": ("Hybrid 4.fract", {}),
+    "hybrid_foldintpow2": ("FoldIntPow2 2.fract", {"raytraced_reflections": 0, "reflect": 0}),
+    "modified_mandelbulb_1": ("modified mandelbulb 1.fract", {}),
+    "modified_mandelbulb_2": ("modified mandelbulb 2.fract", {}),
+    "modified_mandelbulb_3": ("modified mandelbulb 3.fract", {}),
+    "power2_default": ("power 2 - default.fract", {}),
+    "power2_limits": ("power 2 - limits.fract", {}),
+    "quaternion_lathe": ("quaternion - lathe.fract", {}),
+    "xenodreambuie": ("xenodreambuie's formula.fract", {}),
+    "hypercomplex_ao": ("hypercomplex - ambient occlusion.fract", {"slow_shading": 0}),
+    "spherical_folding_menger": ("spherical folding - menger sponge.fract", {}),
+    "folded_trigonometric": ("Folded trigonometric power 8.fract", {}),
+    "rotated_mandelbox_1": ("rotated mandelbox 1.fract", {}),
+    "stereo_hybrid": ("stereo.fract", {}),
+}
+
+# Formulas no example uses, on the benchmark workloads' settings.
+SYNTH_CASES = {
+    "smooth_mandelbox": ("mandelbox_1080p", 48, 32, {"formula": 17, "mandelbox_sharpness": 3,
+                                                     "ambient_occlusion_enabled": 0}),
+    "fold_box_icosa": ("mandelbox_1080p", 48, 32, {"formula": 37, "mandelbox_fold_mode": 5, "mandelbox_solid": 1,
+                                                   "mandelbox_melt": 0, "ambient_occlusion_enabled": 0}),
+    "fold_box_prism6_melt": ("mandelbox_1080p", 48, 32, {"formula": 37, "mandelbox_fold_mode": 6,
+                                                         "mandelbox_solid": 1, "mandelbox_melt": 0.1,
+                                                         "ambient_occlusion_enabled": 0}),
+    "fold_box_dodeca_oct_cube": ("mandelbox_1080p", 48, 32, {"formula": 37, "mandelbox_fold_mode": 3,
+                                                             "mandelbox_solid": 0.9, "mandelbox_melt": 0,
+                                                             "ambient_occlusion_enabled": 0,
+                                                             "view_point_y": -14.0}),
+    "aexion": ("mandelbulb_640x480", 40, 32, {"formula": 19, "c_add": -1.3, "N": 20, "view_point_y": -4.0}),
+    "benesi": ("mandelbulb_640x480", 40, 32, {"formula": 20, "N": 30}),
+    "bristorbrot": ("mandelbulb_640x480", 40, 32, {"formula": 21, "N": 30}),
+    "hybrid_modifiers": ("mandelbulb_640x480", 40, 32,
+                         {"formula": 12, "hybrid_formula_1": 25, "hybrid_power_1": 0.2, "hybrid_iterations_1": 1,
+                          "hybrid_formula_2": 36, "hybrid_power_2": 1.5, "hybrid_iterations_2": 1,
+                          "hybrid_formula_3": 27, "hybrid_power_3": 1.1, "hybrid_iterations_3": 1,
+                          "hybrid_formula_4": 31, "hybrid_power_4": 0.05, "hybrid_iterations_4": 1,
+                          "hybrid_formula_5": 2, "hybrid_power_5": 8, "hybrid_iterations_5": 2,
+                          "hybrid_cyclic": 1, "N": 40}),
+}
+
+# DE fixtures of every run-time formula: (name, workload or example, keys, half-size of the
+# seeded point cube, points)
+FORMULA_DE_ALL = (
+    ("fasttrig", "mandelbulb_640x480", {"formula": 3}, 1.6),
+    ("hypercomplex", "mandelbulb_640x480", {"formula": 4}, 1.6),
+    ("quaternion", "mandelbulb_640x480", {"formula": 5}, 1.6),
+    ("minusfasttrig", "mandelbulb_640x480", {"formula": 6}, 1.6),
+    ("kaleidoscopic", "example:IFS Icosahedron.fract", {}, 2.0),
+    ("ifsfold_bulb", "mandelbulb_640x480",
+     {"IFS_folding_mode": 1, "IFS_scale": 1.0, "IFS_0_x": 1, "IFS_0_y": 0.3, "IFS_0_z": 0.1, "IFS_0_distance": 0.2,
+      "IFS_0_enabled": 1, "IFS_0_alfa": 0.3, "IFS_absZ": 1, "IFS_rot_beta": 0.1}, 1.6),
+    ("xenodreambuie", "mandelbulb_640x480", {"formula": 11}, 1.6),
+    ("mandelbulb2", "mandelbulb_640x480", {"formula": 13}, 1.6),
+    ("mandelbulb3", "mandelbulb_640x480", {"formula": 14}, 1.6),
+    ("mandelbulb4", "mandelbulb_640x480", {"formula": 15}, 1.6),
+    ("foldingintpow2", "mandelbulb_640x480", {"formula": 16, "FoldingIntPow_folding_factor": 2,
+                                              "FoldingIntPow_z_factor": 5}, 1.6),
+    ("smoothmandelbox", "mandelbox_1080p", {"formula": 17, "mandelbox_sharpness": 3}, 4.0),
+    ("aexion", "mandelbulb_640x480", {"formula": 19, "c_add": -1.3}, 1.6),
+    ("benesi", "mandelbulb_640x480", {"formula": 20}, 1.6),
+    ("bristorbrot", "mandelbulb_640x480", {"formula": 21}, 1.6),
+    ("foldbox_tet", "mandelbox_1080p", {"formula": 37, "mandelbox_fold_mode": 0, "mandelbox_solid": 1,
+                                        "mandelbox_melt": 0}, 4.0),
+    ("foldbox_cube_melt", "mandelbox_1080p", {"formula": 37, "mandelbox_fold_mode": 1, "mandelbox_solid": 1,
+                                              "mandelbox_melt": 0.2}, 4.0),
+    ("foldbox_oct", "mandelbox_1080p", {"formula": 37, "mandelbox_fold_mode": 2, "mandelbox_solid": 1,
+                                        "mandelbox_melt": 0}, 4.0),
+    ("foldbox_octcube", "mandelbox_1080p", {"formula": 37, "mandelbox_fold_mode": 4, "mandelbox_solid": 1.1,
+                                            "mandelbox_melt": 0.05}, 4.0),
+    ("foldbox_icosa", "mandelbox_1080p", {"formula": 37, "mandelbox_fold_mode": 5, "mandelbox_solid": 1,
+                                          "mandelbox_melt": 0}, 4.0),
+    ("foldbox_prism5", "mandelbox_1080p", {"formula": 37, "mandelbox_fold_mode": 7, "mandelbox_solid": 1,
+                                           "mandelbox_melt": 0}, 4.0),
+    ("hybrid_box_fasttrig", "example:Hybrid 1.fract", {}, 3.0),
+    ("hybrid_modifiers_a", "mandelbulb_640x480",
+     {"formula": 12, "hybrid_formula_1": 22, "hybrid_power_1": 0.3, "hybrid_iterations_1": 1,
+      "hybrid_formula_2": 23, "hybrid_power_2": 0.2, "hybrid_iterations_2": 1,
+      "hybrid_formula_3": 24, "hybrid_power_3": 0.1, "hybrid_iterations_3": 1,
+      "hybrid_formula_4": 26, "hybrid_power_4": 0.1, "hybrid_iterations_4": 1,
+      "hybrid_formula_5": 2, "hybrid_power_5": 8, "hybrid_iterations_5": 3, "hybrid_cyclic": 1}, 1.6),
+    ("hybrid_modifiers_b", "mandelbulb_640x480",
+     {"formula": 12, "hybrid_formula_1": 28, "hybrid_power_1": 1.1, "hybrid_iterations_1": 1,
+      "hybrid_formula_2": 29, "hybrid_power_2": 0.9, "hybrid_iterations_2": 1,
+      "hybrid_formula_3": 30, "hybrid_power_3": 1.05, "hybrid_iterations_3": 2,
+      "hybrid_formula_4": 32, "hybrid_power_4": 0.1, "hybrid_iterations_4": 1,
+      "hybrid_formula_5": 3, "hybrid_power_5": 2, "hybrid_iterations_5": 2, "hybrid_cyclic": 0}, 1.6),
+    ("hybrid_modifiers_c", "mandelbulb_640x480",
+     {"formula": 12, "hybrid_formula_1": 33, "hybrid_power_1": -0.1, "hybrid_iterations_1": 1,
+      "hybrid_formula_2": 34, "hybrid_power_2": 2, "hybrid_iterations_2": 1,
+      "hybrid_formula_3": 35, "hybrid_power_3": 2, "hybrid_iterations_3": 1,
+      "hybrid_formula_4": 25, "hybrid_power_4": 0.4, "hybrid_iterations_4": 1,
+      "hybrid_formula_5": 1, "hybrid_power_5": 8, "hybrid_iterations_5": 2, "hybrid_cyclic": 1}, 1.6),
+    ("hybrid_modifiers_d", "mandelbulb_640x480",
+     {"formula": 12, "hybrid_formula_1": 27, "hybrid_power_1": 1.2, "hybrid_iterations_1": 1,
+      "hybrid_formula_2": 31, "hybrid_power_2": 0.2, "hybrid_iterations_2": 1,
+      "hybrid_formula_3": 8, "hybrid_power_3": 2, "hybrid_iterations_3": 2,
+      "hybrid_formula_4": 0, "hybrid_formula_5": 10, "hybrid_power_5": 2, "hybrid_iterations_5": 1,
+      "hybrid_cyclic": 1, "IFS_scale": 2, "IFS_offsetX": 1, "IFS_offsetY": 1, "IFS_offsetZ": 1,
+      "IFS_absX": 1, "IFS_absY": 1, "IFS_absZ": 1}, 2.0),
+)
+
+DEFAULTS_FILE = "/root/reference/share/defaults"
+EXAMPLES_DIR = "/root/reference/share/examples"
+
+
+def example_scene(fname: str, extra: dict, w: int = 48, h: int = 32):
+    ov = [f"image_width {w}", f"image_height {h}", "post_SSAO_enabled 0"]
+    ov += [f"{k} {v}" for k, v in extra.items()]
+    return mb.load_settings(os.path.join(EXAMPLES_DIR, fname), DEFAULTS_FILE, ov)
+
+
+def render_example_cases(lib, manifest: dict):
+    for case, (fname, extra) in EXAMPLES.items():
+        sc = example_scene(fname, extra)
+        ok, why = mb.supported(sc)
+        assert ok, (case, why)
+        w, h = sc.image_width, sc.image_height
+        img = mb.CImage.empty(w, h)
+        lib.ref_render(ctypes.byref(sc), 0, h, 0, ctypes.byref(img.as_c()))
+        out = os.path.join(HERE, f"render_ex_{case}.npz")
+        np.savez_compressed(out, scene=np.frombuffer(mb.scene_bytes(sc), np.uint8),
+                            example=np.array(fname), overrides=np.array(json.dumps(extra)),
+                            image_float=img.image_float, zbuffer=img.zbuffer, alpha=img.alpha, opacity=img.opacity,
+                            colour=img.colour, hit=img.hit, iters=img.iters, depth=img.depth)
+        manifest[os.path.basename(out)] = {"example": fname, "size": [w, h], "overrides": extra,
+                                           "formula": int(sc.formula), "hit_fraction": float(img.hit.mean())}
+        print(case, "formula", sc.formula, "hit", img.hit.mean())
+
+
+def formula_de_all(lib, manifest: dict, npts: int = 400):
+    for i, (name, wl, extra, half) in enumerate(FORMULA_DE_ALL):
+        rng = np.random.default_rng(100 + i)
+        if wl.startswith("example:"):
+            sc = example_scene(wl[8:], extra, 64, 48)
+        else:
+            keys = dict(W.WORKLOADS[wl])
+            keys["image_width"], keys["image_height"] = 64, 48
+            keys["perspective"] = W.fov_persp(64, 48)
+            keys.update(extra)
+            sc = W.make_scene(keys)
+        pts = np.ascontiguousarray(rng.uniform(-half, half, (npts, 3)))
+        detail = np.ascontiguousarray(10.0 ** rng.uniform(-6, -2, npts))
+        dist = np.zeros(npts)
+        iters = np.zeros(npts, np.int32)
+        mi = np.zeros(npts, np.uint8)
+        lib.ref_distance(ctypes.byref(sc), ptr(pts), ptr(detail), ctypes.c_long(npts), ptr(dist), ptr(iters),
+                         ptr(mi))
+        colour = np.zeros(npts)
+        lib.ref_colour_value(ctypes.byref(sc), ptr(pts), ctypes.c_long(npts), ptr(colour))
+        out = os.path.join(HERE, f"de_{name}.npz")
+        np.savez_compressed(out, scene=np.frombuffer(mb.scene_bytes(sc), np.uint8), points=pts, detail=detail,
+                            dist=dist, iters=iters, max_iter=mi, colour=colour)
+        manifest[os.path.basename(out)] = {"source": wl, "points": npts, "keys": extra,
+                                           "formula": int(sc.formula), "analytic": int(sc.analitycDE),
+                                           "max_iter_fraction": float(mi.mean())}
+        print(name, "formula", sc.formula, "analytic", sc.analitycDE, "max_iter", mi.mean(),
+              "iters", np.bincount(iters).nonzero()[0][:8])
 
 
 def build_ref() -> ctypes.CDLL:
@@ -241,6 +414,14 @@ def formula_goldens(manifest: dict):
     render_cases(lib, FORMULA_CASES, manifest)
 
 
+def all_formula_goldens(manifest: dict):
+    """Every other formula: DE fixtures, example scenes and synthetic scenes."""
+    lib = build_ref()
+    formula_de_all(lib, manifest)
+    render_example_cases(lib, manifest)
+    render_cases(lib, SYNTH_CASES, manifest)
+
+
 def render_cases(lib, cases: dict, manifest: dict):
     for case, (wl, w, h, extra) in cases.items():
         keys = dict(W.WORKLOADS[wl])
@@ -261,10 +442,10 @@ def render_cases(lib, cases: dict, manifest: dict):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["post"], ["formulas"]):
+    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"]):
         with open(os.path.join(HERE, "MANIFEST.json")) as f:
             manifest = json.load(f)
-        (post_goldens if sys.argv[1] == "post" else formula_goldens)(manifest)
+        {"post": post_goldens, "formulas": formula_goldens, "all_formulas": all_formula_goldens}[sys.argv[1]](manifest)
         with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
             json.dump(manifest, f, indent=1, sort_keys=True)
     else:

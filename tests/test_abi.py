@@ -31,7 +31,7 @@ def test_null_arguments_are_rejected(mblib):
 
 def test_unsupported_features_are_reported(mblib):
     from mandelbulber_gb300 import workloads as W
-    for key, value, text in [("formula", 10, "formula"), ("IFS_folding_mode", 1, "IFS"),
+    for key, value, text in [("formula", 38, "formula"),
                              ("primitive_plane_enabled", 1, "primitive"), ("reflect", 0.5, "environment"),
                              ("iteration_fog_enable", 1, "iteration fog"), ("aux_light_number", 3, "auxiliary")]:
         sc = W.workload("mandelbulb_640x480", **{key: value})

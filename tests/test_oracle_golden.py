@@ -22,7 +22,10 @@ def _scene(z):
     return mb.scene_from_bytes(z["scene"].tobytes())
 
 
-@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox", "trigde", "menger", "vary4d"])
+DES = sorted(os.path.basename(p)[3:-4] for p in glob.glob(os.path.join(GOLDEN, "de_*.npz")))
+
+
+@pytest.mark.parametrize("formula", DES)
 def test_distance_estimator_bit_exact(oracle, mblib, formula):
     z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
     sc = _scene(z)
@@ -32,7 +35,7 @@ def test_distance_estimator_bit_exact(oracle, mblib, formula):
     np.testing.assert_array_equal(mi, z["max_iter"])
 
 
-@pytest.mark.parametrize("formula", ["mandelbulb", "mandelbox", "trigde", "menger", "vary4d"])
+@pytest.mark.parametrize("formula", DES)
 def test_colouring_value_bit_exact(oracle, mblib, formula):
     z = np.load(os.path.join(GOLDEN, f"de_{formula}.npz"))
     sc = _scene(z)
@@ -51,9 +54,13 @@ def test_render_bit_exact(oracle, mblib, case):
         np.testing.assert_array_equal(getattr(img, layer), z[layer], err_msg=f"{case}: layer {layer}")
 
 
-@pytest.mark.parametrize("case", RENDERS[:4])
+KEYED = [c for c in RENDERS if "keys" in np.load(os.path.join(GOLDEN, f"render_{c}.npz")).files]
+
+
+@pytest.mark.parametrize("case", KEYED)
 def test_golden_scene_rebuilds_from_keys(mblib, case):
-    """The stored settings keys rebuild the stored scene bytes (parser + derivations are stable)."""
+    """The stored settings keys rebuild the stored scene bytes (parser + derivations are stable).
+    Fixtures made from the reference's example files store the loaded scene only."""
     from mandelbulber_gb300 import workloads as W
     z = np.load(os.path.join(GOLDEN, f"render_{case}.npz"))
     keys = json.loads(str(z["keys"]))
