@@ -200,6 +200,25 @@ static int gfb_normals(int type, double nv[20][3]) {
   return n;
 }
 
+// Scenes that light with auxiliary lights: random ones or any of the four predefined.
+static bool uses_aux_lights(const mbgb_scene &s) {
+  if (s.auxLightNumber > 0) return true;
+  for (int i = 0; i < 4; i++)
+    if (s.auxLightPreEnabled[i]) return true;
+  return false;
+}
+
+// The volumetric pass samples the march positions (sStep::point): visible aux lights.
+static bool need_step_points(const mbgb_scene &s) { return uses_aux_lights(s) && s.auxLightVisibility > 0.0; }
+
+static bool need_volumetric(const mbgb_scene &s) {
+  return (s.glow_intensity != 0.0) || s.fogEnabled || (s.fogDensity > 0.0) || need_step_points(s);
+}
+
+// Features that the per-pixel engine renders and the wavefront stages do not carry: scenes
+// that use them render on the per-pixel engine.
+static bool per_pixel_only(const mbgb_scene &s) { return uses_aux_lights(s); }
+
 template <typename T>
 static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   memset(&f, 0, sizeof(f));
@@ -407,8 +426,18 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   rgb(p.fogCol1, s.fogColour1);
   rgb(p.fogCol2, s.fogColour2);
   rgb(p.fogCol3, s.fogColour3);
-  // The volumetric pass changes the pixel only through glow, post fog or volumetric fog.
-  p.needVolumetric = (s.glow_intensity != 0.0) || s.fogEnabled || (s.fogDensity > 0.0);
+  p.auxLightNumber = s.auxLightNumber > 0 ? s.auxLightNumber : 0;
+  p.numberOfLights = uses_aux_lights(s) ? std::max(p.auxLightNumber, 4) : 0;
+  p.auxLightIntensity = (T)s.auxLightIntensity;
+  p.auxLightVisibility = (T)s.auxLightVisibility;
+  p.lights = nullptr;
+  p.iterFog = s.iterFogEnabled;
+  p.volLightAny = s.volumetricLightEnabledAny;
+  p.iterFogOpacity = (T)s.iterFogOpacity;
+  p.iterFogOpacityTrim = (T)s.iterFogOpacityTrim;
+  // The volumetric pass changes the pixel only through glow, post fog, volumetric fog and
+  // the visible auxiliary lights.
+  p.needVolumetric = need_volumetric(s);
 }
 
 struct DeviceBuf {
@@ -504,8 +533,8 @@ struct mbgb_context {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;
-  DeviceBuf step[2][3];          // per-pixel engine: [precision][step, dist, thr], kStepCap records per slot
-  DeviceBuf ovstep[2][3];        // overflow pass: kStepSlots records per slot, kOverflowThreads slots
+  DeviceBuf step[2][5];          // per-pixel engine: [precision][step, dist, thr, scan, iters], kStepCap records per slot
+  DeviceBuf ovstep[2][5];        // overflow pass: kStepSlots records per slot, kOverflowThreads slots
   DeviceBuf ovlist;              // overflow pixel list (per-pixel engine)
   DeviceBuf control;             // error flag, start time, stage counters
   DeviceBuf fctl;                // per group: wavefront stage counters / per-pixel tile counter (64 B each)
@@ -516,6 +545,8 @@ struct mbgb_context {
   DeviceBuf out[8];              // device staging for mbgb_render_host / mbgb_render_batch_host
   DeviceBuf wave[2];             // wavefront per-pixel buffers, per precision
   DeviceBuf probe;               // MBGB_PREC_AUTO: distance probes at the ray origins
+  DeviceBuf lightprobe;          // PlaceRandomLights: distances at candidate positions
+  DeviceBuf lights64, lights32;  // auxiliary light tables of the call's frames
   DeviceBuf tune_out;            // autotuner output layers
   DeviceBuf gradacc;             // differentiable render: per-frame dL/dtheta sums
   DeviceBuf post;                // post-processing: gamma table and SSAO direction tables
@@ -566,9 +597,6 @@ extern "C" mbgb_status mbgb_scene_supported(const mbgb_scene *s) {
   if (s->iterFogEnabled) return set_error(MBGB_ERR_UNSUPPORTED, "iteration fog");
   if (s->volumetricLightEnabledAny) return set_error(MBGB_ERR_UNSUPPORTED, "volumetric lights");
   if (s->fakeLightsEnabled) return set_error(MBGB_ERR_UNSUPPORTED, "fake (orbit trap) lights");
-  if (s->auxLightNumber > 0) return set_error(MBGB_ERR_UNSUPPORTED, "random auxiliary lights");
-  for (int i = 0; i < 4; i++)
-    if (s->auxLightPreEnabled[i]) return set_error(MBGB_ERR_UNSUPPORTED, "predefined auxiliary lights");
   if (s->raytracedReflections && s->reflectionsMax > 0)
     return set_error(MBGB_ERR_UNSUPPORTED, "ray-traced reflections");
   if (!s->raytracedReflections && s->reflect > 0)
@@ -618,6 +646,9 @@ extern "C" void mbgb_context_destroy(mbgb_context *c) {
   c->ovlist.release();
   for (auto &b : c->wave) b.release();
   c->probe.release();
+  c->lightprobe.release();
+  c->lights64.release();
+  c->lights32.release();
   c->tune_out.release();
   c->gradacc.release();
   c->post.release();
@@ -789,9 +820,6 @@ static void fill_cam(const mbgb_scene &s, const mbgb_image &img, const mbgb_opts
   cam.depth = img.depth;
 }
 
-static bool need_volumetric(const mbgb_scene &s) {
-  return (s.glow_intensity != 0.0) || s.fogEnabled || (s.fogDensity > 0.0);
-}
 
 // Scenes whose distance estimate the dual-number orbit (exact hits, gradients) covers:
 // formula 2, or formula 8 without rotations, offset or pre-folds, and the analytic
@@ -1014,7 +1042,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
 // the step buffer is in use) the overflow pass.
 static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, const mbgb_image &img,
                                      const Group &g, const mbgb_opts &o, cudaStream_t s, FrameIO io, char *fctl,
-                                     uint64_t *launches) {
+                                     uint64_t *launches, int64_t lightOff) {
   const int prec = g.prec;
   const int block = g.cfg.block;
   const int kf = kernel_formula(scene.formula, scene.ifsFoldingMode);
@@ -1035,10 +1063,13 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   io.tile_counter = (unsigned int *)(fctl + 0);
   io.overflow_count = (unsigned int *)(fctl + 4);
   const bool needVol = need_volumetric(scene);
+  const bool points = need_step_points(scene);
   if (needVol) {
     io.step_step = c->step[prec][0].ptr;
     io.step_dist = c->step[prec][1].ptr;
     io.step_thr = c->step[prec][2].ptr;
+    io.step_scan = points ? c->step[prec][3].ptr : nullptr;
+    io.step_iters = points ? (int *)c->step[prec][4].ptr : nullptr;
     io.overflow_list = (unsigned int *)c->ovlist.ptr;
   }
   MBGB_CUDA(cudaMemsetAsync(fctl, 0, 64, s));
@@ -1049,6 +1080,8 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   ov.step_step = c->ovstep[prec][0].ptr;
   ov.step_dist = c->ovstep[prec][1].ptr;
   ov.step_thr = c->ovstep[prec][2].ptr;
+  ov.step_scan = points ? c->ovstep[prec][3].ptr : nullptr;
+  ov.step_iters = points ? (int *)c->ovstep[prec][4].ptr : nullptr;
   const int ovBlocks = std::max(1, kOverflowThreads / block);
   FractalT<double> fd;
   fill_fractal<double>(scene, fd);
@@ -1056,11 +1089,13 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   if (prec == 0) {
     ParamsT<double> p;
     fill_params<double>(scene, p, o, (const double *)c->ao64.ptr, c->ao_count);
+    if (lightOff >= 0) p.lights = (const LightT<double> *)c->lights64.ptr + lightOff;
     e = launch_render_f64(kf, p, fd, io, grid, block, s);
     if (e == cudaSuccess && needVol) e = launch_render_f64(kf, p, fd, ov, ovBlocks, block, s);
   } else {
     ParamsT<float> p;
     fill_params<float>(scene, p, o, (const float *)c->ao32.ptr, c->ao_count);
+    if (lightOff >= 0) p.lights = (const LightT<float> *)c->lights32.ptr + lightOff;
     e = launch_render_f32(kf, p, fd, io, grid, block, s);
     if (e == cudaSuccess && needVol) e = launch_render_f32(kf, p, fd, ov, ovBlocks, block, s);
   }
@@ -1152,6 +1187,115 @@ static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const
 // Every render call: validate, plan the groups, prepare scratch and frame tables, enqueue
 // (or capture once and replay), and, for calls without a caller stream, wait and read the
 // counters back.
+// PlaceRandomLights (src/shaders.cpp:1134-1208): srand(seed); light after light, candidate
+// positions centre + (Random(2000000) / 1e6 - 1 + Random(1000000) / 1e12 per axis) x radius x
+// multiplier until CalculateDistance (detailSize 0) there is positive, below maxDist x
+// multiplier and not at the iteration limit; the multiplier grows by 1.1 every 1000
+// trials and resets with each light placed. Then the four predefined lights overwrite
+// slots 0-3 (enabled or not). The candidates' distances come from the device, a batch of
+// trials at a time: the batch is generated from a copy of the generator as if every trial
+// failed, and the generator then advances to the first accepted trial.
+static mbgb_status place_lights(mbgb_context *c, const mbgb_scene &s, cudaStream_t st,
+                                std::vector<LightT<double>> &out) {
+  const int nRandom = s.auxLightNumber > 0 ? s.auxLightNumber : 0;
+  out.assign((size_t)std::max(nRandom, 4), LightT<double>{});
+  GlibcRand rng((uint32_t)s.auxLightRandomSeed);
+  if (nRandom > 0) {
+    constexpr int kBatch = 512;
+    constexpr long long kMaxTrials = 20000000;  // the reference loops for ever on a scene no light fits
+    FractalT<double> f;
+    fill_fractal<double>(s, f);
+    const int kf = kernel_formula(s.formula, s.ifsFoldingMode);
+    const size_t o_pts = 0, o_det = 24 * kBatch, o_d = o_det + 8 * kBatch, o_it = o_d + 8 * kBatch,
+                 o_mi = o_it + 4 * kBatch;
+    MBGB_CUDA(c->ensure(c->lightprobe, o_mi + kBatch + 16));
+    char *pb = (char *)c->lightprobe.ptr;
+    const std::vector<double> zeros(kBatch, 0.0);
+    MBGB_CUDA(cudaMemcpyAsync(pb + o_det, zeros.data(), 8 * kBatch, cudaMemcpyHostToDevice, st));
+    std::vector<double> pts(3 * kBatch), dist(kBatch);
+    std::vector<unsigned char> mi(kBatch);
+    std::vector<GlibcRand> after(kBatch, rng);
+    std::vector<double> rmAccept(kBatch);
+    std::vector<int> tnAfter(kBatch);
+    int trial_number = 0;
+    double radius_multiplier = 1.0;
+    long long trials = 0;
+    for (int i = 0; i < nRandom;) {
+      GlibcRand g = rng;
+      int tn = trial_number;
+      double rm = radius_multiplier;
+      for (int b = 0; b < kBatch; b++) {
+        tn++;
+        double r[3];
+        for (int k = 0; k < 3; k++) {
+          const int a = g.random(2000000);
+          const int bb = g.random(1000000);
+          r[k] = (a / 1000000.0 - 1.0) + (bb / 1.0e12);
+        }
+        for (int k = 0; k < 3; k++) pts[3 * b + k] = s.auxLightRandomCenter[k] + r[k] * s.auxLightDistributionRadius * rm;
+        if (tn > 1000) {
+          rm *= 1.1;
+          tn = 0;
+        }
+        after[b] = g;
+        rmAccept[b] = rm;
+        tnAfter[b] = tn;
+      }
+      MBGB_CUDA(cudaMemcpyAsync(pb + o_pts, pts.data(), 24 * kBatch, cudaMemcpyHostToDevice, st));
+      cudaError_t e = launch_distance_f64(kf, f, (const double *)(pb + o_pts), (const double *)(pb + o_det), kBatch,
+                                          (double *)(pb + o_d), (int *)(pb + o_it), (unsigned char *)(pb + o_mi),
+                                          nullptr, st);
+      if (e != cudaSuccess) return cuda_error(e, "light placement distances");
+      MBGB_CUDA(cudaMemcpyAsync(dist.data(), pb + o_d, 8 * kBatch, cudaMemcpyDeviceToHost, st));
+      MBGB_CUDA(cudaMemcpyAsync(mi.data(), pb + o_mi, kBatch, cudaMemcpyDeviceToHost, st));
+      MBGB_CUDA(cudaStreamSynchronize(st));
+      int hit = -1;
+      for (int b = 0; b < kBatch; b++)
+        if (dist[b] > 0 && !mi[b] && dist[b] < s.auxLightMaxDist * rmAccept[b]) {
+          hit = b;
+          break;
+        }
+      if (hit < 0) {
+        rng = after[kBatch - 1];
+        trial_number = tnAfter[kBatch - 1];
+        radius_multiplier = rmAccept[kBatch - 1];
+        trials += kBatch;
+        if (trials > kMaxTrials) return set_error(MBGB_ERR_UNSUPPORTED, "no position found for an auxiliary light");
+        continue;
+      }
+      rng = after[hit];
+      trial_number = tnAfter[hit];
+      radius_multiplier = 1.0;
+      LightT<double> &L = out[(size_t)i];
+      for (int k = 0; k < 3; k++) L.pos[k] = pts[3 * hit + k];
+      int col[3];
+      for (int k = 0; k < 3; k++) col[k] = 20000 + rng.random(80000);
+      // dMax (src/common_math.cpp:34-43)
+      const double a = col[0], b = col[1], cc = col[2];
+      const double maxColour = (a > b) ? ((a > cc) ? a : cc) : ((b > cc) ? b : cc);
+      for (int k = 0; k < 3; k++) L.colour[k] = (int)(col[k] * 65536.0 / maxColour);
+      L.intensity = dist[hit] * dist[hit] / s.auxLightMaxDist;
+      L.enabled = 1;
+      trials += hit + 1;
+      i++;
+    }
+  }
+  for (int i = 0; i < 4; i++) {
+    LightT<double> &L = out[(size_t)i];
+    if (s.auxLightPreEnabled[i]) {
+      for (int k = 0; k < 3; k++) L.pos[k] = s.auxLightPre[i][k];
+      L.intensity = s.auxLightPreIntensity[i];
+      L.colour[0] = s.auxLightPreColour[i].R;
+      L.colour[1] = s.auxLightPreColour[i].G;
+      L.colour[2] = s.auxLightPreColour[i].B;
+      L.enabled = 1;
+    } else {
+      L.enabled = 0;
+    }
+  }
+  return MBGB_OK;
+}
+
 static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int n, const mbgb_image *imgs,
                                  const mbgb_opts *opts_in, const GradRequest *grad = nullptr) {
   if (!c || !scenes || !imgs) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
@@ -1179,6 +1323,9 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
   MBGB_CUDA(cudaSetDevice(c->device));
   cudaStream_t s = o.stream ? (cudaStream_t)o.stream : c->stream;
   const bool sync = o.stream == nullptr;
+  // light tables are placed per call, outside any capture: such calls are not captured
+  for (int i = 0; i < n; i++)
+    if (uses_aux_lights(scenes[i])) o.use_graph = 0;
 
   // a captured graph of the same frames, outputs and options is replayed as it is
   std::vector<char> key;
@@ -1253,7 +1400,8 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
                           ((r1 - r0 + cfg.tileH - 1) / cfg.tileH) * 32;
     const bool rayAO = sc.global_ilumination && !sc.fastGlobalIllumination;
     const double perPix = 1.0 + (rayAO ? c->ao_count : 0);
-    const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && (double)std::max(fpix, fjobs) * perPix < kMaxGroupJobs;
+    const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && !per_pixel_only(sc) &&
+                      (double)std::max(fpix, fjobs) * perPix < kMaxGroupJobs;
     if (!wave && (grad || o.exact_hit))
       return set_error(MBGB_ERR_BAD_PARAM, "exact hits and gradients need the wavefront engine and frames below 4e9 rays");
     Group *g = nullptr;
@@ -1287,6 +1435,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
   // scratch for the largest group of each kind, frame tables of all groups
   size_t wave_bytes[2] = {0, 0};
   bool volPrec[2] = {false, false};
+  bool pointsPrec[2] = {false, false};
   int64_t maxPixPerPixel = 0;
   int64_t maxSlots[2] = {0, 0};
   size_t camsBytes = 0;
@@ -1294,6 +1443,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     const mbgb_scene &rep = scenes[g.frames[0]];
     const bool needVol = need_volumetric(rep);
     if (needVol) volPrec[g.prec] = true;
+    if (!g.wave && need_step_points(rep)) pointsPrec[g.prec] = true;
     if (g.wave) {
       const bool rayAO = rep.global_ilumination && !rep.fastGlobalIllumination;
       const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
@@ -1316,11 +1466,14 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
   for (int p = 0; p < 2; p++) {
     if (wave_bytes[p]) MBGB_CUDA(c->ensure(c->wave[p], wave_bytes[p]));
     const size_t esz = p == 0 ? sizeof(double) : sizeof(float);
+    const int arrays = pointsPrec[p] ? 5 : 3;
+    auto bytes_of = [&](int k) { return k == 4 ? sizeof(int) : esz; };
     if (volPrec[p])
-      for (int k = 0; k < 3; k++)
-        MBGB_CUDA(c->ensure(c->ovstep[p][k], (size_t)kStepSlots * (size_t)kOverflowThreads * esz));
+      for (int k = 0; k < arrays; k++)
+        MBGB_CUDA(c->ensure(c->ovstep[p][k], (size_t)kStepSlots * (size_t)kOverflowThreads * bytes_of(k)));
     if (maxSlots[p])
-      for (int k = 0; k < 3; k++) MBGB_CUDA(c->ensure(c->step[p][k], (size_t)kStepCap * (size_t)maxSlots[p] * esz));
+      for (int k = 0; k < arrays; k++)
+        MBGB_CUDA(c->ensure(c->step[p][k], (size_t)kStepCap * (size_t)maxSlots[p] * bytes_of(k)));
   }
   if (maxPixPerPixel) MBGB_CUDA(c->ensure(c->ovlist, (size_t)maxPixPerPixel * sizeof(unsigned int)));
   MBGB_CUDA(c->ensure(c->control, 256));
@@ -1380,6 +1533,37 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     }
   }
 
+  // auxiliary light tables of the per-pixel frames that light with them
+  std::vector<int64_t> lightOff((size_t)n, -1);
+  {
+    std::vector<LightT<double>> all64;
+    for (auto &g : plan.groups) {
+      if (g.wave || !uses_aux_lights(scenes[g.frames[0]])) continue;
+      std::vector<LightT<double>> L;
+      st = place_lights(c, scenes[g.frames[0]], s, L);
+      if (st != MBGB_OK) return st;
+      lightOff[(size_t)g.frames[0]] = (int64_t)all64.size();
+      all64.insert(all64.end(), L.begin(), L.end());
+    }
+    if (!all64.empty()) {
+      std::vector<LightT<float>> all32(all64.size());
+      for (size_t k = 0; k < all64.size(); k++) {
+        for (int j = 0; j < 3; j++) {
+          all32[k].pos[j] = (float)all64[k].pos[j];
+          all32[k].colour[j] = all64[k].colour[j];
+        }
+        all32[k].intensity = (float)all64[k].intensity;
+        all32[k].enabled = all64[k].enabled;
+      }
+      MBGB_CUDA(c->ensure(c->lights64, sizeof(LightT<double>) * all64.size()));
+      MBGB_CUDA(c->ensure(c->lights32, sizeof(LightT<float>) * all32.size()));
+      MBGB_CUDA(cudaMemcpyAsync(c->lights64.ptr, all64.data(), sizeof(LightT<double>) * all64.size(),
+                                cudaMemcpyHostToDevice, s));
+      MBGB_CUDA(cudaMemcpyAsync(c->lights32.ptr, all32.data(), sizeof(LightT<float>) * all32.size(),
+                                cudaMemcpyHostToDevice, s));
+    }
+  }
+
   // enqueue (inside a capture when use_graph)
   char *ctl = (char *)c->control.ptr;
   FrameIO io{};
@@ -1396,7 +1580,8 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       cudaEvent_t *ev = plan.profile ? &c->gev[kStageEvents * gi] : nullptr;
       mbgb_status r;
       if (!g.wave) {
-        r = enqueue_per_pixel(c, scenes[g.frames[0]], imgs[g.frames[0]], g, o, s, io, gctl, &plan.launches);
+        r = enqueue_per_pixel(c, scenes[g.frames[0]], imgs[g.frames[0]], g, o, s, io, gctl, &plan.launches,
+                              lightOff[(size_t)g.frames[0]]);
       } else if (g.prec == 0) {
         r = enqueue_wave<double>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches);
       } else {

@@ -76,6 +76,16 @@ struct FractalT {
   T hybridPower[5];
 };
 
+// One auxiliary light (sLight, src/shaders.h:25-31): placed at random around a centre
+// (PlaceRandomLights, src/shaders.cpp:1134-1208) or one of the four predefined lights.
+template <typename T>
+struct LightT {
+  T pos[3];
+  int colour[3];   // sRGB, 16-bit range
+  T intensity;
+  int enabled;
+};
+
 // Everything MainThread and the shaders read (sParamRender, src/fractparams.h:67-146).
 template <typename T>
 struct ParamsT {
@@ -117,6 +127,13 @@ struct ParamsT {
   int fogColor[3];
   T fogDensity, fogC1Dist, fogC2Dist, fogDistFactor;
   int fogCol1[3], fogCol2[3], fogCol3[3];
+  // auxiliary lights (AuxLightsShader / LightShading / AuxShadow, src/shaders.cpp:997-1132)
+  int auxLightNumber;      // random lights; the shaders also read lights 0-3 when enabled
+  int numberOfLights;      // max(auxLightNumber, 4), 0 when the scene has no aux lights
+  T auxLightIntensity, auxLightVisibility;
+  const LightT<T> *lights; // device memory, numberOfLights entries
+  int iterFog, volLightAny;  // imageSwitches.iterFogEnabled / volumetricLightEnabled
+  T iterFogOpacity, iterFogOpacityTrim;
 };
 
 // Per-frame camera, resolution, fractal parameter and output layers of a batch (device
@@ -164,6 +181,10 @@ struct FrameIO {
   // list; the overflow pass (overflow_pass = 1) re-renders those pixels with
   // step_cap = kStepSlots and its own, smaller slot set.
   void *step_step, *step_dist, *step_thr;
+  // the march position and iteration count of each record (sStep::point / iters), for the
+  // volumetric terms that sample there (visible aux lights); null when unused
+  void *step_scan;
+  int *step_iters;
   int64_t slots;
   int step_cap;
   int overflow_pass;

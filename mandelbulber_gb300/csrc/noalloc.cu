@@ -109,6 +109,11 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   if (!scene->analitycDE)
     return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
                            "delta-DE formulas render in FP64, which the allocation-free entry point does not carry");
+  bool auxLights = scene->auxLightNumber > 0;
+  for (int i = 0; i < 4; i++) auxLights = auxLights || scene->auxLightPreEnabled[i];
+  if (auxLights)
+    return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
+                           "auxiliary lights are placed per call, which the allocation-free entry point does not do");
   if (o.row_end == 0) o.row_end = scene->image_height;
   if (o.row_begin < 0 || o.row_end > scene->image_height || o.row_begin >= o.row_end)
     return mbgb::set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");

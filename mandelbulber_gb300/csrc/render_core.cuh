@@ -282,6 +282,8 @@ __device__ __forceinline__ int jitter1000(uint32_t seed, uint32_t pixel, uint32_
 template <typename T>
 struct StepBuf {
   T *step, *dist, *thr;
+  T *scan;     // null unless the volumetric pass samples the record positions
+  int *iters;
   int64_t slots, slot;
   __device__ __forceinline__ int64_t at(int i) const { return (int64_t)i * slots + slot; }
 };
@@ -340,6 +342,7 @@ __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, co
     if (useSB) {
       sb.dist[sb.at(i)] = dist;
       sb.thr[sb.at(i)] = distThresh;
+      if (sb.iters) sb.iters[sb.at(i)] = iters;
     }
     if (dist > T(3)) dist = T(3);
     if (dist < distThresh) {
@@ -347,7 +350,10 @@ __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, co
       found = true;
       break;
     }
-    if (useSB) sb.step[sb.at(i)] = step;
+    if (useSB) {
+      sb.step[sb.at(i)] = step;
+      if (sb.scan) sb.scan[sb.at(i)] = scan;
+    }
     step = (dist - stepFrac * distThresh) * p.DE_factor;
     if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, pixel, (uint32_t)i)) / T(10000));
     buffCount++;
@@ -553,6 +559,111 @@ __device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, 
   return AO;
 }
 
+// IterOpacity (src/shaders.cpp:1210-1218)
+template <typename T>
+__device__ __forceinline__ T iter_opacity(const T step, const T iters, const T maxN, const T trim, const T opacitySp) {
+  T opacity = (iters - trim) / maxN;
+  if (opacity < T(0)) opacity = T(0);
+  opacity *= opacity;
+  opacity *= step * opacitySp;
+  if (opacity > T(1)) opacity = T(1);
+  return opacity;
+}
+
+// The threshold a secondary ray compares against, held in a float as the reference does:
+// with iteration fog or volumetric lights the one of the sample's own distance from the
+// eye, else the hit's.
+template <typename T>
+__device__ __forceinline__ T secondary_thresh(const ParamsT<T> &p, const V3<T> point2, const V3<T> eye,
+                                              const T dist_thresh) {
+  float t;
+  if (p.iterFog || p.volLightAny) {
+    if (!p.constantDEThreshold) t = (float)(length3(point2 - eye) * p.resolution * p.persp / p.quality);
+    else t = (float)p.quality;
+  } else {
+    t = (float)dist_thresh;
+  }
+  return (T)t;
+}
+
+// AuxShadow (src/shaders.cpp:1069-1132): march from the point towards a light at `distance`,
+// starting and first stepping at delta. `detail` is the shared detailSize (not changed here);
+// `itersOut` the shared iteration count, which a limits-box early return leaves as it was.
+template <typename T, int FORMULA>
+__device__ __forceinline__ T aux_shadow(const ParamsT<T> &p, const V3<T> point, const T distance, const V3<T> lightVector,
+                                        const T delta, const T dist_thresh, const V3<T> eye, const T detail,
+                                        int &itersOut, Counters &cnt) {
+  T dist = delta;
+  T shadowTemp = T(1);
+  const T DE_factor = (p.iterFog || p.volLightAny) ? T(1) : p.DE_factor;
+  int guard = 0;
+  for (T i = delta; i < distance; i += dist * DE_factor) {
+    const V3<T> point2 = point + lightVector * i;
+    bool mi;
+    dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, itersOut, mi, cnt, fparam_of(p.f));
+    T opacity = T(0);
+    if (p.iterFog)
+      opacity = iter_opacity(dist * DE_factor, T(itersOut), T(p.f.N), p.iterFogOpacityTrim, p.iterFogOpacity);
+    shadowTemp -= opacity * (distance - i) / distance;
+    const T thr = secondary_thresh(p, point2, eye, dist_thresh);
+    if (dist < thr || mi || shadowTemp < T(0)) {
+      if (p.penetrating) {
+        shadowTemp -= (distance - i) / distance;
+        if (shadowTemp < T(0)) shadowTemp = T(0);
+      } else {
+        shadowTemp = T(0);
+      }
+      break;
+    }
+    // hard bound: in FP32 `i += dist` could stop advancing when dist falls below ulp(i)
+    if (++guard >= kMaxSecondarySteps) break;
+  }
+  return shadowTemp;
+}
+
+// AuxLightsShader / LightShading (src/shaders.cpp:997-1067): Lambert and Blinn terms of each
+// auxiliary light, 1 / r^2 falloff shared among `numberOfLights`, shadowed by AuxShadow when
+// either term is above 0.01 (and zero when shadows are on and neither is).
+template <typename T, int FORMULA>
+__device__ __forceinline__ void aux_lights(const ParamsT<T> &p, const V3<T> point, const V3<T> normal, const V3<T> view,
+                                           const T delta, const T dist_thresh, const V3<T> eye, const T detail,
+                                           int &itersOut, Counters &cnt, T shadeSum[3], T specSum[3]) {
+  shadeSum[0] = shadeSum[1] = shadeSum[2] = T(0);
+  specSum[0] = specSum[1] = specSum[2] = T(0);
+  const int number = p.numberOfLights;
+  for (int i = 0; i < number; i++) {
+    const LightT<T> L = p.lights[i];
+    if (!(i < p.auxLightNumber || L.enabled)) continue;
+    const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - point;
+    const T distance = length3(d);
+    const V3<T> lightVector = normalize3(d);
+    const T intensity = p.auxLightIntensity * T(100) * L.intensity / (distance * distance) / T(number);
+    T shade = dot3(normal, lightVector);
+    if (shade < T(0)) shade = T(0);
+    shade = shade * intensity;
+    if (shade > T(500)) shade = T(500);
+    const V3<T> half = normalize3(lightVector - view);
+    T shade2 = dot3(normal, half);
+    if (shade2 < T(0)) shade2 = T(0);
+    shade2 = m_pow(shade2, T(30)) * T(1);
+    shade2 *= intensity * p.specular;
+    if (shade2 > T(15)) shade2 = T(15);
+    if ((shade > T(0.01) || shade2 > T(0.01)) && p.shadow) {
+      const T light = aux_shadow<T, FORMULA>(p, point, distance, lightVector, delta, dist_thresh, eye, detail, itersOut,
+                                             cnt);
+      shade *= light;
+      shade2 *= light;
+    } else if (p.shadow) {
+      shade = T(0);
+      shade2 = T(0);
+    }
+    for (int c = 0; c < 3; c++) {
+      shadeSum[c] += shade * T(L.colour[c]) / T(65536);
+      specSum[c] += shade2 * T(L.colour[c]) / T(65536);
+    }
+  }
+}
+
 // IndexToColour (src/shaders.cpp:1273-1305) -> sRGB in 8-bit range
 template <typename T>
 __device__ __forceinline__ void index_to_colour(const ParamsT<T> &p, int index, int rgb[3]) {
@@ -619,7 +730,8 @@ __device__ __forceinline__ V3<T> background(const ParamsT<T> &p, const V3<T> vie
 // the primary step buffer, far to near, merging steps shorter than distThresh * quality.
 template <typename T>
 __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
-                                           const T depth, T out[4], float &totalOpacityOut, bool &opacitySet) {
+                                           const T depth, const V3<T> eye, const V3<T> view, T out[4],
+                                           float &totalOpacityOut, bool &opacitySet) {
   float totalOpacity = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
   T glowN = T(1) - glow;
@@ -646,6 +758,50 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
     out[1] = glowOpacity * glowG + (T(1) - glowOpacity) * out[1];
     out[2] = glowOpacity * glowB + (T(1) - glowOpacity) * out[2];
     out[3] += glowOpacity;
+    // visible auxiliary lights (src/shaders.cpp:242-296): a bell-shaped glow around each
+    // light, sampled in up to 50 sub-steps near the closest one
+    if (p.auxLightVisibility > T(0) && p.numberOfLights > 0) {
+      const V3<T> point = eye + view * sb.scan[sb.at(index)];
+      T lowestLightSize = T(1e10);
+      T lowestLightDist = T(1e10);
+      for (int i = 0; i < p.numberOfLights; ++i) {
+        const LightT<T> L = p.lights[i];
+        if (!(i < p.auxLightNumber || L.enabled)) continue;
+        const T lightDist = length3(point - V3<T>{L.pos[0], L.pos[1], L.pos[2]});
+        const T lightSize = L.intensity * p.auxLightIntensity * p.auxLightVisibility;
+        const T r2 = lightDist / lightSize;
+        if (r2 < lowestLightSize) {
+          lowestLightSize = r2;
+          lowestLightDist = lightDist;
+        }
+      }
+      int smallSteps = to_i32_x86((double)(T(10) * step / (lowestLightDist + T(1.0e-20))));
+      if (smallSteps > 50) smallSteps = 50;
+      int smallStep_start = 0, smallStep_end = 1;
+      T step2 = step;
+      if (smallSteps > 0) {
+        smallStep_start = 1;
+        smallStep_end = smallSteps + 1;
+        step2 = step / (T(smallSteps) + T(1));
+      }
+      for (int smallStep = smallStep_start; smallStep < smallStep_end; smallStep++) {
+        const V3<T> point2 = point - view * step2 * T(smallStep);
+        for (int i = 0; i < p.numberOfLights; ++i) {
+          const LightT<T> L = p.lights[i];
+          if (!(i < p.auxLightNumber || L.enabled)) continue;
+          const T lightDist = length3(point2 - V3<T>{L.pos[0], L.pos[1], L.pos[2]});
+          const T lightSize = L.intensity * p.auxLightIntensity * p.auxLightVisibility;
+          T r2 = lightDist / lightSize;
+          if (r2 > T(1)) r2 = T(1);
+          const T bellFunction = (m_cos(r2 * T(kPI)) + T(1)) / (r2 * r2 + T(0.02)) * T(0.3);
+          const T lightDensity = step2 * bellFunction / lightSize;
+          out[0] += lightDensity * T(L.colour[0]) / T(65536);
+          out[1] += lightDensity * T(L.colour[1]) / T(65536);
+          out[2] += lightDensity * T(L.colour[2]) / T(65536);
+          out[3] += lightDensity;
+        }
+      }
+    }
     // basic fog
     if (p.postFog) {
       T fogDensity = step / p.fogVisibility;
@@ -752,7 +908,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
   const T dist_thresh = (T)rs.distThresh;
   T detail = (T)rs.distThresh;
   if (rs.found) {
-    // ObjectShader (src/shaders.cpp:21-112), no aux/fake lights, no env mapping
+    // ObjectShader (src/shaders.cpp:21-112), no fake lights, no env mapping
     const V3<T> point{(T)rs.point[0], (T)rs.point[1], (T)rs.point[2]};
     T delta;
     if (p.constantDEThreshold) delta = (T)rs.scan * p.resolution * p.persp;
@@ -783,12 +939,21 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
       }
     }
     const V3<T> ambient2{ambient.x * p.globalIlum, ambient.y * p.globalIlum, ambient.z * p.globalIlum};
-    const T objR = T(0) + (ambient2.x + p.mainLight[0] * shadeV * shadow) * colour.x;
-    const T objG = T(0) + (ambient2.y + p.mainLight[1] * shadeV * shadow) * colour.y;
-    const T objB = T(0) + (ambient2.z + p.mainLight[2] * shadeV * shadow) * colour.z;
-    const T specR = T(0) + p.mainLight[0] * spec * shadow;
-    const T specG = T(0) + p.mainLight[1] * spec * shadow;
-    const T specB = T(0) + p.mainLight[2] * spec * shadow;
+    // auxiliary lights
+    T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
+    if (p.numberOfLights > 0) {
+      int itersOut = rs.iters;
+      aux_lights<T, FORMULA>(p, point, n, viewT, delta, dist_thresh, startT, detail, itersOut, cnt, aux, auxSpec);
+    }
+    T objR = T(0) + (ambient2.x + p.mainLight[0] * shadeV * shadow) * colour.x;
+    T objG = T(0) + (ambient2.y + p.mainLight[1] * shadeV * shadow) * colour.y;
+    T objB = T(0) + (ambient2.z + p.mainLight[2] * shadeV * shadow) * colour.z;
+    objR += (aux[0] + T(0)) * colour.x;
+    objG += (aux[1] + T(0)) * colour.y;
+    objB += (aux[2] + T(0)) * colour.z;
+    const T specR = auxSpec[0] + T(0) + p.mainLight[0] * spec * shadow;
+    const T specG = auxSpec[1] + T(0) + p.mainLight[1] * spec * shadow;
+    const T specB = auxSpec[2] + T(0) + p.mainLight[2] * spec * shadow;
     result[0] = objR + T(0) + specR;
     result[1] = objG + T(0) + specG;
     result[2] = objB + T(0) + specB;
@@ -805,7 +970,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
   bool opacitySet = false;
   // the volumetric pass sees the march depth even for background pixels: the
   // shader input is filled before the depth becomes 1e20 (src/Render3D.cpp:518-541)
-  if (p.needVolumetric) volumetric<T>(p, sb, rs.buffCount, (T)rs.scan, result, totalOpacity, opacitySet);
+  if (p.needVolumetric) volumetric<T>(p, sb, rs.buffCount, (T)rs.scan, startT, viewT, result, totalOpacity, opacitySet);
 
   // buffer writes (src/Render3D.cpp:569-589)
   if (io.opacity) io.opacity[pix] = to_u16_x86((double)totalOpacity * 65535.0);
@@ -835,7 +1000,8 @@ template <typename T, int FORMULA>
 __global__ void __launch_bounds__(128) render_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd, const FrameIO io) {
   const int lane = threadIdx.x & 31;
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, io.slots, slot};
+  StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, (T *)io.step_scan, io.step_iters, io.slots,
+                slot};
   Counters cnt{0, 0, 0, 0};
   const int tilesX = (p.width + kTileW - 1) / kTileW;
   const int rowTiles = (p.row_end - p.row_begin + kTileH - 1) / kTileH;

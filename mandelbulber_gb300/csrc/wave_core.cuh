@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(128, 6) primary_kernel(const __grid_constant__
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, io.slots, slot};
+  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, nullptr, nullptr, io.slots, slot};
   const bool useSB = p.needVolumetric;
   const bool f64 = sizeof(T) == 8;
   const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);

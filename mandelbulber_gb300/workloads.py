@@ -105,6 +105,17 @@ WORKLOADS = {"mandelbulb_640x480": MANDELBULB_640x480, "mandelbox_1080p": MANDEL
 # mandelboxVaryScale4D's own parameters at the values of the reference's default settings
 # (src/settings.cpp:413-417); the
 # other formulas ignore them, so the base scenes keep them at zero
+# Auxiliary-light settings at the reference's default values (share/defaults); the
+# benchmark scenes light with the main light only
+AUX_LIGHTS = {"aux_light_intensity": 1, "aux_light_random_seed": 1234, "aux_light_max_dist": 0.1,
+              "aux_light_distribution_radius": 3,
+              "aux_light_predefined_1_colour_R": 45761, "aux_light_predefined_1_colour_G": 53633,
+              "aux_light_predefined_1_colour_B": 59498, "aux_light_predefined_2_colour_R": 62875,
+              "aux_light_predefined_2_colour_G": 55818, "aux_light_predefined_2_colour_B": 50083,
+              "aux_light_predefined_3_colour_R": 64884, "aux_light_predefined_3_colour_G": 64928,
+              "aux_light_predefined_3_colour_B": 48848, "aux_light_predefined_4_colour_R": 52704,
+              "aux_light_predefined_4_colour_G": 62492, "aux_light_predefined_4_colour_B": 45654}
+
 VARY4D = {"formula": 18, "mandelbox_vary_scale_vary": 0.1, "mandelbox_vary_fold": 1,
           "mandelbox_vary_minr": 0.5, "mandelbox_vary_rpower": 1, "mandelbox_vary_wadd": 0}
 

@@ -786,8 +786,29 @@ double calculate_distance(Calc &c, Vec p, bool *max_iter) {
   return d;
 }
 
+struct OLight {
+  Vec pos;
+  int col[3];
+  double intensity;
+  bool enabled;
+};
+
+struct Frame {
+  const mbgb_scene *s;
+  std::vector<OLight> lights;   // Lights[]
+  int numberOfLights = 0;       // max(lightsPlaced, 4); 0 = no auxiliary lights at all
+  double rm[9];
+  int rzero;
+  Vec start, light;
+  std::vector<Vec> aoDirs;
+  bool exact = false;   // level-set refinement of hits (oracle_render_exact)
+  Derived d;
+};
+
 struct Step {
   double dist, step, thr;
+  Vec point;   // sStep::point
+  int iters;   // sStep::iters
 };
 
 struct Ray {
@@ -819,12 +840,14 @@ Ray ray_marching(const mbgb_scene &s, Calc &c, Vec start, Vec dir, std::vector<S
     dist = calculate_distance(c, point, &mi);
     buf[i].dist = dist;
     buf[i].thr = thr;
+    buf[i].iters = c.itersOut;
     if (dist > 3.0) dist = 3.0;
     if (dist < thr) {
       found = true;
       break;
     }
     buf[i].step = step;
+    buf[i].point = point;
     const double j = jitter ? (1.0 - (rand() % 1001) / 10000.0) : 1.0;
     step = (dist - (s.interiorMode ? 0.8 : 0.5) * thr) * s.DE_factor * j;
     count++;
@@ -1043,8 +1066,8 @@ Vec background(const mbgb_scene &s, Vec view) {
   return {px[0] / 65536.0, px[1] / 65536.0, px[2] / 65536.0};
 }
 
-void volumetric(const mbgb_scene &s, const std::vector<Step> &buf, int count, double depth, double out[4],
-                float *opacity) {
+void volumetric(const mbgb_scene &s, const Frame &f, const std::vector<Step> &buf, int count, double depth, Vec view,
+                double out[4], float *opacity) {
   float total = 0.0f;
   const double glow = count * s.glow_intensity / 512.0 * s.DE_factor;
   double glowN = 1.0 - glow;
@@ -1067,6 +1090,48 @@ void volumetric(const mbgb_scene &s, const std::vector<Step> &buf, int count, do
     out[1] = go * gG + (1.0 - go) * out[1];
     out[2] = go * gB + (1.0 - go) * out[2];
     out[3] += go;
+    // visible auxiliary lights (src/shaders.cpp:242-296)
+    if (s.auxLightVisibility > 0 && f.numberOfLights > 0) {
+      const Vec point = buf[k].point;
+      double lowSize = 1e10, lowDist = 1e10;
+      for (int i = 0; i < f.numberOfLights; ++i) {
+        const OLight &L = f.lights[(size_t)i];
+        if (!(i < s.auxLightNumber || L.enabled)) continue;
+        const double ld = len(sub(point, L.pos));
+        const double size = L.intensity * s.auxLightIntensity * s.auxLightVisibility;
+        const double r2 = ld / size;
+        if (r2 < lowSize) {
+          lowSize = r2;
+          lowDist = ld;
+        }
+      }
+      int small = to_i32(10.0 * step / (lowDist + 1.0e-20));
+      if (small > 50) small = 50;
+      int s0 = 0, s1 = 1;
+      double step2 = step;
+      if (small > 0) {
+        s0 = 1;
+        s1 = small + 1;
+        step2 = step / (small + 1.0);
+      }
+      for (int ss = s0; ss < s1; ss++) {
+        const Vec p2 = sub(point, mul(mul(view, step2), (double)ss));
+        for (int i = 0; i < f.numberOfLights; ++i) {
+          const OLight &L = f.lights[(size_t)i];
+          if (!(i < s.auxLightNumber || L.enabled)) continue;
+          const double ld = len(sub(p2, L.pos));
+          const double size = L.intensity * s.auxLightIntensity * s.auxLightVisibility;
+          double r2 = ld / size;
+          if (r2 > 1.0) r2 = 1.0;
+          const double bell = (cos(r2 * M_PI) + 1.0) / (r2 * r2 + 0.02) * 0.3;
+          const double dens = step2 * bell / size;
+          out[0] += dens * L.col[0] / 65536.0;
+          out[1] += dens * L.col[1] / 65536.0;
+          out[2] += dens * L.col[2] / 65536.0;
+          out[3] += dens;
+        }
+      }
+    }
     if (s.fogEnabled) {
       double fd = step / fogVis;
       if (fd > 1.0) fd = 1.0;
@@ -1104,19 +1169,154 @@ void volumetric(const mbgb_scene &s, const std::vector<Step> &buf, int count, do
   }
 }
 
-struct Frame {
-  const mbgb_scene *s;
-  double rm[9];
-  int rzero;
-  Vec start, light;
-  std::vector<Vec> aoDirs;
-  bool exact = false;   // level-set refinement of hits (oracle_render_exact)
-  Derived d;
-};
+
+// PlaceRandomLights (src/shaders.cpp:1134-1208), with the C library's srand / rand.
+void place_lights(const mbgb_scene &s, const Derived &d, std::vector<OLight> &L) {
+  const int nr = s.auxLightNumber > 0 ? s.auxLightNumber : 0;
+  L.assign((size_t)nr + 4, OLight{});
+  srand((unsigned)s.auxLightRandomSeed);
+  auto rnd = [](int max) { return rand() % (max + 1); };
+  Cnt cnt;
+  Calc c{&s, (int)s.N, s.minN, false, 0.0, 0, &cnt, &d};
+  int trial = 0;
+  double rm = 1.0;
+  long long guard = 0;
+  for (int i = 0; i < nr && guard < 20000000; i++, guard++) {
+    trial++;
+    double r[3];
+    for (int k = 0; k < 3; k++) {
+      const int a = rnd(2000000);
+      const int b = rnd(1000000);
+      r[k] = (a / 1000000.0 - 1.0) + (b / 1.0e12);
+    }
+    const Vec pos{s.auxLightRandomCenter[0] + r[0] * s.auxLightDistributionRadius * rm,
+                  s.auxLightRandomCenter[1] + r[1] * s.auxLightDistributionRadius * rm,
+                  s.auxLightRandomCenter[2] + r[2] * s.auxLightDistributionRadius * rm};
+    bool mi = false;
+    c.detail = 0.0;
+    const double dist = calculate_distance(c, pos, &mi);
+    if (trial > 1000) {
+      rm *= 1.1;
+      trial = 0;
+    }
+    if (dist > 0 && !mi && dist < s.auxLightMaxDist * rm) {
+      rm = 1.0;
+      L[i].pos = pos;
+      int col[3];
+      for (int k = 0; k < 3; k++) col[k] = 20000 + rnd(80000);
+      const double a = col[0], b = col[1], cc = col[2];
+      const double mx = (a > b) ? ((a > cc) ? a : cc) : ((b > cc) ? b : cc);
+      for (int k = 0; k < 3; k++) L[i].col[k] = (int)(col[k] * 65536.0 / mx);
+      L[i].intensity = dist * dist / s.auxLightMaxDist;
+      L[i].enabled = true;
+    } else {
+      i--;
+    }
+  }
+  for (int i = 0; i < 4; i++) {
+    if (s.auxLightPreEnabled[i]) {
+      L[i].pos = Vec{s.auxLightPre[i][0], s.auxLightPre[i][1], s.auxLightPre[i][2]};
+      L[i].intensity = s.auxLightPreIntensity[i];
+      L[i].col[0] = s.auxLightPreColour[i].R;
+      L[i].col[1] = s.auxLightPreColour[i].G;
+      L[i].col[2] = s.auxLightPreColour[i].B;
+      L[i].enabled = true;
+    } else {
+      L[i].enabled = false;
+    }
+  }
+}
+
+double iter_opacity(double step, double iters, double maxN, double trim, double sp) {
+  double o = (iters - trim) / maxN;
+  if (o < 0.0) o = 0.0;
+  o *= o;
+  o *= step * sp;
+  if (o > 1.0) o = 1.0;
+  return o;
+}
+
+// the float threshold of the secondary rays (MainShadow / AuxShadow / AmbientOcclusion)
+float secondary_thresh(const mbgb_scene &s, Vec p2, Vec eye, double thr) {
+  if (s.iterFogEnabled || s.volumetricLightEnabledAny) {
+    if (!s.constantDEThreshold) return (float)(len(sub(p2, eye)) * s.resolution * s.persp / s.quality);
+    return (float)s.quality;
+  }
+  return (float)thr;
+}
+
+// AuxShadow (src/shaders.cpp:1069-1132)
+double aux_shadow(const mbgb_scene &s, Calc &c, Vec p, double distance, Vec lv, double delta, double thr, Vec eye) {
+  double dist = delta;
+  double shadowTemp = 1.0;
+  const double def = (s.iterFogEnabled || s.volumetricLightEnabledAny) ? 1.0 : s.DE_factor;
+  for (double i = delta; i < distance; i += dist * def) {
+    const Vec p2 = add(p, mul(lv, i));
+    bool mi = false;
+    dist = calculate_distance(c, p2, &mi);
+    const double opacity = s.iterFogEnabled
+                               ? iter_opacity(dist * def, c.itersOut, s.N, s.iterFogOpacityTrim, s.iterFogOpacity)
+                               : 0.0;
+    shadowTemp -= opacity * (distance - i) / distance;
+    if (dist < secondary_thresh(s, p2, eye, thr) || mi || shadowTemp < 0.0) {
+      if (s.penetratingLights) {
+        shadowTemp -= (distance - i) / distance;
+        if (shadowTemp < 0.0) shadowTemp = 0.0;
+      } else {
+        shadowTemp = 0.0;
+      }
+      break;
+    }
+  }
+  return shadowTemp;
+}
+
+// AuxLightsShader / LightShading (src/shaders.cpp:997-1067)
+void aux_lights(const mbgb_scene &s, const Frame &f, Calc &c, Vec p, Vec n, Vec view, double delta, double thr,
+                double shade_out[3], double spec_out[3]) {
+  for (int k = 0; k < 3; k++) shade_out[k] = spec_out[k] = 0.0;
+  const int number = f.numberOfLights;
+  for (int i = 0; i < number; i++) {
+    const OLight &L = f.lights[(size_t)i];
+    if (!(i < s.auxLightNumber || L.enabled)) continue;
+    const Vec d = sub(L.pos, p);
+    const double distance = len(d);
+    const Vec lv = normalize(d);
+    const double intensity = s.auxLightIntensity * 100.0 * L.intensity / (distance * distance) / number;
+    double shade = dot(n, lv);
+    if (shade < 0) shade = 0;
+    shade = shade * intensity;
+    if (shade > 500.0) shade = 500.0;
+    const Vec half = normalize(sub(lv, view));
+    double shade2 = dot(n, half);
+    if (shade2 < 0.0) shade2 = 0.0;
+    shade2 = pow(shade2, 30.0) * 1.0;
+    shade2 *= intensity * s.specular;
+    if (shade2 > 15.0) shade2 = 15.0;
+    if ((shade > 0.01 || shade2 > 0.01) && s.shadow) {
+      const double light = aux_shadow(s, c, p, distance, lv, delta, thr, f.start);
+      shade *= light;
+      shade2 *= light;
+    } else if (s.shadow) {
+      shade = 0;
+      shade2 = 0;
+    }
+    for (int k = 0; k < 3; k++) {
+      shade_out[k] += shade * L.col[k] / 65536.0;
+      spec_out[k] += shade2 * L.col[k] / 65536.0;
+    }
+  }
+}
 
 void setup_frame(const mbgb_scene &s, Frame &f) {
   f.s = &s;
   derive(s, f.d);
+  bool anyPre = false;
+  for (int i = 0; i < 4; i++) anyPre = anyPre || s.auxLightPreEnabled[i];
+  if (s.auxLightNumber > 0 || anyPre) {
+    place_lights(s, f.d, f.lights);
+    f.numberOfLights = s.auxLightNumber > 4 ? s.auxLightNumber : 4;
+  }
   // RotateZ(alpha) * RotateX(beta) * RotateY(gamma), identity short-cut when all zero
   double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   int zero = 1;
@@ -1212,9 +1412,12 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
                           s.mainLightIntensity * s.mainLightColour.G / 65536.0,
                           s.mainLightIntensity * s.mainLightColour.B / 65536.0};
     const double cc[3] = {col.x, col.y, col.z};
+    double auxS[3] = {0, 0, 0}, auxSp[3] = {0, 0, 0};
+    if (f.numberOfLights > 0) aux_lights(s, f, c, ray.point, n, view, delta, thr, auxS, auxSp);
     for (int k = 0; k < 3; k++) {
-      const double obj = 0.0 + (a2 + ml[k] * shadeV * shadow) * cc[k];
-      const double spec = 0.0 + ml[k] * sp * shadow;
+      double obj = 0.0 + (a2 + ml[k] * shadeV * shadow) * cc[k];
+      obj += (auxS[k] + 0.0) * cc[k];
+      const double spec = auxSp[k] + 0.0 + ml[k] * sp * shadow;
       out[k] = obj + 0.0 + spec;
     }
     out[3] = 1.0 + 0.0;
@@ -1227,7 +1430,7 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     depthZ = 1e20;
   }
   float opacity = 0.0f;
-  volumetric(s, buf, ray.count, ray.depth, out, &opacity);
+  volumetric(s, f, buf, ray.count, ray.depth, view, out, &opacity);
   const int64_t pix = (int64_t)y * W + x;
   if (img->opacity) img->opacity[pix] = to_u16((double)opacity * 65535.0);
   if (img->alpha) img->alpha[pix] = to_u16(out[3] * 65535.0);

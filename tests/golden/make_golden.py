@@ -128,6 +128,12 @@ EXAMPLES = {
     "folded_trigonometric": ("Folded trigonometric power 8.fract", {}),
     "rotated_mandelbox_1": ("rotated mandelbox 1.fract", {}),
     "stereo_hybrid": ("stereo.fract", {}),
+    # auxiliary lights: random (PlaceRandomLights), predefined, visible in the volumetric pass
+    "aux_backlight": ("Mandelbulb with backlight.fract", {}),
+    "aux_menger_predefined": ("menger sponge.fract", {}),
+    "aux_menger_1000_lights": ("menger sponge 3.fract", {}, 32, 24),
+    "aux_rotated_mandelbox_4": ("rotated mandelbox 4.fract", {}),
+    "aux_coloured_lights": ("tglad - scale 2 - coloured lights.fract", {}),
 }
 
 # Formulas no example uses, on the benchmark workloads' settings.
@@ -153,6 +159,25 @@ SYNTH_CASES = {
                           "hybrid_formula_4": 31, "hybrid_power_4": 0.05, "hybrid_iterations_4": 1,
                           "hybrid_formula_5": 2, "hybrid_power_5": 8, "hybrid_iterations_5": 2,
                           "hybrid_cyclic": 1, "N": 40}),
+}
+
+# Secondary effects on the benchmark workloads' settings.
+EFFECT_CASES = {
+    "aux_random_visible": ("mandelbulb_640x480", 40, 32,
+                           {**W.AUX_LIGHTS, "aux_light_number": 6, "aux_light_random_seed": 7, "aux_light_max_dist": 0.3,
+                            "aux_light_distribution_radius": 2.0, "aux_light_intensity": 1.0,
+                            "aux_light_visibility": 5.0, "glow_intensity": 0}),
+    "aux_predefined_penetrating": ("mandelbox_1080p", 48, 32,
+                                   {**W.AUX_LIGHTS, "aux_light_predefined_1_enabled": 1, "aux_light_predefined_1_x": 2.0,
+                                    "aux_light_predefined_1_y": -6.0, "aux_light_predefined_1_z": 1.0,
+                                    "aux_light_predefined_1_intensity": 4.0,
+                                    "aux_light_predefined_2_enabled": 1, "aux_light_predefined_2_x": -3.0,
+                                    "aux_light_predefined_2_y": -5.0, "aux_light_predefined_2_z": -2.0,
+                                    "aux_light_predefined_2_intensity": 2.0, "penetrating_lights": 1,
+                                    "ambient_occlusion_enabled": 0, "volumetric_fog_density": 0}),
+    "aux_no_shadows": ("mandelbulb_640x480", 40, 32,
+                       {**W.AUX_LIGHTS, "aux_light_number": 3, "aux_light_random_seed": 3, "aux_light_max_dist": 0.5,
+                        "aux_light_distribution_radius": 2.0, "shadows_enabled": 0}),
 }
 
 # DE fixtures of every run-time formula: (name, workload or example, keys, half-size of the
@@ -226,9 +251,12 @@ def example_scene(fname: str, extra: dict, w: int = 48, h: int = 32):
     return mb.load_settings(os.path.join(EXAMPLES_DIR, fname), DEFAULTS_FILE, ov)
 
 
-def render_example_cases(lib, manifest: dict):
-    for case, (fname, extra) in EXAMPLES.items():
-        sc = example_scene(fname, extra)
+def render_example_cases(lib, manifest: dict, only=None):
+    for case, spec in EXAMPLES.items():
+        if only and case not in only:
+            continue
+        fname, extra = spec[0], spec[1]
+        sc = example_scene(fname, extra, *spec[2:])
         ok, why = mb.supported(sc)
         assert ok, (case, why)
         w, h = sc.image_width, sc.image_height
@@ -272,6 +300,13 @@ def formula_de_all(lib, manifest: dict, npts: int = 400):
                                            "max_iter_fraction": float(mi.mean())}
         print(name, "formula", sc.formula, "analytic", sc.analitycDE, "max_iter", mi.mean(),
               "iters", np.bincount(iters).nonzero()[0][:8])
+
+
+def effect_goldens(manifest: dict):
+    """The secondary effects' example scenes and synthetic scenes."""
+    lib = build_ref()
+    render_example_cases(lib, manifest, only=[k for k in EXAMPLES if k.startswith("aux_")])
+    render_cases(lib, EFFECT_CASES, manifest)
 
 
 def build_ref() -> ctypes.CDLL:
@@ -442,10 +477,11 @@ def render_cases(lib, cases: dict, manifest: dict):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"]):
+    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"], ["effects"]):
         with open(os.path.join(HERE, "MANIFEST.json")) as f:
             manifest = json.load(f)
-        {"post": post_goldens, "formulas": formula_goldens, "all_formulas": all_formula_goldens}[sys.argv[1]](manifest)
+        {"post": post_goldens, "formulas": formula_goldens, "all_formulas": all_formula_goldens,
+         "effects": effect_goldens}[sys.argv[1]](manifest)
         with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
             json.dump(manifest, f, indent=1, sort_keys=True)
     else:

@@ -33,7 +33,7 @@ def test_unsupported_features_are_reported(mblib):
     from mandelbulber_gb300 import workloads as W
     for key, value, text in [("formula", 38, "formula"),
                              ("primitive_plane_enabled", 1, "primitive"), ("reflect", 0.5, "environment"),
-                             ("iteration_fog_enable", 1, "iteration fog"), ("aux_light_number", 3, "auxiliary")]:
+                             ("iteration_fog_enable", 1, "iteration fog"), ("raytraced_reflections", 1, "reflections")]:
         sc = W.workload("mandelbulb_640x480", **{key: value})
         ok, why = mb.supported(sc)
         assert not ok and text in why, (key, why)
