@@ -208,16 +208,30 @@ static bool uses_aux_lights(const mbgb_scene &s) {
   return false;
 }
 
-// The volumetric pass samples the march positions (sStep::point): visible aux lights.
-static bool need_step_points(const mbgb_scene &s) { return uses_aux_lights(s) && s.auxLightVisibility > 0.0; }
+// The volumetric pass samples the march positions and iteration counts (sStep::point,
+// iters): visible aux lights, fake lights, volumetric lights, iteration fog.
+static bool need_step_points(const mbgb_scene &s) {
+  return (uses_aux_lights(s) && s.auxLightVisibility > 0.0) || s.fakeLightsEnabled || s.volumetricLightEnabledAny ||
+         s.iterFogEnabled;
+}
 
 static bool need_volumetric(const mbgb_scene &s) {
   return (s.glow_intensity != 0.0) || s.fogEnabled || (s.fogDensity > 0.0) || need_step_points(s);
 }
 
-// Features that the per-pixel engine renders and the wavefront stages do not carry: scenes
+// Features that the per-pixel engine renders and the wavefront stages do not carry (aux,
+// fake and volumetric lights, iteration fog, slow shading, environment mapping): scenes
 // that use them render on the per-pixel engine.
-static bool per_pixel_only(const mbgb_scene &s) { return uses_aux_lights(s); }
+static bool per_pixel_only(const mbgb_scene &s) {
+  return uses_aux_lights(s) || s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled ||
+         s.slowShading || (!s.raytracedReflections && s.reflect > 0);
+}
+
+// The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights is carried
+// by the run-time formula path only.
+static int scene_kernel_formula(const mbgb_scene &s) {
+  return kernel_formula(s.formula, s.ifsFoldingMode || s.fakeLightsEnabled);
+}
 
 template <typename T>
 static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
@@ -327,6 +341,11 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
     f.hybridSegs = hybrid_runs(s, f.hybridForm, f.hybridCount, power);
     for (int i = 0; i < f.hybridSegs; i++) f.hybridPower[i] = (T)power[i];
   }
+  if (s.fakeLightsEnabled) {
+    for (int c = 0; c < 3; c++) f.fakeTrap[c] = (T)s.fakeLightsOrbitTrap[c];
+    f.fakeMinIter = s.fakeLightsMinIter;
+    f.fakeMaxIter = s.fakeLightsMaxIter;
+  }
 }
 
 // MainThread's per-frame preparation (src/Render3D.cpp:213-344) into a kernel parameter block.
@@ -435,6 +454,18 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   p.volLightAny = s.volumetricLightEnabledAny;
   p.iterFogOpacity = (T)s.iterFogOpacity;
   p.iterFogOpacityTrim = (T)s.iterFogOpacityTrim;
+  for (int i = 0; i < 5; i++) {
+    p.volLightEnabled[i] = s.volumetricLightEnabled[i];
+    p.volLightIntensity[i] = (T)s.volumetricLightIntensity[i];
+  }
+  rgb(p.mainLightColour, s.mainLightColour);
+  p.mainLightIntensity = (T)s.mainLightIntensity;
+  p.fakeLights = s.fakeLightsEnabled;
+  p.fakeLightsIntensity = (T)s.fakeLightsIntensity;
+  p.fakeLightsVisibility = (T)s.fakeLightsVisibility;
+  p.fakeLightsVisibilitySize = (T)s.fakeLightsVisibilitySize;
+  p.envMapping = !s.raytracedReflections && s.reflect > 0;
+  p.reflect = (T)s.reflect;
   // The volumetric pass changes the pixel only through glow, post fog, volumetric fog and
   // the visible auxiliary lights.
   p.needVolumetric = need_volumetric(s);
@@ -594,15 +625,9 @@ extern "C" mbgb_status mbgb_scene_supported(const mbgb_scene *s) {
   if (s->planeEnable || s->boxEnable || s->invertedBoxEnable || s->sphereEnable || s->invertedSphereEnable ||
       s->waterEnable || s->onlyPlane)
     return set_error(MBGB_ERR_UNSUPPORTED, "primitive objects");
-  if (s->iterFogEnabled) return set_error(MBGB_ERR_UNSUPPORTED, "iteration fog");
-  if (s->volumetricLightEnabledAny) return set_error(MBGB_ERR_UNSUPPORTED, "volumetric lights");
-  if (s->fakeLightsEnabled) return set_error(MBGB_ERR_UNSUPPORTED, "fake (orbit trap) lights");
   if (s->raytracedReflections && s->reflectionsMax > 0)
     return set_error(MBGB_ERR_UNSUPPORTED, "ray-traced reflections");
-  if (!s->raytracedReflections && s->reflect > 0)
-    return set_error(MBGB_ERR_UNSUPPORTED, "environment mapping (reflect > 0)");
   if (s->texturedBackground) return set_error(MBGB_ERR_UNSUPPORTED, "textured background");
-  if (s->slowShading) return set_error(MBGB_ERR_UNSUPPORTED, "slow shading (averaged normals)");
   if (s->image_width <= 0 || s->image_height <= 0 || s->image_width > 65536 || s->image_height > 65536)
     return set_error(MBGB_ERR_BAD_PARAM, "image size out of range");
   if (s->noOfTiles < 1) return set_error(MBGB_ERR_BAD_PARAM, "tiles must be >= 1");
@@ -1045,7 +1070,7 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
                                      uint64_t *launches, int64_t lightOff) {
   const int prec = g.prec;
   const int block = g.cfg.block;
-  const int kf = kernel_formula(scene.formula, scene.ifsFoldingMode);
+  const int kf = scene_kernel_formula(scene);
   int per_sm = std::max(1, occupancy_render(prec, kf, block));
   if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
   const int grid = c->sms * per_sm;
@@ -1458,7 +1483,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       }
     } else if (needVol) {
       maxPixPerPixel = std::max(maxPixPerPixel, g.npix);
-      int per_sm = std::max(1, occupancy_render(g.prec, kernel_formula(rep.formula, rep.ifsFoldingMode), g.cfg.block));
+      int per_sm = std::max(1, occupancy_render(g.prec, scene_kernel_formula(rep), g.cfg.block));
       if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
       maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_sm * g.cfg.block);
     }

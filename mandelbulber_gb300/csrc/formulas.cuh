@@ -28,7 +28,7 @@ __device__ __forceinline__ double m_cos(double x) { return cos(x); }
 __device__ __forceinline__ float m_cos(float x) { return cosf(x); }
 
 // Compute modes (enumCalculationMode, src/fractal.h:67-70) this path evaluates.
-constexpr int kModeNormal = 0, kModeColour = 1, kModeDelta1 = 3, kModeDelta2 = 4;
+constexpr int kModeNormal = 0, kModeColour = 1, kModeDelta1 = 3, kModeDelta2 = 4, kModeOrbitTrap = 5;
 
 // Formulas that end their orbit at r > 1024 with distance r / |tgladDE|
 // (src/fractal.cpp:1141-1148).
@@ -185,6 +185,7 @@ __device__ __noinline__ T compute_runtime(const FractalT<T> *__restrict__ fp, V3
   const bool hybrid = form == 12;
   T r = orbit_length(z);
   T minv = (sizeof(T) == 8) ? T(1e200) : T(__int_as_float(0x7f800000));
+  T orbitTrapTotal = T(0);
   int seg = 0, segk = 0;  // position in the hybrid sequence
   int L;
   for (L = 0; L < N; L++) {
@@ -706,6 +707,15 @@ __device__ __noinline__ T compute_runtime(const FractalT<T> *__restrict__ fp, V3
     } else if (MODE == kModeDelta2) {
       if (L == count) break;
     }
+    if (MODE == kModeOrbitTrap) {  // src/fractal.cpp:1121-1131
+      const V3<T> delta = z - V3<T>{f.fakeTrap[0], f.fakeTrap[1], f.fakeTrap[2]};
+      distance = length3(delta);
+      if (L >= f.fakeMinIter && L <= f.fakeMaxIter) orbitTrapTotal += T(1.0f) / (distance * distance);
+      if (distance > T(1000)) {
+        distance = orbitTrapTotal;
+        break;
+      }
+    }
     if (form == 7 || form == 10) {
       if (r > T(1000)) { distance = (r - T(2)) / tgladDE; break; }
     } else if (box_formula(form)) {
@@ -726,6 +736,7 @@ __device__ __noinline__ T compute_runtime(const FractalT<T> *__restrict__ fp, V3
     return distance;
   }
   if (MODE == kModeDelta1 || MODE == kModeDelta2) return r;
+  if (MODE == kModeOrbitTrap) return distance;
   // colouring (src/fractal.cpp:1218-1240)
   if (hybrid) {
     if (minv > T(100)) minv = T(100);

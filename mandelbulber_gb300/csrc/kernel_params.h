@@ -74,6 +74,9 @@ struct FractalT {
   int hybridSegs;
   int hybridForm[5], hybridCount[5];
   T hybridPower[5];
+  // Compute<orbitTrap> of the fake lights
+  T fakeTrap[3];
+  int fakeMinIter, fakeMaxIter;
 };
 
 // One auxiliary light (sLight, src/shaders.h:25-31): placed at random around a centre
@@ -134,6 +137,17 @@ struct ParamsT {
   const LightT<T> *lights; // device memory, numberOfLights entries
   int iterFog, volLightAny;  // imageSwitches.iterFogEnabled / volumetricLightEnabled
   T iterFogOpacity, iterFogOpacityTrim;
+  // volumetric lights: [0] the main light, [1..4] the predefined lights
+  int volLightEnabled[5];
+  T volLightIntensity[5];
+  int mainLightColour[3];
+  T mainLightIntensity;
+  // fake (orbit trap) lights (FakeLights, src/shaders.cpp:1225-1271)
+  int fakeLights;
+  T fakeLightsIntensity, fakeLightsVisibility, fakeLightsVisibilitySize;
+  // environment mapping on the default white texture (EnvMapping, src/shaders.cpp:785-811)
+  int envMapping;
+  T reflect;
 };
 
 // Per-frame camera, resolution, fractal parameter and output layers of a batch (device

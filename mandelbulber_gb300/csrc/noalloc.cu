@@ -114,6 +114,10 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   if (auxLights)
     return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
                            "auxiliary lights are placed per call, which the allocation-free entry point does not do");
+  if (scene->iterFogEnabled || scene->volumetricLightEnabledAny || scene->fakeLightsEnabled)
+    return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
+                           "iteration fog, volumetric and fake lights need step positions the allocation-free "
+                           "entry point does not keep");
   if (o.row_end == 0) o.row_end = scene->image_height;
   if (o.row_begin < 0 || o.row_end > scene->image_height || o.row_begin >= o.row_end)
     return mbgb::set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");

@@ -146,7 +146,7 @@ namespace dev {
 template <typename T, int FORMULA, int MODE>
 __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N, int &Lout, Counters &cnt,
                                      const T fparam) {
-  if (FORMULA == 0) {
+  if (FORMULA == 0 || MODE == kModeOrbitTrap) {
     int L;
     const T d = compute_runtime<T, MODE>(&f, z, N, 0, &L, fparam);
     cnt.orbit += (unsigned long long)(L + 1);
@@ -424,7 +424,9 @@ __device__ __forceinline__ void refine(const ParamsT<TP> &p, const FractalT<doub
 // Shaders in precision T (src/shaders.cpp)
 // ---------------------------------------------------------------------------
 
-// CalculateNormals, fast branch (src/shaders.cpp:675-711, 745-757)
+// CalculateNormals (src/shaders.cpp:675-757): forward differences of the distance (N x 5,
+// minN 0), or with slow shading the average of point2 x distance over the 11^3 offsets
+// point2 in [-1, 1]^3 (steps of 0.2, accumulated in double as the reference's loop does).
 template <typename T, int FORMULA>
 __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> point, const T delta, const T dist_thresh,
                                              const T detail, Counters &cnt) {
@@ -433,14 +435,29 @@ __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> po
   int L;
   bool mi;
   const int N5 = p.f.N5;
-  const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam_of(p.f));
-  const T s2 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
-                                         true, L, mi, cnt, fparam_of(p.f));
-  const T s3 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
-                                         true, L, mi, cnt, fparam_of(p.f));
-  const T s4 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
-                                         true, L, mi, cnt, fparam_of(p.f));
-  V3<T> n{s2 - s1, s3 - s1, s4 - s1};
+  V3<T> n;
+  if (!p.slowShading) {
+    const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam_of(p.f));
+    const T s2 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
+                                           true, L, mi, cnt, fparam_of(p.f));
+    const T s3 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
+                                           true, L, mi, cnt, fparam_of(p.f));
+    const T s4 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
+                                           true, L, mi, cnt, fparam_of(p.f));
+    n = V3<T>{s2 - s1, s3 - s1, s4 - s1};
+  } else {
+    n = V3<T>{T(0), T(0), T(0)};
+    for (double px = -1.0; px <= 1.0; px += 0.2) {
+      for (double py = -1.0; py <= 1.0; py += 0.2) {
+        for (double pz = -1.0; pz <= 1.0; pz += 0.2) {
+          const V3<T> p2{(T)px, (T)py, (T)pz};
+          const T dist = calc_distance<T, FORMULA>(p.f, point + p2 * dn, detail, N5, p.f.minN, true, L, mi, cnt,
+                                                   fparam_of(p.f));
+          n = n + p2 * dist;
+        }
+      }
+    }
+  }
   if (n.x == T(0) && n.y == T(0) && n.z == T(0)) {
     n.x = T(1);
   } else {
@@ -449,16 +466,46 @@ __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> po
   return n;
 }
 
-// MainShadow (src/shaders.cpp:480-570), without iteration fog / volumetric lights.
-// `detail` is the shared detailSize state; the reference leaves it at the float-rounded threshold.
+// IterOpacity (src/shaders.cpp:1210-1218)
+template <typename T>
+__device__ __forceinline__ T iter_opacity(const T step, const T iters, const T maxN, const T trim, const T opacitySp) {
+  T opacity = (iters - trim) / maxN;
+  if (opacity < T(0)) opacity = T(0);
+  opacity *= opacity;
+  opacity *= step * opacitySp;
+  if (opacity > T(1)) opacity = T(1);
+  return opacity;
+}
+
+// The threshold a secondary ray compares against, held in a float as the reference does:
+// with iteration fog or volumetric lights the one of the sample's own distance from the
+// eye, else the hit's.
+template <typename T>
+__device__ __forceinline__ T secondary_thresh(const ParamsT<T> &p, const V3<T> point2, const V3<T> eye,
+                                              const T dist_thresh) {
+  float t;
+  if (p.iterFog || p.volLightAny) {
+    if (!p.constantDEThreshold) t = (float)(length3(point2 - eye) * p.resolution * p.persp / p.quality);
+    else t = (float)p.quality;
+  } else {
+    t = (float)dist_thresh;
+  }
+  return (T)t;
+}
+
+// MainShadow (src/shaders.cpp:480-570). `detail` is the shared detailSize state (left at the
+// last float threshold), `itersOut` the shared iteration count. With iteration fog or
+// volumetric lights the march steps at DE factor 1, each sample compares against its own
+// eye-distance threshold and iteration fog absorbs along the way.
 template <typename T, int FORMULA>
 __device__ __forceinline__ T main_shadow(const ParamsT<T> &p, const V3<T> point, const T dist_thresh, const T delta,
-                                         T &detail, const FrameIO &io, Counters &cnt) {
+                                         const V3<T> eye, T &detail, int &itersOut, const FrameIO &io,
+                                         Counters &cnt) {
   T factor = delta / p.resolution;
   if (!p.penetrating) factor = p.viewDistanceMax;
   T dist = dist_thresh;
   detail = dist_thresh;
-  const T DE_factor = p.DE_factor;
+  const T DE_factor = (p.iterFog || p.volLightAny) ? T(1) : p.DE_factor;
   T start = dist_thresh;
   if (p.f.interiorMode) start = dist_thresh * DE_factor;
   T shadowTemp = T(1);
@@ -466,16 +513,13 @@ __device__ __forceinline__ T main_shadow(const ParamsT<T> &p, const V3<T> point,
   T maxSoft = T(0);
   const bool bSoft = p.softShadow != 0;
   const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
-  // the reference stores the threshold in a float (src/shaders.cpp:515)
-  const float thr_f = (float)dist_thresh;
-  const T thr = (T)thr_f;
   int guard = 0;
   for (T i = start; i < factor; i += dist * DE_factor) {
     const V3<T> point2 = point + lv * i;
+    const T thr = secondary_thresh(p, point2, eye, dist_thresh);
     detail = thr;
-    int L;
     bool mi;
-    dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt, fparam_of(p.f));
+    dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, itersOut, mi, cnt, fparam_of(p.f));
     if (bSoft) {
       T angle = (dist - thr) / i;
       if (angle < T(0)) angle = T(0);
@@ -484,6 +528,10 @@ __device__ __forceinline__ T main_shadow(const ParamsT<T> &p, const V3<T> point,
       if (p.penetrating) softShadow *= (factor - i) / factor;
       if (softShadow < T(0)) softShadow = T(0);
       if (softShadow > maxSoft) maxSoft = softShadow;
+    }
+    if (p.iterFog) {
+      const T opacity = iter_opacity(dist * DE_factor, T(itersOut), T(p.f.N), p.iterFogOpacityTrim, p.iterFogOpacity);
+      shadowTemp -= opacity * (factor - i) / factor;
     }
     if (dist < thr || shadowTemp < T(0)) {
       shadowTemp -= (factor - i) / factor;
@@ -522,15 +570,15 @@ __device__ __forceinline__ T fast_ao(const ParamsT<T> &p, const V3<T> point, con
   return ao;
 }
 
-// AmbientOcclusion, ray-traced (src/shaders.cpp:607-673), white light map:
-// every direction weighs (255, 255, 255).
+// AmbientOcclusion, ray-traced (src/shaders.cpp:607-673), white light map: every direction
+// weighs (255, 255, 255). Iteration fog and volumetric lights change the threshold and add
+// absorption as in MainShadow.
 template <typename T, int FORMULA>
 __device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, const T delta, const T dist_thresh,
-                                        const T lastDist, const T detail, Counters &cnt) {
+                                        const T lastDist, const T detail, const V3<T> eye, int &itersOut,
+                                        Counters &cnt) {
   const T start_dist = delta;
   const T end_dist = delta / p.resolution;
-  const float thr_f = (float)dist_thresh;
-  const T thr = (T)thr_f;
   V3<T> AO{T(0), T(0), T(0)};
   for (int v = 0; v < p.aoCount; v++) {
     const V3<T> dir{__ldg(&p.aoVec[3 * v + 0]), __ldg(&p.aoVec[3 * v + 1]), __ldg(&p.aoVec[3 * v + 2])};
@@ -539,9 +587,13 @@ __device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, 
     int guard = 0;
     for (T r = start_dist; r < end_dist && guard < kMaxSecondarySteps; r += dist * T(2), guard++) {
       const V3<T> point2 = point + dir * r;
-      int L;
       bool mi;
-      dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt, fparam_of(p.f));
+      dist = calc_distance<T, FORMULA>(p.f, point2, detail, p.f.N, p.f.minN, false, itersOut, mi, cnt, fparam_of(p.f));
+      if (p.iterFog) {
+        const T opacity = iter_opacity(dist * T(2), T(itersOut), T(p.f.N), p.iterFogOpacityTrim, p.iterFogOpacity);
+        shadowTemp -= opacity * (end_dist - r) / end_dist;
+      }
+      const T thr = secondary_thresh(p, point2, eye, dist_thresh);
       if (dist < thr || mi || shadowTemp < T(0)) {
         shadowTemp -= (end_dist - r) / end_dist;
         if (shadowTemp < T(0)) shadowTemp = T(0);
@@ -559,31 +611,30 @@ __device__ __forceinline__ V3<T> ray_ao(const ParamsT<T> &p, const V3<T> point, 
   return AO;
 }
 
-// IterOpacity (src/shaders.cpp:1210-1218)
-template <typename T>
-__device__ __forceinline__ T iter_opacity(const T step, const T iters, const T maxN, const T trim, const T opacitySp) {
-  T opacity = (iters - trim) / maxN;
-  if (opacity < T(0)) opacity = T(0);
-  opacity *= opacity;
-  opacity *= step * opacitySp;
-  if (opacity > T(1)) opacity = T(1);
-  return opacity;
-}
-
-// The threshold a secondary ray compares against, held in a float as the reference does:
-// with iteration fog or volumetric lights the one of the sample's own distance from the
-// eye, else the hit's.
-template <typename T>
-__device__ __forceinline__ T secondary_thresh(const ParamsT<T> &p, const V3<T> point2, const V3<T> eye,
-                                              const T dist_thresh) {
-  float t;
-  if (p.iterFog || p.volLightAny) {
-    if (!p.constantDEThreshold) t = (float)(length3(point2 - eye) * p.resolution * p.persp / p.quality);
-    else t = (float)p.quality;
-  } else {
-    t = (float)dist_thresh;
-  }
-  return (T)t;
+// EnvMapping (src/shaders.cpp:785-811) on the default texture (src/texture.cpp:67-116): a
+// white 100 x 100 bitmap, bilinearly interpolated, black in its last row. Evaluated in
+// double under both policies: the 8-bit truncation of the interpolated texel and the black
+// row turn last-bit differences of the coordinates into visible steps.
+__device__ __forceinline__ double env_mapping(const V3<double> normal, const V3<double> view) {
+  using T = double;
+  const T d = -dot3(view, normal);
+  const V3<T> reflect = normal * T(2) * d + view;
+  const T alfaTexture = m_atan2(reflect.y, reflect.x) + T(kPI);
+  T betaTexture = m_atan2(reflect.z, m_sqrt(reflect.x * reflect.x + reflect.y * reflect.y));
+  const T texWidth = T(100), texHeight = T(100);
+  if (betaTexture > T(0.5) * T(kPI)) betaTexture = T(0.5) * T(kPI) - betaTexture;
+  if (betaTexture < T(-0.5) * T(kPI)) betaTexture = T(-0.5) * T(kPI) + betaTexture;
+  T dtx = (alfaTexture / (T(2) * T(kPI))) * texWidth + texWidth * T(8.25);
+  T dty = (betaTexture / T(kPI) + T(0.5)) * texHeight + texHeight * T(8);
+  dtx = fmod(dtx, texWidth);
+  dty = fmod(dty, texHeight);
+  if (dtx < T(0)) dtx = T(0);
+  if (dty < T(0)) dty = T(0);
+  if (!(dtx >= T(0) && dtx < texWidth && dty >= T(0) && dty < texHeight - T(1))) return T(0);
+  const T rx = dtx - T((int)dtx), ry = dty - T((int)dty);
+  const T v = T(255) * (T(1) - rx) * (T(1) - ry) + T(255) * (rx) * (T(1) - ry) + T(255) * (T(1) - rx) * ry +
+              T(255) * (rx * ry);
+  return T((unsigned char)(int)v) / T(256);
 }
 
 // AuxShadow (src/shaders.cpp:1069-1132): march from the point towards a light at `distance`,
@@ -726,12 +777,17 @@ __device__ __forceinline__ V3<T> background(const ParamsT<T> &p, const V3<T> vie
   return V3<T>{T(px[0]) / T(65536), T(px[1]) / T(65536), T(px[2]) / T(65536)};
 }
 
-// VolumetricShader (src/shaders.cpp:185-478): glow, post fog and volumetric fog over
-// the primary step buffer, far to near, merging steps shorter than distThresh * quality.
-template <typename T>
+// VolumetricShader (src/shaders.cpp:185-478): glow, visible aux lights, fake lights,
+// volumetric lights, post fog, volumetric fog and iteration fog over the primary step
+// buffer, far to near, merging steps shorter than distThresh * quality. The volumetric
+// lights and the iteration fog trace MainShadow / AuxShadow / AmbientOcclusion from the
+// step positions with the pixel's delta and last distance; `detail` and `itersOut` carry
+// the shared CalculateDistance state through them.
+template <typename T, int FORMULA>
 __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
-                                           const T depth, const V3<T> eye, const V3<T> view, T out[4],
-                                           float &totalOpacityOut, bool &opacitySet) {
+                                           const T depth, const V3<T> eye, const V3<T> view, const T delta,
+                                           const T lastDist, T &detail, int &itersOut, const FrameIO &io,
+                                           Counters &cnt, T out[4], float &totalOpacityOut, bool &opacitySet) {
   float totalOpacity = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
   T glowN = T(1) - glow;
@@ -802,6 +858,48 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
         }
       }
     }
+    // fake lights (orbit trap, src/shaders.cpp:298-307)
+    if (p.fakeLights) {
+      const V3<T> point = eye + view * sb.scan[sb.at(index)];
+      int L;
+      Counters c2{0, 0, 0, 0};
+      T r = compute<T, FORMULA, 5>(p.f, point, p.f.N, L, c2, fparam_of(p.f));
+      cnt.orbit += c2.orbit;
+      cnt.calls += c2.calls;
+      r = m_sqrt(T(1.0f) / (r + T(1.0e-30f)));
+      const T fakeLight = T(1) / (m_pow(r, T(10) / p.fakeLightsVisibilitySize) *
+                                      m_pow(T(10), T(10) / p.fakeLightsVisibilitySize) + T(1e-100));
+      out[0] += fakeLight * step * p.fakeLightsVisibility;
+      out[1] += fakeLight * step * p.fakeLightsVisibility;
+      out[2] += fakeLight * step * p.fakeLightsVisibility;
+      out[3] += fakeLight * step * p.fakeLightsVisibility;
+    }
+    // volumetric lights with shadows in fog (src/shaders.cpp:309-343)
+    if (p.volLightAny) {
+      const V3<T> point = eye + view * sb.scan[sb.at(index)];
+      const T thrStep = sb.thr[sb.at(index)];
+      for (int i = 0; i < 5; i++) {
+        if (i == 0 && p.volLightEnabled[0]) {
+          const T sh = main_shadow<T, FORMULA>(p, point, thrStep, delta, eye, detail, itersOut, io, cnt);
+          out[0] += sh * step * p.volLightIntensity[0] * T(p.mainLightColour[0]) / T(65536);
+          out[1] += sh * step * p.volLightIntensity[0] * T(p.mainLightColour[1]) / T(65536);
+          out[2] += sh * step * p.volLightIntensity[0] * T(p.mainLightColour[2]) / T(65536);
+          out[3] += (sh + sh + sh) / T(3) * step * p.volLightIntensity[0];
+        }
+        if (i > 0 && p.numberOfLights > 0 && p.lights[i - 1].enabled && p.volLightEnabled[i]) {
+          const LightT<T> L = p.lights[i - 1];
+          const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - point;
+          const T distance = length3(d);
+          const T distance2 = distance * distance;
+          const V3<T> lv = normalize3(d);
+          const T light = aux_shadow<T, FORMULA>(p, point, distance, lv, delta, thrStep, eye, detail, itersOut, cnt);
+          out[0] += light * T(L.colour[0]) / T(65536) * p.volLightIntensity[i] * step / distance2;
+          out[1] += light * T(L.colour[1]) / T(65536) * p.volLightIntensity[i] * step / distance2;
+          out[2] += light * T(L.colour[2]) / T(65536) * p.volLightIntensity[i] * step / distance2;
+          out[3] += light * p.volLightIntensity[i] * step / distance2;
+        }
+      }
+    }
     // basic fog
     if (p.postFog) {
       T fogDensity = step / p.fogVisibility;
@@ -834,6 +932,60 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
       out[2] = fogDensity * fb / T(65536) + (T(1) - fogDensity) * out[2];
       totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
       out[3] = fogDensity + (T(1) - fogDensity) * out[3];
+    }
+    // iteration fog (src/shaders.cpp:385-466): the fog colour by the record's iteration
+    // count, lit by the main light and the predefined lights (shadowed) and by ray AO
+    if (p.iterFog) {
+      const int L = sb.iters[sb.at(index)];
+      const T N = T(p.f.N);
+      T opacity = iter_opacity(step, T(L), N, p.iterFogOpacityTrim, p.iterFogOpacity);
+      if (opacity > T(0)) {
+        const V3<T> point = eye + view * sb.scan[sb.at(index)];
+        const T thrStep = sb.thr[sb.at(index)];
+        const T iterFactor = T(2) * (T(L) - p.iterFogOpacityTrim) / (N - p.iterFogOpacityTrim);
+        T k = iterFactor;
+        if (k > T(1)) k = T(1);
+        if (k < T(0)) k = T(0);
+        T kn = T(1) - k;
+        T fogCol[3];
+        for (int c = 0; c < 3; c++) fogCol[c] = (T(p.fogCol1[c]) * kn + T(p.fogCol2[c]) * k);
+        T k2 = iterFactor - T(1);
+        if (k2 < T(0)) k2 = T(0);
+        if (k2 > T(1)) k2 = T(1);
+        kn = T(1) - k2;
+        for (int c = 0; c < 3; c++) fogCol[c] = (fogCol[c] * kn + T(p.fogCol3[c]) * k2);
+        T newColour[3] = {T(0), T(0), T(0)};
+        for (int i = 0; i < 5; i++) {
+          if (i == 0) {
+            if (p.mainLightIntensity * p.directLight > T(0)) {
+              const T sh = main_shadow<T, FORMULA>(p, point, thrStep, delta, eye, detail, itersOut, io, cnt);
+              for (int c = 0; c < 3; c++)
+                newColour[c] += sh * T(p.mainLightColour[c]) / T(65536) * p.mainLightIntensity * p.directLight;
+            }
+          }
+          if (i > 0 && p.numberOfLights > 0 && p.lights[i - 1].enabled) {
+            const LightT<T> Lt = p.lights[i - 1];
+            const V3<T> d = V3<T>{Lt.pos[0], Lt.pos[1], Lt.pos[2]} - point;
+            const T distance = length3(d);
+            const T distance2 = distance * distance;
+            const V3<T> lv = normalize3(d);
+            const T light = aux_shadow<T, FORMULA>(p, point, distance, lv, delta, thrStep, eye, detail, itersOut, cnt);
+            const T intensity = Lt.intensity * T(100);
+            for (int c = 0; c < 3; c++) newColour[c] += light * T(Lt.colour[c]) / T(65536) / distance2 * intensity;
+          }
+        }
+        if (p.ao && !p.fastAO) {
+          const V3<T> AO = ray_ao<T, FORMULA>(p, point, delta, thrStep, lastDist, detail, eye, itersOut, cnt);
+          newColour[0] += AO.x * p.globalIlum;
+          newColour[1] += AO.y * p.globalIlum;
+          newColour[2] += AO.z * p.globalIlum;
+        }
+        if (opacity > T(1)) opacity = T(1);
+        for (int c = 0; c < 3; c++)
+          out[c] = out[c] * (T(1) - opacity) + newColour[c] * opacity * fogCol[c] / T(65536);
+        totalOpacity = (float)(opacity + (T(1) - opacity) * (T)totalOpacity);
+        out[3] = opacity + (T(1) - opacity) * out[3];
+      }
     }
     if (totalOpacity > 1.0f) totalOpacity = 1.0f;
     if (out[3] > T(1)) out[3] = T(1);
@@ -907,19 +1059,21 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
   double depth = rs.scan;
   const T dist_thresh = (T)rs.distThresh;
   T detail = (T)rs.distThresh;
+  int itersOut = rs.iters;   // the shared calcParam->itersOut
+  // shaderInputData.delta (src/Render3D.cpp:530-531), for hits and background alike
+  T delta;
+  if (p.constantDEThreshold) delta = (T)rs.scan * p.resolution * p.persp;
+  else delta = dist_thresh * p.quality;
   if (rs.found) {
-    // ObjectShader (src/shaders.cpp:21-112), no fake lights, no env mapping
+    // ObjectShader (src/shaders.cpp:21-112)
     const V3<T> point{(T)rs.point[0], (T)rs.point[1], (T)rs.point[2]};
-    T delta;
-    if (p.constantDEThreshold) delta = (T)rs.scan * p.resolution * p.persp;
-    else delta = dist_thresh * p.quality;
     const V3<T> n = calc_normal<T, FORMULA>(p, point, delta, dist_thresh, detail, cnt);
     const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
     T shade = dot3(n, lv);
     if (shade < T(0)) shade = T(0);
     const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
     T shadow = T(1);
-    if (p.shadow) shadow = main_shadow<T, FORMULA>(p, point, dist_thresh, delta, detail, io, cnt);
+    if (p.shadow) shadow = main_shadow<T, FORMULA>(p, point, dist_thresh, delta, startT, detail, itersOut, io, cnt);
     // MainSpecular (src/shaders.cpp:770-783)
     V3<T> half = normalize3(lv - viewT);
     T shade2 = dot3(n, half);
@@ -935,25 +1089,52 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
         const T a = fast_ao<T, FORMULA>(p, point, n, dist_thresh, detail, cnt);
         ambient = {a, a, a};
       } else {
-        ambient = ray_ao<T, FORMULA>(p, point, delta, dist_thresh, (T)rs.dist, detail, cnt);
+        ambient = ray_ao<T, FORMULA>(p, point, delta, dist_thresh, (T)rs.dist, detail, startT, itersOut, cnt);
       }
     }
     const V3<T> ambient2{ambient.x * p.globalIlum, ambient.y * p.globalIlum, ambient.z * p.globalIlum};
+    // environment mapping
+    const T env = (p.envMapping ? (T)env_mapping(V3<double>{(double)n.x, (double)n.y, (double)n.z}, view) : T(0)) *
+                  p.reflect;
     // auxiliary lights
     T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
-    if (p.numberOfLights > 0) {
-      int itersOut = rs.iters;
+    if (p.numberOfLights > 0)
       aux_lights<T, FORMULA>(p, point, n, viewT, delta, dist_thresh, startT, detail, itersOut, cnt, aux, auxSpec);
+    // fake (orbit trap) lights (FakeLights, src/shaders.cpp:1225-1271)
+    T fake = T(0), fakeSpec = T(0);
+    if (p.fakeLights) {
+      const T dl = dist_thresh * p.smoothness;
+      int L;
+      const T rr = compute<T, FORMULA, 5>(p.f, point, p.f.N, L, cnt, fparam_of(p.f));
+      const T fakeLight = p.fakeLightsIntensity / rr;
+      const T r = T(1) / (rr + T(1e-30));
+      const T rx = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + dl, point.y + T(0), point.z + T(0)}, p.f.N, L,
+                                                   cnt, fparam_of(p.f)) + T(1e-30));
+      const T ry = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + dl, point.z + T(0)}, p.f.N, L,
+                                                   cnt, fparam_of(p.f)) + T(1e-30));
+      const T rz = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dl}, p.f.N, L,
+                                                   cnt, fparam_of(p.f)) + T(1e-30));
+      V3<T> fln{r - rx, r - ry, r - rz};
+      if (!(fln.x == T(0) && fln.y == T(0) && fln.z == T(0))) fln = normalize3(fln);
+      T fakeLight2 = fakeLight * dot3(n, fln);
+      if (fakeLight2 < T(0)) fakeLight2 = T(0);
+      fake = fakeLight2;
+      const V3<T> fh = normalize3(fln - viewT);
+      T fs = dot3(n, fh);
+      if (fs < T(0)) fs = T(0);
+      fs = m_pow(fs, T(30)) * fakeLight;
+      if (fs > T(15)) fs = T(15);
+      fakeSpec = fs;
     }
-    T objR = T(0) + (ambient2.x + p.mainLight[0] * shadeV * shadow) * colour.x;
-    T objG = T(0) + (ambient2.y + p.mainLight[1] * shadeV * shadow) * colour.y;
-    T objB = T(0) + (ambient2.z + p.mainLight[2] * shadeV * shadow) * colour.z;
-    objR += (aux[0] + T(0)) * colour.x;
-    objG += (aux[1] + T(0)) * colour.y;
-    objB += (aux[2] + T(0)) * colour.z;
-    const T specR = auxSpec[0] + T(0) + p.mainLight[0] * spec * shadow;
-    const T specG = auxSpec[1] + T(0) + p.mainLight[1] * spec * shadow;
-    const T specB = auxSpec[2] + T(0) + p.mainLight[2] * spec * shadow;
+    T objR = env * ambient.x + (ambient2.x + p.mainLight[0] * shadeV * shadow) * colour.x;
+    T objG = env * ambient.y + (ambient2.y + p.mainLight[1] * shadeV * shadow) * colour.y;
+    T objB = env * ambient.z + (ambient2.z + p.mainLight[2] * shadeV * shadow) * colour.z;
+    objR += (aux[0] + fake) * colour.x;
+    objG += (aux[1] + fake) * colour.y;
+    objB += (aux[2] + fake) * colour.z;
+    const T specR = auxSpec[0] + fakeSpec + p.mainLight[0] * spec * shadow;
+    const T specG = auxSpec[1] + fakeSpec + p.mainLight[1] * spec * shadow;
+    const T specB = auxSpec[2] + fakeSpec + p.mainLight[2] * spec * shadow;
     result[0] = objR + T(0) + specR;
     result[1] = objG + T(0) + specG;
     result[2] = objB + T(0) + specB;
@@ -970,7 +1151,9 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
   bool opacitySet = false;
   // the volumetric pass sees the march depth even for background pixels: the
   // shader input is filled before the depth becomes 1e20 (src/Render3D.cpp:518-541)
-  if (p.needVolumetric) volumetric<T>(p, sb, rs.buffCount, (T)rs.scan, startT, viewT, result, totalOpacity, opacitySet);
+  if (p.needVolumetric)
+    volumetric<T, FORMULA>(p, sb, rs.buffCount, (T)rs.scan, startT, viewT, delta, (T)rs.dist, detail, itersOut, io, cnt,
+                           result, totalOpacity, opacitySet);
 
   // buffer writes (src/Render3D.cpp:569-589)
   if (io.opacity) io.opacity[pix] = to_u16_x86((double)totalOpacity * 65535.0);

@@ -177,7 +177,7 @@ struct Calc {
   const Derived *d;
 };
 
-enum { kNormal = 0, kColour = 1, kDelta1 = 3, kDelta2 = 4 };
+enum { kNormal = 0, kColour = 1, kDelta1 = 3, kDelta2 = 4, kOrbitTrap = 5 };
 
 bool box_like(int f) { return f == 8 || f == 17 || f == 18 || f == 37; }
 
@@ -227,6 +227,7 @@ double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
   Vec cst = s.juliaMode ? Vec{s.julia[0], s.julia[1], s.julia[2]} : mul(z, s.constantFactor);
   double r = len(z);
   double minv = 1e200;
+  double trapTotal = 0.0;
   const Vec mbOff{s.mboxOffset[0], s.mboxOffset[1], s.mboxOffset[2]};
   const Vec ifsOff{s.ifsOffset[0], s.ifsOffset[1], s.ifsOffset[2]};
   int L;
@@ -691,6 +692,14 @@ double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
     } else if (mode == kDelta2) {
       if (L == count) break;
     }
+    if (mode == kOrbitTrap) {  // src/fractal.cpp:1121-1131
+      distance = len(sub(z, Vec{s.fakeLightsOrbitTrap[0], s.fakeLightsOrbitTrap[1], s.fakeLightsOrbitTrap[2]}));
+      if (L >= s.fakeLightsMinIter && L <= s.fakeLightsMaxIter) trapTotal += (1.0f / (distance * distance));
+      if (distance > 1000) {
+        distance = trapTotal;
+        break;
+      }
+    }
     if (form == 7 || form == 10) {
       if (r > 1000) { distance = (r - 2.0) / tDE; break; }
     } else if (box_like(form)) {
@@ -711,6 +720,7 @@ double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
     return distance;
   }
   if (mode == kDelta1 || mode == kDelta2) return r;
+  if (mode == kOrbitTrap) return distance;
   if (hybrid) {
     if (minv > 100) minv = 100;
     if (distance > 20) distance = 20;
@@ -916,6 +926,24 @@ bool level_set(const mbgb_scene &s, Calc &c, Vec start, Vec dir, Ray &ray) {
   return false;
 }
 
+double iter_opacity(double step, double iters, double maxN, double trim, double sp) {
+  double o = (iters - trim) / maxN;
+  if (o < 0.0) o = 0.0;
+  o *= o;
+  o *= step * sp;
+  if (o > 1.0) o = 1.0;
+  return o;
+}
+
+// the float threshold of the secondary rays (MainShadow / AuxShadow / AmbientOcclusion)
+float secondary_thresh(const mbgb_scene &s, Vec p2, Vec eye, double thr) {
+  if (s.iterFogEnabled || s.volumetricLightEnabledAny) {
+    if (!s.constantDEThreshold) return (float)(len(sub(p2, eye)) * s.resolution * s.persp / s.quality);
+    return (float)s.quality;
+  }
+  return (float)thr;
+}
+
 Vec calculate_normals(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr) {
   double d = delta * s.smoothness;
   if (s.interiorMode) d = thr * s.quality * 0.2 * s.smoothness;
@@ -924,11 +952,21 @@ Vec calculate_normals(const mbgb_scene &s, Calc &c, Vec p, double delta, double 
   c.minN = 0;
   c.normalMode = true;
   bool mi;
-  const double s1 = calculate_distance(c, p, &mi);
-  const double s2 = calculate_distance(c, Vec{p.x + d, p.y + 0.0, p.z + 0.0}, &mi);
-  const double s3 = calculate_distance(c, Vec{p.x + 0.0, p.y + d, p.z + 0.0}, &mi);
-  const double s4 = calculate_distance(c, Vec{p.x + 0.0, p.y + 0.0, p.z + d}, &mi);
-  Vec n{s2 - s1, s3 - s1, s4 - s1};
+  Vec n{0, 0, 0};
+  if (!s.slowShading) {
+    const double s1 = calculate_distance(c, p, &mi);
+    const double s2 = calculate_distance(c, Vec{p.x + d, p.y + 0.0, p.z + 0.0}, &mi);
+    const double s3 = calculate_distance(c, Vec{p.x + 0.0, p.y + d, p.z + 0.0}, &mi);
+    const double s4 = calculate_distance(c, Vec{p.x + 0.0, p.y + 0.0, p.z + d}, &mi);
+    n = Vec{s2 - s1, s3 - s1, s4 - s1};
+  } else {
+    // averaged binary central difference (src/shaders.cpp:714-742): minN stays as it was
+    c.minN = minN0;
+    Vec q;
+    for (q.x = -1.0; q.x <= 1.0; q.x += 0.2)
+      for (q.y = -1.0; q.y <= 1.0; q.y += 0.2)
+        for (q.z = -1.0; q.z <= 1.0; q.z += 0.2) n = add(n, mul(q, calculate_distance(c, add(p, mul(q, d)), &mi)));
+  }
   c.N = N0;
   c.minN = minN0;
   c.normalMode = false;
@@ -937,12 +975,12 @@ Vec calculate_normals(const mbgb_scene &s, Calc &c, Vec p, double delta, double 
   return n;
 }
 
-double main_shadow(const mbgb_scene &s, Calc &c, Vec p, Vec light, double thr, double delta) {
+double main_shadow(const mbgb_scene &s, Calc &c, Vec p, Vec light, double thr, double delta, Vec eye) {
   double factor = delta / s.resolution;
   if (!s.penetratingLights) factor = s.viewDistanceMax;
   double dist = thr;
   c.detail = thr;
-  const double DE_factor = s.DE_factor;
+  const double DE_factor = (s.iterFogEnabled || s.volumetricLightEnabledAny) ? 1.0 : s.DE_factor;
   double start = thr;
   if (s.interiorMode) start = thr * DE_factor;
   double shadowTemp = 1.0;
@@ -951,7 +989,7 @@ double main_shadow(const mbgb_scene &s, Calc &c, Vec p, Vec light, double thr, d
   const bool bSoft = (!s.iterFogEnabled && !s.limits_enabled && !s.iterThresh) && softRange > 0.0;
   for (double i = start; i < factor; i += dist * DE_factor) {
     const Vec p2 = add(p, mul(light, i));
-    const float thr_f = (float)thr;  // the reference's float threshold
+    const float thr_f = secondary_thresh(s, p2, eye, thr);  // the reference's float threshold
     c.detail = thr_f;
     bool mi;
     dist = calculate_distance(c, p2, &mi);
@@ -964,6 +1002,10 @@ double main_shadow(const mbgb_scene &s, Calc &c, Vec p, Vec light, double thr, d
       if (soft < 0) soft = 0;
       if (soft > maxSoft) maxSoft = soft;
     }
+    const double opacity = s.iterFogEnabled
+                               ? iter_opacity(dist * DE_factor, c.itersOut, s.N, s.iterFogOpacityTrim, s.iterFogOpacity)
+                               : 0.0;
+    shadowTemp -= opacity * (factor - i) / factor;
     if (dist < thr_f || shadowTemp < 0.0) {
       shadowTemp -= (factor - i) / factor;
       if (!s.penetratingLights) shadowTemp = 0.0;
@@ -988,7 +1030,7 @@ double fast_ao(const mbgb_scene &s, Calc &c, Vec p, Vec n, double thr) {
 }
 
 double ray_ao(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr, double lastDist,
-              const std::vector<Vec> &dirs) {
+              const std::vector<Vec> &dirs, Vec eye) {
   const double end = delta / s.resolution;
   double AO = 0;
   for (const Vec &v : dirs) {
@@ -996,9 +1038,13 @@ double ray_ao(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr, dou
     double sh = 1.0;
     for (double r = delta; r < end; r += dist * 2.0) {
       bool mi;
-      dist = calculate_distance(c, add(p, mul(v, r)), &mi);
-      const float thr_f = (float)thr;
-      if (dist < thr_f || mi || sh < 0.0) {
+      const Vec p2 = add(p, mul(v, r));
+      dist = calculate_distance(c, p2, &mi);
+      const double opacity = s.iterFogEnabled
+                                 ? iter_opacity(dist * 2.0, c.itersOut, s.N, s.iterFogOpacityTrim, s.iterFogOpacity)
+                                 : 0.0;
+      sh -= opacity * (end - r) / end;
+      if (dist < secondary_thresh(s, p2, eye, thr) || mi || sh < 0.0) {
         sh -= (end - r) / end;
         if (sh < 0.0) sh = 0.0;
         break;
@@ -1007,6 +1053,27 @@ double ray_ao(const mbgb_scene &s, Calc &c, Vec p, double delta, double thr, dou
     AO += sh * 255;
   }
   return AO / (dirs.size() * 256.0);
+}
+
+// EnvMapping (src/shaders.cpp:785-811) on the default white 100 x 100 texture
+double env_mapping(Vec n, Vec view) {
+  const double d = -dot(view, n);
+  const Vec r = add(mul(mul(n, 2.0), d), view);
+  const double alfa = atan2(r.y, r.x) + M_PI;
+  double beta = atan2(r.z, sqrt(r.x * r.x + r.y * r.y));
+  if (beta > 0.5 * M_PI) beta = 0.5 * M_PI - beta;
+  if (beta < -0.5 * M_PI) beta = -0.5 * M_PI + beta;
+  double x = (alfa / (2.0 * M_PI)) * 100.0 + 100.0 * 8.25;
+  double y = (beta / (M_PI) + 0.5) * 100.0 + 100.0 * 8.0;
+  x = fmod(x, 100.0);
+  y = fmod(y, 100.0);
+  if (x < 0) x = 0;
+  if (y < 0) y = 0;
+  if (!(x >= 0 && x < 100 && y >= 0 && y < 100 - 1.0)) return 0.0;
+  const double rx = (x - (int)x), ry = (y - (int)y);
+  const unsigned char v = (unsigned char)(255 * (1.0 - rx) * (1.0 - ry) + 255 * (rx) * (1.0 - ry) +
+                                          255 * (1.0 - rx) * ry + 255 * (rx * ry));
+  return v / 256.0;
 }
 
 void index_to_colour(const mbgb_scene &s, int index, int out[3]) {
@@ -1066,8 +1133,71 @@ Vec background(const mbgb_scene &s, Vec view) {
   return {px[0] / 65536.0, px[1] / 65536.0, px[2] / 65536.0};
 }
 
-void volumetric(const mbgb_scene &s, const Frame &f, const std::vector<Step> &buf, int count, double depth, Vec view,
-                double out[4], float *opacity) {
+// AuxShadow (src/shaders.cpp:1069-1132)
+double aux_shadow(const mbgb_scene &s, Calc &c, Vec p, double distance, Vec lv, double delta, double thr, Vec eye) {
+  double dist = delta;
+  double shadowTemp = 1.0;
+  const double def = (s.iterFogEnabled || s.volumetricLightEnabledAny) ? 1.0 : s.DE_factor;
+  for (double i = delta; i < distance; i += dist * def) {
+    const Vec p2 = add(p, mul(lv, i));
+    bool mi = false;
+    dist = calculate_distance(c, p2, &mi);
+    const double opacity = s.iterFogEnabled
+                               ? iter_opacity(dist * def, c.itersOut, s.N, s.iterFogOpacityTrim, s.iterFogOpacity)
+                               : 0.0;
+    shadowTemp -= opacity * (distance - i) / distance;
+    if (dist < secondary_thresh(s, p2, eye, thr) || mi || shadowTemp < 0.0) {
+      if (s.penetratingLights) {
+        shadowTemp -= (distance - i) / distance;
+        if (shadowTemp < 0.0) shadowTemp = 0.0;
+      } else {
+        shadowTemp = 0.0;
+      }
+      break;
+    }
+  }
+  return shadowTemp;
+}
+
+// AuxLightsShader / LightShading (src/shaders.cpp:997-1067)
+void aux_lights(const mbgb_scene &s, const Frame &f, Calc &c, Vec p, Vec n, Vec view, double delta, double thr,
+                double shade_out[3], double spec_out[3]) {
+  for (int k = 0; k < 3; k++) shade_out[k] = spec_out[k] = 0.0;
+  const int number = f.numberOfLights;
+  for (int i = 0; i < number; i++) {
+    const OLight &L = f.lights[(size_t)i];
+    if (!(i < s.auxLightNumber || L.enabled)) continue;
+    const Vec d = sub(L.pos, p);
+    const double distance = len(d);
+    const Vec lv = normalize(d);
+    const double intensity = s.auxLightIntensity * 100.0 * L.intensity / (distance * distance) / number;
+    double shade = dot(n, lv);
+    if (shade < 0) shade = 0;
+    shade = shade * intensity;
+    if (shade > 500.0) shade = 500.0;
+    const Vec half = normalize(sub(lv, view));
+    double shade2 = dot(n, half);
+    if (shade2 < 0.0) shade2 = 0.0;
+    shade2 = pow(shade2, 30.0) * 1.0;
+    shade2 *= intensity * s.specular;
+    if (shade2 > 15.0) shade2 = 15.0;
+    if ((shade > 0.01 || shade2 > 0.01) && s.shadow) {
+      const double light = aux_shadow(s, c, p, distance, lv, delta, thr, f.start);
+      shade *= light;
+      shade2 *= light;
+    } else if (s.shadow) {
+      shade = 0;
+      shade2 = 0;
+    }
+    for (int k = 0; k < 3; k++) {
+      shade_out[k] += shade * L.col[k] / 65536.0;
+      spec_out[k] += shade2 * L.col[k] / 65536.0;
+    }
+  }
+}
+
+void volumetric(const mbgb_scene &s, const Frame &f, Calc &c, const std::vector<Step> &buf, int count, double depth,
+                Vec view, double delta, double lastDist, double out[4], float *opacity) {
   float total = 0.0f;
   const double glow = count * s.glow_intensity / 512.0 * s.DE_factor;
   double glowN = 1.0 - glow;
@@ -1132,6 +1262,31 @@ void volumetric(const mbgb_scene &s, const Frame &f, const std::vector<Step> &bu
         }
       }
     }
+    if (s.fakeLightsEnabled) {  // src/shaders.cpp:298-307
+      double r = compute(c, buf[k].point, kOrbitTrap, 0, nullptr);
+      r = sqrt(1.0f / (r + 1.0e-30f));
+      const double fl = 1.0 / (pow(r, 10.0 / s.fakeLightsVisibilitySize) * pow(10.0, 10.0 / s.fakeLightsVisibilitySize) +
+                               1e-100);
+      for (int q = 0; q < 4; q++) out[q] += fl * step * s.fakeLightsVisibility;
+    }
+    for (int i = 0; i < 5; i++) {  // volumetric lights (src/shaders.cpp:309-343)
+      if (i == 0 && s.volumetricLightEnabled[0]) {
+        const double sh = main_shadow(s, c, buf[k].point, f.light, buf[k].thr, delta, f.start);
+        out[0] += sh * step * s.volumetricLightIntensity[0] * s.mainLightColour.R / 65536.0;
+        out[1] += sh * step * s.volumetricLightIntensity[0] * s.mainLightColour.G / 65536.0;
+        out[2] += sh * step * s.volumetricLightIntensity[0] * s.mainLightColour.B / 65536.0;
+        out[3] += (sh + sh + sh) / 3.0 * step * s.volumetricLightIntensity[0];
+      }
+      if (i > 0 && f.numberOfLights > 0 && f.lights[(size_t)i - 1].enabled && s.volumetricLightEnabled[i]) {
+        const OLight &L = f.lights[(size_t)i - 1];
+        const Vec d = sub(L.pos, buf[k].point);
+        const double dd = len(d);
+        const double d2 = dd * dd;
+        const double light = aux_shadow(s, c, buf[k].point, dd, normalize(d), delta, buf[k].thr, f.start);
+        for (int q = 0; q < 3; q++) out[q] += light * L.col[q] / 65536.0 * s.volumetricLightIntensity[i] * step / d2;
+        out[3] += light * s.volumetricLightIntensity[i] * step / d2;
+      }
+    }
     if (s.fogEnabled) {
       double fd = step / fogVis;
       if (fd > 1.0) fd = 1.0;
@@ -1162,6 +1317,51 @@ void volumetric(const mbgb_scene &s, const Frame &f, const std::vector<Step> &bu
       out[2] = fd * fb / 65536.0 + (1.0 - fd) * out[2];
       total = fd + (1.0 - fd) * total;
       out[3] = fd + (1.0 - fd) * out[3];
+    }
+    if (s.iterFogEnabled) {  // iteration fog (src/shaders.cpp:385-466)
+      const int L = buf[k].iters;
+      double op = iter_opacity(step, L, s.N, s.iterFogOpacityTrim, s.iterFogOpacity);
+      if (op > 0) {
+        const double itf = (double)2.0 * (L - s.iterFogOpacityTrim) / (s.N - s.iterFogOpacityTrim);
+        double kk = itf;
+        if (kk > 1.0) kk = 1.0;
+        if (kk < 0.0) kk = 0.0;
+        double kn = 1.0 - kk;
+        const mbgb_rgb fc1 = s.fogColour1, fc2 = s.fogColour2, fc3 = s.fogColour3;
+        double fcol[3] = {fc1.R * kn + fc2.R * kk, fc1.G * kn + fc2.G * kk, fc1.B * kn + fc2.B * kk};
+        double k2 = itf - 1.0;
+        if (k2 < 0.0) k2 = 0.0;
+        if (k2 > 1.0) k2 = 1.0;
+        kn = 1.0 - k2;
+        fcol[0] = fcol[0] * kn + fc3.R * k2;
+        fcol[1] = fcol[1] * kn + fc3.G * k2;
+        fcol[2] = fcol[2] * kn + fc3.B * k2;
+        double nc[3] = {0.0, 0.0, 0.0};
+        if (s.mainLightIntensity * s.directLight > 0.0) {
+          const double sh = main_shadow(s, c, buf[k].point, f.light, buf[k].thr, delta, f.start);
+          nc[0] += sh * s.mainLightColour.R / 65536.0 * s.mainLightIntensity * s.directLight;
+          nc[1] += sh * s.mainLightColour.G / 65536.0 * s.mainLightIntensity * s.directLight;
+          nc[2] += sh * s.mainLightColour.B / 65536.0 * s.mainLightIntensity * s.directLight;
+        }
+        for (int i = 1; i < 5; i++) {
+          if (!(f.numberOfLights > 0 && f.lights[(size_t)i - 1].enabled)) continue;
+          const OLight &Lt = f.lights[(size_t)i - 1];
+          const Vec dv = sub(Lt.pos, buf[k].point);
+          const double dd = len(dv);
+          const double d2 = dd * dd;
+          const double light = aux_shadow(s, c, buf[k].point, dd, normalize(dv), delta, buf[k].thr, f.start);
+          const double inten = Lt.intensity * 100.0;
+          for (int q = 0; q < 3; q++) nc[q] += light * Lt.col[q] / 65536.0 / d2 * inten;
+        }
+        if (s.global_ilumination && !s.fastGlobalIllumination) {
+          const double ao = ray_ao(s, c, buf[k].point, delta, buf[k].thr, lastDist, f.aoDirs, f.start);
+          for (int q = 0; q < 3; q++) nc[q] += ao * s.globalIlum;
+        }
+        if (op > 1.0) op = 1.0;
+        for (int q = 0; q < 3; q++) out[q] = out[q] * (1.0 - op) + nc[q] * op * fcol[q] / 65536.0;
+        total = op + (1.0 - op) * total;
+        out[3] = op + (1.0 - op) * out[3];
+      }
     }
     if (total > 1.0) total = 1.0;
     if (out[3] > 1.0) out[3] = 1.0;
@@ -1223,87 +1423,6 @@ void place_lights(const mbgb_scene &s, const Derived &d, std::vector<OLight> &L)
       L[i].enabled = true;
     } else {
       L[i].enabled = false;
-    }
-  }
-}
-
-double iter_opacity(double step, double iters, double maxN, double trim, double sp) {
-  double o = (iters - trim) / maxN;
-  if (o < 0.0) o = 0.0;
-  o *= o;
-  o *= step * sp;
-  if (o > 1.0) o = 1.0;
-  return o;
-}
-
-// the float threshold of the secondary rays (MainShadow / AuxShadow / AmbientOcclusion)
-float secondary_thresh(const mbgb_scene &s, Vec p2, Vec eye, double thr) {
-  if (s.iterFogEnabled || s.volumetricLightEnabledAny) {
-    if (!s.constantDEThreshold) return (float)(len(sub(p2, eye)) * s.resolution * s.persp / s.quality);
-    return (float)s.quality;
-  }
-  return (float)thr;
-}
-
-// AuxShadow (src/shaders.cpp:1069-1132)
-double aux_shadow(const mbgb_scene &s, Calc &c, Vec p, double distance, Vec lv, double delta, double thr, Vec eye) {
-  double dist = delta;
-  double shadowTemp = 1.0;
-  const double def = (s.iterFogEnabled || s.volumetricLightEnabledAny) ? 1.0 : s.DE_factor;
-  for (double i = delta; i < distance; i += dist * def) {
-    const Vec p2 = add(p, mul(lv, i));
-    bool mi = false;
-    dist = calculate_distance(c, p2, &mi);
-    const double opacity = s.iterFogEnabled
-                               ? iter_opacity(dist * def, c.itersOut, s.N, s.iterFogOpacityTrim, s.iterFogOpacity)
-                               : 0.0;
-    shadowTemp -= opacity * (distance - i) / distance;
-    if (dist < secondary_thresh(s, p2, eye, thr) || mi || shadowTemp < 0.0) {
-      if (s.penetratingLights) {
-        shadowTemp -= (distance - i) / distance;
-        if (shadowTemp < 0.0) shadowTemp = 0.0;
-      } else {
-        shadowTemp = 0.0;
-      }
-      break;
-    }
-  }
-  return shadowTemp;
-}
-
-// AuxLightsShader / LightShading (src/shaders.cpp:997-1067)
-void aux_lights(const mbgb_scene &s, const Frame &f, Calc &c, Vec p, Vec n, Vec view, double delta, double thr,
-                double shade_out[3], double spec_out[3]) {
-  for (int k = 0; k < 3; k++) shade_out[k] = spec_out[k] = 0.0;
-  const int number = f.numberOfLights;
-  for (int i = 0; i < number; i++) {
-    const OLight &L = f.lights[(size_t)i];
-    if (!(i < s.auxLightNumber || L.enabled)) continue;
-    const Vec d = sub(L.pos, p);
-    const double distance = len(d);
-    const Vec lv = normalize(d);
-    const double intensity = s.auxLightIntensity * 100.0 * L.intensity / (distance * distance) / number;
-    double shade = dot(n, lv);
-    if (shade < 0) shade = 0;
-    shade = shade * intensity;
-    if (shade > 500.0) shade = 500.0;
-    const Vec half = normalize(sub(lv, view));
-    double shade2 = dot(n, half);
-    if (shade2 < 0.0) shade2 = 0.0;
-    shade2 = pow(shade2, 30.0) * 1.0;
-    shade2 *= intensity * s.specular;
-    if (shade2 > 15.0) shade2 = 15.0;
-    if ((shade > 0.01 || shade2 > 0.01) && s.shadow) {
-      const double light = aux_shadow(s, c, p, distance, lv, delta, thr, f.start);
-      shade *= light;
-      shade2 *= light;
-    } else if (s.shadow) {
-      shade = 0;
-      shade2 = 0;
-    }
-    for (int k = 0; k < 3; k++) {
-      shade_out[k] += shade * L.col[k] / 65536.0;
-      spec_out[k] += shade2 * L.col[k] / 65536.0;
     }
   }
 }
@@ -1384,16 +1503,16 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
   double out[4] = {0, 0, 0, 0};
   Vec objColour{0, 0, 0};
   double depthZ = ray.depth;
+  const double thr = ray.thr;
+  c.detail = thr;
+  const double delta = s.constantDEThreshold ? ray.depth * s.resolution * s.persp : thr * s.quality;
   if (ray.found) {
-    const double thr = ray.thr;
-    c.detail = thr;
-    const double delta = s.constantDEThreshold ? ray.depth * s.resolution * s.persp : thr * s.quality;
     const Vec n = calculate_normals(s, c, ray.point, delta, thr);
     double shade = dot(n, f.light);
     if (shade < 0) shade = 0;
     const double shadeV = s.directLight * ((1.0 - s.shading) + s.shading * shade);
     double shadow = 1.0;
-    if (s.shadow) shadow = main_shadow(s, c, ray.point, f.light, thr, delta);
+    if (s.shadow) shadow = main_shadow(s, c, ray.point, f.light, thr, delta, f.start);
     Vec half = normalize(sub(f.light, view));
     double sp = dot(n, half);
     if (sp < 0.0) sp = 0.0;
@@ -1405,19 +1524,40 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     double amb = 0.0;
     if (s.global_ilumination) {
       if (s.fastGlobalIllumination) amb = fast_ao(s, c, ray.point, n, thr);
-      else amb = ray_ao(s, c, ray.point, delta, thr, ray.lastDist, f.aoDirs);
+      else amb = ray_ao(s, c, ray.point, delta, thr, ray.lastDist, f.aoDirs, f.start);
     }
     const double a2 = amb * s.globalIlum;
     const double ml[3] = {s.mainLightIntensity * s.mainLightColour.R / 65536.0,
                           s.mainLightIntensity * s.mainLightColour.G / 65536.0,
                           s.mainLightIntensity * s.mainLightColour.B / 65536.0};
     const double cc[3] = {col.x, col.y, col.z};
+    const double env = ((!s.raytracedReflections && s.reflect > 0) ? env_mapping(n, view) : 0.0) * s.reflect;
     double auxS[3] = {0, 0, 0}, auxSp[3] = {0, 0, 0};
     if (f.numberOfLights > 0) aux_lights(s, f, c, ray.point, n, view, delta, thr, auxS, auxSp);
+    // FakeLights (src/shaders.cpp:1225-1271)
+    double fake = 0.0, fakeSp = 0.0;
+    if (s.fakeLightsEnabled) {
+      const double dl = thr * s.smoothness;
+      const double rr = compute(c, ray.point, kOrbitTrap, 0, nullptr);
+      const double fl = s.fakeLightsIntensity / rr;
+      const double r = 1.0 / (rr + 1e-30);
+      const double rx = 1.0 / (compute(c, add(ray.point, Vec{dl, 0.0, 0.0}), kOrbitTrap, 0, nullptr) + 1e-30);
+      const double ry = 1.0 / (compute(c, add(ray.point, Vec{0.0, dl, 0.0}), kOrbitTrap, 0, nullptr) + 1e-30);
+      const double rz = 1.0 / (compute(c, add(ray.point, Vec{0.0, 0.0, dl}), kOrbitTrap, 0, nullptr) + 1e-30);
+      Vec fn{r - rx, r - ry, r - rz};
+      if (!(fn.x == 0 && fn.y == 0 && fn.z == 0)) fn = normalize(fn);
+      fake = fl * dot(n, fn);
+      if (fake < 0) fake = 0;
+      double fs = dot(n, normalize(sub(fn, view)));
+      if (fs < 0.0) fs = 0.0;
+      fs = pow(fs, 30.0) * fl;
+      if (fs > 15.0) fs = 15.0;
+      fakeSp = fs;
+    }
     for (int k = 0; k < 3; k++) {
-      double obj = 0.0 + (a2 + ml[k] * shadeV * shadow) * cc[k];
-      obj += (auxS[k] + 0.0) * cc[k];
-      const double spec = auxSp[k] + 0.0 + ml[k] * sp * shadow;
+      double obj = env * amb + (a2 + ml[k] * shadeV * shadow) * cc[k];
+      obj += (auxS[k] + fake) * cc[k];
+      const double spec = auxSp[k] + fakeSp + ml[k] * sp * shadow;
       out[k] = obj + 0.0 + spec;
     }
     out[3] = 1.0 + 0.0;
@@ -1430,7 +1570,7 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     depthZ = 1e20;
   }
   float opacity = 0.0f;
-  volumetric(s, f, buf, ray.count, ray.depth, view, out, &opacity);
+  volumetric(s, f, c, buf, ray.count, ray.depth, view, delta, ray.lastDist, out, &opacity);
   const int64_t pix = (int64_t)y * W + x;
   if (img->opacity) img->opacity[pix] = to_u16((double)opacity * 65535.0);
   if (img->alpha) img->alpha[pix] = to_u16(out[3] * 65535.0);

@@ -178,6 +178,8 @@ sParamRender *make_params(const mbgb_scene &s) {
   f.doubles.foldingLimit = s.foldingLimit; f.doubles.foldingValue = s.foldingValue;
   f.doubles.foldingSphericalMin = s.foldingSphericalMin; f.doubles.foldingSphericalFixed = s.foldingSphericalFixed;
   f.doubles.power = s.power; f.doubles.cadd = s.cadd; f.doubles.julia = v3(s.julia);
+  f.doubles.fakeLightsOrbitTrap = v3(s.fakeLightsOrbitTrap);
+  f.fakeLightsMinIter = s.fakeLightsMinIter; f.fakeLightsMaxIter = s.fakeLightsMaxIter;
   f.minN = s.minN; f.limits_enabled = s.limits_enabled; f.iterThresh = s.iterThresh; f.analitycDE = s.analitycDE;
   f.juliaMode = s.juliaMode; f.tgladFoldingMode = s.tgladFoldingMode; f.sphericalFoldingMode = s.sphericalFoldingMode;
   f.interiorMode = s.interiorMode; f.linearDEmode = s.linearDEmode; f.constantDEThreshold = s.constantDEThreshold;

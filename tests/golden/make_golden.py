@@ -134,6 +134,20 @@ EXAMPLES = {
     "aux_menger_1000_lights": ("menger sponge 3.fract", {}, 32, 24),
     "aux_rotated_mandelbox_4": ("rotated mandelbox 4.fract", {}),
     "aux_coloured_lights": ("tglad - scale 2 - coloured lights.fract", {}),
+    # slow shading (averaged normals), iteration fog, volumetric lights, environment mapping
+    "fx_slow_hypercomplex_ao": ("hypercomplex - ambient occlusion.fract", {}, 32, 24),
+    "fx_slow_interior_mandelbox": ("interior - mandelbox scale 2.fract", {}, 32, 24),
+    "fx_slow_interior_power8": ("interior - mandelbulb power 8.fract", {}, 32, 24),
+    "fx_iter_fog_1": ("iter fog 1.fract", {}, 32, 24),
+    "fx_iter_fog_2": ("iter fog 2.fract", {}, 32, 24),
+    "fx_iter_fog_3": ("iter fog 3.fract", {}, 32, 24),
+    "fx_iter_fog_4": ("iter fog 4.fract", {}, 32, 24),
+    "fx_volumetric_light_1": ("Volumetric light 1.fract", {}, 32, 24),
+    "fx_volumetric_light_2": ("Volumetric light 2.fract", {}, 32, 24),
+    "fx_volumetric_light_3": ("Volumetric light 3.fract", {}, 32, 24),
+    "fx_envmap_mandelbox": ("constant factor 2.0  - mandelbox scale 2.0.fract", {}),
+    "fx_envmap_hypercomplex_julia": ("hypercomplex - julia - environment mapping.fract", {"textured_background": 0}),
+    "fx_envmap_power2_julia": ("power 2 - julia.fract", {"textured_background": 0}),
 }
 
 # Formulas no example uses, on the benchmark workloads' settings.
@@ -175,6 +189,27 @@ EFFECT_CASES = {
                                     "aux_light_predefined_2_y": -5.0, "aux_light_predefined_2_z": -2.0,
                                     "aux_light_predefined_2_intensity": 2.0, "penetrating_lights": 1,
                                     "ambient_occlusion_enabled": 0, "volumetric_fog_density": 0}),
+    "fake_lights": ("mandelbulb_640x480", 40, 32,
+                    {"fake_lights_enabled": 1, "fake_lights_intensity": 1.0, "fake_lights_visibility": 5.0,
+                     "fake_lights_visibility_size": 5.0, "fake_lights_orbit_trap_X": 2.0,
+                     "fake_lights_orbit_trap_Y": 0.0, "fake_lights_orbit_trap_Z": 0.0,
+                     "fake_lights_min_iter": 1, "fake_lights_max_iter": 2}),
+    "fake_lights_mandelbox": ("mandelbox_1080p", 48, 32,
+                              {"fake_lights_enabled": 1, "fake_lights_intensity": 0.5, "fake_lights_visibility": 2.0,
+                               "fake_lights_visibility_size": 3.0, "fake_lights_orbit_trap_X": 1.0,
+                               "fake_lights_orbit_trap_Y": 1.0, "fake_lights_orbit_trap_Z": 0.0,
+                               "fake_lights_min_iter": 1, "fake_lights_max_iter": 3,
+                               "ambient_occlusion_enabled": 0}),
+    "envmap_mandelbulb": ("mandelbulb_640x480", 40, 32, {"reflect": 0.6, "ambient_occlusion_enabled": 1,
+                                                         "fast_ambient_occlusion_mode": 1}),
+    "slow_shading_mandelbox": ("mandelbox_1080p", 40, 32, {"slow_shading": 1, "ambient_occlusion_enabled": 0}),
+    "iter_fog_mandelbulb": ("mandelbulb_640x480", 40, 32,
+                            {"iteration_fog_enable": 1, "iteration_fog_opacity": 1000, "iteration_fog_opacity_trim": 4,
+                             "N": 20, "ambient_occlusion_enabled": 1, "fast_ambient_occlusion_mode": 0,
+                             "ambient_occlusion_quality": 1}),
+    "volumetric_main_light": ("mandelbox_1080p", 40, 32,
+                              {"volumetric_light_enabled_0": 1, "volumetric_light_intensity_0": 100,
+                               "ambient_occlusion_enabled": 0}),
     "aux_no_shadows": ("mandelbulb_640x480", 40, 32,
                        {**W.AUX_LIGHTS, "aux_light_number": 3, "aux_light_random_seed": 3, "aux_light_max_dist": 0.5,
                         "aux_light_distribution_radius": 2.0, "shadows_enabled": 0}),
@@ -305,7 +340,7 @@ def formula_de_all(lib, manifest: dict, npts: int = 400):
 def effect_goldens(manifest: dict):
     """The secondary effects' example scenes and synthetic scenes."""
     lib = build_ref()
-    render_example_cases(lib, manifest, only=[k for k in EXAMPLES if k.startswith("aux_")])
+    render_example_cases(lib, manifest, only=[k for k in EXAMPLES if k.startswith(("aux_", "fx_"))])
     render_cases(lib, EFFECT_CASES, manifest)
 
 

@@ -5,9 +5,13 @@ import numpy as np
 
 
 def psnr(a: np.ndarray, b: np.ndarray, peak: float = 1.0) -> float:
-    a = np.clip(a.astype(np.float64), 0, peak)
-    b = np.clip(b.astype(np.float64), 0, peak)
-    mse = float(np.mean((a - b) ** 2))
+    """PSNR of the clipped values. A NaN in both images (the reference's own 0/0 in a few
+    delta-DE orbits) counts as equal; a NaN in one of them as an error of `peak`."""
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    na, nb = np.isnan(a), np.isnan(b)
+    err = np.where(na & nb, 0.0, np.where(na | nb, peak, np.clip(a, 0, peak) - np.clip(b, 0, peak)))
+    mse = float(np.mean(err ** 2))
     return float("inf") if mse == 0 else 10.0 * np.log10(peak * peak / mse)
 
 

@@ -133,7 +133,10 @@ def test_render_fp64_against_reference_golden(gpu_ctx, case, engine):
     img = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=engine)
     ref = _golden_image(z, sc.image_width, sc.image_height)
     m = metrics.compare(img, ref)
-    if sc.formula == 8 and sc.perspectiveType == 0:
+    # the Mandelbox frames come out bit for bit, except where the environment map's texel
+    # (an 8-bit truncation of an atan2-derived coordinate) amplifies a libm last bit
+    env_mapped = sc.reflect > 0 and not sc.raytracedReflections
+    if sc.formula == 8 and sc.perspectiveType == 0 and not env_mapped:
         for k in ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]:
             np.testing.assert_array_equal(getattr(img, k), z[k], err_msg=f"{case}: {k}")
         np.testing.assert_allclose(img.image_float, z["image_float"], rtol=0, atol=1e-6)
@@ -219,6 +222,33 @@ def test_delta_de_scenes_render_in_fp64(gpu_ctx, oracle, case, w, h):
     print(case, m)
     assert m["hit_mismatch"] <= 0.005, m
     assert m["psnr_float"] >= 40.0, m
+
+
+EFFECT_SCENES = [("ex_aux_coloured_lights", 96, 64), ("ex_fx_iter_fog_2", 96, 64), ("ex_fx_volumetric_light_2", 96, 64),
+                 ("ex_fx_slow_interior_mandelbox", 64, 48), ("fake_lights_mandelbox", 96, 64),
+                 ("envmap_mandelbulb", 96, 72), ("aux_random_visible", 96, 72)]
+
+
+@pytest.mark.parametrize("case,w,h", EFFECT_SCENES)
+def test_effects_fp32_against_fp64(gpu_ctx, oracle, case, w, h):
+    """Secondary effects (aux / fake / volumetric lights, iteration fog, slow shading,
+    environment mapping) under the FP32 policy against the FP64 render, which the fixtures
+    pin to the reference, at sizes the fixtures do not cover: <= 0.5 % hit mismatch and
+    >= 99 % of the pixels within 0.01 in every channel (the rest are palette-index flips of
+    the FP32 colouring orbit, N x 10 iterations); and the FP64 render against the FP64
+    oracle (>= 60 dB)."""
+    sc = _fixture_scene(case, w, h)
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX)
+    b = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    m = metrics.compare(a, b)
+    close = float(np.mean(np.abs(a.image_float.astype(np.float64) - b.image_float).max(-1) <= 0.01))
+    print(case, "fp32 vs fp64", m, "within 0.01", close)
+    assert m["hit_mismatch"] <= 0.005, m
+    assert close >= 0.99, close
+    ref, _ = oracle_lib.render(oracle, sc)
+    m2 = metrics.compare(b, ref)
+    print(case, "fp64 vs oracle", m2)
+    assert m2["hit_mismatch"] <= 0.005 and m2["psnr_float"] >= 60.0, m2
 
 
 def test_fp32_fix_with_full_fp64_polish(gpu_ctx, oracle):
