@@ -200,6 +200,12 @@ static int gfb_normals(int type, double nv[20][3]) {
   return n;
 }
 
+// Scenes with primitive objects next to (or instead of) the fractal.
+static bool uses_primitives(const mbgb_scene &s) {
+  return s.planeEnable || s.boxEnable || s.invertedBoxEnable || s.sphereEnable || s.invertedSphereEnable ||
+         s.waterEnable || s.onlyPlane;
+}
+
 // Scenes that light with auxiliary lights: random ones or any of the four predefined.
 static bool uses_aux_lights(const mbgb_scene &s) {
   if (s.auxLightNumber > 0) return true;
@@ -224,13 +230,13 @@ static bool need_volumetric(const mbgb_scene &s) {
 // that use them render on the per-pixel engine.
 static bool per_pixel_only(const mbgb_scene &s) {
   return uses_aux_lights(s) || s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled ||
-         s.slowShading || (!s.raytracedReflections && s.reflect > 0);
+         s.slowShading || (!s.raytracedReflections && s.reflect > 0) || uses_primitives(s);
 }
 
-// The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights is carried
-// by the run-time formula path only.
+// The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights and the
+// primitive objects are carried by the run-time formula path only.
 static int scene_kernel_formula(const mbgb_scene &s) {
-  return kernel_formula(s.formula, s.ifsFoldingMode || s.fakeLightsEnabled);
+  return kernel_formula(s.formula, s.ifsFoldingMode || s.fakeLightsEnabled || uses_primitives(s));
 }
 
 template <typename T>
@@ -345,6 +351,37 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
     for (int c = 0; c < 3; c++) f.fakeTrap[c] = (T)s.fakeLightsOrbitTrap[c];
     f.fakeMinIter = s.fakeLightsMinIter;
     f.fakeMaxIter = s.fakeLightsMaxIter;
+  }
+  if (uses_primitives(s)) {
+    f.planeEnable = s.planeEnable;
+    f.boxEnable = s.boxEnable;
+    f.invertedBoxEnable = s.invertedBoxEnable;
+    f.sphereEnable = s.sphereEnable;
+    f.invertedSphereEnable = s.invertedSphereEnable;
+    f.waterEnable = s.waterEnable;
+    f.onlyPlane = s.onlyPlane;
+    f.waterIterations = s.waterIterations;
+    f.frameNo = s.frameNo;
+    // PrimitivePlane normalises the normal on every call (src/primitives.cpp:15-21)
+    const double *nv = s.planeNormal;
+    const double norm = 1.0 / sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+    for (int c = 0; c < 3; c++) {
+      f.planeCentre[c] = (T)s.planeCentre[c];
+      f.planeNormal[c] = (T)(nv[c] * norm);
+      f.boxCentre[c] = (T)s.boxCentre[c];
+      f.boxSize[c] = (T)s.boxSize[c];
+      f.invBoxCentre[c] = (T)s.invertedBoxCentre[c];
+      f.invBoxSize[c] = (T)s.invertedBoxSize[c];
+      f.sphereCentre[c] = (T)s.sphereCentre[c];
+      f.invSphereCentre[c] = (T)s.invertedSphereCentre[c];
+    }
+    f.sphereRadius = (T)s.sphereRadius;
+    f.invSphereRadius = (T)s.invertedSphereRadius;
+    f.waterHeight = (T)s.waterHeight;
+    f.waterAmplitude = (T)s.waterAmplitude;
+    f.waterLength = (T)s.waterLength;
+    f.waterRotation = (T)s.waterRotation;
+    f.waterAnimSpeed = (T)s.waterAnimSpeed;
   }
 }
 
@@ -466,6 +503,12 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   p.fakeLightsVisibilitySize = (T)s.fakeLightsVisibilitySize;
   p.envMapping = !s.raytracedReflections && s.reflect > 0;
   p.reflect = (T)s.reflect;
+  rgb(p.primColour[0], s.primitivePlaneColour);
+  rgb(p.primColour[1], s.primitiveWaterColour);
+  rgb(p.primColour[2], s.primitiveSphereColour);
+  rgb(p.primColour[3], s.primitiveInvertedSphereColour);
+  rgb(p.primColour[4], s.primitiveBoxColour);
+  rgb(p.primColour[5], s.primitiveInvertedBoxColour);
   // The volumetric pass changes the pixel only through glow, post fog, volumetric fog and
   // the visible auxiliary lights.
   p.needVolumetric = need_volumetric(s);
@@ -622,9 +665,6 @@ extern "C" mbgb_status mbgb_scene_supported(const mbgb_scene *s) {
         return set_error(MBGB_ERR_UNSUPPORTED, "hybrid sequence formula " + std::to_string(form[i]) +
                                                    " is not built on the device");
   }
-  if (s->planeEnable || s->boxEnable || s->invertedBoxEnable || s->sphereEnable || s->invertedSphereEnable ||
-      s->waterEnable || s->onlyPlane)
-    return set_error(MBGB_ERR_UNSUPPORTED, "primitive objects");
   if (s->raytracedReflections && s->reflectionsMax > 0)
     return set_error(MBGB_ERR_UNSUPPORTED, "ray-traced reflections");
   if (s->texturedBackground) return set_error(MBGB_ERR_UNSUPPORTED, "textured background");

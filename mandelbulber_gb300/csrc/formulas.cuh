@@ -724,9 +724,17 @@ __device__ __noinline__ T compute_runtime(const FractalT<T> *__restrict__ fp, V3
       if (MODE == kModeNormal) {
         if (r > T(1e2)) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
       } else if (MODE == kModeColour) {
-        distance = orbit_length(z);
-        if (distance < minv) minv = distance;
-        if (distance > T(1e15)) { distance = minv; break; }
+        if (f.onlyPlane) {
+          distance = orbit_length(z);
+          if (distance > T(1e15)) {
+            distance = (T(L) - m_log(m_log(r) / m_log(T(N))) / m_log(p)) / T(100);
+            break;
+          }
+        } else {
+          distance = orbit_length(z);
+          if (distance < minv) minv = distance;
+          if (distance > T(1e15)) { distance = minv; break; }
+        }
       }
     }
   }
@@ -754,12 +762,104 @@ __device__ __noinline__ T compute_runtime(const FractalT<T> *__restrict__ fp, V3
 // escape radius from forward differences with step 1e-10, the three perturbed orbits run
 // to the unperturbed orbit's iteration count. `*Lio` receives itersOut; *orbit and
 // *calls count the orbit iterations and Compute calls.
+// PrimitiveWater (src/primitives.cpp:95-136): a plane at z = height with `iterations`
+// octaves of sine / cosine waves within 10 x amplitude of it.
+template <typename T>
+__device__ __forceinline__ T primitive_water(const FractalT<T> &f, V3<T> point) {
+  const V3<T> plane{T(0), T(0), T(-1)};
+  const V3<T> centre{T(0), T(0), f.waterHeight};
+  T planeDistance = dot3(plane, point - centre);
+  if (planeDistance < f.waterAmplitude * T(10)) {
+    const T ang = f.waterRotation / T(180) * T(M_PI);
+    if (ang != T(0)) {
+      T sn, cs;
+      m_sincos(ang, &sn, &cs);
+      const T m[9] = {cs, -sn, T(0), sn, cs, T(0), T(0), T(0), T(1)};
+      point = rotate(m, 0, point);
+    }
+    const T phase = f.waterAnimSpeed * T(f.frameNo);
+    const T k = T(0.23);
+    T waveX = T(0), waveY = T(0);
+    T pw = T(1), p2 = T(0.05);
+    const T length = f.waterLength;
+    for (int i = 1; i <= f.waterIterations; i++) {
+      const float p3f = (float)(pw * p2);
+      const T p3 = (T)p3f;
+      const T shift = phase / (T(i) / T(3) + T(1));
+      const T wx = m_sin(T(i) + T(0.4) * (waveX)*p3 + m_sin(k * point.y / length * p3) + point.x / length * p3 + shift) / pw;
+      const T wy = m_cos(T(i) + T(0.4) * (waveY)*p3 + m_sin(point.x / length * p3) + k * point.y / length * p3 +
+                         shift * T(0.23)) / pw;
+      waveX += wx;
+      waveY += wy;
+      p2 = p2 + (T(1) - p2) * T(0.7);
+      pw *= T(1.872);
+    }
+    planeDistance += (waveX + waveY) * f.waterAmplitude;
+  }
+  return planeDistance;
+}
+
+// The primitive objects of CalculateDistance (src/fractal.cpp:1383-1434): each enabled one
+// replaces the distance (and the object) where it is closer.
+template <typename T>
+__device__ __forceinline__ T primitives(const FractalT<T> &f, const V3<T> point, T distance, int *objectOut) {
+  if (f.planeEnable) {
+    const V3<T> n{f.planeNormal[0], f.planeNormal[1], f.planeNormal[2]};
+    const T d = dot3(n, point - V3<T>{f.planeCentre[0], f.planeCentre[1], f.planeCentre[2]});
+    if (!f.onlyPlane && d < distance) *objectOut = kObjPlane;
+    distance = (d < distance) ? d : distance;
+  }
+  if (f.boxEnable || f.invertedBoxEnable) {
+    for (int inv = 0; inv < 2; inv++) {
+      if (!(inv ? f.invertedBoxEnable : f.boxEnable)) continue;
+      const T *c = inv ? f.invBoxCentre : f.boxCentre;
+      const T *sz = inv ? f.invBoxSize : f.boxSize;
+      const V3<T> c1{c[0] - T(0.5) * sz[0], c[1] - T(0.5) * sz[1], c[2] - T(0.5) * sz[2]};
+      const V3<T> c2{c[0] + T(0.5) * sz[0], c[1] + T(0.5) * sz[1], c[2] + T(0.5) * sz[2]};
+      // PrimitiveBox / PrimitiveInvertedBox: the planes through the corners, outward for the
+      // box (max), inward for the inverted box (min); the unit normals are exact
+      const T sgn = inv ? T(1) : T(-1);
+      T d = dot3(V3<T>{sgn, T(0), T(0)}, point - c1);
+      T q = dot3(V3<T>{-sgn, T(0), T(0)}, point - c2);
+      d = inv ? ((q < d) ? q : d) : ((q > d) ? q : d);
+      q = dot3(V3<T>{T(0), sgn, T(0)}, point - c1);
+      d = inv ? ((q < d) ? q : d) : ((q > d) ? q : d);
+      q = dot3(V3<T>{T(0), -sgn, T(0)}, point - c2);
+      d = inv ? ((q < d) ? q : d) : ((q > d) ? q : d);
+      q = dot3(V3<T>{T(0), T(0), sgn}, point - c1);
+      d = inv ? ((q < d) ? q : d) : ((q > d) ? q : d);
+      q = dot3(V3<T>{T(0), T(0), -sgn}, point - c2);
+      d = inv ? ((q < d) ? q : d) : ((q > d) ? q : d);
+      if (d < distance) *objectOut = inv ? kObjBoxInv : kObjBox;
+      distance = (d < distance) ? d : distance;
+    }
+  }
+  if (f.sphereEnable) {
+    const T d = length3(point - V3<T>{f.sphereCentre[0], f.sphereCentre[1], f.sphereCentre[2]}) - f.sphereRadius;
+    if (d < distance) *objectOut = kObjSphere;
+    distance = (d < distance) ? d : distance;
+  }
+  if (f.invertedSphereEnable) {
+    const T d =
+        f.invSphereRadius - length3(point - V3<T>{f.invSphereCentre[0], f.invSphereCentre[1], f.invSphereCentre[2]});
+    if (d < distance) *objectOut = kObjSphereInv;
+    distance = (d < distance) ? d : distance;
+  }
+  if (f.waterEnable) {
+    const T d = primitive_water(f, point);
+    if (d < distance) *objectOut = kObjWater;
+    distance = (d < distance) ? d : distance;
+  }
+  return distance;
+}
+
 template <typename T>
 __device__ __noinline__ T calc_distance_runtime(const FractalT<T> *__restrict__ fp, V3<T> point, const T detailSize,
                                                const int N, const int minN, const bool normalMode, int *Lio,
                                                bool *maxIter, unsigned long long *orbit, unsigned long long *calls,
-                                               const T fparam) {
+                                               int *objectOut, const T fparam) {
   const FractalT<T> &f = *fp;
+  *objectOut = kObjFractal;
   T limitBoxDist = T(0);
   if (f.limits) {
     const T ax = point.x - f.amax, bx = -(point.x - f.amin);
@@ -776,7 +876,10 @@ __device__ __noinline__ T calc_distance_runtime(const FractalT<T> *__restrict__ 
   }
   T distance;
   bool mi;
-  if (f.analytic) {
+  if (f.onlyPlane) {
+    distance = T(10);
+    mi = false;
+  } else if (f.analytic) {
     int L;
     distance = compute_runtime<T, kModeNormal>(fp, point, N, 0, &L, fparam);
     *orbit += (unsigned long long)(L + 1);
@@ -839,6 +942,7 @@ __device__ __noinline__ T calc_distance_runtime(const FractalT<T> *__restrict__ 
       if (distance < detailSize) distance = detailSize * T(1.01);
     }
   }
+  distance = primitives(f, point, distance, objectOut);
   if (f.limits) {
     if (limitBoxDist < detailSize) distance = (distance > limitBoxDist) ? distance : limitBoxDist;
   }

@@ -77,7 +77,17 @@ struct FractalT {
   // Compute<orbitTrap> of the fake lights
   T fakeTrap[3];
   int fakeMinIter, fakeMaxIter;
+  // primitive objects of CalculateDistance (sFractalPrimitives, src/fractal.h:195-222;
+  // src/primitives.cpp); the plane normal is stored normalised, as PrimitivePlane uses it
+  int planeEnable, boxEnable, invertedBoxEnable, sphereEnable, invertedSphereEnable, waterEnable, onlyPlane;
+  int waterIterations, frameNo;
+  T planeCentre[3], planeNormal[3], boxCentre[3], boxSize[3], invBoxCentre[3], invBoxSize[3];
+  T sphereCentre[3], sphereRadius, invSphereCentre[3], invSphereRadius;
+  T waterHeight, waterAmplitude, waterLength, waterRotation, waterAnimSpeed;
 };
+
+// enumObjectType (src/fractal.h:82-91): the object a CalculateDistance call ended on.
+enum { kObjFractal = 0, kObjPlane = 1, kObjWater = 2, kObjSphere = 3, kObjSphereInv = 4, kObjBox = 5, kObjBoxInv = 6 };
 
 // One auxiliary light (sLight, src/shaders.h:25-31): placed at random around a centre
 // (PlaceRandomLights, src/shaders.cpp:1134-1208) or one of the four predefined lights.
@@ -148,6 +158,8 @@ struct ParamsT {
   // environment mapping on the default white texture (EnvMapping, src/shaders.cpp:785-811)
   int envMapping;
   T reflect;
+  // primitive colours, 16-bit range: [plane, water, sphere, inverted sphere, box, inverted box]
+  int primColour[6][3];
 };
 
 // Per-frame camera, resolution, fractal parameter and output layers of a batch (device

@@ -182,7 +182,9 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   ov.step_thr = d->ovsteps + 2 * (size_t)kStepSlots * kOverflowThreads;
 
   const bool needVol = (scene->glow_intensity != 0.0) || scene->fogEnabled || (scene->fogDensity > 0.0);
-  const int kf = mbgb::kernel_formula(scene->formula, scene->ifsFoldingMode);
+  const bool primitives = scene->planeEnable || scene->boxEnable || scene->invertedBoxEnable || scene->sphereEnable ||
+                          scene->invertedSphereEnable || scene->waterEnable || scene->onlyPlane;
+  const int kf = mbgb::kernel_formula(scene->formula, scene->ifsFoldingMode || primitives);
   e = mbgb::launch_render_f32(kf, p, fd, io, grid, kNaThreads, s);
   if (e == cudaSuccess && needVol) e = mbgb::launch_render_f32(kf, p, fd, ov, 1, kOverflowThreads, s);
   if (e != cudaSuccess) return mbgb::set_error(MBGB_ERR_CUDA, std::string("render launch: ") + cudaGetErrorString(e));

@@ -113,6 +113,7 @@ struct Counters {
   unsigned long long calls;   // Loop_counter
   unsigned long long steps;   // DE_counter (primary march + refinement)
   unsigned long long missed;  // Missed_DE_counter
+  int objectOut;              // calcParam->objectOut: the object the last distance ended on
 };
 
 // Formulas whose main parameter is the Mandelbox scale (tglad 8, smoothMandelbox 17,
@@ -233,7 +234,7 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
                                            Counters &cnt, const T fparam) {
   if (FORMULA == 0)
     return calc_distance_runtime<T>(&f, point, detailSize, N, minN, normalMode, &L, &maxIter, &cnt.orbit, &cnt.calls,
-                                    fparam);
+                                    &cnt.objectOut, fparam);
   T limitBoxDist = T(0);
   if (f.limits) {
     // MAX(a, b) = a > b ? a : b (gtk MAX macro)
@@ -739,7 +740,11 @@ __device__ __forceinline__ void index_to_colour(const ParamsT<T> &p, int index, 
 // SurfaceColour for the fractal object (src/shaders.cpp:850-879)
 template <typename T, int FORMULA>
 __device__ __forceinline__ V3<T> surface_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt,
-                                                const T fparam) {
+                                                const T fparam, const int objectType = kObjFractal) {
+  if (objectType != kObjFractal) {  // primitive colours (src/shaders.cpp:880-922)
+    const int *c = p.primColour[objectType - 1];
+    return V3<T>{T(c[0]) / T(65536), T(c[1]) / T(65536), T(c[2]) / T(65536)};
+  }
   int L;
   const T c = compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt, fparam);
   int nrCol = to_i32_x86((double)m_floor(c));
@@ -1053,6 +1058,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
     }
     if (rs.found) refine<T, FORMULA>(p, fd, startD, view, rs, cnt);
   }
+  const int objectType = cnt.objectOut;   // shaderInputData.objectType (src/Render3D.cpp:536)
 
   T result[4] = {T(0), T(0), T(0), T(0)};
   V3<T> objColour{T(0), T(0), T(0)};
@@ -1081,7 +1087,7 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
     shade2 = m_pow(shade2, T(30)) * T(1);
     if (shade2 > T(15)) shade2 = T(15);
     const T spec = shade2 * p.specular;
-    const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt, fparam_of(p.f));
+    const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt, fparam_of(p.f), objectType);
     objColour = colour;
     V3<T> ambient{T(0), T(0), T(0)};
     if (p.ao) {

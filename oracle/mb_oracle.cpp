@@ -175,6 +175,7 @@ struct Calc {
   int itersOut;
   Cnt *cnt;
   const Derived *d;
+  int objectOut = 0;  // enumObjectType of the last CalculateDistance
 };
 
 enum { kNormal = 0, kColour = 1, kDelta1 = 3, kDelta2 = 4, kOrbitTrap = 5 };
@@ -707,9 +708,14 @@ double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
     } else if (mode == kNormal) {
       if (r > 1e2) { distance = 0.5 * r * log(r) / r_dz; break; }
     } else if (mode == kColour) {
-      distance = len(z);
-      if (distance < minv) minv = distance;
-      if (distance > 1e15) { distance = minv; break; }
+      if (s.onlyPlane) {
+        distance = len(z);
+        if (distance > 1e15) { distance = (L - log(log(r) / log((double)N)) / log(p)) / 100.0; break; }
+      } else {
+        distance = len(z);
+        if (distance < minv) minv = distance;
+        if (distance > 1e15) { distance = minv; break; }
+      }
     }
   }
   c.cnt->orbit += (uint64_t)(L + 1);
@@ -732,8 +738,76 @@ double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
   return distance * 5000.0;
 }
 
+// PrimitiveWater (src/primitives.cpp:95-136)
+double primitive_water(const mbgb_scene &s, Vec p) {
+  double pd = dot(Vec{0, 0, -1}, sub(p, Vec{0, 0, s.waterHeight}));
+  if (pd < s.waterAmplitude * 10.0) {
+    const double a = s.waterRotation / 180 * M_PI;
+    if (a != 0.0) {
+      const double sn = sin(a), cs = cos(a);
+      const double m[9] = {cs, -sn, 0, sn, cs, 0, 0, 0, 1};
+      p = rot(m, 0, p);
+    }
+    const double phase = s.waterAnimSpeed * s.frameNo, k = 0.23, len_ = s.waterLength;
+    double wx = 0, wy = 0, pw = 1.0, p2 = 0.05;
+    for (int i = 1; i <= s.waterIterations; i++) {
+      const float p3 = pw * p2;
+      const double shift = phase / (i / 3.0 + 1.0);
+      const double tx = sin(i + 0.4 * (wx)*p3 + sin(k * p.y / len_ * p3) + p.x / len_ * p3 + shift) / pw;
+      const double ty = cos(i + 0.4 * (wy)*p3 + sin(p.x / len_ * p3) + k * p.y / len_ * p3 + shift * 0.23) / pw;
+      wx += tx;
+      wy += ty;
+      p2 = p2 + (1.0 - p2) * 0.7;
+      pw *= 1.872;
+    }
+    pd += (wx + wy) * s.waterAmplitude;
+  }
+  return pd;
+}
+
+// PrimitivePlane (src/primitives.cpp:15-21)
+double primitive_plane(Vec p, Vec centre, Vec normal) { return dot(normalize(normal), sub(p, centre)); }
+
+// the primitive objects of CalculateDistance (src/fractal.cpp:1383-1434)
+double primitives(Calc &c, Vec p, double d) {
+  const mbgb_scene &s = *c.s;
+  auto take = [&](double q, int obj) {
+    if (q < d) c.objectOut = obj;
+    d = (q < d) ? q : d;
+  };
+  if (s.planeEnable) {
+    const double q = primitive_plane(p, Vec{s.planeCentre[0], s.planeCentre[1], s.planeCentre[2]},
+                                     Vec{s.planeNormal[0], s.planeNormal[1], s.planeNormal[2]});
+    if (!s.onlyPlane && q < d) c.objectOut = 1;
+    d = (q < d) ? q : d;
+  }
+  for (int inv = 0; inv < 2; inv++) {
+    if (!(inv ? s.invertedBoxEnable : s.boxEnable)) continue;
+    const double *ce = inv ? s.invertedBoxCentre : s.boxCentre;
+    const double *sz = inv ? s.invertedBoxSize : s.boxSize;
+    const Vec c1{ce[0] - 0.5 * sz[0], ce[1] - 0.5 * sz[1], ce[2] - 0.5 * sz[2]};
+    const Vec c2{ce[0] + 0.5 * sz[0], ce[1] + 0.5 * sz[1], ce[2] + 0.5 * sz[2]};
+    const double sg = inv ? 1.0 : -1.0;
+    const Vec nrm[6] = {{sg, 0, 0}, {-sg, 0, 0}, {0, sg, 0}, {0, -sg, 0}, {0, 0, sg}, {0, 0, -sg}};
+    double q = primitive_plane(p, c1, nrm[0]);
+    for (int k = 1; k < 6; k++) {
+      const double r = primitive_plane(p, (k & 1) ? c2 : c1, nrm[k]);
+      q = inv ? ((r < q) ? r : q) : ((r > q) ? r : q);
+    }
+    take(q, inv ? 6 : 5);
+  }
+  if (s.sphereEnable) take(len(sub(p, Vec{s.sphereCentre[0], s.sphereCentre[1], s.sphereCentre[2]})) - s.sphereRadius, 3);
+  if (s.invertedSphereEnable)
+    take(s.invertedSphereRadius -
+             len(sub(p, Vec{s.invertedSphereCentre[0], s.invertedSphereCentre[1], s.invertedSphereCentre[2]})),
+         4);
+  if (s.waterEnable) take(primitive_water(s, p), 2);
+  return d;
+}
+
 double calculate_distance(Calc &c, Vec p, bool *max_iter) {
   const mbgb_scene &s = *c.s;
+  c.objectOut = 0;
   double limit = 0.0;
   if (s.limits_enabled) {
     auto mx = [](double a, double b) { return a > b ? a : b; };
@@ -746,52 +820,58 @@ double calculate_distance(Calc &c, Vec p, bool *max_iter) {
       return limit;
     }
   }
-  int L;
+  int L = c.itersOut;
   double d;
-  int retval;
-  if (s.analitycDE) {
-    d = compute(c, p, kNormal, 0, &L);
-    retval = L;
-    if (max_iter) *max_iter = (L == c.N);
-    c.itersOut = L;
-    if (d < 0) d = 0;
+  int retval = 0;
+  if (s.onlyPlane) {
+    d = 10.0;
+    if (max_iter) *max_iter = false;
   } else {
-    // delta-DE: forward differences of the escape radius (src/fractal.cpp:1308-1381)
-    const double h = 1e-10;
-    const double r = compute(c, p, kDelta1, 0, &L);
-    retval = L;
-    c.itersOut = L;
-    p.x += h; p.y += 0; p.z += 0;
-    const double d1 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
-    p.x -= h; p.y += h; p.z += 0;
-    const double d2 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
-    p.x += 0; p.y -= h; p.z += h;
-    const double d3 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
-    const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
-    d = s.linearDEmode ? 0.5 * r / dr : 0.5 * r * log(r) / dr;
-    if (d < 0) d = 0;
-    if (retval == c.N) {
-      if (max_iter) *max_iter = true;
-      d = 0;
-    } else if (max_iter) {
-      *max_iter = false;
+    if (s.analitycDE) {
+      d = compute(c, p, kNormal, 0, &L);
+      retval = L;
+      if (max_iter) *max_iter = (L == c.N);
+      c.itersOut = L;
+      if (d < 0) d = 0;
+    } else {
+      // delta-DE: forward differences of the escape radius (src/fractal.cpp:1308-1381)
+      const double h = 1e-10;
+      const double r = compute(c, p, kDelta1, 0, &L);
+      retval = L;
+      c.itersOut = L;
+      p.x += h; p.y += 0; p.z += 0;
+      const double d1 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
+      p.x -= h; p.y += h; p.z += 0;
+      const double d2 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
+      p.x += 0; p.y -= h; p.z += h;
+      const double d3 = fabs(compute(c, p, kDelta2, L, &L) - r) / h;
+      const double dr = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+      d = s.linearDEmode ? 0.5 * r / dr : 0.5 * r * log(r) / dr;
+      if (d < 0) d = 0;
+      if (retval == c.N) {
+        if (max_iter) *max_iter = true;
+        d = 0;
+      } else if (max_iter) {
+        *max_iter = false;
+      }
+    }
+    if (L < c.minN && d < c.detail) d = c.detail;
+    if (s.interiorMode && !c.normalMode) {
+      if (d < 0.5 * c.detail || L == c.N) {
+        d = c.detail;
+        if (max_iter) *max_iter = false;
+      }
+    } else if (s.interiorMode && c.normalMode) {
+      if (d < 0.9 * c.detail) {
+        d = c.detail - d;
+        if (max_iter) *max_iter = false;
+      }
+    }
+    if (s.iterThresh && retval < c.N) {
+      if (d < c.detail) d = c.detail * 1.01;
     }
   }
-  if (L < c.minN && d < c.detail) d = c.detail;
-  if (s.interiorMode && !c.normalMode) {
-    if (d < 0.5 * c.detail || L == c.N) {
-      d = c.detail;
-      if (max_iter) *max_iter = false;
-    }
-  } else if (s.interiorMode && c.normalMode) {
-    if (d < 0.9 * c.detail) {
-      d = c.detail - d;
-      if (max_iter) *max_iter = false;
-    }
-  }
-  if (s.iterThresh && retval < c.N) {
-    if (d < c.detail) d = c.detail * 1.01;
-  }
+  d = primitives(c, p, d);
   if (s.limits_enabled && limit < c.detail) d = d > limit ? d : limit;
   return d;
 }
@@ -1096,7 +1176,11 @@ void index_to_colour(const mbgb_scene &s, int index, int out[3]) {
   }
 }
 
-Vec surface_colour(const mbgb_scene &s, Calc &c, Vec p) {
+Vec surface_colour(const mbgb_scene &s, Calc &c, Vec p, int objectType) {
+  const mbgb_rgb *prim[7] = {nullptr, &s.primitivePlaneColour, &s.primitiveWaterColour, &s.primitiveSphereColour,
+                             &s.primitiveInvertedSphereColour, &s.primitiveBoxColour, &s.primitiveInvertedBoxColour};
+  if (objectType != 0) return Vec{prim[objectType]->R / 65536.0, prim[objectType]->G / 65536.0,
+                                  prim[objectType]->B / 65536.0};
   const int N0 = c.N;
   c.N = (int)(s.N * 10);
   int nr = to_i32(floor(compute(c, p, kColour, 0, nullptr)));
@@ -1499,6 +1583,7 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
   if (!cut) ray = ray_marching(s, c, f.start, view, buf, jitter, cnt);
   bool levelMissed = false;
   if (f.exact && ray.found) levelMissed = !level_set(s, c, f.start, view, ray);
+  const int objectType = c.objectOut;
   const int iters = c.itersOut;
   double out[4] = {0, 0, 0, 0};
   Vec objColour{0, 0, 0};
@@ -1519,7 +1604,7 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     sp = pow(sp, 30.0) * 1.0;
     if (sp > 15.0) sp = 15.0;
     sp *= s.specular;
-    const Vec col = surface_colour(s, c, ray.point);
+    const Vec col = surface_colour(s, c, ray.point, objectType);
     objColour = col;
     double amb = 0.0;
     if (s.global_ilumination) {

@@ -235,7 +235,19 @@ sParamRender *make_params(const mbgb_scene &s) {
       f.mandelbox.rot[fold][axis].SetRotation(m.rotation[fold][axis]);
       f.mandelbox.rotinv[fold][axis] = f.mandelbox.rot[fold][axis].Transpose();
     }
-  f.primitives.onlyPlane = false;
+  // primitive objects (sFractalPrimitives, src/fractal.h:195-222)
+  f.primitives.planeEnable = s.planeEnable; f.primitives.boxEnable = s.boxEnable;
+  f.primitives.invertedBoxEnable = s.invertedBoxEnable; f.primitives.sphereEnable = s.sphereEnable;
+  f.primitives.invertedSphereEnable = s.invertedSphereEnable; f.primitives.waterEnable = s.waterEnable;
+  f.primitives.onlyPlane = s.onlyPlane; f.primitives.waterIterations = s.waterIterations;
+  sFractalPrimitivesD &pd = f.doubles.primitives;
+  pd.planeCentre = v3(s.planeCentre); pd.planeNormal = v3(s.planeNormal);
+  pd.boxCentre = v3(s.boxCentre); pd.boxSize = v3(s.boxSize);
+  pd.invertedBoxCentre = v3(s.invertedBoxCentre); pd.invertedBoxSize = v3(s.invertedBoxSize);
+  pd.sphereCentre = v3(s.sphereCentre); pd.sphereRadius = s.sphereRadius;
+  pd.invertedSphereCentre = v3(s.invertedSphereCentre); pd.invertedSphereRadius = s.invertedSphereRadius;
+  pd.waterHeight = s.waterHeight; pd.waterAmplitude = s.waterAmplitude; pd.waterLength = s.waterLength;
+  pd.waterRotation = s.waterRotation; pd.waterAnimSpeed = s.waterAnimSpeed;
 
   p.image_width = s.image_width; p.image_height = s.image_height; p.globalIlumQuality = s.globalIlumQuality;
   p.reflectionsMax = s.reflectionsMax; p.coloring_seed = s.coloring_seed; p.auxLightRandomSeed = s.auxLightRandomSeed;
@@ -250,6 +262,11 @@ sParamRender *make_params(const mbgb_scene &s) {
   p.imageSwitches.raytracedReflections = s.raytracedReflections;
   p.imageSwitches.volumetricLightEnabled = s.volumetricLightEnabledAny;
   p.imageSwitches.iterFogEnabled = s.iterFogEnabled; p.imageSwitches.hdrEnabled = s.hdrEnabled;
+  p.primitivePlaneColour = rgb(s.primitivePlaneColour); p.primitiveBoxColour = rgb(s.primitiveBoxColour);
+  p.primitiveInvertedBoxColour = rgb(s.primitiveInvertedBoxColour);
+  p.primitiveSphereColour = rgb(s.primitiveSphereColour);
+  p.primitiveInvertedSphereColour = rgb(s.primitiveInvertedSphereColour);
+  p.primitiveWaterColour = rgb(s.primitiveWaterColour);
   p.background_color1 = rgb(s.background_color1); p.background_color2 = rgb(s.background_color2);
   p.background_color3 = rgb(s.background_color3);
   p.fogColour1 = rgb(s.fogColour1); p.fogColour2 = rgb(s.fogColour2); p.fogColour3 = rgb(s.fogColour3);

@@ -148,6 +148,10 @@ EXAMPLES = {
     "fx_envmap_mandelbox": ("constant factor 2.0  - mandelbox scale 2.0.fract", {}),
     "fx_envmap_hypercomplex_julia": ("hypercomplex - julia - environment mapping.fract", {"textured_background": 0}),
     "fx_envmap_power2_julia": ("power 2 - julia.fract", {"textured_background": 0}),
+    # primitive objects
+    "fx_primitives_inverted_box": ("primitive objects - inverted box.fract", {"raytraced_reflections": 0}),
+    "fx_primitives_set": ("primitive objects - set.fract", {"raytraced_reflections": 0}),
+    "fx_primitives_water": ("primitive objects - water.fract", {"raytraced_reflections": 0}),
 }
 
 # Formulas no example uses, on the benchmark workloads' settings.
@@ -210,6 +214,25 @@ EFFECT_CASES = {
     "volumetric_main_light": ("mandelbox_1080p", 40, 32,
                               {"volumetric_light_enabled_0": 1, "volumetric_light_intensity_0": 100,
                                "ambient_occlusion_enabled": 0}),
+    "primitives_plane_sphere_box": ("mandelbulb_640x480", 48, 32,
+                                    {"primitive_plane_enabled": 1, "primitive_plane_centre_Z": -0.9,
+                                     "primitive_plane_normal_Z": 1.0, "primitive_plane_normal_X": 0.2,
+                                     "primitive_sphere_enabled": 1, "primitive_sphere_centre_X": 0.9,
+                                     "primitive_sphere_centre_Y": -0.6, "primitive_sphere_radius": 0.35,
+                                     "primitive_box_enabled": 1, "primitive_box_centre_X": -0.9,
+                                     "primitive_box_size_X": 0.4, "primitive_box_size_Y": 0.4,
+                                     "primitive_box_size_Z": 0.8,
+                                     "primitive_plane_colour_R": 40000, "primitive_plane_colour_G": 50000,
+                                     "primitive_plane_colour_B": 60000, "primitive_sphere_colour_R": 65000,
+                                     "primitive_box_colour_G": 65000}),
+    "primitives_water_only_plane": ("mandelbulb_640x480", 48, 32,
+                                    {"primitive_only_plane": 1, "primitive_plane_enabled": 1,
+                                     "primitive_plane_centre_Z": -0.5, "primitive_plane_normal_Z": 1.0,
+                                     "primitive_water_enabled": 1, "primitive_water_level": -0.3,
+                                     "primitive_water_amplitude": 0.02, "primitive_water_length": 0.1,
+                                     "primitive_water_rotation": 30, "primitive_water_iterations": 5,
+                                     "primitive_water_anim_speed": 0.1, "frame_no": 7,
+                                     "primitive_water_colour_B": 60000}),
     "aux_no_shadows": ("mandelbulb_640x480", 40, 32,
                        {**W.AUX_LIGHTS, "aux_light_number": 3, "aux_light_random_seed": 3, "aux_light_max_dist": 0.5,
                         "aux_light_distribution_radius": 2.0, "shadows_enabled": 0}),

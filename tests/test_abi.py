@@ -31,7 +31,7 @@ def test_null_arguments_are_rejected(mblib):
 
 def test_unsupported_features_are_reported(mblib):
     from mandelbulber_gb300 import workloads as W
-    for key, value, text in [("formula", 38, "formula"), ("primitive_plane_enabled", 1, "primitive"),
+    for key, value, text in [("formula", 38, "formula"),
                              ("textured_background", 1, "textured background"),
                              ("raytraced_reflections", 1, "reflections")]:
         sc = W.workload("mandelbulb_640x480", **{key: value})
