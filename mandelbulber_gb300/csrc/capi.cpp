@@ -200,6 +200,12 @@ static int gfb_normals(int type, double nv[20][3]) {
   return n;
 }
 
+// Rays of the reflection loop per pixel: the camera ray plus reflectionsMax reflections when
+// ray-traced reflections are on (src/Render3D.cpp:260-261).
+static int reflection_rays(const mbgb_scene &s) {
+  return 1 + ((s.raytracedReflections && s.reflectionsMax > 0) ? s.reflectionsMax : 0);
+}
+
 // Scenes with primitive objects next to (or instead of) the fractal.
 static bool uses_primitives(const mbgb_scene &s) {
   return s.planeEnable || s.boxEnable || s.invertedBoxEnable || s.sphereEnable || s.invertedSphereEnable ||
@@ -230,7 +236,7 @@ static bool need_volumetric(const mbgb_scene &s) {
 // that use them render on the per-pixel engine.
 static bool per_pixel_only(const mbgb_scene &s) {
   return uses_aux_lights(s) || s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled ||
-         s.slowShading || (!s.raytracedReflections && s.reflect > 0) || uses_primitives(s);
+         s.slowShading || (!s.raytracedReflections && s.reflect > 0) || uses_primitives(s) || reflection_rays(s) > 1;
 }
 
 // The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights and the
@@ -509,6 +515,10 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   rgb(p.primColour[3], s.primitiveInvertedSphereColour);
   rgb(p.primColour[4], s.primitiveBoxColour);
   rgb(p.primColour[5], s.primitiveInvertedBoxColour);
+  p.maxRay = reflection_rays(s) - 1;
+  const double pr[6] = {s.primitivePlaneReflect, s.primitiveWaterReflect, s.primitiveSphereReflect,
+                        s.primitiveInvertedSphereReflect, s.primitiveBoxReflect, s.primitiveInvertedBoxReflect};
+  for (int i = 0; i < 6; i++) p.primReflect[i] = (T)pr[i];
   // The volumetric pass changes the pixel only through glow, post fog, volumetric fog and
   // the visible auxiliary lights.
   p.needVolumetric = need_volumetric(s);
@@ -665,8 +675,8 @@ extern "C" mbgb_status mbgb_scene_supported(const mbgb_scene *s) {
         return set_error(MBGB_ERR_UNSUPPORTED, "hybrid sequence formula " + std::to_string(form[i]) +
                                                    " is not built on the device");
   }
-  if (s->raytracedReflections && s->reflectionsMax > 0)
-    return set_error(MBGB_ERR_UNSUPPORTED, "ray-traced reflections");
+  if (s->raytracedReflections && s->reflectionsMax > 10)
+    return set_error(MBGB_ERR_UNSUPPORTED, "ray-traced reflections: more than 10 reflections");
   if (s->texturedBackground) return set_error(MBGB_ERR_UNSUPPORTED, "textured background");
   if (s->image_width <= 0 || s->image_height <= 0 || s->image_width > 65536 || s->image_height > 65536)
     return set_error(MBGB_ERR_BAD_PARAM, "image size out of range");
@@ -1105,15 +1115,23 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
 
 // Enqueue the per-pixel engine (render_core.cuh) for one frame: main pass, then (when
 // the step buffer is in use) the overflow pass.
+// CTAs per SM of the per-pixel engine: the occupancy limit (or the tuned value); one when the
+// scene keeps step records for several rays of the reflection loop, which bounds their memory
+// (thread slots x rays x kStepCap records).
+static int per_pixel_ctas(const mbgb_scene &scene, int prec, const LaunchCfg &cfg) {
+  int per_sm = std::max(1, occupancy_render(prec, scene_kernel_formula(scene), cfg.block));
+  if (cfg.ctasPerSm > 0) per_sm = std::min(per_sm, cfg.ctasPerSm);
+  if (reflection_rays(scene) > 1 && need_volumetric(scene)) per_sm = 1;
+  return per_sm;
+}
+
 static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, const mbgb_image &img,
                                      const Group &g, const mbgb_opts &o, cudaStream_t s, FrameIO io, char *fctl,
                                      uint64_t *launches, int64_t lightOff) {
   const int prec = g.prec;
   const int block = g.cfg.block;
   const int kf = scene_kernel_formula(scene);
-  int per_sm = std::max(1, occupancy_render(prec, kf, block));
-  if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
-  const int grid = c->sms * per_sm;
+  const int grid = c->sms * per_pixel_ctas(scene, prec, g.cfg);
   io.image_float = img.image_float;
   io.zbuffer = img.zbuffer;
   io.alpha = img.alpha;
@@ -1129,6 +1147,7 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   io.overflow_count = (unsigned int *)(fctl + 4);
   const bool needVol = need_volumetric(scene);
   const bool points = need_step_points(scene);
+  io.rays = reflection_rays(scene);
   if (needVol) {
     io.step_step = c->step[prec][0].ptr;
     io.step_dist = c->step[prec][1].ptr;
@@ -1147,6 +1166,7 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   ov.step_thr = c->ovstep[prec][2].ptr;
   ov.step_scan = points ? c->ovstep[prec][3].ptr : nullptr;
   ov.step_iters = points ? (int *)c->ovstep[prec][4].ptr : nullptr;
+  ov.rays = io.rays;
   const int ovBlocks = std::max(1, kOverflowThreads / block);
   FractalT<double> fd;
   fill_fractal<double>(scene, fd);
@@ -1501,6 +1521,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
   size_t wave_bytes[2] = {0, 0};
   bool volPrec[2] = {false, false};
   bool pointsPrec[2] = {false, false};
+  int maxRays[2] = {1, 1};
   int64_t maxPixPerPixel = 0;
   int64_t maxSlots[2] = {0, 0};
   size_t camsBytes = 0;
@@ -1509,6 +1530,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     const bool needVol = need_volumetric(rep);
     if (needVol) volPrec[g.prec] = true;
     if (!g.wave && need_step_points(rep)) pointsPrec[g.prec] = true;
+    if (!g.wave) maxRays[g.prec] = std::max(maxRays[g.prec], reflection_rays(rep));
     if (g.wave) {
       const bool rayAO = rep.global_ilumination && !rep.fastGlobalIllumination;
       const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
@@ -1523,9 +1545,8 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       }
     } else if (needVol) {
       maxPixPerPixel = std::max(maxPixPerPixel, g.npix);
-      int per_sm = std::max(1, occupancy_render(g.prec, scene_kernel_formula(rep), g.cfg.block));
-      if (g.cfg.ctasPerSm > 0) per_sm = std::min(per_sm, g.cfg.ctasPerSm);
-      maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_sm * g.cfg.block);
+      maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_pixel_ctas(rep, g.prec, g.cfg) *
+                                                        g.cfg.block * reflection_rays(rep));
     }
   }
   for (int p = 0; p < 2; p++) {
@@ -1535,7 +1556,8 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     auto bytes_of = [&](int k) { return k == 4 ? sizeof(int) : esz; };
     if (volPrec[p])
       for (int k = 0; k < arrays; k++)
-        MBGB_CUDA(c->ensure(c->ovstep[p][k], (size_t)kStepSlots * (size_t)kOverflowThreads * bytes_of(k)));
+        MBGB_CUDA(c->ensure(c->ovstep[p][k],
+                            (size_t)kStepSlots * (size_t)kOverflowThreads * (size_t)maxRays[p] * bytes_of(k)));
     if (maxSlots[p])
       for (int k = 0; k < arrays; k++)
         MBGB_CUDA(c->ensure(c->step[p][k], (size_t)kStepCap * (size_t)maxSlots[p] * bytes_of(k)));

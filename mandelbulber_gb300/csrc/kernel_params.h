@@ -160,6 +160,10 @@ struct ParamsT {
   T reflect;
   // primitive colours, 16-bit range: [plane, water, sphere, inverted sphere, box, inverted box]
   int primColour[6][3];
+  // ray-traced reflections (src/Render3D.cpp:441-564): reflections after the camera ray, and
+  // the primitives' reflection coefficients in primColour's order (the fractal's is reflect)
+  int maxRay;
+  T primReflect[6];
 };
 
 // Per-frame camera, resolution, fractal parameter and output layers of a batch (device
@@ -212,6 +216,7 @@ struct FrameIO {
   void *step_scan;
   int *step_iters;
   int64_t slots;
+  int rays;        // record sets per slot: 1, or the rays of the reflection loop
   int step_cap;
   int overflow_pass;
   unsigned int *overflow_count;   // zeroed before the main pass

@@ -114,6 +114,9 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   if (auxLights)
     return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
                            "auxiliary lights are placed per call, which the allocation-free entry point does not do");
+  if (scene->raytracedReflections && scene->reflectionsMax > 0)
+    return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
+                           "ray-traced reflections keep per-ray records the allocation-free entry point does not have");
   if (scene->iterFogEnabled || scene->volumetricLightEnabledAny || scene->fakeLightsEnabled)
     return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
                            "iteration fog, volumetric and fake lights need step positions the allocation-free "

@@ -285,8 +285,26 @@ struct StepBuf {
   T *step, *dist, *thr;
   T *scan;     // null unless the volumetric pass samples the record positions
   int *iters;
-  int64_t slots, slot;
+  int64_t slots, slot;   // record stride (thread slots x rays) and this thread's slot
+  int64_t raySlots;      // thread slots: ray k of the reflection loop uses slot + k x raySlots
   __device__ __forceinline__ int64_t at(int i) const { return (int64_t)i * slots + slot; }
+  __device__ __forceinline__ StepBuf ray(int k) const {
+    StepBuf r = *this;
+    r.slot = slot + (int64_t)k * raySlots;
+    return r;
+  }
+};
+
+// The rays of the reflection loop (sReflect, src/Render3D.h:41-56): the camera ray and up
+// to kMaxRays - 1 reflections.
+constexpr int kMaxRays = 11;
+template <typename T>
+struct RayRec {
+  V3<double> start, view, point;
+  bool found;
+  int buffCount, objectType;
+  double lastDist, depth, distThresh;
+  T reflect;
 };
 
 // Per-pixel march state handed from the march to the shaders.
@@ -309,10 +327,13 @@ constexpr int kMaxSecondarySteps = 1 << 20;
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA>
 __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, const V3<T> dir, const uint32_t pixel,
-                                      const StepBuf<T> &sb, const int stepCap, RayState &rs, Counters &cnt) {
+                                      const StepBuf<T> &sb, const int stepCap, RayState &rs, Counters &cnt,
+                                      const T distThreshIn = T(0)) {
   T scan = p.viewDistanceMin;
-  T distThresh = T(0);  // *distThreshOut is 0.0 for the primary ray (src/Render3D.cpp:443)
-  const T distThreshInit = T(0);
+  // *distThreshOut: 0.0 for the primary ray, the previous ray's threshold for a reflected
+  // one (src/Render3D.cpp:88, 443, 461-462)
+  T distThresh = distThreshIn;
+  const T distThreshInit = distThreshIn;
   T dist = T(0);
   T step = p.viewDistanceMin;
   int buffCount = 0;
@@ -380,14 +401,14 @@ __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, co
 // detailSize keeps the value of the last march step, as in the reference.
 template <typename TP, int FORMULA>
 __device__ __forceinline__ void refine(const ParamsT<TP> &p, const FractalT<double> &fd, const V3<double> start,
-                                       const V3<double> dir, RayState &rs, Counters &cnt) {
+                                       const V3<double> dir, RayState &rs, Counters &cnt,
+                                       const double distThreshInit = 0.0) {
   const double search_accuracy = 0.01 * p.quality_d;
   const double search_limit = 1.0 - search_accuracy;
   double scan = rs.scan;
   double step = rs.step * 0.5;
   double dist = rs.dist;
   double distThresh = rs.distThresh;
-  const double distThreshInit = 0.0;
   V3<double> point{rs.point[0], rs.point[1], rs.point[2]};
   int iters = rs.iters;
   for (int i = 0; i < 20; i++) {
@@ -790,7 +811,8 @@ __device__ __forceinline__ V3<T> background(const ParamsT<T> &p, const V3<T> vie
 // the shared CalculateDistance state through them.
 template <typename T, int FORMULA>
 __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
-                                           const T depth, const V3<T> eye, const V3<T> view, const T delta,
+                                           const T depth, const V3<T> rayStart, const V3<T> eye, const V3<T> view,
+                                           const T delta,
                                            const T lastDist, T &detail, int &itersOut, const FrameIO &io,
                                            Counters &cnt, T out[4], float &totalOpacityOut, bool &opacitySet) {
   float totalOpacity = 0.0f;
@@ -822,7 +844,7 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
     // visible auxiliary lights (src/shaders.cpp:242-296): a bell-shaped glow around each
     // light, sampled in up to 50 sub-steps near the closest one
     if (p.auxLightVisibility > T(0) && p.numberOfLights > 0) {
-      const V3<T> point = eye + view * sb.scan[sb.at(index)];
+      const V3<T> point = rayStart + view * sb.scan[sb.at(index)];
       T lowestLightSize = T(1e10);
       T lowestLightDist = T(1e10);
       for (int i = 0; i < p.numberOfLights; ++i) {
@@ -865,7 +887,7 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
     }
     // fake lights (orbit trap, src/shaders.cpp:298-307)
     if (p.fakeLights) {
-      const V3<T> point = eye + view * sb.scan[sb.at(index)];
+      const V3<T> point = rayStart + view * sb.scan[sb.at(index)];
       int L;
       Counters c2{0, 0, 0, 0};
       T r = compute<T, FORMULA, 5>(p.f, point, p.f.N, L, c2, fparam_of(p.f));
@@ -881,7 +903,7 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
     }
     // volumetric lights with shadows in fog (src/shaders.cpp:309-343)
     if (p.volLightAny) {
-      const V3<T> point = eye + view * sb.scan[sb.at(index)];
+      const V3<T> point = rayStart + view * sb.scan[sb.at(index)];
       const T thrStep = sb.thr[sb.at(index)];
       for (int i = 0; i < 5; i++) {
         if (i == 0 && p.volLightEnabled[0]) {
@@ -945,7 +967,7 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
       const T N = T(p.f.N);
       T opacity = iter_opacity(step, T(L), N, p.iterFogOpacityTrim, p.iterFogOpacity);
       if (opacity > T(0)) {
-        const V3<T> point = eye + view * sb.scan[sb.at(index)];
+        const V3<T> point = rayStart + view * sb.scan[sb.at(index)];
         const T thrStep = sb.thr[sb.at(index)];
         const T iterFactor = T(2) * (T(L) - p.iterFogOpacityTrim) / (N - p.iterFogOpacityTrim);
         T k = iterFactor;
@@ -999,8 +1021,87 @@ __device__ __forceinline__ void volumetric(const ParamsT<T> &p, const StepBuf<T>
   }
 }
 
+// ObjectShader (src/shaders.cpp:21-112) at a hit: normal, main light with shadow and
+// specular, surface colour, AO, environment map, aux and fake lights. Writes the object and
+// specular terms and the surface colour.
+template <typename T, int FORMULA>
+__device__ __forceinline__ void object_shader(const ParamsT<T> &p, const V3<T> point, const V3<T> viewT,
+                                              const V3<double> viewD, const V3<T> eye, const T dist_thresh,
+                                              const T delta, const T lastDist, const int objectType, T &detail,
+                                              int &itersOut, const FrameIO &io, Counters &cnt, T obj[3], T specOut[3],
+                                              V3<T> &objColour) {
+  const V3<T> n = calc_normal<T, FORMULA>(p, point, delta, dist_thresh, detail, cnt);
+  const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
+  T shade = dot3(n, lv);
+  if (shade < T(0)) shade = T(0);
+  const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
+  T shadow = T(1);
+  if (p.shadow) shadow = main_shadow<T, FORMULA>(p, point, dist_thresh, delta, eye, detail, itersOut, io, cnt);
+  // MainSpecular (src/shaders.cpp:770-783)
+  V3<T> half = normalize3(lv - viewT);
+  T shade2 = dot3(n, half);
+  if (shade2 < T(0)) shade2 = T(0);
+  shade2 = m_pow(shade2, T(30)) * T(1);
+  if (shade2 > T(15)) shade2 = T(15);
+  const T spec = shade2 * p.specular;
+  const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt, fparam_of(p.f), objectType);
+  objColour = colour;
+  V3<T> ambient{T(0), T(0), T(0)};
+  if (p.ao) {
+    if (p.fastAO) {
+      const T a = fast_ao<T, FORMULA>(p, point, n, dist_thresh, detail, cnt);
+      ambient = {a, a, a};
+    } else {
+      ambient = ray_ao<T, FORMULA>(p, point, delta, dist_thresh, lastDist, detail, eye, itersOut, cnt);
+    }
+  }
+  const V3<T> ambient2{ambient.x * p.globalIlum, ambient.y * p.globalIlum, ambient.z * p.globalIlum};
+  // environment mapping
+  const T env = (p.envMapping ? (T)env_mapping(V3<double>{(double)n.x, (double)n.y, (double)n.z}, viewD) : T(0)) *
+                p.reflect;
+  // auxiliary lights
+  T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
+  if (p.numberOfLights > 0)
+    aux_lights<T, FORMULA>(p, point, n, viewT, delta, dist_thresh, eye, detail, itersOut, cnt, aux, auxSpec);
+  // fake (orbit trap) lights (FakeLights, src/shaders.cpp:1225-1271)
+  T fake = T(0), fakeSpec = T(0);
+  if (p.fakeLights) {
+    const T dl = dist_thresh * p.smoothness;
+    int L;
+    const T rr = compute<T, FORMULA, 5>(p.f, point, p.f.N, L, cnt, fparam_of(p.f));
+    const T fakeLight = p.fakeLightsIntensity / rr;
+    const T r = T(1) / (rr + T(1e-30));
+    const T rx = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + dl, point.y + T(0), point.z + T(0)}, p.f.N, L,
+                                                 cnt, fparam_of(p.f)) + T(1e-30));
+    const T ry = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + dl, point.z + T(0)}, p.f.N, L,
+                                                 cnt, fparam_of(p.f)) + T(1e-30));
+    const T rz = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dl}, p.f.N, L,
+                                                 cnt, fparam_of(p.f)) + T(1e-30));
+    V3<T> fln{r - rx, r - ry, r - rz};
+    if (!(fln.x == T(0) && fln.y == T(0) && fln.z == T(0))) fln = normalize3(fln);
+    T fakeLight2 = fakeLight * dot3(n, fln);
+    if (fakeLight2 < T(0)) fakeLight2 = T(0);
+    fake = fakeLight2;
+    const V3<T> fh = normalize3(fln - viewT);
+    T fs = dot3(n, fh);
+    if (fs < T(0)) fs = T(0);
+    fs = m_pow(fs, T(30)) * fakeLight;
+    if (fs > T(15)) fs = T(15);
+    fakeSpec = fs;
+  }
+  const T amb[3] = {ambient.x, ambient.y, ambient.z};
+  const T amb2[3] = {ambient2.x, ambient2.y, ambient2.z};
+  const T col[3] = {colour.x, colour.y, colour.z};
+  for (int c = 0; c < 3; c++) {
+    T o = env * amb[c] + (amb2[c] + p.mainLight[c] * shadeV * shadow) * col[c];
+    o += (aux[c] + fake) * col[c];
+    obj[c] = o;
+    specOut[c] = auxSpec[c] + fakeSpec + p.mainLight[c] * spec * shadow;
+  }
+}
+
 // ---------------------------------------------------------------------------
-// One pixel: MainThread pixel body (src/Render3D.cpp:389-589), reflections off.
+// One pixel: MainThread pixel body (src/Render3D.cpp:389-589) with its reflection loop.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA>
 __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT<double> &fd, const FrameIO &io,
@@ -1040,126 +1141,128 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
   const V3<T> viewT{(T)view.x, (T)view.y, (T)view.z};
   const V3<T> startT{(T)startD.x, (T)startD.y, (T)startD.z};
 
-  RayState rs;
-  rs.found = false;
-  rs.overflow = false;
-  rs.buffCount = 0;
-  rs.iters = 0;
-  rs.distThresh = 0.0;
-  rs.dist = 0.0;
-  rs.scan = 0.0;
-  rs.point[0] = rs.point[1] = rs.point[2] = 0.0;
-  if (!hemisphereCut) {
-    march<T, FORMULA>(p, startT, viewT, (uint32_t)pix, sb, stepCap, rs, cnt);
-    if (rs.overflow) {
-      const unsigned int k = atomicAdd(io.overflow_count, 1u);
-      io.overflow_list[k] = (unsigned int)pix;
-      return;
+  // the reflection loop (src/Render3D.cpp:441-564): ray 0 is the camera ray; each hit on a
+  // reflecting object spawns the mirrored ray from just above the hit
+  const int maxRay = p.maxRay;
+  RayRec<T> rec[kMaxRays];
+  V3<double> startRay = startD;
+  V3<double> viewRay = view;
+  double distThreshCarry = 0.0;
+  int rayEnd = 0;
+  int iters0 = 0;
+  int itersState = 0;   // calcParam->itersOut
+  V3<double> point{0.0, 0.0, 0.0};
+  for (int ray = 0; ray <= maxRay; ray++) {
+    RayRec<T> &rb = rec[ray];
+    rb.start = startRay;
+    rb.view = viewRay;
+    RayState rs;
+    rs.found = false;
+    rs.overflow = false;
+    rs.buffCount = 0;
+    rs.iters = itersState;
+    rs.distThresh = distThreshCarry;
+    rs.dist = 0.0;
+    rs.scan = 0.0;
+    rs.point[0] = point.x;
+    rs.point[1] = point.y;
+    rs.point[2] = point.z;
+    if (!hemisphereCut) {
+      const StepBuf<T> sbr = sb.ray(ray);
+      march<T, FORMULA>(p, V3<T>{(T)startRay.x, (T)startRay.y, (T)startRay.z},
+                        V3<T>{(T)viewRay.x, (T)viewRay.y, (T)viewRay.z}, (uint32_t)pix, sbr, stepCap, rs, cnt,
+                        (T)distThreshCarry);
+      if (rs.overflow) {
+        const unsigned int k = atomicAdd(io.overflow_count, 1u);
+        io.overflow_list[k] = (unsigned int)pix;
+        return;
+      }
+      if (rs.found) refine<T, FORMULA>(p, fd, startRay, viewRay, rs, cnt, distThreshCarry);
     }
-    if (rs.found) refine<T, FORMULA>(p, fd, startD, view, rs, cnt);
+    itersState = rs.iters;
+    if (ray == 0) iters0 = rs.iters;
+    point = V3<double>{rs.point[0], rs.point[1], rs.point[2]};
+    distThreshCarry = rs.distThresh;
+    rb.found = rs.found;
+    rb.buffCount = rs.buffCount;
+    rb.point = point;
+    rb.distThresh = rs.distThresh;
+    rb.lastDist = rs.dist;
+    rb.depth = rs.scan;
+    rb.objectType = cnt.objectOut;   // shaderInputData.objectType (src/Render3D.cpp:470)
+    rb.reflect = rb.objectType == kObjFractal ? p.reflect : p.primReflect[rb.objectType - 1];
+    rayEnd = ray;
+    if (!rb.found) break;
+    if (rb.reflect == T(0)) break;
+    // mirrored direction about the hit's normal, started one threshold above the hit
+    T detail = (T)rb.distThresh;
+    const T thr = (T)rb.distThresh;
+    T delta;
+    if (p.constantDEThreshold) delta = (T)rb.depth * p.resolution * p.persp;
+    else delta = thr * p.quality;
+    const V3<T> vn = calc_normal<T, FORMULA>(p, V3<T>{(T)point.x, (T)point.y, (T)point.z}, delta, thr, detail, cnt);
+    const V3<double> vnd{(double)vn.x, (double)vn.y, (double)vn.z};
+    viewRay = viewRay - vnd * dot3(viewRay, vnd) * 2.0;
+    startRay = point + viewRay * rb.distThresh;
   }
-  const int objectType = cnt.objectOut;   // shaderInputData.objectType (src/Render3D.cpp:536)
 
   T result[4] = {T(0), T(0), T(0), T(0)};
   V3<T> objColour{T(0), T(0), T(0)};
-  double depth = rs.scan;
-  const T dist_thresh = (T)rs.distThresh;
-  T detail = (T)rs.distThresh;
-  int itersOut = rs.iters;   // the shared calcParam->itersOut
-  // shaderInputData.delta (src/Render3D.cpp:530-531), for hits and background alike
-  T delta;
-  if (p.constantDEThreshold) delta = (T)rs.scan * p.resolution * p.persp;
-  else delta = dist_thresh * p.quality;
-  if (rs.found) {
-    // ObjectShader (src/shaders.cpp:21-112)
-    const V3<T> point{(T)rs.point[0], (T)rs.point[1], (T)rs.point[2]};
-    const V3<T> n = calc_normal<T, FORMULA>(p, point, delta, dist_thresh, detail, cnt);
-    const V3<T> lv{p.lightVect[0], p.lightVect[1], p.lightVect[2]};
-    T shade = dot3(n, lv);
-    if (shade < T(0)) shade = T(0);
-    const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
-    T shadow = T(1);
-    if (p.shadow) shadow = main_shadow<T, FORMULA>(p, point, dist_thresh, delta, startT, detail, itersOut, io, cnt);
-    // MainSpecular (src/shaders.cpp:770-783)
-    V3<T> half = normalize3(lv - viewT);
-    T shade2 = dot3(n, half);
-    if (shade2 < T(0)) shade2 = T(0);
-    shade2 = m_pow(shade2, T(30)) * T(1);
-    if (shade2 > T(15)) shade2 = T(15);
-    const T spec = shade2 * p.specular;
-    const V3<T> colour = surface_colour<T, FORMULA>(p, point, cnt, fparam_of(p.f), objectType);
-    objColour = colour;
-    V3<T> ambient{T(0), T(0), T(0)};
-    if (p.ao) {
-      if (p.fastAO) {
-        const T a = fast_ao<T, FORMULA>(p, point, n, dist_thresh, detail, cnt);
-        ambient = {a, a, a};
-      } else {
-        ambient = ray_ao<T, FORMULA>(p, point, delta, dist_thresh, (T)rs.dist, detail, startT, itersOut, cnt);
-      }
+  float totalOpacity0 = 0.0f;
+  T alpha0 = T(0);
+  for (int ray = rayEnd; ray >= 0; ray--) {
+    RayRec<T> &rb = rec[ray];
+    const V3<T> viewT{(T)rb.view.x, (T)rb.view.y, (T)rb.view.z};
+    const T dist_thresh = (T)rb.distThresh;
+    T detail = (T)rb.distThresh;
+    int itersOut = itersState;   // the shared calcParam->itersOut
+    // shaderInputData.delta (src/Render3D.cpp:517-518), for hits and background alike
+    T delta;
+    if (p.constantDEThreshold) delta = (T)rb.depth * p.resolution * p.persp;
+    else delta = dist_thresh * p.quality;
+    T obj[3] = {T(0), T(0), T(0)}, spec[3] = {T(0), T(0), T(0)}, bg[3] = {T(0), T(0), T(0)};
+    T alpha = T(0);
+    if (rb.found) {
+      object_shader<T, FORMULA>(p, V3<T>{(T)rb.point.x, (T)rb.point.y, (T)rb.point.z}, viewT, rb.view, startT,
+                                dist_thresh, delta, (T)rb.lastDist, rb.objectType, detail, itersOut, io, cnt, obj, spec,
+                                objColour);
+      alpha = T(1) + T(0);
+    } else {
+      const V3<T> b = background(p, viewT);
+      bg[0] = b.x;
+      bg[1] = b.y;
+      bg[2] = b.z;
     }
-    const V3<T> ambient2{ambient.x * p.globalIlum, ambient.y * p.globalIlum, ambient.z * p.globalIlum};
-    // environment mapping
-    const T env = (p.envMapping ? (T)env_mapping(V3<double>{(double)n.x, (double)n.y, (double)n.z}, view) : T(0)) *
-                  p.reflect;
-    // auxiliary lights
-    T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
-    if (p.numberOfLights > 0)
-      aux_lights<T, FORMULA>(p, point, n, viewT, delta, dist_thresh, startT, detail, itersOut, cnt, aux, auxSpec);
-    // fake (orbit trap) lights (FakeLights, src/shaders.cpp:1225-1271)
-    T fake = T(0), fakeSpec = T(0);
-    if (p.fakeLights) {
-      const T dl = dist_thresh * p.smoothness;
-      int L;
-      const T rr = compute<T, FORMULA, 5>(p.f, point, p.f.N, L, cnt, fparam_of(p.f));
-      const T fakeLight = p.fakeLightsIntensity / rr;
-      const T r = T(1) / (rr + T(1e-30));
-      const T rx = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + dl, point.y + T(0), point.z + T(0)}, p.f.N, L,
-                                                   cnt, fparam_of(p.f)) + T(1e-30));
-      const T ry = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + dl, point.z + T(0)}, p.f.N, L,
-                                                   cnt, fparam_of(p.f)) + T(1e-30));
-      const T rz = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dl}, p.f.N, L,
-                                                   cnt, fparam_of(p.f)) + T(1e-30));
-      V3<T> fln{r - rx, r - ry, r - rz};
-      if (!(fln.x == T(0) && fln.y == T(0) && fln.z == T(0))) fln = normalize3(fln);
-      T fakeLight2 = fakeLight * dot3(n, fln);
-      if (fakeLight2 < T(0)) fakeLight2 = T(0);
-      fake = fakeLight2;
-      const V3<T> fh = normalize3(fln - viewT);
-      T fs = dot3(n, fh);
-      if (fs < T(0)) fs = T(0);
-      fs = m_pow(fs, T(30)) * fakeLight;
-      if (fs > T(15)) fs = T(15);
-      fakeSpec = fs;
+    const T reflect = rb.reflect;
+    T pixel[4];
+    for (int c = 0; c < 3; c++) {
+      if (maxRay > 0 && rayEnd > 0 && ray != rayEnd)
+        pixel[c] = result[c] * reflect + (T(1) - reflect) * (obj[c] + bg[c]) + spec[c];
+      else
+        pixel[c] = obj[c] + bg[c] + spec[c];
     }
-    T objR = env * ambient.x + (ambient2.x + p.mainLight[0] * shadeV * shadow) * colour.x;
-    T objG = env * ambient.y + (ambient2.y + p.mainLight[1] * shadeV * shadow) * colour.y;
-    T objB = env * ambient.z + (ambient2.z + p.mainLight[2] * shadeV * shadow) * colour.z;
-    objR += (aux[0] + fake) * colour.x;
-    objG += (aux[1] + fake) * colour.y;
-    objB += (aux[2] + fake) * colour.z;
-    const T specR = auxSpec[0] + fakeSpec + p.mainLight[0] * spec * shadow;
-    const T specG = auxSpec[1] + fakeSpec + p.mainLight[1] * spec * shadow;
-    const T specB = auxSpec[2] + fakeSpec + p.mainLight[2] * spec * shadow;
-    result[0] = objR + T(0) + specR;
-    result[1] = objG + T(0) + specG;
-    result[2] = objB + T(0) + specB;
-    result[3] = T(1) + T(0);
-  } else {
-    const V3<T> bg = background(p, viewT);
-    result[0] = T(0) + bg.x + T(0);
-    result[1] = T(0) + bg.y + T(0);
-    result[2] = T(0) + bg.z + T(0);
-    result[3] = T(0);
-    depth = 1e20;
+    pixel[3] = rb.found ? alpha + T(0) : T(0) + T(0);
+    float totalOpacity = 0.0f;
+    bool opacitySet = false;
+    // the volumetric pass sees the march depth even for background pixels: the shader
+    // input is filled before the depth becomes 1e20 (src/Render3D.cpp:518-541)
+    if (p.needVolumetric)
+      volumetric<T, FORMULA>(p, sb.ray(ray), rb.buffCount, (T)rb.depth,
+                             V3<T>{(T)rb.start.x, (T)rb.start.y, (T)rb.start.z}, startT, viewT, delta,
+                             (T)rb.lastDist, detail, itersOut, io, cnt, pixel, totalOpacity, opacitySet);
+    itersState = itersOut;
+    result[0] = pixel[0];
+    result[1] = pixel[1];
+    result[2] = pixel[2];
+    if (ray == 0) {
+      totalOpacity0 = totalOpacity;
+      alpha0 = pixel[3];
+    }
   }
-  float totalOpacity = 0.0f;
-  bool opacitySet = false;
-  // the volumetric pass sees the march depth even for background pixels: the
-  // shader input is filled before the depth becomes 1e20 (src/Render3D.cpp:518-541)
-  if (p.needVolumetric)
-    volumetric<T, FORMULA>(p, sb, rs.buffCount, (T)rs.scan, startT, viewT, delta, (T)rs.dist, detail, itersOut, io, cnt,
-                           result, totalOpacity, opacitySet);
+  const double depth = rec[0].found ? rec[0].depth : 1e20;
+  const float totalOpacity = totalOpacity0;
+  result[3] = alpha0;
+  const bool found0 = rec[0].found;
 
   // buffer writes (src/Render3D.cpp:569-589)
   if (io.opacity) io.opacity[pix] = to_u16_x86((double)totalOpacity * 65535.0);
@@ -1175,8 +1278,8 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
     io.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
   }
   if (io.zbuffer) io.zbuffer[pix] = (float)depth;
-  if (io.hit) io.hit[pix] = rs.found ? 1 : 0;
-  if (io.iters) io.iters[pix] = rs.iters;
+  if (io.hit) io.hit[pix] = found0 ? 1 : 0;
+  if (io.iters) io.iters[pix] = iters0;
   if (io.depth) io.depth[pix] = depth;
 }
 
@@ -1189,8 +1292,8 @@ template <typename T, int FORMULA>
 __global__ void __launch_bounds__(128) render_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd, const FrameIO io) {
   const int lane = threadIdx.x & 31;
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, (T *)io.step_scan, io.step_iters, io.slots,
-                slot};
+  StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, (T *)io.step_scan, io.step_iters,
+                io.slots * (io.rays > 0 ? io.rays : 1), slot, io.slots};
   Counters cnt{0, 0, 0, 0};
   const int tilesX = (p.width + kTileW - 1) / kTileW;
   const int rowTiles = (p.row_end - p.row_begin + kTileH - 1) / kTileH;

@@ -908,13 +908,15 @@ struct Ray {
   Vec point;
 };
 
-Ray ray_marching(const mbgb_scene &s, Calc &c, Vec start, Vec dir, std::vector<Step> &buf, bool jitter, Cnt &cnt) {
+Ray ray_marching(const mbgb_scene &s, Calc &c, Vec start, Vec dir, std::vector<Step> &buf, bool jitter, Cnt &cnt,
+                 double thrIn = 0.0) {
   Ray out{};
   Vec point{0, 0, 0};
   bool found = false;
   double scan = s.viewDistanceMin;
-  double thr = 0.0;
-  const double thrInit = 0.0;
+  // *distThreshOut: 0 for the camera ray, the previous ray's threshold for a reflection
+  double thr = thrIn;
+  const double thrInit = thrIn;
   double dist = 0;
   const double limit = 1.0 - 0.01 * s.quality;
   double step = s.viewDistanceMin;
@@ -1552,7 +1554,66 @@ void setup_frame(const mbgb_scene &s, Frame &f) {
   }
 }
 
-void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jitter, const mbgb_image *img, Cnt &cnt) {
+// ObjectShader (src/shaders.cpp:21-112) at a hit: object and specular terms, surface colour.
+void object_shader(const mbgb_scene &s, const Frame &f, Calc &c, Vec point, Vec view, double thr, double delta,
+                   double lastDist, int objectType, double obj[3], double specOut[3], Vec &objColour) {
+  const Vec n = calculate_normals(s, c, point, delta, thr);
+  double shade = dot(n, f.light);
+  if (shade < 0) shade = 0;
+  const double shadeV = s.directLight * ((1.0 - s.shading) + s.shading * shade);
+  double shadow = 1.0;
+  if (s.shadow) shadow = main_shadow(s, c, point, f.light, thr, delta, f.start);
+  Vec half = normalize(sub(f.light, view));
+  double sp = dot(n, half);
+  if (sp < 0.0) sp = 0.0;
+  sp = pow(sp, 30.0) * 1.0;
+  if (sp > 15.0) sp = 15.0;
+  sp *= s.specular;
+  const Vec col = surface_colour(s, c, point, objectType);
+  objColour = col;
+  double amb = 0.0;
+  if (s.global_ilumination) {
+    if (s.fastGlobalIllumination) amb = fast_ao(s, c, point, n, thr);
+    else amb = ray_ao(s, c, point, delta, thr, lastDist, f.aoDirs, f.start);
+  }
+  const double a2 = amb * s.globalIlum;
+  const double ml[3] = {s.mainLightIntensity * s.mainLightColour.R / 65536.0,
+                        s.mainLightIntensity * s.mainLightColour.G / 65536.0,
+                        s.mainLightIntensity * s.mainLightColour.B / 65536.0};
+  const double cc[3] = {col.x, col.y, col.z};
+  const double env = ((!s.raytracedReflections && s.reflect > 0) ? env_mapping(n, view) : 0.0) * s.reflect;
+  double auxS[3] = {0, 0, 0}, auxSp[3] = {0, 0, 0};
+  if (f.numberOfLights > 0) aux_lights(s, f, c, point, n, view, delta, thr, auxS, auxSp);
+  // FakeLights (src/shaders.cpp:1225-1271)
+  double fake = 0.0, fakeSp = 0.0;
+  if (s.fakeLightsEnabled) {
+    const double dl = thr * s.smoothness;
+    const double rr = compute(c, point, kOrbitTrap, 0, nullptr);
+    const double fl = s.fakeLightsIntensity / rr;
+    const double r = 1.0 / (rr + 1e-30);
+    const double rx = 1.0 / (compute(c, add(point, Vec{dl, 0.0, 0.0}), kOrbitTrap, 0, nullptr) + 1e-30);
+    const double ry = 1.0 / (compute(c, add(point, Vec{0.0, dl, 0.0}), kOrbitTrap, 0, nullptr) + 1e-30);
+    const double rz = 1.0 / (compute(c, add(point, Vec{0.0, 0.0, dl}), kOrbitTrap, 0, nullptr) + 1e-30);
+    Vec fn{r - rx, r - ry, r - rz};
+    if (!(fn.x == 0 && fn.y == 0 && fn.z == 0)) fn = normalize(fn);
+    fake = fl * dot(n, fn);
+    if (fake < 0) fake = 0;
+    double fs = dot(n, normalize(sub(fn, view)));
+    if (fs < 0.0) fs = 0.0;
+    fs = pow(fs, 30.0) * fl;
+    if (fs > 15.0) fs = 15.0;
+    fakeSp = fs;
+  }
+  for (int k = 0; k < 3; k++) {
+    double o = env * amb + (a2 + ml[k] * shadeV * shadow) * cc[k];
+    o += (auxS[k] + fake) * cc[k];
+    obj[k] = o;
+    specOut[k] = auxSp[k] + fakeSp + ml[k] * sp * shadow;
+  }
+}
+
+void render_pixel(const Frame &f, int x, int y, std::vector<std::vector<Step>> &bufs, bool jitter,
+                  const mbgb_image *img, Cnt &cnt) {
   const mbgb_scene &s = *f.s;
   const int W = img->width, H = img->height;
   const int tiles = s.noOfTiles;
@@ -1579,90 +1640,89 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
   }
   const Vec view = rot(f.rm, f.rzero, v);
   Calc c{&s, (int)s.N, s.minN, false, 0.0, 0, &cnt, &f.d};
-  Ray ray{};
-  if (!cut) ray = ray_marching(s, c, f.start, view, buf, jitter, cnt);
+  // the reflection loop (src/Render3D.cpp:441-564)
+  const int maxRay = (s.raytracedReflections && s.reflectionsMax > 0) ? s.reflectionsMax : 0;
+  struct Refl {
+    Vec start, view;
+    Ray ray;
+    int objectType;
+    double reflect;
+  };
+  std::vector<Refl> rb((size_t)maxRay + 1);
+  Vec startRay = f.start, viewRay = view;
+  double thrCarry = 0.0;
+  int rayEnd = 0, iters0 = 0;
   bool levelMissed = false;
-  if (f.exact && ray.found) levelMissed = !level_set(s, c, f.start, view, ray);
-  const int objectType = c.objectOut;
-  const int iters = c.itersOut;
-  double out[4] = {0, 0, 0, 0};
-  Vec objColour{0, 0, 0};
-  double depthZ = ray.depth;
-  const double thr = ray.thr;
-  c.detail = thr;
-  const double delta = s.constantDEThreshold ? ray.depth * s.resolution * s.persp : thr * s.quality;
-  if (ray.found) {
-    const Vec n = calculate_normals(s, c, ray.point, delta, thr);
-    double shade = dot(n, f.light);
-    if (shade < 0) shade = 0;
-    const double shadeV = s.directLight * ((1.0 - s.shading) + s.shading * shade);
-    double shadow = 1.0;
-    if (s.shadow) shadow = main_shadow(s, c, ray.point, f.light, thr, delta, f.start);
-    Vec half = normalize(sub(f.light, view));
-    double sp = dot(n, half);
-    if (sp < 0.0) sp = 0.0;
-    sp = pow(sp, 30.0) * 1.0;
-    if (sp > 15.0) sp = 15.0;
-    sp *= s.specular;
-    const Vec col = surface_colour(s, c, ray.point, objectType);
-    objColour = col;
-    double amb = 0.0;
-    if (s.global_ilumination) {
-      if (s.fastGlobalIllumination) amb = fast_ao(s, c, ray.point, n, thr);
-      else amb = ray_ao(s, c, ray.point, delta, thr, ray.lastDist, f.aoDirs, f.start);
+  Vec lastPoint{0, 0, 0};
+  for (int k = 0; k <= maxRay; k++) {
+    Refl &r = rb[(size_t)k];
+    r.start = startRay;
+    r.view = viewRay;
+    r.ray = Ray{};
+    r.ray.thr = thrCarry;
+    r.ray.point = lastPoint;
+    if (!cut) r.ray = ray_marching(s, c, startRay, viewRay, bufs[(size_t)k], jitter, cnt, thrCarry);
+    if (k == 0) {
+      if (f.exact && r.ray.found) levelMissed = !level_set(s, c, f.start, view, r.ray);
+      iters0 = c.itersOut;
     }
-    const double a2 = amb * s.globalIlum;
-    const double ml[3] = {s.mainLightIntensity * s.mainLightColour.R / 65536.0,
-                          s.mainLightIntensity * s.mainLightColour.G / 65536.0,
-                          s.mainLightIntensity * s.mainLightColour.B / 65536.0};
-    const double cc[3] = {col.x, col.y, col.z};
-    const double env = ((!s.raytracedReflections && s.reflect > 0) ? env_mapping(n, view) : 0.0) * s.reflect;
-    double auxS[3] = {0, 0, 0}, auxSp[3] = {0, 0, 0};
-    if (f.numberOfLights > 0) aux_lights(s, f, c, ray.point, n, view, delta, thr, auxS, auxSp);
-    // FakeLights (src/shaders.cpp:1225-1271)
-    double fake = 0.0, fakeSp = 0.0;
-    if (s.fakeLightsEnabled) {
-      const double dl = thr * s.smoothness;
-      const double rr = compute(c, ray.point, kOrbitTrap, 0, nullptr);
-      const double fl = s.fakeLightsIntensity / rr;
-      const double r = 1.0 / (rr + 1e-30);
-      const double rx = 1.0 / (compute(c, add(ray.point, Vec{dl, 0.0, 0.0}), kOrbitTrap, 0, nullptr) + 1e-30);
-      const double ry = 1.0 / (compute(c, add(ray.point, Vec{0.0, dl, 0.0}), kOrbitTrap, 0, nullptr) + 1e-30);
-      const double rz = 1.0 / (compute(c, add(ray.point, Vec{0.0, 0.0, dl}), kOrbitTrap, 0, nullptr) + 1e-30);
-      Vec fn{r - rx, r - ry, r - rz};
-      if (!(fn.x == 0 && fn.y == 0 && fn.z == 0)) fn = normalize(fn);
-      fake = fl * dot(n, fn);
-      if (fake < 0) fake = 0;
-      double fs = dot(n, normalize(sub(fn, view)));
-      if (fs < 0.0) fs = 0.0;
-      fs = pow(fs, 30.0) * fl;
-      if (fs > 15.0) fs = 15.0;
-      fakeSp = fs;
-    }
-    for (int k = 0; k < 3; k++) {
-      double obj = env * amb + (a2 + ml[k] * shadeV * shadow) * cc[k];
-      obj += (auxS[k] + fake) * cc[k];
-      const double spec = auxSp[k] + fakeSp + ml[k] * sp * shadow;
-      out[k] = obj + 0.0 + spec;
-    }
-    out[3] = 1.0 + 0.0;
-  } else {
-    const Vec bg = background(s, view);
-    out[0] = 0.0 + bg.x + 0.0;
-    out[1] = 0.0 + bg.y + 0.0;
-    out[2] = 0.0 + bg.z + 0.0;
-    out[3] = 0.0;
-    depthZ = 1e20;
+    lastPoint = r.ray.point;
+    thrCarry = r.ray.thr;
+    r.objectType = c.objectOut;
+    const double pr[7] = {s.reflect, s.primitivePlaneReflect, s.primitiveWaterReflect, s.primitiveSphereReflect,
+                          s.primitiveInvertedSphereReflect, s.primitiveBoxReflect, s.primitiveInvertedBoxReflect};
+    r.reflect = pr[r.objectType];
+    rayEnd = k;
+    if (!r.ray.found) break;
+    if (r.reflect == 0) break;
+    c.detail = r.ray.thr;
+    const double dl = s.constantDEThreshold ? r.ray.depth * s.resolution * s.persp : r.ray.thr * s.quality;
+    const Vec vn = calculate_normals(s, c, r.ray.point, dl, r.ray.thr);
+    viewRay = sub(viewRay, mul(mul(vn, dot(viewRay, vn)), 2.0));
+    startRay = add(r.ray.point, mul(viewRay, r.ray.thr));
   }
-  float opacity = 0.0f;
-  volumetric(s, f, c, buf, ray.count, ray.depth, view, delta, ray.lastDist, out, &opacity);
+  double result[3] = {0, 0, 0};
+  Vec objColour{0, 0, 0};
+  float opacity0 = 0.0f;
+  double alpha0 = 0.0;
+  for (int k = rayEnd; k >= 0; k--) {
+    Refl &r = rb[(size_t)k];
+    const double thr = r.ray.thr;
+    c.detail = thr;
+    const double delta = s.constantDEThreshold ? r.ray.depth * s.resolution * s.persp : thr * s.quality;
+    double obj[3] = {0, 0, 0}, spec[3] = {0, 0, 0}, bg[3] = {0, 0, 0};
+    double out[4];
+    if (r.ray.found) {
+      object_shader(s, f, c, r.ray.point, r.view, thr, delta, r.ray.lastDist, r.objectType, obj, spec, objColour);
+    } else {
+      const Vec b = background(s, r.view);
+      bg[0] = b.x;
+      bg[1] = b.y;
+      bg[2] = b.z;
+    }
+    for (int q = 0; q < 3; q++) {
+      if (maxRay > 0 && rayEnd > 0 && k != rayEnd)
+        out[q] = result[q] * r.reflect + (1.0 - r.reflect) * (obj[q] + bg[q]) + spec[q];
+      else
+        out[q] = obj[q] + bg[q] + spec[q];
+    }
+    out[3] = r.ray.found ? 1.0 + 0.0 : 0.0 + 0.0;
+    float opacity = 0.0f;
+    volumetric(s, f, c, bufs[(size_t)k], r.ray.count, r.ray.depth, r.view, delta, r.ray.lastDist, out, &opacity);
+    for (int q = 0; q < 3; q++) result[q] = out[q];
+    if (k == 0) {
+      opacity0 = opacity;
+      alpha0 = out[3];
+    }
+  }
+  const double depthZ = rb[0].ray.found ? rb[0].ray.depth : 1e20;
   const int64_t pix = (int64_t)y * W + x;
-  if (img->opacity) img->opacity[pix] = to_u16((double)opacity * 65535.0);
-  if (img->alpha) img->alpha[pix] = to_u16(out[3] * 65535.0);
+  if (img->opacity) img->opacity[pix] = to_u16((double)opacity0 * 65535.0);
+  if (img->alpha) img->alpha[pix] = to_u16(alpha0 * 65535.0);
   if (img->image_float) {
-    img->image_float[3 * pix + 0] = (float)out[0];
-    img->image_float[3 * pix + 1] = (float)out[1];
-    img->image_float[3 * pix + 2] = (float)out[2];
+    img->image_float[3 * pix + 0] = (float)result[0];
+    img->image_float[3 * pix + 1] = (float)result[1];
+    img->image_float[3 * pix + 2] = (float)result[2];
   }
   if (img->colour) {
     img->colour[3 * pix + 0] = to_u8(objColour.x * 255);
@@ -1670,8 +1730,8 @@ void render_pixel(const Frame &f, int x, int y, std::vector<Step> &buf, bool jit
     img->colour[3 * pix + 2] = to_u8(objColour.z * 255);
   }
   if (img->zbuffer) img->zbuffer[pix] = (float)depthZ;
-  if (img->hit) img->hit[pix] = ray.found ? (levelMissed ? 3 : 1) : 0;
-  if (img->iters) img->iters[pix] = iters;
+  if (img->hit) img->hit[pix] = rb[0].ray.found ? (levelMissed ? 3 : 1) : 0;
+  if (img->iters) img->iters[pix] = iters0;
   if (img->depth) img->depth[pix] = depthZ;
 }
 
@@ -1719,11 +1779,12 @@ static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int 
   std::atomic<int> next(row0);
   std::vector<Cnt> cnts(threads);
   auto worker = [&](int t) {
-    std::vector<Step> buf(10002);
+    const int rays = 1 + ((s->raytracedReflections && s->reflectionsMax > 0) ? s->reflectionsMax : 0);
+    std::vector<std::vector<Step>> bufs((size_t)rays, std::vector<Step>(10002));
     for (;;) {
       const int y = next.fetch_add(1);
       if (y >= row1) break;
-      for (int x = 0; x < img->width; x++) render_pixel(f, x, y, buf, jitter != 0, img, cnts[t]);
+      for (int x = 0; x < img->width; x++) render_pixel(f, x, y, bufs, jitter != 0, img, cnts[t]);
     }
   };
   if (threads == 1) {

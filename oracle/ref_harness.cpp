@@ -12,7 +12,7 @@
 //   * the Mandelbox matrices of RecalculateIFSParams (src/callbacks.cpp:1549-1556);
 //   * a restatement of RayMarching (src/Render3D.cpp:79-199) with the Random()
 //     step jitter behind a switch, and of the MainThread pixel body
-//     (src/Render3D.cpp:213-344, 389-589) for reflections off.
+//     (src/Render3D.cpp:213-344, 389-589) with its reflection loop.
 // Distance estimates, normals, shadows, AO, colouring, background and the
 // volumetric pass are the reference's compiled functions.
 // Used only by tests/golden/make_golden.py to produce golden vectors.
@@ -169,6 +169,10 @@ sParamRender *make_params(const mbgb_scene &s) {
   a.reflect = s.reflect; a.globalIlum = s.globalIlum; a.brightness = s.brightness; a.glow_intensity = s.glow_intensity;
   a.fogVisibility = s.fogVisibility; a.coloring_speed = s.coloring_speed; a.imageGamma = s.imageGamma;
   a.paletteOffset = s.paletteOffset; a.mainLightIntensity = s.mainLightIntensity; a.contrast = s.contrast;
+  d.primitivePlaneReflect = s.primitivePlaneReflect; d.primitiveBoxReflect = s.primitiveBoxReflect;
+  d.primitiveInvertedBoxReflect = s.primitiveInvertedBoxReflect; d.primitiveSphereReflect = s.primitiveSphereReflect;
+  d.primitiveInvertedSphereReflect = s.primitiveInvertedSphereReflect;
+  d.primitiveWaterReflect = s.primitiveWaterReflect;
   d.vp = v3(s.vp);
   d.auxLightRandomCenter = v3(s.auxLightRandomCenter);
 
@@ -399,6 +403,18 @@ int ref_render(const mbgb_scene *s, int row0, int row1, int jitter, const mbgb_i
   vector.y = sin(param.doubles.mainLightAlpha - 0.5 * M_PI) * cos(-param.doubles.mainLightBeta);
   vector.z = sin(-param.doubles.mainLightBeta);
   shadowVector = mRot.RotateVector(vector);
+  // per-ray step buffers of the reflection loop (src/Render3D.cpp:260-268)
+  int maxRay = param.reflectionsMax;
+  if (!param.imageSwitches.raytracedReflections) maxRay = 0;
+  struct Refl {
+    CVector3 start, viewVector, point;
+    bool found;
+    int buffCount, objectType;
+    double lastDist, depth, distThresh, reflect;
+    sStep *stepBuff;
+  };
+  Refl *reflectBuff = new Refl[maxRay + 2];
+  for (int i = 0; i < maxRay + 1; i++) reflectBuff[i].stepBuff = new sStep[10002];
   sStep *stepBuff = new sStep[10002];
   sVectorsAround *vectorsAround = new sVectorsAround[10000];
   int counter = 0;
@@ -464,72 +480,134 @@ int ref_render(const mbgb_scene *s, int row0, int row1, int jitter, const mbgb_i
         viewVector.z = z2 * fov;
       }
       viewVector = mRot.RotateVector(viewVector);
+      // the reflection loop of MainThread (src/Render3D.cpp:441-564)
       double distThresh = 0.0;
       CVector3 point;
-      bool found = false;
-      int buffCount = 0;
-      double lastDist = 0, depth = 0;
-      calcParam.itersOut = 0;
-      if (!hemisphereCut)
-        point = ray_marching(&param, &calcParam, start, viewVector, maxDepth, true, stepBuff, &buffCount, &distThresh,
-                             &lastDist, &found, &depth, jitter != 0);
-      const int itersAtEnd = calcParam.itersOut;
+      CVector3 startRay = start;
+      sShaderOutput resultShader = {0.0, 0.0, 0.0, 0.0};
       sShaderOutput objectColour = {0.0, 0.0, 0.0, 0.0};
-      sShaderOutput objectShader = {0.0, 0.0, 0.0, 0.0};
-      sShaderOutput backgroudShader = {0.0, 0.0, 0.0, 0.0};
-      sShaderOutput specular = {0.0, 0.0, 0.0, 0.0};
-      sShaderInputData in;
-      in.calcParam = &calcParam;
-      in.param = &param;
-      in.dist_thresh = distThresh;
-      if (param.fractal.constantDEThreshold) in.delta = depth * param.doubles.resolution * param.doubles.persp;
-      else in.delta = distThresh * param.doubles.quality;
-      in.calcParam->doubles.detailSize = distThresh;
-      in.lightVect = shadowVector;
-      in.point = point;
-      in.viewVector = viewVector;
-      in.eyePoint = start;
-      in.vectorsCount = vectorsCount;
-      in.vectorsAround = vectorsAround;
-      in.lastDist = lastDist;
-      in.envMappingTexture = param.envmapTexture;
-      in.depth = depth;
-      in.stepCount = buffCount;
-      in.stepBuff = stepBuff;
-      in.objectType = calcParam.objectOut;
-      if (found) {
-        objectShader = ObjectShader(in, &objectColour, &specular);
-      } else {
-        backgroudShader = BackgroundShader(in);
-        depth = 1e20;  // reflectBuff depth only; in.depth keeps the march depth (src/Render3D.cpp:528-541)
+      int rayEnd = 0;
+      int itersAtEnd = 0;
+      calcParam.itersOut = 0;  // the iters layer (not a reference output) starts at 0 per pixel
+      for (int ray = 0; ray <= maxRay; ray++) {
+        Refl &rb = reflectBuff[ray];
+        rb.start = startRay;
+        rb.viewVector = viewVector;
+        rb.found = false;
+        rb.buffCount = 0;
+        rb.depth = 0;
+        rb.lastDist = 0;
+        if (!hemisphereCut) {
+          point = ray_marching(&param, &calcParam, startRay, viewVector, maxDepth, true, rb.stepBuff, &rb.buffCount,
+                               &distThresh, &rb.lastDist, &rb.found, &rb.depth, jitter != 0);
+        } else {
+          rb.found = false;
+        }
+        if (ray == 0) itersAtEnd = calcParam.itersOut;
+        rb.point = point;
+        rb.distThresh = distThresh;
+        rb.objectType = calcParam.objectOut;
+        if (calcParam.objectOut == objFractal) rb.reflect = param.doubles.imageAdjustments.reflect;
+        if (calcParam.objectOut == objWater) rb.reflect = param.doubles.primitiveWaterReflect;
+        if (calcParam.objectOut == objPlane) rb.reflect = param.doubles.primitivePlaneReflect;
+        if (calcParam.objectOut == objBox) rb.reflect = param.doubles.primitiveBoxReflect;
+        if (calcParam.objectOut == objBoxInv) rb.reflect = param.doubles.primitiveInvertedBoxReflect;
+        if (calcParam.objectOut == objSphere) rb.reflect = param.doubles.primitiveSphereReflect;
+        if (calcParam.objectOut == objSphereInv) rb.reflect = param.doubles.primitiveInvertedSphereReflect;
+        rayEnd = ray;
+        if (!rb.found) break;
+        if (rb.reflect == 0) break;
+        startRay = point;
+        sShaderInputData sd;
+        sd.calcParam = &calcParam;
+        sd.param = &param;
+        sd.dist_thresh = rb.distThresh;
+        sd.calcParam->doubles.detailSize = rb.distThresh;
+        sd.lightVect = shadowVector;
+        sd.point = point;
+        sd.viewVector = viewVector;
+        if (param.fractal.constantDEThreshold) sd.delta = rb.depth * param.doubles.resolution * param.doubles.persp;
+        else sd.delta = rb.distThresh * param.doubles.quality;
+        CVector3 vn = CalculateNormals(sd);
+        viewVector = viewVector - vn * viewVector.Dot(vn) * 2.0;
+        startRay = startRay + viewVector * rb.distThresh;
       }
-      sShaderOutput pixel;
-      pixel.R = objectShader.R + backgroudShader.R + specular.R;
-      pixel.G = objectShader.G + backgroudShader.G + specular.G;
-      pixel.B = objectShader.B + backgroudShader.B + specular.B;
-      pixel.alpha = objectShader.alpha + backgroudShader.alpha;
-      // the reference leaves opacityOut unset when no step group is composited; 0 here
-      sShaderOutput opacityOut = {0.0, 0.0, 0.0, 0.0};
-      sShaderOutput vol = VolumetricShader(in, pixel, &opacityOut);
+      unsigned short opacity16 = 0, alpha16 = 0;
+      for (int ray = rayEnd; ray >= 0; ray--) {
+        Refl &rb = reflectBuff[ray];
+        sShaderOutput objectShader = {0.0, 0.0, 0.0, 0.0};
+        sShaderOutput backgroudShader = {0.0, 0.0, 0.0, 0.0};
+        sShaderOutput specular = {0.0, 0.0, 0.0, 0.0};
+        sShaderInputData in;
+        in.calcParam = &calcParam;
+        in.param = &param;
+        in.dist_thresh = rb.distThresh;
+        if (param.fractal.constantDEThreshold) in.delta = rb.depth * param.doubles.resolution * param.doubles.persp;
+        else in.delta = rb.distThresh * param.doubles.quality;
+        in.calcParam->doubles.detailSize = rb.distThresh;
+        in.lightVect = shadowVector;
+        in.point = rb.point;
+        in.viewVector = rb.viewVector;
+        in.eyePoint = start;
+        in.vectorsCount = vectorsCount;
+        in.vectorsAround = vectorsAround;
+        in.lastDist = rb.lastDist;
+        in.envMappingTexture = param.envmapTexture;
+        in.depth = rb.depth;
+        in.stepCount = rb.buffCount;
+        in.stepBuff = rb.stepBuff;
+        in.objectType = (enumObjectType)rb.objectType;
+        if (rb.found) {
+          objectShader = ObjectShader(in, &objectColour, &specular);
+        } else {
+          backgroudShader = BackgroundShader(in);
+          rb.depth = 1e20;  // reflectBuff depth only; in.depth keeps the march depth (src/Render3D.cpp:528-541)
+        }
+        const double reflect = rb.reflect;
+        sShaderOutput pixel;
+        if (maxRay > 0 && rayEnd > 0 && ray != rayEnd) {
+          pixel.R = resultShader.R * reflect + (1.0 - reflect) * (objectShader.R + backgroudShader.R) + specular.R;
+          pixel.G = resultShader.G * reflect + (1.0 - reflect) * (objectShader.G + backgroudShader.G) + specular.G;
+          pixel.B = resultShader.B * reflect + (1.0 - reflect) * (objectShader.B + backgroudShader.B) + specular.B;
+        } else {
+          pixel.R = objectShader.R + backgroudShader.R + specular.R;
+          pixel.G = objectShader.G + backgroudShader.G + specular.G;
+          pixel.B = objectShader.B + backgroudShader.B + specular.B;
+        }
+        pixel.alpha = objectShader.alpha + backgroudShader.alpha;
+        // the reference leaves opacityOut unset when no step group is composited; 0 here
+        sShaderOutput opacityOut = {0.0, 0.0, 0.0, 0.0};
+        sShaderOutput vol = VolumetricShader(in, pixel, &opacityOut);
+        resultShader.R = vol.R;
+        resultShader.G = vol.G;
+        resultShader.B = vol.B;
+        if (ray == 0) {
+          opacity16 = (unsigned short)(opacityOut.R * 65535.0);
+          alpha16 = (unsigned short)(vol.alpha * 65535.0);
+        }
+      }
       const long pix = (long)yScr * width + xScr;
-      if (img->opacity) img->opacity[pix] = (unsigned short)(opacityOut.R * 65535.0);
-      if (img->alpha) img->alpha[pix] = (unsigned short)(vol.alpha * 65535.0);
+      if (img->opacity) img->opacity[pix] = opacity16;
+      if (img->alpha) img->alpha[pix] = alpha16;
       if (img->image_float) {
-        img->image_float[3 * pix + 0] = vol.R;
-        img->image_float[3 * pix + 1] = vol.G;
-        img->image_float[3 * pix + 2] = vol.B;
+        img->image_float[3 * pix + 0] = resultShader.R;
+        img->image_float[3 * pix + 1] = resultShader.G;
+        img->image_float[3 * pix + 2] = resultShader.B;
       }
       if (img->colour) {
         img->colour[3 * pix + 0] = objectColour.R * 255;
         img->colour[3 * pix + 1] = objectColour.G * 255;
         img->colour[3 * pix + 2] = objectColour.B * 255;
       }
-      if (img->zbuffer) img->zbuffer[pix] = (float)depth;
-      if (img->hit) img->hit[pix] = found ? 1 : 0;
+      const double depth0 = reflectBuff[0].depth;
+      if (img->zbuffer) img->zbuffer[pix] = (float)depth0;
+      if (img->hit) img->hit[pix] = reflectBuff[0].found ? 1 : 0;
       if (img->iters) img->iters[pix] = itersAtEnd;
-      if (img->depth) img->depth[pix] = depth;
+      if (img->depth) img->depth[pix] = depth0;
     }
   }
+  for (int i = 0; i < maxRay + 1; i++) delete[] reflectBuff[i].stepBuff;
+  delete[] reflectBuff;
   delete[] stepBuff;
   delete[] vectorsAround;
   delete param.lightmapTexture;

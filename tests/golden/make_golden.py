@@ -152,6 +152,15 @@ EXAMPLES = {
     "fx_primitives_inverted_box": ("primitive objects - inverted box.fract", {"raytraced_reflections": 0}),
     "fx_primitives_set": ("primitive objects - set.fract", {"raytraced_reflections": 0}),
     "fx_primitives_water": ("primitive objects - water.fract", {"raytraced_reflections": 0}),
+    # ray-traced reflections
+    "fx_reflections_1": ("raytraced reflections 1.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_2": ("raytraced reflections 2.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_tglad_scale_m2": ("tglad - scale -2.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_quaternion_julia": ("quaternion - julia.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_foldintpow2": ("FoldIntPow2 3.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_primitives_set": ("primitive objects - set.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_primitives_water": ("primitive objects - water.fract", {"textured_background": 0}, 32, 24),
+    "fx_reflections_inverted_box": ("primitive objects - inverted box.fract", {"textured_background": 0}, 32, 24),
 }
 
 # Formulas no example uses, on the benchmark workloads' settings.

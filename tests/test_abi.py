@@ -33,8 +33,8 @@ def test_unsupported_features_are_reported(mblib):
     from mandelbulber_gb300 import workloads as W
     for key, value, text in [("formula", 38, "formula"),
                              ("textured_background", 1, "textured background"),
-                             ("raytraced_reflections", 1, "reflections")]:
-        sc = W.workload("mandelbulb_640x480", **{key: value})
+                             ("reflections_max", 11, "reflections")]:
+        sc = W.workload("mandelbulb_640x480", raytraced_reflections=1, **{key: value})
         ok, why = mb.supported(sc)
         assert not ok and text in why, (key, why)
     ok, why = mb.supported(W.workload("mandelbox_1080p"))
