@@ -282,6 +282,44 @@ def grad_section(ctx, torch, dev, args) -> dict:
             "check": "tests/test_gpu_grad.py: adjoint vs central differences (h = 1e-4, FP64) within 1e-3"}
 
 
+# Scenes of the other formulas and of the secondary effects (from the committed fixtures,
+# which hold the reference's example scenes), rendered at a larger size for the coverage
+# section: (fixture, width, height).
+COVERAGE_SCENES = [
+    ("trigde_40x32", 480, 270), ("ex_power2_default", 480, 270), ("ex_quaternion_lathe", 480, 270),
+    ("menger_48x32", 480, 270), ("ex_ifs_icosahedron", 480, 270), ("ex_hybrid_1", 480, 270),
+    ("ex_modified_mandelbulb_3", 480, 270), ("smooth_mandelbox", 480, 270), ("vary4d_48x32", 480, 270),
+    ("fold_box_icosa", 480, 270), ("ex_aux_coloured_lights", 480, 270), ("ex_fx_iter_fog_2", 480, 270),
+    ("ex_fx_volumetric_light_2", 480, 270), ("ex_fx_reflections_1", 480, 270), ("ex_fx_primitives_set", 480, 270),
+    ("ex_fx_envmap_mandelbox", 480, 270), ("fake_lights_mandelbox", 480, 270),
+    ("ex_fx_slow_interior_mandelbox", 240, 135),
+]
+
+
+def coverage_section(ctx) -> dict:
+    """Every other formula and the secondary effects: one frame of each scene at 480x270
+    (slow shading 240x135) under the FP32 policy after one untimed frame, device time from
+    the library's CUDA events around its launches. Delta-DE formulas render in FP64 (the
+    `fp64` flag), the effect scenes on the per-pixel engine."""
+    import mandelbulber_gb300 as mb
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden")
+    out = {}
+    for case, w, h in COVERAGE_SCENES:
+        z = np.load(os.path.join(golden, f"render_{case}.npz"))
+        sc = mb.scene_from_bytes(z["scene"].tobytes())
+        sc.image_width, sc.image_height = w, h
+        sc.resolution = 1.0 / w / sc.noOfTiles
+        ctx.render(sc, precision=mb.PREC_FP32_FIX)
+        img = ctx.render(sc, precision=mb.PREC_FP32_FIX)
+        st = ctx.stats()
+        out[case] = {"formula": int(sc.formula), "size": [w, h], "ms": float(st.kernel_ms),
+                     "mpix_per_s": w * h / (st.kernel_ms * 1e3) if st.kernel_ms > 0 else None,
+                     "de_evaluations_per_s": st.de_calls / (st.kernel_ms / 1e3) if st.kernel_ms > 0 else None,
+                     "fp64": bool(st.auto_fp64), "launches": int(st.launches),
+                     "hit_fraction": float(img.hit.mean())}
+    return out
+
+
 def run_once(args) -> int:
     """One frame of the workload at a small size (plus `--warmup` frames): the ncu profiling case."""
     import mandelbulber_gb300 as mb
@@ -312,6 +350,7 @@ def main() -> int:
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-frame flight batch")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient workload")
+    ap.add_argument("--no-coverage", action="store_true", help="skip the other formulas / effects scenes")
     ap.add_argument("--grad-steps", type=int, default=5)
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
@@ -457,6 +496,7 @@ def main() -> int:
     launches_per_frame = int(ctx.stats().launches)
 
     batch = None if args.no_batch else batch_section(ctx, torch, dev, stream, flush, args, world, dist)
+    coverage = None if args.no_coverage else coverage_section(ctx)
     grads = None if args.no_grad else grad_section(ctx, torch, dev, args)
 
     cpu = None
@@ -495,6 +535,7 @@ def main() -> int:
         "gpu_launches": args.steps * launches_per_frame,
         "batch": batch,
         "grads": grads,
+        "coverage": coverage,
         "clocks": clocks,
         "cpu_baseline": cpu,
         "wall_s_timed_region": wall32,

@@ -432,6 +432,14 @@ mbgb_status mbgb_compile_image16_device(mbgb_context *ctx, const mbgb_scene *sce
 mbgb_status mbgb_ssao_device(mbgb_context *ctx, const mbgb_scene *scene, const mbgb_image *layers,
                              uint16_t *image16);
 
+/* PostRendering_DOF (src/image.cpp:57-206) in place on image16 (device, RGB16) and the alpha
+ * layer of `layers` (device), reading its z-buffer: radius scene->DOFRadius x width / 1000,
+ * focus 10^(scene->DOFFocus / 10 - 16). The splat order is the reference's: z-buffer
+ * quicksort, then its Random() shuffle drawn from rand() seeded with `seed` (the reference
+ * continues its process's rand() stream there). Synchronous. */
+mbgb_status mbgb_dof_device(mbgb_context *ctx, const mbgb_scene *scene, const mbgb_image *layers,
+                            uint16_t *image16, uint32_t seed);
+
 #ifdef __cplusplus
 }
 #endif

@@ -133,6 +133,8 @@ FUNCTIONS = {
     "mbgb_compile_image16_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), ctypes.c_void_p, ctypes.c_int32,
                                                    ctypes.c_int32, ctypes.c_void_p]),
     "mbgb_ssao_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), ctypes.c_void_p]),
+    "mbgb_dof_device": (ctypes.c_int, [ctypes.c_void_p, _P(mbgb_scene), _P(mbgb_image), ctypes.c_void_p,
+                                       ctypes.c_uint32]),
 }
 
 

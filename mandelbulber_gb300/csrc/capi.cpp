@@ -618,7 +618,7 @@ struct mbgb_context {
   int sms = 0;
   cudaStream_t stream = nullptr;
   DeviceBuf step[2][5];          // per-pixel engine: [precision][step, dist, thr, scan, iters], kStepCap records per slot
-  DeviceBuf ovstep[2][5];        // overflow pass: kStepSlots records per slot, kOverflowThreads slots
+  DeviceBuf ovstep[2][5];        // overflow passes: kStepSlots records per slot and ray
   DeviceBuf ovlist;              // overflow pixel list (per-pixel engine)
   DeviceBuf control;             // error flag, start time, stage counters
   DeviceBuf fctl;                // per group: wavefront stage counters / per-pixel tile counter (64 B each)
@@ -1115,14 +1115,31 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
 
 // Enqueue the per-pixel engine (render_core.cuh) for one frame: main pass, then (when
 // the step buffer is in use) the overflow pass.
-// CTAs per SM of the per-pixel engine: the occupancy limit (or the tuned value); one when the
-// scene keeps step records for several rays of the reflection loop, which bounds their memory
-// (thread slots x rays x kStepCap records).
-static int per_pixel_ctas(const mbgb_scene &scene, int prec, const LaunchCfg &cfg) {
+// CTAs per SM of the per-pixel engine: the occupancy limit (or the tuned value), lowered when
+// the step records of the reflection loop's rays (thread slots x rays x kStepCap records)
+// would pass 16 GB.
+static int per_pixel_ctas(const mbgb_scene &scene, int prec, const LaunchCfg &cfg, int sms) {
   int per_sm = std::max(1, occupancy_render(prec, scene_kernel_formula(scene), cfg.block));
   if (cfg.ctasPerSm > 0) per_sm = std::min(per_sm, cfg.ctasPerSm);
-  if (reflection_rays(scene) > 1 && need_volumetric(scene)) per_sm = 1;
+  const int rays = reflection_rays(scene);
+  if (rays > 1 && need_volumetric(scene)) {
+    const double esz = prec == 0 ? 8.0 : 4.0;
+    const double perSlot = (double)rays * kStepCap * (3 * esz + (need_step_points(scene) ? esz + 4 : 0));
+    const double cap = 16e9 / (perSlot * (double)sms * cfg.block);
+    per_sm = std::max(1, std::min(per_sm, (int)cap));
+  }
   return per_sm;
+}
+
+// Thread slots of the per-pixel engine's overflow pass (pixels whose rays need more than
+// kStepCap records): 2048, fewer when their kStepSlots records per ray of the reflection loop
+// would pass 4 GB.
+static int overflow_slots(const mbgb_scene &scene, int prec) {
+  const double esz = prec == 0 ? 8.0 : 4.0;
+  const double perSlot =
+      (double)reflection_rays(scene) * kStepSlots * (3 * esz + (need_step_points(scene) ? esz + 4 : 0));
+  const int slots = (int)std::min(2048.0, 4e9 / perSlot);
+  return std::max(kOverflowThreads, slots / 128 * 128);
 }
 
 static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, const mbgb_image &img,
@@ -1131,7 +1148,7 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   const int prec = g.prec;
   const int block = g.cfg.block;
   const int kf = scene_kernel_formula(scene);
-  const int grid = c->sms * per_pixel_ctas(scene, prec, g.cfg);
+  const int grid = c->sms * per_pixel_ctas(scene, prec, g.cfg, c->sms);
   io.image_float = img.image_float;
   io.zbuffer = img.zbuffer;
   io.alpha = img.alpha;
@@ -1160,14 +1177,15 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   FrameIO ov = io;
   ov.overflow_pass = 1;
   ov.step_cap = kStepSlots;
-  ov.slots = kOverflowThreads;
+  const int ovSlots = overflow_slots(scene, prec);
+  ov.slots = ovSlots;
   ov.step_step = c->ovstep[prec][0].ptr;
   ov.step_dist = c->ovstep[prec][1].ptr;
   ov.step_thr = c->ovstep[prec][2].ptr;
   ov.step_scan = points ? c->ovstep[prec][3].ptr : nullptr;
   ov.step_iters = points ? (int *)c->ovstep[prec][4].ptr : nullptr;
   ov.rays = io.rays;
-  const int ovBlocks = std::max(1, kOverflowThreads / block);
+  const int ovBlocks = std::max(1, ovSlots / block);
   FractalT<double> fd;
   fill_fractal<double>(scene, fd);
   cudaError_t e;
@@ -1521,7 +1539,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
   size_t wave_bytes[2] = {0, 0};
   bool volPrec[2] = {false, false};
   bool pointsPrec[2] = {false, false};
-  int maxRays[2] = {1, 1};
+  int64_t ovRecords[2] = {kOverflowThreads, kOverflowThreads};   // overflow slots x rays
   int64_t maxPixPerPixel = 0;
   int64_t maxSlots[2] = {0, 0};
   size_t camsBytes = 0;
@@ -1530,7 +1548,9 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     const bool needVol = need_volumetric(rep);
     if (needVol) volPrec[g.prec] = true;
     if (!g.wave && need_step_points(rep)) pointsPrec[g.prec] = true;
-    if (!g.wave) maxRays[g.prec] = std::max(maxRays[g.prec], reflection_rays(rep));
+    if (!g.wave)
+      ovRecords[g.prec] =
+          std::max(ovRecords[g.prec], (int64_t)overflow_slots(rep, g.prec) * reflection_rays(rep));
     if (g.wave) {
       const bool rayAO = rep.global_ilumination && !rep.fastGlobalIllumination;
       const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
@@ -1545,7 +1565,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       }
     } else if (needVol) {
       maxPixPerPixel = std::max(maxPixPerPixel, g.npix);
-      maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_pixel_ctas(rep, g.prec, g.cfg) *
+      maxSlots[g.prec] = std::max(maxSlots[g.prec], (int64_t)c->sms * per_pixel_ctas(rep, g.prec, g.cfg, c->sms) *
                                                         g.cfg.block * reflection_rays(rep));
     }
   }
@@ -1556,8 +1576,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     auto bytes_of = [&](int k) { return k == 4 ? sizeof(int) : esz; };
     if (volPrec[p])
       for (int k = 0; k < arrays; k++)
-        MBGB_CUDA(c->ensure(c->ovstep[p][k],
-                            (size_t)kStepSlots * (size_t)kOverflowThreads * (size_t)maxRays[p] * bytes_of(k)));
+        MBGB_CUDA(c->ensure(c->ovstep[p][k], (size_t)kStepSlots * (size_t)ovRecords[p] * bytes_of(k)));
     if (maxSlots[p])
       for (int k = 0; k < arrays; k++)
         MBGB_CUDA(c->ensure(c->step[p][k], (size_t)kStepCap * (size_t)maxSlots[p] * bytes_of(k)));
@@ -2062,6 +2081,16 @@ extern "C" mbgb_status mbgb_ssao_device(mbgb_context *c, const mbgb_scene *scene
   MBGB_CUDA(cudaSetDevice(c->device));
   MBGB_CUDA(c->ensure(c->post, std::max<size_t>(sizeof(int) * 65536, 16 * (size_t)(scene->SSAOQuality + 1))));
   return ssao_device(*scene, *layers, image16, c->post.ptr, c->stream);
+}
+
+extern "C" mbgb_status mbgb_dof_device(mbgb_context *c, const mbgb_scene *scene, const mbgb_image *layers,
+                                       uint16_t *image16, uint32_t seed) {
+  if (!c || !scene || !layers || !image16) return set_error(MBGB_ERR_BAD_PARAM, "NULL argument");
+  if (!layers->zbuffer || !layers->alpha) return set_error(MBGB_ERR_BAD_PARAM, "DOF needs the z-buffer and alpha layers");
+  if (layers->width <= 0 || layers->height <= 0) return set_error(MBGB_ERR_BAD_PARAM, "bad image size");
+  std::lock_guard<std::mutex> lk(c->mu);
+  MBGB_CUDA(cudaSetDevice(c->device));
+  return dof_device(*scene, *layers, image16, seed, c->stream);
 }
 
 // CompileImage / CalculatePixel / CalculateGammaTable (src/cimage.cpp:132-214), progressive factor 1.

@@ -18,7 +18,8 @@
 // The frame loop follows MainRender (src/Render3D.cpp:1940-2480): frames whose output file
 // exists are skipped, keyframe frames come from the Catmull-Rom splines of the keyframes,
 // flight frames read "x y z alpha beta gamma" per line; each frame is rendered, compiled
-// to 16 bits (CompileImage), post-processed with SSAO when post_SSAO_enabled is set, and
+// to 16 bits (CompileImage), post-processed with SSAO when post_SSAO_enabled is set and with
+// the depth of field when post_DOF_enabled is set, and
 // written as IndexFilename(file_destination, ext, frame) = destination%05d.ext.
 // JPEG needs libjpeg, which this build does not carry: -format jpg writes an 8-bit PNG.
 // Network rendering (-ip, -port) and tiled output are not part of this build.
@@ -222,6 +223,9 @@ bool render_jobs(mbgb_context *ctx, const std::vector<Job> &jobs, const Args &a)
     const size_t px = (size_t)w * h;
     ok = mbgb_compile_image16_device(ctx, &sc, outs[i].image_float, w, h, img16[i]) == MBGB_OK;
     if (ok && sc.SSAOEnabled) ok = mbgb_ssao_device(ctx, &sc, &outs[i], img16[i]) == MBGB_OK;
+    // the DOF shuffle draws from rand(); the reference continues its process's stream there,
+    // this build seeds it with the scene's colouring seed
+    if (ok && sc.DOFEnabled) ok = mbgb_dof_device(ctx, &sc, &outs[i], img16[i], (uint32_t)sc.coloring_seed) == MBGB_OK;
     if (!ok) {
       fprintf(stderr, "mbgb_cli: post-processing: %s\n", mbgb_last_error());
       break;

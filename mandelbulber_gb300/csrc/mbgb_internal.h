@@ -42,5 +42,7 @@ mbgb_status compile16_device(const mbgb_scene &scene, const float *image_float, 
                              uint16_t *image16, int *gamma_dev, cudaStream_t s);
 mbgb_status ssao_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, void *tables,
                         cudaStream_t s);
+mbgb_status dof_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, uint32_t seed,
+                       cudaStream_t s);
 
 }  // namespace mbgb

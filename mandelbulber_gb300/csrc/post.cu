@@ -1,16 +1,19 @@
 // Post-processing of a rendered frame on the device: CompileImage (src/cimage.cpp:132-214)
-// into the 16-bit image, and the screen-space ambient occlusion pass PostRendering_SSAO /
-// ThreadSSAO (src/image.cpp:249-478), which the reference runs after CompileImage when
-// post_SSAO_enabled is set (src/Render3D.cpp:1094-1099).
+// into the 16-bit image, the screen-space ambient occlusion pass PostRendering_SSAO /
+// ThreadSSAO (src/image.cpp:249-478) and the depth of field PostRendering_DOF
+// (src/image.cpp:57-206), which the reference runs in that order after the render when
+// post_SSAO_enabled / post_DOF_enabled are set (src/Render3D.cpp:1093-1106).
 //
 // Built with --fmad=false: the FP64 SSAO and the compile step follow the reference's
 // double-precision operation order, so results match it to the last bit except where
 // CUDA's atan / tanhf round differently from the host's libm.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "mbgb.h"
@@ -34,6 +37,50 @@ __global__ void compile16_kernel(const float *__restrict__ image_float, int64_t 
     const unsigned short q = (unsigned short)((double)v * 65535.0);
     image16[i] = (uint16_t)gamma[q];
   }
+}
+
+// One splat of PostRendering_DOF (src/image.cpp:148-182): the pixel at (x, y) spreads its
+// original RGB16 / alpha over the pixels within `size` at opacity (blur - r) / factor.
+struct DofSplat {
+  int x, y, size, centre;   // centre: the pixel index of (x, y)
+  double blur, factor;
+};
+
+constexpr int kDofTile = 16;
+
+// Each CTA owns one 16 x 16 tile; each thread owns one pixel of it and applies, in the
+// splat order, every splat of the tile's list that covers its pixel. A pixel's value after
+// the pass is the reference's sequential in-place fold: splats change only pixels they cover
+// and read only the frame's original values at their centres.
+__global__ void dof_kernel(const DofSplat *__restrict__ splats, const int64_t *__restrict__ tileStart,
+                           const int *__restrict__ tileList, const int tilesX, const int width, const int height,
+                           const uint16_t *__restrict__ image0, const uint16_t *__restrict__ alpha0,
+                           uint16_t *__restrict__ image16, uint16_t *__restrict__ alpha) {
+  const int tile = blockIdx.x;
+  const int xx = (tile % tilesX) * kDofTile + (int)(threadIdx.x % kDofTile);
+  const int yy = (tile / tilesX) * kDofTile + (int)(threadIdx.x / kDofTile);
+  if (xx >= width || yy >= height) return;
+  const int64_t q = (int64_t)yy * width + xx;
+  uint16_t v[3] = {image16[3 * q + 0], image16[3 * q + 1], image16[3 * q + 2]};
+  uint16_t a = alpha[q];
+  for (int64_t k = tileStart[tile]; k < tileStart[tile + 1]; k++) {
+    const DofSplat sp = splats[tileList[k]];
+    const int dx = xx - sp.x, dy = yy - sp.y;
+    if (dx < -sp.size || dx > sp.size || dy < -sp.size || dy > sp.size) continue;
+    const double r = (double)sqrtf((float)dx * dx + dy * dy);
+    double op = (sp.blur - r) / sp.factor;
+    if (op > 1.0) op = 1.0;
+    if (op < 0.0) op = 0.0;
+    if (op > 0.0) {
+      const double opN = 1.0 - op;
+      for (int c = 0; c < 3; c++) v[c] = (uint16_t)(v[c] * opN + image0[3 * (int64_t)sp.centre + c] * op);
+      a = (uint16_t)(a * opN + alpha0[sp.centre] * op);
+    }
+  }
+  image16[3 * q + 0] = v[0];
+  image16[3 * q + 1] = v[1];
+  image16[3 * q + 2] = v[2];
+  alpha[q] = a;
 }
 
 // Screen position of a pixel sample (x, y may be fractional) at depth z in the plane
@@ -180,6 +227,142 @@ mbgb_status ssao_device(const mbgb_scene &scene, const mbgb_image &layers, uint1
   if (e == cudaSuccess) e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(MBGB_ERR_CUDA, std::string("SSAO kernel: ") + cudaGetErrorString(e));
+  return MBGB_OK;
+}
+
+}  // namespace mbgb
+
+namespace {
+
+struct SortZ {
+  float z;
+  int i;
+};
+
+// QuickSortZBuffer (src/common_math.h:53-84): Hoare partition around the middle element, on
+// [l, p]; an explicit stack instead of recursion (the two parts are disjoint).
+void quicksort_z(std::vector<SortZ> &d, int l0, int p0) {
+  std::vector<std::pair<int, int>> stack{{l0, p0}};
+  while (!stack.empty()) {
+    const int l = stack.back().first, p = stack.back().second;
+    stack.pop_back();
+    int i = l, j = p;
+    const SortZ x = d[(size_t)((l + p) / 2)];
+    do {
+      while (d[(size_t)i].z < x.z) i++;
+      while (x.z < d[(size_t)j].z) j--;
+      if (i <= j) {
+        std::swap(d[(size_t)i], d[(size_t)j]);
+        i++;
+        j--;
+      }
+    } while (i <= j);
+    if (i < p) stack.push_back({i, p});
+    if (l < j) stack.push_back({l, j});
+  }
+}
+
+}  // namespace
+
+namespace mbgb {
+
+// PostRendering_DOF (src/image.cpp:57-206). The host sorts the z-buffer with the
+// reference's quicksort (element 0 stays in place, as there), shuffles it with its Random()
+// swaps (rand() seeded with `seed`; the reference continues the process's rand() stream),
+// and lists, per 16 x 16 tile, the splats that reach it in splat order (far to near); the
+// device applies the splats (dof_kernel).
+mbgb_status dof_device(const mbgb_scene &scene, const mbgb_image &layers, uint16_t *image16, uint32_t seed,
+                       cudaStream_t s) {
+  const int width = layers.width, height = layers.height;
+  const int64_t n = (int64_t)width * height;
+  if (n <= 0 || n > (int64_t)1 << 30) return set_error(MBGB_ERR_BAD_PARAM, "DOF: image size out of range");
+  const double deep = scene.DOFRadius * width / 1000.0;
+  const double neutral = pow(10, scene.DOFFocus / 10.0 - 16.0);
+  std::vector<SortZ> sortz((size_t)n);
+  std::vector<float> zb((size_t)n);
+  cudaError_t e = cudaMemcpyAsync(zb.data(), layers.zbuffer, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(MBGB_ERR_CUDA, std::string("DOF z-buffer: ") + cudaGetErrorString(e));
+  for (int64_t p = 0; p < n; p++) sortz[(size_t)p] = SortZ{zb[(size_t)p], (int)p};
+  if (n > 2) quicksort_z(sortz, 1, (int)n - 1);
+  // randomise the order within similar blur sizes (src/image.cpp:96-138)
+  GlibcRand rng(seed);
+  for (int64_t i = n - 1; i >= 0; i--) {
+    const SortZ temp = sortz[(size_t)i];
+    const double z1 = temp.z;
+    const double size1 = (z1 - neutral) / z1 * deep;
+    int randomStep = (int)i;
+    bool done = false;
+    int64_t ii;
+    do {
+      ii = i - rng.random(randomStep);
+      if (ii <= 0) ii = 0;
+      const double z2 = sortz[(size_t)ii].z;
+      const double size2 = (z2 - neutral) / z2 * deep;
+      if (size1 == 0 && size2 == 0) done = true;
+      if (size1 * size2 > 0) {
+        const double sizeCompare = size1 > 0 ? size2 / size1 : size1 / size2;
+        done = sizeCompare > 0.7;
+      } else {
+        done = false;
+      }
+      randomStep = (int)(randomStep * 0.7 - 1);
+      if (randomStep <= 0) done = true;
+    } while (!done);
+    sortz[(size_t)i] = sortz[(size_t)ii];
+    sortz[(size_t)ii] = temp;
+  }
+  // splats in order, and the tiles each reaches
+  const int tilesX = (width + kDofTile - 1) / kDofTile, tilesY = (height + kDofTile - 1) / kDofTile;
+  std::vector<DofSplat> splats((size_t)n);
+  std::vector<int64_t> count((size_t)tilesX * tilesY + 1, 0);
+  for (int64_t k = 0; k < n; k++) {
+    const int ii = sortz[(size_t)(n - k - 1)].i;
+    const int x = ii % width, y = ii / width;
+    const double z = zb[(size_t)ii];
+    double blur = fabs(z - neutral) / z * deep;
+    if (blur > 100) blur = 100.0;
+    const int size = (int)blur;
+    splats[(size_t)k] = DofSplat{x, y, size, ii, blur, blur * blur * sqrt(blur) * kPi / 3.0};
+    const int tx0 = std::max(0, x - size) / kDofTile, tx1 = std::min(width - 1, x + size) / kDofTile;
+    const int ty0 = std::max(0, y - size) / kDofTile, ty1 = std::min(height - 1, y + size) / kDofTile;
+    for (int ty = ty0; ty <= ty1; ty++)
+      for (int tx = tx0; tx <= tx1; tx++) count[(size_t)ty * tilesX + tx + 1]++;
+  }
+  for (size_t t = 1; t < count.size(); t++) count[t] += count[t - 1];
+  std::vector<int> list((size_t)count.back());
+  std::vector<int64_t> fill(count.begin(), count.end() - 1);
+  for (int64_t k = 0; k < n; k++) {
+    const DofSplat &sp = splats[(size_t)k];
+    const int tx0 = std::max(0, sp.x - sp.size) / kDofTile, tx1 = std::min(width - 1, sp.x + sp.size) / kDofTile;
+    const int ty0 = std::max(0, sp.y - sp.size) / kDofTile, ty1 = std::min(height - 1, sp.y + sp.size) / kDofTile;
+    for (int ty = ty0; ty <= ty1; ty++)
+      for (int tx = tx0; tx <= tx1; tx++) list[(size_t)fill[(size_t)ty * tilesX + tx]++] = (int)k;
+  }
+  // device buffers: splats, tile starts, lists, original image and alpha
+  const size_t bSplat = sizeof(DofSplat) * (size_t)n, bStart = sizeof(int64_t) * count.size(),
+               bList = sizeof(int) * list.size(), bImg = sizeof(uint16_t) * 3 * (size_t)n,
+               bAlpha = sizeof(uint16_t) * (size_t)n;
+  char *buf = nullptr;
+  e = cudaMallocAsync((void **)&buf, bSplat + bStart + bList + bImg + bAlpha + 64, s);
+  if (e != cudaSuccess) return set_error(MBGB_ERR_CUDA, std::string("DOF buffers: ") + cudaGetErrorString(e));
+  char *pSplat = buf, *pStart = pSplat + bSplat, *pList = pStart + bStart, *pImg = pList + bList;
+  pImg = (char *)(((uintptr_t)pImg + 15) & ~(uintptr_t)15);
+  char *pAlpha = pImg + bImg;
+  e = cudaMemcpyAsync(pSplat, splats.data(), bSplat, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pStart, count.data(), bStart, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && bList) e = cudaMemcpyAsync(pList, list.data(), bList, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pImg, image16, bImg, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pAlpha, layers.alpha, bAlpha, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess)
+    dof_kernel<<<tilesX * tilesY, kDofTile * kDofTile, 0, s>>>(
+        (const DofSplat *)pSplat, (const int64_t *)pStart, (const int *)pList, tilesX, width, height,
+        (const uint16_t *)pImg, (const uint16_t *)pAlpha, image16, layers.alpha);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFreeAsync(buf, s);
+  cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(MBGB_ERR_CUDA, std::string("DOF kernel: ") + cudaGetErrorString(e));
   return MBGB_OK;
 }
 

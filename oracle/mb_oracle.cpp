@@ -24,6 +24,7 @@
 //   render_rows                       MainThread pixel body      src/Render3D.cpp:213-344, 389-589
 //   compile16                         CompileImage / CalculatePixel / CalculateGammaTable src/cimage.cpp:132-214
 //   ssao                              PostRendering_SSAO / ThreadSSAO src/image.cpp:249-478
+//   oracle_dof                        PostRendering_DOF / QuickSortZBuffer src/image.cpp:57-206
 //   level_set                         (not in the reference) Newton refinement of a hit onto
 //                                     DE(P) = thr, the surface the differentiable render's
 //                                     gradients are checked on; off unless oracle_render_exact
@@ -1898,6 +1899,80 @@ void oracle_ssao(int w, int h, const float *zbuf, const unsigned short *opacity,
         image16[3 * p + c] = (unsigned short)v;
       }
     }
+  }
+}
+
+// PostRendering_DOF (src/image.cpp:57-206): QuickSortZBuffer on [1, n-1], the Random()
+// shuffle (srand(seed) first), then the in-place splats far to near.
+void oracle_dof(int w, int h, const float *zbuffer, unsigned short *alpha, unsigned short *image16, double deep,
+                double neutral, unsigned int seed) {
+  const int n = w * h;
+  struct SZ {
+    float z;
+    int i;
+  };
+  std::vector<SZ> d((size_t)n);
+  for (int p = 0; p < n; p++) d[(size_t)p] = SZ{zbuffer[p], p};
+  // Hoare partition around the middle element (src/common_math.h:53-84)
+  std::vector<std::pair<int, int>> st;
+  if (n > 2) st.push_back({1, n - 1});
+  while (!st.empty()) {
+    const int l = st.back().first, p = st.back().second;
+    st.pop_back();
+    int i = l, j = p;
+    const SZ x = d[(size_t)((l + p) / 2)];
+    do {
+      while (d[(size_t)i].z < x.z) i++;
+      while (x.z < d[(size_t)j].z) j--;
+      if (i <= j) std::swap(d[(size_t)i++], d[(size_t)j--]);
+    } while (i <= j);
+    if (l < j) st.push_back({l, j});
+    if (i < p) st.push_back({i, p});
+  }
+  srand(seed);
+  for (int i = n - 1; i >= 0; i--) {
+    const SZ t = d[(size_t)i];
+    const double s1 = ((double)t.z - neutral) / t.z * deep;
+    int rs = i, ii;
+    bool done;
+    do {
+      ii = i - rand() % (rs + 1);
+      if (ii <= 0) ii = 0;
+      const double s2 = ((double)d[(size_t)ii].z - neutral) / d[(size_t)ii].z * deep;
+      done = (s1 == 0 && s2 == 0);
+      if (s1 * s2 > 0) done = (s1 > 0 ? s2 / s1 : s1 / s2) > 0.7;
+      else done = false;
+      rs = (int)(rs * 0.7 - 1);
+      if (rs <= 0) done = true;
+    } while (!done);
+    d[(size_t)i] = d[(size_t)ii];
+    d[(size_t)ii] = t;
+  }
+  const std::vector<unsigned short> img0(image16, image16 + 3 * (size_t)n), a0(alpha, alpha + n);
+  for (int k = 0; k < n; k++) {
+    const int c = d[(size_t)(n - k - 1)].i;
+    const int x = c % w, y = c / w;
+    const double z = zbuffer[c];
+    double blur = fabs(z - neutral) / z * deep;
+    if (blur > 100) blur = 100.0;
+    const int size = (int)blur;
+    const double factor = blur * blur * sqrt(blur) * M_PI / 3.0;
+    for (int yy = y - size; yy <= y + size; yy++)
+      for (int xx = x - size; xx <= x + size; xx++) {
+        if (xx < 0 || xx >= w || yy < 0 || yy >= h) continue;
+        const int dx = xx - x, dy = yy - y;
+        const double r = sqrtf((float)dx * dx + dy * dy);
+        double op = (blur - r) / factor;
+        if (op > 1.0) op = 1.0;
+        if (op < 0.0) op = 0.0;
+        if (op > 0.0) {
+          const double opN = 1.0 - op;
+          const size_t q = (size_t)yy * w + xx;
+          for (int ch = 0; ch < 3; ch++)
+            image16[3 * q + ch] = (unsigned short)(image16[3 * q + ch] * opN + img0[3 * (size_t)c + ch] * op);
+          alpha[q] = (unsigned short)(alpha[q] * opN + a0[(size_t)c] * op);
+        }
+      }
   }
 }
 

@@ -2,6 +2,7 @@
 // src/image.cpp PostRendering_SSAO), compiled in place from the reference tree with
 // oracle/ref_stubs_post. Test infrastructure only: it pins the oracle's restatement of
 // these two steps and produces golden vectors.
+#include <cstdlib>
 #include <cstring>
 
 #include "cimage.hpp"
@@ -68,6 +69,21 @@ void ref_ssao(int w, int h, const float *zbuffer, const unsigned short *opacity,
   img.progressiveFactor = 1;
   PostRendering_SSAO(&img, persp, quality, (enumPerspectiveType)perspective_type, true);
   memcpy(image16, img.GetImage16Ptr(), sizeof(unsigned short) * 3 * n);
+}
+
+// PostRendering_DOF with the reference's own code, rand() seeded with `seed` first.
+void ref_dof(int w, int h, const float *zbuffer, unsigned short *alpha, unsigned short *image16, double deep,
+             double neutral, unsigned int seed) {
+  cImage img(w, h);
+  const size_t n = (size_t)w * h;
+  memcpy(img.GetZBufferPtr(), zbuffer, sizeof(float) * n);
+  memcpy(img.GetAlphaBufPtr(), alpha, sizeof(unsigned short) * n);
+  memcpy(img.GetImage16Ptr(), image16, sizeof(unsigned short) * 3 * n);
+  img.progressiveFactor = 1;
+  srand(seed);
+  PostRendering_DOF(&img, deep, neutral);
+  memcpy(image16, img.GetImage16Ptr(), sizeof(unsigned short) * 3 * n);
+  memcpy(alpha, img.GetAlphaBufPtr(), sizeof(unsigned short) * n);
 }
 
 }  // extern "C"

@@ -490,6 +490,42 @@ def post_goldens(manifest: dict):
         print(case, "ssao changed", np.mean(img16 != compiled))
 
 
+# Depth of field on rendered fixtures: (render fixture, DOF radius, DOF focus, seed).
+DOF_CASES = {
+    "mandelbox_96x54": ("mandelbox_96x54", 20.0, 162.0, 1),
+    "mandelbulb_64x48": ("mandelbulb_64x48", 40.0, 155.0, 7),
+    "ifs_icosahedron": ("ex_ifs_icosahedron", 80.0, 158.0, 12345),
+}
+
+
+def dof_goldens(manifest: dict):
+    """PostRendering_DOF of the reference (libmbref_post.so) on compiled render fixtures."""
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libmbref_post.so"))
+    lib.ref_compile_image.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_dof.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_double, ctypes.c_double, ctypes.c_uint]
+    for case, (render, radius, focus, seed) in DOF_CASES.items():
+        z = np.load(os.path.join(HERE, f"render_{render}.npz"))
+        h, w = z["zbuffer"].shape
+        img_f = np.ascontiguousarray(z["image_float"], np.float32)
+        img16 = np.zeros((h, w, 3), np.uint16)
+        lib.ref_compile_image(w, h, ptr(img_f), 1.0, 1.0, 1.0, 0, ptr(img16))
+        compiled = img16.copy()
+        alpha = np.ascontiguousarray(z["alpha"]).copy()
+        alpha_in = alpha.copy()
+        deep = radius * w / 1000.0
+        neutral = 10.0 ** (focus / 10.0 - 16.0)
+        lib.ref_dof(w, h, ptr(np.ascontiguousarray(z["zbuffer"])), ptr(alpha), ptr(img16), deep, neutral, seed)
+        out = os.path.join(HERE, f"dof_{case}.npz")
+        np.savez_compressed(out, render=np.array(render), radius=radius, focus=focus, seed=seed,
+                            image16_in=compiled, alpha_in=alpha_in, image16_dof=img16, alpha_dof=alpha)
+        manifest[os.path.basename(out)] = {"render": render, "radius": radius, "focus": focus, "seed": seed,
+                                           "changed_by_dof": float(np.mean(img16 != compiled))}
+        print(case, "dof changed", np.mean(img16 != compiled))
+
+
 def formula_goldens(manifest: dict):
     """DE and render fixtures of the run-time formulas from the reference's own code."""
     lib = build_ref()
@@ -544,11 +580,11 @@ def render_cases(lib, cases: dict, manifest: dict):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"], ["effects"]):
+    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"], ["effects"], ["dof"]):
         with open(os.path.join(HERE, "MANIFEST.json")) as f:
             manifest = json.load(f)
         {"post": post_goldens, "formulas": formula_goldens, "all_formulas": all_formula_goldens,
-         "effects": effect_goldens}[sys.argv[1]](manifest)
+         "effects": effect_goldens, "dof": dof_goldens}[sys.argv[1]](manifest)
         with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
             json.dump(manifest, f, indent=1, sort_keys=True)
     else:

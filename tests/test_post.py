@@ -102,3 +102,53 @@ def test_device_compile_and_ssao_match_reference(gpu_ctx, name):
         lib.mbgb_last_error()
     torch.cuda.synchronize()
     _within_one(img16.cpu().numpy().view(np.uint16), z["image16_ssao"], "ssao (atan)")
+
+
+DOFS = sorted(os.path.basename(p)[4:-4] for p in glob.glob(os.path.join(GOLDEN, "dof_*.npz")))
+
+
+def _dof_case(name):
+    z = np.load(os.path.join(GOLDEN, f"dof_{name}.npz"))
+    r = np.load(os.path.join(GOLDEN, f"render_{str(z['render'])}.npz"))
+    sc = mb.scene_from_bytes(r["scene"].tobytes())
+    sc.DOFRadius, sc.DOFFocus = float(z["radius"]), float(z["focus"])
+    return z, r, sc
+
+
+@pytest.mark.parametrize("name", DOFS)
+def test_oracle_dof_matches_reference(name):
+    """PostRendering_DOF (src/image.cpp:57-206): the oracle's restatement of the z-buffer
+    quicksort, the Random() shuffle and the in-place splats equals the reference bit for bit."""
+    z, r, sc = _dof_case(name)
+    lib = oracle_lib.load()
+    h, w = r["zbuffer"].shape
+    lib.oracle_dof.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_double, ctypes.c_double, ctypes.c_uint]
+    img16 = z["image16_in"].copy()
+    alpha = z["alpha_in"].copy()
+    lib.oracle_dof(w, h, _p(np.ascontiguousarray(r["zbuffer"])), _p(alpha), _p(img16), sc.DOFRadius * w / 1000.0,
+                   10.0 ** (sc.DOFFocus / 10.0 - 16.0), int(z["seed"]))
+    np.testing.assert_array_equal(img16, z["image16_dof"])
+    np.testing.assert_array_equal(alpha, z["alpha_dof"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", DOFS)
+def test_device_dof_matches_reference(gpu_ctx, name):
+    """mbgb_dof_device: the splat order from the host, the splats per 16 x 16 tile on the
+    device, each pixel folding its splats in order: equal to the reference bit for bit."""
+    import torch
+    z, r, sc = _dof_case(name)
+    lib = mb.library()
+    h, w = r["zbuffer"].shape
+    img16 = torch.tensor(z["image16_in"].view(np.int16), device="cuda")
+    alpha = torch.tensor(z["alpha_in"].view(np.int16), device="cuda")
+    zb = torch.tensor(np.ascontiguousarray(r["zbuffer"]), device="cuda")
+    torch.cuda.synchronize()
+    layers = mb.mbgb_image(w, h, None, ctypes.c_void_p(zb.data_ptr()), ctypes.c_void_p(alpha.data_ptr()), None,
+                           None, None, None, None)
+    assert lib.mbgb_dof_device(gpu_ctx._h, ctypes.byref(sc), ctypes.byref(layers), img16.data_ptr(),
+                               int(z["seed"])) == 0, lib.mbgb_last_error()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(img16.cpu().numpy().view(np.uint16), z["image16_dof"])
+    np.testing.assert_array_equal(alpha.cpu().numpy().view(np.uint16), z["alpha_dof"])
