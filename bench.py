@@ -231,6 +231,7 @@ def batch_section(ctx, torch, dev, stream, flush, args, world, dist) -> dict:
             "de_evaluations_per_s": world * st.de_calls * steps / t_graph,
             "tuning": {"tile": [tuning.tile_w, tuning.tile_h], "threads_per_cta": tuning.threads_per_cta,
                        "ctas_per_sm": tuning.ctas_per_sm, "refill_min": tuning.refill_min,
+                       "orbit_refill": tuning.orbit_refill,
                        "tuned_ms": tuning.ms, "default_ms": tuning.ms_default, "trials": tuning.trials,
                        "tuning_frame": [big.image_width, big.image_height]},
             "scene": "Mandelbulb power 8, N 250, flight through 8 seeded keyframes (shell r 2-4, looking at "

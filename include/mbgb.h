@@ -236,6 +236,11 @@ typedef struct mbgb_opts {
   int32_t exact_hit;           /* wavefront: 1 = after the binary refinement every hit is moved in FP64
                                 * (Newton steps) onto the level set DE(P) = thr, the surface the
                                 * differentiable render differentiates; 0 = the reference's window */
+  int32_t orbit_refill;        /* wavefront, lean FP32 orbits (Mandelbox, power-8 Mandelbulb), shadow/AO
+                                * rays: a warp runs orbit iterations until this many of its busy lanes
+                                * have ended their orbits, then steps those rays on; 0 = tuned, else 8
+                                * for the Mandelbulb and off for the Mandelbox (short orbits); -1 = off:
+                                * lanes step on only after every orbit of the estimate ended */
 } mbgb_opts;
 
 /* Launch configuration picked by mbgb_autotune. */
@@ -247,6 +252,7 @@ typedef struct mbgb_tuning {
   double ms;                   /* device time of the picked configuration on the tuning frame */
   double ms_default;           /* device time of the default configuration (8 x 4, 128, max, 1) */
   int32_t trials;              /* configurations timed */
+  int32_t orbit_refill;        /* ended orbits before a warp steps its shadow/AO rays on (0 = off) */
 } mbgb_tuning;
 
 /* Render engines (same results within the precision policy's tolerance). */

@@ -579,6 +579,8 @@ struct LaunchCfg {
   int block = 128;                      // threads per CTA
   int ctasPerSm = 0;                    // 0 = the occupancy limit
   int refill = 1;                       // idle lanes before a warp refills
+  int orbitRefill = -1;                 // ended lean orbits before a warp steps them on (0 = off,
+                                        // -1 = by scene: on for the power-8 Mandelbulb's long orbits)
 };
 
 // Scene class an autotuned configuration applies to.
@@ -967,6 +969,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
       cfg.block = it->second.threads_per_cta;
       cfg.ctasPerSm = it->second.ctas_per_sm;
       cfg.refill = it->second.refill_min;
+      cfg.orbitRefill = it->second.orbit_refill;
     }
   }
   if (o.tile_w > 0 && o.tile_h > 0) {
@@ -976,6 +979,12 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
   if (o.threads_per_cta > 0) cfg.block = o.threads_per_cta;
   if (o.ctas_per_sm > 0) cfg.ctasPerSm = o.ctas_per_sm;
   if (o.refill_min > 0) cfg.refill = o.refill_min;
+  if (o.orbit_refill != 0) cfg.orbitRefill = o.orbit_refill < 0 ? 0 : o.orbit_refill;
+  // Orbit-granular refill pays where orbit lengths spread widely (Mandelbulb, N up to
+  // hundreds); the Mandelbox's short orbits (bailout 1024 within ~15 iterations) lose more
+  // to the extra step passes than they gain (measured at 1080p: 11.2 ms per-estimate
+  // refill, 12.5-17.7 ms orbit refill 24-1).
+  if (cfg.orbitRefill < 0) cfg.orbitRefill = fast_mandelbulb(s) ? 8 : 0;
   return cfg;
 }
 
@@ -1067,6 +1076,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.pool_cap = w.poolCap;
   wb.polish_all = o.polish_all;
   wb.refill_min = g.cfg.refill;
+  wb.orbit_refill = g.cfg.orbitRefill;
   wb.exact_hit = o.exact_hit ? 1 : 0;
   wb.npix = g.npix;
   MBGB_CUDA(cudaMemsetAsync(ctl, 0, 64, s));
@@ -1256,6 +1266,7 @@ static mbgb_status check_opts(const mbgb_opts &o) {
   if ((o.tile_w != 0 || o.tile_h != 0) && (o.tile_w <= 0 || o.tile_h <= 0 || o.tile_w * o.tile_h != 32))
     return set_error(MBGB_ERR_BAD_PARAM, "tile_w x tile_h must be 32");
   if (o.refill_min < 0 || o.refill_min > 32) return set_error(MBGB_ERR_BAD_PARAM, "refill_min must be in [0, 32]");
+  if (o.orbit_refill < -1 || o.orbit_refill > 32) return set_error(MBGB_ERR_BAD_PARAM, "orbit_refill must be in [-1, 32]");
   if (o.ctas_per_sm < 0) return set_error(MBGB_ERR_BAD_PARAM, "negative ctas_per_sm");
   if (o.row_begin < 0 || o.row_end < 0) return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
   return MBGB_OK;
@@ -1517,7 +1528,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
         if (!same) continue;
         const LaunchCfg &hc = h.cfg;
         if (hc.tileW != cfg.tileW || hc.tileH != cfg.tileH || hc.block != cfg.block ||
-            hc.ctasPerSm != cfg.ctasPerSm || hc.refill != cfg.refill)
+            hc.ctasPerSm != cfg.ctasPerSm || hc.refill != cfg.refill || hc.orbitRefill != cfg.orbitRefill)
           continue;
         g = &h;
         break;
@@ -1834,6 +1845,7 @@ static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const
     o.threads_per_cta = cfg.block;
     o.ctas_per_sm = cfg.ctasPerSm;
     o.refill_min = cfg.refill;
+    o.orbit_refill = cfg.orbitRefill > 0 ? cfg.orbitRefill : (cfg.orbitRefill == 0 ? -1 : 0);
     double best = 1e30;
     for (int r = 0; r < 3; r++) {
       mbgb_status st = render_frames(c, scene, 1, &img, &o);
@@ -1888,12 +1900,22 @@ static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const
     cand.refill = rf;
     if ((st = consider(cand)) != MBGB_OK) return st;
   }
+  if (fast_mandelbox(*scene) || fast_mandelbulb(*scene)) {
+    const LaunchCfg chosen = cur;
+    for (int orf : {0, 8, 16}) {
+      if (orf == (fast_mandelbulb(*scene) ? 8 : 0)) continue;   // the default, timed already
+      LaunchCfg cand = chosen;
+      cand.orbitRefill = orf;
+      if ((st = consider(cand)) != MBGB_OK) return st;
+    }
+  }
   mbgb_tuning t{};
   t.tile_w = cur.tileW;
   t.tile_h = cur.tileH;
   t.threads_per_cta = cur.block;
   t.ctas_per_sm = cur.ctasPerSm;
   t.refill_min = cur.refill;
+  t.orbit_refill = cur.orbitRefill < 0 ? (fast_mandelbulb(*scene) ? 8 : 0) : cur.orbitRefill;
   t.ms = curMs;
   t.ms_default = defMs;
   t.trials = trials;

@@ -37,39 +37,64 @@ __device__ __forceinline__ float rcp_approx(const float x) {
   return r;
 }
 
+// The lean FP32 orbits below spell out every multiply-add (fmaf, __fmul_rn) so that the
+// compiler has no contraction left to choose: the one-call orbits and their resumable
+// versions then round identically in every kernel that inlines them.
+__device__ __forceinline__ float norm2_rn(const float x, const float y, const float z) {
+  return fmaf(z, z, fmaf(y, y, __fmul_rn(x, x)));
+}
+
+// Constants of the lean Mandelbox iteration.
+struct LeanBoxK {
+  float fl, sa, sb, km1;
+  __device__ __forceinline__ explicit LeanBoxK(const FractalT<float> &f) {
+    fl = f.mbFoldLimit;
+    const float mR2 = f.mbMinR * f.mbMinR;
+    const float fR2 = f.mbFixedR * f.mbFixedR;
+    const float k1 = fR2 / mR2;   // >= 1 in the lean class (min radius <= fixed radius)
+    km1 = k1 - 1.0f;
+    sa = km1 > 0.0f ? fR2 / km1 : 0.0f;
+    sb = km1 > 0.0f ? 1.0f / km1 : 0.0f;
+  }
+};
+
+// One Mandelbox iteration (scale s, constant c); returns the new squared radius.
+// Box fold: clamp(x) * 2 - x, identical to fv - x / -fv - x (fold value = 2 x fold limit;
+// the product by 2 is exact, so the FMA rounds once, as the two-step form does). Sphere
+// fold: fR2/mR2 inside mR2, fR2/r2 between mR2 and fR2, 1 outside; the clamp of fR2/r2 to
+// [1, k1], written 1 + (k1 - 1) sat((fR2/r2 - 1) / (k1 - 1)) so that the clamp rides on
+// the FMA pipe's saturation instead of two min/max instructions, with the approximate
+// reciprocal feeding one saturating FMA (measured +11 % orbit rate).
+__device__ __forceinline__ float box_iteration(const LeanBoxK &k, const float s, float &x, float &y, float &z,
+                                               float &dr, const float cx, const float cy, const float cz) {
+  x = fmaf(fminf(fmaxf(x, -k.fl), k.fl), 2.0f, -x);
+  y = fmaf(fminf(fmaxf(y, -k.fl), k.fl), 2.0f, -y);
+  z = fmaf(fminf(fmaxf(z, -k.fl), k.fl), 2.0f, -z);
+  const float r2 = norm2_rn(x, y, z);
+  const float kf = fmaf(__saturatef(fmaf(k.sa, rcp_approx(r2), -k.sb)), k.km1, 1.0f);
+  const float ks = __fmul_rn(kf, s);
+  x = fmaf(x, ks, cx);
+  y = fmaf(y, ks, cy);
+  z = fmaf(z, ks, cz);
+  dr = fmaf(dr, fabsf(ks), 1.0f);   // |k s| = k |s| (k > 0), one instruction
+  return norm2_rn(x, y, z);
+}
+
 // Mandelbox orbit (formula 8, normal mode) for the common case: no rotation, no offset,
 // no pre-folds, julia off, fold value = 2 x fold limit. Squared radius throughout: the
 // bailout r > 1024 becomes r^2 > 1024^2 and the sphere fold tests r^2 directly, so the
-// loop has no square root; the fold is clamp(x)*2 - x, identical to fv - x / -fv - x.
+// loop has no square root.
 __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const float px, const float py,
                                                 const float pz, const int N, int &Lout, Counters &cnt,
                                                 const float s) {
-  const float fl = f.mbFoldLimit;
-  const float mR2 = f.mbMinR * f.mbMinR;
-  const float fR2 = f.mbFixedR * f.mbFixedR;
-  const float k1 = fR2 / mR2;   // >= 1 in the lean class (min radius <= fixed radius)
-  const float km1 = k1 - 1.0f;
-  const float sa = km1 > 0.0f ? fR2 / km1 : 0.0f, sb = km1 > 0.0f ? 1.0f / km1 : 0.0f;
-  const float cx = px * f.constantFactor, cy = py * f.constantFactor, cz = pz * f.constantFactor;
+  const LeanBoxK k(f);
+  const float cx = __fmul_rn(px, f.constantFactor), cy = __fmul_rn(py, f.constantFactor),
+              cz = __fmul_rn(pz, f.constantFactor);
   float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
   int L;
 #pragma unroll 5
   for (L = 0; L < N; L++) {
-    x = fminf(fmaxf(x, -fl), fl) * 2.0f - x;
-    y = fminf(fmaxf(y, -fl), fl) * 2.0f - y;
-    z = fminf(fmaxf(z, -fl), fl) * 2.0f - z;
-    float r2 = x * x + y * y + z * z;
-    // sphere fold: fR2/mR2 inside mR2, fR2/r2 between mR2 and fR2, 1 outside; the clamp of
-    // fR2/r2 to [1, k1], written 1 + (k1 - 1) sat((fR2/r2 - 1) / (k1 - 1)) so that the
-    // clamp rides on the FMA pipe's saturation instead of two min/max instructions, with
-    // the approximate reciprocal feeding one saturating FMA (measured +11 % orbit rate)
-    const float k = fmaf(__saturatef(fmaf(sa, rcp_approx(r2), -sb)), km1, 1.0f);
-    const float ks = k * s;
-    x = fmaf(x, ks, cx);
-    y = fmaf(y, ks, cy);
-    z = fmaf(z, ks, cz);
-    dr = fmaf(dr, fabsf(ks), 1.0f);   // |k s| = k |s| (k > 0), one instruction
-    r2 = x * x + y * y + z * z;
+    const float r2 = box_iteration(k, s, x, y, z, dr, cx, cy, cz);
     if (r2 > 1048576.0f) {
       dist = sqrtf(r2) / fabsf(dr);
       break;
@@ -82,12 +107,37 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
   return dist;
 }
 
-// Mandelbulb power 8 (trig_optim, src/fractal.cpp:211-225) without transcendentals:
-// theta = asin(z/r) in [-pi/2, pi/2] has cos = rho/r >= 0 and sin = z/r; phi = atan2(y, x)
-// has cos = x/rho, sin = y/rho (phi = 0 when rho = 0, as atan2(0, 0)). Three angle
-// doublings (c, s) -> (c^2 - s^2, 2cs) give 8*theta and 8*phi; r^8 and r^7 come from r^2.
-// MODE 0 returns the distance estimate 0.5*r*ln(r)/dr at the bailout r > 100;
-// MODE 1 returns the colouring value (min |z| until |z| > 1e15, times 5000).
+// One Mandelbulb power-8 iteration (trig_optim, src/fractal.cpp:211-225) without
+// transcendentals: theta = asin(z/r) in [-pi/2, pi/2] has cos = rho/r >= 0 and sin = z/r;
+// phi = atan2(y, x) has cos = x/rho, sin = y/rho (phi = 0 when rho = 0, as atan2(0, 0)).
+// Three angle doublings (c, s) -> (c^2 - s^2, 2cs) give 8*theta and 8*phi; r^8 and r^7 come
+// from r^2. Returns the new squared radius.
+__device__ __forceinline__ float bulb8_iteration(float &x, float &y, float &z, const float r2, float &r_dz,
+                                                 const float cx, const float cy, const float cz) {
+  const float rho2 = fmaf(y, y, __fmul_rn(x, x));
+  const float inv_r = rsqrtf(r2);
+  const bool axis = rho2 == 0.0f;
+  const float inv_rho = axis ? 0.0f : rsqrtf(rho2);
+  float ct = __fmul_rn(__fmul_rn(rho2, inv_rho), inv_r), st = __fmul_rn(z, inv_r);
+  float cp = axis ? 1.0f : __fmul_rn(x, inv_rho), sp = axis ? 0.0f : __fmul_rn(y, inv_rho);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const float ct2 = fmaf(ct, ct, -__fmul_rn(st, st)), st2 = __fmul_rn(__fmul_rn(2.0f, st), ct);
+    const float cp2 = fmaf(cp, cp, -__fmul_rn(sp, sp)), sp2 = __fmul_rn(__fmul_rn(2.0f, sp), cp);
+    ct = ct2; st = st2; cp = cp2; sp = sp2;
+  }
+  const float r4 = __fmul_rn(r2, r2);
+  const float r8 = __fmul_rn(r4, r4);
+  r_dz = fmaf(__fmul_rn(__fmul_rn(8.0f, r8), inv_r), r_dz, 1.0f);   // p * r^(p-1) * r_dz + 1
+  const float t = __fmul_rn(ct, r8);
+  x = fmaf(t, cp, cx);
+  y = fmaf(t, sp, cy);
+  z = fmaf(st, r8, cz);
+  return norm2_rn(x, y, z);
+}
+
+// Mandelbulb power 8 orbit. MODE 0 returns the distance estimate 0.5*r*ln(r)/dr at the
+// bailout r > 100; MODE 1 returns the colouring value (min |z| until |z| > 1e15, times 5000).
 template <int MODE>
 __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, const float px, const float py,
                                                   const float pz, const int N, int &Lout, Counters &cnt) {
@@ -95,37 +145,18 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
   if (f.juliaMode) {
     cx = f.julia[0]; cy = f.julia[1]; cz = f.julia[2];
   } else {
-    cx = px * f.constantFactor; cy = py * f.constantFactor; cz = pz * f.constantFactor;
+    cx = __fmul_rn(px, f.constantFactor); cy = __fmul_rn(py, f.constantFactor); cz = __fmul_rn(pz, f.constantFactor);
   }
   float x = px, y = py, z = pz, r_dz = 1.0f, dist = 0.0f;
-  float r2 = x * x + y * y + z * z;
+  float r2 = norm2_rn(x, y, z);
   float minr2 = __int_as_float(0x7f800000);
   int L;
   for (L = 0; L < N; L++) {
-    const float rho2 = x * x + y * y;
-    const float inv_r = rsqrtf(r2);
-    const bool axis = rho2 == 0.0f;
-    const float inv_rho = axis ? 0.0f : rsqrtf(rho2);
-    float ct = rho2 * inv_rho * inv_r, st = z * inv_r;
-    float cp = axis ? 1.0f : x * inv_rho, sp = axis ? 0.0f : y * inv_rho;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const float ct2 = ct * ct - st * st, st2 = 2.0f * st * ct;
-      const float cp2 = cp * cp - sp * sp, sp2 = 2.0f * sp * cp;
-      ct = ct2; st = st2; cp = cp2; sp = sp2;
-    }
-    const float r4 = r2 * r2;
-    const float r8 = r4 * r4;
-    r_dz = fmaf(8.0f * r8 * inv_r, r_dz, 1.0f);   // p * r^(p-1) * r_dz + 1
-    const float t = ct * r8;
-    x = fmaf(t, cp, cx);
-    y = fmaf(t, sp, cy);
-    z = fmaf(st, r8, cz);
-    r2 = x * x + y * y + z * z;
+    r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
     if (MODE == 0) {
       if (r2 > 1.0e4f) {
         const float r = sqrtf(r2);
-        dist = 0.5f * r * __logf(r) / r_dz;
+        dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
         break;
       }
     } else {
@@ -143,6 +174,109 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
   // colouring: min |z| after a bailout, else the last |z|
   return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
 }
+
+// Resumable lean orbits (distance mode) for the orbit-granular lane refill of the shadow/AO
+// stage: the state of mandelbox_fast / mandelbulb8_fast<0> between batches of kUnroll
+// iterations, through the same iteration functions. start() begins the orbit of a point;
+// advance() runs up to kUnroll iterations and returns true once the orbit has ended
+// (bailout or N iterations), with its distance in `dist` and its end iteration in L, the
+// values the one-call versions return.
+template <int FORMULA>
+struct LeanOrbit;
+
+template <>
+struct LeanOrbit<8> {
+  static constexpr int kUnroll = 5;
+  LeanBoxK k;
+  float cf;
+  int N;
+  float x, y, z, dr, cx, cy, cz, s;
+  int L;
+  __device__ __forceinline__ explicit LeanOrbit(const FractalT<float> &f) : k(f) {
+    cf = f.constantFactor;
+    N = f.N;
+    x = y = z = cx = cy = cz = s = 0.0f;
+    dr = 1.0f;
+    L = 0;
+  }
+  // scale: the frame's Mandelbox scale
+  __device__ __forceinline__ void start(const V3<float> p, const float scale) {
+    x = p.x; y = p.y; z = p.z;
+    cx = __fmul_rn(p.x, cf); cy = __fmul_rn(p.y, cf); cz = __fmul_rn(p.z, cf);
+    dr = 1.0f;
+    s = scale;
+    L = 0;
+  }
+  __device__ __forceinline__ bool advance(float &dist) {
+    if (L >= N) {
+      dist = 0.0f;
+      return true;
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const float r2 = box_iteration(k, s, x, y, z, dr, cx, cy, cz);
+      if (r2 > 1048576.0f) {
+        dist = sqrtf(r2) / fabsf(dr);
+        return true;
+      }
+      if (++L == N) {
+        dist = 0.0f;
+        return true;
+      }
+    }
+    return false;
+  }
+};
+
+template <>
+struct LeanOrbit<2> {
+  static constexpr int kUnroll = 2;
+  float jx, jy, jz, cf;
+  int N;
+  bool julia;
+  float x, y, z, r2, r_dz, cx, cy, cz;
+  int L;
+  __device__ __forceinline__ explicit LeanOrbit(const FractalT<float> &f) {
+    julia = f.juliaMode;
+    jx = f.julia[0]; jy = f.julia[1]; jz = f.julia[2];
+    cf = f.constantFactor;
+    N = f.N;
+    x = y = z = r2 = cx = cy = cz = 0.0f;
+    r_dz = 1.0f;
+    L = 0;
+  }
+  __device__ __forceinline__ void start(const V3<float> p, const float) {
+    if (julia) {
+      cx = jx; cy = jy; cz = jz;
+    } else {
+      cx = __fmul_rn(p.x, cf); cy = __fmul_rn(p.y, cf); cz = __fmul_rn(p.z, cf);
+    }
+    x = p.x; y = p.y; z = p.z;
+    r_dz = 1.0f;
+    r2 = norm2_rn(x, y, z);
+    L = 0;
+  }
+  __device__ __forceinline__ bool advance(float &dist) {
+    if (L >= N) {
+      dist = 0.0f;
+      return true;
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
+      if (r2 > 1.0e4f) {
+        const float r = sqrtf(r2);
+        dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
+        return true;
+      }
+      if (++L == N) {
+        dist = 0.0f;
+        return true;
+      }
+    }
+    return false;
+  }
+};
 
 // FP64 versions of the lean orbits for the FP32 policy's FP64 polish, which needs FP64
 // accuracy but not the reference's operation order: the squared radius throughout (no
@@ -844,22 +978,206 @@ __device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const FrameC
 // Jobs [0, nShadow): one shadow ray per hit; then aoCount x hits AO rays,
 // direction-major so a warp's initial 32 rays share a direction.
 // ---------------------------------------------------------------------------
+
+// a + b * c with the product and the sum rounded separately (the reference's order), in
+// both precisions and whatever the unit's contraction setting.
+__device__ __forceinline__ float add_mul_rn(const float a, const float b, const float c) {
+  return __fadd_rn(a, __fmul_rn(b, c));
+}
+__device__ __forceinline__ double add_mul_rn(const double a, const double b, const double c) {
+  return __dadd_rn(a, __dmul_rn(b, c));
+}
+template <typename T>
+__device__ __forceinline__ V3<T> ray_at(const V3<T> &o, const V3<T> &d, const T r) {
+  return V3<T>{add_mul_rn(o.x, d.x, r), add_mul_rn(o.y, d.y, r), add_mul_rn(o.z, d.z, r)};
+}
+
+// State of one shadow (kind 0) or AO (kind 1) ray.
+template <typename T>
+struct SecondaryRay {
+  int kind;
+  unsigned int j;   // AO direction
+  int64_t gp;       // pixel of the batch
+  V3<T> point, dir;
+  T r, end, sh, thr, detail, maxSoft, stepMul, fpar;
+  int guard;
+};
+
+// Starts job `job`: MainShadow's (src/shaders.cpp:480-570) or AmbientOcclusion's
+// (src/shaders.cpp:572-640) loop set-up for one ray. Returns false when the loop body
+// never runs (the result is written at once).
+template <typename T>
+__device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveBufs<T> &wb,
+                                                const FrameCam<T> *__restrict__ cams, const int ncams,
+                                                const unsigned int nh, const unsigned int nShadow,
+                                                const unsigned int job, SecondaryRay<T> &s) {
+  s.kind = job < nShadow ? 0 : 1;
+  if (s.kind == 0) {
+    s.gp = (int64_t)wb.hit_list[job];
+  } else {
+    const unsigned int q = job - nShadow;
+    s.j = q / nh;
+    s.gp = (int64_t)wb.hit_list[q % nh];
+  }
+  const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, s.gp)];
+  const HitInfo<T> h = hit_info(p, c, wb, s.gp);
+  s.point = h.point;
+  s.fpar = c.fparam;
+  // MainShadow and AmbientOcclusion compare with the threshold stored in a float
+  s.thr = (T)(float)h.thr;
+  s.sh = T(1);
+  s.maxSoft = T(0);
+  s.guard = 0;
+  const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
+  const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
+  if (s.kind == 0) {
+    s.dir = {c.lightVect[0], c.lightVect[1], c.lightVect[2]};
+    s.end = factor;
+    s.r = shadowStart;
+    s.detail = s.thr;
+    s.stepMul = p.DE_factor;
+  } else {
+    s.dir = {__ldg(&p.aoVec[3 * s.j + 0]), __ldg(&p.aoVec[3 * s.j + 1]), __ldg(&p.aoVec[3 * s.j + 2])};
+    s.end = h.delta / c.resolution;
+    s.r = h.delta;
+    // detailSize after MainShadow: the float threshold if its loop ran at least once
+    s.detail = (p.shadow && shadowStart < factor) ? s.thr : h.thr;
+    s.stepMul = T(2);
+  }
+  if (!(s.r < s.end)) {
+    if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? T(1) : s.sh;
+    else wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    return false;
+  }
+  return true;
+}
+
+// One loop iteration of the ray after its distance estimate `dist` (maxIter `mi`) at
+// point + dir * r. Returns true when the ray has ended (its result is written).
+template <typename T>
+__device__ __forceinline__ bool secondary_step(const ParamsT<T> &p, const WaveBufs<T> &wb, SecondaryRay<T> &s,
+                                               const T dist, const bool mi) {
+  bool done = false;
+  if (s.kind == 0) {
+    if (p.softShadow) {
+      T angle = (dist - s.thr) / s.r;
+      if (angle < T(0)) angle = T(0);
+      if (dist < s.thr) angle = T(0);
+      T soft = (T(1) - angle / p.softRange);
+      if (p.penetrating) soft *= (s.end - s.r) / s.end;
+      if (soft < T(0)) soft = T(0);
+      if (soft > s.maxSoft) s.maxSoft = soft;
+    }
+    if (dist < s.thr || s.sh < T(0)) {
+      s.sh -= (s.end - s.r) / s.end;
+      if (!p.penetrating) s.sh = T(0);
+      if (s.sh < T(0)) s.sh = T(0);
+      done = true;
+    }
+  } else {
+    if (dist < s.thr || mi || s.sh < T(0)) {
+      s.sh -= (s.end - s.r) / s.end;
+      if (s.sh < T(0)) s.sh = T(0);
+      done = true;
+    }
+  }
+  if (!done) {
+    s.r = add_mul_rn(s.r, dist, s.stepMul);
+    if (!(s.r < s.end) || ++s.guard >= kMaxSecondarySteps) done = true;
+  }
+  if (done) {
+    if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? (T(1) - s.maxSoft) : s.sh;
+    else wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+  }
+  return done;
+}
+
+// Lean FP32 orbits: lanes are refilled per orbit rather than per distance estimate. The
+// warp runs orbit iterations in batches of LeanOrbit::kUnroll until wb.orbit_refill of its
+// busy lanes have ended their orbits (or all have); then those lanes take their ray's next
+// step (or a new ray) and start the next orbit, while the others keep their orbit state.
+// Every distance is the one mandelbox_fast / mandelbulb8_fast returns at the same point.
+template <int FORMULA>
+__device__ __forceinline__ void secondary_lean(const ParamsT<float> &p, const FrameIO &io, const WaveBufs<float> &wb,
+                                               const FrameCam<float> *__restrict__ cams, const int ncams) {
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  const unsigned int nShadow = p.shadow ? nh : 0u;
+  const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
+  const unsigned int njobs = nShadow + nAO;
+  const unsigned int threshold = (unsigned int)wb.orbit_refill;
+  const int minN = p.f.minN;
+  Counters cnt{0, 0, 0, 0};
+  LeanOrbit<FORMULA> orb(p.f);
+  SecondaryRay<float> s{};
+  bool active = false, exhausted = false, orbiting = false;
+  float odist = 0.0f;
+  for (;;) {
+    // lanes whose orbit ended: the distance estimate's clamps, then the ray's step
+    if (active && !orbiting) {
+      cnt.orbit += (unsigned long long)(orb.L + 1);
+      cnt.calls += 1;
+      float d = odist;
+      if (d < 0.0f) d = 0.0f;
+      if (orb.L < minN && d < s.detail) d = s.detail;
+      if (secondary_step(p, wb, s, d, orb.L == orb.N)) {
+        active = false;
+      } else {
+        orb.start(ray_at(s.point, s.dir, s.r), s.fpar);
+        orbiting = true;
+      }
+    }
+    // idle lanes take new rays until every lane is busy or the jobs are spent
+    for (;;) {
+      const bool need = !active && !exhausted;
+      if (!__any_sync(0xffffffffu, need)) break;
+      if (io.budget_ns && (threadIdx.x & 31) == 0 && deadline_passed(io)) atomicExch(io.error_flag, 1);
+      const bool stop = *(volatile int *)io.error_flag != 0;
+      const unsigned int job = claim_jobs(wb.ctl + 2, need);
+      if (need) {
+        if (stop || job >= njobs) {
+          exhausted = true;
+        } else if (secondary_begin(p, wb, cams, ncams, nh, nShadow, job, s)) {
+          active = true;
+          orb.start(ray_at(s.point, s.dir, s.r), s.fpar);
+          orbiting = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    // orbit iterations until enough busy lanes have ended theirs
+    for (;;) {
+      if (orbiting && orb.advance(odist)) orbiting = false;
+      const unsigned int busy = __ballot_sync(0xffffffffu, active);
+      const unsigned int ended = __ballot_sync(0xffffffffu, active && !orbiting);
+      if ((unsigned int)__popc(ended) >= threshold || ended == busy) break;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+  }
+}
+
 template <typename T, int FORMULA, bool FAST>
 __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                         const FrameCam<T> *__restrict__ cams, const int ncams) {
+  if constexpr (FAST && sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
+    if (wb.orbit_refill > 0) {
+      secondary_lean<FORMULA>(p, io, wb, cams, ncams);
+      return;
+    }
+  }
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
   const unsigned int nShadow = p.shadow ? nh : 0u;
   const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
   const unsigned int njobs = nShadow + nAO;
   Counters cnt{0, 0, 0, 0};
   bool active = false, exhausted = false;
-  int kind = 0;
-  unsigned int j = 0;
-  int64_t gp = 0;
-  V3<T> point{T(0), T(0), T(0)}, dir{T(0), T(0), T(0)};
-  T r = T(0), end = T(0), dist = T(0), sh = T(1), thr = T(0), detail = T(0), maxSoft = T(0), stepMul = T(0);
-  T fpar = T(0);
-  int guard = 0;
+  SecondaryRay<T> s{};
   for (;;) {
     // a warp claims new jobs once refill_min of its lanes are idle, or when none is busy
     const bool need = !active && !exhausted;
@@ -869,51 +1187,8 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       const bool stop = *(volatile int *)io.error_flag != 0;
       const unsigned int job = claim_jobs(wb.ctl + 2, need);
       if (need) {
-        if (stop || job >= njobs) {
-          exhausted = true;
-        } else {
-          kind = job < nShadow ? 0 : 1;
-          if (kind == 0) {
-            gp = (int64_t)wb.hit_list[job];
-          } else {
-            const unsigned int q = job - nShadow;
-            j = q / nh;
-            gp = (int64_t)wb.hit_list[q % nh];
-          }
-          const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
-          const HitInfo<T> h = hit_info(p, c, wb, gp);
-          point = h.point;
-          fpar = c.fparam;
-          // MainShadow and AmbientOcclusion compare with the threshold stored in a float
-          thr = (T)(float)h.thr;
-          sh = T(1);
-          maxSoft = T(0);
-          guard = 0;
-          const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
-          const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
-          if (kind == 0) {
-            dir = {c.lightVect[0], c.lightVect[1], c.lightVect[2]};
-            end = factor;
-            r = shadowStart;
-            dist = h.thr;
-            detail = thr;
-            stepMul = p.DE_factor;
-          } else {
-            dir = {__ldg(&p.aoVec[3 * j + 0]), __ldg(&p.aoVec[3 * j + 1]), __ldg(&p.aoVec[3 * j + 2])};
-            end = h.delta / c.resolution;
-            r = h.delta;
-            dist = wb.dist[gp];
-            // detailSize after MainShadow: the float threshold if its loop ran at least once
-            detail = (p.shadow && shadowStart < factor) ? thr : h.thr;
-            stepMul = T(2);
-          }
-          active = true;
-          if (!(r < end)) {  // loop body never runs
-            if (kind == 0) wb.shadow[gp] = p.softShadow ? T(1) : sh;
-            else wb.ao[(int64_t)j * wb.npix + gp] = sh;
-            active = false;
-          }
-        }
+        if (stop || job >= njobs) exhausted = true;
+        else active = secondary_begin(p, wb, cams, ncams, nh, nShadow, job, s);
       }
     }
     if (!__any_sync(0xffffffffu, active)) {
@@ -921,43 +1196,11 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       continue;
     }
     if (active) {
-      const V3<T> point2 = point + dir * r;
+      const V3<T> point2 = ray_at(s.point, s.dir, s.r);
       int L;
       bool mi;
-      dist = wave_distance<T, FORMULA, FAST>(p.f, point2, detail, p.f.N, p.f.minN, false, L, mi, cnt, fpar);
-      bool done = false;
-      if (kind == 0) {
-        if (p.softShadow) {
-          T angle = (dist - thr) / r;
-          if (angle < T(0)) angle = T(0);
-          if (dist < thr) angle = T(0);
-          T soft = (T(1) - angle / p.softRange);
-          if (p.penetrating) soft *= (end - r) / end;
-          if (soft < T(0)) soft = T(0);
-          if (soft > maxSoft) maxSoft = soft;
-        }
-        if (dist < thr || sh < T(0)) {
-          sh -= (end - r) / end;
-          if (!p.penetrating) sh = T(0);
-          if (sh < T(0)) sh = T(0);
-          done = true;
-        }
-      } else {
-        if (dist < thr || mi || sh < T(0)) {
-          sh -= (end - r) / end;
-          if (sh < T(0)) sh = T(0);
-          done = true;
-        }
-      }
-      if (!done) {
-        r += dist * stepMul;
-        if (!(r < end) || ++guard >= kMaxSecondarySteps) done = true;
-      }
-      if (done) {
-        if (kind == 0) wb.shadow[gp] = p.softShadow ? (T(1) - maxSoft) : sh;
-        else wb.ao[(int64_t)j * wb.npix + gp] = sh;
-        active = false;
-      }
+      const T dist = wave_distance<T, FORMULA, FAST>(p.f, point2, s.detail, p.f.N, p.f.minN, false, L, mi, cnt, s.fpar);
+      if (secondary_step(p, wb, s, dist, mi)) active = false;
     }
   }
   for (int off = 16; off > 0; off >>= 1) {

@@ -38,6 +38,8 @@ struct WaveBufs {
   uint32_t pool_cap;                     // chunks
   int polish_all;                        // 1: every hit takes the FP64 polish
   int refill_min;                        // idle lanes of a warp before it claims new rays
+  int orbit_refill;                      // lean FP32 orbits, shadow/AO stage: ended orbits of a warp
+                                         // before those lanes step on; 0 = refill per distance estimate
   int exact_hit;                         // 1: hits are refined in FP64 to the level set DE = thr
   int64_t npix;
 };

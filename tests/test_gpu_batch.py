@@ -4,7 +4,7 @@ A batch renders frames of MainRender's keyframe / flight loops (src/Render3D.cpp
 in one launch sequence; every frame must come out exactly as the same frame rendered
 alone, because each pixel's arithmetic does not depend on which warp or launch renders
 it. The same holds for the tuned launch configurations (tile shape, threads per CTA,
-CTAs per SM, refill threshold) and for graph replays: those tests compare bit for bit.
+CTAs per SM, refill thresholds) and for graph replays: those tests compare bit for bit.
 The flight frames are also held against the FP64 oracle with the FP32 policy's bar
 (hit/miss mismatch <= 0.1 %, float-image PSNR >= 45 dB).
 """
@@ -68,6 +68,7 @@ def test_autotune_and_tuned_render(gpu_ctx, flight_small):
     assert t.tile_w * t.tile_h == 32
     assert t.threads_per_cta in (64, 128)
     assert t.refill_min in (1, 4, 8, 16)
+    assert t.orbit_refill in (0, 8, 16)
     assert t.trials >= 8 and 0 < t.ms <= t.ms_default * 1.0001
     ref = gpu_ctx.render_batch(flight_small[:8])
     tuned = gpu_ctx.render_batch(flight_small[:8], autotune=True)
@@ -82,6 +83,22 @@ def test_launch_shapes_do_not_change_pixels(gpu_ctx, flight_small, tile, refill,
     got = gpu_ctx.render_batch(frames, tile=tile, refill_min=refill, threads_per_cta=threads)
     for i in range(len(frames)):
         _same(ref[i], got[i], f"frame {i}")
+
+
+@pytest.mark.parametrize("orbit_refill", [-1, 1, 4, 16, 32])
+def test_orbit_refill_does_not_change_pixels(gpu_ctx, flight_small, orbit_refill):
+    # The shadow/AO stage's orbit-granular lane refill (lean Mandelbox and power-8
+    # Mandelbulb orbits) reorders work between lanes only: every layer and the orbit and
+    # distance-estimate counts of the stage match the per-estimate refill (-1) bit for bit.
+    box = W.workload("mandelbox_1080p", 320, 180)
+    for i, f in enumerate([box] + flight_small[8:10]):
+        ref = gpu_ctx.render(f, orbit_refill=-1, profile_stages=True)
+        ref_st = gpu_ctx.stats()
+        got = gpu_ctx.render(f, orbit_refill=orbit_refill, profile_stages=True)
+        st = gpu_ctx.stats()
+        _same(ref, got, f"frame {i}, orbit_refill {orbit_refill}")
+        assert st.stage_orbit[2] == ref_st.stage_orbit[2] and st.stage_de[2] == ref_st.stage_de[2]
+        assert st.stage_de[2] > 0
 
 
 def test_mixed_batch_groups(gpu_ctx):
@@ -123,6 +140,10 @@ def test_batch_rejects_bad_arguments(gpu_ctx, flight_small):
         gpu_ctx.render_batch(flight_small[:2], tile=(8, 8))
     with pytest.raises(mb.MbgbError):
         gpu_ctx.render_batch(flight_small[:2], refill_min=33)
+    with pytest.raises(mb.MbgbError):
+        gpu_ctx.render_batch(flight_small[:2], orbit_refill=33)
+    with pytest.raises(mb.MbgbError):
+        gpu_ctx.render_batch(flight_small[:2], orbit_refill=-2)
     # one AO direction table per call: frames tracing AO rays must share its quality
     q2 = W.workload("mandelbox_1080p", 64, 36)
     q3 = W.workload("mandelbox_1080p", 64, 36, ambient_occlusion_quality=3)
