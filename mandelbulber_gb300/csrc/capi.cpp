@@ -276,6 +276,14 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   f.mbFoldValue = (T)s.mboxFoldingValue;
   f.mbMinR = (T)s.mboxFoldingSphericalMin;
   f.mbFixedR = (T)s.mboxFoldingSphericalFixed;
+  {
+    // the same IEEE operations as a device-side derivation (no contraction in host code)
+    const T mR2 = f.mbMinR * f.mbMinR, fR2 = f.mbFixedR * f.mbFixedR;
+    const T km1 = fR2 / mR2 - T(1);
+    f.leanKm1 = km1;
+    f.leanSa = km1 > T(0) ? fR2 / km1 : T(0);
+    f.leanSb = km1 > T(0) ? T(1) / km1 : T(0);
+  }
   f.mbColX = (T)s.mboxColorFactorX;
   f.mbColY = (T)s.mboxColorFactorY;
   f.mbColZ = (T)s.mboxColorFactorZ;
@@ -813,6 +821,7 @@ static void clear_unused(FractalT<T> &f) {
     f.mbRotEnabled = f.mbMainRotZero = 0;
     memset(f.mbRotZero, 0, sizeof(f.mbRotZero));
     f.mbScale = f.mbFoldLimit = f.mbFoldValue = f.mbMinR = f.mbFixedR = T(0);
+    f.leanKm1 = f.leanSa = f.leanSb = T(0);
     f.mbColX = f.mbColY = f.mbColZ = f.mbColR = f.mbColSp1 = f.mbColSp2 = T(0);
     for (int k = 0; k < 3; k++) f.mbOffset[k] = T(0);
     memset(f.mbMainRot, 0, sizeof(f.mbMainRot));

@@ -47,6 +47,9 @@ struct FractalT {
   T julia[3];
   T foldingLimit, foldingValue, sphFixed, sphMin;
   T mbScale, mbFoldLimit, mbFoldValue, mbMinR, mbFixedR;
+  // lean Mandelbox sphere fold, derived on the host in T's arithmetic: k1 - 1 = fR^2/mR^2 - 1,
+  // fR^2/(k1 - 1) and 1/(k1 - 1) (0 when k1 <= 1)
+  T leanKm1, leanSa, leanSb;
   T mbOffset[3];
   T mbColX, mbColY, mbColZ, mbColR, mbColSp1, mbColSp2;
   T mbMainRot[9];

@@ -44,18 +44,20 @@ __device__ __forceinline__ float norm2_rn(const float x, const float y, const fl
   return fmaf(z, z, fmaf(y, y, __fmul_rn(x, x)));
 }
 
+// Distance estimate r / |dr| at the bailout from the squared radius, with the approximate
+// square root and quotient (MUFU rsqrt/rcp; a few ulp, far inside the FP32 policy's
+// tolerance): once per orbit, where the correctly rounded forms cost more than an iteration.
+__device__ __forceinline__ float box_bailout_dist(const float r2, const float dr) {
+  return __fdividef(__fmul_rn(r2, rsqrtf(r2)), fabsf(dr));
+}
+
 // Constants of the lean Mandelbox iteration.
 struct LeanBoxK {
   float fl, sa, sb, km1;
-  __device__ __forceinline__ explicit LeanBoxK(const FractalT<float> &f) {
-    fl = f.mbFoldLimit;
-    const float mR2 = f.mbMinR * f.mbMinR;
-    const float fR2 = f.mbFixedR * f.mbFixedR;
-    const float k1 = fR2 / mR2;   // >= 1 in the lean class (min radius <= fixed radius)
-    km1 = k1 - 1.0f;
-    sa = km1 > 0.0f ? fR2 / km1 : 0.0f;
-    sb = km1 > 0.0f ? 1.0f / km1 : 0.0f;
-  }
+  // k1 = fR2/mR2 >= 1 in the lean class (min radius <= fixed radius); the quotients are
+  // derived once on the host (FractalT::leanKm1, leanSa, leanSb)
+  __device__ __forceinline__ explicit LeanBoxK(const FractalT<float> &f)
+      : fl(f.mbFoldLimit), sa(f.leanSa), sb(f.leanSb), km1(f.leanKm1) {}
 };
 
 // One Mandelbox iteration (scale s, constant c); returns the new squared radius.
@@ -96,7 +98,7 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
   for (L = 0; L < N; L++) {
     const float r2 = box_iteration(k, s, x, y, z, dr, cx, cy, cz);
     if (r2 > 1048576.0f) {
-      dist = sqrtf(r2) / fabsf(dr);
+      dist = box_bailout_dist(r2, dr);
       break;
     }
   }
@@ -216,7 +218,7 @@ struct LeanOrbit<8> {
     for (int u = 0; u < kUnroll; u++) {
       const float r2 = box_iteration(k, s, x, y, z, dr, cx, cy, cz);
       if (r2 > 1048576.0f) {
-        dist = sqrtf(r2) / fabsf(dr);
+        dist = box_bailout_dist(r2, dr);
         return true;
       }
       if (++L == N) {
