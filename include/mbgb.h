@@ -228,7 +228,7 @@ typedef struct mbgb_opts {
                                 * hits whose FP32 bisection stopped early within 1e-4 of a window edge */
   int32_t tile_w, tile_h;      /* wavefront: pixel tile of a warp's first 32 primary rays (tile_w * tile_h
                                 * = 32); 0,0 = autotuned or 8 x 4 */
-  int32_t refill_min;          /* wavefront: idle lanes of a warp before it claims new rays; 0 = tuned or 1 */
+  int32_t refill_min;          /* wavefront: idle lanes of a warp before it claims new rays; 0 = tuned or 8 */
   int32_t autotune;            /* 1: tile shape, threads per CTA, CTAs per SM and refill_min that are 0
                                 * come from mbgb_autotune, run once per scene class and context */
   int32_t use_graph;           /* 1: the launches are captured once in a CUDA graph and replayed while
@@ -250,7 +250,7 @@ typedef struct mbgb_tuning {
   int32_t ctas_per_sm;         /* resident CTAs per SM of the ray stages */
   int32_t refill_min;          /* idle lanes before a warp refills */
   double ms;                   /* device time of the picked configuration on the tuning frame */
-  double ms_default;           /* device time of the default configuration (8 x 4, 128, max, 1) */
+  double ms_default;           /* device time of the default configuration (8 x 4, 128, max, 8) */
   int32_t trials;              /* configurations timed */
   int32_t orbit_refill;        /* ended orbits before a warp steps its shadow/AO rays on (0 = off) */
 } mbgb_tuning;

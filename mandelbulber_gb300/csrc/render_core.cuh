@@ -1313,7 +1313,7 @@ __global__ void __launch_bounds__(128) render_kernel(const __grid_constant__ Par
     if (lane == 0) {
       t = atomicAdd(io.tile_counter, 1u);
       if (deadline_passed(io)) { atomicExch(io.error_flag, 1); stop = 1; }
-      if (*(volatile int *)io.error_flag) stop = 1;
+      if (io.budget_ns && *(volatile int *)io.error_flag) stop = 1;
     }
     t = __shfl_sync(0xffffffffu, t, 0);
     stop = __shfl_sync(0xffffffffu, stop, 0);
