@@ -321,6 +321,43 @@ def coverage_section(ctx) -> dict:
     return out
 
 
+def configs_section(ctx) -> dict:
+    """The other single-frame configurations at full size: config 1 (Mandelbulb power 8, N 250,
+    640x480, hard shadows) and config 4 (deep zoom: Mandelbulb N 1000, 1024x1024, the camera
+    1e-6 from a seeded surface point). Per configuration and precision policy: the library's
+    device time of one frame (CUDA events around its launches; best of three after a warm-up,
+    one frame for FP64 and for the deep zoom, whose frames take seconds), the policy
+    MBGB_PREC_AUTO picked, and the FP32_FIX frame's hit mismatch
+    and float-image PSNR against the FP64 frame (the deep zoom is why AUTO exists: FP32 cannot
+    resolve a 1e-6 camera distance)."""
+    import mandelbulber_gb300 as mb
+    from mandelbulber_gb300 import workloads as W
+    from tests import metrics
+    out = {}
+    for name in ("mandelbulb_640x480", "deep_zoom_1024"):
+        sc = W.workload(name) if name != "deep_zoom_1024" else W.deep_zoom(ctx, size=1024)
+        npx = sc.image_width * sc.image_height
+        rec = {"size": [sc.image_width, sc.image_height], "formula": int(sc.formula), "N": int(sc.N)}
+        imgs = {}
+        for pol, key in ((mb.PREC_FP32_FIX, "fp32_fix"), (mb.PREC_FP64, "fp64"), (mb.PREC_AUTO, "auto")):
+            imgs[key] = ctx.render(sc, precision=pol)
+            best = float("inf")
+            for _ in range(1 if key == "fp64" or name == "deep_zoom_1024" else 3):
+                ctx.render(sc, precision=pol, image=imgs[key])
+                st = ctx.stats()
+                best = min(best, st.kernel_ms)
+            rec[key] = {"ms": best, "mpix_per_s": npx / (best * 1e3),
+                        "de_evaluations_per_s": st.de_calls / (best / 1e3)}
+            if key == "auto":
+                rec["auto_picked_fp64"] = bool(st.auto_fp64)
+        rec["fp32_fix_vs_fp64"] = metrics.compare(imgs["fp32_fix"], imgs["fp64"])
+        if rec["auto_picked_fp64"]:
+            rec["auto_vs_fp64_identical"] = bool(all(np.array_equal(getattr(imgs["auto"], k), getattr(imgs["fp64"], k))
+                                                     for k in ("image_float", "zbuffer", "hit")))
+        out[name] = rec
+    return out
+
+
 def run_once(args) -> int:
     """One frame of the workload at a small size (plus `--warmup` frames): the ncu profiling case."""
     import mandelbulber_gb300 as mb
@@ -352,6 +389,7 @@ def main() -> int:
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-grad", action="store_true", help="skip the gradient workload")
     ap.add_argument("--no-coverage", action="store_true", help="skip the other formulas / effects scenes")
+    ap.add_argument("--no-configs", action="store_true", help="skip config 1 (Mandelbulb 640x480) and the deep zoom")
     ap.add_argument("--grad-steps", type=int, default=5)
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
@@ -498,6 +536,7 @@ def main() -> int:
 
     batch = None if args.no_batch else batch_section(ctx, torch, dev, stream, flush, args, world, dist)
     coverage = None if args.no_coverage else coverage_section(ctx)
+    configs = None if args.no_configs else configs_section(ctx)
     grads = None if args.no_grad else grad_section(ctx, torch, dev, args)
 
     cpu = None
@@ -537,6 +576,7 @@ def main() -> int:
         "batch": batch,
         "grads": grads,
         "coverage": coverage,
+        "configs": configs,
         "clocks": clocks,
         "cpu_baseline": cpu,
         "wall_s_timed_region": wall32,

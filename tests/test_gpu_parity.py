@@ -160,6 +160,24 @@ def test_render_fp32_fix_against_oracle(gpu_ctx, oracle, name, size, engine):
     assert m["psnr_float"] >= 45.0, m
 
 
+def test_deep_zoom_against_oracle(gpu_ctx, oracle):
+    """Deep zoom (Mandelbulb power 8, N 1000, camera 1e-6 from a seeded surface point) at
+    48x48: MBGB_PREC_AUTO picks FP64 and renders the FP64 frame exactly; that frame meets
+    the FP64 Mandelbulb bar against the oracle (hit mismatch <= 0.5 %, PSNR >= 35 dB)."""
+    sc = W.deep_zoom(gpu_ctx, size=48)
+    ref, _ = oracle_lib.render(oracle, sc)
+    auto = gpu_ctx.render(sc, precision=mb.PREC_AUTO)
+    assert gpu_ctx.stats().auto_fp64 == 1
+    f64 = gpu_ctx.render(sc, precision=mb.PREC_FP64)
+    for k in LAYERS:
+        np.testing.assert_array_equal(getattr(auto, k), getattr(f64, k), err_msg=k)
+    m = metrics.compare(f64, ref)
+    print("deep zoom", m)
+    assert m["hit_fraction"] > 0.5, m
+    assert m["hit_mismatch"] <= 0.005, m
+    assert m["psnr_float"] >= 35.0, m
+
+
 def _fixture_scene(case, w, h):
     """The scene of render fixture `case` at another size (same perspective)."""
     z = np.load(os.path.join(GOLDEN, f"render_{case}.npz"))
