@@ -607,7 +607,7 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 // Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128, 6) primary_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
+__global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
