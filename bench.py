@@ -38,9 +38,9 @@ WORKLOAD = "mandelbox_1080p"
 # plus sqrt and divide of each DE evaluation
 FLOPS_PER_ITER = {8: 21, 2: 27}
 # dram__bytes_read.sum + dram__bytes_write.sum of secondary_kernel per 1080p launch: an ncu
-# --set full capture at 480x270 read 2.35 MB and wrote 0 B; the traffic is the per-hit
+# --set full capture at 480x270 read 2.36 MB and wrote 256 B; the traffic is the per-hit
 # inputs and AO slots, so it scales with the pixel count (x16)
-DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 37.6e6}
+DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 37.8e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
 
 
