@@ -397,7 +397,8 @@ __device__ __forceinline__ void march(const ParamsT<T> &p, const V3<T> start, co
   rs.point[2] = (double)pt.z;
 }
 
-// Binary hit refinement (src/Render3D.cpp:145-183), always in FP64.
+// Binary hit refinement (src/Render3D.cpp:145-183) in FP64 (the FP64 policy; refine_fix below
+// is the FP32 policy's).
 // detailSize keeps the value of the last march step, as in the reference.
 template <typename TP, int FORMULA>
 __device__ __forceinline__ void refine(const ParamsT<TP> &p, const FractalT<double> &fd, const V3<double> start,
@@ -440,6 +441,81 @@ __device__ __forceinline__ void refine(const ParamsT<TP> &p, const FractalT<doub
   rs.point[0] = point.x;
   rs.point[1] = point.y;
   rs.point[2] = point.z;
+}
+
+// FP32 policy: the binary refinement in FP32, then, for a hit whose FP32 bisection stopped
+// early with dist/thr within 1e-4 of a window edge, the FP64 re-evaluation at the FP32 result
+// and the bisection iterations it has left in FP64 (the rule of the wavefront engine's polish
+// stage). A bisection that used all 20 iterations keeps its FP32 depth: FP64 would have no
+// iteration left to move it.
+template <int FORMULA>
+__device__ __forceinline__ void refine_fix(const ParamsT<float> &p, const FractalT<double> &fd, const V3<double> start,
+                                           const V3<double> dir, RayState &rs, Counters &cnt,
+                                           const double distThreshInit = 0.0) {
+  using T = float;
+  const T search_limit = T(1) - T(0.01) * p.quality;
+  const T thrScale = p.resolution * p.persp / p.quality;
+  const T thrInit = (T)distThreshInit;
+  const V3<T> startT{(T)start.x, (T)start.y, (T)start.z}, dirT{(T)dir.x, (T)dir.y, (T)dir.z};
+  const T detail = (T)rs.detail;
+  T scan = (T)rs.scan;
+  T step = (T)rs.step * T(0.5);
+  T dist = (T)rs.dist;
+  T thr = (T)rs.distThresh;
+  V3<T> point = startT + dirT * scan;
+  int iters = rs.iters;
+  int bis = 0;
+  for (; bis < 20; bis++) {
+    cnt.steps++;
+    if (dist < thr && dist > thr * search_limit) break;
+    if (dist > thr) scan += step;
+    else if (dist < thr * search_limit) scan -= step;
+    point = startT + dirT * scan;
+    thr = p.constantDEThreshold ? p.quality : scan * thrScale + thrInit;
+    bool mi;
+    dist = calc_distance<T, FORMULA>(p.f, point, detail, p.f.N, p.f.minN, false, iters, mi, cnt, fparam_of(p.f));
+    step *= T(0.5);
+  }
+  const T q = dist / thr;
+  const bool clear = (q > search_limit + T(1e-4)) && (q < T(1) - T(1e-4));
+  if (!clear && bis < 20) {
+    const double search_limit_d = 1.0 - 0.01 * p.quality_d;
+    auto thr_of = [&](double sc) {
+      return p.constantDEThreshold ? p.quality_d : sc * p.resolution_d * p.persp_d / p.quality_d + distThreshInit;
+    };
+    double scanD = (double)scan, stepD = (double)step;
+    double thrD = thr_of(scanD);
+    V3<double> pointD = start + dir * scanD;
+    bool mi;
+    double distD = calc_distance<double, FORMULA>(fd, pointD, rs.detail, fd.N, fd.minN, false, iters, mi, cnt,
+                                                  fparam_of(fd));
+    cnt.steps++;
+    for (int it = bis; it < 20; it++) {
+      if (distD < thrD && distD > thrD * search_limit_d) break;
+      if (distD > thrD) scanD += stepD;
+      else if (distD < thrD * search_limit_d) scanD -= stepD;
+      pointD = start + dir * scanD;
+      thrD = thr_of(scanD);
+      distD = calc_distance<double, FORMULA>(fd, pointD, rs.detail, fd.N, fd.minN, false, iters, mi, cnt,
+                                             fparam_of(fd));
+      cnt.steps++;
+      stepD *= 0.5;
+    }
+    rs.scan = scanD;
+    rs.dist = distD;
+    rs.distThresh = thrD;
+    rs.point[0] = pointD.x;
+    rs.point[1] = pointD.y;
+    rs.point[2] = pointD.z;
+  } else {
+    rs.scan = (double)scan;
+    rs.dist = (double)dist;
+    rs.distThresh = (double)thr;
+    rs.point[0] = (double)point.x;
+    rs.point[1] = (double)point.y;
+    rs.point[2] = (double)point.z;
+  }
+  rs.iters = iters;
 }
 
 // ---------------------------------------------------------------------------
@@ -1177,7 +1253,10 @@ __device__ __forceinline__ void render_pixel(const ParamsT<T> &p, const FractalT
         io.overflow_list[k] = (unsigned int)pix;
         return;
       }
-      if (rs.found) refine<T, FORMULA>(p, fd, startRay, viewRay, rs, cnt, distThreshCarry);
+      if (rs.found) {
+        if constexpr (sizeof(T) == 4) refine_fix<FORMULA>(p, fd, startRay, viewRay, rs, cnt, distThreshCarry);
+        else refine<T, FORMULA>(p, fd, startRay, viewRay, rs, cnt, distThreshCarry);
+      }
     }
     itersState = rs.iters;
     if (ray == 0) iters0 = rs.iters;
