@@ -564,6 +564,7 @@ def main() -> int:
                      "frame_achieved": flops32 / (total32 / args.steps) / 1e12,
                      "work": f"{FLOPS_PER_ITER[f]} FP ops per orbit iteration + {FLOPS_PER_DE[f]} per DE evaluation"},
         "stages": stages32,
+        "fp64_polished_hits": int(st32.fp64_polished),
         "fp64_plain": {"value": value64, "unit": "Mpix/s", "ms_per_step": 1e3 * total64 / args.fp64_steps,
                        "steps": args.fp64_steps, "stages": stages64,
                        "roofline": {"kernel": top64, "bound": "fp64_alu", "achieved": ach64, "peak": peak64,
