@@ -67,18 +67,20 @@ struct LeanBoxK {
 // [1, k1], written 1 + (k1 - 1) sat((fR2/r2 - 1) / (k1 - 1)) so that the clamp rides on
 // the FMA pipe's saturation instead of two min/max instructions, with the approximate
 // reciprocal feeding one saturating FMA (measured +11 % orbit rate).
-__device__ __forceinline__ float box_iteration(const LeanBoxK &k, const float s, float &x, float &y, float &z,
-                                               float &dr, const float cx, const float cy, const float cz) {
+// The scale rides on the same FMA: k s = s + (s (k1 - 1)) sat(...), with skm1 = s (k1 - 1)
+// formed once per orbit (one rounding where k and k s took two; one instruction less).
+__device__ __forceinline__ float box_iteration(const LeanBoxK &k, const float s, const float skm1, float &x,
+                                               float &y, float &z, float &dr, const float cx, const float cy,
+                                               const float cz) {
   x = fmaf(fminf(fmaxf(x, -k.fl), k.fl), 2.0f, -x);
   y = fmaf(fminf(fmaxf(y, -k.fl), k.fl), 2.0f, -y);
   z = fmaf(fminf(fmaxf(z, -k.fl), k.fl), 2.0f, -z);
   const float r2 = norm2_rn(x, y, z);
-  const float kf = fmaf(__saturatef(fmaf(k.sa, rcp_approx(r2), -k.sb)), k.km1, 1.0f);
-  const float ks = __fmul_rn(kf, s);
+  const float ks = fmaf(__saturatef(fmaf(k.sa, rcp_approx(r2), -k.sb)), skm1, s);
   x = fmaf(x, ks, cx);
   y = fmaf(y, ks, cy);
   z = fmaf(z, ks, cz);
-  dr = fmaf(dr, fabsf(ks), 1.0f);   // |k s| = k |s| (k > 0), one instruction
+  dr = fmaf(dr, fabsf(ks), 1.0f);   // |k s| with the operand's absolute-value modifier
   return norm2_rn(x, y, z);
 }
 
@@ -90,13 +92,14 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
                                                 const float pz, const int N, int &Lout, Counters &cnt,
                                                 const float s) {
   const LeanBoxK k(f);
+  const float skm1 = __fmul_rn(s, k.km1);
   const float cx = __fmul_rn(px, f.constantFactor), cy = __fmul_rn(py, f.constantFactor),
               cz = __fmul_rn(pz, f.constantFactor);
   float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
   int L;
 #pragma unroll 5
   for (L = 0; L < N; L++) {
-    const float r2 = box_iteration(k, s, x, y, z, dr, cx, cy, cz);
+    const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
     if (r2 > 1048576.0f) {
       dist = box_bailout_dist(r2, dr);
       break;
@@ -192,12 +195,12 @@ struct LeanOrbit<8> {
   LeanBoxK k;
   float cf;
   int N;
-  float x, y, z, dr, cx, cy, cz, s;
+  float x, y, z, dr, cx, cy, cz, s, skm1;
   int L;
   __device__ __forceinline__ explicit LeanOrbit(const FractalT<float> &f) : k(f) {
     cf = f.constantFactor;
     N = f.N;
-    x = y = z = cx = cy = cz = s = 0.0f;
+    x = y = z = cx = cy = cz = s = skm1 = 0.0f;
     dr = 1.0f;
     L = 0;
   }
@@ -207,6 +210,7 @@ struct LeanOrbit<8> {
     cx = __fmul_rn(p.x, cf); cy = __fmul_rn(p.y, cf); cz = __fmul_rn(p.z, cf);
     dr = 1.0f;
     s = scale;
+    skm1 = __fmul_rn(scale, k.km1);
     L = 0;
   }
   __device__ __forceinline__ bool advance(float &dist) {
@@ -216,7 +220,7 @@ struct LeanOrbit<8> {
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) {
-      const float r2 = box_iteration(k, s, x, y, z, dr, cx, cy, cz);
+      const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
       if (r2 > 1048576.0f) {
         dist = box_bailout_dist(r2, dr);
         return true;
