@@ -1003,7 +1003,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
 // Byte layout of the wavefront buffers for `npix` pixels (256-byte aligned pieces).
 struct WaveLayout {
   size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
-  size_t pstep, pdist, pthr, pprev;
+  size_t prec, pprev;
   uint32_t poolCap;
   size_t total;
 };
@@ -1034,9 +1034,7 @@ static WaveLayout wave_layout(int64_t npix, size_t ts, int aoN, bool needVol) {
   w.ovl = take(npix * 4);
   w.last = take(npix * 4);
   w.poolCap = needVol ? (uint32_t)std::min<int64_t>(npix * kPoolChunksPerPixel, 0x7fffffff) : 1u;
-  w.pstep = take((size_t)w.poolCap * kChunk * ts);
-  w.pdist = take((size_t)w.poolCap * kChunk * ts);
-  w.pthr = take((size_t)w.poolCap * kChunk * ts);
+  w.prec = take((size_t)w.poolCap * kChunk * 4 * ts);
   w.pprev = take((size_t)w.poolCap * 4);
   w.total = off;
   return w;
@@ -1081,9 +1079,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.overflow_list = (uint32_t *)(base + w.ovl);
   wb.ctl = ctl;
   wb.last_chunk = (int32_t *)(base + w.last);
-  wb.pool_step = (T *)(base + w.pstep);
-  wb.pool_dist = (T *)(base + w.pdist);
-  wb.pool_thr = (T *)(base + w.pthr);
+  wb.pool_rec = (T *)(base + w.prec);
   wb.pool_prev = (int32_t *)(base + w.pprev);
   wb.pool_cap = w.poolCap;
   wb.polish_all = o.polish_all;

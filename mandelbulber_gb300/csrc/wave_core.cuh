@@ -439,6 +439,24 @@ __device__ __forceinline__ unsigned int claim_jobs(unsigned int *counter, const 
   return base + (unsigned int)__popc(mask & ((1u << lane) - 1u));
 }
 
+// One pooled step record: dist, thr, step in a 16-byte (float) or 32-byte (double) slot.
+__device__ __forceinline__ void store_record(float *r, const float dist, const float thr, const float step) {
+  *reinterpret_cast<float4 *>(r) = make_float4(dist, thr, step, 0.0f);
+}
+__device__ __forceinline__ void store_record(double *r, const double dist, const double thr, const double step) {
+  reinterpret_cast<double2 *>(r)[0] = make_double2(dist, thr);
+  reinterpret_cast<double2 *>(r)[1] = make_double2(step, 0.0);
+}
+__device__ __forceinline__ void load_record(const float *r, float &dist, float &thr, float &step) {
+  const float4 q = *reinterpret_cast<const float4 *>(r);
+  dist = q.x; thr = q.y; step = q.z;
+}
+__device__ __forceinline__ void load_record(const double *r, double &dist, double &thr, double &step) {
+  const double2 a = reinterpret_cast<const double2 *>(r)[0];
+  const double2 b = reinterpret_cast<const double2 *>(r)[1];
+  dist = a.x; thr = a.y; step = b.x;
+}
+
 // Frame of a primary job / of a pixel of the batch (binary search over the frame table).
 template <typename T>
 __device__ __forceinline__ int frame_of_job(const FrameCam<T> *__restrict__ cams, const int n, const unsigned int job) {
@@ -739,8 +757,9 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
               continue;
             }
             rec = (int64_t)chunk * kChunk + (i % kChunk);
-            wb.pool_dist[rec] = dist;
-            wb.pool_thr[rec] = thr;
+            // the record's step slot holds the step that reached this point; the walk
+            // never reads it for the hit record
+            store_record(wb.pool_rec + 4 * rec, dist, thr, step);
           }
         }
         if (dist > T(3)) dist = T(3);
@@ -751,10 +770,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           bis = 0;
           if (dist < thr && dist > thr * search_limit) done = true;
         } else {
-          if (useSB) {
-            if (io.overflow_pass) sb.step[sb.at(i)] = step;
-            else wb.pool_step[rec] = step;
-          }
+          if (useSB && io.overflow_pass) sb.step[sb.at(i)] = step;
           step = (dist - stepFrac * thr) * p.DE_factor;
           if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)gp, (uint32_t)i)) / T(10000));
           buffCount++;
@@ -1239,7 +1255,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
 // holds the records from kChunk * (nchunks - 1) on.
 template <typename T>
 struct PoolRecords {
-  const T *step, *dist, *thr;
+  const T *rec;            // [chunk * kChunk + r][4]: dist, thr, step, unused
   const int32_t *prev;
   int32_t last;      // chunk holding the last written record
   int lastRec;       // index of the last written record: buffCount for a hit (its hit step
@@ -1268,9 +1284,8 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
       chunkBase -= kChunk;
     }
     const int64_t rec = (int64_t)chunk * kChunk + (index - chunkBase);
-    T step = pr.step[rec];
-    const T distance = pr.dist[rec];
-    const T dist_thresh = pr.thr[rec];
+    T distance, dist_thresh, step;
+    load_record(pr.rec + 4 * rec, distance, dist_thresh, step);
     totalStep += step;
     if (totalStep < dist_thresh * p.quality) continue;
     step = totalStep;
@@ -1416,7 +1431,7 @@ __global__ void __launch_bounds__(128) compose_kernel(const __grid_constant__ Pa
       bool set = false;
       if (p.needVolumetric) {
         const int count = wb.count[gp];
-        const PoolRecords<T> pr{wb.pool_step, wb.pool_dist, wb.pool_thr, wb.pool_prev, wb.last_chunk[gp],
+        const PoolRecords<T> pr{wb.pool_rec, wb.pool_prev, wb.last_chunk[gp],
                                 hit ? count : count - 1};
         volumetric_pool<T>(p, pr, count, wb.scan[gp], res, totalOpacity, set);
       }

@@ -32,7 +32,8 @@ struct WaveBufs {
   uint32_t *overflow_list;
   // Step records of the primary rays: chunks of kChunk records linked backwards
   // (prev), allocated by bump counter; the pixel keeps its last chunk.
-  T *pool_step, *pool_dist, *pool_thr;   // [chunk * kChunk + r]
+  T *pool_rec;                           // [chunk * kChunk + r][4]: dist, thr, step, unused
+                                         // (one 16- or 32-byte record: one store, one load)
   int32_t *pool_prev;                    // [chunk]
   int32_t *last_chunk;                   // [npix], -1 = no records
   uint32_t pool_cap;                     // chunks
