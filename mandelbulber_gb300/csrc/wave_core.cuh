@@ -2,23 +2,27 @@
 // split into ray-granular stages so that SIMT lanes stay busy.
 //
 //   primary_kernel   one primary ray per job: RayMarching's march and binary refinement
-//                    (src/Render3D.cpp:79-199); at the end of each ray the lane folds
-//                    the ray's step records into the volumetric pass's affine map and
-//                    takes the next pixel (lane refill).
-//   polish_kernel    FP32 policy: the last bisection steps in FP64 at every hit.
+//                    (src/Render3D.cpp:79-199) with lane refill; the march's step records
+//                    go to a pool of chained 32-record chunks (the overflow pass, for rays
+//                    the pool cannot hold, folds them into the volumetric pass's affine
+//                    map at once).
+//   polish_kernel    FP32 policy: the last bisection steps in FP64 for the hits whose FP32
+//                    bisection stopped within 1e-4 of a window edge.
 //   secondary_kernel one shadow ray (MainShadow, src/shaders.cpp:480-570) or one AO
 //                    direction (AmbientOcclusion, src/shaders.cpp:607-673) per job,
 //                    with lane refill; results go to per-pixel slots.
 //   compose_kernel   normals, colour, specular, fast AO, background, the volumetric
-//                    map and the cImage writes (ObjectShader / BackgroundShader /
-//                    VolumetricShader, src/shaders.cpp:21-478).
+//                    pass over the pooled records (or the overflow pass's affine map) and
+//                    the cImage writes (ObjectShader / BackgroundShader / VolumetricShader,
+//                    src/shaders.cpp:21-478).
 //
 // The volumetric pass is affine in the pixel colour it starts from: every glow, post-fog
 // and volumetric-fog group computes out = a*C + (1 - a)*out, so the whole pass is
 // out = A*base + B with one A for the three channels; alpha and opacity do not depend on
 // the base colour (its alpha is 1 for a hit and 0 otherwise, known when the march ends).
-// Lane refill: each warp keeps 32 rays in flight; when rays end, one atomicAdd on the
-// job counter hands the free lanes their next jobs (popc of the ballot).
+// Lane refill: each warp keeps up to 32 rays in flight; once refill_min of its lanes are
+// idle (or none is busy), one atomicAdd on the job counter hands them their next jobs (popc
+// of the ballot).
 #pragma once
 
 #include "dual.cuh"
