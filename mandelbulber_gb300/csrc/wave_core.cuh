@@ -1343,7 +1343,7 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
 // over every pixel of the batch.
 // ---------------------------------------------------------------------------
 template <typename T, int FORMULA, bool FAST>
-__global__ void __launch_bounds__(128) compose_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
+__global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compose_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   Counters cnt{0, 0, 0, 0};
   const int64_t total = wb.npix;
