@@ -507,6 +507,10 @@ def main() -> int:
     peak_lib.mbgb_peak_tflops.restype = ctypes.c_double
     peak32 = peak_lib.mbgb_peak_tflops(0, dev)
     peak64 = peak_lib.mbgb_peak_tflops(1, dev)
+    peak_lib.mbgb_box_orbit_rate.restype = ctypes.c_double
+    # the lean Mandelbox iteration alone (every lane busy, no ray bookkeeping): the ceiling
+    # this instruction mix allows, against which the dominant kernel's orbit rate is read
+    loop_rate = peak_lib.mbgb_box_orbit_rate(dev) if scene.formula == 8 else -1.0
     f = scene.formula
     stage_names = ["primary_kernel", "polish_kernel", "secondary_kernel", "compose_kernel"]
 
@@ -562,7 +566,14 @@ def main() -> int:
                      "flops_per_launch": int(work32),
                      "frame_flops": int(flops32),
                      "frame_achieved": flops32 / (total32 / args.steps) / 1e12,
-                     "work": f"{FLOPS_PER_ITER[f]} FP ops per orbit iteration + {FLOPS_PER_DE[f]} per DE evaluation"},
+                     "work": f"{FLOPS_PER_ITER[f]} FP ops per orbit iteration + {FLOPS_PER_DE[f]} per DE evaluation",
+                     "orbit_loop_ceiling": None if loop_rate <= 0 else {
+                         "iterations_per_s": loop_rate * 1e12,
+                         "tflops": loop_rate * FLOPS_PER_ITER[f],
+                         "kernel_iterations_per_s": stages32[top32]["orbit_iterations"] / sec32,
+                         "frac": stages32[top32]["orbit_iterations"] / sec32 / (loop_rate * 1e12),
+                         "what": "the lean Mandelbox iteration alone on bounded orbits (libmbgb_peak.so): "
+                                 "the issue-bound ceiling of this instruction mix"}},
         "stages": stages32,
         "fp64_polished_hits": int(st32.fp64_polished),
         "fp64_plain": {"value": value64, "unit": "Mpix/s", "ms_per_step": 1e3 * total64 / args.fp64_steps,

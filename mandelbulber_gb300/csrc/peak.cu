@@ -1,11 +1,41 @@
 // ALU peak microbenchmark used by bench.py as the roofline denominator of the
 // ray-march kernels: dependent-free FMA chains in FP32 or FP64, sized to fill
 // every SM. Reports FLOP/s counting one FMA as two operations.
+// Also the orbit-loop ceiling of the lean Mandelbox iteration: the render kernels'
+// iteration (lean_orbit.cuh) on bounded orbits, every lane busy, no ray bookkeeping.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
+#include "lean_orbit.cuh"
+
 namespace {
+
+using mbgb::dev::LeanBoxK;
+
+// Orbits of points near the origin (inside the scale-2 Mandelbox, so no lane leaves early),
+// n iterations each with the bailout test evaluated every iteration as in the renderer.
+__global__ void box_orbit_loop(float *out, unsigned long long *count, int orbits, int n, LeanBoxK k, float s,
+                               float skm1) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  float acc = 0.0f;
+  unsigned long long it = 0;
+  for (int o = 0; o < orbits; o++) {
+    const float cx = 1e-4f * (float)((tid + 7 * o) & 1023), cy = 1e-4f * (float)((tid * 3 + o) & 1023),
+                cz = 1e-4f * (float)((tid * 5 + 3 * o) & 1023);
+    float x = cx, y = cy, z = cz, dr = 1.0f;
+    int L;
+#pragma unroll 5
+    for (L = 0; L < n; L++) {
+      const float r2 = mbgb::dev::box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
+      if (r2 > 1048576.0f) break;
+    }
+    it += (unsigned long long)(L + 1);
+    acc += x + y + z + dr;
+  }
+  if (acc == -1.2345f) out[tid] = acc;  // keeps the orbits live
+  atomicAdd(count, it);
+}
 
 template <typename T>
 __global__ void fma_chains(T *out, int iters, T a, T b) {
@@ -52,4 +82,45 @@ extern "C" double mbgb_peak_tflops(int fp64, int device) {
   if (cudaGetLastError() != cudaSuccess) return -1.0;
   const double flops = 2.0 * 64.0 * (double)iters * grid * block;
   return flops / (best * 1e-3) / 1e12;
+}
+
+// Iterations per second (in units of 1e12) of the lean Mandelbox iteration in isolation, for
+// scale 2, fold limit 1, min radius 0.5, fixed radius 1 (the 1080p Mandelbox workload),
+// 128-thread CTAs at 10 per SM (the shadow/AO kernel's occupancy), best of five timed runs.
+extern "C" double mbgb_box_orbit_rate(int device) {
+  if (cudaSetDevice(device) != cudaSuccess) return -1.0;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return -1.0;
+  const int block = 128, grid = prop.multiProcessorCount * 10, orbits = 64, n = 60;
+  const float fR2 = 1.0f, mR2 = 0.25f, km1 = fR2 / mR2 - 1.0f, s = 2.0f;
+  const LeanBoxK k{1.0f, fR2 / km1, 1.0f / km1, km1};
+  void *out = nullptr, *count = nullptr;
+  if (cudaMalloc(&out, (size_t)grid * block * 4) != cudaSuccess) return -1.0;
+  if (cudaMalloc(&count, 8) != cudaSuccess) {
+    cudaFree(out);
+    return -1.0;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 6; rep++) {
+    cudaMemset(count, 0, 8);
+    cudaEventRecord(e0);
+    box_orbit_loop<<<grid, block>>>((float *)out, (unsigned long long *)count, orbits, n, k, s, s * km1);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    unsigned long long h = 0;
+    cudaMemcpy(&h, count, 8, cudaMemcpyDeviceToHost);
+    const double rate = (double)h / (ms * 1e-3) / 1e12;
+    if (rep > 0 && rate > best) best = rate;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  cudaFree(count);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  return best;
 }
