@@ -375,7 +375,7 @@ def run_once(args) -> int:
     return 0
 
 
-def main() -> int:
+def make_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -394,7 +394,11 @@ def main() -> int:
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
     ap.add_argument("--precision", default="fp32_fix", choices=["fp32_fix", "fp64"])
-    args = ap.parse_args()
+    return ap
+
+
+def main() -> int:
+    args = make_parser().parse_args()
     args.warmup = max(args.warmup, 3)
 
     rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
