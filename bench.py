@@ -4,8 +4,8 @@
 Workload (default): the 1920x1080 Mandelbox scene (scale 2, 15 iterations, hard
 shadows, ray-traced AO with 29 directions, volumetric fog 0.5, glow), rendered
 with the FP32 march + FP64 hit refinement policy. One step = one full frame.
-The same frame in the plain FP64 policy is timed beside it (the north-star
-ratio), and the two are compared (hit/miss mismatch, PSNR).
+The same frame in the plain FP64 policy is timed beside it (the headline metric's
+FP32-vs-FP64 ratio), and the two are compared (hit/miss mismatch, PSNR).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 

@@ -11,7 +11,7 @@ Tolerances (stated per test):
     >= 90 % and PSNR >= 35 dB on the 32x32 .. 64x48 golden frames (one flipped
     pixel of a 32x32 frame alone costs several dB).
   * FP32 + FP64-refinement policy: hit/miss mismatch <= 0.1 % and PSNR >= 45 dB
-    of the float image against the FP64 oracle (the spec bar), at sizes the
+    of the float image against the FP64 oracle (the headline metric's bar), at sizes the
     oracle finishes in seconds.
 """
 import ctypes
