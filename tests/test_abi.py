@@ -49,3 +49,15 @@ def test_context_without_gpu_fails_loudly(mblib):
     with pytest.raises(mb.MbgbError) as e:
         mb.Context(0)
     assert e.value.status == 7
+
+
+def test_option_structs_follow_the_header():
+    """The Python mirrors of mbgb_opts / mbgb_tuning are read from include/mbgb.h: the launch
+    options land in their fields, and the defaults (0) select the library's own choices."""
+    o = mb.make_opts(refill_min=4, orbit_refill=-1, tile=(16, 2), threads_per_cta=64)
+    assert (o.refill_min, o.orbit_refill, o.tile_w, o.tile_h, o.threads_per_cta) == (4, -1, 16, 2, 64)
+    d = mb.make_opts()
+    assert d.refill_min == 0 and d.orbit_refill == 0 and d.autotune == 0
+    names = [f[0] for f in mb.mbgb_tuning._fields_]
+    assert {"tile_w", "tile_h", "threads_per_cta", "ctas_per_sm", "refill_min", "orbit_refill", "ms"} <= set(names)
+    assert ctypes.sizeof(mb.mbgb_opts) % 8 == 0
