@@ -365,11 +365,12 @@ def run_once(args) -> int:
     w, h = (int(v) for v in args.once.lower().split("x"))
     scene = W.workload(args.workload, w, h)
     prec = mb.PREC_FP64 if args.precision == "fp64" else mb.PREC_FP32_FIX
+    engine = mb.ENGINE_PER_PIXEL if args.engine == "per_pixel" else mb.ENGINE_WAVEFRONT
     with mb.Context(0) as ctx:
         for _ in range(args.warmup + 1):
-            img = ctx.render(scene, precision=prec)
+            img = ctx.render(scene, precision=prec, engine=engine)
         st = ctx.stats()
-    print(json.dumps({"workload": args.workload, "size": [w, h], "precision": args.precision,
+    print(json.dumps({"workload": args.workload, "size": [w, h], "precision": args.precision, "engine": args.engine,
                       "kernel_ms": st.kernel_ms, "orbit_iterations": st.orbit_iterations, "de_calls": st.de_calls,
                       "hit_fraction": float(img.hit.mean())}))
     return 0
@@ -394,6 +395,8 @@ def make_parser() -> argparse.ArgumentParser:
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
     ap.add_argument("--precision", default="fp32_fix", choices=["fp32_fix", "fp64"])
+    ap.add_argument("--engine", default="wavefront", choices=["wavefront", "per_pixel"],
+                    help="with --once: the render engine of the profiling case")
     return ap
 
 
