@@ -11,8 +11,10 @@ FP32-vs-FP64 ratio), and the two are compared (hit/miss mismatch, PSNR).
 
 `--impl reference` times the CPU implementation of the path (the oracle
 restatement, built with the reference's -O3 -ffast-math flags, its
-one-worker-per-core row claiming and rand() step jitter) on a bounded band of
-rows of the same frame, with every host thread.
+one-worker-per-core row claiming and rand() step jitter) on a bounded sample of
+rows spread evenly over the same frame, with every host thread. It loads the
+frame's scene from the committed bytes in tests/golden/bench_scenes.npz and
+loads nothing but the oracle library.
 """
 from __future__ import annotations
 
@@ -42,6 +44,41 @@ FLOPS_PER_ITER = {8: 21, 2: 27}
 # inputs and AO slots, so it scales with the pixel count (x16)
 DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 37.8e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
+PRECISION = "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement"
+# the single-frame workloads bench.py times (the scenes are built by mandelbulber_gb300.workloads;
+# their bytes are committed in tests/golden/bench_scenes.npz for the reference arm)
+WORKLOADS = {
+    "mandelbox_1080p": {"width": 1920, "height": 1080,
+                        "scene": "Mandelbox scale 2 (formula 8), N 15, camera (0,-20,0), 53 deg FOV, hard shadow, "
+                                 "ray AO q2 (29 dirs), volumetric fog 0.5, glow"},
+    "mandelbulb_640x480": {"width": 640, "height": 480,
+                           "scene": "Mandelbulb power 8 (formula 2), N 250, camera (0,-3.5,0), 53 deg FOV, "
+                                    "hard shadow, no AO / fog / glow"},
+}
+BENCH_SCENES = os.path.join(ROOT, "tests", "golden", "bench_scenes.npz")
+
+
+def reference_rows(threads: int) -> int:
+    """Rows of one reference-arm step: four per host thread (the dynamic row claiming then
+    balances rows of unequal cost), at least 32."""
+    return max(4 * threads, 32)
+
+
+def bench_config(workload: str, world: int) -> dict:
+    """The `config` of both arms' lines (identical, so the two lines describe one workload)."""
+    wl = WORKLOADS[workload]
+    threads = os.cpu_count() or 1
+    return {"workload": workload, "width": wl["width"], "height": wl["height"], "scene": wl["scene"],
+            "precision": PRECISION, "l2": "flushed between timed frames (512 MiB write)",
+            "parallelism": f"replicas x{world}",
+            "reference_sample": (f"--impl reference: {reference_rows(threads)} of the {wl['height']} rows per step, "
+                                 f"spread evenly over the frame, {threads} host threads, Mpix/s of those rows")}
+
+
+def bench_scene_buffer(workload: str):
+    """The committed mbgb_scene bytes of a workload as a ctypes buffer (no product import)."""
+    z = np.load(BENCH_SCENES)
+    return ctypes.create_string_buffer(z[workload].tobytes())
 
 
 def max_over_ranks(seconds: float, dist, device) -> float:
@@ -125,52 +162,56 @@ class ClockSampler:
 
 
 def cpu_sample(scene, seconds: float, jitter: bool = True):
-    """Times the CPU oracle on a band of rows sized to about `seconds` of work; returns (Mpix/s, desc)."""
+    """Times the CPU oracle on rows spread evenly over the frame, as many as about `seconds`
+    of work takes; returns (Mpix/s, desc)."""
     from tests import oracle_lib
     lib = oracle_lib.load(fast=True)
     threads = os.cpu_count() or 1
     w, h = scene.image_width, scene.image_height
-    mid = h // 2
-    rows = max(threads, 8)
+    n = max(threads, 8)
     while True:
-        r0 = max(0, mid - rows // 2)
-        r1 = min(h, r0 + rows)
+        rows = oracle_lib.sample_rows(h, n)
         t0 = time.perf_counter()
-        oracle_lib.render(lib, scene, rows=(r0, r1), jitter=jitter, threads=threads)
+        oracle_lib.render_row_list(lib, ctypes.addressof(scene), w, h, rows, jitter=jitter, threads=threads)
         dt = time.perf_counter() - t0
-        if dt >= seconds * 0.5 or r1 - r0 >= h:
+        if dt >= seconds * 0.5 or len(rows) >= h:
             break
-        rows = min(h, int(rows * max(2.0, seconds / max(dt, 1e-3) * 0.9)))
-    px = (r1 - r0) * w
-    return px / dt / 1e6, {"rows": [r0, r1], "pixels": px, "seconds": dt, "threads": threads}
+        n = min(h, int(n * max(2.0, seconds / max(dt, 1e-3) * 0.9)))
+    px = len(rows) * w
+    return px / dt / 1e6, {"rows": len(rows), "pixels": px, "seconds": dt, "threads": threads}
 
 
 def run_reference(args, rank: int, world: int) -> int:
+    """The reference arm: the CPU implementation of the path on the host cores, on the same
+    workload and config as the GPU arm, one bounded row sample per step."""
     if rank != 0:
         return 0
-    from mandelbulber_gb300 import workloads as W
-    scene = W.workload(args.workload)
     from tests import oracle_lib
+    wl = WORKLOADS[args.workload]
+    w, h = wl["width"], wl["height"]
+    scene = bench_scene_buffer(args.workload)
     lib = oracle_lib.load(fast=True)
     threads = os.cpu_count() or 1
-    w, h = scene.image_width, scene.image_height
-    band = max(threads, 16)
-    r0 = h // 2 - band // 2
+    rows = oracle_lib.sample_rows(h, reference_rows(threads))
+    layers = oracle_lib.alloc_layers(w, h)
     for _ in range(args.warmup):
-        oracle_lib.render(lib, scene, rows=(r0, r0 + max(2, band // 4)), jitter=True, threads=threads)
+        oracle_lib.render_row_list(lib, ctypes.addressof(scene), w, h, rows[::4], jitter=True, threads=threads,
+                                   layers=layers)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle_lib.render(lib, scene, rows=(r0, r0 + band), jitter=True, threads=threads)
+        oracle_lib.render_row_list(lib, ctypes.addressof(scene), w, h, rows, jitter=True, threads=threads,
+                                   layers=layers)
         times.append(time.perf_counter() - t0)
-    px = band * w
+    px = len(rows) * w
     value = px * len(times) / sum(times) / 1e6
-    sample = (f"rows {r0}-{r0 + band} of the {w}x{h} frame ({px} px per step), CPU oracle restatement "
-              f"(-O3 -ffast-math), rand() step jitter, one worker per host thread, dynamic rows")
+    sample = (f"{len(rows)} rows spread evenly over the {w}x{h} frame ({px} px per step), the CPU oracle "
+              f"restatement (bit-exact to the reference's own compiled code on every golden) built with the "
+              f"reference flags -O3 -ffast-math, rand() step jitter, one worker per host thread, dynamic rows")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "width": w, "height": h},
+            "config": bench_config(args.workload, world),
             "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -440,9 +481,9 @@ def main() -> int:
     ptrs = {k: v.data_ptr() for k, v in L.items()}
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
 
-    def timed_frames(precision, steps, warmup):
+    def timed_frames(precision, steps, warmup, **opts):
         for _ in range(warmup):
-            ctx.render_device(scene, ptrs, precision=precision, stream=stream.cuda_stream)
+            ctx.render_device(scene, ptrs, precision=precision, stream=stream.cuda_stream, **opts)
         stream.synchronize()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         if dist:
@@ -453,7 +494,7 @@ def main() -> int:
             with torch.cuda.stream(stream):
                 flush.zero_()                      # L2 flush between timed frames (512 MiB > 129 MB L2)
                 e0.record(stream)
-            ctx.render_device(scene, ptrs, precision=precision, stream=stream.cuda_stream)
+            ctx.render_device(scene, ptrs, precision=precision, stream=stream.cuda_stream, **opts)
             e1.record(stream)
         stream.synchronize()
         torch.cuda.synchronize(dev)
@@ -481,6 +522,40 @@ def main() -> int:
     b = ctx.render(scene, precision=mb.PREC_FP64)
     parity = metrics.compare(a, b)
 
+    # the same policy with every hit's bisection finished in FP64 (polish_all), beside the
+    # headline's selective polish of the hits that stopped early near a window edge
+    pa_steps = max(3, args.steps // 4)
+    total_pa, _, _ = timed_frames(mb.PREC_FP32_FIX, pa_steps, 1, polish_all=True)
+    ctx.render_device(scene, ptrs, precision=mb.PREC_FP32_FIX, polish_all=True)
+    st_pa = ctx.stats()
+    polish_all = {"value": whole_job_rate(world, npx, pa_steps, total_pa) / 1e6, "unit": "Mpix/s",
+                  "ms_per_step": 1e3 * total_pa / pa_steps, "steps": pa_steps,
+                  "fp64_polished_hits": int(st_pa.fp64_polished),
+                  "parity_vs_fp64": metrics.compare(ctx.render(scene, precision=mb.PREC_FP32_FIX, polish_all=True), b)}
+
+    # the allocation-free entry point (static scratch, per-pixel engine) on the same frame
+    lib = mb.library()
+    na_img = mb.mbgb_image(w, h, *[ctypes.c_void_p(ptrs[n]) for n in ("image_float", "zbuffer", "alpha",
+                                                                         "opacity", "colour")], None, None, None)
+    na_opts = mb.make_opts(precision=mb.PREC_FP32_FIX, stream=stream.cuda_stream)
+    for _ in range(2):
+        assert lib.mbgb_render_device_noalloc(ctypes.byref(scene), ctypes.byref(na_img), ctypes.byref(na_opts)) == 0, \
+            lib.mbgb_last_error()
+    na_steps = max(3, args.steps // 4)
+    na_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(na_steps)]
+    stream.synchronize()
+    for e0, e1 in na_evs:
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+        lib.mbgb_render_device_noalloc(ctypes.byref(scene), ctypes.byref(na_img), ctypes.byref(na_opts))
+        e1.record(stream)
+    stream.synchronize()
+    na_ms = sum(a.elapsed_time(b_) for a, b_ in na_evs) / na_steps
+    noalloc = {"value": npx / (na_ms * 1e3), "unit": "Mpix/s", "ms_per_step": na_ms, "steps": na_steps,
+               "engine": "per-pixel (one pixel per thread), 96-thread CTAs, one per SM, 256 step records per "
+                         "slot in static device arrays"}
+
     # end to end through the public host entry point: pinned host layers, copies inside the timed region
     host = mb.CImage.empty(w, h)
     pinned = {}
@@ -495,7 +570,6 @@ def main() -> int:
                                   for n in ("image_float", "zbuffer", "alpha", "opacity", "colour")],
                           None, None, None)
     opts = mb.make_opts(precision=mb.PREC_FP32_FIX)
-    lib = mb.library()
     for _ in range(2):
         lib.mbgb_render_host(ctx._h, ctypes.byref(scene), ctypes.byref(img_c), ctypes.byref(opts))
     e2e_t = []
@@ -554,7 +628,7 @@ def main() -> int:
     if rank == 0 and world == 1 and not args.no_cpu:
         v, desc = cpu_sample(scene, args.cpu_seconds)
         cpu = {"value": v, "unit": "Mpix/s", "cores": desc["threads"], "kind": "port",
-               "sample": (f"rows {desc['rows'][0]}-{desc['rows'][1]} of the {w}x{h} frame ({desc['pixels']} px, "
+               "sample": (f"{desc['rows']} rows spread evenly over the {w}x{h} frame ({desc['pixels']} px, "
                           f"{desc['seconds']:.1f} s), CPU oracle restatement built with the reference flags "
                           f"-O3 -ffast-math, rand() step jitter, {desc['threads']} host threads")}
 
@@ -562,11 +636,7 @@ def main() -> int:
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total32 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": args.workload, "width": w, "height": h,
-                   "scene": "Mandelbox scale 2 (formula 8), N 15, camera (0,-20,0), 53 deg FOV, hard shadow, "
-                            "ray AO q2 (29 dirs), volumetric fog 0.5, glow",
-                   "precision": "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement",
-                   "l2": "flushed between timed frames (512 MiB write)", "parallelism": f"replicas x{world}"},
+        "config": bench_config(args.workload, world),
         "roofline": {"kernel": top32, "bound": "fp32_alu", "achieved": ach32, "peak": peak32, "unit": "TFLOP/s",
                      "frac": ach32 / peak32 if peak32 > 0 else None, "traffic": traffic,
                      "peak_source": "measured live: FP32 FMA-chain microbenchmark (libmbgb_peak.so)",
@@ -588,6 +658,8 @@ def main() -> int:
                        "roofline": {"kernel": top64, "bound": "fp64_alu", "achieved": ach64, "peak": peak64,
                                     "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 > 0 else None}},
         "ratio_vs_fp64": value / value64,
+        "polish_all": polish_all,
+        "noalloc": noalloc,
         "parity_vs_fp64": parity,
         "e2e": {"value": e2e_value, "unit": "Mpix/s", "h2d_bytes_per_step": ctypes.sizeof(mb.mbgb_scene),
                 "d2h_bytes_per_step": d2h},

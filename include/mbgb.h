@@ -396,12 +396,16 @@ mbgb_status mbgb_autotune(mbgb_context *ctx, const mbgb_scene *scene, const mbgb
  * that every GPU loading this library holds until the process exits. `out` holds
  * device pointers; the render runs on the current device and on opts->stream
  * (NULL = the legacy default stream, and the call then waits for the frame and
- * reports a device-deadline timeout). Limits: precision MBGB_PREC_FP32_FIX (or
- * MBGB_PREC_AUTO) only; at most 4194304 pixels (e.g. 2048 x 2048), larger frames are
- * rejected with MBGB_ERR_BAD_PARAM. The first call on a device resolves the arrays'
- * device addresses, so make that first call before any stream capture. All calls
- * share the arrays: calls that overlap on the GPU (other streams, other host
- * threads) race and must be serialised by the caller. */
+ * reports a device-deadline timeout). `opts` may be NULL (FP32_FIX, default stream).
+ * Limits: precision MBGB_PREC_FP32_FIX only (MBGB_PREC_AUTO, which picks FP64 for deep
+ * zooms, and MBGB_PREC_FP64 are rejected with MBGB_ERR_BAD_PARAM); at most 4194304
+ * pixels (e.g. 2048 x 2048), larger frames are rejected with MBGB_ERR_BAD_PARAM.
+ * The first call on a device resolves the arrays' device addresses, so make that
+ * first call before any stream capture. A call whose AO quality (globalIlumQuality)
+ * differs from the previous call's on that device copies the AO direction table from
+ * host memory on opts->stream; calls at an unchanged quality copy nothing. All calls
+ * share the arrays, which keep the last call's contents: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the caller. */
 mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const mbgb_image *out, const mbgb_opts *opts);
 
 /* Distance estimate at points (CalculateDistance, src/fractal.cpp:1245-1448) with

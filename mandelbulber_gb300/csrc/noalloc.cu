@@ -10,7 +10,8 @@
 // fixed-size static device arrays defined below, 79.4 MB (75.8 MiB) in total,
 // which every GPU that loads the library holds until the process exits.
 //
-// Limits: FP32-with-FP64-refinement policy only; at most kNaMaxPixels pixels
+// Limits: FP32-with-FP64-refinement policy only (MBGB_PREC_FP32_FIX; MBGB_PREC_AUTO is
+// refused, since it would pick FP64 for deep zooms); at most kNaMaxPixels pixels
 // (the overflow pixel list is sized for that); rays longer than kNaStepCap step
 // records go to the overflow pass (exact, but slower than mbgb_render_device).
 #include <cuda_runtime.h>
@@ -52,6 +53,8 @@ struct DeviceSymbols {
   unsigned long long *control = nullptr;
   int sms = 0;
   bool ready = false;
+  int aoQuality = -1;   // globalIlumQuality whose direction table g_na_ao holds (-1: none yet)
+  int aoCount = 0;      // directions in that table
 };
 
 DeviceSymbols g_sym[kMaxDevices];
@@ -104,8 +107,13 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
                            "image larger than the allocation-free scratch allows (4194304 pixels, e.g. 2048 x 2048)");
   mbgb_opts o{};
   if (opts_in) o = *opts_in;
-  if (o.precision != MBGB_PREC_FP32_FIX && o.precision != MBGB_PREC_AUTO)
-    return mbgb::set_error(MBGB_ERR_BAD_PARAM, "the allocation-free entry point renders the FP32_FIX policy only");
+  else o.precision = MBGB_PREC_FP32_FIX;   // NULL options: the one policy this entry point renders
+  // MBGB_PREC_AUTO is refused, not mapped to FP32_FIX: for a deep zoom AUTO picks FP64 in
+  // every other entry point, and this one carries no FP64 pipeline to honour that pick.
+  if (o.precision != MBGB_PREC_FP32_FIX)
+    return mbgb::set_error(MBGB_ERR_BAD_PARAM,
+                           "the allocation-free entry point renders the FP32_FIX policy only (MBGB_PREC_AUTO "
+                           "may pick FP64, which it does not carry)");
   if (!scene->analitycDE)
     return mbgb::set_error(MBGB_ERR_UNSUPPORTED,
                            "delta-DE formulas render in FP64, which the allocation-free entry point does not carry");
@@ -132,16 +140,25 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   if (st != MBGB_OK) return st;
   cudaStream_t s = (cudaStream_t)o.stream;
 
-  // AO direction table into the static array (every call rewrites what it uses)
+  // AO direction table (src/Render3D.cpp:272-313) in the static array: uploaded only when the
+  // scene's AO quality differs from the table the array already holds, so a frame loop at one
+  // quality copies it once. The copy reads pageable host memory, which the runtime stages
+  // before cudaMemcpyAsync returns, so the host array is free again without a stream sync.
   int aoCount = 0;
   {
     std::lock_guard<std::mutex> lk(g_ao_mu);
-    aoCount = mbgb::ao_vectors_into(scene->globalIlumQuality, g_ao_host, kMaxAOVectors);
-    e = cudaMemcpyAsync(d->ao, g_ao_host, sizeof(float) * 3 * (size_t)(aoCount > 0 ? aoCount : 1),
-                        cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // the host staging buffer is reused by the next call
+    if (d->aoQuality != scene->globalIlumQuality) {
+      const int n = mbgb::ao_vectors_into(scene->globalIlumQuality, g_ao_host, kMaxAOVectors);
+      e = cudaMemcpyAsync(d->ao, g_ao_host, sizeof(float) * 3 * (size_t)(n > 0 ? n : 1), cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) {
+        d->aoQuality = -1;
+        return mbgb::set_error(MBGB_ERR_CUDA, std::string("AO table copy: ") + cudaGetErrorString(e));
+      }
+      d->aoQuality = scene->globalIlumQuality;
+      d->aoCount = n;
+    }
+    aoCount = d->aoCount;
   }
-  if (e != cudaSuccess) return mbgb::set_error(MBGB_ERR_CUDA, std::string("AO table copy: ") + cudaGetErrorString(e));
 
   // counters, tile counter, overflow count and flags must start at zero on every call
   e = cudaMemsetAsync(d->control, 0, sizeof(g_na_control), s);

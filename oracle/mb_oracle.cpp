@@ -1770,9 +1770,20 @@ void oracle_colour_value(const mbgb_scene *s, const double *pts, long n, double 
 // counter (the reference's one-worker-per-core row claiming). jitter != 0 uses
 // the C library's shared rand() stream, as the reference does.
 // counters (may be NULL): [0] orbit iterations, [1] DE calls, [2] march steps.
+// Rows [row0, row1), or the `nlist` rows of `list` when it is not NULL, claimed one at a
+// time by `threads` workers (the reference's dynamic row claiming, src/Render3D.cpp:815-849).
 static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
-                       unsigned long long *counters, bool exact) {
-  if (!s || !img || row0 < 0 || row1 > img->height || row0 > row1) return 1;
+                       unsigned long long *counters, bool exact, const int *list = nullptr, int nlist = 0) {
+  if (!s || !img) return 1;
+  if (list) {
+    if (nlist < 0) return 1;
+    for (int i = 0; i < nlist; i++)
+      if (list[i] < 0 || list[i] >= img->height) return 1;
+    row0 = 0;
+    row1 = nlist;
+  } else if (row0 < 0 || row1 > img->height || row0 > row1) {
+    return 1;
+  }
   Frame f;
   setup_frame(*s, f);
   f.exact = exact;
@@ -1783,8 +1794,9 @@ static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int 
     const int rays = 1 + ((s->raytracedReflections && s->reflectionsMax > 0) ? s->reflectionsMax : 0);
     std::vector<std::vector<Step>> bufs((size_t)rays, std::vector<Step>(10002));
     for (;;) {
-      const int y = next.fetch_add(1);
-      if (y >= row1) break;
+      const int k = next.fetch_add(1);
+      if (k >= row1) break;
+      const int y = list ? list[k] : k;
       for (int x = 0; x < img->width; x++) render_pixel(f, x, y, bufs, jitter != 0, img, cnts[t]);
     }
   };
@@ -1979,6 +1991,13 @@ void oracle_dof(int w, int h, const float *zbuffer, unsigned short *alpha, unsig
 int oracle_render(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
                   unsigned long long *counters) {
   return render_rows(s, row0, row1, jitter, threads, img, counters, false);
+}
+
+// The render of an explicit list of rows (the CPU baseline's sample spread over a frame).
+int oracle_render_row_list(const mbgb_scene *s, const int *rows, int nrows, int jitter, int threads,
+                           const mbgb_image *img, unsigned long long *counters) {
+  if (!rows) return 1;
+  return render_rows(s, 0, 0, jitter, threads, img, counters, false, rows, nrows);
 }
 
 // The same render with every hit moved onto the level set DE(P) = thr after the

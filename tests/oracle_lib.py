@@ -57,6 +57,46 @@ def colour_value(lib, scene, points: np.ndarray):
     return out
 
 
+LAYERS = (("image_float", np.float32, 3), ("zbuffer", np.float32, 1), ("alpha", np.uint16, 1),
+          ("opacity", np.uint16, 1), ("colour", np.uint8, 3), ("hit", np.uint8, 1), ("iters", np.int32, 1),
+          ("depth", np.float64, 1))
+
+
+class RawImage(ctypes.Structure):
+    """mbgb_image (include/mbgb.h) for callers that do not load the product package."""
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32)] + [(n, ctypes.c_void_p) for n, _, _ in LAYERS]
+
+
+def sample_rows(height: int, n: int) -> list:
+    """`n` rows spread evenly over a frame of `height` rows (the CPU baseline's sample)."""
+    n = max(1, min(n, height))
+    return sorted({int((i + 0.5) * height / n) for i in range(n)})
+
+
+def alloc_layers(width: int, height: int) -> dict:
+    return {n: np.zeros(width * height * c, dt) for n, dt, c in LAYERS}
+
+
+def render_row_list(lib, scene_ptr: int, width: int, height: int, rows, jitter=False, threads=None, layers=None):
+    """Renders the listed rows of a frame on the CPU into numpy layers (`layers` from
+    alloc_layers, or new ones); `scene_ptr` is the address of an mbgb_scene (a ctypes struct
+    or a buffer holding its bytes). Returns (layers dict, counters). Loads nothing but the
+    oracle library."""
+    if layers is None:
+        layers = alloc_layers(width, height)
+    img = RawImage(width, height, *[layers[n].ctypes.data_as(ctypes.c_void_p) for n, _, _ in LAYERS])
+    rl = np.ascontiguousarray(rows, np.int32)
+    cnt = np.zeros(3, np.uint64)
+    lib.oracle_render_row_list.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.oracle_render_row_list.restype = ctypes.c_int
+    rc = lib.oracle_render_row_list(scene_ptr, _p(rl), len(rl), int(jitter), threads or os.cpu_count() or 1,
+                                    ctypes.addressof(img), _p(cnt))
+    if rc != 0:
+        raise RuntimeError("oracle_render_row_list rejected its arguments")
+    return layers, cnt
+
+
 def render(lib, scene, rows=None, jitter=False, threads=None):
     """Renders the scene on the CPU; returns (CImage, counters)."""
     import mandelbulber_gb300 as mb

@@ -59,14 +59,25 @@ def test_noalloc_matches_render_device_on_two_calls(mblib):
             ctx.render_device(sc, {k: v.data_ptr() for k, v in layers.items()}, precision=mb.PREC_FP32_FIX)
             torch.cuda.synchronize()
             refs.append(_to_image(layers, w, h))
+        # The first scene must send rays through the overflow pass, whose records and pixel
+        # list are static arrays too. The context's per-pixel engine keeps 1024 records per
+        # ray before it overflows, the allocation-free one 256, so a long ray there is one here.
+        ctx.render(scenes[0], precision=mb.PREC_FP32_FIX, engine=mb.ENGINE_PER_PIXEL)
+        assert ctx.stats().long_rays > 0
     opts = mb.make_opts(precision=mb.PREC_FP32_FIX)
-    for sc, ref in zip(scenes, refs):       # two calls in a row share the static scratch
+    for call, (sc, ref) in enumerate(zip(scenes, refs)):   # two calls in a row share the static scratch
         w, h = sc.image_width, sc.image_height
         layers = _device_layers(w, h, 0xA5)  # garbage: every pixel must be written
         img_c = _c_image(layers, w, h)
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc = lib.mbgb_render_device_noalloc(ctypes.byref(sc), ctypes.byref(img_c), ctypes.byref(opts))
         assert rc == 0, lib.mbgb_last_error()
         torch.cuda.synchronize()
+        if call > 0:
+            # after the first call (which may load the module that holds the static arrays)
+            # the entry point takes no device memory at all
+            assert torch.cuda.mem_get_info()[0] == free_before
         got = _to_image(layers, w, h)
         m = metrics.compare(got, ref)
         assert m["hit_mismatch"] <= 0.001 and m["psnr_float"] >= 45.0, m
@@ -83,6 +94,7 @@ def test_noalloc_rejects_what_its_scratch_cannot_hold(mblib):
     assert b"4194304 pixels" in lib.mbgb_last_error()
     small = W.workload("mandelbox_1080p", 64, 36)
     img = mb.mbgb_image(64, 36, *([None] * 8))
-    opts = mb.make_opts(precision=mb.PREC_FP64)
-    assert lib.mbgb_render_device_noalloc(ctypes.byref(small), ctypes.byref(img), ctypes.byref(opts)) == 1
-    assert b"FP32_FIX" in lib.mbgb_last_error()
+    for prec in (mb.PREC_FP64, mb.PREC_AUTO):   # AUTO may pick FP64, which this entry point does not carry
+        opts = mb.make_opts(precision=prec)
+        assert lib.mbgb_render_device_noalloc(ctypes.byref(small), ctypes.byref(img), ctypes.byref(opts)) == 1
+        assert b"FP32_FIX" in lib.mbgb_last_error()
