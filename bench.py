@@ -39,10 +39,11 @@ WORKLOAD = "mandelbox_1080p"
 # 3 fold add/sub + 5 for x^2+y^2+z^2 + 5 sphere fold (1 div) + 6 for z*scale+c + 2 for DE*|s|+1,
 # plus sqrt and divide of each DE evaluation
 FLOPS_PER_ITER = {8: 21, 2: 27}
-# dram__bytes_read.sum + dram__bytes_write.sum of secondary_kernel per 1080p launch: an ncu
-# --set full capture at 480x270 read 2.36 MB and wrote 256 B; the traffic is the per-hit
-# inputs and AO slots, so it scales with the pixel count (x16)
-DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 37.8e6}
+# dram__bytes_read.sum + dram__bytes_write.sum of secondary_kernel in one full 1920x1080
+# launch of this workload (a one-pass ncu capture of `bench.py --once 1920x1080`): 49.2 MB
+# read + 167.2 MB written, mostly the per-direction AO result slots, which outgrow L2 at
+# this size (at 480x270 they stay in L2, and a small capture sees almost no DRAM traffic)
+DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 216.4e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
 PRECISION = "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement"
 # the single-frame workloads bench.py times (the scenes are built by mandelbulber_gb300.workloads;

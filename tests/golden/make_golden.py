@@ -19,6 +19,13 @@ the tests rebuild the exact input without the reference tree.
     python tests/golden/make_golden.py formulas # the trig_DE / menger / vary4D fixtures only
     python tests/golden/make_golden.py all_formulas # every other formula: DE fixtures, example
                                                 # scenes (share/examples) and synthetic scenes
+    python tests/golden/make_golden.py settings # every shipped settings file as the reference
+                                                # reads it, and the bench workloads' scenes
+
+Every scene is read by the reference's own settings code (src/settings.cpp compiled in
+place into oracle/_ref/libmbref_settings.so) and the -nogui derivations, never by this
+build's reader: the parity tests then inherit no parsing of this build. The reference tree
+is found through oracle/Makefile (MBGB_REF_TREE).
 """
 from __future__ import annotations
 
@@ -36,6 +43,7 @@ sys.path.insert(0, ROOT)
 
 import mandelbulber_gb300 as mb  # noqa: E402
 from mandelbulber_gb300 import workloads as W  # noqa: E402
+from tests import oracle_lib  # noqa: E402
 
 # Small frames covering the hot-path features; the keys are applied on top of a workload.
 CASES = {
@@ -308,14 +316,74 @@ FORMULA_DE_ALL = (
       "IFS_absX": 1, "IFS_absY": 1, "IFS_absZ": 1}, 2.0),
 )
 
-DEFAULTS_FILE = "/root/reference/share/defaults"
-EXAMPLES_DIR = "/root/reference/share/examples"
+REF_TREE = oracle_lib.ref_tree()
+DEFAULTS_FILE = os.path.join(REF_TREE, "share", "defaults")
+EXAMPLES_DIR = os.path.join(REF_TREE, "share", "examples")
+KEYFRAMES_DIR = os.path.join(REF_TREE, "share", "exampleKeyframes")
+
+
+def ref_settings_lib():
+    lib = oracle_lib.load_ref_settings()
+    if lib is None:
+        raise SystemExit(f"the reference tree is not at {REF_TREE} (set MBGB_REF_TREE)")
+    return lib
+
+
+def make_scene(overrides: dict) -> mb.mbgb_scene:
+    """The scene of a key list (the workload base updated with `overrides`) as the
+    reference's own LoadOneSetting / LoadSettingsPost and the -nogui derivations read it."""
+    keys = dict(W.BASE)
+    keys.update(overrides)
+    return oracle_lib.ref_scene_from_keys(ref_settings_lib(), mb.mbgb_scene(), keys)
+
+
+def workload_scene(name: str, w: int | None = None, h: int | None = None) -> mb.mbgb_scene:
+    keys = dict(W.WORKLOADS[name])
+    if w and h:
+        keys["image_width"], keys["image_height"] = w, h
+        keys["perspective"] = W.fov_persp(w, h)
+    return make_scene(keys)
 
 
 def example_scene(fname: str, extra: dict, w: int = 48, h: int = 32):
+    """An example file read by the reference's own LoadSettings2 after share/defaults."""
     ov = [f"image_width {w}", f"image_height {h}", "post_SSAO_enabled 0"]
     ov += [f"{k} {v}" for k, v in extra.items()]
-    return mb.load_settings(os.path.join(EXAMPLES_DIR, fname), DEFAULTS_FILE, ov)
+    return oracle_lib.ref_scene_from_settings(ref_settings_lib(), mb.mbgb_scene(), DEFAULTS_FILE,
+                                              os.path.join(EXAMPLES_DIR, fname), ov)
+
+
+def settings_files() -> list:
+    """share/defaults, every share/examples/*.fract and every share/exampleKeyframes/*.fract."""
+    ex = sorted(f for f in os.listdir(EXAMPLES_DIR) if f.endswith(".fract"))
+    kf = sorted(f for f in os.listdir(KEYFRAMES_DIR) if f.endswith(".fract"))
+    return ([("defaults", DEFAULTS_FILE)] + [("examples/" + f, os.path.join(EXAMPLES_DIR, f)) for f in ex]
+            + [("exampleKeyframes/" + f, os.path.join(KEYFRAMES_DIR, f)) for f in kf])
+
+
+def settings_goldens(manifest: dict):
+    """settings_reference.npz: each shipped settings file as the reference reads it (after
+    share/defaults, as LoadSettings does), with the SHA-256 of the file it read;
+    bench_scenes.npz: the bench workloads' scenes as the reference reads their key lists."""
+    import hashlib
+    lib = ref_settings_lib()
+    names, shas, blobs = [], [], []
+    for name, path in settings_files():
+        sc = oracle_lib.ref_scene_from_settings(lib, mb.mbgb_scene(), None if name == "defaults" else DEFAULTS_FILE,
+                                                path)
+        with open(path, "rb") as f:
+            shas.append(hashlib.sha256(f.read()).hexdigest())
+        names.append(name)
+        blobs.append(np.frombuffer(mb.scene_bytes(sc), np.uint8))
+    np.savez_compressed(os.path.join(HERE, "settings_reference.npz"), names=np.array(names), sha256=np.array(shas),
+                        scenes=np.stack(blobs))
+    manifest["settings_reference.npz"] = {"files": len(names), "reader": "src/settings.cpp LoadSettings2 "
+                                          "(oracle/_ref/libmbref_settings.so) + -nogui derivations"}
+    bench = {n: np.frombuffer(mb.scene_bytes(workload_scene(n)), np.uint8) for n in ("mandelbox_1080p",
+                                                                                      "mandelbulb_640x480")}
+    np.savez_compressed(os.path.join(HERE, "bench_scenes.npz"), **bench)
+    manifest["bench_scenes.npz"] = {"workloads": sorted(bench), "reader": "src/settings.cpp LoadOneSetting"}
+    print(len(names), "settings files;", "bench scenes", sorted(bench))
 
 
 def render_example_cases(lib, manifest: dict, only=None):
@@ -349,7 +417,7 @@ def formula_de_all(lib, manifest: dict, npts: int = 400):
             keys["image_width"], keys["image_height"] = 64, 48
             keys["perspective"] = W.fov_persp(64, 48)
             keys.update(extra)
-            sc = W.make_scene(keys)
+            sc = make_scene(keys)
         pts = np.ascontiguousarray(rng.uniform(-half, half, (npts, 3)))
         detail = np.ascontiguousarray(10.0 ** rng.uniform(-6, -2, npts))
         dist = np.zeros(npts)
@@ -400,7 +468,7 @@ def main():
     manifest = {}
     for formula, wl in (("mandelbulb", "mandelbulb_640x480"), ("mandelbox", "mandelbox_1080p")):
         rng = np.random.default_rng(1234 if formula == "mandelbulb" else 5678)
-        sc = W.workload(wl, 64, 48)
+        sc = workload_scene(wl, 64, 48)
         pts = np.ascontiguousarray(de_points(formula, rng))
         n = len(pts)
         detail = np.ascontiguousarray(10.0 ** rng.uniform(-6, -2, n))
@@ -419,7 +487,7 @@ def main():
         keys["image_width"], keys["image_height"] = w, h
         keys["perspective"] = W.fov_persp(w, h)
         keys.update(extra)
-        sc = W.make_scene(keys)
+        sc = make_scene(keys)
         img = mb.CImage.empty(w, h)
         lib.ref_render(ctypes.byref(sc), 0, h, 0, ctypes.byref(img.as_c()))
         out = os.path.join(HERE, f"render_{case}.npz")
@@ -535,7 +603,7 @@ def formula_goldens(manifest: dict):
         keys["image_width"], keys["image_height"] = 64, 48
         keys["perspective"] = W.fov_persp(64, 48)
         keys.update(extra)
-        sc = W.make_scene(keys)
+        sc = make_scene(keys)
         pts = np.ascontiguousarray(rng.uniform(-half, half, (2000, 3)))
         n = len(pts)
         detail = np.ascontiguousarray(10.0 ** rng.uniform(-6, -2, n))
@@ -566,7 +634,7 @@ def render_cases(lib, cases: dict, manifest: dict):
         keys["image_width"], keys["image_height"] = w, h
         keys["perspective"] = W.fov_persp(w, h)
         keys.update(extra)
-        sc = W.make_scene(keys)
+        sc = make_scene(keys)
         img = mb.CImage.empty(w, h)
         lib.ref_render(ctypes.byref(sc), 0, h, 0, ctypes.byref(img.as_c()))
         out = os.path.join(HERE, f"render_{case}.npz")
@@ -580,11 +648,11 @@ def render_cases(lib, cases: dict, manifest: dict):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"], ["effects"], ["dof"]):
+    if sys.argv[1:] in (["post"], ["formulas"], ["all_formulas"], ["effects"], ["dof"], ["settings"]):
         with open(os.path.join(HERE, "MANIFEST.json")) as f:
             manifest = json.load(f)
         {"post": post_goldens, "formulas": formula_goldens, "all_formulas": all_formula_goldens,
-         "effects": effect_goldens, "dof": dof_goldens}[sys.argv[1]](manifest)
+         "effects": effect_goldens, "dof": dof_goldens, "settings": settings_goldens}[sys.argv[1]](manifest)
         with open(os.path.join(HERE, "MANIFEST.json"), "w") as f:
             json.dump(manifest, f, indent=1, sort_keys=True)
     else:

@@ -35,6 +35,59 @@ def load(fast: bool = False) -> ctypes.CDLL:
     return lib
 
 
+def ref_tree() -> str:
+    """Where the reference tree lies (MBGB_REF_TREE, else oracle/Makefile's default)."""
+    env = os.environ.get("MBGB_REF_TREE")
+    if env:
+        return env
+    return subprocess.check_output(["make", "-s", "-C", ORACLE_DIR, "print-ref-tree"], text=True).strip()
+
+
+def load_ref_settings():
+    """The reference's own settings reader (oracle/_ref/libmbref_settings.so, built from the
+    reference tree in place), or None where the tree is absent."""
+    if "settings" in _cache:
+        return _cache["settings"]
+    lib = None
+    if os.path.isfile(os.path.join(ref_tree(), "src", "settings.cpp")):
+        subprocess.check_call(["make", "-s", "-C", ORACLE_DIR, "ref"])
+        lib = ctypes.CDLL(os.path.join(ORACLE_DIR, "_ref", "libmbref_settings.so"))
+        vp = ctypes.c_void_p
+        lib.ref_scene_from_settings.argtypes = [ctypes.c_char_p, ctypes.c_char_p, vp, ctypes.c_int, vp]
+        lib.ref_scene_from_settings.restype = ctypes.c_int
+        lib.ref_scene_from_keys.argtypes = [vp, vp, ctypes.c_int, vp]
+        lib.ref_scene_from_keys.restype = ctypes.c_int
+    _cache["settings"] = lib
+    return lib
+
+
+def settings_value(v) -> str:
+    """A settings value as the workload builder writes it (floats by repr)."""
+    return repr(float(v)) if isinstance(v, float) else str(v)
+
+
+def ref_scene_from_settings(lib, scene, defaults, path, overrides=()):
+    """Fills the ctypes mbgb_scene `scene` through the reference's LoadSettings2 of the
+    defaults file and `path` (each followed by the overrides) + the -nogui derivations."""
+    ov = [o.encode() for o in overrides]
+    arr = (ctypes.c_char_p * max(1, len(ov)))(*ov)
+    rc = lib.ref_scene_from_settings(defaults.encode() if defaults else None, path.encode(), arr, len(ov),
+                                     ctypes.addressof(scene))
+    if rc != 0:
+        raise RuntimeError(f"the reference's LoadSettings2 could not read {path}")
+    return scene
+
+
+def ref_scene_from_keys(lib, scene, keys: dict):
+    """Fills `scene` through the reference's LoadOneSetting of each key (in order) on a
+    zeroed sParamRender, LoadSettingsPost and the -nogui derivations."""
+    ks = [k.encode() for k in keys]
+    vs = [settings_value(v).encode() for v in keys.values()]
+    lib.ref_scene_from_keys((ctypes.c_char_p * len(ks))(*ks), (ctypes.c_char_p * len(vs))(*vs), len(ks),
+                            ctypes.addressof(scene))
+    return scene
+
+
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
