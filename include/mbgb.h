@@ -241,6 +241,9 @@ typedef struct mbgb_opts {
                                 * have ended their orbits, then steps those rays on; 0 = tuned, else 8
                                 * for the Mandelbulb and off for the Mandelbox (short orbits); -1 = off:
                                 * lanes step on only after every orbit of the estimate ended */
+  int32_t pair_rays;           /* wavefront, lean FP32 Mandelbox (orbit_refill off), shadow/AO rays: 0 = two
+                                * rays per thread whose orbits advance together in packed FP32 (f32x2)
+                                * instructions; -1 = one ray per thread. Same pixels either way */
 } mbgb_opts;
 
 /* Launch configuration picked by mbgb_autotune. */

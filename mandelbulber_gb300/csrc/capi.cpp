@@ -592,6 +592,7 @@ struct LaunchCfg {
   int refill = 8;
   int orbitRefill = -1;                 // ended lean orbits before a warp steps them on (0 = off,
                                         // -1 = by scene: on for the power-8 Mandelbulb's long orbits)
+  bool pairRays = true;                 // lean FP32 Mandelbox shadow/AO rays two per thread (packed f32x2)
 };
 
 // Scene class an autotuned configuration applies to.
@@ -992,6 +993,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
   if (o.ctas_per_sm > 0) cfg.ctasPerSm = o.ctas_per_sm;
   if (o.refill_min > 0) cfg.refill = o.refill_min;
   if (o.orbit_refill != 0) cfg.orbitRefill = o.orbit_refill < 0 ? 0 : o.orbit_refill;
+  if (o.pair_rays < 0) cfg.pairRays = false;
   // Orbit-granular refill pays where orbit lengths spread widely (Mandelbulb, N up to
   // hundreds); the Mandelbox's short orbits (bailout 1024 within ~15 iterations) lose more
   // to the extra step passes than they gain (measured at 1080p: 11.2 ms per-estimate
@@ -1087,12 +1089,15 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.orbit_refill = g.cfg.orbitRefill;
   wb.exact_hit = o.exact_hit ? 1 : 0;
   wb.npix = g.npix;
+  // shadow/AO rays two per thread (secondary_pair_kernel): the lean FP32 Mandelbox with
+  // per-estimate refill, which the pair kernel's packed orbit serves
+  wb.pair_rays = (sizeof(T) == 4 && fast_mandelbox(scene) && g.cfg.pairRays && g.cfg.orbitRefill <= 0) ? 1 : 0;
   MBGB_CUDA(cudaMemsetAsync(ctl, 0, 64, s));
 
   const int block = g.cfg.block;
   const int kf = kernel_formula(scene.formula, scene.ifsFoldingMode);
   int occ1 = std::max(1, wave_occupancy<T>(kf, block, 0));
-  int occ2 = std::max(1, wave_occupancy<T>(kf, block, 1));
+  int occ2 = std::max(1, wave_occupancy<T>(kf, block, wb.pair_rays ? 2 : 1));
   if (g.cfg.ctasPerSm > 0) {
     occ1 = std::min(occ1, g.cfg.ctasPerSm);
     occ2 = std::min(occ2, g.cfg.ctasPerSm);
@@ -1275,6 +1280,7 @@ static mbgb_status check_opts(const mbgb_opts &o) {
     return set_error(MBGB_ERR_BAD_PARAM, "tile_w x tile_h must be 32");
   if (o.refill_min < 0 || o.refill_min > 32) return set_error(MBGB_ERR_BAD_PARAM, "refill_min must be in [0, 32]");
   if (o.orbit_refill < -1 || o.orbit_refill > 32) return set_error(MBGB_ERR_BAD_PARAM, "orbit_refill must be in [-1, 32]");
+  if (o.pair_rays < -1 || o.pair_rays > 0) return set_error(MBGB_ERR_BAD_PARAM, "pair_rays must be 0 or -1");
   if (o.ctas_per_sm < 0) return set_error(MBGB_ERR_BAD_PARAM, "negative ctas_per_sm");
   if (o.row_begin < 0 || o.row_end < 0) return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
   return MBGB_OK;

@@ -61,5 +61,90 @@ __device__ __forceinline__ float box_iteration(const LeanBoxK &k, const float s,
   return norm2_rn(x, y, z);
 }
 
+// ---- Packed FP32 (f32x2): two orbits per thread ----
+// A pair of floats in one 64-bit register pair: low half = ray A, high half = ray B. The
+// f32x2 add / mul / fma each round both halves exactly as the scalar .rn instructions do,
+// in one issue slot; min/max, saturation and the MUFU reciprocal have no packed form and
+// stay scalar per half.
+using f2 = unsigned long long;
+
+__device__ __forceinline__ f2 f2_pack(const float lo, const float hi) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float f2_lo(const f2 v) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  return lo;
+}
+__device__ __forceinline__ float f2_hi(const f2 v) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  return hi;
+}
+__device__ __forceinline__ f2 f2_fma(const f2 a, const f2 b, const f2 c) {
+  f2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ f2 f2_mul(const f2 a, const f2 b) {
+  f2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
+// The state of two lean Mandelbox orbits, kept NEGATED (nx = -x, ncx = -cx): f32x2 has no
+// operand negation, and with the sign folded into the state every step of box_iteration is
+// one packed FMA that rounds exactly as its scalar counterpart:
+//   fold   clamp(-x) = -clamp(x) (the clamp interval is symmetric), so
+//          fma(clamp(nx), -2, nx) = round(2 clamp(x) - x), the scalar fold (positive form);
+//   scale  fma(x, -ks, -cx) = -round(x ks + cx) (round to nearest is odd-symmetric), with
+//          -ks = fma(t, -s(k1-1), -s);
+//   dr     |ks| = fma(t, |s(k1-1)|, |s|): s and s(k1-1) share a sign (k1 >= 1), so this is
+//          |fma(t, s(k1-1), s)| exactly.
+// Squared radii are sign-free. Per ray (half): -s, -s(k1-1), |s|, |s(k1-1)|.
+struct BoxPair {
+  f2 nx, ny, nz, dr, ncx, ncy, ncz;
+  f2 ns, nskm1, as, askm1;
+};
+
+__device__ __forceinline__ void box_pair_start(BoxPair &o, const LeanBoxK &k, const float cf, const float pxA,
+                                               const float pyA, const float pzA, const float sA, const float pxB,
+                                               const float pyB, const float pzB, const float sB) {
+  o.nx = f2_pack(-pxA, -pxB);
+  o.ny = f2_pack(-pyA, -pyB);
+  o.nz = f2_pack(-pzA, -pzB);
+  o.ncx = f2_pack(-__fmul_rn(pxA, cf), -__fmul_rn(pxB, cf));
+  o.ncy = f2_pack(-__fmul_rn(pyA, cf), -__fmul_rn(pyB, cf));
+  o.ncz = f2_pack(-__fmul_rn(pzA, cf), -__fmul_rn(pzB, cf));
+  o.dr = f2_pack(1.0f, 1.0f);
+  const float skA = __fmul_rn(sA, k.km1), skB = __fmul_rn(sB, k.km1);
+  o.ns = f2_pack(-sA, -sB);
+  o.nskm1 = f2_pack(-skA, -skB);
+  o.as = f2_pack(fabsf(sA), fabsf(sB));
+  o.askm1 = f2_pack(fabsf(skA), fabsf(skB));
+}
+
+// One iteration of both orbits (box_iteration per half, bit for bit); returns both new
+// squared radii.
+__device__ __forceinline__ f2 box_iteration_x2(const LeanBoxK &k, BoxPair &o) {
+  const float fl = k.fl;
+  const f2 m2 = f2_pack(-2.0f, -2.0f), one = f2_pack(1.0f, 1.0f);
+  const f2 cx = f2_pack(fminf(fmaxf(f2_lo(o.nx), -fl), fl), fminf(fmaxf(f2_hi(o.nx), -fl), fl));
+  const f2 cy = f2_pack(fminf(fmaxf(f2_lo(o.ny), -fl), fl), fminf(fmaxf(f2_hi(o.ny), -fl), fl));
+  const f2 cz = f2_pack(fminf(fmaxf(f2_lo(o.nz), -fl), fl), fminf(fmaxf(f2_hi(o.nz), -fl), fl));
+  const f2 x = f2_fma(cx, m2, o.nx), y = f2_fma(cy, m2, o.ny), z = f2_fma(cz, m2, o.nz);
+  const f2 r2 = f2_fma(z, z, f2_fma(y, y, f2_mul(x, x)));
+  const f2 t = f2_pack(__saturatef(fmaf(k.sa, rcp_approx(f2_lo(r2)), -k.sb)),
+                       __saturatef(fmaf(k.sa, rcp_approx(f2_hi(r2)), -k.sb)));
+  const f2 nks = f2_fma(t, o.nskm1, o.ns), aks = f2_fma(t, o.askm1, o.as);
+  o.nx = f2_fma(x, nks, o.ncx);
+  o.ny = f2_fma(y, nks, o.ncy);
+  o.nz = f2_fma(z, nks, o.ncz);
+  o.dr = f2_fma(o.dr, aks, one);
+  return f2_fma(o.nz, o.nz, f2_fma(o.ny, o.ny, f2_mul(o.nx, o.nx)));
+}
+
 }  // namespace dev
 }  // namespace mbgb

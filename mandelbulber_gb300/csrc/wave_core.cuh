@@ -1155,6 +1155,126 @@ __device__ __forceinline__ void secondary_lean(const ParamsT<float> &p, const Fr
   }
 }
 
+// Two lean Mandelbox orbits at once (mandelbox_fast for each of two points, bit for bit):
+// the packed iteration box_iteration_x2 advances both until both have ended. A ray whose
+// squared radius passes the bailout keeps iterating with the other (its half of the packed
+// state is ignored from then on); its distance and end iteration are taken at its bailout,
+// and its bailout bound becomes +inf so that it never triggers again. Returns the two
+// distances (0 for an orbit that reached N) and end iterations (N when no bailout).
+__device__ __forceinline__ void mandelbox_fast_x2(const FractalT<float> &f, const V3<float> a, const float sA,
+                                                  const V3<float> b, const float sB, const int N, float &dA,
+                                                  int &LA, float &dB, int &LB) {
+  const LeanBoxK k = lean_box_k(f);
+  BoxPair o;
+  box_pair_start(o, k, f.constantFactor, a.x, a.y, a.z, sA, b.x, b.y, b.z, sB);
+  const float kInf = __int_as_float(0x7f800000);
+  float thA = 1048576.0f, thB = 1048576.0f;
+  dA = dB = 0.0f;
+  LA = LB = N;
+#pragma unroll 5
+  for (int L = 0; L < N; L++) {
+    const f2 r2 = box_iteration_x2(k, o);
+    const float r2A = f2_lo(r2), r2B = f2_hi(r2);
+    if (r2A > thA || r2B > thB) {
+      if (r2A > thA) {
+        dA = box_bailout_dist(r2A, f2_lo(o.dr));
+        LA = L;
+        thA = kInf;
+      }
+      if (r2B > thB) {
+        dB = box_bailout_dist(r2B, f2_hi(o.dr));
+        LB = L;
+        thB = kInf;
+      }
+      if (thA == kInf && thB == kInf) break;
+    }
+  }
+}
+
+// Shadow / AO rays of the lean FP32 Mandelbox two per thread (slots 0 and 1), so that the
+// orbit iterations of both run as packed f32x2 instructions (one issue slot for two FMAs;
+// the stage is issue-bound). Each slot follows secondary_kernel's per-estimate loop: a
+// distance estimate, then the ray's step (secondary_step), refills when 2 x refill_min of
+// the warp's 64 slots are idle (one atomicAdd for all of them: slot-0 jobs first, then
+// slot-1 jobs). An idle slot's orbit repeats the other slot's point and is discarded.
+// Results are bit-identical to secondary_kernel's: the same orbit values, clamps and steps.
+// (A template, so that every translation unit that includes this header may instantiate it.)
+template <int FORMULA>
+__global__ void __launch_bounds__(128) secondary_pair_kernel(const __grid_constant__ ParamsT<float> p,
+                                                             const FrameIO io, const WaveBufs<float> wb,
+                                                             const FrameCam<float> *__restrict__ cams,
+                                                             const int ncams) {
+  static_assert(FORMULA == 8, "the packed orbit is the lean Mandelbox's");
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  const unsigned int nShadow = p.shadow ? nh : 0u;
+  const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
+  const unsigned int njobs = nShadow + nAO;
+  const unsigned int lane = threadIdx.x & 31u;
+  const int N = p.f.N, minN = p.f.minN;
+  Counters cnt{0, 0, 0, 0};
+  SecondaryRay<float> s0{}, s1{};
+  bool act0 = false, act1 = false, exhausted = false;
+  for (;;) {
+    const bool need0 = !act0 && !exhausted, need1 = !act1 && !exhausted;
+    const unsigned int m0 = __ballot_sync(0xffffffffu, need0), m1 = __ballot_sync(0xffffffffu, need1);
+    const unsigned int idle = (unsigned int)(__popc(m0) + __popc(m1));
+    if (idle && (idle >= 2u * (unsigned int)wb.refill_min || !__any_sync(0xffffffffu, act0 || act1))) {
+      if (io.budget_ns && lane == 0 && deadline_passed(io)) atomicExch(io.error_flag, 1);
+      // the flag is only ever set by an expired deadline: no read (an L2 round trip) without one
+      const bool stop = io.budget_ns && *(volatile int *)io.error_flag != 0;
+      unsigned int base = 0;
+      const unsigned int leader = (unsigned int)(__ffs(m0 | m1) - 1);
+      if (lane == leader) base = atomicAdd(wb.ctl + 2, idle);
+      base = __shfl_sync(0xffffffffu, base, leader);
+      const unsigned int below = (1u << lane) - 1u;
+      const unsigned int job0 = base + (unsigned int)__popc(m0 & below);
+      const unsigned int job1 = base + (unsigned int)__popc(m0) + (unsigned int)__popc(m1 & below);
+      if (need0) {
+        if (stop || job0 >= njobs) exhausted = true;
+        else act0 = secondary_begin(p, wb, cams, ncams, nh, nShadow, job0, s0);
+      }
+      if (need1) {
+        if (stop || job1 >= njobs) exhausted = true;
+        else act1 = secondary_begin(p, wb, cams, ncams, nh, nShadow, job1, s1);
+      }
+    }
+    if (!__any_sync(0xffffffffu, act0 || act1)) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    if (act0 || act1) {
+      const V3<float> q0 = act0 ? ray_at(s0.point, s0.dir, s0.r) : ray_at(s1.point, s1.dir, s1.r);
+      const V3<float> q1 = act1 ? ray_at(s1.point, s1.dir, s1.r) : q0;
+      const float f0 = act0 ? s0.fpar : s1.fpar, f1 = act1 ? s1.fpar : f0;
+      float d0, d1;
+      int L0, L1;
+      mandelbox_fast_x2(p.f, q0, f0, q1, f1, N, d0, L0, d1, L1);
+      if (act0) {   // wave_distance's clamps, then the ray's step
+        cnt.orbit += (unsigned long long)(L0 + 1);
+        cnt.calls += 1;
+        if (d0 < 0.0f) d0 = 0.0f;
+        if (L0 < minN && d0 < s0.detail) d0 = s0.detail;
+        if (secondary_step(p, wb, s0, d0, L0 == N)) act0 = false;
+      }
+      if (act1) {
+        cnt.orbit += (unsigned long long)(L1 + 1);
+        cnt.calls += 1;
+        if (d1 < 0.0f) d1 = 0.0f;
+        if (L1 < minN && d1 < s1.detail) d1 = s1.detail;
+        if (secondary_step(p, wb, s1, d1, L1 == N)) act1 = false;
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+  }
+}
+
 template <typename T, int FORMULA, bool FAST>
 __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                         const FrameCam<T> *__restrict__ cams, const int ncams) {

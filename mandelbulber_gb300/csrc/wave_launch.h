@@ -42,6 +42,8 @@ struct WaveBufs {
   int orbit_refill;                      // lean FP32 orbits, shadow/AO stage: ended orbits of a warp
                                          // before those lanes step on; 0 = refill per distance estimate
   int exact_hit;                         // 1: hits are refined in FP64 to the level set DE = thr
+  int pair_rays;                         // lean FP32 Mandelbox, shadow/AO stage: 1 = two rays per
+                                         // thread with packed f32x2 orbits (secondary_pair_kernel)
   int64_t npix;
 };
 

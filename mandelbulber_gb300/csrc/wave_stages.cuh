@@ -24,7 +24,13 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   if (L.wb.exact_hit)
     dev::level_set_kernel<T, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
   mark(3);
-  dev::secondary_kernel<T, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
+  bool pair = false;
+  if constexpr (sizeof(T) == 4 && F == 8 && FAST) pair = L.wb.pair_rays && L.wb.orbit_refill <= 0;
+  if constexpr (sizeof(T) == 4 && F == 8 && FAST) {
+    if (pair) dev::secondary_pair_kernel<8><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
+  }
+  if (!pair)
+    dev::secondary_kernel<T, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
   mark(4);
   dev::compose_kernel<T, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
   mark(5);
@@ -38,8 +44,14 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
 template <typename T, int F, bool FAST>
 int stage_occupancy(int block, int which) {
   int n = 0;
-  if (which == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<T, F, FAST>, block, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<T, F, FAST>, block, 0);
+  if (which == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::primary_kernel<T, F, FAST>, block, 0);
+  } else if (which == 2) {   // the two-rays-per-thread shadow/AO kernel
+    if constexpr (sizeof(T) == 4 && F == 8 && FAST)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_pair_kernel<8>, block, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, dev::secondary_kernel<T, F, FAST>, block, 0);
+  }
   return n;
 }
 

@@ -178,3 +178,20 @@ def test_per_frame_fractal_parameter(gpu_ctx):
     batch = gpu_ctx.render_batch(boxes, precision=mb.PREC_FP64)
     for i, f in enumerate(boxes):
         _same(batch[i], gpu_ctx.render(f, precision=mb.PREC_FP64), f"FP64 scale frame {i}")
+
+
+@pytest.mark.parametrize("size,extra", [((480, 270), {}), ((320, 180), {"ambient_occlusion_quality": 3}),
+                                        ((256, 144), {"mandelbox_scale": -1.5}),
+                                        ((240, 135), {"shadows_cone_angle": 2.0, "penetrating_lights": 1})])
+def test_pair_rays_do_not_change_pixels(gpu_ctx, size, extra):
+    """The lean Mandelbox's shadow/AO rays two per thread (packed f32x2 orbits,
+    secondary_pair_kernel) give the frame of one ray per thread bit for bit, for positive
+    and negative scales (|k s| from its own packed FMA) and soft / penetrating shadows."""
+    sc = W.workload("mandelbox_1080p", *size, **extra)
+    one = gpu_ctx.render(sc, pair_rays=-1, profile_stages=True)
+    st1 = gpu_ctx.stats()
+    two = gpu_ctx.render(sc, profile_stages=True)
+    st2 = gpu_ctx.stats()
+    _same(one, two, f"pair rays {size} {extra}")
+    assert st1.stage_orbit[2] == st2.stage_orbit[2] and st1.stage_de[2] == st2.stage_de[2]
+    assert st2.stage_de[2] > 0
