@@ -363,10 +363,12 @@ def coverage_section(ctx) -> dict:
     return out
 
 
-def configs_section(ctx) -> dict:
+def configs_section(ctx, cpu_seconds: float = 0.0) -> dict:
     """The other single-frame configurations at full size: config 1 (Mandelbulb power 8, N 250,
-    640x480, hard shadows) and config 4 (deep zoom: Mandelbulb N 1000, 1024x1024, the camera
-    1e-6 from a seeded surface point). Per configuration and precision policy: the library's
+    640x480, hard shadows; at the reference's escape radius r > 100 and at the
+    configuration's r > 10, with the CPU implementation's Mpix/s beside each) and config 4
+    (deep zoom: Mandelbulb N 1000, 1024x1024, the camera 1e-6 from a seeded surface point).
+    Per configuration and precision policy: the library's
     device time of one frame (CUDA events around its launches; best of three after a warm-up,
     one frame for FP64 and for the deep zoom, whose frames take seconds), the policy
     MBGB_PREC_AUTO picked, and the FP32_FIX frame's hit mismatch
@@ -376,10 +378,16 @@ def configs_section(ctx) -> dict:
     from mandelbulber_gb300 import workloads as W
     from tests import metrics
     out = {}
-    for name in ("mandelbulb_640x480", "deep_zoom_1024"):
-        sc = W.workload(name) if name != "deep_zoom_1024" else W.deep_zoom(ctx, size=1024)
+    for name in ("mandelbulb_640x480", "mandelbulb_640x480_r10", "deep_zoom_1024"):
+        if name == "deep_zoom_1024":
+            sc = W.deep_zoom(ctx, size=1024)
+        else:
+            sc = W.workload("mandelbulb_640x480")
+            if name.endswith("_r10"):
+                sc.bailoutRadius = 10   # the configuration's r > 10 (the reference hard-codes r > 100)
         npx = sc.image_width * sc.image_height
-        rec = {"size": [sc.image_width, sc.image_height], "formula": int(sc.formula), "N": int(sc.N)}
+        rec = {"size": [sc.image_width, sc.image_height], "formula": int(sc.formula), "N": int(sc.N),
+               "escape_radius": int(sc.bailoutRadius) or 100}
         imgs = {}
         for pol, key in ((mb.PREC_FP32_FIX, "fp32_fix"), (mb.PREC_FP64, "fp64"), (mb.PREC_AUTO, "auto")):
             imgs[key] = ctx.render(sc, precision=pol)
@@ -396,6 +404,13 @@ def configs_section(ctx) -> dict:
         if rec["auto_picked_fp64"]:
             rec["auto_vs_fp64_identical"] = bool(all(np.array_equal(getattr(imgs["auto"], k), getattr(imgs["fp64"], k))
                                                      for k in ("image_float", "zbuffer", "hit")))
+        if cpu_seconds > 0 and name != "deep_zoom_1024":
+            # the CPU implementation of the path on this configuration (the reference's
+            # pthreads path restated: -O3 -ffast-math, rand() jitter, every host thread)
+            v, desc = cpu_sample(sc, cpu_seconds)
+            rec["cpu_reference"] = {"value": v, "unit": "Mpix/s", "cores": desc["threads"], "kind": "port",
+                                    "sample": f"{desc['rows']} rows spread evenly over the frame, "
+                                              f"{desc['seconds']:.1f} s"}
         out[name] = rec
     return out
 
@@ -418,6 +433,32 @@ def run_once(args) -> int:
     return 0
 
 
+def run_noise_floor(args) -> int:
+    """The reference's run-to-run noise floor on the Mandelbulb configuration (640x480): the
+    CPU implementation with the reference's shipped step jitter (Random() over the shared
+    rand() stream, src/Render3D.cpp:129-133, src/common_math.cpp:25-32) rendered with one
+    thread and with every host thread, and the two frames compared. The shared stream hands
+    its numbers to whichever thread asks next, so the jitter each pixel sees depends on the
+    thread count. Also each against the deterministic (jitter-off) strict FP64 oracle."""
+    import mandelbulber_gb300 as mb  # noqa: F401  (CImage for the oracle's layers)
+    from mandelbulber_gb300 import workloads as W
+    from tests import metrics, oracle_lib
+    lib = oracle_lib.load(fast=True)
+    sc = W.workload("mandelbulb_640x480")
+    threads = os.cpu_count() or 1
+    out = {"mode": "noise_floor", "workload": "mandelbulb_640x480", "threads": [1, threads]}
+    imgs = {}
+    for t in (1, threads):
+        t0 = time.perf_counter()
+        imgs[t], _ = oracle_lib.render(lib, sc, jitter=True, threads=t)
+        out[f"seconds_{t}_threads"] = time.perf_counter() - t0
+    strict, _ = oracle_lib.render(oracle_lib.load(), sc, jitter=False, threads=threads)
+    out["jitter_1_vs_all_threads"] = metrics.compare(imgs[1], imgs[threads])
+    out["jitter_all_threads_vs_no_jitter"] = metrics.compare(imgs[threads], strict)
+    print(json.dumps(out))
+    return 0
+
+
 def make_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,6 +478,8 @@ def make_parser() -> argparse.ArgumentParser:
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
     ap.add_argument("--precision", default="fp32_fix", choices=["fp32_fix", "fp64"])
+    ap.add_argument("--noise-floor", action="store_true",
+                    help="measure the reference's jitter noise floor on the Mandelbulb configuration (CPU) and exit")
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "per_pixel"],
                     help="with --once: the render engine of the profiling case")
     return ap
@@ -451,6 +494,8 @@ def main() -> int:
         return run_reference(args, rank, world)
     if args.once:
         return run_once(args)
+    if args.noise_floor:
+        return run_noise_floor(args)
 
     import torch
     import mandelbulber_gb300 as mb
@@ -622,7 +667,8 @@ def main() -> int:
 
     batch = None if args.no_batch else batch_section(ctx, torch, dev, stream, flush, args, world, dist)
     coverage = None if args.no_coverage else coverage_section(ctx)
-    configs = None if args.no_configs else configs_section(ctx)
+    configs = None if args.no_configs else configs_section(ctx, 0.0 if (args.no_cpu or rank != 0 or world > 1)
+                                                               else args.cpu_seconds / 2)
     grads = None if args.no_grad else grad_section(ctx, torch, dev, args)
 
     cpu = None

@@ -174,7 +174,9 @@ typedef struct mbgb_scene {
   uint8_t planeEnable, boxEnable, invertedBoxEnable, sphereEnable, invertedSphereEnable;
   uint8_t waterEnable, onlyPlane;
   uint8_t paletteLoaded;        /* palette came from the file (not generated from coloring_seed) */
-  uint8_t pad_[2];
+  uint16_t bailoutRadius;       /* not in the reference: escape radius of the trigonometric formulas' distance
+                                 * mode (trig_DE, trig_optim); 0 = the reference's hard-coded r > 100
+                                 * (src/fractal.cpp:1151-1157). No settings key sets it. */
 
   /* ---- colours (sRGB, 16-bit range unless noted) ---- */
   mbgb_rgb background_color1, background_color2, background_color3;

@@ -245,10 +245,29 @@ static int scene_kernel_formula(const mbgb_scene &s) {
   return kernel_formula(s.formula, s.ifsFoldingMode || s.fakeLightsEnabled || uses_primitives(s));
 }
 
+// The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
+// julia, limits, iteration threshold or interior mode, fold value = 2 x fold limit, and
+// min radius <= fixed radius (so that the sphere fold is a clamp).
+static bool fast_mandelbox(const mbgb_scene &s) {
+  return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
+         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
+         s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
+         s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
+         s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
+}
+
+// The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,
+// no pre-folds, limits, iteration threshold or interior mode).
+static bool fast_mandelbulb(const mbgb_scene &s) {
+  return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
+         !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode;
+}
+
 template <typename T>
 static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   memset(&f, 0, sizeof(f));
   f.formula = s.formula;
+  f.lean = (fast_mandelbox(s) || fast_mandelbulb(s)) ? 1 : 0;
   f.N = (int)s.N;
   f.N5 = (int)(s.N * 5);
   f.N10 = (int)(s.N * 10);
@@ -263,6 +282,8 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   f.mbMainRotZero = s.mboxMainRotZero;
   f.power = (T)s.power;
   f.constantFactor = (T)s.constantFactor;
+  f.bailout = s.bailoutRadius ? (T)s.bailoutRadius : T(100);
+  f.bailout2 = f.bailout * f.bailout;
   for (int c = 0; c < 3; c++) {
     f.julia[c] = (T)s.julia[c];
     f.mbOffset[c] = (T)s.mboxOffset[c];
@@ -776,23 +797,6 @@ static mbgb_status ensure_ao(mbgb_context *c, int quality, cudaStream_t s) {
   return MBGB_OK;
 }
 
-// The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
-// julia, limits, iteration threshold or interior mode, fold value = 2 x fold limit, and
-// min radius <= fixed radius (so that the sphere fold is a clamp).
-static bool fast_mandelbox(const mbgb_scene &s) {
-  return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
-         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
-         s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
-         s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
-         s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
-}
-
-// The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,
-// no pre-folds, limits, iteration threshold or interior mode).
-static bool fast_mandelbulb(const mbgb_scene &s) {
-  return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
-         !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode;
-}
 
 // Per-frame fields of ParamsT (camera, size, rows, light direction) cleared, so that
 // two frames compare equal exactly when one launch sequence can render both.

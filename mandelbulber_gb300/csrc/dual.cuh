@@ -212,7 +212,7 @@ __device__ __forceinline__ Dual<T, K> de_dual_seeded(const FractalT<T> &f, DV3<T
       rp = rp * r;
       z = {(cth * cph) * rp + c.x, (cth * sph) * rp + c.y, sth * rp + c.z};
       r = dlength(z);
-      if (r.v > T(100)) {
+      if (r.v > f.bailout) {
         dist = (r * dlog(r)) * T(0.5) / r_dz;
         break;
       }

@@ -722,7 +722,7 @@ __device__ __noinline__ T compute_runtime(const FractalT<T> *__restrict__ fp, V3
       if (r > T(1024)) { distance = r / m_fabs(tgladDE); break; }
     } else {
       if (MODE == kModeNormal) {
-        if (r > T(1e2)) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
+        if (r > f.bailout) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
       } else if (MODE == kModeColour) {
         if (f.onlyPlane) {
           distance = orbit_length(z);

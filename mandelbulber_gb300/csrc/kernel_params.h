@@ -41,9 +41,14 @@ struct FractalT {
   int minN;
   int juliaMode, tgladFoldingMode, sphericalFoldingMode;
   int limits, iterThresh, interiorMode;
+  int lean;         // the lean FP32 orbit applies (Mandelbox without rotations, offsets, pre-folds or julia;
+                    // power-8 Mandelbulb without pre-folds): CalculateDistance takes it in FP32
   int mbRotEnabled, mbMainRotZero;
   int mbRotZero[2][3];
   T power, constantFactor;
+  // escape radius of the trigonometric formulas' distance mode and its square (the reference's
+  // r > 100, src/fractal.cpp:1151-1157, unless the scene's bailoutRadius overrides it)
+  T bailout, bailout2;
   T julia[3];
   T foldingLimit, foldingValue, sphFixed, sphMin;
   T mbScale, mbFoldLimit, mbFoldValue, mbMinR, mbFixedR;

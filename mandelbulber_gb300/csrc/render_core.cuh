@@ -10,6 +10,7 @@
 // The reference functions each part follows are cited at the function.
 #pragma once
 
+#include "lean_orbit.cuh"
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -206,7 +207,7 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
       if (r > T(1024)) { distance = r / m_fabs(tgladDE); break; }
     } else {
       if (MODE == 0) {
-        if (r > T(100)) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
+        if (r > f.bailout) { distance = T(0.5) * r * m_log(r) / r_dz; break; }
       } else {
         distance = orbit_length(z);
         if (distance < minv) minv = distance;
@@ -226,6 +227,110 @@ __device__ __forceinline__ T compute(const FractalT<T> &f, V3<T> z, const int N,
   }
 }
 
+// Constants of the lean Mandelbox iteration from the fractal block (the quotients are
+// derived on the host: FractalT::leanKm1, leanSa, leanSb).
+__device__ __forceinline__ LeanBoxK lean_box_k(const FractalT<float> &f) {
+  return LeanBoxK{f.mbFoldLimit, f.leanSa, f.leanSb, f.leanKm1};
+}
+
+// Mandelbox orbit (formula 8, normal mode) for the common case: no rotation, no offset,
+// no pre-folds, julia off, fold value = 2 x fold limit. Squared radius throughout: the
+// bailout r > 1024 becomes r^2 > 1024^2 and the sphere fold tests r^2 directly, so the
+// loop has no square root.
+__device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const float px, const float py,
+                                                const float pz, const int N, int &Lout, Counters &cnt,
+                                                const float s) {
+  const LeanBoxK k = lean_box_k(f);
+  const float skm1 = __fmul_rn(s, k.km1);
+  const float cx = __fmul_rn(px, f.constantFactor), cy = __fmul_rn(py, f.constantFactor),
+              cz = __fmul_rn(pz, f.constantFactor);
+  float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
+  int L;
+#pragma unroll 5
+  for (L = 0; L < N; L++) {
+    const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
+    if (r2 > 1048576.0f) {
+      dist = box_bailout_dist(r2, dr);
+      break;
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (L == N) dist = 0.0f;
+  return dist;
+}
+
+// One Mandelbulb power-8 iteration (trig_optim, src/fractal.cpp:211-225) without
+// transcendentals: theta = asin(z/r) in [-pi/2, pi/2] has cos = rho/r >= 0 and sin = z/r;
+// phi = atan2(y, x) has cos = x/rho, sin = y/rho (phi = 0 when rho = 0, as atan2(0, 0)).
+// Three angle doublings (c, s) -> (c^2 - s^2, 2cs) give 8*theta and 8*phi; r^8 and r^7 come
+// from r^2. Returns the new squared radius.
+__device__ __forceinline__ float bulb8_iteration(float &x, float &y, float &z, const float r2, float &r_dz,
+                                                 const float cx, const float cy, const float cz) {
+  const float rho2 = fmaf(y, y, __fmul_rn(x, x));
+  const float inv_r = rsqrtf(r2);
+  const bool axis = rho2 == 0.0f;
+  const float inv_rho = axis ? 0.0f : rsqrtf(rho2);
+  float ct = __fmul_rn(__fmul_rn(rho2, inv_rho), inv_r), st = __fmul_rn(z, inv_r);
+  float cp = axis ? 1.0f : __fmul_rn(x, inv_rho), sp = axis ? 0.0f : __fmul_rn(y, inv_rho);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const float ct2 = fmaf(ct, ct, -__fmul_rn(st, st)), st2 = __fmul_rn(__fmul_rn(2.0f, st), ct);
+    const float cp2 = fmaf(cp, cp, -__fmul_rn(sp, sp)), sp2 = __fmul_rn(__fmul_rn(2.0f, sp), cp);
+    ct = ct2; st = st2; cp = cp2; sp = sp2;
+  }
+  const float r4 = __fmul_rn(r2, r2);
+  const float r8 = __fmul_rn(r4, r4);
+  r_dz = fmaf(__fmul_rn(__fmul_rn(8.0f, r8), inv_r), r_dz, 1.0f);   // p * r^(p-1) * r_dz + 1
+  const float t = __fmul_rn(ct, r8);
+  x = fmaf(t, cp, cx);
+  y = fmaf(t, sp, cy);
+  z = fmaf(st, r8, cz);
+  return norm2_rn(x, y, z);
+}
+
+// Mandelbulb power 8 orbit. MODE 0 returns the distance estimate 0.5*r*ln(r)/dr at the
+// bailout r > 100 (or the scene's bailoutRadius: r^2 > FractalT::bailout2); MODE 1 returns
+// the colouring value (min |z| until |z| > 1e15, times 5000).
+template <int MODE>
+__device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, const float px, const float py,
+                                                  const float pz, const int N, int &Lout, Counters &cnt) {
+  float cx, cy, cz;
+  if (f.juliaMode) {
+    cx = f.julia[0]; cy = f.julia[1]; cz = f.julia[2];
+  } else {
+    cx = __fmul_rn(px, f.constantFactor); cy = __fmul_rn(py, f.constantFactor); cz = __fmul_rn(pz, f.constantFactor);
+  }
+  float x = px, y = py, z = pz, r_dz = 1.0f, dist = 0.0f;
+  float r2 = norm2_rn(x, y, z);
+  float minr2 = __int_as_float(0x7f800000);
+  const float bail2 = f.bailout2;
+  int L;
+  for (L = 0; L < N; L++) {
+    r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
+    if (MODE == 0) {
+      if (r2 > bail2) {
+        const float r = sqrtf(r2);
+        dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
+        break;
+      }
+    } else {
+      if (r2 < minr2) minr2 = r2;
+      if (r2 > 1.0e30f) break;
+    }
+  }
+  cnt.orbit += (unsigned long long)(L + 1);
+  cnt.calls += 1;
+  Lout = L;
+  if (MODE == 0) {
+    if (L == N) dist = 0.0f;
+    return dist;
+  }
+  // colouring: min |z| after a bailout, else the last |z|
+  return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
+}
+
 // CalculateDistance, analytic branch (src/fractal.cpp:1245-1300, 1436-1445).
 // `L` (itersOut) is left untouched when the limits box returns early, as in the reference.
 template <typename T, int FORMULA>
@@ -235,6 +340,20 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
   if (FORMULA == 0)
     return calc_distance_runtime<T>(&f, point, detailSize, N, minN, normalMode, &L, &maxIter, &cnt.orbit, &cnt.calls,
                                     &cnt.objectOut, fparam);
+  if constexpr (sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
+    // the lean FP32 orbits (no limits, interior mode or iteration threshold: f.lean says so)
+    if (f.lean) {
+      int Li;
+      T distance;
+      if constexpr (FORMULA == 8) distance = mandelbox_fast(f, point.x, point.y, point.z, N, Li, cnt, fparam);
+      else distance = mandelbulb8_fast<0>(f, point.x, point.y, point.z, N, Li, cnt);
+      maxIter = (Li == N);
+      L = Li;
+      if (distance < T(0)) distance = T(0);
+      if (Li < minN && distance < detailSize) distance = detailSize;
+      return distance;
+    }
+  }
   T limitBoxDist = T(0);
   if (f.limits) {
     // MAX(a, b) = a > b ? a : b (gtk MAX macro)
@@ -843,7 +962,14 @@ __device__ __forceinline__ V3<T> surface_colour(const ParamsT<T> &p, const V3<T>
     return V3<T>{T(c[0]) / T(65536), T(c[1]) / T(65536), T(c[2]) / T(65536)};
   }
   int L;
-  const T c = compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt, fparam);
+  T c;
+  if constexpr (sizeof(T) == 4 && FORMULA == 2) {
+    // the power-8 Mandelbulb's colouring orbit without transcendentals (f.lean)
+    c = p.f.lean ? mandelbulb8_fast<1>(p.f, point.x, point.y, point.z, p.f.N10, L, cnt)
+                 : compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt, fparam);
+  } else {
+    c = compute<T, FORMULA, 1>(p.f, point, p.f.N10, L, cnt, fparam);
+  }
   int nrCol = to_i32_x86((double)m_floor(c));
   // abs(nrCol) % (248 * 256) with the magnitude taken as unsigned, as the reference
   // binary computes it: an out-of-range conversion (INT_MIN) gives 2^31 % 63488 = 2048.

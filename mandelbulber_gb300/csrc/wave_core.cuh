@@ -34,108 +34,6 @@ namespace mbgb {
 
 namespace dev {
 
-// Constants of the lean Mandelbox iteration from the fractal block (the quotients are
-// derived on the host: FractalT::leanKm1, leanSa, leanSb).
-__device__ __forceinline__ LeanBoxK lean_box_k(const FractalT<float> &f) {
-  return LeanBoxK{f.mbFoldLimit, f.leanSa, f.leanSb, f.leanKm1};
-}
-
-// Mandelbox orbit (formula 8, normal mode) for the common case: no rotation, no offset,
-// no pre-folds, julia off, fold value = 2 x fold limit. Squared radius throughout: the
-// bailout r > 1024 becomes r^2 > 1024^2 and the sphere fold tests r^2 directly, so the
-// loop has no square root.
-__device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const float px, const float py,
-                                                const float pz, const int N, int &Lout, Counters &cnt,
-                                                const float s) {
-  const LeanBoxK k = lean_box_k(f);
-  const float skm1 = __fmul_rn(s, k.km1);
-  const float cx = __fmul_rn(px, f.constantFactor), cy = __fmul_rn(py, f.constantFactor),
-              cz = __fmul_rn(pz, f.constantFactor);
-  float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
-  int L;
-#pragma unroll 5
-  for (L = 0; L < N; L++) {
-    const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
-    if (r2 > 1048576.0f) {
-      dist = box_bailout_dist(r2, dr);
-      break;
-    }
-  }
-  cnt.orbit += (unsigned long long)(L + 1);
-  cnt.calls += 1;
-  Lout = L;
-  if (L == N) dist = 0.0f;
-  return dist;
-}
-
-// One Mandelbulb power-8 iteration (trig_optim, src/fractal.cpp:211-225) without
-// transcendentals: theta = asin(z/r) in [-pi/2, pi/2] has cos = rho/r >= 0 and sin = z/r;
-// phi = atan2(y, x) has cos = x/rho, sin = y/rho (phi = 0 when rho = 0, as atan2(0, 0)).
-// Three angle doublings (c, s) -> (c^2 - s^2, 2cs) give 8*theta and 8*phi; r^8 and r^7 come
-// from r^2. Returns the new squared radius.
-__device__ __forceinline__ float bulb8_iteration(float &x, float &y, float &z, const float r2, float &r_dz,
-                                                 const float cx, const float cy, const float cz) {
-  const float rho2 = fmaf(y, y, __fmul_rn(x, x));
-  const float inv_r = rsqrtf(r2);
-  const bool axis = rho2 == 0.0f;
-  const float inv_rho = axis ? 0.0f : rsqrtf(rho2);
-  float ct = __fmul_rn(__fmul_rn(rho2, inv_rho), inv_r), st = __fmul_rn(z, inv_r);
-  float cp = axis ? 1.0f : __fmul_rn(x, inv_rho), sp = axis ? 0.0f : __fmul_rn(y, inv_rho);
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const float ct2 = fmaf(ct, ct, -__fmul_rn(st, st)), st2 = __fmul_rn(__fmul_rn(2.0f, st), ct);
-    const float cp2 = fmaf(cp, cp, -__fmul_rn(sp, sp)), sp2 = __fmul_rn(__fmul_rn(2.0f, sp), cp);
-    ct = ct2; st = st2; cp = cp2; sp = sp2;
-  }
-  const float r4 = __fmul_rn(r2, r2);
-  const float r8 = __fmul_rn(r4, r4);
-  r_dz = fmaf(__fmul_rn(__fmul_rn(8.0f, r8), inv_r), r_dz, 1.0f);   // p * r^(p-1) * r_dz + 1
-  const float t = __fmul_rn(ct, r8);
-  x = fmaf(t, cp, cx);
-  y = fmaf(t, sp, cy);
-  z = fmaf(st, r8, cz);
-  return norm2_rn(x, y, z);
-}
-
-// Mandelbulb power 8 orbit. MODE 0 returns the distance estimate 0.5*r*ln(r)/dr at the
-// bailout r > 100; MODE 1 returns the colouring value (min |z| until |z| > 1e15, times 5000).
-template <int MODE>
-__device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, const float px, const float py,
-                                                  const float pz, const int N, int &Lout, Counters &cnt) {
-  float cx, cy, cz;
-  if (f.juliaMode) {
-    cx = f.julia[0]; cy = f.julia[1]; cz = f.julia[2];
-  } else {
-    cx = __fmul_rn(px, f.constantFactor); cy = __fmul_rn(py, f.constantFactor); cz = __fmul_rn(pz, f.constantFactor);
-  }
-  float x = px, y = py, z = pz, r_dz = 1.0f, dist = 0.0f;
-  float r2 = norm2_rn(x, y, z);
-  float minr2 = __int_as_float(0x7f800000);
-  int L;
-  for (L = 0; L < N; L++) {
-    r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
-    if (MODE == 0) {
-      if (r2 > 1.0e4f) {
-        const float r = sqrtf(r2);
-        dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
-        break;
-      }
-    } else {
-      if (r2 < minr2) minr2 = r2;
-      if (r2 > 1.0e30f) break;
-    }
-  }
-  cnt.orbit += (unsigned long long)(L + 1);
-  cnt.calls += 1;
-  Lout = L;
-  if (MODE == 0) {
-    if (L == N) dist = 0.0f;
-    return dist;
-  }
-  // colouring: min |z| after a bailout, else the last |z|
-  return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
-}
-
 // Resumable lean orbits (distance mode) for the orbit-granular lane refill of the shadow/AO
 // stage: the state of mandelbox_fast / mandelbulb8_fast<0> between batches of kUnroll
 // iterations, through the same iteration functions. start() begins the orbit of a point;
@@ -193,13 +91,14 @@ struct LeanOrbit<8> {
 template <>
 struct LeanOrbit<2> {
   static constexpr int kUnroll = 2;
-  float jx, jy, jz, cf;
+  float jx, jy, jz, cf, bail2;
   int N;
   bool julia;
   float x, y, z, r2, r_dz, cx, cy, cz;
   int L;
   __device__ __forceinline__ explicit LeanOrbit(const FractalT<float> &f) {
     julia = f.juliaMode;
+    bail2 = f.bailout2;
     jx = f.julia[0]; jy = f.julia[1]; jz = f.julia[2];
     cf = f.constantFactor;
     N = f.N;
@@ -226,7 +125,7 @@ struct LeanOrbit<2> {
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) {
       r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
-      if (r2 > 1.0e4f) {
+      if (r2 > bail2) {
         const float r = sqrtf(r2);
         dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
         return true;
@@ -309,7 +208,7 @@ __device__ __forceinline__ double mandelbulb8_lean_d(const FractalT<double> &f, 
     y = fma(t, sp, cy);
     z = fma(st, r8, cz);
     r2 = x * x + y * y + z * z;
-    if (r2 > 1.0e4) {
+    if (r2 > f.bailout2) {
       const double r = sqrt(r2);
       dist = 0.5 * r * log(r) / r_dz;
       break;
@@ -1419,19 +1318,28 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   Counters cnt{0, 0, 0, 0};
   const int64_t total = wb.npix;
-  for (int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gp < total;
-       gp += (int64_t)gridDim.x * blockDim.x) {
-    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
+  const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  // a warp's 32 consecutive pixels of the float RGB and RGB8 layers, staged so that they
+  // leave as 16-byte stores (cImage's interleaved layers, src/cimage.hpp:155-162)
+  __shared__ __align__(16) float stageImg[4][96];
+  __shared__ __align__(16) uint8_t stageCol[4][96];
+  // the warp walks the pixels together, 32 at a time, so that it can vote on the vector stores
+  for (int64_t gw = (int64_t)blockIdx.x * blockDim.x + warp * 32; gw < total; gw += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t gp = gw + lane;
+    const bool inBatch = gp < total;
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, inBatch ? gp : total - 1)];
     const int64_t pix = gp - c.pixBase;   // pixel within the frame's own layers
     const int x = (int)(pix % c.width), y = (int)(pix / c.width);
-    if (y < c.row_begin || y >= c.row_end) continue;
+    const bool valid = inBatch && y >= c.row_begin && y < c.row_end;
+    T out0 = T(0), out1 = T(0), out2 = T(0);
+    V3<T> objColour{T(0), T(0), T(0)};
+    if (valid) {
     const uint8_t flags = wb.flags[gp];
     const bool hit = (flags & 1) != 0;
     V3<T> viewT;
     camera_dir(p, c, x, y, viewT);
     const V3<T> lv{c.lightVect[0], c.lightVect[1], c.lightVect[2]};
     T base[3];
-    V3<T> objColour{T(0), T(0), T(0)};
     if (hit) {
       const HitInfo<T> h = hit_info(p, c, wb, gp);
       // CalculateNormals (src/shaders.cpp:675-711): 4 DEs at N x 5, minN 0
@@ -1491,7 +1399,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
       base[1] = T(0) + bg.y + T(0);
       base[2] = T(0) + bg.z + T(0);
     }
-    T out0, out1, out2, alpha, opacity;
+    T alpha, opacity;
     if (flags & 4) {
       // a long ray of the overflow pass: its volumetric pass was folded into an affine map
       const T A = wb.vol[0 * wb.npix + gp];
@@ -1520,21 +1428,49 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
     const double depth = hit ? (double)wb.scan[gp] : 1e20;
     if (c.opacity) c.opacity[pix] = to_u16_x86((double)opacity * 65535.0);
     if (c.alpha) c.alpha[pix] = to_u16_x86((double)alpha * 65535.0);
-    if (c.image_float) {
-      c.image_float[3 * pix + 0] = (float)out0;
-      c.image_float[3 * pix + 1] = (float)out1;
-      c.image_float[3 * pix + 2] = (float)out2;
-    }
-    if (c.colour) {
-      c.colour[3 * pix + 0] = to_u8_x86((double)(objColour.x * T(255)));
-      c.colour[3 * pix + 1] = to_u8_x86((double)(objColour.y * T(255)));
-      c.colour[3 * pix + 2] = to_u8_x86((double)(objColour.z * T(255)));
-    }
     if (c.zbuffer) c.zbuffer[pix] = (float)depth;
     // debug layer: 0 miss, 1 hit, 3 hit whose exact_hit refinement missed the level set
     if (c.hit) c.hit[pix] = hit ? ((flags & 8) ? 3 : 1) : 0;
     if (c.iters) c.iters[pix] = wb.iters[gp];
     if (c.depth) c.depth[pix] = depth;
+    }
+    // The interleaved layers: 16-byte stores of the warp's 32 pixels, staged in shared memory,
+    // when all of them lie in one frame's rendered rows at 16-byte-aligned addresses.
+    const int64_t base0 = __shfl_sync(0xffffffffu, c.pixBase, 0);
+    const int64_t pix0 = gw - base0;     // the frame pixel of lane 0
+    const bool aligned = (!c.image_float || ((uintptr_t)(c.image_float + 3 * pix0) & 15u) == 0) &&
+                         (!c.colour || ((uintptr_t)(c.colour + 3 * pix0) & 15u) == 0);
+    const bool vec = __all_sync(0xffffffffu, valid && c.pixBase == base0 && aligned);
+    const uint8_t col[3] = {to_u8_x86((double)(objColour.x * T(255))), to_u8_x86((double)(objColour.y * T(255))),
+                            to_u8_x86((double)(objColour.z * T(255)))};
+    if (vec) {
+      // 32 pixels x 12 bytes = 24 float4 stores, 32 x 3 bytes = 6 uint4 stores
+      float *si = stageImg[warp];
+      uint8_t *sc = stageCol[warp];
+      si[3 * lane + 0] = (float)out0;
+      si[3 * lane + 1] = (float)out1;
+      si[3 * lane + 2] = (float)out2;
+      sc[3 * lane + 0] = col[0];
+      sc[3 * lane + 1] = col[1];
+      sc[3 * lane + 2] = col[2];
+      __syncwarp();
+      if (c.image_float && lane < 24)
+        reinterpret_cast<float4 *>(c.image_float + 3 * pix0)[lane] = reinterpret_cast<const float4 *>(si)[lane];
+      if (c.colour && lane < 6)
+        reinterpret_cast<uint4 *>(c.colour + 3 * pix0)[lane] = reinterpret_cast<const uint4 *>(sc)[lane];
+      __syncwarp();
+    } else if (valid) {
+      if (c.image_float) {
+        c.image_float[3 * pix + 0] = (float)out0;
+        c.image_float[3 * pix + 1] = (float)out1;
+        c.image_float[3 * pix + 2] = (float)out2;
+      }
+      if (c.colour) {
+        c.colour[3 * pix + 0] = col[0];
+        c.colour[3 * pix + 1] = col[1];
+        c.colour[3 * pix + 2] = col[2];
+      }
+    }
   }
   for (int off = 16; off > 0; off >>= 1) {
     cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);

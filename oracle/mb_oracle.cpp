@@ -707,7 +707,9 @@ double compute(const Calc &c, Vec z, int mode, int count, int *Lout) {
     } else if (box_like(form)) {
       if (r > 1024) { distance = r / fabs(tDE); break; }
     } else if (mode == kNormal) {
-      if (r > 1e2) { distance = 0.5 * r * log(r) / r_dz; break; }
+      // the reference's r > 100 (src/fractal.cpp:1151-1157), or the scene's bailoutRadius
+      const double bail = s.bailoutRadius ? (double)s.bailoutRadius : 1e2;
+      if (r > bail) { distance = 0.5 * r * log(r) / r_dz; break; }
     } else if (mode == kColour) {
       if (s.onlyPlane) {
         distance = len(z);

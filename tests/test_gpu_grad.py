@@ -29,6 +29,10 @@ from tests import metrics, oracle_lib
 pytestmark = pytest.mark.gpu
 H = 1e-4
 REL_TOL = 1e-3
+# Least fraction of all pixels each parameter's interior mask must cover (the frames are 256 x
+# 256, about half of the pixels hit): power, camera x / y / z, light alpha / beta.
+MASK_FLOOR = [0.005] * 6
+ORACLE_MASK_FLOOR = [0.02] * 6
 
 
 @pytest.fixture(scope="module")
@@ -88,7 +92,10 @@ def _adjoint_vs_fd(ctx, problem, precision):
               / (2 * H)).cpu().numpy()
         adj = ((2 * (I.double() - T.double()))[..., None] * jac.double() * m[..., None]).sum(
             dim=(1, 2, 3))[:, j].cpu().numpy()
-        assert float(mask.float().mean()) > 0.005, (D.NAMES[j], float(mask.float().mean()))
+        frac = float(mask.float().mean())
+        hit_frac = frac / max(float((R.hit == 1).float().mean()), 1e-12)
+        print(f"interior mask {D.NAMES[j]}: {frac:.4f} of pixels, {hit_frac:.4f} of hits ({precision=})")
+        assert frac > MASK_FLOOR[j], (D.NAMES[j], frac)
         rel = np.abs(adj - fd) / np.abs(fd)
         worst = max(worst, float(rel.max()))
         assert (rel <= REL_TOL).all(), (D.NAMES[j], fd, adj, rel)
@@ -134,7 +141,8 @@ def test_adjoint_matches_oracle_central_differences(gpu_ctx, oracle, problem):
         fd = float((((Ip - Tn) ** 2 - (Im - Tn) ** 2) * m).sum() / (2 * H))
         adj = float(((2 * (I[0].double().cpu().numpy() - Tn))[..., None] * jac[0].double().cpu().numpy()
                      * m[..., None]).sum(axis=(0, 1, 2))[j])
-        assert mask.mean() > 0.02, (D.NAMES[j], mask.mean())
+        print(f"oracle interior mask {D.NAMES[j]}: {mask.mean():.4f} of pixels")
+        assert mask.mean() > ORACLE_MASK_FLOOR[j], (D.NAMES[j], mask.mean())
         assert abs(adj - fd) <= REL_TOL * abs(fd), (D.NAMES[j], fd, adj)
 
 

@@ -357,3 +357,22 @@ def test_device_deadline_returns_timeout_and_context_survives(gpu_ctx):
     small = W.workload("mandelbox_1080p", 64, 36)
     img = gpu_ctx.render(small, precision=mb.PREC_FP32_FIX)
     assert img.hit.mean() > 0.5
+
+
+@pytest.mark.parametrize("precision", [mb.PREC_FP64, mb.PREC_FP32_FIX], ids=["fp64", "fp32_fix"])
+def test_mandelbulb_escape_radius_10_against_oracle(gpu_ctx, oracle, precision):
+    """The Mandelbulb configuration's r > 10 escape radius (scene bailoutRadius; the
+    reference hard-codes r > 100) on the device and in the oracle: the FP64 Mandelbulb bar
+    (hit mismatch <= 0.5 %, PSNR >= 35 dB) and the FP32 policy's bar (<= 0.1 %, >= 45 dB)."""
+    sc = W.workload("mandelbulb_640x480", 320, 240)
+    sc.bailoutRadius = 10
+    ref, _ = oracle_lib.render(oracle, sc)
+    img = gpu_ctx.render(sc, precision=precision)
+    m = metrics.compare(img, ref)
+    print("r > 10", precision, m)
+    if precision == mb.PREC_FP64:
+        assert m["hit_mismatch"] <= 0.005 and m["psnr_float"] >= 35.0, m
+    else:
+        assert m["hit_mismatch"] <= 0.001 and m["psnr_float"] >= 45.0, m
+    default = gpu_ctx.render(W.workload("mandelbulb_640x480", 320, 240), precision=precision)
+    assert not np.array_equal(default.depth, img.depth)
