@@ -613,7 +613,7 @@ struct LaunchCfg {
   int refill = 8;
   int orbitRefill = -1;                 // ended lean orbits before a warp steps them on (0 = off,
                                         // -1 = by scene: on for the power-8 Mandelbulb's long orbits)
-  bool pairRays = true;                 // lean FP32 Mandelbox shadow/AO rays two per thread (packed f32x2)
+  bool pairRays = false;                // lean FP32 Mandelbox shadow/AO rays two per thread (packed f32x2)
 };
 
 // Scene class an autotuned configuration applies to.
@@ -997,7 +997,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
   if (o.ctas_per_sm > 0) cfg.ctasPerSm = o.ctas_per_sm;
   if (o.refill_min > 0) cfg.refill = o.refill_min;
   if (o.orbit_refill != 0) cfg.orbitRefill = o.orbit_refill < 0 ? 0 : o.orbit_refill;
-  if (o.pair_rays < 0) cfg.pairRays = false;
+  if (o.pair_rays > 0) cfg.pairRays = true;
   // Orbit-granular refill pays where orbit lengths spread widely (Mandelbulb, N up to
   // hundreds); the Mandelbox's short orbits (bailout 1024 within ~15 iterations) lose more
   // to the extra step passes than they gain (measured at 1080p: 11.2 ms per-estimate
@@ -1284,7 +1284,7 @@ static mbgb_status check_opts(const mbgb_opts &o) {
     return set_error(MBGB_ERR_BAD_PARAM, "tile_w x tile_h must be 32");
   if (o.refill_min < 0 || o.refill_min > 32) return set_error(MBGB_ERR_BAD_PARAM, "refill_min must be in [0, 32]");
   if (o.orbit_refill < -1 || o.orbit_refill > 32) return set_error(MBGB_ERR_BAD_PARAM, "orbit_refill must be in [-1, 32]");
-  if (o.pair_rays < -1 || o.pair_rays > 0) return set_error(MBGB_ERR_BAD_PARAM, "pair_rays must be 0 or -1");
+  if (o.pair_rays < 0 || o.pair_rays > 1) return set_error(MBGB_ERR_BAD_PARAM, "pair_rays must be 0 or 1");
   if (o.ctas_per_sm < 0) return set_error(MBGB_ERR_BAD_PARAM, "negative ctas_per_sm");
   if (o.row_begin < 0 || o.row_end < 0) return set_error(MBGB_ERR_BAD_PARAM, "row range out of bounds");
   return MBGB_OK;

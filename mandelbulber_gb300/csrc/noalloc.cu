@@ -12,8 +12,9 @@
 //
 // Limits: FP32-with-FP64-refinement policy only (MBGB_PREC_FP32_FIX; MBGB_PREC_AUTO is
 // refused, since it would pick FP64 for deep zooms); at most kNaMaxPixels pixels
-// (the overflow pixel list is sized for that); rays longer than kNaStepCap step
-// records go to the overflow pass (exact, but slower than mbgb_render_device).
+// (the overflow pixel list is sized for that); rays longer than a thread slot's step
+// records (256 at the default launch of one 96-thread CTA per SM; fewer with more CTAs per
+// SM, opts->ctas_per_sm) go to the overflow pass (exact, but slower than mbgb_render_device).
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -31,15 +32,17 @@ using mbgb::kMaxAOVectors;
 using mbgb::kOverflowThreads;
 using mbgb::kStepSlots;
 
-constexpr int kNaMaxCtas = 160;                      // one CTA per SM (GB300 has 152)
+constexpr int kNaMaxCtas = 160;                      // CTAs of the default launch: one per SM (GB300 has 152)
 constexpr int kNaThreads = 96;                       // threads per CTA
-constexpr int kNaSlots = kNaMaxCtas * kNaThreads;    // thread slots of the main pass
-constexpr int kNaStepCap = 256;                      // step records per slot in the main pass
+constexpr int kNaSlots = kNaMaxCtas * kNaThreads;    // thread slots of the default launch
+constexpr int kNaStepCap = 256;                      // step records per slot of the default launch
+constexpr long long kNaRecords = (long long)kNaStepCap * kNaSlots;   // records per step array
+constexpr int kNaMinStepCap = 32;                    // fewest records per slot a launch may keep
 constexpr long long kNaMaxPixels = 4194304;          // 2048 x 2048; 1920 x 1080 fits
 constexpr int kMaxDevices = 64;
 
 // Static scratch (sizes in floats unless noted):
-__device__ __align__(256) float g_na_steps[3][(size_t)kNaStepCap * kNaSlots];              // 47.2 MB
+__device__ __align__(256) float g_na_steps[3][(size_t)kNaRecords];                          // 47.2 MB
 __device__ __align__(256) float g_na_ovsteps[3][(size_t)kStepSlots * kOverflowThreads];    // 15.4 MB
 __device__ __align__(256) unsigned int g_na_ovlist[kNaMaxPixels];                          // 16.8 MB
 __device__ __align__(256) float g_na_ao[3 * kMaxAOVectors];                                // 117 KiB
@@ -168,7 +171,16 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   mbgb::FractalT<double> fd;
   mbgb::prepare_frame_f32(*scene, o, d->ao, aoCount, &p, &fd);
 
-  const int grid = d->sms < kNaMaxCtas ? d->sms : kNaMaxCtas;
+  // CTAs per SM (opts->ctas_per_sm, default 1): more resident warps, each slot then keeping
+  // fewer step records (the arrays' records divided among the slots); rays longer than that
+  // take the overflow pass
+  const int perSm = o.ctas_per_sm > 0 ? o.ctas_per_sm : 1;
+  const long long gridL = (long long)d->sms * perSm;
+  const long long slotsL = gridL * kNaThreads;
+  if (kNaRecords / slotsL < kNaMinStepCap)
+    return mbgb::set_error(MBGB_ERR_BAD_PARAM, "ctas_per_sm leaves fewer than 32 step records per thread slot");
+  const int grid = perSm == 1 && d->sms > kNaMaxCtas ? kNaMaxCtas : (int)gridL;
+  const int stepCap = (int)(kNaRecords / ((long long)grid * kNaThreads));
   mbgb::FrameIO io{};
   io.image_float = img->image_float;
   io.zbuffer = img->zbuffer;
@@ -178,11 +190,11 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   io.hit = img->hit;
   io.iters = img->iters;
   io.depth = img->depth;
-  io.step_step = d->steps + 0 * (size_t)kNaStepCap * kNaSlots;
-  io.step_dist = d->steps + 1 * (size_t)kNaStepCap * kNaSlots;
-  io.step_thr = d->steps + 2 * (size_t)kNaStepCap * kNaSlots;
+  io.step_step = d->steps + 0 * (size_t)kNaRecords;
+  io.step_dist = d->steps + 1 * (size_t)kNaRecords;
+  io.step_thr = d->steps + 2 * (size_t)kNaRecords;
   io.slots = (int64_t)grid * kNaThreads;
-  io.step_cap = kNaStepCap;
+  io.step_cap = stepCap;
   io.overflow_pass = 0;
   char *ctl = (char *)d->control;
   io.tile_counter = (unsigned int *)(ctl + 0);

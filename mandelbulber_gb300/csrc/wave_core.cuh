@@ -1097,6 +1097,11 @@ __device__ __forceinline__ void mandelbox_fast_x2(const FractalT<float> &f, cons
 // the warp's 64 slots are idle (one atomicAdd for all of them: slot-0 jobs first, then
 // slot-1 jobs). An idle slot's orbit repeats the other slot's point and is discarded.
 // Results are bit-identical to secondary_kernel's: the same orbit values, clamps and steps.
+// Measured on the 1080p Mandelbox (GB300): 12.1 ms against secondary_kernel's 9.8 ms. The
+// packed iteration alone is 18 % faster (26 % fewer instructions, but the FMA and ALU pipes
+// then throttle issue), while here the per-estimate tails run twice per lane, a pair waits for
+// its longer orbit, and 80 registers leave 22 warps per SM against 36: 6 % fewer instructions
+// at 70 % issue against 88 %. So it is opt-in (opts.pair_rays = 1).
 // (A template, so that every translation unit that includes this header may instantiate it.)
 template <int FORMULA>
 __global__ void __launch_bounds__(128) secondary_pair_kernel(const __grid_constant__ ParamsT<float> p,

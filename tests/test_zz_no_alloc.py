@@ -4,8 +4,9 @@ Callers that cannot allocate device memory while they render (an application who
 memory manager has reserved the GPU for its own pool, a plugin inside such a host, a
 frame loop that must not call cudaMalloc/cudaFree because they synchronise the
 device) use this entry point; its scratch is static device memory shared by all
-calls. The test renders through it twice in a row — first a scene whose long rays
-go through the overflow pass, then the benchmark scene — and checks each frame
+calls. The test renders through it three times in a row — first a scene whose long rays
+go through the overflow pass, then the benchmark scene at the default launch and with
+three CTAs per SM (fewer step records per thread slot) — and checks each frame
 against mbgb_render_device on the same scene with the FP32 parity tolerance used
 by the other tests (<= 0.1 % hit mismatch, >= 45 dB PSNR of the float image).
 The two entry points run the same FP32 kernel, but the allocation-free one keeps
@@ -64,14 +65,17 @@ def test_noalloc_matches_render_device_on_two_calls(mblib):
         # ray before it overflows, the allocation-free one 256, so a long ray there is one here.
         ctx.render(scenes[0], precision=mb.PREC_FP32_FIX, engine=mb.ENGINE_PER_PIXEL)
         assert ctx.stats().long_rays > 0
-    opts = mb.make_opts(precision=mb.PREC_FP32_FIX)
-    for call, (sc, ref) in enumerate(zip(scenes, refs)):   # two calls in a row share the static scratch
+    opts = [mb.make_opts(precision=mb.PREC_FP32_FIX), mb.make_opts(precision=mb.PREC_FP32_FIX),
+            mb.make_opts(precision=mb.PREC_FP32_FIX, ctas_per_sm=3)]
+    scenes.append(scenes[1])   # a third call: three CTAs per SM, fewer records per thread slot
+    refs.append(refs[1])
+    for call, (sc, ref) in enumerate(zip(scenes, refs)):   # calls in a row share the static scratch
         w, h = sc.image_width, sc.image_height
         layers = _device_layers(w, h, 0xA5)  # garbage: every pixel must be written
         img_c = _c_image(layers, w, h)
         torch.cuda.synchronize()
         free_before = torch.cuda.mem_get_info()[0]
-        rc = lib.mbgb_render_device_noalloc(ctypes.byref(sc), ctypes.byref(img_c), ctypes.byref(opts))
+        rc = lib.mbgb_render_device_noalloc(ctypes.byref(sc), ctypes.byref(img_c), ctypes.byref(opts[call]))
         assert rc == 0, lib.mbgb_last_error()
         torch.cuda.synchronize()
         if call > 0:
