@@ -425,11 +425,30 @@ def run_once(args) -> int:
     engine = mb.ENGINE_PER_PIXEL if args.engine == "per_pixel" else mb.ENGINE_WAVEFRONT
     with mb.Context(0) as ctx:
         for _ in range(args.warmup + 1):
-            img = ctx.render(scene, precision=prec, engine=engine)
+            img = ctx.render(scene, precision=prec, engine=engine, pair_rays=int(args.pair_rays))
         st = ctx.stats()
     print(json.dumps({"workload": args.workload, "size": [w, h], "precision": args.precision, "engine": args.engine,
                       "kernel_ms": st.kernel_ms, "orbit_iterations": st.orbit_iterations, "de_calls": st.de_calls,
                       "hit_fraction": float(img.hit.mean())}))
+    return 0
+
+
+def run_peaks(args) -> int:
+    """The ALU microbenchmarks of libmbgb_peak.so, twice each: FP32 / packed FP32 (f32x2) /
+    FP64 FMA chains (TFLOP/s) and the lean Mandelbox iteration alone, scalar and two orbits
+    per thread with packed FMAs (T iterations/s). The profiling case of those loops."""
+    import mandelbulber_gb300 as mb
+    mb.library(build_if_missing=True)
+    lib = ctypes.CDLL(os.path.join(ROOT, "mandelbulber_gb300", "libmbgb_peak.so"))
+    for fn in ("mbgb_peak_tflops", "mbgb_box_orbit_rate", "mbgb_box_orbit_rate_x2"):
+        getattr(lib, fn).restype = ctypes.c_double
+    out = {"mode": "peaks"}
+    for rep in range(2):
+        out[f"rep{rep}"] = {"fp32_fma_tflops": lib.mbgb_peak_tflops(0, 0), "fp32x2_fma_tflops": lib.mbgb_peak_tflops(2, 0),
+                            "fp64_fma_tflops": lib.mbgb_peak_tflops(1, 0),
+                            "box_orbit_titer_per_s": lib.mbgb_box_orbit_rate(0),
+                            "box_orbit_x2_titer_per_s": lib.mbgb_box_orbit_rate_x2(0)}
+    print(json.dumps(out))
     return 0
 
 
@@ -478,6 +497,9 @@ def make_parser() -> argparse.ArgumentParser:
     ap.add_argument("--once", default=None, metavar="WxH",
                     help="render the workload once at this size (warm-up frames first) and exit: the profiling case")
     ap.add_argument("--precision", default="fp32_fix", choices=["fp32_fix", "fp64"])
+    ap.add_argument("--pair-rays", action="store_true",
+                    help="with --once: the lean Mandelbox's shadow/AO rays two per thread (secondary_pair_kernel)")
+    ap.add_argument("--peaks", action="store_true", help="run the ALU peak and orbit-loop microbenchmarks and exit")
     ap.add_argument("--noise-floor", action="store_true",
                     help="measure the reference's jitter noise floor on the Mandelbulb configuration (CPU) and exit")
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "per_pixel"],
@@ -496,6 +518,8 @@ def main() -> int:
         return run_once(args)
     if args.noise_floor:
         return run_noise_floor(args)
+    if args.peaks:
+        return run_peaks(args)
 
     import torch
     import mandelbulber_gb300 as mb
@@ -599,7 +623,7 @@ def main() -> int:
     stream.synchronize()
     na_ms = sum(a.elapsed_time(b_) for a, b_ in na_evs) / na_steps
     noalloc = {"value": npx / (na_ms * 1e3), "unit": "Mpix/s", "ms_per_step": na_ms, "steps": na_steps,
-               "engine": "per-pixel (one pixel per thread), 96-thread CTAs, one per SM, 256 step records per "
+               "engine": "per-pixel (one pixel per thread), 96-thread CTAs, two per SM, 134 step records per "
                          "slot in static device arrays"}
 
     # end to end through the public host entry point: pinned host layers, copies inside the timed region

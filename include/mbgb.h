@@ -403,7 +403,7 @@ mbgb_status mbgb_autotune(mbgb_context *ctx, const mbgb_scene *scene, const mbgb
  * device pointers; the render runs on the current device and on opts->stream
  * (NULL = the legacy default stream, and the call then waits for the frame and
  * reports a device-deadline timeout). `opts` may be NULL (FP32_FIX, default stream).
- * opts->ctas_per_sm (0 = 1) sets the resident 96-thread CTAs per SM: the static step
+ * opts->ctas_per_sm (0 = 2) sets the resident 96-thread CTAs per SM: the static step
  * records are then divided among more thread slots (at least 32 per slot, else
  * MBGB_ERR_BAD_PARAM), and rays longer than a slot's records take the slower overflow pass.
  * Limits: precision MBGB_PREC_FP32_FIX only (MBGB_PREC_AUTO, which picks FP64 for deep

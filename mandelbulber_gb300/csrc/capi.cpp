@@ -246,21 +246,22 @@ static int scene_kernel_formula(const mbgb_scene &s) {
 }
 
 // The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
-// julia, limits, iteration threshold or interior mode, fold value = 2 x fold limit, and
-// min radius <= fixed radius (so that the sphere fold is a clamp).
+// julia or limits, fold value = 2 x fold limit, and min radius <= fixed radius (so that the
+// sphere fold is a clamp). Interior mode and the iteration threshold only post-process the
+// orbit's result (distance_post), which every path applies.
 static bool fast_mandelbox(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
-         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode &&
+         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled &&
          s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
          s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
          s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
 }
 
 // The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,
-// no pre-folds, limits, iteration threshold or interior mode).
+// no pre-folds or limits).
 static bool fast_mandelbulb(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
-         !s.ifsFoldingMode && !s.limits_enabled && !s.iterThresh && !s.interiorMode;
+         !s.ifsFoldingMode && !s.limits_enabled;
 }
 
 template <typename T>

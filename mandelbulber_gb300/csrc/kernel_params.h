@@ -41,8 +41,8 @@ struct FractalT {
   int minN;
   int juliaMode, tgladFoldingMode, sphericalFoldingMode;
   int limits, iterThresh, interiorMode;
-  int lean;         // the lean FP32 orbit applies (Mandelbox without rotations, offsets, pre-folds or julia;
-                    // power-8 Mandelbulb without pre-folds): CalculateDistance takes it in FP32
+  int lean;         // the lean FP32 orbit applies (Mandelbox without rotations, offsets, pre-folds, julia or
+                    // limits; power-8 Mandelbulb without pre-folds or limits): CalculateDistance takes it in FP32
   int mbRotEnabled, mbMainRotZero;
   int mbRotZero[2][3];
   T power, constantFactor;

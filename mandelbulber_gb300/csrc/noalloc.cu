@@ -13,8 +13,8 @@
 // Limits: FP32-with-FP64-refinement policy only (MBGB_PREC_FP32_FIX; MBGB_PREC_AUTO is
 // refused, since it would pick FP64 for deep zooms); at most kNaMaxPixels pixels
 // (the overflow pixel list is sized for that); rays longer than a thread slot's step
-// records (256 at the default launch of one 96-thread CTA per SM; fewer with more CTAs per
-// SM, opts->ctas_per_sm) go to the overflow pass (exact, but slower than mbgb_render_device).
+// records (134 at the default launch of two 96-thread CTAs per SM on 152 SMs; 256 at one,
+// opts->ctas_per_sm) go to the overflow pass (exact, but slower than mbgb_render_device).
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -38,6 +38,7 @@ constexpr int kNaSlots = kNaMaxCtas * kNaThreads;    // thread slots of the defa
 constexpr int kNaStepCap = 256;                      // step records per slot of the default launch
 constexpr long long kNaRecords = (long long)kNaStepCap * kNaSlots;   // records per step array
 constexpr int kNaMinStepCap = 32;                    // fewest records per slot a launch may keep
+constexpr int kNaDefaultCtasPerSm = 2;               // default launch: 134 records per slot on 152 SMs
 constexpr long long kNaMaxPixels = 4194304;          // 2048 x 2048; 1920 x 1080 fits
 constexpr int kMaxDevices = 64;
 
@@ -171,10 +172,11 @@ extern "C" mbgb_status mbgb_render_device_noalloc(const mbgb_scene *scene, const
   mbgb::FractalT<double> fd;
   mbgb::prepare_frame_f32(*scene, o, d->ao, aoCount, &p, &fd);
 
-  // CTAs per SM (opts->ctas_per_sm, default 1): more resident warps, each slot then keeping
+  // CTAs per SM (opts->ctas_per_sm, default 2): more resident warps, each slot then keeping
   // fewer step records (the arrays' records divided among the slots); rays longer than that
-  // take the overflow pass
-  const int perSm = o.ctas_per_sm > 0 ? o.ctas_per_sm : 1;
+  // take the overflow pass. 1080p Mandelbox, GB300: 156 / 84 / 80 / 301 ms at 1 / 2 / 3 / 4
+  // CTAs per SM (256 / 134 / 89 / 67 records per slot); 2 keeps headroom for longer rays.
+  const int perSm = o.ctas_per_sm > 0 ? o.ctas_per_sm : kNaDefaultCtasPerSm;
   const long long gridL = (long long)d->sms * perSm;
   const long long slotsL = gridL * kNaThreads;
   if (kNaRecords / slotsL < kNaMinStepCap)

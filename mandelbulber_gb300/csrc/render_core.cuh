@@ -331,6 +331,30 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
   return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
 }
 
+// CalculateDistance after the orbit (src/fractal.cpp:1291-1300, 1436-1445): the clamp at 0,
+// minN, interior mode, the iteration threshold and the limit box, on the orbit's distance
+// and end iteration Li. Shared by the generic and the lean orbits.
+template <typename T>
+__device__ __forceinline__ T distance_post(const FractalT<T> &f, T distance, const int Li, const int N, const int minN,
+                                           const T detailSize, const bool normalMode, const T limitBoxDist,
+                                           bool &maxIter) {
+  maxIter = (Li == N);
+  if (distance < T(0)) distance = T(0);
+  if (Li < minN && distance < detailSize) distance = detailSize;
+  if (f.interiorMode && !normalMode) {
+    if (distance < T(0.5) * detailSize || Li == N) { distance = detailSize; maxIter = false; }
+  } else if (f.interiorMode && normalMode) {
+    if (distance < T(0.9) * detailSize) { distance = detailSize - distance; maxIter = false; }
+  }
+  if (f.iterThresh && Li < N) {
+    if (distance < detailSize) distance = detailSize * T(1.01);
+  }
+  if (f.limits) {
+    if (limitBoxDist < detailSize) distance = (distance > limitBoxDist) ? distance : limitBoxDist;
+  }
+  return distance;
+}
+
 // CalculateDistance, analytic branch (src/fractal.cpp:1245-1300, 1436-1445).
 // `L` (itersOut) is left untouched when the limits box returns early, as in the reference.
 template <typename T, int FORMULA>
@@ -340,20 +364,6 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
   if (FORMULA == 0)
     return calc_distance_runtime<T>(&f, point, detailSize, N, minN, normalMode, &L, &maxIter, &cnt.orbit, &cnt.calls,
                                     &cnt.objectOut, fparam);
-  if constexpr (sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
-    // the lean FP32 orbits (no limits, interior mode or iteration threshold: f.lean says so)
-    if (f.lean) {
-      int Li;
-      T distance;
-      if constexpr (FORMULA == 8) distance = mandelbox_fast(f, point.x, point.y, point.z, N, Li, cnt, fparam);
-      else distance = mandelbulb8_fast<0>(f, point.x, point.y, point.z, N, Li, cnt);
-      maxIter = (Li == N);
-      L = Li;
-      if (distance < T(0)) distance = T(0);
-      if (Li < minN && distance < detailSize) distance = detailSize;
-      return distance;
-    }
-  }
   T limitBoxDist = T(0);
   if (f.limits) {
     // MAX(a, b) = a > b ? a : b (gtk MAX macro)
@@ -371,23 +381,22 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
     }
   }
   int Li;
-  T distance = compute<T, FORMULA, 0>(f, point, N, Li, cnt, fparam);
-  maxIter = (Li == N);
+  T distance;
+  if constexpr (sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
+    // the lean FP32 orbits where the fractal allows them (f.lean): the same distance estimate
+    // without square roots and divisions in the loop (Mandelbox) or transcendentals (power-8
+    // Mandelbulb)
+    if (f.lean) {
+      if constexpr (FORMULA == 8) distance = mandelbox_fast(f, point.x, point.y, point.z, N, Li, cnt, fparam);
+      else distance = mandelbulb8_fast<0>(f, point.x, point.y, point.z, N, Li, cnt);
+    } else {
+      distance = compute<T, FORMULA, 0>(f, point, N, Li, cnt, fparam);
+    }
+  } else {
+    distance = compute<T, FORMULA, 0>(f, point, N, Li, cnt, fparam);
+  }
   L = Li;
-  if (distance < T(0)) distance = T(0);
-  if (Li < minN && distance < detailSize) distance = detailSize;
-  if (f.interiorMode && !normalMode) {
-    if (distance < T(0.5) * detailSize || Li == N) { distance = detailSize; maxIter = false; }
-  } else if (f.interiorMode && normalMode) {
-    if (distance < T(0.9) * detailSize) { distance = detailSize - distance; maxIter = false; }
-  }
-  if (f.iterThresh && Li < N) {
-    if (distance < detailSize) distance = detailSize * T(1.01);
-  }
-  if (f.limits) {
-    if (limitBoxDist < detailSize) distance = (distance > limitBoxDist) ? distance : limitBoxDist;
-  }
-  return distance;
+  return distance_post(f, distance, Li, N, minN, detailSize, normalMode, limitBoxDist, maxIter);
 }
 
 // Counter-hash stand-in for the march jitter Random(1000) (src/Render3D.cpp:129-133):

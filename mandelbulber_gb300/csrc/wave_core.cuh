@@ -230,35 +230,20 @@ __device__ __forceinline__ double polish_distance(const FractalT<double> &f, con
     double distance;
     if constexpr (FORMULA == 8) distance = mandelbox_lean_d(f, p.x, p.y, p.z, f.N, Li, cnt, fparam);
     else distance = mandelbulb8_lean_d(f, p.x, p.y, p.z, f.N, Li, cnt);
-    maxIter = (Li == f.N);
     L = Li;
-    if (distance < 0.0) distance = 0.0;
-    if (Li < f.minN && distance < detail) distance = detail;
-    return distance;
+    return distance_post(f, distance, Li, f.N, f.minN, detail, false, 0.0, maxIter);
   } else {
     return calc_distance<double, FORMULA>(f, p, detail, f.N, f.minN, false, L, maxIter, cnt, fparam);
   }
 }
 
-// CalculateDistance with the orbit chosen at compile time: FAST selects mandelbox_fast
-// (formula 8) or mandelbulb8_fast (formula 2, power 8).
+// CalculateDistance of the wavefront stages: the lean FP32 orbits run where the fractal
+// allows them (FractalT::lean, which the FAST instantiations are launched for).
 template <typename T, int FORMULA, bool FAST>
 __device__ __forceinline__ T wave_distance(const FractalT<T> &f, const V3<T> p, const T detail, const int N,
                                            const int minN, const bool normalMode, int &L, bool &maxIter,
                                            Counters &cnt, const T fparam) {
-  if constexpr (FAST && sizeof(T) == 4) {
-    int Li;
-    T distance;
-    if constexpr (FORMULA == 8) distance = mandelbox_fast(f, p.x, p.y, p.z, N, Li, cnt, fparam);
-    else distance = mandelbulb8_fast<0>(f, p.x, p.y, p.z, N, Li, cnt);
-    maxIter = (Li == N);
-    L = Li;
-    if (distance < T(0)) distance = T(0);
-    if (Li < minN && distance < detail) distance = detail;
-    return distance;
-  } else {
-    return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);
-  }
+  return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);
 }
 
 // SurfaceColour (src/shaders.cpp:850-879) with the fast power-8 colouring orbit when it applies.
@@ -1007,10 +992,9 @@ __device__ __forceinline__ void secondary_lean(const ParamsT<float> &p, const Fr
     if (active && !orbiting) {
       cnt.orbit += (unsigned long long)(orb.L + 1);
       cnt.calls += 1;
-      float d = odist;
-      if (d < 0.0f) d = 0.0f;
-      if (orb.L < minN && d < s.detail) d = s.detail;
-      if (secondary_step(p, wb, s, d, orb.L == orb.N)) {
+      bool mi;
+      const float d = distance_post(p.f, odist, orb.L, orb.N, minN, s.detail, false, 0.0f, mi);
+      if (secondary_step(p, wb, s, d, mi)) {
         active = false;
       } else {
         orb.start(ray_at(s.point, s.dir, s.r), s.fpar);
@@ -1153,19 +1137,19 @@ __global__ void __launch_bounds__(128) secondary_pair_kernel(const __grid_consta
       float d0, d1;
       int L0, L1;
       mandelbox_fast_x2(p.f, q0, f0, q1, f1, N, d0, L0, d1, L1);
-      if (act0) {   // wave_distance's clamps, then the ray's step
+      if (act0) {   // CalculateDistance's post-processing, then the ray's step
         cnt.orbit += (unsigned long long)(L0 + 1);
         cnt.calls += 1;
-        if (d0 < 0.0f) d0 = 0.0f;
-        if (L0 < minN && d0 < s0.detail) d0 = s0.detail;
-        if (secondary_step(p, wb, s0, d0, L0 == N)) act0 = false;
+        bool mi;
+        d0 = distance_post(p.f, d0, L0, N, minN, s0.detail, false, 0.0f, mi);
+        if (secondary_step(p, wb, s0, d0, mi)) act0 = false;
       }
       if (act1) {
         cnt.orbit += (unsigned long long)(L1 + 1);
         cnt.calls += 1;
-        if (d1 < 0.0f) d1 = 0.0f;
-        if (L1 < minN && d1 < s1.detail) d1 = s1.detail;
-        if (secondary_step(p, wb, s1, d1, L1 == N)) act1 = false;
+        bool mi;
+        d1 = distance_post(p.f, d1, L1, N, minN, s1.detail, false, 0.0f, mi);
+        if (secondary_step(p, wb, s1, d1, mi)) act1 = false;
       }
     }
   }
