@@ -232,11 +232,12 @@ static bool need_volumetric(const mbgb_scene &s) {
 }
 
 // Features that the per-pixel engine renders and the wavefront stages do not carry (aux,
-// fake and volumetric lights, iteration fog, slow shading, environment mapping): scenes
-// that use them render on the per-pixel engine.
+// fake and volumetric lights, iteration fog, ray-traced reflections): scenes that use them
+// render on the per-pixel engine. Slow shading, environment mapping and primitive objects
+// are composition-stage work the wavefront carries.
 static bool per_pixel_only(const mbgb_scene &s) {
   return uses_aux_lights(s) || s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled ||
-         s.slowShading || (!s.raytracedReflections && s.reflect > 0) || uses_primitives(s) || reflection_rays(s) > 1;
+         reflection_rays(s) > 1;
 }
 
 // The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights and the
@@ -245,23 +246,29 @@ static int scene_kernel_formula(const mbgb_scene &s) {
   return kernel_formula(s.formula, s.ifsFoldingMode || s.fakeLightsEnabled || uses_primitives(s));
 }
 
+// The instantiation CalculateDistance of a scene runs (the wavefront stages, distance probes,
+// light placement): the primitive objects need the run-time formula path.
+static int distance_kernel_formula(const mbgb_scene &s) {
+  return kernel_formula(s.formula, s.ifsFoldingMode || uses_primitives(s));
+}
+
 // The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
-// julia or limits, fold value = 2 x fold limit, and min radius <= fixed radius (so that the
+// julia, limits or primitive objects, fold value = 2 x fold limit, and min radius <= fixed radius (so that the
 // sphere fold is a clamp). Interior mode and the iteration threshold only post-process the
 // orbit's result (distance_post), which every path applies.
 static bool fast_mandelbox(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
-         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled &&
+         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled && !uses_primitives(s) &&
          s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
          s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
          s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
 }
 
 // The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,
-// no pre-folds or limits).
+// no pre-folds, limits or primitive objects).
 static bool fast_mandelbulb(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
-         !s.ifsFoldingMode && !s.limits_enabled;
+         !s.ifsFoldingMode && !s.limits_enabled && !uses_primitives(s);
 }
 
 template <typename T>
@@ -918,7 +925,7 @@ static void fill_cam(const mbgb_scene &s, const mbgb_image &img, const mbgb_opts
 
 // Scenes whose distance estimate the dual-number orbit (exact hits, gradients) covers:
 // formula 2, or formula 8 without rotations, offset or pre-folds, and the analytic
-// estimate without limits, iteration threshold or interior mode.
+// estimate without limits, iteration threshold, interior mode or primitive objects.
 static mbgb_status level_set_supported(const mbgb_scene &s) {
   if (s.formula != MBGB_FORMULA_TRIG_OPTIM && s.formula != MBGB_FORMULA_TGLAD)
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: formulas 2 and 8 only");
@@ -930,6 +937,7 @@ static mbgb_status level_set_supported(const mbgb_scene &s) {
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: Mandelbox rotations or offset");
   if (s.limits_enabled || s.iterThresh || s.interiorMode)
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: limits, iteration threshold or interior mode");
+  if (uses_primitives(s)) return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: primitive objects");
   return MBGB_OK;
 }
 
@@ -939,6 +947,8 @@ static mbgb_status grad_supported(const mbgb_scene &s) {
   if (need_volumetric(s)) return set_error(MBGB_ERR_UNSUPPORTED, "gradients: glow or fog");
   if (s.shadow && (s.penetratingLights || tan(s.shadowConeAngle / 180.0 * M_PI) > 0.0))
     return set_error(MBGB_ERR_UNSUPPORTED, "gradients: soft or penetrating shadows");
+  // the gradient differentiates the four-sample normal of the fractal
+  if (s.slowShading) return set_error(MBGB_ERR_UNSUPPORTED, "gradients: slow shading");
   return MBGB_OK;
 }
 
@@ -1100,7 +1110,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   MBGB_CUDA(cudaMemsetAsync(ctl, 0, 64, s));
 
   const int block = g.cfg.block;
-  const int kf = kernel_formula(scene.formula, scene.ifsFoldingMode);
+  const int kf = distance_kernel_formula(scene);
   int occ1 = std::max(1, wave_occupancy<T>(kf, block, 0));
   int occ2 = std::max(1, wave_occupancy<T>(kf, block, wb.pair_rays ? 2 : 1));
   if (g.cfg.ctasPerSm > 0) {
@@ -1258,7 +1268,7 @@ static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int
   for (int i = 0; i < n; i++) {
     FractalT<double> fp;
     fill_fractal<double>(scenes[i], fp);
-    cudaError_t pe = launch_distance_f64(kernel_formula(scenes[i].formula, scenes[i].ifsFoldingMode), fp, (const double *)(pb + o_pts) + 3 * i,
+    cudaError_t pe = launch_distance_f64(distance_kernel_formula(scenes[i]), fp, (const double *)(pb + o_pts) + 3 * i,
                                          (const double *)(pb + o_det) + i, 1, (double *)(pb + o_d) + i,
                                          (int *)(pb + o_it) + i, (unsigned char *)(pb + o_mi) + i, nullptr, s);
     if (pe != cudaSuccess) return cuda_error(pe, "precision probe");
@@ -1338,7 +1348,7 @@ static mbgb_status place_lights(mbgb_context *c, const mbgb_scene &s, cudaStream
     constexpr long long kMaxTrials = 20000000;  // the reference loops for ever on a scene no light fits
     FractalT<double> f;
     fill_fractal<double>(s, f);
-    const int kf = kernel_formula(s.formula, s.ifsFoldingMode);
+    const int kf = distance_kernel_formula(s);
     const size_t o_pts = 0, o_det = 24 * kBatch, o_d = o_det + 8 * kBatch, o_it = o_d + 8 * kBatch,
                  o_mi = o_it + 4 * kBatch;
     MBGB_CUDA(c->ensure(c->lightprobe, o_mi + kBatch + 16));
@@ -1905,7 +1915,7 @@ static mbgb_status autotune_impl(mbgb_context *c, const mbgb_scene *scene, const
     if ((st = consider(cand)) != MBGB_OK) return st;
   }
   {
-    const int kf = kernel_formula(scene->formula, scene->ifsFoldingMode);
+    const int kf = distance_kernel_formula(*scene);
     const int occ = std::max(1, prec == 0 ? occupancy_wave_f64(kf, cur.block, 0) : occupancy_wave_f32(kf, cur.block, 0));
     if (occ >= 2) {
       LaunchCfg cand = cur;
@@ -2087,12 +2097,12 @@ extern "C" mbgb_status mbgb_distance_device(mbgb_context *c, const mbgb_scene *s
   if (precision == MBGB_PREC_FP64 || !scene->analitycDE) {  // delta-DE: FP64 under every policy
     FractalT<double> f;
     fill_fractal<double>(*scene, f);
-    e = launch_distance_f64(kernel_formula(scene->formula, scene->ifsFoldingMode), f, points, detail, n, dist, iters,
+    e = launch_distance_f64(distance_kernel_formula(*scene), f, points, detail, n, dist, iters,
                             max_iter, nullptr, c->stream);
   } else {
     FractalT<float> f;
     fill_fractal<float>(*scene, f);
-    e = launch_distance_f32(kernel_formula(scene->formula, scene->ifsFoldingMode), f, points, detail, n, dist, iters,
+    e = launch_distance_f32(distance_kernel_formula(*scene), f, points, detail, n, dist, iters,
                             max_iter, nullptr, c->stream);
   }
   if (e != cudaSuccess) return cuda_error(e, "distance kernel launch");

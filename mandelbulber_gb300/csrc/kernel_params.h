@@ -31,6 +31,13 @@ inline int kernel_formula(int formula, bool ifsFolding) {
   return ((formula == 2 || formula == 8) && !ifsFolding) ? formula : 0;
 }
 
+template <typename T>
+struct FractalT;
+// Primitive objects next to (or instead of) the fractal: CalculateDistance then takes the
+// nearest object (src/fractal.cpp:1383-1435), which only the run-time formula path carries.
+template <typename T>
+inline bool fractal_has_primitives(const FractalT<T> &f);
+
 // Fractal / distance-estimator parameters (sFractal, src/fractal.h:255-293).
 template <typename T>
 struct FractalT {
@@ -93,6 +100,12 @@ struct FractalT {
   T sphereCentre[3], sphereRadius, invSphereCentre[3], invSphereRadius;
   T waterHeight, waterAmplitude, waterLength, waterRotation, waterAnimSpeed;
 };
+
+template <typename T>
+inline bool fractal_has_primitives(const FractalT<T> &f) {
+  return f.planeEnable || f.boxEnable || f.invertedBoxEnable || f.sphereEnable || f.invertedSphereEnable ||
+         f.waterEnable || f.onlyPlane;
+}
 
 // enumObjectType (src/fractal.h:82-91): the object a CalculateDistance call ended on.
 enum { kObjFractal = 0, kObjPlane = 1, kObjWater = 2, kObjSphere = 3, kObjSphereInv = 4, kObjBox = 5, kObjBoxInv = 6 };

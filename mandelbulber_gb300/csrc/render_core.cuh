@@ -654,8 +654,20 @@ __device__ __forceinline__ void refine_fix(const ParamsT<float> &p, const Fracta
 // minN 0), or with slow shading the average of point2 x distance over the 11^3 offsets
 // point2 in [-1, 1]^3 (steps of 0.2, accumulated in double as the reference's loop does).
 template <typename T, int FORMULA>
+__device__ __forceinline__ V3<T> calc_normal_fp(const ParamsT<T> &p, const V3<T> point, const T delta,
+                                                const T dist_thresh, const T detail, Counters &cnt, const T fparam);
+
+// CalculateNormals at the fractal's own parameter (a frame of a batch may carry its own:
+// calc_normal_fp).
+template <typename T, int FORMULA>
 __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> point, const T delta, const T dist_thresh,
                                              const T detail, Counters &cnt) {
+  return calc_normal_fp<T, FORMULA>(p, point, delta, dist_thresh, detail, cnt, fparam_of(p.f));
+}
+
+template <typename T, int FORMULA>
+__device__ __forceinline__ V3<T> calc_normal_fp(const ParamsT<T> &p, const V3<T> point, const T delta,
+                                                const T dist_thresh, const T detail, Counters &cnt, const T fparam) {
   T dn = delta * p.smoothness;
   if (p.f.interiorMode) dn = dist_thresh * p.quality * T(0.2) * p.smoothness;
   int L;
@@ -663,13 +675,13 @@ __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> po
   const int N5 = p.f.N5;
   V3<T> n;
   if (!p.slowShading) {
-    const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam_of(p.f));
+    const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam);
     const T s2 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
-                                           true, L, mi, cnt, fparam_of(p.f));
+                                           true, L, mi, cnt, fparam);
     const T s3 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
-                                           true, L, mi, cnt, fparam_of(p.f));
+                                           true, L, mi, cnt, fparam);
     const T s4 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
-                                           true, L, mi, cnt, fparam_of(p.f));
+                                           true, L, mi, cnt, fparam);
     n = V3<T>{s2 - s1, s3 - s1, s4 - s1};
   } else {
     n = V3<T>{T(0), T(0), T(0)};
@@ -678,7 +690,7 @@ __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> po
         for (double pz = -1.0; pz <= 1.0; pz += 0.2) {
           const V3<T> p2{(T)px, (T)py, (T)pz};
           const T dist = calc_distance<T, FORMULA>(p.f, point + p2 * dn, detail, N5, p.f.minN, true, L, mi, cnt,
-                                                   fparam_of(p.f));
+                                                   fparam);
           n = n + p2 * dist;
         }
       }

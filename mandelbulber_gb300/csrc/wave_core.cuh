@@ -249,7 +249,7 @@ __device__ __forceinline__ T wave_distance(const FractalT<T> &f, const V3<T> p, 
 // SurfaceColour (src/shaders.cpp:850-879) with the fast power-8 colouring orbit when it applies.
 template <typename T, int FORMULA, bool FAST>
 __device__ __forceinline__ V3<T> wave_colour(const ParamsT<T> &p, const V3<T> point, Counters &cnt,
-                                             const T fparam) {
+                                             const T fparam, const int objectType = kObjFractal) {
   if constexpr (FAST && FORMULA == 2 && sizeof(T) == 4) {
     int L;
     const float c = mandelbulb8_fast<1>(p.f, point.x, point.y, point.z, p.f.N10, L, cnt);
@@ -263,7 +263,7 @@ __device__ __forceinline__ V3<T> wave_colour(const ParamsT<T> &p, const V3<T> po
     }
     return V3<T>{T(rgb[0]) / T(256), T(rgb[1]) / T(256), T(rgb[2]) / T(256)};
   } else {
-    return surface_colour<T, FORMULA>(p, point, cnt, fparam);
+    return surface_colour<T, FORMULA>(p, point, cnt, fparam, objectType);
   }
 }
 
@@ -644,7 +644,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
       if (++guardSteps > (1 << 24)) done = true;
       if (done) {
         const bool found = phase == 1;
-        uint8_t flags = found ? 1 : 0;
+        // bits 4-6: the object the last distance estimate ended on (primitives; 0 = fractal)
+        uint8_t flags = (uint8_t)((found ? 1 : 0) | ((cnt.objectOut & 7) << 4));
         if (io.overflow_pass && useSB) {
           // rare long rays: fold the records now (the slot is reused); compose applies the map
           T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
@@ -760,6 +761,7 @@ __global__ void __launch_bounds__(128) polish_kernel(const __grid_constant__ Par
     wb.dist[gp] = (float)dist;
     wb.thr[gp] = (float)thr;
     wb.iters[gp] = iters;
+    wb.flags[gp] = (uint8_t)((wb.flags[gp] & 0x8f) | ((cnt.objectOut & 7) << 4));
     wb.point[0 * wb.npix + gp] = (float)point.x;
     wb.point[1 * wb.npix + gp] = (float)point.y;
     wb.point[2 * wb.npix + gp] = (float)point.z;
@@ -1331,22 +1333,10 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
     T base[3];
     if (hit) {
       const HitInfo<T> h = hit_info(p, c, wb, gp);
-      // CalculateNormals (src/shaders.cpp:675-711): 4 DEs at N x 5, minN 0
-      T dn = h.delta * p.smoothness;
-      if (p.f.interiorMode) dn = h.thr * p.quality * T(0.2) * p.smoothness;
-      int L;
-      bool mi;
-      const int N5 = p.f.N5;
-      const T s1 = wave_distance<T, FORMULA, FAST>(p.f, h.point, h.thr, N5, 0, true, L, mi, cnt, c.fparam);
-      const T s2 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + dn, h.point.y + T(0), h.point.z + T(0)},
-                                                   h.thr, N5, 0, true, L, mi, cnt, c.fparam);
-      const T s3 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + T(0), h.point.y + dn, h.point.z + T(0)},
-                                                   h.thr, N5, 0, true, L, mi, cnt, c.fparam);
-      const T s4 = wave_distance<T, FORMULA, FAST>(p.f, V3<T>{h.point.x + T(0), h.point.y + T(0), h.point.z + dn},
-                                                   h.thr, N5, 0, true, L, mi, cnt, c.fparam);
-      V3<T> nrm{s2 - s1, s3 - s1, s4 - s1};
-      if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
-      else nrm = normalize3(nrm);
+      // CalculateNormals (src/shaders.cpp:675-757): 4 DEs at N x 5, minN 0, or the slow
+      // shading's 11^3 samples
+      const V3<T> nrm = calc_normal_fp<T, FORMULA>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+      const int objectType = (flags >> 4) & 7;
       T shade = dot3(nrm, lv);
       if (shade < T(0)) shade = T(0);
       const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
@@ -1357,7 +1347,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
       shade2 = m_pow(shade2, T(30)) * T(1);
       if (shade2 > T(15)) shade2 = T(15);
       const T spec = shade2 * p.specular;
-      const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt, c.fparam);
+      const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt, c.fparam, objectType);
       objColour = colour;
       V3<T> ambient{T(0), T(0), T(0)};
       if (p.ao) {
@@ -1376,9 +1366,13 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
         }
       }
       const T a2x = ambient.x * p.globalIlum, a2y = ambient.y * p.globalIlum, a2z = ambient.z * p.globalIlum;
-      const T objR = T(0) + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
-      const T objG = T(0) + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
-      const T objB = T(0) + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
+      // environment mapping (ObjectShader, src/shaders.cpp:71-76) of the default white texture
+      const T env = (p.envMapping ? (T)env_mapping(V3<double>{(double)nrm.x, (double)nrm.y, (double)nrm.z},
+                                                   V3<double>{(double)viewT.x, (double)viewT.y, (double)viewT.z})
+                                  : T(0)) * p.reflect;
+      const T objR = env * ambient.x + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
+      const T objG = env * ambient.y + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
+      const T objB = env * ambient.z + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
       base[0] = objR + T(0) + (T(0) + p.mainLight[0] * spec * shadow);
       base[1] = objG + T(0) + (T(0) + p.mainLight[1] * spec * shadow);
       base[2] = objB + T(0) + (T(0) + p.mainLight[2] * spec * shadow);

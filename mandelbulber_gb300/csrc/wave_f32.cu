@@ -5,7 +5,7 @@
 namespace mbgb {
 
 cudaError_t launch_wave_f32(const WaveLaunch<float> &L, cudaStream_t s) {
-  const int kf = kernel_formula(L.p.f.formula, L.p.f.ifsFolding);
+  const int kf = kernel_formula(L.p.f.formula, L.p.f.ifsFolding || fractal_has_primitives(L.p.f));
   if (kf == 2) return L.fast ? run_stages<float, 2, true>(L, s) : run_stages<float, 2, false>(L, s);
   if (kf == 8) return L.fast ? run_stages<float, 8, true>(L, s) : run_stages<float, 8, false>(L, s);
   return launch_wave_f32_runtime(L, s);

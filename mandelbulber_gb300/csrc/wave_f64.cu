@@ -5,7 +5,7 @@
 namespace mbgb {
 
 cudaError_t launch_wave_f64(const WaveLaunch<double> &L, cudaStream_t s) {
-  const int kf = kernel_formula(L.p.f.formula, L.p.f.ifsFolding);
+  const int kf = kernel_formula(L.p.f.formula, L.p.f.ifsFolding || fractal_has_primitives(L.p.f));
   if (kf == 2) return L.fast ? run_stages<double, 2, false>(L, s) : run_stages<double, 2, false>(L, s);
   if (kf == 8) return L.fast ? run_stages<double, 8, false>(L, s) : run_stages<double, 8, false>(L, s);
   return launch_wave_f64_runtime(L, s);
