@@ -286,6 +286,7 @@ static void fill_fractal(const mbgb_scene &s, FractalT<T> &f) {
   f.limits = s.limits_enabled;
   f.iterThresh = s.iterThresh;
   f.interiorMode = s.interiorMode;
+  f.distPost = (s.limits_enabled || s.iterThresh || s.interiorMode) ? 1 : 0;
   f.mbRotEnabled = s.mboxRotationsEnabled;
   f.mbMainRotZero = s.mboxMainRotZero;
   f.power = (T)s.power;

@@ -48,6 +48,7 @@ struct FractalT {
   int minN;
   int juliaMode, tgladFoldingMode, sphericalFoldingMode;
   int limits, iterThresh, interiorMode;
+  int distPost;     // limits || iterThresh || interiorMode: CalculateDistance post-processes the orbit's result
   int lean;         // the lean FP32 orbit applies (Mandelbox without rotations, offsets, pre-folds, julia or
                     // limits; power-8 Mandelbulb without pre-folds or limits): CalculateDistance takes it in FP32
   int mbRotEnabled, mbMainRotZero;

@@ -341,6 +341,7 @@ __device__ __forceinline__ T distance_post(const FractalT<T> &f, T distance, con
   maxIter = (Li == N);
   if (distance < T(0)) distance = T(0);
   if (Li < minN && distance < detailSize) distance = detailSize;
+  if (!f.distPost) return distance;   // none of the three below: one uniform test per estimate
   if (f.interiorMode && !normalMode) {
     if (distance < T(0.5) * detailSize || Li == N) { distance = detailSize; maxIter = false; }
   } else if (f.interiorMode && normalMode) {
@@ -397,6 +398,26 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
   }
   L = Li;
   return distance_post(f, distance, Li, N, minN, detailSize, normalMode, limitBoxDist, maxIter);
+}
+
+// CalculateDistance with the lean orbit chosen at compile time: LEAN (the FP32 instantiations
+// launched for FractalT::lean scenes) calls the lean orbit directly, so that the kernel holds
+// no generic orbit; otherwise calc_distance.
+template <typename T, int FORMULA, bool LEAN>
+__device__ __forceinline__ T distance_est(const FractalT<T> &f, const V3<T> p, const T detail, const int N,
+                                          const int minN, const bool normalMode, int &L, bool &maxIter,
+                                          Counters &cnt, const T fparam) {
+  if constexpr (LEAN && sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
+    int Li;
+    T distance;
+    if constexpr (FORMULA == 8) distance = mandelbox_fast(f, p.x, p.y, p.z, N, Li, cnt, fparam);
+    else distance = mandelbulb8_fast<0>(f, p.x, p.y, p.z, N, Li, cnt);
+    L = Li;
+    // the lean scenes have no limits box (FractalT::lean), so its distance is 0 here
+    return distance_post(f, distance, Li, N, minN, detail, normalMode, T(0), maxIter);
+  } else {
+    return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);
+  }
 }
 
 // Counter-hash stand-in for the march jitter Random(1000) (src/Render3D.cpp:129-133):
@@ -653,7 +674,7 @@ __device__ __forceinline__ void refine_fix(const ParamsT<float> &p, const Fracta
 // CalculateNormals (src/shaders.cpp:675-757): forward differences of the distance (N x 5,
 // minN 0), or with slow shading the average of point2 x distance over the 11^3 offsets
 // point2 in [-1, 1]^3 (steps of 0.2, accumulated in double as the reference's loop does).
-template <typename T, int FORMULA>
+template <typename T, int FORMULA, bool LEAN = false>
 __device__ __forceinline__ V3<T> calc_normal_fp(const ParamsT<T> &p, const V3<T> point, const T delta,
                                                 const T dist_thresh, const T detail, Counters &cnt, const T fparam);
 
@@ -665,7 +686,7 @@ __device__ __forceinline__ V3<T> calc_normal(const ParamsT<T> &p, const V3<T> po
   return calc_normal_fp<T, FORMULA>(p, point, delta, dist_thresh, detail, cnt, fparam_of(p.f));
 }
 
-template <typename T, int FORMULA>
+template <typename T, int FORMULA, bool LEAN>
 __device__ __forceinline__ V3<T> calc_normal_fp(const ParamsT<T> &p, const V3<T> point, const T delta,
                                                 const T dist_thresh, const T detail, Counters &cnt, const T fparam) {
   T dn = delta * p.smoothness;
@@ -675,12 +696,12 @@ __device__ __forceinline__ V3<T> calc_normal_fp(const ParamsT<T> &p, const V3<T>
   const int N5 = p.f.N5;
   V3<T> n;
   if (!p.slowShading) {
-    const T s1 = calc_distance<T, FORMULA>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam);
-    const T s2 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
+    const T s1 = distance_est<T, FORMULA, LEAN>(p.f, point, detail, N5, 0, true, L, mi, cnt, fparam);
+    const T s2 = distance_est<T, FORMULA, LEAN>(p.f, V3<T>{point.x + dn, point.y + T(0), point.z + T(0)}, detail, N5, 0,
                                            true, L, mi, cnt, fparam);
-    const T s3 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
+    const T s3 = distance_est<T, FORMULA, LEAN>(p.f, V3<T>{point.x + T(0), point.y + dn, point.z + T(0)}, detail, N5, 0,
                                            true, L, mi, cnt, fparam);
-    const T s4 = calc_distance<T, FORMULA>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
+    const T s4 = distance_est<T, FORMULA, LEAN>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dn}, detail, N5, 0,
                                            true, L, mi, cnt, fparam);
     n = V3<T>{s2 - s1, s3 - s1, s4 - s1};
   } else {
@@ -689,7 +710,7 @@ __device__ __forceinline__ V3<T> calc_normal_fp(const ParamsT<T> &p, const V3<T>
       for (double py = -1.0; py <= 1.0; py += 0.2) {
         for (double pz = -1.0; pz <= 1.0; pz += 0.2) {
           const V3<T> p2{(T)px, (T)py, (T)pz};
-          const T dist = calc_distance<T, FORMULA>(p.f, point + p2 * dn, detail, N5, p.f.minN, true, L, mi, cnt,
+          const T dist = distance_est<T, FORMULA, LEAN>(p.f, point + p2 * dn, detail, N5, p.f.minN, true, L, mi, cnt,
                                                    fparam);
           n = n + p2 * dist;
         }

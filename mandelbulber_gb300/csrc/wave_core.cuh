@@ -237,13 +237,14 @@ __device__ __forceinline__ double polish_distance(const FractalT<double> &f, con
   }
 }
 
-// CalculateDistance of the wavefront stages: the lean FP32 orbits run where the fractal
-// allows them (FractalT::lean, which the FAST instantiations are launched for).
+// CalculateDistance of the wavefront stages. The FAST instantiations (launched where the
+// fractal allows the lean FP32 orbits, FractalT::lean) call the lean orbit directly, so that
+// their code holds no generic orbit; the others take calc_distance.
 template <typename T, int FORMULA, bool FAST>
 __device__ __forceinline__ T wave_distance(const FractalT<T> &f, const V3<T> p, const T detail, const int N,
                                            const int minN, const bool normalMode, int &L, bool &maxIter,
                                            Counters &cnt, const T fparam) {
-  return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);
+  return distance_est<T, FORMULA, FAST>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);
 }
 
 // SurfaceColour (src/shaders.cpp:850-879) with the fast power-8 colouring orbit when it applies.
@@ -1335,7 +1336,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
       const HitInfo<T> h = hit_info(p, c, wb, gp);
       // CalculateNormals (src/shaders.cpp:675-757): 4 DEs at N x 5, minN 0, or the slow
       // shading's 11^3 samples
-      const V3<T> nrm = calc_normal_fp<T, FORMULA>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+      const V3<T> nrm = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
       const int objectType = (flags >> 4) & 7;
       T shade = dot3(nrm, lv);
       if (shade < T(0)) shade = T(0);

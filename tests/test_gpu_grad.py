@@ -29,10 +29,12 @@ from tests import metrics, oracle_lib
 pytestmark = pytest.mark.gpu
 H = 1e-4
 REL_TOL = 1e-3
-# Least fraction of all pixels each parameter's interior mask must cover (the frames are 256 x
-# 256, about half of the pixels hit): power, camera x / y / z, light alpha / beta.
-MASK_FLOOR = [0.005] * 6
-ORACLE_MASK_FLOOR = [0.02] * 6
+# Least fraction of all pixels each parameter's interior mask must cover: power, camera
+# x / y / z, light alpha / beta. The seeded 256 x 256 frames (about 30 % of the pixels hit)
+# measure 18.1 / 5.0 / 12.9 / 3.4 / 25.9 / 27.4 % on the GPU renders (both policies) and
+# 17.7 / 5.1 / 13.2 / 3.7 / 25.4 / 27.0 % on the oracle's; the floors sit at ~80 % of that.
+MASK_FLOOR = [0.145, 0.04, 0.103, 0.027, 0.207, 0.219]
+ORACLE_MASK_FLOOR = [0.141, 0.041, 0.105, 0.029, 0.203, 0.216]
 
 
 @pytest.fixture(scope="module")
