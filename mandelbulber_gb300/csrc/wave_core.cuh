@@ -1301,6 +1301,63 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
   }
 }
 
+// The slow shading's normal (CalculateNormals, src/shaders.cpp:713-757): the sum over the
+// 11^3 offsets p2 in [-1, 1]^3 (steps of 0.2 accumulated in double, as the reference's loop
+// forms them) of p2 x distance(point + p2 dn). One pixel's 1331 estimates are up to
+// 1331 x N5 orbit iterations, which on one lane bound the whole frame; here the warp computes
+// them for each of its hit pixels in turn, 42 per lane, into shared memory, and the pixel's
+// own lane sums them in the reference's loop order (so the FP64 sum is the reference's).
+// `need` marks the lanes whose pixel is a hit; each gets its unnormalised sum in `sum`.
+// `axis` is the warp's 11-entry table of offsets in shared memory.
+constexpr int kSlowAxis = 11, kSlowSamples = kSlowAxis * kSlowAxis * kSlowAxis;
+template <typename T, int FORMULA, bool FAST>
+__device__ __forceinline__ void slow_normal_warp(const ParamsT<T> &p, const WaveBufs<T> &wb,
+                                              const FrameCam<T> *__restrict__ cams, const int ncams,
+                                              const int64_t gw, const bool need, T *dists, T *axis, V3<T> *sum,
+                                              Counters *cntOut) {
+  const unsigned int lane = threadIdx.x & 31u;
+  Counters cnt{0, 0, 0, 0};
+  if (lane == 0) {
+    double v = -1.0;
+    for (int i = 0; i < kSlowAxis; i++) {   // -1.0, -0.8, ... 0.9999999999999999 (<= 1.0)
+      axis[i] = (T)v;
+      v += 0.2;
+    }
+  }
+  __syncwarp();
+  unsigned int mask = __ballot_sync(0xffffffffu, need);
+  while (mask) {
+    const unsigned int j = (unsigned int)(__ffs(mask) - 1);
+    mask &= mask - 1u;
+    const int64_t gj = gw + j;
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gj)];
+    const HitInfo<T> h = hit_info(p, c, wb, gj);
+    T dn = h.delta * p.smoothness;
+    if (p.f.interiorMode) dn = h.thr * p.quality * T(0.2) * p.smoothness;
+    for (int k = (int)lane; k < kSlowSamples; k += 32) {
+      const int ix = k / (kSlowAxis * kSlowAxis), iy = (k / kSlowAxis) % kSlowAxis, iz = k % kSlowAxis;
+      const V3<T> p2{axis[ix], axis[iy], axis[iz]};
+      int L;
+      bool mi;
+      dists[k] = distance_est<T, FORMULA, FAST>(p.f, h.point + p2 * dn, h.thr, p.f.N5, p.f.minN, true, L, mi, cnt,
+                                                c.fparam);
+    }
+    __syncwarp();
+    if (lane == j) {
+      V3<T> n{T(0), T(0), T(0)};
+      for (int k = 0; k < kSlowSamples; k++) {
+        const int ix = k / (kSlowAxis * kSlowAxis), iy = (k / kSlowAxis) % kSlowAxis, iz = k % kSlowAxis;
+        const V3<T> p2{axis[ix], axis[iy], axis[iz]};
+        n = n + p2 * dists[k];
+      }
+      *sum = n;
+    }
+    __syncwarp();
+  }
+  cntOut->orbit += cnt.orbit;
+  cntOut->calls += cnt.calls;
+}
+
 // ---------------------------------------------------------------------------
 // Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589),
 // over every pixel of the batch.
@@ -1325,6 +1382,14 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
     const bool valid = inBatch && y >= c.row_begin && y < c.row_end;
     T out0 = T(0), out1 = T(0), out2 = T(0);
     V3<T> objColour{T(0), T(0), T(0)};
+    V3<T> slowSum{T(0), T(0), T(0)};
+    if (p.slowShading) {   // the warp's hit pixels' slow-shading normals, computed together
+      extern __shared__ __align__(16) unsigned char composeDyn[];
+      __shared__ T slowAxis[4][kSlowAxis];
+      T *dists = reinterpret_cast<T *>(composeDyn) + (size_t)warp * kSlowSamples;
+      slow_normal_warp<T, FORMULA, FAST>(p, wb, cams, ncams, gw, valid && (wb.flags[gp] & 1), dists, slowAxis[warp],
+                                         &slowSum, &cnt);
+    }
     if (valid) {
     const uint8_t flags = wb.flags[gp];
     const bool hit = (flags & 1) != 0;
@@ -1336,7 +1401,14 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
       const HitInfo<T> h = hit_info(p, c, wb, gp);
       // CalculateNormals (src/shaders.cpp:675-757): 4 DEs at N x 5, minN 0, or the slow
       // shading's 11^3 samples
-      const V3<T> nrm = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+      V3<T> nrm;
+      if (p.slowShading) {
+        nrm = slowSum;
+        if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
+        else nrm = normalize3(nrm);
+      } else {
+        nrm = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+      }
       const int objectType = (flags >> 4) & 7;
       T shade = dot3(nrm, lv);
       if (shade < T(0)) shade = T(0);

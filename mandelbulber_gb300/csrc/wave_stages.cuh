@@ -32,7 +32,10 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   if (!pair)
     dev::secondary_kernel<T, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
   mark(4);
-  dev::compose_kernel<T, F, FAST><<<L.compose_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
+  // slow shading: one warp's 11^3 normal samples in dynamic shared memory per warp
+  const size_t composeSmem = L.p.slowShading ? (size_t)(L.block / 32) * dev::kSlowSamples * sizeof(T) : 0;
+  dev::compose_kernel<T, F, FAST><<<L.compose_grid, L.block, composeSmem, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams,
+                                                                             L.ncams);
   mark(5);
   if (L.gcams)
     dev::grad_kernel<T, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 5), L.wb, L.cams, L.gcams,
