@@ -212,7 +212,9 @@ enum {
   MBGB_PREC_FP32_FIX = 1,      /* FP32 march/orbit with FP64 camera origin and FP64 hit refinement */
   MBGB_PREC_AUTO = 2           /* FP32_FIX unless the pixel footprint at the nearest surface (FP64 distance
                                 * estimate at the ray origin x resolution x persp / quality) is below 1e-5 of
-                                * the scene scale, then FP64 for the whole frame; the probe synchronises */
+                                * the scene scale, or the scene has the limit box (limits_enabled: its cut
+                                * faces expose the fractal's interior, whose colouring orbits FP32 does not
+                                * reproduce), then FP64 for the whole frame; the probe synchronises */
 };
 
 typedef struct mbgb_opts {

@@ -253,22 +253,23 @@ static int distance_kernel_formula(const mbgb_scene &s) {
 }
 
 // The lean FP32 Mandelbox orbit applies: formula 8 without rotations, offset, pre-folds,
-// julia, limits or primitive objects, fold value = 2 x fold limit, and min radius <= fixed radius (so that the
-// sphere fold is a clamp). Interior mode and the iteration threshold only post-process the
-// orbit's result (distance_post), which every path applies.
+// julia or primitive objects, fold value = 2 x fold limit, and min radius <= fixed radius (so
+// that the sphere fold is a clamp). The limit box, interior mode and the iteration threshold
+// only test the point before the orbit or post-process its result (limit_box, distance_post),
+// which every lean path applies.
 static bool fast_mandelbox(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TGLAD && !s.mboxRotationsEnabled && s.mboxMainRotZero && !s.juliaMode &&
-         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !s.limits_enabled && !uses_primitives(s) &&
+         !s.tgladFoldingMode && !s.sphericalFoldingMode && !s.ifsFoldingMode && !uses_primitives(s) &&
          s.mboxOffset[0] == 0.0 && s.mboxOffset[1] == 0.0 && s.mboxOffset[2] == 0.0 &&
          s.mboxFoldingValue == 2.0 * s.mboxFoldingLimit &&
          s.mboxFoldingSphericalMin <= s.mboxFoldingSphericalFixed;
 }
 
 // The power-8 Mandelbulb orbit without transcendentals applies (formula 2, power 8,
-// no pre-folds, limits or primitive objects).
+// no pre-folds or primitive objects).
 static bool fast_mandelbulb(const mbgb_scene &s) {
   return s.formula == MBGB_FORMULA_TRIG_OPTIM && s.power == 8.0 && !s.tgladFoldingMode && !s.sphericalFoldingMode &&
-         !s.ifsFoldingMode && !s.limits_enabled && !uses_primitives(s);
+         !s.ifsFoldingMode && !uses_primitives(s);
 }
 
 template <typename T>
@@ -1141,7 +1142,9 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.ov.step_thr = c->ovstep[prec][2].ptr;
   L.overflow = needVol;
   for (int k = 0; k < kStageEvents; k++) L.ev[k] = ev ? ev[k] : nullptr;
-  L.fast = fast_mandelbox(scene) || fast_mandelbulb(scene);
+  // the FAST instantiations hold no limit box test: limit-box scenes take the generic kernels,
+  // whose CalculateDistance runs the lean orbit after the box test (FractalT::lean)
+  L.fast = (fast_mandelbox(scene) || fast_mandelbulb(scene)) && !scene.limits_enabled;
   fill_fractal<double>(scene, L.fd);
   fill_params<T>(scene, L.p, o, (const T *)(prec == 0 ? c->ao64.ptr : c->ao32.ptr), c->ao_count);
   cudaError_t e;
@@ -1248,8 +1251,8 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
 
 // MBGB_PREC_AUTO, deep-zoom rule: FP64 for the whole frame when the pixel footprint at the
 // nearest surface, d * resolution * persp / quality with d the FP64 distance estimate at
-// the ray origin, is below 1e-5 of the scene scale (max(1, |origin|)). One probe launch
-// covers every frame of the call.
+// the ray origin, is below 1e-5 of the scene scale (max(1, |origin|)), and for scenes with
+// the limit box. One probe launch covers every frame of the call.
 static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int n, const mbgb_opts &o,
                                   cudaStream_t s, std::vector<int> &prec) {
   std::vector<double> pts(3 * (size_t)n), det((size_t)n, 1e-300);
@@ -1284,6 +1287,9 @@ static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int
                                  ? scenes[i].quality
                                  : d[i] * scenes[i].resolution * scenes[i].persp / scenes[i].quality;
     prec[i] = footprint < 1e-5 * scale ? 0 : 1;
+    // a limit box that cuts the fractal exposes its interior, where the colouring orbit
+    // (N x 10 iterations) and the AO samples' escape test never settle and FP32 flips them
+    if (scenes[i].limits_enabled) prec[i] = 0;
   }
   return MBGB_OK;
 }

@@ -49,8 +49,8 @@ struct FractalT {
   int juliaMode, tgladFoldingMode, sphericalFoldingMode;
   int limits, iterThresh, interiorMode;
   int distPost;     // limits || iterThresh || interiorMode: CalculateDistance post-processes the orbit's result
-  int lean;         // the lean FP32 orbit applies (Mandelbox without rotations, offsets, pre-folds, julia or
-                    // limits; power-8 Mandelbulb without pre-folds or limits): CalculateDistance takes it in FP32
+  int lean;         // the lean FP32 orbit applies (Mandelbox without rotations, offsets, pre-folds or julia;
+                    // power-8 Mandelbulb without pre-folds): CalculateDistance takes it in FP32
   int mbRotEnabled, mbMainRotZero;
   int mbRotZero[2][3];
   T power, constantFactor;

@@ -331,6 +331,25 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
   return (L < N ? sqrtf(minr2) : sqrtf(r2)) * 5000.0f;
 }
 
+// CalculateDistance's limit box (src/fractal.cpp:1252-1262): the distance to the box, and true
+// when the point lies farther from it than detailSize (the estimate is then that distance,
+// with no orbit and itersOut left as it was).
+template <typename T>
+__device__ __forceinline__ bool limit_box(const FractalT<T> &f, const V3<T> point, const T detailSize,
+                                          T &limitBoxDist) {
+  if (!f.limits) return false;
+  // MAX(a, b) = a > b ? a : b (gtk MAX macro)
+  const T ax = point.x - f.amax, bx = -(point.x - f.amin);
+  const T ay = point.y - f.bmax, by = -(point.y - f.bmin);
+  const T az = point.z - f.cmax, bz = -(point.z - f.cmin);
+  const T da = ax > bx ? ax : bx;
+  const T db = ay > by ? ay : by;
+  const T dc = az > bz ? az : bz;
+  // dMax (src/common_math.cpp:34-43)
+  limitBoxDist = (da > db) ? ((da > dc) ? da : dc) : ((db > dc) ? db : dc);
+  return limitBoxDist > detailSize;
+}
+
 // CalculateDistance after the orbit (src/fractal.cpp:1291-1300, 1436-1445): the clamp at 0,
 // minN, interior mode, the iteration threshold and the limit box, on the orbit's distance
 // and end iteration Li. Shared by the generic and the lean orbits.
@@ -366,20 +385,9 @@ __device__ __forceinline__ T calc_distance(const FractalT<T> &f, const V3<T> poi
     return calc_distance_runtime<T>(&f, point, detailSize, N, minN, normalMode, &L, &maxIter, &cnt.orbit, &cnt.calls,
                                     &cnt.objectOut, fparam);
   T limitBoxDist = T(0);
-  if (f.limits) {
-    // MAX(a, b) = a > b ? a : b (gtk MAX macro)
-    const T ax = point.x - f.amax, bx = -(point.x - f.amin);
-    const T ay = point.y - f.bmax, by = -(point.y - f.bmin);
-    const T az = point.z - f.cmax, bz = -(point.z - f.cmin);
-    const T da = ax > bx ? ax : bx;
-    const T db = ay > by ? ay : by;
-    const T dc = az > bz ? az : bz;
-    // dMax (src/common_math.cpp:34-43)
-    limitBoxDist = (da > db) ? ((da > dc) ? da : dc) : ((db > dc) ? db : dc);
-    if (limitBoxDist > detailSize) {
-      maxIter = false;
-      return limitBoxDist;
-    }
+  if (limit_box(f, point, detailSize, limitBoxDist)) {
+    maxIter = false;
+    return limitBoxDist;
   }
   int Li;
   T distance;
@@ -413,7 +421,8 @@ __device__ __forceinline__ T distance_est(const FractalT<T> &f, const V3<T> p, c
     if constexpr (FORMULA == 8) distance = mandelbox_fast(f, p.x, p.y, p.z, N, Li, cnt, fparam);
     else distance = mandelbulb8_fast<0>(f, p.x, p.y, p.z, N, Li, cnt);
     L = Li;
-    // the lean scenes have no limits box (FractalT::lean), so its distance is 0 here
+    // the LEAN instantiations are launched for scenes without the limit box (its distance is 0
+    // here); limit-box scenes take calc_distance, which runs the lean orbit after the box test
     return distance_post(f, distance, Li, N, minN, detail, normalMode, T(0), maxIter);
   } else {
     return calc_distance<T, FORMULA>(f, p, detail, N, minN, normalMode, L, maxIter, cnt, fparam);

@@ -1775,7 +1775,8 @@ void oracle_colour_value(const mbgb_scene *s, const double *pts, long n, double 
 // Rows [row0, row1), or the `nlist` rows of `list` when it is not NULL, claimed one at a
 // time by `threads` workers (the reference's dynamic row claiming, src/Render3D.cpp:815-849).
 static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int threads, const mbgb_image *img,
-                       unsigned long long *counters, bool exact, const int *list = nullptr, int nlist = 0) {
+                       unsigned long long *counters, bool exact, const int *list = nullptr, int nlist = 0,
+                       unsigned long long *pixel_work = nullptr) {
   if (!s || !img) return 1;
   if (list) {
     if (nlist < 0) return 1;
@@ -1799,7 +1800,16 @@ static int render_rows(const mbgb_scene *s, int row0, int row1, int jitter, int 
       const int k = next.fetch_add(1);
       if (k >= row1) break;
       const int y = list ? list[k] : k;
-      for (int x = 0; x < img->width; x++) render_pixel(f, x, y, bufs, jitter != 0, img, cnts[t]);
+      for (int x = 0; x < img->width; x++) {
+        const Cnt before = cnts[t];
+        render_pixel(f, x, y, bufs, jitter != 0, img, cnts[t]);
+        if (pixel_work) {   // this pixel's orbit iterations, DE calls and march steps
+          unsigned long long *w = pixel_work + 3 * ((size_t)y * img->width + x);
+          w[0] = cnts[t].orbit - before.orbit;
+          w[1] = cnts[t].calls - before.calls;
+          w[2] = cnts[t].steps - before.steps;
+        }
+      }
     }
   };
   if (threads == 1) {
@@ -2000,6 +2010,14 @@ int oracle_render_row_list(const mbgb_scene *s, const int *rows, int nrows, int 
                            const mbgb_image *img, unsigned long long *counters) {
   if (!rows) return 1;
   return render_rows(s, 0, 0, jitter, threads, img, counters, false, rows, nrows);
+}
+
+// The render of rows [row0, row1) with each pixel's work recorded: pixel_work[3 (y w + x) + k]
+// = its orbit iterations, DE calls and march steps (all rays of the pixel, in order).
+int oracle_render_pixel_work(const mbgb_scene *s, int row0, int row1, int threads, const mbgb_image *img,
+                             unsigned long long *pixel_work) {
+  if (!pixel_work) return 1;
+  return render_rows(s, row0, row1, 0, threads, img, nullptr, false, nullptr, 0, pixel_work);
 }
 
 // The same render with every hit moved onto the level set DE(P) = thr after the

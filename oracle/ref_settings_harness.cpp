@@ -293,6 +293,7 @@ int ref_scene_from_settings(const char *defaults_path, const char *path, const c
   noGUIdata.overrideStrings.clear();
   if (ok) finish(p, out);
   delete p;
+  fflush(stdout);   // the reader's messages leave with the call that printed them
   return ok ? 0 : 1;
 }
 
@@ -305,6 +306,7 @@ int ref_scene_from_keys(const char *const *keys, const char *const *values, int 
   LoadSettingsPost(*p);
   finish(p, out);
   delete p;
+  fflush(stdout);
   return 0;
 }
 

@@ -31,6 +31,8 @@ def load(fast: bool = False) -> ctypes.CDLL:
     lib.oracle_compile16.restype = None
     lib.oracle_ssao.restype = None
     lib.oracle_render_exact.restype = ctypes.c_int
+    lib.oracle_render_pixel_work.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
+    lib.oracle_render_pixel_work.restype = ctypes.c_int
     _cache[key] = lib
     return lib
 
@@ -176,3 +178,18 @@ def render_exact(lib, scene, threads=None):
     if rc != 0:
         raise RuntimeError("oracle_render_exact rejected its arguments")
     return img
+
+
+def pixel_work(lib, scene, threads=None):
+    """Renders the scene on the CPU and returns (CImage, work) where work[y, x] = (orbit
+    iterations, DE calls, march steps) of that pixel's rays."""
+    import mandelbulber_gb300 as mb
+    w, h = scene.image_width, scene.image_height
+    img = mb.CImage.empty(w, h)
+    work = np.zeros((h, w, 3), np.uint64)
+    c = img.as_c()
+    rc = lib.oracle_render_pixel_work(ctypes.addressof(scene), 0, h, threads or os.cpu_count() or 1,
+                                      ctypes.addressof(c), _p(work))
+    if rc != 0:
+        raise RuntimeError("oracle_render_pixel_work rejected its arguments")
+    return img, work

@@ -376,3 +376,36 @@ def test_mandelbulb_escape_radius_10_against_oracle(gpu_ctx, oracle, precision):
         assert m["hit_mismatch"] <= 0.001 and m["psnr_float"] >= 45.0, m
     default = gpu_ctx.render(W.workload("mandelbulb_640x480", 320, 240), precision=precision)
     assert not np.array_equal(default.depth, img.depth)
+
+
+@pytest.mark.parametrize("engine", ENGINES, ids=["wavefront", "per_pixel"])
+def test_mandelbox_limit_box_on_the_lean_orbit(gpu_ctx, oracle, engine):
+    """The limit box (src/fractal.cpp:1252-1262) on the Mandelbox that the lean FP32 orbit
+    renders: the box test runs before the orbit and its distance bounds the result after it,
+    in every stage (march, polish, shadow and AO rays, normals).
+      * FP64: bit-exact to the oracle on the exact layers.
+      * FP32 + FP64-fix: hit mismatch <= 0.1 %, depth within 1e-5 (p99), iterations agree on
+        >= 99.9 % of hits, and >= 45 dB on the pixels the box does not cut (same hit and depth
+        as without the box). The cut faces expose the fractal's interior, where the colouring
+        orbit (N x 10 iterations) and the AO samples' escape test never settle: FP32 flips
+        their palette index and occlusion there (about 25 dB over the whole frame, the same
+        with the generic FP32 orbit), so AUTO renders limit-box scenes in FP64.
+    """
+    box = dict(limits_enabled=1, x_max=1.5, y_min=-2.5, z_max=2.0)
+    sc = W.workload("mandelbox_1080p", 320, 180, **box)
+    ref, _ = oracle_lib.render(oracle, sc)
+    b = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=engine)
+    for k in ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]:
+        np.testing.assert_array_equal(getattr(b, k), getattr(ref, k), err_msg=k)
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, engine=engine)
+    m = metrics.compare(a, ref)
+    plain, _ = oracle_lib.render(oracle, W.workload("mandelbox_1080p", 320, 180))
+    uncut = (ref.hit == plain.hit) & (np.abs(ref.depth - plain.depth) <= 1e-9 * np.abs(plain.depth))
+    m["psnr_uncut"] = metrics.psnr(a.image_float[uncut], ref.image_float[uncut])
+    m["cut_fraction"] = float(1.0 - uncut.mean())
+    print("limit box", engine, m)
+    assert m["hit_mismatch"] <= 0.001 and m["depth_rel_p99"] <= 1e-5 and m["iters_agree"] >= 0.999, m
+    assert m["psnr_uncut"] >= 45.0 and 0.1 < m["cut_fraction"] < 0.9, m
+    auto = gpu_ctx.render(sc, precision=mb.PREC_AUTO, engine=engine)
+    for k in ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]:
+        np.testing.assert_array_equal(getattr(auto, k), getattr(ref, k), err_msg=k)
