@@ -210,11 +210,13 @@ typedef struct mbgb_image {
 enum {
   MBGB_PREC_FP64 = 0,          /* every DE evaluation and every march in double */
   MBGB_PREC_FP32_FIX = 1,      /* FP32 march/orbit with FP64 camera origin and FP64 hit refinement */
-  MBGB_PREC_AUTO = 2           /* FP32_FIX unless the pixel footprint at the nearest surface (FP64 distance
-                                * estimate at the ray origin x resolution x persp / quality) is below 1e-5 of
-                                * the scene scale, or the scene has the limit box (limits_enabled: its cut
-                                * faces expose the fractal's interior, whose colouring orbits FP32 does not
-                                * reproduce), then FP64 for the whole frame; the probe synchronises */
+  MBGB_PREC_AUTO = 2           /* FP32_FIX unless the hit bisection's window at the nearest surface
+                                * (0.01 x quality x the threshold there: FP64 distance estimate at the ray
+                                * origin x resolution x persp / quality, or the constant threshold) is below
+                                * 1e-7 of the scene scale (about one FP32 ulp), or the scene has the limit box
+                                * (limits_enabled: its cut faces expose the fractal's interior, whose colouring
+                                * orbits FP32 does not reproduce), then FP64 for the whole frame; the probe
+                                * synchronises */
 };
 
 typedef struct mbgb_opts {

@@ -232,12 +232,14 @@ static bool need_volumetric(const mbgb_scene &s) {
 }
 
 // Features that the per-pixel engine renders and the wavefront stages do not carry (aux,
-// fake and volumetric lights, iteration fog, ray-traced reflections): scenes that use them
-// render on the per-pixel engine. Slow shading, environment mapping and primitive objects
-// are composition-stage work the wavefront carries.
+// fake and volumetric lights, iteration fog): scenes that use them render on the per-pixel
+// engine. Slow shading, environment mapping and primitive objects are composition-stage work
+// the wavefront carries; ray-traced reflections are further primary passes, one per depth,
+// except with slow shading (whose warp-wide normals serve the camera rays only) or the limit
+// box (whose early return leaves itersOut to the next ray, src/fractal.cpp:1252-1262).
 static bool per_pixel_only(const mbgb_scene &s) {
   return uses_aux_lights(s) || s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled ||
-         reflection_rays(s) > 1;
+         (reflection_rays(s) > 1 && (s.slowShading || s.limits_enabled));
 }
 
 // The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights and the
@@ -940,6 +942,7 @@ static mbgb_status level_set_supported(const mbgb_scene &s) {
   if (s.limits_enabled || s.iterThresh || s.interiorMode)
     return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: limits, iteration threshold or interior mode");
   if (uses_primitives(s)) return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: primitive objects");
+  if (reflection_rays(s) > 1) return set_error(MBGB_ERR_UNSUPPORTED, "exact hits / gradients: reflections");
   return MBGB_OK;
 }
 
@@ -951,6 +954,7 @@ static mbgb_status grad_supported(const mbgb_scene &s) {
     return set_error(MBGB_ERR_UNSUPPORTED, "gradients: soft or penetrating shadows");
   // the gradient differentiates the four-sample normal of the fractal
   if (s.slowShading) return set_error(MBGB_ERR_UNSUPPORTED, "gradients: slow shading");
+  if (reflection_rays(s) > 1) return set_error(MBGB_ERR_UNSUPPORTED, "gradients: reflections");
   return MBGB_OK;
 }
 
@@ -1023,11 +1027,15 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
 struct WaveLayout {
   size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
   size_t prec, pprev;
+  size_t rstart, rdir, rthr, rlist;
   uint32_t poolCap;
   size_t total;
 };
 
-static WaveLayout wave_layout(int64_t npix, size_t ts, int aoN, bool needVol) {
+// `npixFrame` pixels with `rays` rays each (the reflection loop's depths): every per-ray array
+// holds rays x npixFrame entries.
+static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVol, int rays) {
+  const int64_t npix = npixFrame * rays;
   WaveLayout w{};
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -1052,9 +1060,19 @@ static WaveLayout wave_layout(int64_t npix, size_t ts, int aoN, bool needVol) {
   w.pol = take(npix * 4);
   w.ovl = take(npix * 4);
   w.last = take(npix * 4);
-  w.poolCap = needVol ? (uint32_t)std::min<int64_t>(npix * kPoolChunksPerPixel, 0x7fffffff) : 1u;
+  // rays beyond the pool take the overflow pass (exact, but one ray per thread of a narrow
+  // pass); with reflections every depth's rays share it
+  const int64_t chunksPerPixel = rays > 1 ? (int64_t)kPoolChunksPerReflectedRay * rays : kPoolChunksPerPixel;
+  int64_t chunks = npixFrame * chunksPerPixel;
+  if (rays > 1) chunks = std::min<int64_t>(chunks, (int64_t)(8e9 / (kChunk * 4 * ts)));   // 8 GB at most
+  w.poolCap = needVol ? (uint32_t)std::min<int64_t>(chunks, 0x7fffffff) : 1u;
   w.prec = take((size_t)w.poolCap * kChunk * 4 * ts);
   w.pprev = take((size_t)w.poolCap * 4);
+  const size_t refl = rays > 1 ? (size_t)npix : 0;
+  w.rstart = take(3 * refl * sizeof(double));
+  w.rdir = take(3 * refl * sizeof(double));
+  w.rthr = take(refl * sizeof(double));
+  w.rlist = take((rays > 1 ? (size_t)npixFrame : 0) * 4);
   w.total = off;
   return w;
 }
@@ -1076,7 +1094,8 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   const bool needVol = need_volumetric(scene);
   const bool rayAO = scene.global_ilumination && !scene.fastGlobalIllumination;
   const int aoN = rayAO ? c->ao_count : 0;
-  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol);
+  const int rays = reflection_rays(scene);
+  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays);
   char *base = (char *)c->wave[prec].ptr;
   WaveLaunch<T> L;
   WaveBufs<T> &wb = L.wb;
@@ -1105,7 +1124,14 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.refill_min = g.cfg.refill;
   wb.orbit_refill = g.cfg.orbitRefill;
   wb.exact_hit = o.exact_hit ? 1 : 0;
-  wb.npix = g.npix;
+  wb.npix = g.npix * rays;
+  wb.npix_frame = g.npix;
+  wb.rays = rays;
+  wb.depth = 0;
+  wb.ray_start = (double *)(base + w.rstart);
+  wb.ray_dir = (double *)(base + w.rdir);
+  wb.ray_thr0 = (double *)(base + w.rthr);
+  wb.ray_list = (uint32_t *)(base + w.rlist);
   // shadow/AO rays two per thread (secondary_pair_kernel): the lean FP32 Mandelbox with
   // per-estimate refill, which the pair kernel's packed orbit serves
   wb.pair_rays = (sizeof(T) == 4 && fast_mandelbox(scene) && g.cfg.pairRays && g.cfg.orbitRefill <= 0) ? 1 : 0;
@@ -1122,7 +1148,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.grid = c->sms * occ1;
   L.grid2 = c->sms * occ2;
   L.block = block;
-  L.ov_grid = std::max(1, kOverflowThreads / block);
+  L.ov_grid = std::max(1, kWaveOverflowThreads / block);
   L.polish_grid = c->sms * 8;
   L.compose_grid = (int)std::max<int64_t>(1, std::min<int64_t>((g.npix + block - 1) / block, (int64_t)c->sms * 32));
   L.cams = (const FrameCam<T> *)((char *)c->cams.ptr + g.cams_off);
@@ -1136,7 +1162,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.ov = io;
   L.ov.overflow_pass = 1;
   L.ov.step_cap = kStepSlots;
-  L.ov.slots = kOverflowThreads;
+  L.ov.slots = kWaveOverflowThreads;
   L.ov.step_step = c->ovstep[prec][0].ptr;
   L.ov.step_dist = c->ovstep[prec][1].ptr;
   L.ov.step_thr = c->ovstep[prec][2].ptr;
@@ -1151,7 +1177,10 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   if constexpr (sizeof(T) == 8) e = launch_wave_f64(L, s);
   else e = launch_wave_f32(L, s);
   if (e != cudaSuccess) return cuda_error(e, "wavefront launch");
-  *launches += 3 + (needVol ? 1 : 0) + (prec == 1 ? 1 : 0) + (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
+  // per ray depth: primary (+ overflow) pass and polish; per further depth the reflect and
+  // counter kernels
+  *launches += 2 + (int64_t)rays * (1 + (needVol ? 1 : 0) + (prec == 1 ? 1 : 0)) + 2 * (int64_t)(rays - 1) +
+               (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
   return MBGB_OK;
 }
 
@@ -1249,10 +1278,13 @@ static mbgb_status enqueue_per_pixel(mbgb_context *c, const mbgb_scene &scene, c
   return MBGB_OK;
 }
 
-// MBGB_PREC_AUTO, deep-zoom rule: FP64 for the whole frame when the pixel footprint at the
-// nearest surface, d * resolution * persp / quality with d the FP64 distance estimate at
-// the ray origin, is below 1e-5 of the scene scale (max(1, |origin|)), and for scenes with
-// the limit box. One probe launch covers every frame of the call.
+// MBGB_PREC_AUTO, deep-zoom rule: FP64 for the whole frame when the hit bisection's window at
+// the nearest surface, 0.01 x quality x the threshold there (src/Render3D.cpp:145-183; the
+// threshold is d * resolution * persp / quality with d the FP64 distance estimate at the ray
+// origin, or the constant threshold `quality`), is below 1e-7 of the scene scale
+// (max(1, |origin|)): about one FP32 ulp. For quality 1 that is a pixel footprint below 1e-5
+// of the scale. Scenes with the limit box render in FP64 too. One probe launch covers every
+// frame of the call.
 static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int n, const mbgb_opts &o,
                                   cudaStream_t s, std::vector<int> &prec) {
   std::vector<double> pts(3 * (size_t)n), det((size_t)n, 1e-300);
@@ -1283,10 +1315,11 @@ static mbgb_status auto_precision(mbgb_context *c, const mbgb_scene *scenes, int
   for (int i = 0; i < n; i++) {
     const double *st = &pts[3 * i];
     const double scale = std::max(1.0, sqrt(st[0] * st[0] + st[1] * st[1] + st[2] * st[2]));
-    const double footprint = scenes[i].constantDEThreshold
-                                 ? scenes[i].quality
-                                 : d[i] * scenes[i].resolution * scenes[i].persp / scenes[i].quality;
-    prec[i] = footprint < 1e-5 * scale ? 0 : 1;
+    const double thr = scenes[i].constantDEThreshold
+                           ? scenes[i].quality
+                           : d[i] * scenes[i].resolution * scenes[i].persp / scenes[i].quality;
+    const double window = 0.01 * scenes[i].quality * thr;
+    prec[i] = window < 1e-7 * scale ? 0 : 1;
     // a limit box that cuts the fractal exposes its interior, where the colouring orbit
     // (N x 10 iterations) and the AO samples' escape test never settle and FP32 flips them
     if (scenes[i].limits_enabled) prec[i] = 0;
@@ -1549,7 +1582,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     const int64_t fjobs = (int64_t)((sc.image_width + cfg.tileW - 1) / cfg.tileW) *
                           ((r1 - r0 + cfg.tileH - 1) / cfg.tileH) * 32;
     const bool rayAO = sc.global_ilumination && !sc.fastGlobalIllumination;
-    const double perPix = 1.0 + (rayAO ? c->ao_count : 0);
+    const double perPix = (1.0 + (rayAO ? c->ao_count : 0)) * reflection_rays(sc);
     const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && !per_pixel_only(sc) &&
                       (double)std::max(fpix, fjobs) * perPix < kMaxGroupJobs;
     if (!wave && (grad || o.exact_hit))
@@ -1598,10 +1631,13 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     if (!g.wave)
       ovRecords[g.prec] =
           std::max(ovRecords[g.prec], (int64_t)overflow_slots(rep, g.prec) * reflection_rays(rep));
+    else if (needVol)
+      ovRecords[g.prec] = std::max<int64_t>(ovRecords[g.prec], kWaveOverflowThreads);
     if (g.wave) {
       const bool rayAO = rep.global_ilumination && !rep.fastGlobalIllumination;
       const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
-      wave_bytes[g.prec] = std::max(wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol).total);
+      wave_bytes[g.prec] = std::max(
+          wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol, reflection_rays(rep)).total);
       g.cams_off = camsBytes;
       const size_t cs = g.prec == 0 ? sizeof(FrameCam<double>) : sizeof(FrameCam<float>);
       camsBytes += (cs * g.frames.size() + 255) & ~(size_t)255;

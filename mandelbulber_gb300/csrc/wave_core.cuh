@@ -320,6 +320,12 @@ __device__ __forceinline__ int frame_of_pixel(const FrameCam<T> *__restrict__ ca
   return lo;
 }
 
+// Pixel of the batch a ray belongs to (rays of reflection depth d sit at d * npix_frame + pixel).
+template <typename T>
+__device__ __forceinline__ int64_t pixel_of_ray(const WaveBufs<T> &wb, const int64_t ri) {
+  return ri < wb.npix_frame ? ri : ri % wb.npix_frame;
+}
+
 // Job index within a frame -> pixel: tiles of tileW x tileH (32 pixels) in row-major
 // tile order, so a warp's first 32 jobs cover one tile.
 __device__ __forceinline__ void job_pixel(const int width, const int row_begin, const int tileW, const int tileH,
@@ -469,7 +475,9 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 // ---------------------------------------------------------------------------
 // Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
-template <typename T, int FORMULA, bool FAST>
+// REFL: the batch has reflected rays (WaveBufs::rays > 1); without, the kernel holds no
+// reflected-ray state.
+template <typename T, int FORMULA, bool FAST, bool REFL = false>
 __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
@@ -480,8 +488,11 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
   const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
   const T search_limit = T(1) - T(0.01) * p.quality;
   const int stepCap = io.overflow_pass ? kStepSlots : io.step_cap;
-  // jobs: every frame's tiles (partial tiles included), or the overflow list
+  // jobs: every frame's tiles (partial tiles included), the reflected rays of this depth, or
+  // the overflow list
+  const int depth = REFL ? wb.depth : 0;
   const unsigned int nJobs = io.overflow_pass ? *(volatile unsigned int *)&wb.ctl[3]
+                             : depth > 0      ? *(volatile unsigned int *)&wb.ctl[10]
                                               : cams[ncams - 1].jobBase + cams[ncams - 1].jobCount;
   Counters cnt{0, 0, 0, 0};
   unsigned int *jobCounter = io.overflow_pass ? (wb.ctl + 4) : (wb.ctl + 0);
@@ -489,10 +500,12 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
   // per-lane ray state
   bool active = false, exhausted = false;
   int64_t gp = 0;   // pixel of the batch
+  int64_t ri = 0;   // ray: depth * npix_frame + gp
   int phase = 0, i = 0, buffCount = 0, iters = 0, bis = 0;
   int chunk = -1;   // current pool chunk of the ray's step records (main pass)
   V3<T> dir{T(0), T(0), T(0)}, start{T(0), T(0), T(0)};
   T res = T(0), persp = T(0), thrScale = T(0), fpar = T(0);
+  T thrInit = T(0);   // a reflected ray's thresholds add the previous ray's (0 for camera rays)
   T scan = T(0), step = T(0), thr = T(0), dist = T(0), detail = T(0);  // detail: detailSize of the march
   int guardSteps = 0;
   for (;;) {
@@ -510,8 +523,10 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           exhausted = true;
         } else {
           int x, y, fr;
-          if (io.overflow_pass) {
-            gp = (int64_t)wb.overflow_list[job];
+          if (io.overflow_pass || depth > 0) {
+            ri = io.overflow_pass ? (int64_t)wb.overflow_list[job]
+                                  : (int64_t)depth * wb.npix_frame + (int64_t)wb.ray_list[job];
+            gp = REFL ? pixel_of_ray(wb, ri) : ri;
             fr = frame_of_pixel(cams, ncams, gp);
             const int64_t local = gp - cams[fr].pixBase;
             x = (int)(local % cams[fr].width);
@@ -521,11 +536,22 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             const FrameCam<T> &c = cams[fr];
             job_pixel(c.width, c.row_begin, c.tileW, c.tileH, job - c.jobBase, x, y);
             gp = c.pixBase + (int64_t)y * c.width + x;
+            ri = gp;
           }
           const FrameCam<T> &c = cams[fr];
           if (x < c.width && y < c.row_end) {
-            const bool marched = camera_dir(p, c, x, y, dir);
-            start = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
+            bool marched = true;
+            if (!REFL || ri < wb.npix_frame) {
+              marched = camera_dir(p, c, x, y, dir);
+              start = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
+              thrInit = T(0);
+            } else {
+              // a reflected ray (src/Render3D.cpp:441-462): marched in T from its FP64 origin
+              // and direction, its thresholds offset by the previous ray's
+              start = {(T)wb.ray_start[ri], (T)wb.ray_start[wb.npix + ri], (T)wb.ray_start[2 * wb.npix + ri]};
+              dir = {(T)wb.ray_dir[ri], (T)wb.ray_dir[wb.npix + ri], (T)wb.ray_dir[2 * wb.npix + ri]};
+              thrInit = (T)wb.ray_thr0[ri];
+            }
             res = c.resolution;
             persp = c.persp;
             fpar = c.fparam;
@@ -543,11 +569,11 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             active = true;
             if (!marched) {
               // fisheye cut: no march, background with an empty step buffer
-              wb.flags[gp] = 2;
-              wb.scan[gp] = T(0);
-              wb.count[gp] = 0;
-              wb.iters[gp] = 0;
-              wb.last_chunk[gp] = -1;
+              wb.flags[ri] = 2;
+              wb.scan[ri] = T(0);
+              wb.count[ri] = 0;
+              wb.iters[ri] = 0;
+              wb.last_chunk[ri] = -1;
               active = false;
             }
           }
@@ -563,8 +589,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
       const V3<T> point = start + dir * scan;
       if (phase == 0) {
         if (p.constantDEThreshold) thr = p.quality;
-        else if (f64) thr = scan * res * persp / p.quality;
-        else thr = scan * thrScale;
+        else if (f64) thr = REFL ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
+        else thr = REFL ? scan * thrScale + thrInit : scan * thrScale;
         if (p.perspType == 1 || p.perspType == 2) thr *= T(kPI);
         detail = thr;
       }
@@ -593,7 +619,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             if (full) {
               // the pool is spent: re-marched by the overflow pass with slot records
               const unsigned int k = atomicAdd(wb.ctl + 3, 1u);
-              wb.overflow_list[k] = (unsigned int)gp;
+              wb.overflow_list[k] = (unsigned int)ri;
               active = false;
               continue;
             }
@@ -624,8 +650,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           if (dist > thr) scan += step;
           else if (dist < thr * search_limit) scan -= step;
           if (p.constantDEThreshold) thr = p.quality;
-          else if (f64) thr = scan * res * persp / p.quality;
-          else thr = scan * thrScale;
+          else if (f64) thr = REFL ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
+          else thr = REFL ? scan * thrScale + thrInit : scan * thrScale;
           bis = 1;
         }
       } else {
@@ -637,8 +663,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           if (dist > thr) scan += step;
           else if (dist < thr * search_limit) scan -= step;
           if (p.constantDEThreshold) thr = p.quality;
-          else if (f64) thr = scan * res * persp / p.quality;
-          else thr = scan * thrScale;
+          else if (f64) thr = REFL ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
+          else thr = REFL ? scan * thrScale + thrInit : scan * thrScale;
           bis++;
         }
       }
@@ -651,26 +677,26 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           // rare long rays: fold the records now (the slot is reused); compose applies the map
           T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
           volumetric_affine<T>(p, sb, buffCount, scan, found ? T(1) : T(0), vol);
-          for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + gp] = vol[c];
+          for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + ri] = vol[c];
           flags |= 4;
         }
-        wb.flags[gp] = flags;
-        wb.last_chunk[gp] = chunk;
-        wb.scan[gp] = scan;
-        wb.dist[gp] = dist;
-        wb.thr[gp] = thr;
-        wb.step[gp] = step;
-        wb.detail[gp] = detail;
-        wb.bis_left[gp] = 20 - bis;
-        wb.count[gp] = buffCount;
-        wb.iters[gp] = iters;
+        wb.flags[ri] = flags;
+        wb.last_chunk[ri] = chunk;
+        wb.scan[ri] = scan;
+        wb.dist[ri] = dist;
+        wb.thr[ri] = thr;
+        wb.step[ri] = step;
+        wb.detail[ri] = detail;
+        wb.bis_left[ri] = 20 - bis;
+        wb.count[ri] = buffCount;
+        wb.iters[ri] = iters;
         const V3<T> hp = start + dir * scan;
-        wb.point[0 * wb.npix + gp] = hp.x;
-        wb.point[1 * wb.npix + gp] = hp.y;
-        wb.point[2 * wb.npix + gp] = hp.z;
+        wb.point[0 * wb.npix + ri] = hp.x;
+        wb.point[1 * wb.npix + ri] = hp.y;
+        wb.point[2 * wb.npix + ri] = hp.z;
         if (found) {
           const unsigned int k = atomicAdd(wb.ctl + 1, 1u);
-          wb.hit_list[k] = (unsigned int)gp;
+          wb.hit_list[k] = (unsigned int)ri;
           // FP32 policy: the FP64 polish re-checks every hit whose FP32 bisection stopped
           // early but not clearly inside the window (dist/thr within 1e-4 of an edge). A
           // bisection that used all 20 steps has none left to continue, so FP64 would keep
@@ -681,7 +707,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             const bool clear = (q > search_limit + T(1e-4)) && (q < T(1) - T(1e-4));
             if (wb.polish_all || wb.exact_hit || (!clear && bis < 20)) {
               const unsigned int m = atomicAdd(wb.ctl + 6, 1u);
-              wb.polish_list[m] = (unsigned int)gp;
+              wb.polish_list[m] = (unsigned int)ri;
             }
           }
         }
@@ -728,19 +754,27 @@ __global__ void __launch_bounds__(128) polish_kernel(const __grid_constant__ Par
   for (unsigned int w = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; w * lanes < nh; w += warps) {
     const unsigned int k = w * lanes + lane;
     if (k >= nh) break;
-    const int64_t gp = (int64_t)wb.polish_list[k];
-    const FrameCam<float> &c = cams[frame_of_pixel(cams, ncams, gp)];
-    const int64_t local = gp - c.pixBase;
+    const int64_t gp = (int64_t)wb.polish_list[k];   // the ray (pixel + depth x npix_frame)
+    const int64_t px = pixel_of_ray(wb, gp);
+    const FrameCam<float> &c = cams[frame_of_pixel(cams, ncams, px)];
+    const int64_t local = px - c.pixBase;
     const int x = (int)(local % c.width), y = (int)(local / c.width);
-    V3<double> dir;
-    camera_ray(p, c, x, y, dir);
-    const V3<double> start{c.start[0], c.start[1], c.start[2]};
+    V3<double> dir, start;
+    double thrInit = 0.0;
+    if (gp < wb.npix_frame) {
+      camera_ray(p, c, x, y, dir);
+      start = {c.start[0], c.start[1], c.start[2]};
+    } else {   // a reflected ray: its FP64 origin and direction, thresholds offset
+      start = {wb.ray_start[gp], wb.ray_start[wb.npix + gp], wb.ray_start[2 * wb.npix + gp]};
+      dir = {wb.ray_dir[gp], wb.ray_dir[wb.npix + gp], wb.ray_dir[2 * wb.npix + gp]};
+      thrInit = wb.ray_thr0[gp];
+    }
     double scan = (double)wb.scan[gp];
     double step = (double)wb.step[gp];
     const double detail = (double)wb.detail[gp];
     const int left = wb.bis_left[gp];
     auto thr_of = [&](double sc) {
-      return p.constantDEThreshold ? p.quality_d : sc * c.resolution_d * c.persp_d / p.quality_d;
+      return p.constantDEThreshold ? p.quality_d : sc * c.resolution_d * c.persp_d / p.quality_d + thrInit;
     };
     double thr = thr_of(scan);
     V3<double> point = start + dir * scan;
@@ -853,6 +887,76 @@ __device__ __forceinline__ HitInfo<T> hit_info(const ParamsT<T> &p, const FrameC
 }
 
 // ---------------------------------------------------------------------------
+// Stage 2c (ray-traced reflections, src/Render3D.cpp:441-499): every hit of the current depth
+// on a reflecting object spawns the mirrored ray of the next depth, started one threshold
+// above the hit. The normal is CalculateNormals at the hit (N x 5 iterations, minN 0) in the
+// march precision; direction and origin are formed in FP64, as the reflection loop does.
+// ---------------------------------------------------------------------------
+template <typename T, int FORMULA, bool FAST>
+__global__ void __launch_bounds__(128) reflect_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io,
+                                                      const WaveBufs<T> wb, const FrameCam<T> *__restrict__ cams,
+                                                      const int ncams) {
+  // this depth's hits: the hit list from the count before its primary pass to the count now
+  const unsigned int h0 = *(volatile unsigned int *)&wb.ctl[8];
+  const unsigned int h1 = *(volatile unsigned int *)&wb.ctl[1];
+  Counters cnt{0, 0, 0, 0};
+  for (unsigned int k = h0 + blockIdx.x * blockDim.x + threadIdx.x; k < h1; k += gridDim.x * blockDim.x) {
+    const int64_t ri = (int64_t)wb.hit_list[k];
+    const int objectType = (wb.flags[ri] >> 4) & 7;
+    // sReflect::reflect of the object the ray hit (src/Render3D.cpp:470-478)
+    const T reflect = objectType == kObjFractal ? p.reflect : p.primReflect[objectType - 1];
+    if (reflect == T(0)) continue;
+    const int64_t gp = pixel_of_ray(wb, ri);
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
+    const HitInfo<T> h = hit_info(p, c, wb, ri);
+    const V3<T> vn = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+    V3<double> view;
+    if (ri < wb.npix_frame) {
+      const int64_t local = gp - c.pixBase;
+      camera_ray(p, c, (int)(local % c.width), (int)(local / c.width), view);
+    } else {
+      view = {wb.ray_dir[ri], wb.ray_dir[wb.npix + ri], wb.ray_dir[2 * wb.npix + ri]};
+    }
+    const V3<double> vnd{(double)vn.x, (double)vn.y, (double)vn.z};
+    view = view - vnd * dot3(view, vnd) * 2.0;
+    const double distThresh = (double)h.thr;
+    const V3<double> point{(double)h.point.x, (double)h.point.y, (double)h.point.z};
+    const V3<double> startRay = point + view * distThresh;
+    const int64_t rn = ri + wb.npix_frame;
+    wb.ray_start[rn] = startRay.x;
+    wb.ray_start[wb.npix + rn] = startRay.y;
+    wb.ray_start[2 * wb.npix + rn] = startRay.z;
+    wb.ray_dir[rn] = view.x;
+    wb.ray_dir[wb.npix + rn] = view.y;
+    wb.ray_dir[2 * wb.npix + rn] = view.z;
+    wb.ray_thr0[rn] = distThresh;
+    const unsigned int m = atomicAdd(wb.ctl + 9, 1u);
+    wb.ray_list[m] = (unsigned int)gp;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+  }
+}
+
+// Between two reflection depths (one thread): the next depth's rays become the current ones,
+// the per-depth job, overflow and polish counters restart, the hit count so far is kept.
+template <typename T>
+__global__ void next_depth_kernel(uint32_t *ctl) {
+  ctl[8] = ctl[1];
+  ctl[10] = ctl[9];
+  ctl[9] = 0;
+  ctl[0] = 0;
+  ctl[3] = 0;
+  ctl[4] = 0;
+  ctl[6] = 0;
+}
+
+// ---------------------------------------------------------------------------
 // Stage 3: shadow rays and ray-traced AO directions of all hits, lane refill.
 // Jobs [0, nShadow): one shadow ray per hit; then aoCount x hits AO rays,
 // direction-major so a warp's initial 32 rays share a direction.
@@ -876,7 +980,7 @@ template <typename T>
 struct SecondaryRay {
   int kind;
   unsigned int j;   // AO direction
-  int64_t gp;       // pixel of the batch
+  int64_t gp;       // ray of the batch (pixel + reflection depth x npix_frame)
   V3<T> point, dir;
   T r, end, sh, thr, detail, maxSoft, stepMul, fpar;
   int guard;
@@ -898,7 +1002,7 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
     s.j = q / nh;
     s.gp = (int64_t)wb.hit_list[q % nh];
   }
-  const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, s.gp)];
+  const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, pixel_of_ray(wb, s.gp))];
   const HitInfo<T> h = hit_info(p, c, wb, s.gp);
   s.point = h.point;
   s.fpar = c.fparam;
@@ -1359,14 +1463,76 @@ __device__ __forceinline__ void slow_normal_warp(const ParamsT<T> &p, const Wave
 }
 
 // ---------------------------------------------------------------------------
+// ObjectShader (src/shaders.cpp:21-112) at the hit of ray `ri` from the stages' results: the
+// normal (or the slow shading's, when `slowSum` is given), main light with its shadow and
+// specular term, surface colour, AO and environment mapping. Writes the object and specular
+// terms as the reflection loop combines them (src/Render3D.cpp:541-552) and the colour.
+template <typename T, int FORMULA, bool FAST>
+__device__ __forceinline__ void shade_hit(const ParamsT<T> &p, const FrameCam<T> &c, const WaveBufs<T> &wb,
+                                          const int64_t ri, const uint8_t flags, const V3<T> viewT,
+                                          const V3<double> viewD, const V3<T> *slowSum, Counters &cnt, T obj[3],
+                                          T spec[3], V3<T> &colourOut) {
+  const V3<T> lv{c.lightVect[0], c.lightVect[1], c.lightVect[2]};
+  const HitInfo<T> h = hit_info(p, c, wb, ri);
+  // CalculateNormals (src/shaders.cpp:675-757): 4 DEs at N x 5, minN 0, or the slow
+  // shading's 11^3 samples
+  V3<T> nrm;
+  if (slowSum) {
+    nrm = *slowSum;
+    if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
+    else nrm = normalize3(nrm);
+  } else {
+    nrm = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+  }
+  const int objectType = (flags >> 4) & 7;
+  T shade = dot3(nrm, lv);
+  if (shade < T(0)) shade = T(0);
+  const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
+  const T shadow = p.shadow ? wb.shadow[ri] : T(1);
+  V3<T> half = normalize3(lv - viewT);
+  T shade2 = dot3(nrm, half);
+  if (shade2 < T(0)) shade2 = T(0);
+  shade2 = m_pow(shade2, T(30)) * T(1);
+  if (shade2 > T(15)) shade2 = T(15);
+  const T specT = shade2 * p.specular;
+  const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt, c.fparam, objectType);
+  colourOut = colour;
+  V3<T> ambient{T(0), T(0), T(0)};
+  if (p.ao) {
+    if (p.fastAO) {
+      // detailSize after MainShadow: the float threshold if its loop ran
+      const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
+      const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
+      const T detail = (p.shadow && shadowStart < factor) ? (T)(float)h.thr : h.thr;
+      const T a = wave_fast_ao<T, FORMULA, FAST>(p, h.point, nrm, h.thr, detail, cnt, c.fparam);
+      ambient = {a, a, a};
+    } else {
+      T acc = T(0);
+      for (int jj = 0; jj < p.aoCount; jj++) acc += wb.ao[(int64_t)jj * wb.npix + ri] * p.aoWeight[0];
+      const T div = T(p.aoCount) * T(256);
+      ambient = {acc / div, acc / div, acc / div};
+    }
+  }
+  const T a2x = ambient.x * p.globalIlum, a2y = ambient.y * p.globalIlum, a2z = ambient.z * p.globalIlum;
+  // environment mapping (ObjectShader, src/shaders.cpp:71-76) of the default white texture
+  const T env = (p.envMapping ? (T)env_mapping(V3<double>{(double)nrm.x, (double)nrm.y, (double)nrm.z}, viewD)
+                              : T(0)) * p.reflect;
+  obj[0] = env * ambient.x + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
+  obj[1] = env * ambient.y + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
+  obj[2] = env * ambient.z + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
+  // no auxiliary or fake lights on this engine: their specular terms are the reference's zeros
+  for (int k = 0; k < 3; k++) spec[k] = T(0) + p.mainLight[k] * specT * shadow;
+}
+
+// ---------------------------------------------------------------------------
 // Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589),
 // over every pixel of the batch.
 // ---------------------------------------------------------------------------
-template <typename T, int FORMULA, bool FAST>
+template <typename T, int FORMULA, bool FAST, bool REFL = false>
 __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compose_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   Counters cnt{0, 0, 0, 0};
-  const int64_t total = wb.npix;
+  const int64_t total = wb.npix_frame;
   const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   // a warp's 32 consecutive pixels of the float RGB and RGB8 layers, staged so that they
   // leave as 16-byte stores (cImage's interleaved layers, src/cimage.hpp:155-162)
@@ -1391,102 +1557,93 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
                                          &slowSum, &cnt);
     }
     if (valid) {
-    const uint8_t flags = wb.flags[gp];
-    const bool hit = (flags & 1) != 0;
-    V3<T> viewT;
-    camera_dir(p, c, x, y, viewT);
-    const V3<T> lv{c.lightVect[0], c.lightVect[1], c.lightVect[2]};
-    T base[3];
-    if (hit) {
-      const HitInfo<T> h = hit_info(p, c, wb, gp);
-      // CalculateNormals (src/shaders.cpp:675-757): 4 DEs at N x 5, minN 0, or the slow
-      // shading's 11^3 samples
-      V3<T> nrm;
-      if (p.slowShading) {
-        nrm = slowSum;
-        if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
-        else nrm = normalize3(nrm);
+    // the reflection loop (src/Render3D.cpp:441-499): ray d + 1 was marched when ray d hit an
+    // object that reflects; the last ray marched closes the loop
+    int rayEnd = 0;
+    for (int d = 0; d + 1 < (REFL ? wb.rays : 1); d++) {
+      const uint8_t f = wb.flags[(int64_t)d * wb.npix_frame + gp];
+      if (!(f & 1)) break;
+      const int ot = (f >> 4) & 7;
+      if ((ot == kObjFractal ? p.reflect : p.primReflect[ot - 1]) == T(0)) break;
+      rayEnd = d + 1;
+    }
+    T result[3] = {T(0), T(0), T(0)};
+    T alpha = T(0), opacity = T(0);
+    // far to near (src/Render3D.cpp:501-566): each ray's object or background, the farther
+    // rays' result weighed by its reflectance, then its VolumetricShader
+    for (int d = rayEnd; d >= 0; d--) {
+      const int64_t ri = (int64_t)d * wb.npix_frame + gp;
+      const uint8_t flags = wb.flags[ri];
+      const bool hit = (flags & 1) != 0;
+      V3<T> viewT;
+      V3<double> viewD;
+      if (d == 0) {
+        camera_dir(p, c, x, y, viewT);
+        viewD = {(double)viewT.x, (double)viewT.y, (double)viewT.z};
       } else {
-        nrm = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+        viewD = {wb.ray_dir[ri], wb.ray_dir[wb.npix + ri], wb.ray_dir[2 * wb.npix + ri]};
+        viewT = {(T)viewD.x, (T)viewD.y, (T)viewD.z};
       }
-      const int objectType = (flags >> 4) & 7;
-      T shade = dot3(nrm, lv);
-      if (shade < T(0)) shade = T(0);
-      const T shadeV = p.directLight * ((T(1) - p.shading) + p.shading * shade);
-      const T shadow = p.shadow ? wb.shadow[gp] : T(1);
-      V3<T> half = normalize3(lv - viewT);
-      T shade2 = dot3(nrm, half);
-      if (shade2 < T(0)) shade2 = T(0);
-      shade2 = m_pow(shade2, T(30)) * T(1);
-      if (shade2 > T(15)) shade2 = T(15);
-      const T spec = shade2 * p.specular;
-      const V3<T> colour = wave_colour<T, FORMULA, FAST>(p, h.point, cnt, c.fparam, objectType);
-      objColour = colour;
-      V3<T> ambient{T(0), T(0), T(0)};
-      if (p.ao) {
-        if (p.fastAO) {
-          // detailSize after MainShadow: the float threshold if its loop ran
-          const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
-          const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
-          const T detail = (p.shadow && shadowStart < factor) ? (T)(float)h.thr : h.thr;
-          const T a = wave_fast_ao<T, FORMULA, FAST>(p, h.point, nrm, h.thr, detail, cnt, c.fparam);
-          ambient = {a, a, a};
-        } else {
-          T acc = T(0);
-          for (int jj = 0; jj < p.aoCount; jj++) acc += wb.ao[(int64_t)jj * wb.npix + gp] * p.aoWeight[0];
-          const T div = T(p.aoCount) * T(256);
-          ambient = {acc / div, acc / div, acc / div};
+      T obj[3] = {T(0), T(0), T(0)}, spec[3] = {T(0), T(0), T(0)}, bg[3] = {T(0), T(0), T(0)};
+      T reflect = T(0);
+      if (hit) {
+        V3<T> colour;
+        shade_hit<T, FORMULA, FAST>(p, c, wb, ri, flags, viewT, viewD, (p.slowShading && d == 0) ? &slowSum : nullptr,
+                                    cnt, obj, spec, colour);
+        if (d == 0) objColour = colour;
+        const int ot = (flags >> 4) & 7;
+        reflect = ot == kObjFractal ? p.reflect : p.primReflect[ot - 1];
+      } else {
+        const V3<T> b = background(p, viewT);
+        bg[0] = b.x;
+        bg[1] = b.y;
+        bg[2] = b.z;
+      }
+      T base[3];
+      for (int k = 0; k < 3; k++) {
+        if (d != rayEnd) base[k] = result[k] * reflect + (T(1) - reflect) * (obj[k] + bg[k]) + spec[k];
+        else base[k] = obj[k] + bg[k] + spec[k];
+      }
+      T a, o;
+      if (flags & 4) {
+        // a long ray of the overflow pass: its volumetric pass was folded into an affine map
+        const T A = wb.vol[0 * wb.npix + ri];
+        result[0] = A * base[0] + wb.vol[1 * wb.npix + ri];
+        result[1] = A * base[1] + wb.vol[2 * wb.npix + ri];
+        result[2] = A * base[2] + wb.vol[3 * wb.npix + ri];
+        a = wb.vol[4 * wb.npix + ri];
+        o = wb.vol[5 * wb.npix + ri];
+      } else {
+        // VolumetricShader over the ray's pooled step records, far to near, on this base colour
+        T res[4] = {base[0], base[1], base[2], hit ? T(1) + T(0) : T(0)};
+        float totalOpacity = 0.0f;
+        bool set = false;
+        if (p.needVolumetric) {
+          const int count = wb.count[ri];
+          const PoolRecords<T> pr{wb.pool_rec, wb.pool_prev, wb.last_chunk[ri], hit ? count : count - 1};
+          volumetric_pool<T>(p, pr, count, wb.scan[ri], res, totalOpacity, set);
         }
+        result[0] = res[0];
+        result[1] = res[1];
+        result[2] = res[2];
+        a = res[3];
+        o = (T)totalOpacity;
       }
-      const T a2x = ambient.x * p.globalIlum, a2y = ambient.y * p.globalIlum, a2z = ambient.z * p.globalIlum;
-      // environment mapping (ObjectShader, src/shaders.cpp:71-76) of the default white texture
-      const T env = (p.envMapping ? (T)env_mapping(V3<double>{(double)nrm.x, (double)nrm.y, (double)nrm.z},
-                                                   V3<double>{(double)viewT.x, (double)viewT.y, (double)viewT.z})
-                                  : T(0)) * p.reflect;
-      const T objR = env * ambient.x + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
-      const T objG = env * ambient.y + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
-      const T objB = env * ambient.z + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
-      base[0] = objR + T(0) + (T(0) + p.mainLight[0] * spec * shadow);
-      base[1] = objG + T(0) + (T(0) + p.mainLight[1] * spec * shadow);
-      base[2] = objB + T(0) + (T(0) + p.mainLight[2] * spec * shadow);
-    } else {
-      const V3<T> bg = background(p, viewT);
-      base[0] = T(0) + bg.x + T(0);
-      base[1] = T(0) + bg.y + T(0);
-      base[2] = T(0) + bg.z + T(0);
-    }
-    T alpha, opacity;
-    if (flags & 4) {
-      // a long ray of the overflow pass: its volumetric pass was folded into an affine map
-      const T A = wb.vol[0 * wb.npix + gp];
-      out0 = A * base[0] + wb.vol[1 * wb.npix + gp];
-      out1 = A * base[1] + wb.vol[2 * wb.npix + gp];
-      out2 = A * base[2] + wb.vol[3 * wb.npix + gp];
-      alpha = wb.vol[4 * wb.npix + gp];
-      opacity = wb.vol[5 * wb.npix + gp];
-    } else {
-      // VolumetricShader over the ray's pooled step records, far to near, on this base colour
-      T res[4] = {base[0], base[1], base[2], hit ? T(1) + T(0) : T(0)};
-      float totalOpacity = 0.0f;
-      bool set = false;
-      if (p.needVolumetric) {
-        const int count = wb.count[gp];
-        const PoolRecords<T> pr{wb.pool_rec, wb.pool_prev, wb.last_chunk[gp],
-                                hit ? count : count - 1};
-        volumetric_pool<T>(p, pr, count, wb.scan[gp], res, totalOpacity, set);
+      if (d == 0) {
+        alpha = a;
+        opacity = o;
       }
-      out0 = res[0];
-      out1 = res[1];
-      out2 = res[2];
-      alpha = res[3];
-      opacity = (T)totalOpacity;
     }
+    out0 = result[0];
+    out1 = result[1];
+    out2 = result[2];
+    const bool hit = (wb.flags[gp] & 1) != 0;
     const double depth = hit ? (double)wb.scan[gp] : 1e20;
     if (c.opacity) c.opacity[pix] = to_u16_x86((double)opacity * 65535.0);
     if (c.alpha) c.alpha[pix] = to_u16_x86((double)alpha * 65535.0);
     if (c.zbuffer) c.zbuffer[pix] = (float)depth;
     // debug layer: 0 miss, 1 hit, 3 hit whose exact_hit refinement missed the level set
-    if (c.hit) c.hit[pix] = hit ? ((flags & 8) ? 3 : 1) : 0;
+    if (c.hit) c.hit[pix] = hit ? ((wb.flags[gp] & 8) ? 3 : 1) : 0;
     if (c.iters) c.iters[pix] = wb.iters[gp];
     if (c.depth) c.depth[pix] = depth;
     }

@@ -28,7 +28,9 @@ struct WaveBufs {
   uint32_t *polish_list; // [npix] hits the FP64 polish re-evaluates
   uint32_t *ctl;         // [0] primary jobs, [1] hits, [2] secondary jobs, [3] overflow count,
                          // [4] overflow-pass jobs, [5] pool chunks, [6] polish count,
-                         // [7] exact_hit refinements that missed the level set (zeroed per group)
+                         // [7] exact_hit refinements that missed the level set, [8] hits before
+                         // the current ray depth, [9] rays of the next depth, [10] rays of the
+                         // current depth (zeroed per group)
   uint32_t *overflow_list;
   // Step records of the primary rays: chunks of kChunk records linked backwards
   // (prev), allocated by bump counter; the pixel keeps its last chunk.
@@ -44,7 +46,19 @@ struct WaveBufs {
   int exact_hit;                         // 1: hits are refined in FP64 to the level set DE = thr
   int pair_rays;                         // lean FP32 Mandelbox, shadow/AO stage: 1 = two rays per
                                          // thread with packed f32x2 orbits (secondary_pair_kernel)
-  int64_t npix;
+  int64_t npix;                          // rays of the batch: rays x npix_frame (the stride of every
+                                         // [k][npix] array above)
+  // Ray-traced reflections (the reflection loop of src/Render3D.cpp:441-564): the ray of depth
+  // d of pixel gp sits at index d * npix_frame + gp of every per-ray array above. reflect_kernel
+  // writes the origin, direction and initial threshold of each depth's next rays.
+  int64_t npix_frame;                    // pixels of the batch
+  int rays;                              // 1 + reflectionsMax with reflections, else 1
+  int depth;                             // ray depth of this launch (primary, polish, reflect)
+  double *ray_start;                     // [3][npix] origin of a reflected ray
+  double *ray_dir;                       // [3][npix] its direction
+  double *ray_thr0;                      // [npix] the previous ray's distThresh, which the reflected
+                                         // ray's thresholds add (src/Render3D.cpp:88, 461-462)
+  uint32_t *ray_list;                    // [npix_frame] pixels whose next ray is marched
 };
 
 // Stage events of one launch sequence (see WaveLaunch::ev) and the stats slot of each
@@ -54,6 +68,8 @@ constexpr int kStages = 6;
 
 constexpr int kChunk = 32;       // step records per pool chunk
 constexpr int kPoolChunksPerPixel = 4;   // pool budget; rays beyond it take the overflow pass
+constexpr int kPoolChunksPerReflectedRay = 6;   // the same with reflections, per ray of the loop
+constexpr int kWaveOverflowThreads = 2048;      // threads of the wavefront's overflow pass
 
 // Parameters of the differentiable render: [0] fractal parameter (power of formula 2,
 // scale of formula 8), [1..3] camera position, [4] main light alpha, [5] main light beta.

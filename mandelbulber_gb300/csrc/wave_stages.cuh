@@ -14,12 +14,35 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
     if (L.ev[0]) cudaEventRecord(L.ev[k], s);
   };
   mark(0);
-  dev::primary_kernel<T, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), L.wb, L.cams, L.ncams);
-  if (L.overflow)
-    dev::primary_kernel<T, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), L.wb, L.cams, L.ncams);
-  mark(1);
-  if constexpr (sizeof(T) == 4)
-    dev::polish_kernel<F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), L.wb, L.cams, L.ncams);
+  // one primary pass (and FP64 polish) per ray depth of the reflection loop; between two
+  // depths the reflect stage spawns the next depth's rays from this depth's hits
+  for (int d = 0; d < L.wb.rays; d++) {
+    WaveBufs<T> wbd = L.wb;
+    wbd.depth = d;
+    if (d > 0) {
+      WaveBufs<T> wbp = L.wb;
+      wbp.depth = d - 1;
+      dev::reflect_kernel<T, F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 0), wbp, L.cams, L.ncams);
+      dev::next_depth_kernel<T><<<1, 1, 0, s>>>(L.wb.ctl);
+    }
+    if (L.wb.rays > 1) {
+      dev::primary_kernel<T, F, FAST, true><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), wbd, L.cams,
+                                                                        L.ncams);
+      if (L.overflow)
+        dev::primary_kernel<T, F, FAST, true><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), wbd, L.cams,
+                                                                             L.ncams);
+    } else {
+      dev::primary_kernel<T, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), wbd, L.cams, L.ncams);
+      if (L.overflow)
+        dev::primary_kernel<T, F, FAST><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), wbd, L.cams,
+                                                                       L.ncams);
+    }
+    // with reflections the primary stage's time holds every depth's march, polish and reflection
+    if (L.wb.rays == 1) mark(1);
+    if constexpr (sizeof(T) == 4)
+      dev::polish_kernel<F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), wbd, L.cams, L.ncams);
+  }
+  if (L.wb.rays > 1) mark(1);
   mark(2);
   if (L.wb.exact_hit)
     dev::level_set_kernel<T, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
@@ -34,8 +57,12 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   mark(4);
   // slow shading: one warp's 11^3 normal samples in dynamic shared memory per warp
   const size_t composeSmem = L.p.slowShading ? (size_t)(L.block / 32) * dev::kSlowSamples * sizeof(T) : 0;
-  dev::compose_kernel<T, F, FAST><<<L.compose_grid, L.block, composeSmem, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams,
-                                                                             L.ncams);
+  if (L.wb.rays > 1)
+    dev::compose_kernel<T, F, FAST, true><<<L.compose_grid, L.block, composeSmem, s>>>(L.p, stage_io(L.io, 3), L.wb,
+                                                                                     L.cams, L.ncams);
+  else
+    dev::compose_kernel<T, F, FAST><<<L.compose_grid, L.block, composeSmem, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams,
+                                                                               L.ncams);
   mark(5);
   if (L.gcams)
     dev::grad_kernel<T, F, FAST><<<L.grad_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 5), L.wb, L.cams, L.gcams,
