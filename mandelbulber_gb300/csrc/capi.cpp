@@ -231,15 +231,29 @@ static bool need_volumetric(const mbgb_scene &s) {
   return (s.glow_intensity != 0.0) || s.fogEnabled || (s.fogDensity > 0.0) || need_step_points(s);
 }
 
-// Features that the per-pixel engine renders and the wavefront stages do not carry (aux,
-// fake and volumetric lights, iteration fog): scenes that use them render on the per-pixel
-// engine. Slow shading, environment mapping and primitive objects are composition-stage work
-// the wavefront carries; ray-traced reflections are further primary passes, one per depth,
-// except with slow shading (whose warp-wide normals serve the camera rays only) or the limit
-// box (whose early return leaves itersOut to the next ray, src/fractal.cpp:1252-1262).
+// Auxiliary lights of a scene (random ones, then the four predefined): numberOfLights.
+static int aux_light_count(const mbgb_scene &s) {
+  return uses_aux_lights(s) ? std::max(s.auxLightNumber > 0 ? s.auxLightNumber : 0, 4) : 0;
+}
+
+// Features that the per-pixel engine renders and the wavefront stages do not carry (fake and
+// volumetric lights, iteration fog): scenes that use them render on the per-pixel engine.
+// Slow shading, environment mapping and primitive objects are composition-stage work the
+// wavefront carries; ray-traced reflections are further primary passes, one per depth, except
+// with slow shading (whose warp-wide normals serve the camera rays only) or the limit box
+// (whose early return leaves itersOut to the next ray, src/fractal.cpp:1252-1262). Auxiliary
+// lights are a normal stage, AuxShadow jobs in the shadow stage and their sums in the
+// composition, except with slow shading (the jobs need the normals first) or when one shadow
+// factor per light and ray would pass 4 GB.
 static bool per_pixel_only(const mbgb_scene &s) {
-  return uses_aux_lights(s) || s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled ||
-         (reflection_rays(s) > 1 && (s.slowShading || s.limits_enabled));
+  if (s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled) return true;
+  if (reflection_rays(s) > 1 && (s.slowShading || s.limits_enabled)) return true;
+  if (uses_aux_lights(s)) {
+    if (s.slowShading) return true;
+    const double rays = (double)s.image_width * s.image_height * reflection_rays(s);
+    if (rays * aux_light_count(s) * sizeof(double) > 4e9) return true;
+  }
+  return false;
 }
 
 // The instantiation a scene's kernels run: Compute<orbitTrap> of the fake lights and the
@@ -1027,14 +1041,16 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
 struct WaveLayout {
   size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
   size_t prec, pprev;
-  size_t rstart, rdir, rthr, rlist;
+  size_t rstart, rdir, rthr, rlist, normal, auxsh;
   uint32_t poolCap;
   size_t total;
 };
 
 // `npixFrame` pixels with `rays` rays each (the reflection loop's depths): every per-ray array
 // holds rays x npixFrame entries.
-static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVol, int rays) {
+// `auxN` auxiliary lights: hit normals, and with `auxShadows` one AuxShadow factor per light.
+static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVol, int rays, int auxN,
+                              bool auxShadows) {
   const int64_t npix = npixFrame * rays;
   WaveLayout w{};
   size_t off = 0;
@@ -1073,6 +1089,8 @@ static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVo
   w.rdir = take(3 * refl * sizeof(double));
   w.rthr = take(refl * sizeof(double));
   w.rlist = take((rays > 1 ? (size_t)npixFrame : 0) * 4);
+  w.normal = take(auxN > 0 ? 3 * (size_t)npix * ts : 0);
+  w.auxsh = take(auxN > 0 && auxShadows ? (size_t)auxN * npix * ts : 0);
   w.total = off;
   return w;
 }
@@ -1088,14 +1106,15 @@ static int wave_occupancy(int formula, int block, int which) {
 template <typename T>
 static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const Group &g, const mbgb_opts &o,
                                 cudaStream_t s, FrameIO io, uint32_t *ctl, cudaEvent_t *ev, bool grad,
-                                uint64_t *launches) {
+                                uint64_t *launches, int64_t lightOff) {
   const mbgb_scene &scene = scenes[g.frames[0]];
   const int prec = sizeof(T) == 8 ? 0 : 1;
   const bool needVol = need_volumetric(scene);
   const bool rayAO = scene.global_ilumination && !scene.fastGlobalIllumination;
   const int aoN = rayAO ? c->ao_count : 0;
   const int rays = reflection_rays(scene);
-  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays);
+  const int auxN = aux_light_count(scene);
+  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays, auxN, scene.shadow != 0);
   char *base = (char *)c->wave[prec].ptr;
   WaveLaunch<T> L;
   WaveBufs<T> &wb = L.wb;
@@ -1132,6 +1151,8 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.ray_dir = (double *)(base + w.rdir);
   wb.ray_thr0 = (double *)(base + w.rthr);
   wb.ray_list = (uint32_t *)(base + w.rlist);
+  wb.normal = auxN > 0 ? (T *)(base + w.normal) : nullptr;
+  wb.auxsh = auxN > 0 && scene.shadow ? (T *)(base + w.auxsh) : nullptr;
   // shadow/AO rays two per thread (secondary_pair_kernel): the lean FP32 Mandelbox with
   // per-estimate refill, which the pair kernel's packed orbit serves
   wb.pair_rays = (sizeof(T) == 4 && fast_mandelbox(scene) && g.cfg.pairRays && g.cfg.orbitRefill <= 0) ? 1 : 0;
@@ -1166,6 +1187,8 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.ov.step_step = c->ovstep[prec][0].ptr;
   L.ov.step_dist = c->ovstep[prec][1].ptr;
   L.ov.step_thr = c->ovstep[prec][2].ptr;
+  // the visible auxiliary lights of a long ray sample its record positions
+  L.ov.step_scan = need_step_points(scene) ? c->ovstep[prec][3].ptr : nullptr;
   L.overflow = needVol;
   for (int k = 0; k < kStageEvents; k++) L.ev[k] = ev ? ev[k] : nullptr;
   // the FAST instantiations hold no limit box test: limit-box scenes take the generic kernels,
@@ -1173,6 +1196,10 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.fast = (fast_mandelbox(scene) || fast_mandelbulb(scene)) && !scene.limits_enabled;
   fill_fractal<double>(scene, L.fd);
   fill_params<T>(scene, L.p, o, (const T *)(prec == 0 ? c->ao64.ptr : c->ao32.ptr), c->ao_count);
+  if (lightOff >= 0)
+    L.p.lights = (const LightT<T> *)(prec == 0 ? c->lights64.ptr : c->lights32.ptr) + lightOff;
+  else if (auxN > 0)
+    return set_error(MBGB_ERR_CUDA, "auxiliary lights were not placed");
   cudaError_t e;
   if constexpr (sizeof(T) == 8) e = launch_wave_f64(L, s);
   else e = launch_wave_f32(L, s);
@@ -1180,7 +1207,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   // per ray depth: primary (+ overflow) pass and polish; per further depth the reflect and
   // counter kernels
   *launches += 2 + (int64_t)rays * (1 + (needVol ? 1 : 0) + (prec == 1 ? 1 : 0)) + 2 * (int64_t)(rays - 1) +
-               (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
+               (wb.normal ? 1 : 0) + (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
   return MBGB_OK;
 }
 
@@ -1582,17 +1609,19 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     const int64_t fjobs = (int64_t)((sc.image_width + cfg.tileW - 1) / cfg.tileW) *
                           ((r1 - r0 + cfg.tileH - 1) / cfg.tileH) * 32;
     const bool rayAO = sc.global_ilumination && !sc.fastGlobalIllumination;
-    const double perPix = (1.0 + (rayAO ? c->ao_count : 0)) * reflection_rays(sc);
+    const double perPix = (1.0 + (rayAO ? c->ao_count : 0) + aux_light_count(sc)) * reflection_rays(sc);
     const bool wave = o.engine == MBGB_ENGINE_WAVEFRONT && !per_pixel_only(sc) &&
                       (double)std::max(fpix, fjobs) * perPix < kMaxGroupJobs;
     if (!wave && (grad || o.exact_hit))
       return set_error(MBGB_ERR_BAD_PARAM, "exact hits and gradients need the wavefront engine and frames below 4e9 rays");
     Group *g = nullptr;
-    if (wave) {
+    // a frame with auxiliary lights keeps its own group: its lights are placed for it
+    if (wave && !uses_aux_lights(sc)) {
       for (auto &h : plan.groups) {
         if (!h.wave || h.prec != prec[i]) continue;
         if ((double)std::max(h.npix + fpix, h.jobs + fjobs) * perPix >= kMaxGroupJobs) continue;
         const mbgb_scene &rep = scenes[h.frames[0]];
+        if (uses_aux_lights(rep)) continue;
         const bool same = prec[i] == 0 ? same_shared<double>(rep, sc, o) : same_shared<float>(rep, sc, o);
         if (!same) continue;
         const LaunchCfg &hc = h.cfg;
@@ -1627,7 +1656,7 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     const mbgb_scene &rep = scenes[g.frames[0]];
     const bool needVol = need_volumetric(rep);
     if (needVol) volPrec[g.prec] = true;
-    if (!g.wave && need_step_points(rep)) pointsPrec[g.prec] = true;
+    if (need_step_points(rep)) pointsPrec[g.prec] = true;
     if (!g.wave)
       ovRecords[g.prec] =
           std::max(ovRecords[g.prec], (int64_t)overflow_slots(rep, g.prec) * reflection_rays(rep));
@@ -1636,8 +1665,10 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     if (g.wave) {
       const bool rayAO = rep.global_ilumination && !rep.fastGlobalIllumination;
       const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
-      wave_bytes[g.prec] = std::max(
-          wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol, reflection_rays(rep)).total);
+      wave_bytes[g.prec] =
+          std::max(wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol, reflection_rays(rep),
+                                                   aux_light_count(rep), rep.shadow != 0)
+                                           .total);
       g.cams_off = camsBytes;
       const size_t cs = g.prec == 0 ? sizeof(FrameCam<double>) : sizeof(FrameCam<float>);
       camsBytes += (cs * g.frames.size() + 255) & ~(size_t)255;
@@ -1722,12 +1753,12 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     }
   }
 
-  // auxiliary light tables of the per-pixel frames that light with them
+  // auxiliary light tables of the frames that light with them
   std::vector<int64_t> lightOff((size_t)n, -1);
   {
     std::vector<LightT<double>> all64;
     for (auto &g : plan.groups) {
-      if (g.wave || !uses_aux_lights(scenes[g.frames[0]])) continue;
+      if (!uses_aux_lights(scenes[g.frames[0]])) continue;
       std::vector<LightT<double>> L;
       st = place_lights(c, scenes[g.frames[0]], s, L);
       if (st != MBGB_OK) return st;
@@ -1772,9 +1803,11 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
         r = enqueue_per_pixel(c, scenes[g.frames[0]], imgs[g.frames[0]], g, o, s, io, gctl, &plan.launches,
                               lightOff[(size_t)g.frames[0]]);
       } else if (g.prec == 0) {
-        r = enqueue_wave<double>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches);
+        r = enqueue_wave<double>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches,
+                                 lightOff[(size_t)g.frames[0]]);
       } else {
-        r = enqueue_wave<float>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches);
+        r = enqueue_wave<float>(c, scenes, g, o, s, io, (uint32_t *)gctl, ev, plan.grad, &plan.launches,
+                                lightOff[(size_t)g.frames[0]]);
       }
       if (r != MBGB_OK) return r;
     }

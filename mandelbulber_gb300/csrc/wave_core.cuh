@@ -281,12 +281,14 @@ __device__ __forceinline__ unsigned int claim_jobs(unsigned int *counter, const 
 }
 
 // One pooled step record: dist, thr, step in a 16-byte (float) or 32-byte (double) slot.
-__device__ __forceinline__ void store_record(float *r, const float dist, const float thr, const float step) {
-  *reinterpret_cast<float4 *>(r) = make_float4(dist, thr, step, 0.0f);
+__device__ __forceinline__ void store_record(float *r, const float dist, const float thr, const float step,
+                                             const float scan) {
+  *reinterpret_cast<float4 *>(r) = make_float4(dist, thr, step, scan);
 }
-__device__ __forceinline__ void store_record(double *r, const double dist, const double thr, const double step) {
+__device__ __forceinline__ void store_record(double *r, const double dist, const double thr, const double step,
+                                             const double scan) {
   reinterpret_cast<double2 *>(r)[0] = make_double2(dist, thr);
-  reinterpret_cast<double2 *>(r)[1] = make_double2(step, 0.0);
+  reinterpret_cast<double2 *>(r)[1] = make_double2(step, scan);
 }
 __device__ __forceinline__ void load_record(const float *r, float &dist, float &thr, float &step) {
   const float4 q = *reinterpret_cast<const float4 *>(r);
@@ -297,6 +299,9 @@ __device__ __forceinline__ void load_record(const double *r, double &dist, doubl
   const double2 b = reinterpret_cast<const double2 *>(r)[1];
   dist = a.x; thr = a.y; step = b.x;
 }
+// the record's march position (sStep::point = start + view * scan)
+__device__ __forceinline__ float record_scan(const float *r) { return r[3]; }
+__device__ __forceinline__ double record_scan(const double *r) { return r[3]; }
 
 // Frame of a primary job / of a pixel of the batch (binary search over the frame table).
 template <typename T>
@@ -397,12 +402,61 @@ __device__ __forceinline__ bool camera_dir(const ParamsT<T> &p, const FrameCam<T
   return ok;
 }
 
+// Visible auxiliary lights (VolumetricShader, src/shaders.cpp:242-296) at one step group of a
+// ray: a bell-shaped glow around each light, sampled in up to 50 sub-steps near the closest
+// one; adds to out[0..3] in the reference's order (the same arithmetic as the per-pixel
+// engine's `volumetric`).
+template <typename T>
+__device__ __forceinline__ void visible_aux_lights(const ParamsT<T> &p, const V3<T> point, const V3<T> view,
+                                                   const T step, T out[4]) {
+  T lowestLightSize = T(1e10);
+  T lowestLightDist = T(1e10);
+  for (int i = 0; i < p.numberOfLights; ++i) {
+    const LightT<T> L = p.lights[i];
+    if (!(i < p.auxLightNumber || L.enabled)) continue;
+    const T lightDist = length3(point - V3<T>{L.pos[0], L.pos[1], L.pos[2]});
+    const T lightSize = L.intensity * p.auxLightIntensity * p.auxLightVisibility;
+    const T r2 = lightDist / lightSize;
+    if (r2 < lowestLightSize) {
+      lowestLightSize = r2;
+      lowestLightDist = lightDist;
+    }
+  }
+  int smallSteps = to_i32_x86((double)(T(10) * step / (lowestLightDist + T(1.0e-20))));
+  if (smallSteps > 50) smallSteps = 50;
+  int smallStep_start = 0, smallStep_end = 1;
+  T step2 = step;
+  if (smallSteps > 0) {
+    smallStep_start = 1;
+    smallStep_end = smallSteps + 1;
+    step2 = step / (T(smallSteps) + T(1));
+  }
+  for (int smallStep = smallStep_start; smallStep < smallStep_end; smallStep++) {
+    const V3<T> point2 = point - view * step2 * T(smallStep);
+    for (int i = 0; i < p.numberOfLights; ++i) {
+      const LightT<T> L = p.lights[i];
+      if (!(i < p.auxLightNumber || L.enabled)) continue;
+      const T lightDist = length3(point2 - V3<T>{L.pos[0], L.pos[1], L.pos[2]});
+      const T lightSize = L.intensity * p.auxLightIntensity * p.auxLightVisibility;
+      T r2 = lightDist / lightSize;
+      if (r2 > T(1)) r2 = T(1);
+      const T bellFunction = (m_cos(r2 * T(kPI)) + T(1)) / (r2 * r2 + T(0.02)) * T(0.3);
+      const T lightDensity = step2 * bellFunction / lightSize;
+      out[0] += lightDensity * T(L.colour[0]) / T(65536);
+      out[1] += lightDensity * T(L.colour[1]) / T(65536);
+      out[2] += lightDensity * T(L.colour[2]) / T(65536);
+      out[3] += lightDensity;
+    }
+  }
+}
+
 // The volumetric pass over one ray's records (VolumetricShader's glow, post fog and
 // volumetric fog, src/shaders.cpp:185-478) as the affine map out = A*base + B, plus
 // the alpha and opacity it leaves for a base alpha of `alpha0`.
-template <typename T>
+template <typename T, bool EFX>
 __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
-                                                  const T depth, const T alpha0, T vol[6]) {
+                                                  const T depth, const T alpha0, const V3<T> rayStart,
+                                                  const V3<T> view, T vol[6]) {
   T A = T(1), B0 = T(0), B1 = T(0), B2 = T(0), alpha = alpha0;
   float totalOpacity = 0.0f, opacityOut = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
@@ -426,6 +480,15 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
     B1 = go * gG + (T(1) - go) * B1;
     B2 = go * gB + (T(1) - go) * B2;
     alpha += go;
+    if (EFX && p.auxLightVisibility > T(0) && p.numberOfLights > 0 && sb.scan) {
+      // the visible lights add to the colour: the map's offset
+      T add[4] = {B0, B1, B2, alpha};
+      visible_aux_lights<T>(p, rayStart + view * sb.scan[sb.at(index)], view, step, add);
+      B0 = add[0];
+      B1 = add[1];
+      B2 = add[2];
+      alpha = add[3];
+    }
     if (p.postFog) {
       T fd = step / p.fogVisibility;
       if (fd > T(1)) fd = T(1);
@@ -475,14 +538,15 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 // ---------------------------------------------------------------------------
 // Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
-// REFL: the batch has reflected rays (WaveBufs::rays > 1); without, the kernel holds no
-// reflected-ray state.
-template <typename T, int FORMULA, bool FAST, bool REFL = false>
+// EFX: the effects variant (reflected rays, WaveBufs::rays > 1, or auxiliary lights); the
+// plain variant holds neither's state.
+template <typename T, int FORMULA, bool FAST, bool EFX = false>
 __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, nullptr, nullptr, io.slots, slot};
+  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, (T *)io.step_scan, nullptr, io.slots,
+                      slot};
   const bool useSB = p.needVolumetric;
   const bool f64 = sizeof(T) == 8;
   const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
@@ -490,7 +554,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
   const int stepCap = io.overflow_pass ? kStepSlots : io.step_cap;
   // jobs: every frame's tiles (partial tiles included), the reflected rays of this depth, or
   // the overflow list
-  const int depth = REFL ? wb.depth : 0;
+  const int depth = EFX ? wb.depth : 0;
   const unsigned int nJobs = io.overflow_pass ? *(volatile unsigned int *)&wb.ctl[3]
                              : depth > 0      ? *(volatile unsigned int *)&wb.ctl[10]
                                               : cams[ncams - 1].jobBase + cams[ncams - 1].jobCount;
@@ -526,7 +590,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           if (io.overflow_pass || depth > 0) {
             ri = io.overflow_pass ? (int64_t)wb.overflow_list[job]
                                   : (int64_t)depth * wb.npix_frame + (int64_t)wb.ray_list[job];
-            gp = REFL ? pixel_of_ray(wb, ri) : ri;
+            gp = EFX ? pixel_of_ray(wb, ri) : ri;
             fr = frame_of_pixel(cams, ncams, gp);
             const int64_t local = gp - cams[fr].pixBase;
             x = (int)(local % cams[fr].width);
@@ -541,7 +605,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           const FrameCam<T> &c = cams[fr];
           if (x < c.width && y < c.row_end) {
             bool marched = true;
-            if (!REFL || ri < wb.npix_frame) {
+            if (!EFX || ri < wb.npix_frame) {
               marched = camera_dir(p, c, x, y, dir);
               start = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
               thrInit = T(0);
@@ -589,8 +653,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
       const V3<T> point = start + dir * scan;
       if (phase == 0) {
         if (p.constantDEThreshold) thr = p.quality;
-        else if (f64) thr = REFL ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
-        else thr = REFL ? scan * thrScale + thrInit : scan * thrScale;
+        else if (f64) thr = EFX ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
+        else thr = EFX ? scan * thrScale + thrInit : scan * thrScale;
         if (p.perspType == 1 || p.perspType == 2) thr *= T(kPI);
         detail = thr;
       }
@@ -626,7 +690,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             rec = (int64_t)chunk * kChunk + (i % kChunk);
             // the record's step slot holds the step that reached this point; the walk
             // never reads it for the hit record
-            store_record(wb.pool_rec + 4 * rec, dist, thr, step);
+            store_record(wb.pool_rec + 4 * rec, dist, thr, step, scan);
           }
         }
         if (dist > T(3)) dist = T(3);
@@ -637,7 +701,10 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           bis = 0;
           if (dist < thr && dist > thr * search_limit) done = true;
         } else {
-          if (useSB && io.overflow_pass) sb.step[sb.at(i)] = step;
+          if (useSB && io.overflow_pass) {
+            sb.step[sb.at(i)] = step;
+            if (sb.scan) sb.scan[sb.at(i)] = scan;
+          }
           step = (dist - stepFrac * thr) * p.DE_factor;
           if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)gp, (uint32_t)i)) / T(10000));
           buffCount++;
@@ -650,8 +717,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           if (dist > thr) scan += step;
           else if (dist < thr * search_limit) scan -= step;
           if (p.constantDEThreshold) thr = p.quality;
-          else if (f64) thr = REFL ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
-          else thr = REFL ? scan * thrScale + thrInit : scan * thrScale;
+          else if (f64) thr = EFX ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
+          else thr = EFX ? scan * thrScale + thrInit : scan * thrScale;
           bis = 1;
         }
       } else {
@@ -663,8 +730,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           if (dist > thr) scan += step;
           else if (dist < thr * search_limit) scan -= step;
           if (p.constantDEThreshold) thr = p.quality;
-          else if (f64) thr = REFL ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
-          else thr = REFL ? scan * thrScale + thrInit : scan * thrScale;
+          else if (f64) thr = EFX ? scan * res * persp / p.quality + thrInit : scan * res * persp / p.quality;
+          else thr = EFX ? scan * thrScale + thrInit : scan * thrScale;
           bis++;
         }
       }
@@ -676,7 +743,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
         if (io.overflow_pass && useSB) {
           // rare long rays: fold the records now (the slot is reused); compose applies the map
           T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
-          volumetric_affine<T>(p, sb, buffCount, scan, found ? T(1) : T(0), vol);
+          volumetric_affine<T, EFX>(p, sb, buffCount, scan, found ? T(1) : T(0), start, dir, vol);
           for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + ri] = vol[c];
           flags |= 4;
         }
@@ -943,6 +1010,34 @@ __global__ void __launch_bounds__(128) reflect_kernel(const __grid_constant__ Pa
   }
 }
 
+// Auxiliary lights: CalculateNormals (src/shaders.cpp:675-757: 4 DEs at N x 5, minN 0) at
+// every hit of every depth, before the shadow stage, whose AuxShadow jobs test each light's
+// Lambert and Blinn terms; the composition stage reads the same normals.
+template <typename T, int FORMULA, bool FAST>
+__global__ void __launch_bounds__(128) normal_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io,
+                                                     const WaveBufs<T> wb, const FrameCam<T> *__restrict__ cams,
+                                                     const int ncams) {
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  Counters cnt{0, 0, 0, 0};
+  for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += gridDim.x * blockDim.x) {
+    const int64_t ri = (int64_t)wb.hit_list[k];
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, pixel_of_ray(wb, ri))];
+    const HitInfo<T> h = hit_info(p, c, wb, ri);
+    const V3<T> n = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
+    wb.normal[ri] = n.x;
+    wb.normal[wb.npix + ri] = n.y;
+    wb.normal[2 * wb.npix + ri] = n.z;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    cnt.orbit += __shfl_down_sync(0xffffffffu, cnt.orbit, off);
+    cnt.calls += __shfl_down_sync(0xffffffffu, cnt.calls, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&io.counters[0], cnt.orbit);
+    atomicAdd(&io.counters[1], cnt.calls);
+  }
+}
+
 // Between two reflection depths (one thread): the next depth's rays become the current ones,
 // the per-depth job, overflow and polish counters restart, the hit count so far is kept.
 template <typename T>
@@ -975,38 +1070,125 @@ __device__ __forceinline__ V3<T> ray_at(const V3<T> &o, const V3<T> &d, const T 
   return V3<T>{add_mul_rn(o.x, d.x, r), add_mul_rn(o.y, d.y, r), add_mul_rn(o.z, d.z, r)};
 }
 
-// State of one shadow (kind 0) or AO (kind 1) ray.
+// Lambert and Blinn terms of one auxiliary light at a hit (LightShading, src/shaders.cpp:1023-1067),
+// 1 / r^2 falloff shared among `number` lights. The shadow stage tests them to decide whether
+// the light's AuxShadow is traced; the composition stage weighs them by its result.
+template <typename T>
+struct AuxTerms {
+  T shade, shade2, distance;
+  V3<T> lightVector;
+};
+template <typename T>
+__device__ __forceinline__ AuxTerms<T> aux_light_terms(const ParamsT<T> &p, const LightT<T> &L, const int number,
+                                                       const V3<T> point, const V3<T> normal, const V3<T> view) {
+  AuxTerms<T> a;
+  const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - point;
+  a.distance = length3(d);
+  a.lightVector = normalize3(d);
+  const T intensity = p.auxLightIntensity * T(100) * L.intensity / (a.distance * a.distance) / T(number);
+  T shade = dot3(normal, a.lightVector);
+  if (shade < T(0)) shade = T(0);
+  shade = shade * intensity;
+  if (shade > T(500)) shade = T(500);
+  const V3<T> half = normalize3(a.lightVector - view);
+  T shade2 = dot3(normal, half);
+  if (shade2 < T(0)) shade2 = T(0);
+  shade2 = m_pow(shade2, T(30)) * T(1);
+  shade2 *= intensity * p.specular;
+  if (shade2 > T(15)) shade2 = T(15);
+  a.shade = shade;
+  a.shade2 = shade2;
+  return a;
+}
+
+// Direction of ray `ri` in the march precision: the camera ray for depth 0, the reflected
+// direction otherwise.
+template <typename T>
+__device__ __forceinline__ V3<T> ray_view(const ParamsT<T> &p, const FrameCam<T> &c, const WaveBufs<T> &wb,
+                                          const int64_t ri, const int64_t gp) {
+  V3<T> v;
+  if (ri < wb.npix_frame) {
+    const int64_t local = gp - c.pixBase;
+    camera_dir(p, c, (int)(local % c.width), (int)(local / c.width), v);
+  } else {
+    v = {(T)wb.ray_dir[ri], (T)wb.ray_dir[wb.npix + ri], (T)wb.ray_dir[2 * wb.npix + ri]};
+  }
+  return v;
+}
+
+// Jobs of the shadow stage: one main-light shadow ray per hit, aoCount AO rays per hit, and
+// (aux lights with shadows) one AuxShadow per enabled light and hit.
+struct SecondaryJobs {
+  unsigned int nShadow, nAO, nAux;
+};
+template <typename T, bool EFX = false>
+__device__ __forceinline__ SecondaryJobs secondary_jobs(const ParamsT<T> &p, const WaveBufs<T> &wb,
+                                                        const unsigned int nh) {
+  SecondaryJobs j;
+  j.nShadow = p.shadow ? nh : 0u;
+  j.nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
+  j.nAux = (EFX && p.shadow && wb.auxsh) ? nh * (unsigned int)p.numberOfLights : 0u;
+  return j;
+}
+
+// State of one shadow (kind 0), AO (kind 1) or auxiliary-light shadow (kind 2) ray.
 template <typename T>
 struct SecondaryRay {
   int kind;
-  unsigned int j;   // AO direction
+  unsigned int j;   // AO direction or auxiliary light
   int64_t gp;       // ray of the batch (pixel + reflection depth x npix_frame)
   V3<T> point, dir;
   T r, end, sh, thr, detail, maxSoft, stepMul, fpar;
   int guard;
 };
 
-// Starts job `job`: MainShadow's (src/shaders.cpp:480-570) or AmbientOcclusion's
-// (src/shaders.cpp:572-640) loop set-up for one ray. Returns false when the loop body
-// never runs (the result is written at once).
+// AuxShadow's set-up (kind 2): it runs for an enabled light whose Lambert or Blinn term passes
+// 0.01 (AuxLightsShader, src/shaders.cpp:1043-1052); the others keep the factor 1, unused.
 template <typename T>
+__device__ __forceinline__ void aux_shadow_begin(const ParamsT<T> &p, const WaveBufs<T> &wb, const FrameCam<T> &c,
+                                              const HitInfo<T> &h, const int64_t px, SecondaryRay<T> &s) {
+  const LightT<T> L = p.lights[s.j];
+  bool trace = s.j < (unsigned int)p.auxLightNumber || L.enabled;
+  if (trace) {
+    const V3<T> nrm{wb.normal[s.gp], wb.normal[wb.npix + s.gp], wb.normal[2 * wb.npix + s.gp]};
+    const AuxTerms<T> a = aux_light_terms(p, L, p.numberOfLights, h.point, nrm, ray_view(p, c, wb, s.gp, px));
+    trace = a.shade > T(0.01) || a.shade2 > T(0.01);
+    s.dir = a.lightVector;
+    s.end = a.distance;
+  }
+  s.r = h.delta;
+  s.stepMul = p.DE_factor;
+  if (!trace) s.end = T(0);
+}
+
+// Starts job `job`: MainShadow's (src/shaders.cpp:480-570), AmbientOcclusion's
+// (src/shaders.cpp:572-640) or AuxShadow's (src/shaders.cpp:1069-1132) loop set-up for one
+// ray. Returns false when the loop body never runs (the result is written at once).
+template <typename T, bool EFX = false>
 __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveBufs<T> &wb,
                                                 const FrameCam<T> *__restrict__ cams, const int ncams,
-                                                const unsigned int nh, const unsigned int nShadow,
+                                                const unsigned int nh, const SecondaryJobs &jn,
                                                 const unsigned int job, SecondaryRay<T> &s) {
-  s.kind = job < nShadow ? 0 : 1;
-  if (s.kind == 0) {
+  if (job < jn.nShadow) {
+    s.kind = 0;
     s.gp = (int64_t)wb.hit_list[job];
+  } else if (job < jn.nShadow + jn.nAO) {
+    const unsigned int q = job - jn.nShadow;
+    s.kind = 1;
+    s.j = q / nh;
+    s.gp = (int64_t)wb.hit_list[q % nh];
   } else {
-    const unsigned int q = job - nShadow;
+    const unsigned int q = job - jn.nShadow - jn.nAO;
+    s.kind = 2;
     s.j = q / nh;
     s.gp = (int64_t)wb.hit_list[q % nh];
   }
-  const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, pixel_of_ray(wb, s.gp))];
+  const int64_t px = pixel_of_ray(wb, s.gp);
+  const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, px)];
   const HitInfo<T> h = hit_info(p, c, wb, s.gp);
   s.point = h.point;
   s.fpar = c.fparam;
-  // MainShadow and AmbientOcclusion compare with the threshold stored in a float
+  // MainShadow, AmbientOcclusion and AuxShadow compare with the threshold stored in a float
   s.thr = (T)(float)h.thr;
   s.sh = T(1);
   s.maxSoft = T(0);
@@ -1020,16 +1202,21 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
     s.detail = s.thr;
     s.stepMul = p.DE_factor;
   } else {
-    s.dir = {__ldg(&p.aoVec[3 * s.j + 0]), __ldg(&p.aoVec[3 * s.j + 1]), __ldg(&p.aoVec[3 * s.j + 2])};
-    s.end = h.delta / c.resolution;
-    s.r = h.delta;
     // detailSize after MainShadow: the float threshold if its loop ran at least once
     s.detail = (p.shadow && shadowStart < factor) ? s.thr : h.thr;
-    s.stepMul = T(2);
+    if (s.kind == 1) {
+      s.dir = {__ldg(&p.aoVec[3 * s.j + 0]), __ldg(&p.aoVec[3 * s.j + 1]), __ldg(&p.aoVec[3 * s.j + 2])};
+      s.end = h.delta / c.resolution;
+      s.r = h.delta;
+      s.stepMul = T(2);
+    } else if constexpr (EFX) {
+      aux_shadow_begin(p, wb, c, h, px, s);
+    }
   }
   if (!(s.r < s.end)) {
     if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? T(1) : s.sh;
-    else wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    else if (!EFX || s.kind == 1) wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    else wb.auxsh[(int64_t)s.j * wb.npix + s.gp] = s.sh;
     return false;
   }
   return true;
@@ -1037,7 +1224,7 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
 
 // One loop iteration of the ray after its distance estimate `dist` (maxIter `mi`) at
 // point + dir * r. Returns true when the ray has ended (its result is written).
-template <typename T>
+template <typename T, bool EFX = false>
 __device__ __forceinline__ bool secondary_step(const ParamsT<T> &p, const WaveBufs<T> &wb, SecondaryRay<T> &s,
                                                const T dist, const bool mi) {
   bool done = false;
@@ -1057,10 +1244,20 @@ __device__ __forceinline__ bool secondary_step(const ParamsT<T> &p, const WaveBu
       if (s.sh < T(0)) s.sh = T(0);
       done = true;
     }
-  } else {
+  } else if (!EFX || s.kind == 1) {
     if (dist < s.thr || mi || s.sh < T(0)) {
       s.sh -= (s.end - s.r) / s.end;
       if (s.sh < T(0)) s.sh = T(0);
+      done = true;
+    }
+  } else {
+    if (dist < s.thr || mi || s.sh < T(0)) {
+      if (p.penetrating) {
+        s.sh -= (s.end - s.r) / s.end;
+        if (s.sh < T(0)) s.sh = T(0);
+      } else {
+        s.sh = T(0);
+      }
       done = true;
     }
   }
@@ -1070,7 +1267,8 @@ __device__ __forceinline__ bool secondary_step(const ParamsT<T> &p, const WaveBu
   }
   if (done) {
     if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? (T(1) - s.maxSoft) : s.sh;
-    else wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    else if (!EFX || s.kind == 1) wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    else wb.auxsh[(int64_t)s.j * wb.npix + s.gp] = s.sh;
   }
   return done;
 }
@@ -1084,9 +1282,8 @@ template <int FORMULA>
 __device__ __forceinline__ void secondary_lean(const ParamsT<float> &p, const FrameIO &io, const WaveBufs<float> &wb,
                                                const FrameCam<float> *__restrict__ cams, const int ncams) {
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
-  const unsigned int nShadow = p.shadow ? nh : 0u;
-  const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
-  const unsigned int njobs = nShadow + nAO;
+  const SecondaryJobs jn = secondary_jobs(p, wb, nh);
+  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux;
   const unsigned int threshold = (unsigned int)wb.orbit_refill;
   const int minN = p.f.minN;
   Counters cnt{0, 0, 0, 0};
@@ -1119,7 +1316,7 @@ __device__ __forceinline__ void secondary_lean(const ParamsT<float> &p, const Fr
       if (need) {
         if (stop || job >= njobs) {
           exhausted = true;
-        } else if (secondary_begin(p, wb, cams, ncams, nh, nShadow, job, s)) {
+        } else if (secondary_begin(p, wb, cams, ncams, nh, jn, job, s)) {
           active = true;
           orb.start(ray_at(s.point, s.dir, s.r), s.fpar);
           orbiting = true;
@@ -1201,9 +1398,8 @@ __global__ void __launch_bounds__(128) secondary_pair_kernel(const __grid_consta
                                                              const int ncams) {
   static_assert(FORMULA == 8, "the packed orbit is the lean Mandelbox's");
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
-  const unsigned int nShadow = p.shadow ? nh : 0u;
-  const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
-  const unsigned int njobs = nShadow + nAO;
+  const SecondaryJobs jn = secondary_jobs(p, wb, nh);
+  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux;
   const unsigned int lane = threadIdx.x & 31u;
   const int N = p.f.N, minN = p.f.minN;
   Counters cnt{0, 0, 0, 0};
@@ -1226,11 +1422,11 @@ __global__ void __launch_bounds__(128) secondary_pair_kernel(const __grid_consta
       const unsigned int job1 = base + (unsigned int)__popc(m0) + (unsigned int)__popc(m1 & below);
       if (need0) {
         if (stop || job0 >= njobs) exhausted = true;
-        else act0 = secondary_begin(p, wb, cams, ncams, nh, nShadow, job0, s0);
+        else act0 = secondary_begin(p, wb, cams, ncams, nh, jn, job0, s0);
       }
       if (need1) {
         if (stop || job1 >= njobs) exhausted = true;
-        else act1 = secondary_begin(p, wb, cams, ncams, nh, nShadow, job1, s1);
+        else act1 = secondary_begin(p, wb, cams, ncams, nh, jn, job1, s1);
       }
     }
     if (!__any_sync(0xffffffffu, act0 || act1)) {
@@ -1270,19 +1466,18 @@ __global__ void __launch_bounds__(128) secondary_pair_kernel(const __grid_consta
   }
 }
 
-template <typename T, int FORMULA, bool FAST>
+template <typename T, int FORMULA, bool FAST, bool EFX = false>
 __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                         const FrameCam<T> *__restrict__ cams, const int ncams) {
-  if constexpr (FAST && sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
+  if constexpr (FAST && !EFX && sizeof(T) == 4 && (FORMULA == 8 || FORMULA == 2)) {
     if (wb.orbit_refill > 0) {
       secondary_lean<FORMULA>(p, io, wb, cams, ncams);
       return;
     }
   }
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
-  const unsigned int nShadow = p.shadow ? nh : 0u;
-  const unsigned int nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
-  const unsigned int njobs = nShadow + nAO;
+  const SecondaryJobs jn = secondary_jobs<T, EFX>(p, wb, nh);
+  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux;
   Counters cnt{0, 0, 0, 0};
   bool active = false, exhausted = false;
   SecondaryRay<T> s{};
@@ -1297,7 +1492,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       const unsigned int job = claim_jobs(wb.ctl + 2, need);
       if (need) {
         if (stop || job >= njobs) exhausted = true;
-        else active = secondary_begin(p, wb, cams, ncams, nh, nShadow, job, s);
+        else active = secondary_begin<T, EFX>(p, wb, cams, ncams, nh, jn, job, s);
       }
     }
     if (!__any_sync(0xffffffffu, active)) {
@@ -1309,7 +1504,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       int L;
       bool mi;
       const T dist = wave_distance<T, FORMULA, FAST>(p.f, point2, s.detail, p.f.N, p.f.minN, false, L, mi, cnt, s.fpar);
-      if (secondary_step(p, wb, s, dist, mi)) active = false;
+      if (secondary_step<T, EFX>(p, wb, s, dist, mi)) active = false;
     }
   }
   for (int off = 16; off > 0; off >>= 1) {
@@ -1326,18 +1521,20 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
 // holds the records from kChunk * (nchunks - 1) on.
 template <typename T>
 struct PoolRecords {
-  const T *rec;            // [chunk * kChunk + r][4]: dist, thr, step, unused
+  const T *rec;            // [chunk * kChunk + r][4]: dist, thr, step, scan
   const int32_t *prev;
   int32_t last;      // chunk holding the last written record
   int lastRec;       // index of the last written record: buffCount for a hit (its hit step
                      // writes distance and threshold), buffCount - 1 otherwise
 };
 
-// VolumetricShader (src/shaders.cpp:185-478; glow, post fog, volumetric fog) reading the
-// pooled records far to near; same arithmetic as `volumetric` in render_core.cuh.
-template <typename T>
+// VolumetricShader (src/shaders.cpp:185-478; glow, visible aux lights, post fog, volumetric
+// fog) reading the pooled records far to near; same arithmetic as `volumetric` in
+// render_core.cuh.
+template <typename T, bool EFX>
 __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolRecords<T> &pr, const int stepCount,
-                                                const T depth, T out[4], float &totalOpacityOut, bool &opacitySet) {
+                                                const T depth, const V3<T> rayStart, const V3<T> view, T out[4],
+                                                float &totalOpacityOut, bool &opacitySet) {
   float totalOpacity = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
   T glowN = T(1) - glow;
@@ -1366,6 +1563,8 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
     out[1] = glowOpacity * glowG + (T(1) - glowOpacity) * out[1];
     out[2] = glowOpacity * glowB + (T(1) - glowOpacity) * out[2];
     out[3] += glowOpacity;
+    if (EFX && p.auxLightVisibility > T(0) && p.numberOfLights > 0)
+      visible_aux_lights<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), view, step, out);
     if (p.postFog) {
       T fogDensity = step / p.fogVisibility;
       if (fogDensity > T(1)) fogDensity = T(1);
@@ -1463,11 +1662,46 @@ __device__ __forceinline__ void slow_normal_warp(const ParamsT<T> &p, const Wave
 }
 
 // ---------------------------------------------------------------------------
+// Auxiliary lights at a hit (AuxLightsShader, src/shaders.cpp:997-1067), each weighed by its
+// AuxShadow from the shadow stage, added to ObjectShader's terms as src/shaders.cpp:98-107 does
+// (no fake lights on this engine: their terms are 0).
+template <typename T>
+__device__ __forceinline__ void aux_light_sums(const ParamsT<T> &p, const WaveBufs<T> &wb, const int64_t ri,
+                                            const V3<T> point, const V3<T> nrm, const V3<T> viewT,
+                                            const V3<T> colour, const T specT, const T shadow, T obj[3],
+                                            T spec[3]) {
+  T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
+  const int number = p.numberOfLights;
+  for (int i = 0; i < number; i++) {
+    const LightT<T> L = p.lights[i];
+    if (!(i < p.auxLightNumber || L.enabled)) continue;
+    const AuxTerms<T> a = aux_light_terms(p, L, number, point, nrm, viewT);
+    T sh1 = a.shade, sh2 = a.shade2;
+    if ((sh1 > T(0.01) || sh2 > T(0.01)) && p.shadow) {
+      const T light = wb.auxsh[(int64_t)i * wb.npix + ri];
+      sh1 *= light;
+      sh2 *= light;
+    } else if (p.shadow) {
+      sh1 = T(0);
+      sh2 = T(0);
+    }
+    for (int k = 0; k < 3; k++) {
+      aux[k] += sh1 * T(L.colour[k]) / T(65536);
+      auxSpec[k] += sh2 * T(L.colour[k]) / T(65536);
+    }
+  }
+  const T col[3] = {colour.x, colour.y, colour.z};
+  for (int k = 0; k < 3; k++) {
+    obj[k] += (aux[k] + T(0)) * col[k];
+    spec[k] = auxSpec[k] + T(0) + p.mainLight[k] * specT * shadow;
+  }
+}
+
 // ObjectShader (src/shaders.cpp:21-112) at the hit of ray `ri` from the stages' results: the
 // normal (or the slow shading's, when `slowSum` is given), main light with its shadow and
 // specular term, surface colour, AO and environment mapping. Writes the object and specular
 // terms as the reflection loop combines them (src/Render3D.cpp:541-552) and the colour.
-template <typename T, int FORMULA, bool FAST>
+template <typename T, int FORMULA, bool FAST, bool EFX>
 __device__ __forceinline__ void shade_hit(const ParamsT<T> &p, const FrameCam<T> &c, const WaveBufs<T> &wb,
                                           const int64_t ri, const uint8_t flags, const V3<T> viewT,
                                           const V3<double> viewD, const V3<T> *slowSum, Counters &cnt, T obj[3],
@@ -1481,6 +1715,8 @@ __device__ __forceinline__ void shade_hit(const ParamsT<T> &p, const FrameCam<T>
     nrm = *slowSum;
     if (nrm.x == T(0) && nrm.y == T(0) && nrm.z == T(0)) nrm.x = T(1);
     else nrm = normalize3(nrm);
+  } else if (EFX && wb.normal) {   // computed by the normal stage (auxiliary lights)
+    nrm = {wb.normal[ri], wb.normal[wb.npix + ri], wb.normal[2 * wb.npix + ri]};
   } else {
     nrm = calc_normal_fp<T, FORMULA, FAST>(p, h.point, h.delta, h.thr, h.thr, cnt, c.fparam);
   }
@@ -1520,15 +1756,19 @@ __device__ __forceinline__ void shade_hit(const ParamsT<T> &p, const FrameCam<T>
   obj[0] = env * ambient.x + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
   obj[1] = env * ambient.y + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
   obj[2] = env * ambient.z + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
-  // no auxiliary or fake lights on this engine: their specular terms are the reference's zeros
-  for (int k = 0; k < 3; k++) spec[k] = T(0) + p.mainLight[k] * specT * shadow;
+  if (EFX && p.numberOfLights > 0) {
+    aux_light_sums(p, wb, ri, h.point, nrm, viewT, colour, specT, shadow, obj, spec);
+  } else {
+    // no auxiliary or fake lights: their specular terms are the reference's zeros
+    for (int k = 0; k < 3; k++) spec[k] = T(0) + p.mainLight[k] * specT * shadow;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Stage 4: per-pixel composition and the cImage writes (src/Render3D.cpp:501-589),
 // over every pixel of the batch.
 // ---------------------------------------------------------------------------
-template <typename T, int FORMULA, bool FAST, bool REFL = false>
+template <typename T, int FORMULA, bool FAST, bool EFX = false>
 __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compose_kernel(const __grid_constant__ ParamsT<T> p, const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   Counters cnt{0, 0, 0, 0};
@@ -1560,7 +1800,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
     // the reflection loop (src/Render3D.cpp:441-499): ray d + 1 was marched when ray d hit an
     // object that reflects; the last ray marched closes the loop
     int rayEnd = 0;
-    for (int d = 0; d + 1 < (REFL ? wb.rays : 1); d++) {
+    for (int d = 0; d + 1 < (EFX ? wb.rays : 1); d++) {
       const uint8_t f = wb.flags[(int64_t)d * wb.npix_frame + gp];
       if (!(f & 1)) break;
       const int ot = (f >> 4) & 7;
@@ -1588,7 +1828,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
       T reflect = T(0);
       if (hit) {
         V3<T> colour;
-        shade_hit<T, FORMULA, FAST>(p, c, wb, ri, flags, viewT, viewD, (p.slowShading && d == 0) ? &slowSum : nullptr,
+        shade_hit<T, FORMULA, FAST, EFX>(p, c, wb, ri, flags, viewT, viewD, (p.slowShading && d == 0) ? &slowSum : nullptr,
                                     cnt, obj, spec, colour);
         if (d == 0) objColour = colour;
         const int ot = (flags >> 4) & 7;
@@ -1621,7 +1861,10 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
         if (p.needVolumetric) {
           const int count = wb.count[ri];
           const PoolRecords<T> pr{wb.pool_rec, wb.pool_prev, wb.last_chunk[ri], hit ? count : count - 1};
-          volumetric_pool<T>(p, pr, count, wb.scan[ri], res, totalOpacity, set);
+          const V3<T> rayStart = d == 0 ? V3<T>{(T)c.start[0], (T)c.start[1], (T)c.start[2]}
+                                        : V3<T>{(T)wb.ray_start[ri], (T)wb.ray_start[wb.npix + ri],
+                                                (T)wb.ray_start[2 * wb.npix + ri]};
+          volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, res, totalOpacity, set);
         }
         result[0] = res[0];
         result[1] = res[1];

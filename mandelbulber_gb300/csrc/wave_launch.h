@@ -24,6 +24,9 @@ struct WaveBufs {
   T *vol;                // [6][npix] overflow pass only: A, B.r, B.g, B.b, alpha, opacity
   T *shadow;             // [npix]
   T *ao;                 // [aoCount][npix] per-direction shadowTemp
+  T *normal;             // [3][npix] hit normals (auxiliary lights: null without them)
+  T *auxsh;              // [numberOfLights][npix] AuxShadow of each auxiliary light at each hit
+                         // (null without aux lights or shadows)
   uint32_t *hit_list;    // [npix] hits (secondary rays)
   uint32_t *polish_list; // [npix] hits the FP64 polish re-evaluates
   uint32_t *ctl;         // [0] primary jobs, [1] hits, [2] secondary jobs, [3] overflow count,
@@ -34,7 +37,7 @@ struct WaveBufs {
   uint32_t *overflow_list;
   // Step records of the primary rays: chunks of kChunk records linked backwards
   // (prev), allocated by bump counter; the pixel keeps its last chunk.
-  T *pool_rec;                           // [chunk * kChunk + r][4]: dist, thr, step, unused
+  T *pool_rec;                           // [chunk * kChunk + r][4]: dist, thr, step, scan
                                          // (one 16- or 32-byte record: one store, one load)
   int32_t *pool_prev;                    // [chunk]
   int32_t *last_chunk;                   // [npix], -1 = no records

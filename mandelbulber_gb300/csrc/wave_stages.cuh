@@ -13,6 +13,9 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   auto mark = [&](int k) {
     if (L.ev[0]) cudaEventRecord(L.ev[k], s);
   };
+  // the effects variant of the primary, shadow and composition stages: reflected rays or
+  // auxiliary lights
+  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0;
   mark(0);
   // one primary pass (and FP64 polish) per ray depth of the reflection loop; between two
   // depths the reflect stage spawns the next depth's rays from this depth's hits
@@ -25,7 +28,7 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
       dev::reflect_kernel<T, F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 0), wbp, L.cams, L.ncams);
       dev::next_depth_kernel<T><<<1, 1, 0, s>>>(L.wb.ctl);
     }
-    if (L.wb.rays > 1) {
+    if (efx) {
       dev::primary_kernel<T, F, FAST, true><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), wbd, L.cams,
                                                                         L.ncams);
       if (L.overflow)
@@ -47,17 +50,25 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   if (L.wb.exact_hit)
     dev::level_set_kernel<T, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
   mark(3);
+  // auxiliary lights: the hit normals, which the AuxShadow jobs test (counted with composition)
+  if (L.wb.normal)
+    dev::normal_kernel<T, F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
   bool pair = false;
-  if constexpr (sizeof(T) == 4 && F == 8 && FAST) pair = L.wb.pair_rays && L.wb.orbit_refill <= 0;
+  if constexpr (sizeof(T) == 4 && F == 8 && FAST) pair = L.wb.pair_rays && L.wb.orbit_refill <= 0 && !efx;
   if constexpr (sizeof(T) == 4 && F == 8 && FAST) {
     if (pair) dev::secondary_pair_kernel<8><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
   }
-  if (!pair)
-    dev::secondary_kernel<T, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
+  if (!pair) {
+    if (efx)
+      dev::secondary_kernel<T, F, FAST, true><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams,
+                                                                          L.ncams);
+    else
+      dev::secondary_kernel<T, F, FAST><<<L.grid2, L.block, 0, s>>>(L.p, stage_io(L.io, 2), L.wb, L.cams, L.ncams);
+  }
   mark(4);
   // slow shading: one warp's 11^3 normal samples in dynamic shared memory per warp
   const size_t composeSmem = L.p.slowShading ? (size_t)(L.block / 32) * dev::kSlowSamples * sizeof(T) : 0;
-  if (L.wb.rays > 1)
+  if (efx)
     dev::compose_kernel<T, F, FAST, true><<<L.compose_grid, L.block, composeSmem, s>>>(L.p, stage_io(L.io, 3), L.wb,
                                                                                      L.cams, L.ncams);
   else

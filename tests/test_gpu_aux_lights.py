@@ -1,0 +1,94 @@
+"""Auxiliary lights on the wavefront engine (needs a GPU).
+
+AuxLightsShader (src/shaders.cpp:997-1067) lights every hit with each auxiliary light's
+Lambert and Blinn terms, shadowed by AuxShadow (src/shaders.cpp:1069-1132) when either term
+passes 0.01; VolumetricShader adds the visible lights' glow along the ray
+(src/shaders.cpp:242-296). On the wavefront a normal stage computes the hit normals, the
+shadow stage runs one AuxShadow job per enabled light and hit, and the composition stage sums
+the lights in the reference's order. Checks:
+  * every aux-light fixture in FP64 on the wavefront equals the per-pixel engine on hit,
+    iterations and depth, float image within 60 dB, and takes the wavefront's stages;
+  * the Mandelbox fixtures in FP64 at larger sizes equal the oracle bit for bit;
+  * the FP32 + FP64-fix policy against the oracle: hit mismatch <= 0.5 %, >= 99 % of the
+    pixels within 0.01 (the effect scenes' bar).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import mandelbulber_gb300 as mb
+from tests import metrics, oracle_lib
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+EXACT = ["hit", "iters", "depth", "zbuffer", "alpha", "opacity", "colour"]
+
+
+def _scene(case, w=None, h=None):
+    z = np.load(os.path.join(GOLDEN, f"render_{case}.npz"))
+    sc = mb.scene_from_bytes(z["scene"].tobytes())
+    if w:
+        sc.image_width, sc.image_height = w, h
+        sc.resolution = 1.0 / w / sc.noOfTiles
+    return sc
+
+
+def _uses_aux(sc) -> bool:
+    return sc.auxLightNumber > 0 or any(sc.auxLightPreEnabled[i] for i in range(4))
+
+
+def _on_wavefront(sc) -> bool:
+    return _uses_aux(sc) and not (sc.fakeLightsEnabled or sc.volumetricLightEnabledAny or sc.iterFogEnabled
+                                  or sc.slowShading or (sc.raytracedReflections and sc.limits_enabled))
+
+
+AUX_CASES = sorted(c for c in (os.path.basename(p)[7:-4] for p in glob.glob(os.path.join(GOLDEN, "render_*.npz")))
+                   if _on_wavefront(_scene(c)))
+
+
+def test_aux_fixtures_reach_the_wavefront():
+    assert len(AUX_CASES) >= 6, AUX_CASES
+
+
+@pytest.mark.parametrize("case", AUX_CASES)
+def test_wavefront_aux_lights_equal_the_per_pixel_engine_in_fp64(gpu_ctx, case):
+    sc = _scene(case)
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=mb.ENGINE_WAVEFRONT)
+    wave_launches = gpu_ctx.stats().launches
+    b = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=mb.ENGINE_PER_PIXEL)
+    for k in ["hit", "iters", "depth"]:
+        np.testing.assert_array_equal(getattr(a, k), getattr(b, k), err_msg=f"{case}: {k}")
+    m = metrics.compare(a, b)
+    print(case, "wavefront vs per-pixel", m, "launches", wave_launches)
+    assert m["psnr_float"] >= 60.0, m
+    # primary, normal, shadow and composition stages at least
+    assert wave_launches >= 4, wave_launches
+
+
+@pytest.mark.parametrize("case,w,h", [("ex_aux_coloured_lights", 128, 96), ("aux_predefined_penetrating", 128, 96),
+                                      ("ex_aux_rotated_mandelbox_4", 128, 96)])
+def test_mandelbox_aux_lights_fp64_equal_the_oracle(gpu_ctx, oracle, case, w, h):
+    sc = _scene(case, w, h)
+    assert _on_wavefront(sc) and sc.formula == 8
+    ref, _ = oracle_lib.render(oracle, sc)
+    img = gpu_ctx.render(sc, precision=mb.PREC_FP64, engine=mb.ENGINE_WAVEFRONT)
+    for k in EXACT:
+        np.testing.assert_array_equal(getattr(img, k), getattr(ref, k), err_msg=f"{case}: {k}")
+    np.testing.assert_allclose(img.image_float, ref.image_float, rtol=0, atol=1e-6)
+
+
+@pytest.mark.parametrize("case,w,h", [("ex_aux_coloured_lights", 192, 108), ("aux_random_visible", 160, 120),
+                                      ("ex_aux_menger_predefined", 160, 120), ("ex_aux_backlight", 128, 96),
+                                      ("aux_no_shadows", 128, 96)])
+def test_fp32_aux_lights_against_the_oracle(gpu_ctx, oracle, case, w, h):
+    sc = _scene(case, w, h)
+    assert _on_wavefront(sc)
+    ref, _ = oracle_lib.render(oracle, sc)
+    a = gpu_ctx.render(sc, precision=mb.PREC_FP32_FIX, engine=mb.ENGINE_WAVEFRONT)
+    m = metrics.compare(a, ref)
+    close = float(np.mean(np.abs(a.image_float.astype(np.float64) - ref.image_float).max(-1) <= 0.01))
+    print(case, "fp32 wavefront vs oracle", m, "within 0.01", close)
+    assert m["hit_mismatch"] <= 0.005, m
+    assert close >= 0.99, close
