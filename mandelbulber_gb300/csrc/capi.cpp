@@ -236,8 +236,8 @@ static int aux_light_count(const mbgb_scene &s) {
   return uses_aux_lights(s) ? std::max(s.auxLightNumber > 0 ? s.auxLightNumber : 0, 4) : 0;
 }
 
-// Features that the per-pixel engine renders and the wavefront stages do not carry (fake and
-// volumetric lights, iteration fog): scenes that use them render on the per-pixel engine.
+// Features that the per-pixel engine renders and the wavefront stages do not carry (fake
+// lights, iteration fog): scenes that use them render on the per-pixel engine.
 // Slow shading, environment mapping and primitive objects are composition-stage work the
 // wavefront carries; ray-traced reflections are further primary passes, one per depth, except
 // with slow shading (whose warp-wide normals serve the camera rays only) or the limit box
@@ -246,7 +246,12 @@ static int aux_light_count(const mbgb_scene &s) {
 // composition, except with slow shading (the jobs need the normals first) or when one shadow
 // factor per light and ray would pass 4 GB.
 static bool per_pixel_only(const mbgb_scene &s) {
-  if (s.fakeLightsEnabled || s.volumetricLightEnabledAny || s.iterFogEnabled) return true;
+  if (s.fakeLightsEnabled || s.iterFogEnabled) return true;
+  // volumetric lights: samples of the volumetric walk; the shadows they trace take the
+  // detailSize of their start (src/fractal.cpp:1291-1293), which the distance post-processing
+  // of limits, iteration threshold and interior mode reads as well
+  if (s.volumetricLightEnabledAny && (s.limits_enabled || s.iterThresh || s.interiorMode || s.slowShading))
+    return true;
   if (reflection_rays(s) > 1 && (s.slowShading || s.limits_enabled)) return true;
   if (uses_aux_lights(s)) {
     if (s.slowShading) return true;
@@ -1041,7 +1046,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
 struct WaveLayout {
   size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
   size_t prec, pprev;
-  size_t rstart, rdir, rthr, rlist, normal, auxsh;
+  size_t rstart, rdir, rthr, rlist, normal, auxsh, sbase, sray, srec, sres;
   uint32_t poolCap;
   size_t total;
 };
@@ -1049,8 +1054,9 @@ struct WaveLayout {
 // `npixFrame` pixels with `rays` rays each (the reflection loop's depths): every per-ray array
 // holds rays x npixFrame entries.
 // `auxN` auxiliary lights: hit normals, and with `auxShadows` one AuxShadow factor per light.
+// `volLights`: the volumetric walk's samples (at most one per pool record) and their shadows.
 static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVol, int rays, int auxN,
-                              bool auxShadows) {
+                              bool auxShadows, bool volLights) {
   const int64_t npix = npixFrame * rays;
   WaveLayout w{};
   size_t off = 0;
@@ -1091,6 +1097,11 @@ static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVo
   w.rlist = take((rays > 1 ? (size_t)npixFrame : 0) * 4);
   w.normal = take(auxN > 0 ? 3 * (size_t)npix * ts : 0);
   w.auxsh = take(auxN > 0 && auxShadows ? (size_t)auxN * npix * ts : 0);
+  const size_t samples = volLights && needVol ? (size_t)w.poolCap * kChunk : 0;
+  w.sbase = take(volLights ? (size_t)npix * 4 : 0);
+  w.sray = take(samples * 4);
+  w.srec = take(samples * 4);
+  w.sres = take(samples * kSampleResults * ts);
   w.total = off;
   return w;
 }
@@ -1114,7 +1125,8 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   const int aoN = rayAO ? c->ao_count : 0;
   const int rays = reflection_rays(scene);
   const int auxN = aux_light_count(scene);
-  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays, auxN, scene.shadow != 0);
+  const bool volLights = scene.volumetricLightEnabledAny != 0;
+  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays, auxN, scene.shadow != 0, volLights);
   char *base = (char *)c->wave[prec].ptr;
   WaveLaunch<T> L;
   WaveBufs<T> &wb = L.wb;
@@ -1153,6 +1165,11 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.ray_list = (uint32_t *)(base + w.rlist);
   wb.normal = auxN > 0 ? (T *)(base + w.normal) : nullptr;
   wb.auxsh = auxN > 0 && scene.shadow ? (T *)(base + w.auxsh) : nullptr;
+  wb.sample_base = volLights ? (uint32_t *)(base + w.sbase) : nullptr;
+  wb.sample_ray = volLights && needVol ? (uint32_t *)(base + w.sray) : nullptr;
+  wb.sample_rec = volLights && needVol ? (int32_t *)(base + w.srec) : nullptr;
+  wb.sample_res = volLights && needVol ? (T *)(base + w.sres) : nullptr;
+  wb.sample_cap = volLights && needVol ? w.poolCap * (uint32_t)kChunk : 0u;
   // shadow/AO rays two per thread (secondary_pair_kernel): the lean FP32 Mandelbox with
   // per-estimate refill, which the pair kernel's packed orbit serves
   wb.pair_rays = (sizeof(T) == 4 && fast_mandelbox(scene) && g.cfg.pairRays && g.cfg.orbitRefill <= 0) ? 1 : 0;
@@ -1207,7 +1224,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   // per ray depth: primary (+ overflow) pass and polish; per further depth the reflect and
   // counter kernels
   *launches += 2 + (int64_t)rays * (1 + (needVol ? 1 : 0) + (prec == 1 ? 1 : 0)) + 2 * (int64_t)(rays - 1) +
-               (wb.normal ? 1 : 0) + (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
+               (wb.normal ? 1 : 0) + (wb.sample_ray ? 1 : 0) + (wb.exact_hit ? 1 : 0) + (grad ? 1 : 0);
   return MBGB_OK;
 }
 
@@ -1615,13 +1632,14 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     if (!wave && (grad || o.exact_hit))
       return set_error(MBGB_ERR_BAD_PARAM, "exact hits and gradients need the wavefront engine and frames below 4e9 rays");
     Group *g = nullptr;
-    // a frame with auxiliary lights keeps its own group: its lights are placed for it
-    if (wave && !uses_aux_lights(sc)) {
+    // a frame with auxiliary lights keeps its own group (its lights are placed for it), and so
+    // does one with volumetric lights (the long rays' fold reads the scene's own parameters)
+    if (wave && !uses_aux_lights(sc) && !sc.volumetricLightEnabledAny) {
       for (auto &h : plan.groups) {
         if (!h.wave || h.prec != prec[i]) continue;
         if ((double)std::max(h.npix + fpix, h.jobs + fjobs) * perPix >= kMaxGroupJobs) continue;
         const mbgb_scene &rep = scenes[h.frames[0]];
-        if (uses_aux_lights(rep)) continue;
+        if (uses_aux_lights(rep) || rep.volumetricLightEnabledAny) continue;
         const bool same = prec[i] == 0 ? same_shared<double>(rep, sc, o) : same_shared<float>(rep, sc, o);
         if (!same) continue;
         const LaunchCfg &hc = h.cfg;
@@ -1667,7 +1685,8 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       const size_t ts = g.prec == 0 ? sizeof(double) : sizeof(float);
       wave_bytes[g.prec] =
           std::max(wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol, reflection_rays(rep),
-                                                   aux_light_count(rep), rep.shadow != 0)
+                                                   aux_light_count(rep), rep.shadow != 0,
+                                                   rep.volumetricLightEnabledAny != 0)
                                            .total);
       g.cams_off = camsBytes;
       const size_t cs = g.prec == 0 ? sizeof(FrameCam<double>) : sizeof(FrameCam<float>);

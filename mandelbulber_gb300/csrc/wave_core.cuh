@@ -303,6 +303,17 @@ __device__ __forceinline__ void load_record(const double *r, double &dist, doubl
 __device__ __forceinline__ float record_scan(const float *r) { return r[3]; }
 __device__ __forceinline__ double record_scan(const double *r) { return r[3]; }
 
+// Backward walk over a ray's pooled records: record `index` of a chain whose last chunk
+// holds the records from kChunk * (nchunks - 1) on.
+template <typename T>
+struct PoolRecords {
+  const T *rec;            // [chunk * kChunk + r][4]: dist, thr, step, scan
+  const int32_t *prev;
+  int32_t last;      // chunk holding the last written record
+  int lastRec;       // index of the last written record: buffCount for a hit (its hit step
+                     // writes distance and threshold), buffCount - 1 otherwise
+};
+
 // Frame of a primary job / of a pixel of the batch (binary search over the frame table).
 template <typename T>
 __device__ __forceinline__ int frame_of_job(const FrameCam<T> *__restrict__ cams, const int n, const unsigned int job) {
@@ -450,13 +461,53 @@ __device__ __forceinline__ void visible_aux_lights(const ParamsT<T> &p, const V3
   }
 }
 
+// Volumetric lights at one step group (VolumetricShader, src/shaders.cpp:309-343) from the
+// group's MainShadow (`sh`, main light, volumetric light 0) and the predefined aux lights'
+// AuxShadow (`aux[i]`, volumetric lights 1-4); adds to out[0..3] in the reference's order.
+template <typename T>
+__device__ __forceinline__ void volumetric_light_terms(const ParamsT<T> &p, const V3<T> point, const T step,
+                                                       const T sh, const T aux[4], T out[4]) {
+  for (int i = 0; i < 5; i++) {
+    if (i == 0 && p.volLightEnabled[0]) {
+      out[0] += sh * step * p.volLightIntensity[0] * T(p.mainLightColour[0]) / T(65536);
+      out[1] += sh * step * p.volLightIntensity[0] * T(p.mainLightColour[1]) / T(65536);
+      out[2] += sh * step * p.volLightIntensity[0] * T(p.mainLightColour[2]) / T(65536);
+      out[3] += (sh + sh + sh) / T(3) * step * p.volLightIntensity[0];
+    }
+    if (i > 0 && p.numberOfLights > 0 && p.lights[i - 1].enabled && p.volLightEnabled[i]) {
+      const LightT<T> L = p.lights[i - 1];
+      const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - point;
+      const T distance = length3(d);
+      const T distance2 = distance * distance;
+      const T light = aux[i - 1];
+      out[0] += light * T(L.colour[0]) / T(65536) * p.volLightIntensity[i] * step / distance2;
+      out[1] += light * T(L.colour[1]) / T(65536) * p.volLightIntensity[i] * step / distance2;
+      out[2] += light * T(L.colour[2]) / T(65536) * p.volLightIntensity[i] * step / distance2;
+      out[3] += light * p.volLightIntensity[i] * step / distance2;
+    }
+  }
+}
+
+// The results of the shadow stage for the volumetric walk of one ray: sample `base + k` is
+// the walk's k-th step group.
+template <typename T>
+struct VolSamples {
+  const T *res;    // [kSampleResults][cap]
+  uint32_t cap, base;
+};
+
 // The volumetric pass over one ray's records (VolumetricShader's glow, post fog and
 // volumetric fog, src/shaders.cpp:185-478) as the affine map out = A*base + B, plus
 // the alpha and opacity it leaves for a base alpha of `alpha0`.
-template <typename T, bool EFX>
+// Effects variant: the visible aux lights and the volumetric lights, whose MainShadow and
+// AuxShadow (render_core.cuh's, with the ray's `delta` and the camera `eye`) run here in line.
+template <typename T, bool EFX, int FORMULA>
 __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
                                                   const T depth, const T alpha0, const V3<T> rayStart,
-                                                  const V3<T> view, T vol[6]) {
+                                                  const V3<T> view, const T delta, const V3<T> eye,
+                                                  const FrameIO &io, Counters &cnt, T vol[6]) {
+  T detail = T(0);
+  int itersOut = 0;
   T A = T(1), B0 = T(0), B1 = T(0), B2 = T(0), alpha = alpha0;
   float totalOpacity = 0.0f, opacityOut = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
@@ -484,6 +535,26 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
       // the visible lights add to the colour: the map's offset
       T add[4] = {B0, B1, B2, alpha};
       visible_aux_lights<T>(p, rayStart + view * sb.scan[sb.at(index)], view, step, add);
+      B0 = add[0];
+      B1 = add[1];
+      B2 = add[2];
+      alpha = add[3];
+    }
+    if (EFX && p.volLightAny && sb.scan) {
+      const V3<T> point = rayStart + view * sb.scan[sb.at(index)];
+      const T thrStep = sb.thr[sb.at(index)];
+      T sh = T(1), aux[4] = {T(1), T(1), T(1), T(1)};
+      if (p.volLightEnabled[0]) sh = main_shadow<T, FORMULA>(p, point, thrStep, delta, eye, detail, itersOut, io, cnt);
+      for (int j = 0; j < 4; j++) {
+        if (p.numberOfLights > 0 && p.lights[j].enabled && p.volLightEnabled[j + 1]) {
+          const LightT<T> L = p.lights[j];
+          const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - point;
+          aux[j] = aux_shadow<T, FORMULA>(p, point, length3(d), normalize3(d), delta, thrStep, eye, detail, itersOut,
+                                          cnt);
+        }
+      }
+      T add[4] = {B0, B1, B2, alpha};
+      volumetric_light_terms<T>(p, point, step, sh, aux, add);
       B0 = add[0];
       B1 = add[1];
       B2 = add[2];
@@ -538,9 +609,11 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
 // ---------------------------------------------------------------------------
 // Stage 1: primary rays with lane refill, over every frame of the batch.
 // ---------------------------------------------------------------------------
-// EFX: the effects variant (reflected rays, WaveBufs::rays > 1, or auxiliary lights); the
-// plain variant holds neither's state.
-template <typename T, int FORMULA, bool FAST, bool EFX = false>
+// EFX: the effects variant (reflected rays, WaveBufs::rays > 1, auxiliary or volumetric
+// lights); the plain variant holds none of their state.
+// OVF (effects variant): the overflow pass's instantiation, whose fold of a long ray's records
+// traces the volumetric lights' shadows in line; the main pass's holds no fold.
+template <typename T, int FORMULA, bool FAST, bool EFX = false, bool OVF = false>
 __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary_kernel(const __grid_constant__ ParamsT<T> p, const __grid_constant__ FractalT<double> fd,
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
@@ -740,10 +813,15 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
         const bool found = phase == 1;
         // bits 4-6: the object the last distance estimate ended on (primitives; 0 = fractal)
         uint8_t flags = (uint8_t)((found ? 1 : 0) | ((cnt.objectOut & 7) << 4));
-        if (io.overflow_pass && useSB) {
+        if ((!EFX || OVF) && io.overflow_pass && useSB) {
           // rare long rays: fold the records now (the slot is reused); compose applies the map
           T vol[6] = {T(1), T(0), T(0), T(0), found ? T(1) : T(0), T(0)};
-          volumetric_affine<T, EFX>(p, sb, buffCount, scan, found ? T(1) : T(0), start, dir, vol);
+          const T rayDelta = p.constantDEThreshold ? scan * res * persp : thr * p.quality;
+          volumetric_affine<T, EFX, FORMULA>(p, sb, buffCount, scan, found ? T(1) : T(0), start, dir, rayDelta,
+                                             V3<T>{(T)cams[frame_of_pixel(cams, ncams, gp)].start[0],
+                                                   (T)cams[frame_of_pixel(cams, ncams, gp)].start[1],
+                                                   (T)cams[frame_of_pixel(cams, ncams, gp)].start[2]},
+                                             io, cnt, vol);
           for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + ri] = vol[c];
           flags |= 4;
         }
@@ -1038,6 +1116,67 @@ __global__ void __launch_bounds__(128) normal_kernel(const __grid_constant__ Par
   }
 }
 
+// Volumetric lights: the step groups of every ray that the volumetric walk visits (records
+// summed far to near until the sum reaches thr x quality, src/shaders.cpp:198-205), each
+// ray's samples contiguous and in the walk's order. One thread per pixel walks the rays the
+// reflection loop marched; long rays of the overflow pass fold theirs in that pass.
+template <typename T, typename F>
+__device__ __forceinline__ void walk_groups(const ParamsT<T> &p, const PoolRecords<T> &pr, const int stepCount, F fn) {
+  T totalStep = T(0);
+  int32_t chunk = pr.last;
+  int chunkBase = (pr.lastRec / kChunk) * kChunk;
+  for (int index = stepCount - 1; index > 0; index--) {
+    while (index < chunkBase) {
+      chunk = pr.prev[chunk];
+      chunkBase -= kChunk;
+    }
+    const int64_t rec = (int64_t)chunk * kChunk + (index - chunkBase);
+    T distance, dist_thresh, step;
+    load_record(pr.rec + 4 * rec, distance, dist_thresh, step);
+    totalStep += step;
+    if (totalStep < dist_thresh * p.quality) continue;
+    totalStep = T(0);
+    fn(rec);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ ParamsT<T> p, const WaveBufs<T> wb,
+                                                     const FrameCam<T> *__restrict__ cams, const int ncams) {
+  for (int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gp < wb.npix_frame;
+       gp += (int64_t)gridDim.x * blockDim.x) {
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
+    const int64_t pix = gp - c.pixBase;
+    const int y = (int)(pix / c.width);
+    if (y < c.row_begin || y >= c.row_end) continue;
+    int rayEnd = 0;
+    for (int d = 0; d + 1 < wb.rays; d++) {
+      const uint8_t f = wb.flags[(int64_t)d * wb.npix_frame + gp];
+      if (!(f & 1)) break;
+      const int ot = (f >> 4) & 7;
+      if ((ot == kObjFractal ? p.reflect : p.primReflect[ot - 1]) == T(0)) break;
+      rayEnd = d + 1;
+    }
+    for (int d = 0; d <= rayEnd; d++) {
+      const int64_t ri = (int64_t)d * wb.npix_frame + gp;
+      const uint8_t flags = wb.flags[ri];
+      if (flags & 4) continue;
+      const int count = wb.count[ri];
+      const PoolRecords<T> pr{wb.pool_rec, wb.pool_prev, wb.last_chunk[ri], (flags & 1) ? count : count - 1};
+      unsigned int n = 0;
+      walk_groups(p, pr, count, [&](int64_t) { n++; });
+      const unsigned int base = n ? atomicAdd(wb.ctl + 11, n) : 0u;
+      wb.sample_base[ri] = base;
+      unsigned int k = base;
+      walk_groups(p, pr, count, [&](int64_t rec) {
+        wb.sample_ray[k] = (uint32_t)ri;
+        wb.sample_rec[k] = (int32_t)rec;
+        k++;
+      });
+    }
+  }
+}
+
 // Between two reflection depths (one thread): the next depth's rays become the current ones,
 // the per-depth job, overflow and polish counters restart, the hit count so far is kept.
 template <typename T>
@@ -1120,6 +1259,7 @@ __device__ __forceinline__ V3<T> ray_view(const ParamsT<T> &p, const FrameCam<T>
 // (aux lights with shadows) one AuxShadow per enabled light and hit.
 struct SecondaryJobs {
   unsigned int nShadow, nAO, nAux;
+  unsigned int nSamples;   // volumetric-light samples: kSampleResults jobs each
 };
 template <typename T, bool EFX = false>
 __device__ __forceinline__ SecondaryJobs secondary_jobs(const ParamsT<T> &p, const WaveBufs<T> &wb,
@@ -1128,6 +1268,7 @@ __device__ __forceinline__ SecondaryJobs secondary_jobs(const ParamsT<T> &p, con
   j.nShadow = p.shadow ? nh : 0u;
   j.nAO = (p.ao && !p.fastAO) ? nh * (unsigned int)p.aoCount : 0u;
   j.nAux = (EFX && p.shadow && wb.auxsh) ? nh * (unsigned int)p.numberOfLights : 0u;
+  j.nSamples = (EFX && wb.sample_ray) ? *(volatile unsigned int *)&wb.ctl[11] : 0u;
   return j;
 }
 
@@ -1140,6 +1281,12 @@ struct SecondaryRay {
   V3<T> point, dir;
   T r, end, sh, thr, detail, maxSoft, stepMul, fpar;
   int guard;
+  // effects variant: where the result goes, and with iteration fog or volumetric lights the
+  // per-sample threshold of the eye distance (src/shaders.cpp:515-519, 646-650)
+  T *out;
+  V3<T> eye;
+  T res, persp;
+  int fog;
 };
 
 // AuxShadow's set-up (kind 2): it runs for an enabled light whose Lambert or Blinn term passes
@@ -1159,6 +1306,147 @@ __device__ __forceinline__ void aux_shadow_begin(const ParamsT<T> &p, const Wave
   s.r = h.delta;
   s.stepMul = p.DE_factor;
   if (!trace) s.end = T(0);
+}
+
+// Origin and direction of ray `ri` in the march precision (the volumetric walk's rayStart and
+// view): the camera's for depth 0, the reflected ray's otherwise.
+template <typename T>
+__device__ __forceinline__ void ray_origin_view(const ParamsT<T> &p, const FrameCam<T> &c, const WaveBufs<T> &wb,
+                                                const int64_t ri, const int64_t gp, V3<T> &start, V3<T> &view) {
+  if (ri < wb.npix_frame) {
+    start = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
+    const int64_t local = gp - c.pixBase;
+    camera_dir(p, c, (int)(local % c.width), (int)(local / c.width), view);
+  } else {
+    start = {(T)wb.ray_start[ri], (T)wb.ray_start[wb.npix + ri], (T)wb.ray_start[2 * wb.npix + ri]};
+    view = {(T)wb.ray_dir[ri], (T)wb.ray_dir[wb.npix + ri], (T)wb.ray_dir[2 * wb.npix + ri]};
+  }
+}
+
+// The threshold a secondary ray compares against with iteration fog or volumetric lights:
+// the one of the sample's own distance from the eye, held in a float (the per-pixel engine's
+// secondary_thresh, src/shaders.cpp:515-519).
+template <typename T>
+__device__ __forceinline__ T fog_thresh(const ParamsT<T> &p, const V3<T> point2, const V3<T> eye, const T res,
+                                        const T persp) {
+  float t;
+  if (!p.constantDEThreshold) t = (float)(length3(point2 - eye) * res * persp / p.quality);
+  else t = (float)p.quality;
+  return (T)t;
+}
+
+// The effects variant's job set-up: the plain variant's jobs (shadow, AO, AuxShadow at every
+// hit of every depth) and, with volumetric lights, MainShadow and the four predefined lights'
+// AuxShadow from every step group of the volumetric walk (src/shaders.cpp:309-343). With
+// iteration fog or volumetric lights every march steps at DE factor 1 and compares against
+// its samples' eye-distance thresholds (MainShadow, AuxShadow, AmbientOcclusion). detailSize
+// after MainShadow is taken as the float threshold it starts from; CalculateDistance reads it
+// only in the minN clause (src/fractal.cpp:1291-1293), whose escape in the first iteration
+// gives a distance far above any threshold of these scenes.
+template <typename T>
+__device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const WaveBufs<T> &wb,
+                                                    const FrameCam<T> *__restrict__ cams, const int ncams,
+                                                    const unsigned int nh, const SecondaryJobs &jn,
+                                                    const unsigned int job, SecondaryRay<T> &s) {
+  unsigned int q = job;
+  bool sample = false;
+  unsigned int si = 0;
+  if (q < jn.nShadow) {
+    s.kind = 0;
+    s.gp = (int64_t)wb.hit_list[q];
+  } else if ((q -= jn.nShadow) < jn.nAO) {
+    s.kind = 1;
+    s.j = q / nh;
+    s.gp = (int64_t)wb.hit_list[q % nh];
+  } else if ((q -= jn.nAO) < jn.nAux) {
+    s.kind = 2;
+    s.j = q / nh;
+    s.gp = (int64_t)wb.hit_list[q % nh];
+  } else {
+    q -= jn.nAux;
+    sample = true;
+    if (q < jn.nSamples) {
+      s.kind = 0;
+      si = q;
+    } else {
+      q -= jn.nSamples;
+      s.kind = 2;
+      s.j = q / jn.nSamples;
+      si = q % jn.nSamples;
+    }
+    s.gp = (int64_t)wb.sample_ray[si];
+  }
+  const int64_t px = pixel_of_ray(wb, s.gp);
+  const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, px)];
+  const HitInfo<T> h = hit_info(p, c, wb, s.gp);   // the ray's threshold, depth and delta
+  s.fog = (p.iterFog || p.volLightAny) ? 1 : 0;
+  s.eye = {(T)c.start[0], (T)c.start[1], (T)c.start[2]};
+  s.res = c.resolution;
+  s.persp = c.persp;
+  s.fpar = c.fparam;
+  s.sh = T(1);
+  s.maxSoft = T(0);
+  s.guard = 0;
+  const T deF = s.fog ? T(1) : p.DE_factor;
+  const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
+  T distThresh = h.thr;
+  if (sample) {
+    // the group's position and threshold (src/shaders.cpp:309-343)
+    const int64_t rec = (int64_t)wb.sample_rec[si];
+    V3<T> rs, rv;
+    ray_origin_view(p, c, wb, s.gp, px, rs, rv);
+    s.point = rs + rv * record_scan(wb.pool_rec + 4 * rec);
+    T dd, st;
+    load_record(wb.pool_rec + 4 * rec, dd, distThresh, st);
+  } else {
+    s.point = h.point;
+  }
+  // MainShadow, AmbientOcclusion and AuxShadow compare with the threshold stored in a float
+  s.thr = (T)(float)distThresh;
+  const T shadowStart = p.f.interiorMode ? distThresh * deF : distThresh;
+  bool trace = true;
+  if (s.kind == 0) {
+    s.dir = {c.lightVect[0], c.lightVect[1], c.lightVect[2]};
+    s.end = factor;
+    s.r = shadowStart;
+    s.detail = s.thr;
+    s.stepMul = deF;
+    if (sample) trace = p.volLightEnabled[0] != 0;
+    s.out = sample ? wb.sample_res + si : wb.shadow + s.gp;
+  } else {
+    // detailSize after MainShadow: the float threshold if its loop ran at least once
+    s.detail = (p.shadow && shadowStart < factor) ? s.thr : distThresh;
+    if (s.kind == 1) {
+      s.dir = {__ldg(&p.aoVec[3 * s.j + 0]), __ldg(&p.aoVec[3 * s.j + 1]), __ldg(&p.aoVec[3 * s.j + 2])};
+      s.end = h.delta / c.resolution;
+      s.r = h.delta;
+      s.stepMul = T(2);
+      s.out = wb.ao + (int64_t)s.j * wb.npix + s.gp;
+    } else if (!sample) {
+      aux_shadow_begin(p, wb, c, h, px, s);
+      s.stepMul = deF;
+      s.out = wb.auxsh + (int64_t)s.j * wb.npix + s.gp;
+    } else {
+      // the volumetric light of a predefined aux light (src/shaders.cpp:325-341)
+      trace = p.numberOfLights > 0 && p.volLightEnabled[s.j + 1] != 0 && p.lights[s.j].enabled;
+      if (trace) {
+        const LightT<T> L = p.lights[s.j];
+        const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - s.point;
+        s.end = length3(d);
+        s.dir = normalize3(d);
+      }
+      s.r = h.delta;
+      s.stepMul = deF;
+      s.detail = s.thr;
+      s.out = wb.sample_res + (int64_t)(s.j + 1) * wb.sample_cap + si;
+    }
+  }
+  if (!trace) s.end = T(0);
+  if (!(s.r < s.end)) {
+    *s.out = (s.kind == 0 && p.softShadow) ? T(1) : s.sh;
+    return false;
+  }
+  return true;
 }
 
 // Starts job `job`: MainShadow's (src/shaders.cpp:480-570), AmbientOcclusion's
@@ -1209,14 +1497,11 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
       s.end = h.delta / c.resolution;
       s.r = h.delta;
       s.stepMul = T(2);
-    } else if constexpr (EFX) {
-      aux_shadow_begin(p, wb, c, h, px, s);
     }
   }
   if (!(s.r < s.end)) {
     if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? T(1) : s.sh;
-    else if (!EFX || s.kind == 1) wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
-    else wb.auxsh[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    else wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
     return false;
   }
   return true;
@@ -1266,9 +1551,12 @@ __device__ __forceinline__ bool secondary_step(const ParamsT<T> &p, const WaveBu
     if (!(s.r < s.end) || ++s.guard >= kMaxSecondarySteps) done = true;
   }
   if (done) {
-    if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? (T(1) - s.maxSoft) : s.sh;
-    else if (!EFX || s.kind == 1) wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
-    else wb.auxsh[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    if constexpr (EFX) {
+      *s.out = (s.kind == 0 && p.softShadow) ? (T(1) - s.maxSoft) : s.sh;
+    } else {
+      if (s.kind == 0) wb.shadow[s.gp] = p.softShadow ? (T(1) - s.maxSoft) : s.sh;
+      else wb.ao[(int64_t)s.j * wb.npix + s.gp] = s.sh;
+    }
   }
   return done;
 }
@@ -1477,7 +1765,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
   }
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
   const SecondaryJobs jn = secondary_jobs<T, EFX>(p, wb, nh);
-  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux;
+  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux + (unsigned int)kSampleResults * jn.nSamples;
   Counters cnt{0, 0, 0, 0};
   bool active = false, exhausted = false;
   SecondaryRay<T> s{};
@@ -1492,7 +1780,8 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       const unsigned int job = claim_jobs(wb.ctl + 2, need);
       if (need) {
         if (stop || job >= njobs) exhausted = true;
-        else active = secondary_begin<T, EFX>(p, wb, cams, ncams, nh, jn, job, s);
+        else if constexpr (EFX) active = secondary_begin_efx<T>(p, wb, cams, ncams, nh, jn, job, s);
+        else active = secondary_begin<T>(p, wb, cams, ncams, nh, jn, job, s);
       }
     }
     if (!__any_sync(0xffffffffu, active)) {
@@ -1501,6 +1790,12 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
     }
     if (active) {
       const V3<T> point2 = ray_at(s.point, s.dir, s.r);
+      if constexpr (EFX) {
+        if (s.fog) {   // the sample's own threshold; MainShadow's detailSize follows it
+          s.thr = fog_thresh(p, point2, s.eye, s.res, s.persp);
+          if (s.kind == 0) s.detail = s.thr;
+        }
+      }
       int L;
       bool mi;
       const T dist = wave_distance<T, FORMULA, FAST>(p.f, point2, s.detail, p.f.N, p.f.minN, false, L, mi, cnt, s.fpar);
@@ -1517,24 +1812,16 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
   }
 }
 
-// Backward walk over a ray's pooled records: record `index` of a chain whose last chunk
-// holds the records from kChunk * (nchunks - 1) on.
-template <typename T>
-struct PoolRecords {
-  const T *rec;            // [chunk * kChunk + r][4]: dist, thr, step, scan
-  const int32_t *prev;
-  int32_t last;      // chunk holding the last written record
-  int lastRec;       // index of the last written record: buffCount for a hit (its hit step
-                     // writes distance and threshold), buffCount - 1 otherwise
-};
 
 // VolumetricShader (src/shaders.cpp:185-478; glow, visible aux lights, post fog, volumetric
 // fog) reading the pooled records far to near; same arithmetic as `volumetric` in
 // render_core.cuh.
 template <typename T, bool EFX>
 __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolRecords<T> &pr, const int stepCount,
-                                                const T depth, const V3<T> rayStart, const V3<T> view, T out[4],
-                                                float &totalOpacityOut, bool &opacitySet) {
+                                                const T depth, const V3<T> rayStart, const V3<T> view,
+                                                const VolSamples<T> vs, T out[4], float &totalOpacityOut,
+                                                bool &opacitySet) {
+  uint32_t group = vs.base;
   float totalOpacity = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
   T glowN = T(1) - glow;
@@ -1565,6 +1852,12 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
     out[3] += glowOpacity;
     if (EFX && p.auxLightVisibility > T(0) && p.numberOfLights > 0)
       visible_aux_lights<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), view, step, out);
+    if (EFX && p.volLightAny) {
+      const T aux[4] = {vs.res[1 * (int64_t)vs.cap + group], vs.res[2 * (int64_t)vs.cap + group],
+                        vs.res[3 * (int64_t)vs.cap + group], vs.res[4 * (int64_t)vs.cap + group]};
+      volumetric_light_terms<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), step, vs.res[group], aux, out);
+    }
+    group++;
     if (p.postFog) {
       T fogDensity = step / p.fogVisibility;
       if (fogDensity > T(1)) fogDensity = T(1);
@@ -1864,7 +2157,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
           const V3<T> rayStart = d == 0 ? V3<T>{(T)c.start[0], (T)c.start[1], (T)c.start[2]}
                                         : V3<T>{(T)wb.ray_start[ri], (T)wb.ray_start[wb.npix + ri],
                                                 (T)wb.ray_start[2 * wb.npix + ri]};
-          volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, res, totalOpacity, set);
+          const VolSamples<T> vs{wb.sample_res, wb.sample_cap, wb.sample_ray ? wb.sample_base[ri] : 0u};
+          volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, vs, res, totalOpacity, set);
         }
         result[0] = res[0];
         result[1] = res[1];

@@ -33,7 +33,7 @@ struct WaveBufs {
                          // [4] overflow-pass jobs, [5] pool chunks, [6] polish count,
                          // [7] exact_hit refinements that missed the level set, [8] hits before
                          // the current ray depth, [9] rays of the next depth, [10] rays of the
-                         // current depth (zeroed per group)
+                         // current depth, [11] volumetric-light samples (zeroed per group)
   uint32_t *overflow_list;
   // Step records of the primary rays: chunks of kChunk records linked backwards
   // (prev), allocated by bump counter; the pixel keeps its last chunk.
@@ -62,7 +62,18 @@ struct WaveBufs {
   double *ray_thr0;                      // [npix] the previous ray's distThresh, which the reflected
                                          // ray's thresholds add (src/Render3D.cpp:88, 461-462)
   uint32_t *ray_list;                    // [npix_frame] pixels whose next ray is marched
+  // Volumetric lights (VolumetricShader, src/shaders.cpp:309-343): the step groups that the
+  // volumetric walk visits, far to near, each ray's contiguous; the shadow stage traces
+  // MainShadow and the predefined lights' AuxShadow from each, the composition reads them.
+  uint32_t *sample_base;                 // [npix] first sample of each ray
+  uint32_t *sample_ray;                  // [sample_cap] ray of the sample
+  int32_t *sample_rec;                   // [sample_cap] pool record of the group's position
+  T *sample_res;                         // [kSampleResults][sample_cap] MainShadow, AuxShadow of
+                                         // predefined lights 0-3
+  uint32_t sample_cap;                   // samples (every group has a record: the pool's records)
 };
+
+constexpr int kSampleResults = 5;
 
 // Stage events of one launch sequence (see WaveLaunch::ev) and the stats slot of each
 // stage: primary 0, polish 1, shadow/AO 2, compose 3, level set 4, gradient 5.

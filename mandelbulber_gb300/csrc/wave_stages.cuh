@@ -15,7 +15,7 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   };
   // the effects variant of the primary, shadow and composition stages: reflected rays or
   // auxiliary lights
-  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0;
+  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0 || L.p.volLightAny;
   mark(0);
   // one primary pass (and FP64 polish) per ray depth of the reflection loop; between two
   // depths the reflect stage spawns the next depth's rays from this depth's hits
@@ -32,8 +32,8 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
       dev::primary_kernel<T, F, FAST, true><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), wbd, L.cams,
                                                                         L.ncams);
       if (L.overflow)
-        dev::primary_kernel<T, F, FAST, true><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), wbd, L.cams,
-                                                                             L.ncams);
+        dev::primary_kernel<T, F, FAST, true, true><<<L.ov_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.ov, 0), wbd,
+                                                                                   L.cams, L.ncams);
     } else {
       dev::primary_kernel<T, F, FAST><<<L.grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 0), wbd, L.cams, L.ncams);
       if (L.overflow)
@@ -50,6 +50,9 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   if (L.wb.exact_hit)
     dev::level_set_kernel<T, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);
   mark(3);
+  // volumetric lights: the volumetric walk's step groups, whose shadows the shadow stage traces
+  if (L.wb.sample_ray)
+    dev::sample_kernel<T><<<L.compose_grid, L.block, 0, s>>>(L.p, L.wb, L.cams, L.ncams);
   // auxiliary lights: the hit normals, which the AuxShadow jobs test (counted with composition)
   if (L.wb.normal)
     dev::normal_kernel<T, F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
