@@ -237,7 +237,7 @@ static int aux_light_count(const mbgb_scene &s) {
 }
 
 // Features that the per-pixel engine renders and the wavefront stages do not carry (fake
-// lights, iteration fog): scenes that use them render on the per-pixel engine.
+// lights): scenes that use them render on the per-pixel engine.
 // Slow shading, environment mapping and primitive objects are composition-stage work the
 // wavefront carries; ray-traced reflections are further primary passes, one per depth, except
 // with slow shading (whose warp-wide normals serve the camera rays only) or the limit box
@@ -246,11 +246,12 @@ static int aux_light_count(const mbgb_scene &s) {
 // composition, except with slow shading (the jobs need the normals first) or when one shadow
 // factor per light and ray would pass 4 GB.
 static bool per_pixel_only(const mbgb_scene &s) {
-  if (s.fakeLightsEnabled || s.iterFogEnabled) return true;
-  // volumetric lights: samples of the volumetric walk; the shadows they trace take the
-  // detailSize of their start (src/fractal.cpp:1291-1293), which the distance post-processing
-  // of limits, iteration threshold and interior mode reads as well
-  if (s.volumetricLightEnabledAny && (s.limits_enabled || s.iterThresh || s.interiorMode || s.slowShading))
+  if (s.fakeLightsEnabled) return true;
+  // volumetric lights and iteration fog: samples of the volumetric walk; the shadows they
+  // trace take the detailSize of their start (src/fractal.cpp:1291-1293), which the distance
+  // post-processing of limits, iteration threshold and interior mode reads as well
+  if ((s.volumetricLightEnabledAny || s.iterFogEnabled) &&
+      (s.limits_enabled || s.iterThresh || s.interiorMode || s.slowShading))
     return true;
   if (reflection_rays(s) > 1 && (s.slowShading || s.limits_enabled)) return true;
   if (uses_aux_lights(s)) {
@@ -1046,7 +1047,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
 struct WaveLayout {
   size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
   size_t prec, pprev;
-  size_t rstart, rdir, rthr, rlist, normal, auxsh, sbase, sray, srec, sres;
+  size_t rstart, rdir, rthr, rlist, normal, auxsh, sbase, sray, srec, sstep, sres, piters;
   uint32_t poolCap;
   size_t total;
 };
@@ -1054,9 +1055,10 @@ struct WaveLayout {
 // `npixFrame` pixels with `rays` rays each (the reflection loop's depths): every per-ray array
 // holds rays x npixFrame entries.
 // `auxN` auxiliary lights: hit normals, and with `auxShadows` one AuxShadow factor per light.
-// `volLights`: the volumetric walk's samples (at most one per pool record) and their shadows.
+// `sampleRes` > 0 (volumetric lights, iteration fog): the volumetric walk's samples (at most
+// one per pool record) with `sampleRes` results each; `iterFog`: the records' itersOut.
 static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVol, int rays, int auxN,
-                              bool auxShadows, bool volLights) {
+                              bool auxShadows, int sampleRes, bool iterFog) {
   const int64_t npix = npixFrame * rays;
   WaveLayout w{};
   size_t off = 0;
@@ -1097,11 +1099,13 @@ static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVo
   w.rlist = take((rays > 1 ? (size_t)npixFrame : 0) * 4);
   w.normal = take(auxN > 0 ? 3 * (size_t)npix * ts : 0);
   w.auxsh = take(auxN > 0 && auxShadows ? (size_t)auxN * npix * ts : 0);
-  const size_t samples = volLights && needVol ? (size_t)w.poolCap * kChunk : 0;
-  w.sbase = take(volLights ? (size_t)npix * 4 : 0);
+  const size_t samples = sampleRes > 0 && needVol ? (size_t)w.poolCap * kChunk : 0;
+  w.sbase = take(sampleRes > 0 ? (size_t)npix * 4 : 0);
   w.sray = take(samples * 4);
   w.srec = take(samples * 4);
-  w.sres = take(samples * kSampleResults * ts);
+  w.sstep = take(samples * ts);
+  w.sres = take(samples * (size_t)sampleRes * ts);
+  w.piters = take(iterFog && needVol ? (size_t)w.poolCap * kChunk * 4 : 0);
   w.total = off;
   return w;
 }
@@ -1125,8 +1129,10 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   const int aoN = rayAO ? c->ao_count : 0;
   const int rays = reflection_rays(scene);
   const int auxN = aux_light_count(scene);
-  const bool volLights = scene.volumetricLightEnabledAny != 0;
-  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays, auxN, scene.shadow != 0, volLights);
+  const bool volLights = scene.volumetricLightEnabledAny != 0 || scene.iterFogEnabled != 0;
+  const int sampleRes = volLights ? kSampleShadows + (scene.iterFogEnabled ? aoN : 0) : 0;
+  const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays, auxN, scene.shadow != 0, sampleRes,
+                                   scene.iterFogEnabled != 0);
   char *base = (char *)c->wave[prec].ptr;
   WaveLaunch<T> L;
   WaveBufs<T> &wb = L.wb;
@@ -1168,8 +1174,11 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   wb.sample_base = volLights ? (uint32_t *)(base + w.sbase) : nullptr;
   wb.sample_ray = volLights && needVol ? (uint32_t *)(base + w.sray) : nullptr;
   wb.sample_rec = volLights && needVol ? (int32_t *)(base + w.srec) : nullptr;
+  wb.sample_step = volLights && needVol ? (T *)(base + w.sstep) : nullptr;
   wb.sample_res = volLights && needVol ? (T *)(base + w.sres) : nullptr;
   wb.sample_cap = volLights && needVol ? w.poolCap * (uint32_t)kChunk : 0u;
+  wb.sample_nres = sampleRes;
+  wb.pool_iters = scene.iterFogEnabled && needVol ? (int32_t *)(base + w.piters) : nullptr;
   // shadow/AO rays two per thread (secondary_pair_kernel): the lean FP32 Mandelbox with
   // per-estimate refill, which the pair kernel's packed orbit serves
   wb.pair_rays = (sizeof(T) == 4 && fast_mandelbox(scene) && g.cfg.pairRays && g.cfg.orbitRefill <= 0) ? 1 : 0;
@@ -1206,6 +1215,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   L.ov.step_thr = c->ovstep[prec][2].ptr;
   // the visible auxiliary lights of a long ray sample its record positions
   L.ov.step_scan = need_step_points(scene) ? c->ovstep[prec][3].ptr : nullptr;
+  L.ov.step_iters = need_step_points(scene) ? (int *)c->ovstep[prec][4].ptr : nullptr;
   L.overflow = needVol;
   for (int k = 0; k < kStageEvents; k++) L.ev[k] = ev ? ev[k] : nullptr;
   // the FAST instantiations hold no limit box test: limit-box scenes take the generic kernels,
@@ -1634,12 +1644,12 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     Group *g = nullptr;
     // a frame with auxiliary lights keeps its own group (its lights are placed for it), and so
     // does one with volumetric lights (the long rays' fold reads the scene's own parameters)
-    if (wave && !uses_aux_lights(sc) && !sc.volumetricLightEnabledAny) {
+    if (wave && !uses_aux_lights(sc) && !sc.volumetricLightEnabledAny && !sc.iterFogEnabled) {
       for (auto &h : plan.groups) {
         if (!h.wave || h.prec != prec[i]) continue;
         if ((double)std::max(h.npix + fpix, h.jobs + fjobs) * perPix >= kMaxGroupJobs) continue;
         const mbgb_scene &rep = scenes[h.frames[0]];
-        if (uses_aux_lights(rep) || rep.volumetricLightEnabledAny) continue;
+        if (uses_aux_lights(rep) || rep.volumetricLightEnabledAny || rep.iterFogEnabled) continue;
         const bool same = prec[i] == 0 ? same_shared<double>(rep, sc, o) : same_shared<float>(rep, sc, o);
         if (!same) continue;
         const LaunchCfg &hc = h.cfg;
@@ -1686,7 +1696,10 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       wave_bytes[g.prec] =
           std::max(wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol, reflection_rays(rep),
                                                    aux_light_count(rep), rep.shadow != 0,
-                                                   rep.volumetricLightEnabledAny != 0)
+                                                   (rep.volumetricLightEnabledAny || rep.iterFogEnabled)
+                                                       ? kSampleShadows + (rep.iterFogEnabled && rayAO ? c->ao_count : 0)
+                                                       : 0,
+                                                   rep.iterFogEnabled != 0)
                                            .total);
       g.cams_off = camsBytes;
       const size_t cs = g.prec == 0 ? sizeof(FrameCam<double>) : sizeof(FrameCam<float>);

@@ -492,20 +492,87 @@ __device__ __forceinline__ void volumetric_light_terms(const ParamsT<T> &p, cons
 // the walk's k-th step group.
 template <typename T>
 struct VolSamples {
-  const T *res;    // [kSampleResults][cap]
+  const T *res;            // [WaveBufs::sample_nres][cap]
+  const int32_t *iters;    // the pool records' itersOut (iteration fog)
   uint32_t cap, base;
 };
+
+// Iteration fog at one step group (VolumetricShader, src/shaders.cpp:385-466): the fog colour
+// by the record's iteration count, lit by the main light and the predefined aux lights through
+// the group's shadows and by the ray-traced AO, blended in by the group's opacity. `res` holds
+// the group's results at stride `cap`: MainShadow, 4 AuxShadow, then the AO directions.
+template <typename T>
+__device__ __forceinline__ void iteration_fog_term(const ParamsT<T> &p, const V3<T> point, const T step, const int L,
+                                                   const T *res, const uint32_t cap, T out[4],
+                                                   float &totalOpacity) {
+  const T N = T(p.f.N);
+  T opacity = iter_opacity(step, T(L), N, p.iterFogOpacityTrim, p.iterFogOpacity);
+  if (!(opacity > T(0))) return;
+  const T iterFactor = T(2) * (T(L) - p.iterFogOpacityTrim) / (N - p.iterFogOpacityTrim);
+  T k = iterFactor;
+  if (k > T(1)) k = T(1);
+  if (k < T(0)) k = T(0);
+  T kn = T(1) - k;
+  T fogCol[3];
+  for (int c = 0; c < 3; c++) fogCol[c] = (T(p.fogCol1[c]) * kn + T(p.fogCol2[c]) * k);
+  T k2 = iterFactor - T(1);
+  if (k2 < T(0)) k2 = T(0);
+  if (k2 > T(1)) k2 = T(1);
+  kn = T(1) - k2;
+  for (int c = 0; c < 3; c++) fogCol[c] = (fogCol[c] * kn + T(p.fogCol3[c]) * k2);
+  T newColour[3] = {T(0), T(0), T(0)};
+  for (int i = 0; i < 5; i++) {
+    if (i == 0) {
+      if (p.mainLightIntensity * p.directLight > T(0)) {
+        const T sh = res[0];
+        for (int c = 0; c < 3; c++)
+          newColour[c] += sh * T(p.mainLightColour[c]) / T(65536) * p.mainLightIntensity * p.directLight;
+      }
+    }
+    if (i > 0 && p.numberOfLights > 0 && p.lights[i - 1].enabled) {
+      const LightT<T> Lt = p.lights[i - 1];
+      const V3<T> d = V3<T>{Lt.pos[0], Lt.pos[1], Lt.pos[2]} - point;
+      const T distance = length3(d);
+      const T distance2 = distance * distance;
+      const T light = res[(int64_t)i * cap];
+      const T intensity = Lt.intensity * T(100);
+      for (int c = 0; c < 3; c++) newColour[c] += light * T(Lt.colour[c]) / T(65536) / distance2 * intensity;
+    }
+  }
+  if (p.ao && !p.fastAO) {
+    // AmbientOcclusion (src/shaders.cpp:607-673): the directions' shadowTemp, weighed and averaged
+    V3<T> AO{T(0), T(0), T(0)};
+    for (int v = 0; v < p.aoCount; v++) {
+      const T sh = res[(int64_t)(kSampleShadows + v) * cap];
+      AO.x += sh * p.aoWeight[0];
+      AO.y += sh * p.aoWeight[1];
+      AO.z += sh * p.aoWeight[2];
+    }
+    const T div = T(p.aoCount) * T(256);
+    AO.x /= div;
+    AO.y /= div;
+    AO.z /= div;
+    newColour[0] += AO.x * p.globalIlum;
+    newColour[1] += AO.y * p.globalIlum;
+    newColour[2] += AO.z * p.globalIlum;
+  }
+  if (opacity > T(1)) opacity = T(1);
+  for (int c = 0; c < 3; c++) out[c] = out[c] * (T(1) - opacity) + newColour[c] * opacity * fogCol[c] / T(65536);
+  totalOpacity = (float)(opacity + (T(1) - opacity) * (T)totalOpacity);
+  out[3] = opacity + (T(1) - opacity) * out[3];
+}
 
 // The volumetric pass over one ray's records (VolumetricShader's glow, post fog and
 // volumetric fog, src/shaders.cpp:185-478) as the affine map out = A*base + B, plus
 // the alpha and opacity it leaves for a base alpha of `alpha0`.
-// Effects variant: the visible aux lights and the volumetric lights, whose MainShadow and
-// AuxShadow (render_core.cuh's, with the ray's `delta` and the camera `eye`) run here in line.
+// Effects variant: the visible aux lights, the volumetric lights and the iteration fog, whose
+// MainShadow, AuxShadow and AO (render_core.cuh's, with the ray's `delta`, last distance and
+// the camera `eye`) run here in line.
 template <typename T, bool EFX, int FORMULA>
 __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const StepBuf<T> &sb, const int stepCount,
                                                   const T depth, const T alpha0, const V3<T> rayStart,
                                                   const V3<T> view, const T delta, const V3<T> eye,
-                                                  const FrameIO &io, Counters &cnt, T vol[6]) {
+                                                  const T lastDist, const FrameIO &io, Counters &cnt, T vol[6]) {
   T detail = T(0);
   int itersOut = 0;
   T A = T(1), B0 = T(0), B1 = T(0), B2 = T(0), alpha = alpha0;
@@ -594,6 +661,59 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
       totalOpacity = (float)(fd + (T(1) - fd) * (T)totalOpacity);
       alpha = fd + (T(1) - fd) * alpha;
     }
+    if (EFX && p.iterFog && sb.iters && sb.scan) {
+      // iteration fog (src/shaders.cpp:385-466) with its shadows and AO traced here
+      const int L = sb.iters[sb.at(index)];
+      const T N = T(p.f.N);
+      T opacity = iter_opacity(step, T(L), N, p.iterFogOpacityTrim, p.iterFogOpacity);
+      if (opacity > T(0)) {
+        const V3<T> point = rayStart + view * sb.scan[sb.at(index)];
+        const T thrStep = sb.thr[sb.at(index)];
+        const T iterFactor = T(2) * (T(L) - p.iterFogOpacityTrim) / (N - p.iterFogOpacityTrim);
+        T k = iterFactor;
+        if (k > T(1)) k = T(1);
+        if (k < T(0)) k = T(0);
+        T kn = T(1) - k;
+        T fogCol[3];
+        for (int c = 0; c < 3; c++) fogCol[c] = (T(p.fogCol1[c]) * kn + T(p.fogCol2[c]) * k);
+        T k2 = iterFactor - T(1);
+        if (k2 < T(0)) k2 = T(0);
+        if (k2 > T(1)) k2 = T(1);
+        kn = T(1) - k2;
+        for (int c = 0; c < 3; c++) fogCol[c] = (fogCol[c] * kn + T(p.fogCol3[c]) * k2);
+        T newColour[3] = {T(0), T(0), T(0)};
+        if (p.mainLightIntensity * p.directLight > T(0)) {
+          const T sh = main_shadow<T, FORMULA>(p, point, thrStep, delta, eye, detail, itersOut, io, cnt);
+          for (int c = 0; c < 3; c++)
+            newColour[c] += sh * T(p.mainLightColour[c]) / T(65536) * p.mainLightIntensity * p.directLight;
+        }
+        for (int i = 1; i < 5; i++) {
+          if (p.numberOfLights > 0 && p.lights[i - 1].enabled) {
+            const LightT<T> Lt = p.lights[i - 1];
+            const V3<T> d = V3<T>{Lt.pos[0], Lt.pos[1], Lt.pos[2]} - point;
+            const T distance = length3(d);
+            const T distance2 = distance * distance;
+            const T light =
+                aux_shadow<T, FORMULA>(p, point, distance, normalize3(d), delta, thrStep, eye, detail, itersOut, cnt);
+            const T intensity = Lt.intensity * T(100);
+            for (int c = 0; c < 3; c++) newColour[c] += light * T(Lt.colour[c]) / T(65536) / distance2 * intensity;
+          }
+        }
+        if (p.ao && !p.fastAO) {
+          const V3<T> AO = ray_ao<T, FORMULA>(p, point, delta, thrStep, lastDist, detail, eye, itersOut, cnt);
+          newColour[0] += AO.x * p.globalIlum;
+          newColour[1] += AO.y * p.globalIlum;
+          newColour[2] += AO.z * p.globalIlum;
+        }
+        if (opacity > T(1)) opacity = T(1);
+        A = A * (T(1) - opacity);
+        B0 = B0 * (T(1) - opacity) + newColour[0] * opacity * fogCol[0] / T(65536);
+        B1 = B1 * (T(1) - opacity) + newColour[1] * opacity * fogCol[1] / T(65536);
+        B2 = B2 * (T(1) - opacity) + newColour[2] * opacity * fogCol[2] / T(65536);
+        totalOpacity = (float)(opacity + (T(1) - opacity) * (T)totalOpacity);
+        alpha = opacity + (T(1) - opacity) * alpha;
+      }
+    }
     if (totalOpacity > 1.0f) totalOpacity = 1.0f;
     if (alpha > T(1)) alpha = T(1);
     opacityOut = totalOpacity;
@@ -618,8 +738,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
                                                       const FrameIO io, const WaveBufs<T> wb,
                                                       const FrameCam<T> *__restrict__ cams, const int ncams) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, (T *)io.step_scan, nullptr, io.slots,
-                      slot};
+  const StepBuf<T> sb{(T *)io.step_step, (T *)io.step_dist, (T *)io.step_thr, (T *)io.step_scan, io.step_iters,
+                      io.slots, slot};
   const bool useSB = p.needVolumetric;
   const bool f64 = sizeof(T) == 8;
   const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
@@ -741,6 +861,9 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
           if (io.overflow_pass) {
             sb.dist[sb.at(i)] = dist;
             sb.thr[sb.at(i)] = thr;
+            if constexpr (EFX) {
+              if (sb.iters) sb.iters[sb.at(i)] = iters;
+            }
           } else {
             // main pass: records go to the batch's pool in chunks of kChunk
             bool full = false;
@@ -764,6 +887,9 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             // the record's step slot holds the step that reached this point; the walk
             // never reads it for the hit record
             store_record(wb.pool_rec + 4 * rec, dist, thr, step, scan);
+            if constexpr (EFX) {
+              if (wb.pool_iters) wb.pool_iters[rec] = iters;
+            }
           }
         }
         if (dist > T(3)) dist = T(3);
@@ -821,7 +947,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
                                              V3<T>{(T)cams[frame_of_pixel(cams, ncams, gp)].start[0],
                                                    (T)cams[frame_of_pixel(cams, ncams, gp)].start[1],
                                                    (T)cams[frame_of_pixel(cams, ncams, gp)].start[2]},
-                                             io, cnt, vol);
+                                             dist, io, cnt, vol);
           for (int c = 0; c < 6; c++) wb.vol[c * wb.npix + ri] = vol[c];
           flags |= 4;
         }
@@ -1116,9 +1242,10 @@ __global__ void __launch_bounds__(128) normal_kernel(const __grid_constant__ Par
   }
 }
 
-// Volumetric lights: the step groups of every ray that the volumetric walk visits (records
-// summed far to near until the sum reaches thr x quality, src/shaders.cpp:198-205), each
-// ray's samples contiguous and in the walk's order. One thread per pixel walks the rays the
+// Volumetric lights and iteration fog: the step groups of every ray that the volumetric walk
+// lights (records summed far to near until the sum reaches thr x quality,
+// src/shaders.cpp:198-205; group_has_sample), each ray's samples contiguous and in the walk's
+// order. One thread per pixel walks the rays the
 // reflection loop marched; long rays of the overflow pass fold theirs in that pass.
 template <typename T, typename F>
 __device__ __forceinline__ void walk_groups(const ParamsT<T> &p, const PoolRecords<T> &pr, const int stepCount, F fn) {
@@ -1135,9 +1262,20 @@ __device__ __forceinline__ void walk_groups(const ParamsT<T> &p, const PoolRecor
     load_record(pr.rec + 4 * rec, distance, dist_thresh, step);
     totalStep += step;
     if (totalStep < dist_thresh * p.quality) continue;
+    const T merged = totalStep;
     totalStep = T(0);
-    fn(rec);
+    fn(rec, merged);
   }
+}
+
+// A step group the shadow stage traces from: every group with volumetric lights, those of
+// positive iteration-fog opacity (src/shaders.cpp:387-390) with iteration fog.
+template <typename T>
+__device__ __forceinline__ bool group_has_sample(const ParamsT<T> &p, const int32_t *iters, const int64_t rec,
+                                                 const T step) {
+  if (p.volLightAny) return true;
+  return p.iterFog &&
+         iter_opacity(step, T(iters[rec]), T(p.f.N), p.iterFogOpacityTrim, p.iterFogOpacity) > T(0);
 }
 
 template <typename T>
@@ -1164,13 +1302,17 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Par
       const int count = wb.count[ri];
       const PoolRecords<T> pr{wb.pool_rec, wb.pool_prev, wb.last_chunk[ri], (flags & 1) ? count : count - 1};
       unsigned int n = 0;
-      walk_groups(p, pr, count, [&](int64_t) { n++; });
+      walk_groups(p, pr, count, [&](int64_t rec, T step) {
+        if (group_has_sample(p, wb.pool_iters, rec, step)) n++;
+      });
       const unsigned int base = n ? atomicAdd(wb.ctl + 11, n) : 0u;
       wb.sample_base[ri] = base;
       unsigned int k = base;
-      walk_groups(p, pr, count, [&](int64_t rec) {
+      walk_groups(p, pr, count, [&](int64_t rec, T step) {
+        if (!group_has_sample(p, wb.pool_iters, rec, step)) return;
         wb.sample_ray[k] = (uint32_t)ri;
         wb.sample_rec[k] = (int32_t)rec;
+        wb.sample_step[k] = step;
         k++;
       });
     }
@@ -1259,7 +1401,7 @@ __device__ __forceinline__ V3<T> ray_view(const ParamsT<T> &p, const FrameCam<T>
 // (aux lights with shadows) one AuxShadow per enabled light and hit.
 struct SecondaryJobs {
   unsigned int nShadow, nAO, nAux;
-  unsigned int nSamples;   // volumetric-light samples: kSampleResults jobs each
+  unsigned int nSamples;   // volumetric-light / iteration-fog samples: WaveBufs::sample_nres jobs each
 };
 template <typename T, bool EFX = false>
 __device__ __forceinline__ SecondaryJobs secondary_jobs(const ParamsT<T> &p, const WaveBufs<T> &wb,
@@ -1363,17 +1505,14 @@ __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const W
     s.j = q / nh;
     s.gp = (int64_t)wb.hit_list[q % nh];
   } else {
+    // sample jobs, result-major: [0] MainShadow, [1, 4] AuxShadow of predefined light r - 1,
+    // [5, ...) AO direction r - 5 (iteration fog)
     q -= jn.nAux;
     sample = true;
-    if (q < jn.nSamples) {
-      s.kind = 0;
-      si = q;
-    } else {
-      q -= jn.nSamples;
-      s.kind = 2;
-      s.j = q / jn.nSamples;
-      si = q % jn.nSamples;
-    }
+    const unsigned int r = q / jn.nSamples;
+    si = q % jn.nSamples;
+    s.kind = r == 0 ? 0 : (r < (unsigned int)kSampleShadows ? 2 : 1);
+    s.j = r == 0 ? 0u : (r < (unsigned int)kSampleShadows ? r - 1 : r - kSampleShadows);
     s.gp = (int64_t)wb.sample_ray[si];
   }
   const int64_t px = pixel_of_ray(wb, s.gp);
@@ -1390,6 +1529,7 @@ __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const W
   const T deF = s.fog ? T(1) : p.DE_factor;
   const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
   T distThresh = h.thr;
+  bool fogGroup = false;   // the group takes part in the iteration fog (positive opacity)
   if (sample) {
     // the group's position and threshold (src/shaders.cpp:309-343)
     const int64_t rec = (int64_t)wb.sample_rec[si];
@@ -1398,6 +1538,8 @@ __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const W
     s.point = rs + rv * record_scan(wb.pool_rec + 4 * rec);
     T dd, st;
     load_record(wb.pool_rec + 4 * rec, dd, distThresh, st);
+    fogGroup = p.iterFog && iter_opacity(wb.sample_step[si], T(wb.pool_iters[rec]), T(p.f.N), p.iterFogOpacityTrim,
+                                         p.iterFogOpacity) > T(0);
   } else {
     s.point = h.point;
   }
@@ -1411,7 +1553,9 @@ __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const W
     s.r = shadowStart;
     s.detail = s.thr;
     s.stepMul = deF;
-    if (sample) trace = p.volLightEnabled[0] != 0;
+    // volumetric light 0, or the iteration fog's main light (src/shaders.cpp:313, 409)
+    if (sample)
+      trace = (p.volLightAny && p.volLightEnabled[0] != 0) || (fogGroup && p.mainLightIntensity * p.directLight > T(0));
     s.out = sample ? wb.sample_res + si : wb.shadow + s.gp;
   } else {
     // detailSize after MainShadow: the float threshold if its loop ran at least once
@@ -1421,14 +1565,22 @@ __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const W
       s.end = h.delta / c.resolution;
       s.r = h.delta;
       s.stepMul = T(2);
-      s.out = wb.ao + (int64_t)s.j * wb.npix + s.gp;
+      if (sample) {   // the iteration fog's AO at the group (src/shaders.cpp:444-450)
+        trace = fogGroup;
+        s.detail = s.thr;
+        s.out = wb.sample_res + (int64_t)(kSampleShadows + s.j) * wb.sample_cap + si;
+      } else {
+        s.out = wb.ao + (int64_t)s.j * wb.npix + s.gp;
+      }
     } else if (!sample) {
       aux_shadow_begin(p, wb, c, h, px, s);
       s.stepMul = deF;
       s.out = wb.auxsh + (int64_t)s.j * wb.npix + s.gp;
     } else {
-      // the volumetric light of a predefined aux light (src/shaders.cpp:325-341)
-      trace = p.numberOfLights > 0 && p.volLightEnabled[s.j + 1] != 0 && p.lights[s.j].enabled;
+      // the volumetric light of a predefined aux light, or its iteration-fog light
+      // (src/shaders.cpp:325-341, 423-441)
+      trace = p.numberOfLights > 0 && ((p.volLightAny && p.volLightEnabled[s.j + 1] != 0) || fogGroup) &&
+              p.lights[s.j].enabled;
       if (trace) {
         const LightT<T> L = p.lights[s.j];
         const V3<T> d = V3<T>{L.pos[0], L.pos[1], L.pos[2]} - s.point;
@@ -1765,7 +1917,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
   }
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
   const SecondaryJobs jn = secondary_jobs<T, EFX>(p, wb, nh);
-  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux + (unsigned int)kSampleResults * jn.nSamples;
+  const unsigned int njobs = jn.nShadow + jn.nAO + jn.nAux + (unsigned int)wb.sample_nres * jn.nSamples;
   Counters cnt{0, 0, 0, 0};
   bool active = false, exhausted = false;
   SecondaryRay<T> s{};
@@ -1799,6 +1951,13 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       int L;
       bool mi;
       const T dist = wave_distance<T, FORMULA, FAST>(p.f, point2, s.detail, p.f.N, p.f.minN, false, L, mi, cnt, s.fpar);
+      if constexpr (EFX) {
+        // iteration fog absorbs along every march (MainShadow, AmbientOcclusion, AuxShadow:
+        // src/shaders.cpp:535-539, 655-659, 1095-1099), at the march's own step factor
+        if (p.iterFog)
+          s.sh -= iter_opacity(dist * s.stepMul, T(L), T(p.f.N), p.iterFogOpacityTrim, p.iterFogOpacity) *
+                  (s.end - s.r) / s.end;
+      }
       if (secondary_step<T, EFX>(p, wb, s, dist, mi)) active = false;
     }
   }
@@ -1852,12 +2011,13 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
     out[3] += glowOpacity;
     if (EFX && p.auxLightVisibility > T(0) && p.numberOfLights > 0)
       visible_aux_lights<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), view, step, out);
+    // the group's shadow-stage results (volumetric lights, iteration fog)
+    const bool sampled = EFX && (p.volLightAny || p.iterFog) && group_has_sample(p, vs.iters, rec, step);
     if (EFX && p.volLightAny) {
       const T aux[4] = {vs.res[1 * (int64_t)vs.cap + group], vs.res[2 * (int64_t)vs.cap + group],
                         vs.res[3 * (int64_t)vs.cap + group], vs.res[4 * (int64_t)vs.cap + group]};
       volumetric_light_terms<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), step, vs.res[group], aux, out);
     }
-    group++;
     if (p.postFog) {
       T fogDensity = step / p.fogVisibility;
       if (fogDensity > T(1)) fogDensity = T(1);
@@ -1890,6 +2050,10 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
       totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
       out[3] = fogDensity + (T(1) - fogDensity) * out[3];
     }
+    if (EFX && p.iterFog && sampled)
+      iteration_fog_term<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), step, vs.iters[rec], vs.res + group,
+                            vs.cap, out, totalOpacity);
+    if (sampled) group++;
     if (totalOpacity > 1.0f) totalOpacity = 1.0f;
     if (out[3] > T(1)) out[3] = T(1);
     totalOpacityOut = totalOpacity;
@@ -2157,7 +2321,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
           const V3<T> rayStart = d == 0 ? V3<T>{(T)c.start[0], (T)c.start[1], (T)c.start[2]}
                                         : V3<T>{(T)wb.ray_start[ri], (T)wb.ray_start[wb.npix + ri],
                                                 (T)wb.ray_start[2 * wb.npix + ri]};
-          const VolSamples<T> vs{wb.sample_res, wb.sample_cap, wb.sample_ray ? wb.sample_base[ri] : 0u};
+          const VolSamples<T> vs{wb.sample_res, wb.pool_iters, wb.sample_cap, wb.sample_ray ? wb.sample_base[ri] : 0u};
           volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, vs, res, totalOpacity, set);
         }
         result[0] = res[0];

@@ -62,18 +62,24 @@ struct WaveBufs {
   double *ray_thr0;                      // [npix] the previous ray's distThresh, which the reflected
                                          // ray's thresholds add (src/Render3D.cpp:88, 461-462)
   uint32_t *ray_list;                    // [npix_frame] pixels whose next ray is marched
-  // Volumetric lights (VolumetricShader, src/shaders.cpp:309-343): the step groups that the
-  // volumetric walk visits, far to near, each ray's contiguous; the shadow stage traces
-  // MainShadow and the predefined lights' AuxShadow from each, the composition reads them.
+  // Volumetric lights and iteration fog (VolumetricShader, src/shaders.cpp:309-343, 385-466):
+  // the step groups that the volumetric walk lights, far to near, each ray's contiguous; the
+  // shadow stage traces MainShadow, the predefined lights' AuxShadow and (iteration fog) the
+  // AO directions from each, the composition reads them.
   uint32_t *sample_base;                 // [npix] first sample of each ray
   uint32_t *sample_ray;                  // [sample_cap] ray of the sample
   int32_t *sample_rec;                   // [sample_cap] pool record of the group's position
-  T *sample_res;                         // [kSampleResults][sample_cap] MainShadow, AuxShadow of
-                                         // predefined lights 0-3
+  T *sample_step;                        // [sample_cap] the group's summed step
+  T *sample_res;                         // [sample_nres][sample_cap] MainShadow, AuxShadow of the
+                                         // predefined lights 0-3, then (iteration fog with ray AO)
+                                         // each AO direction's shadowTemp
   uint32_t sample_cap;                   // samples (every group has a record: the pool's records)
+  int sample_nres;                       // results per sample
+  int32_t *pool_iters;                   // [chunk * kChunk + r] itersOut at each record (iteration
+                                         // fog; null without)
 };
 
-constexpr int kSampleResults = 5;
+constexpr int kSampleShadows = 5;        // MainShadow and the four predefined lights' AuxShadow
 
 // Stage events of one launch sequence (see WaveLaunch::ev) and the stats slot of each
 // stage: primary 0, polish 1, shadow/AO 2, compose 3, level set 4, gradient 5.

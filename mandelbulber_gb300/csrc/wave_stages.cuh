@@ -15,7 +15,7 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   };
   // the effects variant of the primary, shadow and composition stages: reflected rays or
   // auxiliary lights
-  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0 || L.p.volLightAny;
+  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0 || L.p.volLightAny || L.p.iterFog;
   mark(0);
   // one primary pass (and FP64 polish) per ray depth of the reflection loop; between two
   // depths the reflect stage spawns the next depth's rays from this depth's hits
