@@ -236,8 +236,7 @@ static int aux_light_count(const mbgb_scene &s) {
   return uses_aux_lights(s) ? std::max(s.auxLightNumber > 0 ? s.auxLightNumber : 0, 4) : 0;
 }
 
-// Features that the per-pixel engine renders and the wavefront stages do not carry (fake
-// lights): scenes that use them render on the per-pixel engine.
+// Scenes the wavefront stages do not carry render on the per-pixel engine.
 // Slow shading, environment mapping and primitive objects are composition-stage work the
 // wavefront carries; ray-traced reflections are further primary passes, one per depth, except
 // with slow shading (whose warp-wide normals serve the camera rays only) or the limit box
@@ -246,11 +245,10 @@ static int aux_light_count(const mbgb_scene &s) {
 // composition, except with slow shading (the jobs need the normals first) or when one shadow
 // factor per light and ray would pass 4 GB.
 static bool per_pixel_only(const mbgb_scene &s) {
-  if (s.fakeLightsEnabled) return true;
-  // volumetric lights and iteration fog: samples of the volumetric walk; the shadows they
-  // trace take the detailSize of their start (src/fractal.cpp:1291-1293), which the distance
-  // post-processing of limits, iteration threshold and interior mode reads as well
-  if ((s.volumetricLightEnabledAny || s.iterFogEnabled) &&
+  // volumetric lights, iteration fog and fake lights: samples of the volumetric walk; the
+  // shadows they trace take the detailSize of their start (src/fractal.cpp:1291-1293), which
+  // the distance post-processing of limits, iteration threshold and interior mode reads as well
+  if ((s.volumetricLightEnabledAny || s.iterFogEnabled || s.fakeLightsEnabled) &&
       (s.limits_enabled || s.iterThresh || s.interiorMode || s.slowShading))
     return true;
   if (reflection_rays(s) > 1 && (s.slowShading || s.limits_enabled)) return true;
@@ -1129,8 +1127,10 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   const int aoN = rayAO ? c->ao_count : 0;
   const int rays = reflection_rays(scene);
   const int auxN = aux_light_count(scene);
-  const bool volLights = scene.volumetricLightEnabledAny != 0 || scene.iterFogEnabled != 0;
-  const int sampleRes = volLights ? kSampleShadows + (scene.iterFogEnabled ? aoN : 0) : 0;
+  const bool volLights =
+      scene.volumetricLightEnabledAny != 0 || scene.iterFogEnabled != 0 || scene.fakeLightsEnabled != 0;
+  const int sampleRes =
+      volLights ? kSampleShadows + (scene.iterFogEnabled ? aoN : 0) + (scene.fakeLightsEnabled ? 1 : 0) : 0;
   const WaveLayout w = wave_layout(g.npix, sizeof(T), aoN, needVol, rays, auxN, scene.shadow != 0, sampleRes,
                                    scene.iterFogEnabled != 0);
   char *base = (char *)c->wave[prec].ptr;
@@ -1644,12 +1644,14 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
     Group *g = nullptr;
     // a frame with auxiliary lights keeps its own group (its lights are placed for it), and so
     // does one with volumetric lights (the long rays' fold reads the scene's own parameters)
-    if (wave && !uses_aux_lights(sc) && !sc.volumetricLightEnabledAny && !sc.iterFogEnabled) {
+    if (wave && !uses_aux_lights(sc) && !sc.volumetricLightEnabledAny && !sc.iterFogEnabled &&
+        !sc.fakeLightsEnabled) {
       for (auto &h : plan.groups) {
         if (!h.wave || h.prec != prec[i]) continue;
         if ((double)std::max(h.npix + fpix, h.jobs + fjobs) * perPix >= kMaxGroupJobs) continue;
         const mbgb_scene &rep = scenes[h.frames[0]];
-        if (uses_aux_lights(rep) || rep.volumetricLightEnabledAny || rep.iterFogEnabled) continue;
+        if (uses_aux_lights(rep) || rep.volumetricLightEnabledAny || rep.iterFogEnabled || rep.fakeLightsEnabled)
+          continue;
         const bool same = prec[i] == 0 ? same_shared<double>(rep, sc, o) : same_shared<float>(rep, sc, o);
         if (!same) continue;
         const LaunchCfg &hc = h.cfg;
@@ -1696,8 +1698,11 @@ static mbgb_status render_frames(mbgb_context *c, const mbgb_scene *scenes, int 
       wave_bytes[g.prec] =
           std::max(wave_bytes[g.prec], wave_layout(g.npix, ts, rayAO ? c->ao_count : 0, needVol, reflection_rays(rep),
                                                    aux_light_count(rep), rep.shadow != 0,
-                                                   (rep.volumetricLightEnabledAny || rep.iterFogEnabled)
-                                                       ? kSampleShadows + (rep.iterFogEnabled && rayAO ? c->ao_count : 0)
+                                                   (rep.volumetricLightEnabledAny || rep.iterFogEnabled ||
+                                                    rep.fakeLightsEnabled)
+                                                       ? kSampleShadows +
+                                                             (rep.iterFogEnabled && rayAO ? c->ao_count : 0) +
+                                                             (rep.fakeLightsEnabled ? 1 : 0)
                                                        : 0,
                                                    rep.iterFogEnabled != 0)
                                            .total);

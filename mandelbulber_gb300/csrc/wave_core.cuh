@@ -461,6 +461,19 @@ __device__ __forceinline__ void visible_aux_lights(const ParamsT<T> &p, const V3
   }
 }
 
+// The volumetric fake light of one step group (src/shaders.cpp:298-307) from its orbit trap
+// distance `r`; adds to out[0..3].
+template <typename T>
+__device__ __forceinline__ void fake_light_glow(const ParamsT<T> &p, T r, const T step, T out[4]) {
+  r = m_sqrt(T(1.0f) / (r + T(1.0e-30f)));
+  const T fakeLight = T(1) / (m_pow(r, T(10) / p.fakeLightsVisibilitySize) *
+                                  m_pow(T(10), T(10) / p.fakeLightsVisibilitySize) + T(1e-100));
+  out[0] += fakeLight * step * p.fakeLightsVisibility;
+  out[1] += fakeLight * step * p.fakeLightsVisibility;
+  out[2] += fakeLight * step * p.fakeLightsVisibility;
+  out[3] += fakeLight * step * p.fakeLightsVisibility;
+}
+
 // Volumetric lights at one step group (VolumetricShader, src/shaders.cpp:309-343) from the
 // group's MainShadow (`sh`, main light, volumetric light 0) and the predefined aux lights'
 // AuxShadow (`aux[i]`, volumetric lights 1-4); adds to out[0..3] in the reference's order.
@@ -495,6 +508,7 @@ struct VolSamples {
   const T *res;            // [WaveBufs::sample_nres][cap]
   const int32_t *iters;    // the pool records' itersOut (iteration fog)
   uint32_t cap, base;
+  int fakeRes;             // the orbit trap's result (fake lights): the last one
 };
 
 // Iteration fog at one step group (VolumetricShader, src/shaders.cpp:385-466): the fog colour
@@ -602,6 +616,17 @@ __device__ __forceinline__ void volumetric_affine(const ParamsT<T> &p, const Ste
       // the visible lights add to the colour: the map's offset
       T add[4] = {B0, B1, B2, alpha};
       visible_aux_lights<T>(p, rayStart + view * sb.scan[sb.at(index)], view, step, add);
+      B0 = add[0];
+      B1 = add[1];
+      B2 = add[2];
+      alpha = add[3];
+    }
+    if (EFX && p.fakeLights && sb.scan) {
+      Counters c2{0, 0, 0, 0};
+      int L;
+      const T r = compute<T, FORMULA, 5>(p.f, rayStart + view * sb.scan[sb.at(index)], p.f.N, L, c2, fparam_of(p.f));
+      T add[4] = {B0, B1, B2, alpha};
+      fake_light_glow<T>(p, r, step, add);
       B0 = add[0];
       B1 = add[1];
       B2 = add[2];
@@ -1268,12 +1293,12 @@ __device__ __forceinline__ void walk_groups(const ParamsT<T> &p, const PoolRecor
   }
 }
 
-// A step group the shadow stage traces from: every group with volumetric lights, those of
-// positive iteration-fog opacity (src/shaders.cpp:387-390) with iteration fog.
+// A step group the shadow stage traces from: every group with volumetric or fake lights, those
+// of positive iteration-fog opacity (src/shaders.cpp:387-390) with iteration fog.
 template <typename T>
 __device__ __forceinline__ bool group_has_sample(const ParamsT<T> &p, const int32_t *iters, const int64_t rec,
                                                  const T step) {
-  if (p.volLightAny) return true;
+  if (p.volLightAny || p.fakeLights) return true;
   return p.iterFog &&
          iter_opacity(step, T(iters[rec]), T(p.f.N), p.iterFogOpacityTrim, p.iterFogOpacity) > T(0);
 }
@@ -1485,7 +1510,7 @@ __device__ __forceinline__ T fog_thresh(const ParamsT<T> &p, const V3<T> point2,
 // after MainShadow is taken as the float threshold it starts from; CalculateDistance reads it
 // only in the minN clause (src/fractal.cpp:1291-1293), whose escape in the first iteration
 // gives a distance far above any threshold of these scenes.
-template <typename T>
+template <typename T, int FORMULA>
 __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const WaveBufs<T> &wb,
                                                     const FrameCam<T> *__restrict__ cams, const int ncams,
                                                     const unsigned int nh, const SecondaryJobs &jn,
@@ -1511,6 +1536,20 @@ __device__ __forceinline__ bool secondary_begin_efx(const ParamsT<T> &p, const W
     sample = true;
     const unsigned int r = q / jn.nSamples;
     si = q % jn.nSamples;
+    if (p.fakeLights && r == (unsigned int)wb.sample_nres - 1) {
+      // the fake lights' orbit trap at the group (src/shaders.cpp:298-307): no march
+      const int64_t ri = (int64_t)wb.sample_ray[si];
+      const int64_t gpx = pixel_of_ray(wb, ri);
+      const FrameCam<T> &cf = cams[frame_of_pixel(cams, ncams, gpx)];
+      const int64_t rec = (int64_t)wb.sample_rec[si];
+      V3<T> rs, rv;
+      ray_origin_view(p, cf, wb, ri, gpx, rs, rv);
+      Counters c2{0, 0, 0, 0};
+      int L;
+      wb.sample_res[(int64_t)r * wb.sample_cap + si] =
+          compute<T, FORMULA, 5>(p.f, rs + rv * record_scan(wb.pool_rec + 4 * rec), p.f.N, L, c2, cf.fparam);
+      return false;
+    }
     s.kind = r == 0 ? 0 : (r < (unsigned int)kSampleShadows ? 2 : 1);
     s.j = r == 0 ? 0u : (r < (unsigned int)kSampleShadows ? r - 1 : r - kSampleShadows);
     s.gp = (int64_t)wb.sample_ray[si];
@@ -1932,7 +1971,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
       const unsigned int job = claim_jobs(wb.ctl + 2, need);
       if (need) {
         if (stop || job >= njobs) exhausted = true;
-        else if constexpr (EFX) active = secondary_begin_efx<T>(p, wb, cams, ncams, nh, jn, job, s);
+        else if constexpr (EFX) active = secondary_begin_efx<T, FORMULA>(p, wb, cams, ncams, nh, jn, job, s);
         else active = secondary_begin<T>(p, wb, cams, ncams, nh, jn, job, s);
       }
     }
@@ -2011,8 +2050,10 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
     out[3] += glowOpacity;
     if (EFX && p.auxLightVisibility > T(0) && p.numberOfLights > 0)
       visible_aux_lights<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), view, step, out);
-    // the group's shadow-stage results (volumetric lights, iteration fog)
-    const bool sampled = EFX && (p.volLightAny || p.iterFog) && group_has_sample(p, vs.iters, rec, step);
+    // the group's shadow-stage results (fake and volumetric lights, iteration fog)
+    const bool sampled =
+        EFX && (p.volLightAny || p.iterFog || p.fakeLights) && group_has_sample(p, vs.iters, rec, step);
+    if (EFX && p.fakeLights) fake_light_glow<T>(p, vs.res[(int64_t)vs.fakeRes * vs.cap + group], step, out);
     if (EFX && p.volLightAny) {
       const T aux[4] = {vs.res[1 * (int64_t)vs.cap + group], vs.res[2 * (int64_t)vs.cap + group],
                         vs.res[3 * (int64_t)vs.cap + group], vs.res[4 * (int64_t)vs.cap + group]};
@@ -2120,14 +2161,11 @@ __device__ __forceinline__ void slow_normal_warp(const ParamsT<T> &p, const Wave
 
 // ---------------------------------------------------------------------------
 // Auxiliary lights at a hit (AuxLightsShader, src/shaders.cpp:997-1067), each weighed by its
-// AuxShadow from the shadow stage, added to ObjectShader's terms as src/shaders.cpp:98-107 does
-// (no fake lights on this engine: their terms are 0).
+// AuxShadow from the shadow stage: the diffuse and specular sums.
 template <typename T>
 __device__ __forceinline__ void aux_light_sums(const ParamsT<T> &p, const WaveBufs<T> &wb, const int64_t ri,
-                                            const V3<T> point, const V3<T> nrm, const V3<T> viewT,
-                                            const V3<T> colour, const T specT, const T shadow, T obj[3],
-                                            T spec[3]) {
-  T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
+                                               const V3<T> point, const V3<T> nrm, const V3<T> viewT, T aux[3],
+                                               T auxSpec[3]) {
   const int number = p.numberOfLights;
   for (int i = 0; i < number; i++) {
     const LightT<T> L = p.lights[i];
@@ -2147,12 +2185,39 @@ __device__ __forceinline__ void aux_light_sums(const ParamsT<T> &p, const WaveBu
       auxSpec[k] += sh2 * T(L.colour[k]) / T(65536);
     }
   }
-  const T col[3] = {colour.x, colour.y, colour.z};
-  for (int k = 0; k < 3; k++) {
-    obj[k] += (aux[k] + T(0)) * col[k];
-    spec[k] = auxSpec[k] + T(0) + p.mainLight[k] * specT * shadow;
-  }
 }
+
+// Fake (orbit trap) lights at a hit (FakeLights, src/shaders.cpp:1225-1271): the trap distance
+// and its gradient by forward differences of dist_thresh x smoothness give a light direction;
+// Lambert and Blinn terms of that light.
+template <typename T, int FORMULA>
+__device__ __forceinline__ void fake_light_terms(const ParamsT<T> &p, const V3<T> point, const V3<T> n,
+                                                 const V3<T> viewT, const T dist_thresh, const T fparam,
+                                                 Counters &cnt, T &fake, T &fakeSpec) {
+  const T dl = dist_thresh * p.smoothness;
+  int L;
+  const T rr = compute<T, FORMULA, 5>(p.f, point, p.f.N, L, cnt, fparam);
+  const T fakeLight = p.fakeLightsIntensity / rr;
+  const T r = T(1) / (rr + T(1e-30));
+  const T rx = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + dl, point.y + T(0), point.z + T(0)}, p.f.N, L, cnt,
+                                               fparam) + T(1e-30));
+  const T ry = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + dl, point.z + T(0)}, p.f.N, L, cnt,
+                                               fparam) + T(1e-30));
+  const T rz = T(1) / (compute<T, FORMULA, 5>(p.f, V3<T>{point.x + T(0), point.y + T(0), point.z + dl}, p.f.N, L, cnt,
+                                               fparam) + T(1e-30));
+  V3<T> fln{r - rx, r - ry, r - rz};
+  if (!(fln.x == T(0) && fln.y == T(0) && fln.z == T(0))) fln = normalize3(fln);
+  T fakeLight2 = fakeLight * dot3(n, fln);
+  if (fakeLight2 < T(0)) fakeLight2 = T(0);
+  fake = fakeLight2;
+  const V3<T> fh = normalize3(fln - viewT);
+  T fs = dot3(n, fh);
+  if (fs < T(0)) fs = T(0);
+  fs = m_pow(fs, T(30)) * fakeLight;
+  if (fs > T(15)) fs = T(15);
+  fakeSpec = fs;
+}
+
 
 // ObjectShader (src/shaders.cpp:21-112) at the hit of ray `ri` from the stages' results: the
 // normal (or the slow shading's, when `slowSum` is given), main light with its shadow and
@@ -2213,8 +2278,17 @@ __device__ __forceinline__ void shade_hit(const ParamsT<T> &p, const FrameCam<T>
   obj[0] = env * ambient.x + (a2x + p.mainLight[0] * shadeV * shadow) * colour.x;
   obj[1] = env * ambient.y + (a2y + p.mainLight[1] * shadeV * shadow) * colour.y;
   obj[2] = env * ambient.z + (a2z + p.mainLight[2] * shadeV * shadow) * colour.z;
-  if (EFX && p.numberOfLights > 0) {
-    aux_light_sums(p, wb, ri, h.point, nrm, viewT, colour, specT, shadow, obj, spec);
+  if (EFX && (p.numberOfLights > 0 || p.fakeLights)) {
+    // auxiliary and fake lights, added as ObjectShader does (src/shaders.cpp:98-107)
+    T aux[3] = {T(0), T(0), T(0)}, auxSpec[3] = {T(0), T(0), T(0)};
+    if (p.numberOfLights > 0) aux_light_sums(p, wb, ri, h.point, nrm, viewT, aux, auxSpec);
+    T fake = T(0), fakeSpec = T(0);
+    if (p.fakeLights) fake_light_terms<T, FORMULA>(p, h.point, nrm, viewT, h.thr, c.fparam, cnt, fake, fakeSpec);
+    const T col[3] = {colour.x, colour.y, colour.z};
+    for (int k = 0; k < 3; k++) {
+      obj[k] += (aux[k] + fake) * col[k];
+      spec[k] = auxSpec[k] + fakeSpec + p.mainLight[k] * specT * shadow;
+    }
   } else {
     // no auxiliary or fake lights: their specular terms are the reference's zeros
     for (int k = 0; k < 3; k++) spec[k] = T(0) + p.mainLight[k] * specT * shadow;
@@ -2321,7 +2395,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
           const V3<T> rayStart = d == 0 ? V3<T>{(T)c.start[0], (T)c.start[1], (T)c.start[2]}
                                         : V3<T>{(T)wb.ray_start[ri], (T)wb.ray_start[wb.npix + ri],
                                                 (T)wb.ray_start[2 * wb.npix + ri]};
-          const VolSamples<T> vs{wb.sample_res, wb.pool_iters, wb.sample_cap, wb.sample_ray ? wb.sample_base[ri] : 0u};
+          const VolSamples<T> vs{wb.sample_res, wb.pool_iters, wb.sample_cap, wb.sample_ray ? wb.sample_base[ri] : 0u,
+                                 wb.sample_nres - 1};
           volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, vs, res, totalOpacity, set);
         }
         result[0] = res[0];

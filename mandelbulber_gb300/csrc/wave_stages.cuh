@@ -13,9 +13,9 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   auto mark = [&](int k) {
     if (L.ev[0]) cudaEventRecord(L.ev[k], s);
   };
-  // the effects variant of the primary, shadow and composition stages: reflected rays or
-  // auxiliary lights
-  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0 || L.p.volLightAny || L.p.iterFog;
+  // the effects variant of the primary, shadow and composition stages: reflected rays,
+  // auxiliary, volumetric or fake lights, iteration fog
+  const bool efx = L.wb.rays > 1 || L.p.numberOfLights > 0 || L.p.volLightAny || L.p.iterFog || L.p.fakeLights;
   mark(0);
   // one primary pass (and FP64 polish) per ray depth of the reflection loop; between two
   // depths the reflect stage spawns the next depth's rays from this depth's hits
