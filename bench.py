@@ -420,14 +420,22 @@ def run_once(args) -> int:
     import mandelbulber_gb300 as mb
     from mandelbulber_gb300 import workloads as W
     w, h = (int(v) for v in args.once.lower().split("x"))
-    scene = W.workload(args.workload, w, h)
+    if args.fixture:
+        # a committed render fixture's scene (an effect scene) at this size
+        z = np.load(os.path.join(ROOT, "tests", "golden", f"render_{args.fixture}.npz"))
+        scene = mb.scene_from_bytes(z["scene"].tobytes())
+        scene.image_width, scene.image_height = w, h
+        scene.resolution = 1.0 / w / scene.noOfTiles
+    else:
+        scene = W.workload(args.workload, w, h)
     prec = mb.PREC_FP64 if args.precision == "fp64" else mb.PREC_FP32_FIX
     engine = mb.ENGINE_PER_PIXEL if args.engine == "per_pixel" else mb.ENGINE_WAVEFRONT
     with mb.Context(0) as ctx:
         for _ in range(args.warmup + 1):
             img = ctx.render(scene, precision=prec, engine=engine, pair_rays=int(args.pair_rays))
         st = ctx.stats()
-    print(json.dumps({"workload": args.workload, "size": [w, h], "precision": args.precision, "engine": args.engine,
+    print(json.dumps({"workload": args.fixture or args.workload, "size": [w, h], "precision": args.precision,
+                      "engine": args.engine,
                       "kernel_ms": st.kernel_ms, "orbit_iterations": st.orbit_iterations, "de_calls": st.de_calls,
                       "hit_fraction": float(img.hit.mean())}))
     return 0
@@ -502,6 +510,8 @@ def make_parser() -> argparse.ArgumentParser:
     ap.add_argument("--peaks", action="store_true", help="run the ALU peak and orbit-loop microbenchmarks and exit")
     ap.add_argument("--noise-floor", action="store_true",
                     help="measure the reference's jitter noise floor on the Mandelbulb configuration (CPU) and exit")
+    ap.add_argument("--fixture", default=None, metavar="NAME",
+                    help="with --once: the scene of tests/golden/render_NAME.npz (effect scenes) instead of --workload")
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "per_pixel"],
                     help="with --once: the render engine of the profiling case")
     return ap
