@@ -251,6 +251,10 @@ typedef struct mbgb_opts {
                                 * rays per thread whose orbits advance together in packed FP32 (f32x2)
                                 * instructions; 0 = one ray per thread (faster on GB300: 9.8 against
                                 * 12.1 ms on the 1080p Mandelbox). Same pixels either way */
+  int32_t hit_order;           /* wavefront, one ray per pixel (no reflections): the order of the shadow/AO
+                                * jobs over the hits. 2 = the primary rays' pixel-tile order (a tile's rays
+                                * share a warp), 1 = the order the primary rays finished in, 0 = tile order
+                                * from 2^20 pixels per launch group on. Same pixels either way */
 } mbgb_opts;
 
 /* Launch configuration picked by mbgb_autotune. */

@@ -162,7 +162,7 @@ def make_opts(precision: int = PREC_FP32_FIX, jitter: bool = False, jitter_seed:
               ctas_per_sm: int = 0, threads_per_cta: int = 0, deadline_ms: int = 0, stream: int = 0,
               engine: int = ENGINE_WAVEFRONT, profile_stages: bool = False, polish_all: bool = False,
               tile=None, refill_min: int = 0, autotune: bool = False, use_graph: bool = False,
-              exact_hit: bool = False, orbit_refill: int = 0, pair_rays: int = 0) -> mbgb_opts:
+              exact_hit: bool = False, orbit_refill: int = 0, pair_rays: int = 0, hit_order: int = 0) -> mbgb_opts:
     r0, r1 = rows if rows else (0, 0)
     tw, th = tile if tile else (0, 0)
     return mbgb_opts(precision=precision, jitter=int(jitter), jitter_seed=jitter_seed, row_begin=r0, row_end=r1,
@@ -170,7 +170,7 @@ def make_opts(precision: int = PREC_FP32_FIX, jitter: bool = False, jitter_seed:
                      stream=stream if stream else None, engine=engine, profile_stages=int(profile_stages),
                      polish_all=int(polish_all), tile_w=tw, tile_h=th, refill_min=refill_min,
                      autotune=int(autotune), use_graph=int(use_graph), exact_hit=int(exact_hit),
-                     orbit_refill=orbit_refill, pair_rays=pair_rays)
+                     orbit_refill=orbit_refill, pair_rays=pair_rays, hit_order=hit_order)
 
 
 _LAYERS = ["image_float", "zbuffer", "alpha", "opacity", "colour", "hit", "iters", "depth"]

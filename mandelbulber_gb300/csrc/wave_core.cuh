@@ -1355,6 +1355,83 @@ __global__ void __launch_bounds__(128) sample_kernel(const __grid_constant__ Par
   }
 }
 
+// The hit list in the primary jobs' tile order, for the shadow stage. The primary stage
+// appends hits as rays finish, which interleaves the ~300 K rays in flight from all over the
+// frame, so consecutive shadow and AO jobs would start far apart; in job order a warp's 32
+// jobs are the hits of one pixel tile (8 x 4 by default). A segment of kHitSeg primary jobs is
+// one block of kHitSegWarps warps, each warp 32 x 32 consecutive jobs: the count pass stores
+// each warp's hits, one block turns the counts into offsets, the scatter pass writes each
+// warp's hits in order at its offset. A hit is a job's pixel inside its frame's rendered rows
+// whose ray found the surface (the set the primary stage counted). `gp` returns the pixel.
+template <typename T>
+__device__ __forceinline__ bool pixel_hit(const WaveBufs<T> &wb, const FrameCam<T> *__restrict__ cams,
+                                          const int ncams, const int64_t job, int64_t &gp) {
+  const unsigned int nJobs = cams[ncams - 1].jobBase + cams[ncams - 1].jobCount;
+  if (job >= (int64_t)nJobs) return false;
+  const FrameCam<T> &c = cams[frame_of_job(cams, ncams, (unsigned int)job)];
+  int x, y;
+  job_pixel(c.width, c.row_begin, c.tileW, c.tileH, (unsigned int)job - c.jobBase, x, y);
+  if (x >= c.width || y >= c.row_end) return false;
+  gp = c.pixBase + (int64_t)y * c.width + x;
+  return (wb.flags[gp] & 1) != 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) hit_count_kernel(const WaveBufs<T> wb, const FrameCam<T> *__restrict__ cams,
+                                                        const int ncams) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t base = (int64_t)blockIdx.x * kHitSeg + (int64_t)warp * 1024;
+  unsigned int n = 0;
+  for (int k = 0; k < 32; k++) {
+    int64_t gp;
+    n += __popc(__ballot_sync(0xffffffffu, pixel_hit(wb, cams, ncams, base + k * 32 + lane, gp)));
+  }
+  if (lane == 0) wb.seg_count[(int64_t)blockIdx.x * kHitSegWarps + warp] = n;
+}
+
+// Exclusive prefix sum of the `n` warp counts in place (one block of 1024 threads; T is the
+// stage's precision, so that each instantiating unit has its own copy).
+template <typename T>
+__global__ void __launch_bounds__(1024) hit_scan_kernel(uint32_t *counts, const int64_t n) {
+  __shared__ uint32_t part[1024];
+  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t b = (int64_t)threadIdx.x * per, e = b + per < n ? b + per : n;
+  uint32_t sum = 0;
+  for (int64_t i = b; i < e; i++) sum += counts[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (unsigned int t = 0; t < blockDim.x; t++) {
+      const uint32_t v = part[t];
+      part[t] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  uint32_t run = part[threadIdx.x];
+  for (int64_t i = b; i < e; i++) {
+    const uint32_t v = counts[i];
+    counts[i] = run;
+    run += v;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) hit_scatter_kernel(const WaveBufs<T> wb, const FrameCam<T> *__restrict__ cams,
+                                                          const int ncams) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t off = wb.seg_count[(int64_t)blockIdx.x * kHitSegWarps + warp];
+  const int64_t base = (int64_t)blockIdx.x * kHitSeg + (int64_t)warp * 1024;
+  for (int k = 0; k < 32; k++) {
+    int64_t gp = 0;
+    const bool hit = pixel_hit(wb, cams, ncams, base + k * 32 + lane, gp);
+    const unsigned int m = __ballot_sync(0xffffffffu, hit);
+    if (hit) wb.hit_list[off + __popc(m & ((1u << lane) - 1u))] = (uint32_t)gp;
+    off += __popc(m);
+  }
+}
+
 // Between two reflection depths (one thread): the next depth's rays become the current ones,
 // the per-depth job, overflow and polish counters restart, the hit count so far is kept.
 template <typename T>

@@ -77,7 +77,13 @@ struct WaveBufs {
   int sample_nres;                       // results per sample
   int32_t *pool_iters;                   // [chunk * kChunk + r] itersOut at each record (iteration
                                          // fog; null without)
+  uint32_t *seg_count;                   // [segments][kHitSegWarps] hits per warp of each segment
+                                         // of kHitSeg primary jobs (hit list in tile order; null =
+                                         // kept in completion order)
 };
+
+constexpr int kHitSegWarps = 4;          // warps per segment of the hit-list compaction
+constexpr int kHitSeg = kHitSegWarps * 32 * 32;   // primary jobs per segment: 32 per lane
 
 constexpr int kSampleShadows = 5;        // MainShadow and the four predefined lights' AuxShadow
 
@@ -122,6 +128,7 @@ struct WaveLaunch {
   // after the gradient stage
   cudaEvent_t ev[kStageEvents];
   int grad_grid;     // blocks of the gradient stage
+  int64_t hit_jobs;  // primary jobs of the batch (the hit list's compaction walks them)
 };
 
 // Stage k adds its counters at io.counters + 4 * k.

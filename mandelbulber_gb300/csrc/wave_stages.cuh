@@ -46,6 +46,13 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
       dev::polish_kernel<F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, stage_io(L.io, 1), wbd, L.cams, L.ncams);
   }
   if (L.wb.rays > 1) mark(1);
+  // the hit list in tile order (one ray per pixel): a tile's shadow and AO rays share a warp
+  if (L.wb.seg_count) {
+    const int segs = (int)((L.hit_jobs + kHitSeg - 1) / kHitSeg);
+    dev::hit_count_kernel<T><<<segs, kHitSegWarps * 32, 0, s>>>(L.wb, L.cams, L.ncams);
+    dev::hit_scan_kernel<T><<<1, 1024, 0, s>>>(L.wb.seg_count, (int64_t)segs * kHitSegWarps);
+    dev::hit_scatter_kernel<T><<<segs, kHitSegWarps * 32, 0, s>>>(L.wb, L.cams, L.ncams);
+  }
   mark(2);
   if (L.wb.exact_hit)
     dev::level_set_kernel<T, F><<<L.polish_grid, L.block, 0, s>>>(L.p, L.fd, L.wb, L.cams, L.ncams);

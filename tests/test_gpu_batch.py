@@ -35,8 +35,9 @@ def test_flight_batch_equals_single_frames(gpu_ctx, flight_small):
     st = gpu_ctx.stats()
     assert st.frames == 64
     assert st.pixels == sum(f.image_width * f.image_height for f in flight_small)
-    # one launch sequence: primary, polish, secondary, compose
-    assert st.launches == 4, st.launches
+    # one launch sequence: primary, polish, secondary, compose, and from 2^20 pixels on the
+    # three launches that put the hit list in tile order
+    assert st.launches == 4 + (3 if st.pixels >= 1 << 20 else 0), st.launches
     for i in (0, 1, 7, 8, 31, 63):
         single = gpu_ctx.render(flight_small[i])
         _same(batch[i], single, f"frame {i}")
@@ -195,3 +196,25 @@ def test_pair_rays_do_not_change_pixels(gpu_ctx, size, extra):
     _same(one, two, f"pair rays {size} {extra}")
     assert st1.stage_orbit[2] == st2.stage_orbit[2] and st1.stage_de[2] == st2.stage_de[2]
     assert st2.stage_de[2] > 0
+
+
+@pytest.mark.parametrize("name,size,precision", [("mandelbox_1080p", (480, 270), mb.PREC_FP32_FIX),
+                                                 ("mandelbox_1080p", (320, 180), mb.PREC_FP64),
+                                                 ("mandelbulb_640x480", (320, 240), mb.PREC_FP32_FIX)])
+def test_hit_order_does_not_change_pixels(gpu_ctx, name, size, precision):
+    """The shadow stage's jobs in the primary rays' tile order (hit_order 2, the hit list
+    compacted) or in their completion order (1) give the same frame bit for bit, with the
+    same shadow-stage work; a row range keeps its rows' hits only."""
+    sc = W.workload(name, *size)
+    frames, work = [], []
+    for order in (1, 2):
+        frames.append(gpu_ctx.render(sc, precision=precision, hit_order=order, profile_stages=True))
+        st = gpu_ctx.stats()
+        work.append((st.stage_orbit[2], st.stage_de[2]))
+    _same(frames[0], frames[1], f"hit order {name} {size}")
+    assert work[0] == work[1] and work[0][1] > 0
+    rows = (size[1] // 3, size[1] // 2)
+    part = gpu_ctx.render(sc, precision=precision, hit_order=2, rows=rows)
+    full = frames[1]
+    np.testing.assert_array_equal(part.hit[rows[0]:rows[1]], full.hit[rows[0]:rows[1]])
+    np.testing.assert_array_equal(part.image_float[rows[0]:rows[1]], full.image_float[rows[0]:rows[1]])
