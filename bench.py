@@ -40,10 +40,10 @@ WORKLOAD = "mandelbox_1080p"
 # plus sqrt and divide of each DE evaluation
 FLOPS_PER_ITER = {8: 21, 2: 27}
 # dram__bytes_read.sum + dram__bytes_write.sum of secondary_kernel in one full 1920x1080
-# launch of this workload (a one-pass ncu capture of `bench.py --once 1920x1080`): 49.2 MB
-# read + 167.2 MB written, mostly the per-direction AO result slots, which outgrow L2 at
+# launch of this workload (a one-pass ncu capture of `bench.py --once 1920x1080`): 45.0 MB
+# read + 169.3 MB written, mostly the per-direction AO result slots, which outgrow L2 at
 # this size (at 480x270 they stay in L2, and a small capture sees almost no DRAM traffic)
-DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 216.4e6}
+DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 214.3e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
 PRECISION = "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement"
 # the single-frame workloads bench.py times (the scenes are built by mandelbulber_gb300.workloads;
@@ -432,7 +432,8 @@ def run_once(args) -> int:
     engine = mb.ENGINE_PER_PIXEL if args.engine == "per_pixel" else mb.ENGINE_WAVEFRONT
     with mb.Context(0) as ctx:
         for _ in range(args.warmup + 1):
-            img = ctx.render(scene, precision=prec, engine=engine, pair_rays=int(args.pair_rays))
+            img = ctx.render(scene, precision=prec, engine=engine, pair_rays=int(args.pair_rays),
+                             hit_order=args.hit_order)
         st = ctx.stats()
     print(json.dumps({"workload": args.fixture or args.workload, "size": [w, h], "precision": args.precision,
                       "engine": args.engine,
@@ -510,6 +511,8 @@ def make_parser() -> argparse.ArgumentParser:
     ap.add_argument("--peaks", action="store_true", help="run the ALU peak and orbit-loop microbenchmarks and exit")
     ap.add_argument("--noise-floor", action="store_true",
                     help="measure the reference's jitter noise floor on the Mandelbulb configuration (CPU) and exit")
+    ap.add_argument("--hit-order", type=int, default=0, choices=[0, 1, 2],
+                    help="with --once: opts.hit_order (0 automatic, 1 completion order, 2 tile order)")
     ap.add_argument("--fixture", default=None, metavar="NAME",
                     help="with --once: the scene of tests/golden/render_NAME.npz (effect scenes) instead of --workload")
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "per_pixel"],
