@@ -321,7 +321,8 @@ def grad_section(ctx, torch, dev, args) -> dict:
             "ms_per_batch": 1e3 * wall / steps, "device_ms_per_batch": e0.elapsed_time(e1) / steps,
             "grad_pixels": int(st.grad_pixels), "grad_skipped": int(st.grad_skipped),
             "launches_per_batch": int(st.launches), "finite": bool(np.isfinite(g).all()), "stage_ms": stage_ms,
-            "precision": "fp32 forward with fp64 level-set hits; fp64 derivative arithmetic",
+            "precision": "fp32 forward, fp32 level-set hits and dual-number orbits (fp64 for a sample whose "
+                         "tangents leave fp32's range or whose Newton step fails), fp64 shading algebra",
             "check": "tests/test_gpu_grad.py: adjoint vs central differences (h = 1e-4, FP64) within 1e-3"}
 
 

@@ -174,7 +174,19 @@ struct DV3 {
 
 template <typename T, int K>
 __device__ __forceinline__ Dual<T, K> dlength(const DV3<T, K> &v) {
-  return dsqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+  if constexpr (sizeof(T) == 4) {
+    // FP32: the tangent as (x/r) dx + (y/r) dy + (z/r) dz, without the squares' tangents
+    // 2 x dx, which leave FP32's range at an orbit's escape step (x ~ 1e16, dx ~ 1e35)
+    Dual<T, K> r;
+    r.v = m_sqrt(v.x.v * v.x.v + v.y.v * v.y.v + v.z.v * v.z.v);
+    const T inv = r.v > T(0) ? T(1) / r.v : T(0);
+    const T ux = v.x.v * inv, uy = v.y.v * inv, uz = v.z.v * inv;
+#pragma unroll
+    for (int k = 0; k < K; k++) r.d[k] = ux * v.x.d[k] + uy * v.y.d[k] + uz * v.z.d[k];
+    return r;
+  } else {
+    return dsqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+  }
 }
 
 // Compute<normal> of formula 2 (src/fractal.cpp:211-225) or formula 8 without rotations
@@ -199,6 +211,11 @@ __device__ __forceinline__ Dual<T, K> de_dual_seeded(const FractalT<T> &f, DV3<T
     const D p = fp;
     const D pm1 = p + T(-1);
     D r_dz = dconst<T, K>(T(1));
+    // FP32: the running derivative's tangents grow like r_dz^2 and leave FP32's range near
+    // the surface, so they are carried relative to r_dz (q = d r_dz / r_dz), which stays small
+    T rdz = T(1), q[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) q[k] = T(0);
     for (L = 0; L < N; L++) {
       const D th0 = dasin(z.z / r);
       const D ph0 = datan2(z.y, z.x);
@@ -208,12 +225,30 @@ __device__ __forceinline__ Dual<T, K> de_dual_seeded(const FractalT<T> &f, DV3<T
       D sth, cth, sph, cph;
       dsincos(th, sth, cth);
       dsincos(ph, sph, cph);
-      r_dz = rp * r_dz * p + T(1);
+      if constexpr (sizeof(T) == 4) {
+        // r_dz' = A r_dz + 1 with A = r^(p-1) p: d r_dz' / r_dz' = (dA + A q) r_dz / r_dz'
+        const D A = rp * p;
+        const T nv = A.v * rdz + T(1);
+        const T ratio = rdz / nv;
+#pragma unroll
+        for (int k = 0; k < K; k++) q[k] = (A.d[k] + A.v * q[k]) * ratio;
+        rdz = nv;
+      } else {
+        r_dz = rp * r_dz * p + T(1);
+      }
       rp = rp * r;
       z = {(cth * cph) * rp + c.x, (cth * sph) * rp + c.y, sth * rp + c.z};
       r = dlength(z);
       if (r.v > f.bailout) {
-        dist = (r * dlog(r)) * T(0.5) / r_dz;
+        if constexpr (sizeof(T) == 4) {
+          // dist = num / r_dz: d dist = d num / r_dz - dist q
+          const D num = (r * dlog(r)) * T(0.5);
+          dist.v = num.v / rdz;
+#pragma unroll
+          for (int k = 0; k < K; k++) dist.d[k] = num.d[k] / rdz - dist.v * q[k];
+        } else {
+          dist = (r * dlog(r)) * T(0.5) / r_dz;
+        }
         break;
       }
     }
@@ -300,6 +335,37 @@ __device__ __forceinline__ bool level_set_hit(const FractalT<double> &f, const V
     // the bisection window already brackets the root to a small fraction of thr
     const double lim = thr / sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
     if (fabs(dt) > lim) return false;
+    tt += dt;
+  }
+  return false;
+}
+
+// The same refinement in FP32 for the FP32 policy, on its own distance estimate and ray
+// (the march's): Newton steps until |F| <= 2e-5 thr, about FP32's resolution of an estimate
+// near the surface, which puts t within an ulp or two of the FP32 root. Returns false where
+// the FP64 refinement takes over.
+template <int FORMULA>
+__device__ __forceinline__ bool level_set_hit_f32(const FractalT<float> &f, const V3<float> o, const V3<float> d,
+                                                  const float k, const float thrConst, float &t, int &iters,
+                                                  const float fparam) {
+  float tt = t;
+  const float lenD = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+  for (int it = 0; it < 16; it++) {
+    int L;
+    const Dual<float, 1> de = de_along<float, FORMULA>(f, o + d * tt, d, f.N, L, fparam);
+    const float thr = k > 0.0f ? tt * k : thrConst;
+    if (L == f.N || L < f.minN || !isfinite(de.v) || !isfinite(de.d[0])) return false;
+    const float F = de.v - thr;
+    if (fabsf(F) <= 2e-5f * thr) {
+      t = tt;
+      iters = L;
+      return true;
+    }
+    const float Ft = de.d[0] - k;
+    if (!(Ft < 0.0f)) return false;
+    const float dt = -F / Ft;
+    // the bisection window already brackets the root to a small fraction of thr
+    if (fabsf(dt) > thr / lenD) return false;
     tt += dt;
   }
   return false;

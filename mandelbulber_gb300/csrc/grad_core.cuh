@@ -24,12 +24,34 @@
 namespace mbgb {
 namespace dev {
 
+// The distance estimate and its derivatives by the point and the fractal parameter, in the
+// policy's precision: FP32 dual orbits for the FP32 policy (the running derivative's
+// tangents carried relative to it, de_dual_seeded), FP64 for the FP64 policy; the shading
+// algebra after them runs in FP64 for both.
+template <typename T, int FORMULA>
+__device__ __forceinline__ Dual<double, 4> de_dual_policy(const ParamsT<T> &p, const FractalT<double> &fd,
+                                                          const V3<double> P, const int N, int &L, const T fparam,
+                                                          const double fparam_d) {
+  if constexpr (sizeof(T) == 4) {
+    const Dual<float, 4> r = de_dual<float, FORMULA>(p.f, V3<float>{(float)P.x, (float)P.y, (float)P.z}, N, L, fparam);
+    bool finite = isfinite(r.v);
+#pragma unroll
+    for (int k = 0; k < 4; k++) finite = finite && isfinite(r.d[k]);
+    // a tangent that left FP32's range: this sample in FP64
+    if (!finite) return de_dual<double, FORMULA>(fd, P, N, L, fparam_d);
+    Dual<double, 4> o;
+    o.v = (double)r.v;
+#pragma unroll
+    for (int k = 0; k < 4; k++) o.d[k] = (double)r.d[k];
+    return o;
+  } else {
+    return de_dual<double, FORMULA>(fd, P, N, L, fparam_d);
+  }
+}
+
 // One hit pixel: dI_c/dtheta_j into jac[3 * j + c]. Returns false for pixels that are not
 // differentiated (no hit, level set not reached, grazing ray, non-finite result).
-// The derivative arithmetic runs in FP64 for both policies: the tangents of an orbit grow
-// like its running derivative r_dz, which for orbits near the surface leaves FP32's range
-// (about 3e38) long before the orbit escapes. The forward state (hit point, threshold,
-// shadow, colour) is the policy's own.
+// The forward state (hit point, threshold, shadow, colour) is the policy's own.
 template <typename T, int FORMULA, bool FAST>
 __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const FractalT<double> &fd,
                                                const WaveBufs<T> &wb, const FrameCam<T> &c, const GradCam<T> &g,
@@ -48,9 +70,9 @@ __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const Fracta
   // The first sample of the normal is the distance at P with N x 5 iterations. An orbit that
   // escapes within N iterations is the same computation as the N-iteration estimate the
   // implicit differentiation needs, so that one is reused (one FP64 dual orbit less per pixel).
-  const Dual<double, 4> s1 = de_dual<double, FORMULA>(fd, P, fd.N5, L, c.fparam_d);
+  const Dual<double, 4> s1 = de_dual_policy<T, FORMULA>(p, fd, P, fd.N5, L, c.fparam, c.fparam_d);
   // implicit differentiation of the hit distance
-  const Dual<double, 4> de = L < fd.N ? s1 : de_dual<double, FORMULA>(fd, P, fd.N, L, c.fparam_d);
+  const Dual<double, 4> de = L < fd.N ? s1 : de_dual_policy<T, FORMULA>(p, fd, P, fd.N, L, c.fparam, c.fparam_d);
   const double Ft = de.d[0] * d.x + de.d[1] * d.y + de.d[2] * d.z - k;
   if (!(Ft < 0.0)) return false;
   double dt[kGradParams];
@@ -73,9 +95,12 @@ __device__ __forceinline__ bool pixel_jacobian(const ParamsT<T> &p, const Fracta
   const V3<T> PT{wb.point[0 * wb.npix + gp], wb.point[1 * wb.npix + gp], wb.point[2 * wb.npix + gp]};
   const V3<T> PxT{PT.x + dnT, PT.y, PT.z}, PyT{PT.x, PT.y + dnT, PT.z}, PzT{PT.x, PT.y, PT.z + dnT};
   const int N5 = fd.N5;
-  const Dual<double, 4> sx = de_dual<double, FORMULA>(fd, V3<double>{(double)PxT.x, P.y, P.z}, N5, L, c.fparam_d);
-  const Dual<double, 4> sy = de_dual<double, FORMULA>(fd, V3<double>{P.x, (double)PyT.y, P.z}, N5, L, c.fparam_d);
-  const Dual<double, 4> sz = de_dual<double, FORMULA>(fd, V3<double>{P.x, P.y, (double)PzT.z}, N5, L, c.fparam_d);
+  const Dual<double, 4> sx =
+      de_dual_policy<T, FORMULA>(p, fd, V3<double>{(double)PxT.x, P.y, P.z}, N5, L, c.fparam, c.fparam_d);
+  const Dual<double, 4> sy =
+      de_dual_policy<T, FORMULA>(p, fd, V3<double>{P.x, (double)PyT.y, P.z}, N5, L, c.fparam, c.fparam_d);
+  const Dual<double, 4> sz =
+      de_dual_policy<T, FORMULA>(p, fd, V3<double>{P.x, P.y, (double)PzT.z}, N5, L, c.fparam, c.fparam_d);
   const V3<double> gv{sx.v - s1.v, sy.v - s1.v, sz.v - s1.v};
   const double glen = sqrt(gv.x * gv.x + gv.y * gv.y + gv.z * gv.z);
   V3<double> n{1.0, 0.0, 0.0};

@@ -1046,6 +1046,9 @@ template <int FORMULA, bool FAST>
 __global__ void __launch_bounds__(128) polish_kernel(const __grid_constant__ ParamsT<float> p, const __grid_constant__ FractalT<double> fd,
                                                      const FrameIO io, const WaveBufs<float> wb,
                                                      const FrameCam<float> *__restrict__ cams, const int ncams) {
+  // exact_hit: every hit is on the polish list for the level-set stage, which refines it
+  // from the FP32 bisection (in FP32, FP64 where that fails): no FP64 bisection here
+  if (wb.exact_hit) return;
   const unsigned int nh = *(volatile unsigned int *)&wb.ctl[6];
   Counters cnt{0, 0, 0, 0};
   const double search_limit = 1.0 - 0.01 * p.quality_d;
@@ -1130,6 +1133,27 @@ __global__ void __launch_bounds__(128) level_set_kernel(const __grid_constant__ 
     const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, gp)];
     const int64_t local = gp - c.pixBase;
     const int x = (int)(local % c.width), y = (int)(local / c.width);
+    if constexpr (sizeof(T) == 4) {
+      // FP32 policy: Newton in FP32 on the march's own ray; FP64 only where that fails
+      V3<float> dirf;
+      camera_dir(p, c, x, y, dirf);
+      const V3<float> startf{(float)c.start[0], (float)c.start[1], (float)c.start[2]};
+      const float kf = p.constantDEThreshold ? 0.0f : c.resolution * c.persp / p.quality;
+      float tf = wb.scan[gp];
+      int lf = wb.iters[gp];
+      if (level_set_hit_f32<FORMULA>(p.f, startf, dirf, kf, p.quality, tf, lf, c.fparam)) {
+        const float thr = p.constantDEThreshold ? p.quality : tf * kf;
+        const V3<float> point = startf + dirf * tf;
+        wb.scan[gp] = tf;
+        wb.dist[gp] = thr;
+        wb.thr[gp] = thr;
+        wb.iters[gp] = lf;
+        wb.point[0 * wb.npix + gp] = point.x;
+        wb.point[1 * wb.npix + gp] = point.y;
+        wb.point[2 * wb.npix + gp] = point.z;
+        continue;
+      }
+    }
     V3<double> dir;
     camera_ray(p, c, x, y, dir);
     const V3<double> start{c.start[0], c.start[1], c.start[2]};
