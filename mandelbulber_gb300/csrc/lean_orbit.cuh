@@ -61,6 +61,41 @@ __device__ __forceinline__ float box_iteration(const LeanBoxK &k, const float s,
   return norm2_rn(x, y, z);
 }
 
+// The lean Mandelbox orbit of (x, y, z) with constant c, at most N iterations: returns the
+// distance estimate r / |dr| at the first iteration whose radius passes the bailout
+// (r^2 > 1024^2), with that iteration's index in L, or 0 with L = N when the orbit stays
+// bounded. The iterations run in blocks of kBoxBlock, each followed by its bailout test,
+// and the iteration count is tested once per block (a remainder loop takes N mod
+// kBoxBlock), so the loop spends no instructions on the count inside a block.
+constexpr int kBoxBlock = 5;
+
+__device__ __forceinline__ float box_orbit(const LeanBoxK &k, const float s, const float skm1, float x, float y,
+                                           float z, const float cx, const float cy, const float cz, const int N,
+                                           int &L) {
+  float dr = 1.0f;
+  int l = 0;
+  for (; l <= N - kBoxBlock; l += kBoxBlock) {
+#pragma unroll
+    for (int u = 0; u < kBoxBlock; u++) {
+      const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
+      if (r2 > 1048576.0f) {
+        L = l + u;
+        return box_bailout_dist(r2, dr);
+      }
+    }
+  }
+#pragma unroll 1
+  for (; l < N; l++) {
+    const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
+    if (r2 > 1048576.0f) {
+      L = l;
+      return box_bailout_dist(r2, dr);
+    }
+  }
+  L = N;
+  return 0.0f;
+}
+
 // ---- Packed FP32 (f32x2): two orbits per thread ----
 // A pair of floats in one 64-bit register pair: low half = ray A, high half = ray B. The
 // f32x2 add / mul / fma each round both halves exactly as the scalar .rn instructions do,

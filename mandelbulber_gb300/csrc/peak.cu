@@ -14,7 +14,8 @@ namespace {
 using mbgb::dev::LeanBoxK;
 
 // Orbits of points near the origin (inside the scale-2 Mandelbox, so no lane leaves early),
-// n iterations each with the bailout test evaluated every iteration as in the renderer.
+// n iterations each through the renderer's orbit loop (box_orbit: the bailout test after
+// every iteration, the count test once per block).
 __global__ void box_orbit_loop(float *out, unsigned long long *count, int orbits, int n, LeanBoxK k, float s,
                                float skm1) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -23,15 +24,10 @@ __global__ void box_orbit_loop(float *out, unsigned long long *count, int orbits
   for (int o = 0; o < orbits; o++) {
     const float cx = 1e-4f * (float)((tid + 7 * o) & 1023), cy = 1e-4f * (float)((tid * 3 + o) & 1023),
                 cz = 1e-4f * (float)((tid * 5 + 3 * o) & 1023);
-    float x = cx, y = cy, z = cz, dr = 1.0f;
     int L;
-#pragma unroll 5
-    for (L = 0; L < n; L++) {
-      const float r2 = mbgb::dev::box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
-      if (r2 > 1048576.0f) break;
-    }
+    const float d = mbgb::dev::box_orbit(k, s, skm1, cx, cy, cz, cx, cy, cz, n, L);
     it += (unsigned long long)(L + 1);
-    acc += x + y + z + dr;
+    acc += d + (float)L;
   }
   if (acc == -1.2345f) out[tid] = acc;  // keeps the orbits live
   atomicAdd(count, it);

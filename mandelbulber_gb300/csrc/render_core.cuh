@@ -244,20 +244,11 @@ __device__ __forceinline__ float mandelbox_fast(const FractalT<float> &f, const 
   const float skm1 = __fmul_rn(s, k.km1);
   const float cx = __fmul_rn(px, f.constantFactor), cy = __fmul_rn(py, f.constantFactor),
               cz = __fmul_rn(pz, f.constantFactor);
-  float x = px, y = py, z = pz, dr = 1.0f, dist = 0.0f;
   int L;
-#pragma unroll 5
-  for (L = 0; L < N; L++) {
-    const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
-    if (r2 > 1048576.0f) {
-      dist = box_bailout_dist(r2, dr);
-      break;
-    }
-  }
+  const float dist = box_orbit(k, s, skm1, px, py, pz, cx, cy, cz, N, L);
   cnt.orbit += (unsigned long long)(L + 1);
   cnt.calls += 1;
   Lout = L;
-  if (L == N) dist = 0.0f;
   return dist;
 }
 
