@@ -547,6 +547,18 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   rgb(p.fogCol1, s.fogColour1);
   rgb(p.fogCol2, s.fogColour2);
   rgb(p.fogCol3, s.fogColour3);
+  p.fogInvC1Dist = (T)(1.0 / s.fogColour1Distance);
+  p.fogInvC2Dist = (T)(1.0 / s.fogColour2Distance);
+  p.fogInvVisibility = (T)(1.0 / (double)p.fogVisibility);
+  p.fogDistFactor2 = p.fogDistFactor * p.fogDistFactor;
+  for (int c = 0; c < 3; c++) {
+    p.glowCol1[c] = (T)p.glow1[c] / (T)65536;
+    p.glowCol2[c] = (T)p.glow2[c] / (T)65536;
+    p.fogColorS[c] = (T)p.fogColor[c] / (T)65536;
+    p.fogCol1S[c] = (T)p.fogCol1[c] / (T)65536;
+    p.fogCol2S[c] = (T)p.fogCol2[c] / (T)65536;
+    p.fogCol3S[c] = (T)p.fogCol3[c] / (T)65536;
+  }
   p.auxLightNumber = s.auxLightNumber > 0 ? s.auxLightNumber : 0;
   p.numberOfLights = uses_aux_lights(s) ? std::max(p.auxLightNumber, 4) : 0;
   p.auxLightIntensity = (T)s.auxLightIntensity;

@@ -303,11 +303,46 @@ __device__ __forceinline__ void load_record(const double *r, double &dist, doubl
 __device__ __forceinline__ float record_scan(const float *r) { return r[3]; }
 __device__ __forceinline__ double record_scan(const double *r) { return r[3]; }
 
+// The narrow record of the plain variant: distance and threshold only (8 or 16 bytes). The
+// walk recomputes each record's step from the record before it (march_step), as the march
+// formed it, and reads no march position.
+__device__ __forceinline__ void store_record_narrow(float *r, const float dist, const float thr) {
+  *reinterpret_cast<float2 *>(r) = make_float2(dist, thr);
+}
+__device__ __forceinline__ void store_record_narrow(double *r, const double dist, const double thr) {
+  *reinterpret_cast<double2 *>(r) = make_double2(dist, thr);
+}
+__device__ __forceinline__ void load_record_narrow(const float *r, float &dist, float &thr) {
+  const float2 q = *reinterpret_cast<const float2 *>(r);
+  dist = q.x; thr = q.y;
+}
+__device__ __forceinline__ void load_record_narrow(const double *r, double &dist, double &thr) {
+  const double2 q = *reinterpret_cast<const double2 *>(r);
+  dist = q.x; thr = q.y;
+}
+
+// The march's next step after the estimate `dist` at threshold `thr` of march step i
+// (src/Render3D.cpp:129-137): the distance clamped at 3, less stepFrac thresholds, times the
+// DE factor, with the step jitter when it is on. One function for the march and for the
+// volumetric walk's recomputation, so that both round alike (the FP32 form spells out its
+// multiply-add).
+template <typename T>
+__device__ __forceinline__ T march_step(const ParamsT<T> &p, T dist, const T thr, const T stepFrac,
+                                        const uint32_t pixel, const uint32_t i) {
+  if (dist > T(3)) dist = T(3);
+  T step;
+  if constexpr (sizeof(T) == 4) step = __fmul_rn(__fmaf_rn(-stepFrac, thr, dist), p.DE_factor);
+  else step = (dist - stepFrac * thr) * p.DE_factor;
+  if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, pixel, i)) / T(10000));
+  return step;
+}
+
 // Backward walk over a ray's pooled records: record `index` of a chain whose last chunk
 // holds the records from kChunk * (nchunks - 1) on.
 template <typename T>
 struct PoolRecords {
-  const T *rec;            // [chunk * kChunk + r][4]: dist, thr, step, scan
+  const T *rec;            // [chunk * kChunk + r][W]: W = 4 (dist, thr, step, scan; effects
+                           // variant) or 2 (dist, thr; plain variant)
   const int32_t *prev;
   int32_t last;      // chunk holding the last written record
   int lastRec;       // index of the last written record: buffCount for a hit (its hit step
@@ -317,11 +352,11 @@ struct PoolRecords {
 // The walk's next chunk (toward the ray's start) and that chunk's link, requested into L2
 // while the walk reads the current chunk: the backward walk is otherwise one dependent miss
 // per chunk and one miss per 128-byte line.
-template <typename T>
+template <int W = 4, typename T>
 __device__ __forceinline__ void prefetch_chunk(const PoolRecords<T> &pr, const int32_t chunk) {
   if (chunk < 0) return;
-  const char *b = reinterpret_cast<const char *>(pr.rec + (int64_t)4 * kChunk * chunk);
-  for (int o = 0; o < 4 * kChunk * (int)sizeof(T); o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(b + o));
+  const char *b = reinterpret_cast<const char *>(pr.rec + (int64_t)W * kChunk * chunk);
+  for (int o = 0; o < W * kChunk * (int)sizeof(T); o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(b + o));
   asm volatile("prefetch.global.L2 [%0];" ::"l"(pr.prev + chunk));
 }
 
@@ -921,8 +956,9 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             }
             rec = (int64_t)chunk * kChunk + (i % kChunk);
             // the record's step slot holds the step that reached this point; the walk
-            // never reads it for the hit record
-            store_record(wb.pool_rec + 4 * rec, dist, thr, step, scan);
+            // never reads it for the hit record. The plain variant stores the narrow record.
+            if constexpr (EFX) store_record(wb.pool_rec + 4 * rec, dist, thr, step, scan);
+            else store_record_narrow(wb.pool_rec + 2 * rec, dist, thr);
             if constexpr (EFX) {
               if (wb.pool_iters) wb.pool_iters[rec] = iters;
             }
@@ -940,8 +976,7 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 8 : 6) primary
             sb.step[sb.at(i)] = step;
             if (sb.scan) sb.scan[sb.at(i)] = scan;
           }
-          step = (dist - stepFrac * thr) * p.DE_factor;
-          if (p.jitter) step = step * (T(1) - T(jitter1000(p.jitter_seed, (uint32_t)gp, (uint32_t)i)) / T(10000));
+          step = march_step(p, dist, thr, stepFrac, (uint32_t)gp, (uint32_t)i);
           buffCount++;
           scan += step;
           i++;
@@ -2129,8 +2164,8 @@ __global__ void __launch_bounds__(128) secondary_kernel(const __grid_constant__ 
 template <typename T, bool EFX>
 __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolRecords<T> &pr, const int stepCount,
                                                 const T depth, const V3<T> rayStart, const V3<T> view,
-                                                const VolSamples<T> vs, T out[4], float &totalOpacityOut,
-                                                bool &opacitySet) {
+                                                const VolSamples<T> vs, const uint32_t pixel, T out[4],
+                                                float &totalOpacityOut, bool &opacitySet) {
   uint32_t group = vs.base;
   float totalOpacity = 0.0f;
   const T glow = T(stepCount) * p.glowIntensity / T(512) * p.DE_factor;
@@ -2140,26 +2175,54 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
   const T glowG = (T(p.glow1[1]) * glowN + T(p.glow2[1]) * glow) / T(65536);
   const T glowB = (T(p.glow1[2]) * glowN + T(p.glow2[2]) * glow) / T(65536);
   const T fogIntensity = p.fogDensity;
+  // The FP32 policy's plain variant forms the group terms with the host's reciprocals and
+  // pre-scaled colours and with approximate quotients (__fdividef) where the divisor varies:
+  // a few ulp of the group's opacities, against five correctly rounded divisions per group.
+  constexpr bool kFastTerms = sizeof(T) == 4 && !EFX;
+  const T glowPerDepth = kFastTerms ? glow / depth : T(0);
   T totalStep = T(0);
+  // records of W values: the effects variant's (dist, thr, step, scan), the plain variant's
+  // narrow (dist, thr), whose step the walk recomputes from the record before
+  constexpr int W = EFX ? 4 : 2;
+  const T stepFrac = p.f.interiorMode ? T(0.8) : T(0.5);
   int32_t chunk = pr.last;
   int chunkBase = (pr.lastRec / kChunk) * kChunk;   // first record index of `chunk`
   int32_t link = (stepCount > 1 && chunk >= 0) ? pr.prev[chunk] : -1;   // the chunk before `chunk`
-  prefetch_chunk(pr, link);
-  for (int index = stepCount - 1; index > 0; index--) {
-    while (index < chunkBase) {
+  prefetch_chunk<W>(pr, link);
+  // the chunk holding record `at` (the walk only moves toward the ray's start)
+  auto seek = [&](const int at) -> int64_t {
+    while (at < chunkBase) {
       chunk = link;
       chunkBase -= kChunk;
       link = pr.prev[chunk];
-      prefetch_chunk(pr, link);
+      prefetch_chunk<W>(pr, link);
     }
-    const int64_t rec = (int64_t)chunk * kChunk + (index - chunkBase);
+    return (int64_t)chunk * kChunk + (at - chunkBase);
+  };
+  T curDist = T(0), curThr = T(0);   // narrow records: record `index`, read the turn before
+  if (!EFX && stepCount > 1) load_record_narrow(pr.rec + 2 * seek(stepCount - 1), curDist, curThr);
+  for (int index = stepCount - 1; index > 0; index--) {
     T distance, dist_thresh, step;
-    load_record(pr.rec + 4 * rec, distance, dist_thresh, step);
+    int64_t rec;
+    if constexpr (EFX) {
+      rec = seek(index);
+      load_record(pr.rec + 4 * rec, distance, dist_thresh, step);
+    } else {
+      // the step that reached record `index` is the march's step after record index - 1
+      rec = seek(index - 1);
+      T prevDist, prevThr;
+      load_record_narrow(pr.rec + 2 * rec, prevDist, prevThr);
+      step = march_step(p, prevDist, prevThr, stepFrac, pixel, (uint32_t)(index - 1));
+      distance = curDist;
+      dist_thresh = curThr;
+      curDist = prevDist;
+      curThr = prevThr;
+    }
     totalStep += step;
     if (totalStep < dist_thresh * p.quality) continue;
     step = totalStep;
     totalStep = T(0);
-    const T glowOpacity = glow * step / depth;
+    const T glowOpacity = kFastTerms ? step * glowPerDepth : glow * step / depth;
     out[0] = glowOpacity * glowR + (T(1) - glowOpacity) * out[0];
     out[1] = glowOpacity * glowG + (T(1) - glowOpacity) * out[1];
     out[2] = glowOpacity * glowB + (T(1) - glowOpacity) * out[2];
@@ -2176,15 +2239,34 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
       volumetric_light_terms<T>(p, rayStart + view * record_scan(pr.rec + 4 * rec), step, vs.res[group], aux, out);
     }
     if (p.postFog) {
-      T fogDensity = step / p.fogVisibility;
+      T fogDensity = kFastTerms ? step * p.fogInvVisibility : step / p.fogVisibility;
       if (fogDensity > T(1)) fogDensity = T(1);
-      out[0] = fogDensity * T(p.fogColor[0]) / T(65536) + (T(1) - fogDensity) * out[0];
-      out[1] = fogDensity * T(p.fogColor[1]) / T(65536) + (T(1) - fogDensity) * out[1];
-      out[2] = fogDensity * T(p.fogColor[2]) / T(65536) + (T(1) - fogDensity) * out[2];
+      if constexpr (kFastTerms) {
+        for (int c = 0; c < 3; c++) out[c] = fogDensity * p.fogColorS[c] + (T(1) - fogDensity) * out[c];
+      } else {
+        out[0] = fogDensity * T(p.fogColor[0]) / T(65536) + (T(1) - fogDensity) * out[0];
+        out[1] = fogDensity * T(p.fogColor[1]) / T(65536) + (T(1) - fogDensity) * out[1];
+        out[2] = fogDensity * T(p.fogColor[2]) / T(65536) + (T(1) - fogDensity) * out[2];
+      }
       totalOpacity = (float)(fogDensity + (T(1) - fogDensity) * (T)totalOpacity);
       out[3] = fogDensity + (T(1) - fogDensity) * out[3];
     }
-    if (fogIntensity > T(0)) {
+    if (kFastTerms && fogIntensity > T(0)) {
+      const float densityTemp =
+          __fdividef((float)step * (float)p.fogDistFactor, fmaf((float)distance, (float)distance, (float)p.fogDistFactor2));
+      const float k = fminf((float)distance * (float)p.fogInvC1Dist, 1.0f);
+      const float k2 = fminf((float)distance * (float)p.fogInvC2Dist * k, 1.0f);
+      const float kn = 1.0f - k, kn2 = 1.0f - k2;
+      const float fi = (float)fogIntensity * densityTemp;
+      const float fogDensity = fminf(__fdividef(0.3f * fi, 1.0f + fi), 1.0f);
+      const float keep = 1.0f - fogDensity;
+      for (int c = 0; c < 3; c++) {
+        const float fc = ((float)p.fogCol1S[c] * kn + (float)p.fogCol2S[c] * k) * kn2 + (float)p.fogCol3S[c] * k2;
+        out[c] = (T)(fogDensity * fc + keep * (float)out[c]);
+      }
+      totalOpacity = fogDensity + keep * totalOpacity;
+      out[3] = (T)(fogDensity + keep * (float)out[3]);
+    } else if (fogIntensity > T(0)) {
       const T fogReduce = p.fogDistFactor;
       const T densityTemp = (step * fogReduce) / (distance * distance + fogReduce * fogReduce);
       T k = distance / p.fogC1Dist;
@@ -2513,7 +2595,8 @@ __global__ void __launch_bounds__(128, (FAST && sizeof(T) == 4) ? 10 : 1) compos
                                                 (T)wb.ray_start[2 * wb.npix + ri]};
           const VolSamples<T> vs{wb.sample_res, wb.pool_iters, wb.sample_cap, wb.sample_ray ? wb.sample_base[ri] : 0u,
                                  wb.sample_nres - 1};
-          volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, vs, res, totalOpacity, set);
+          volumetric_pool<T, EFX>(p, pr, count, wb.scan[ri], rayStart, viewT, vs, (uint32_t)gp, res, totalOpacity,
+                                  set);
         }
         result[0] = res[0];
         result[1] = res[1];

@@ -38,7 +38,8 @@ struct WaveBufs {
   // Step records of the primary rays: chunks of kChunk records linked backwards
   // (prev), allocated by bump counter; the pixel keeps its last chunk.
   T *pool_rec;                           // [chunk * kChunk + r][4]: dist, thr, step, scan
-                                         // (one 16- or 32-byte record: one store, one load)
+                                         // (effects variant: one 16- or 32-byte record), or
+                                         // [chunk * kChunk + r][2]: dist, thr (plain variant)
   int32_t *pool_prev;                    // [chunk]
   int32_t *last_chunk;                   // [npix], -1 = no records
   uint32_t pool_cap;                     // chunks
