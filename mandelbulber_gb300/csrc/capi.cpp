@@ -1057,7 +1057,7 @@ static LaunchCfg resolve_cfg(const mbgb_context *c, const mbgb_opts &o, const mb
 struct WaveLayout {
   size_t flags, scan, dist, thr, step, detail, bis, point, iters, count, vol, shadow, ao, hit, pol, ovl, last;
   size_t prec, pprev;
-  size_t rstart, rdir, rthr, rlist, normal, auxsh, sbase, sray, srec, sstep, sres, piters, segc;
+  size_t rstart, rdir, rthr, rlist, normal, auxsh, sbase, sray, srec, sstep, sres, piters, segc, hset;
   uint32_t poolCap;
   size_t total;
 };
@@ -1118,6 +1118,7 @@ static WaveLayout wave_layout(int64_t npixFrame, size_t ts, int aoN, bool needVo
   w.sres = take(samples * (size_t)sampleRes * ts);
   w.piters = take(iterFog && needVol ? (size_t)w.poolCap * kChunk * 4 : 0);
   w.segc = take(rays == 1 ? (size_t)((jobs + kHitSeg - 1) / kHitSeg) * kHitSegWarps * 4 : 0);
+  w.hset = take(rays == 1 ? (size_t)npix * 8 * ts : 0);
   w.total = off;
   return w;
 }
@@ -1247,6 +1248,12 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
     L.p.lights = (const LightT<T> *)(prec == 0 ? c->lights64.ptr : c->lights32.ptr) + lightOff;
   else if (auxN > 0)
     return set_error(MBGB_ERR_CUDA, "auxiliary lights were not placed");
+  // the plain variant's per-hit shadow/AO set-up (hit_setup_kernel), formed once per hit in
+  // hit-list order; the effects variant sets its jobs up itself. Decided with the same test
+  // as the device's launch sequence.
+  const bool efx = rays > 1 || L.p.numberOfLights > 0 || L.p.volLightAny || L.p.iterFog || L.p.fakeLights;
+  const bool secondaryJobs = scene.shadow != 0 || rayAO;
+  wb.hit_setup = (!efx && rays == 1 && secondaryJobs) ? (T *)(base + w.hset) : nullptr;
   cudaError_t e;
   if constexpr (sizeof(T) == 8) e = launch_wave_f64(L, s);
   else e = launch_wave_f32(L, s);
@@ -1255,6 +1262,7 @@ static mbgb_status enqueue_wave(mbgb_context *c, const mbgb_scene *scenes, const
   // counter kernels
   *launches += 2 + (int64_t)rays * (1 + (needVol ? 1 : 0) + (prec == 1 ? 1 : 0)) + 2 * (int64_t)(rays - 1) +
                (wb.normal ? 1 : 0) + (wb.sample_ray ? 1 : 0) + (wb.seg_count ? 3 : 0) + (wb.exact_hit ? 1 : 0) +
+               (wb.hit_setup ? 1 : 0) +
                (grad ? 1 : 0);
   return MBGB_OK;
 }

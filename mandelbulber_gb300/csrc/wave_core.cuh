@@ -1337,6 +1337,61 @@ __global__ void __launch_bounds__(128) normal_kernel(const __grid_constant__ Par
   }
 }
 
+// The shadow/AO set-up of one hit (plain variant): the hit point, its threshold, the AO and
+// shadow marches' start (delta, shadow start) and end (delta / resolution, and the shadow's
+// factor: delta / resolution when penetrating, else the view distance), as
+// MainShadow and AmbientOcclusion form them (src/shaders.cpp:480-570, 572-640).
+template <typename T>
+struct HitSetup {
+  V3<T> point;
+  T thr, delta, aoEnd, shadowEnd, shadowStart;
+};
+__device__ __forceinline__ void store_hit_setup(float *q, const HitSetup<float> &h) {
+  reinterpret_cast<float4 *>(q)[0] = make_float4(h.point.x, h.point.y, h.point.z, h.thr);
+  reinterpret_cast<float4 *>(q)[1] = make_float4(h.delta, h.aoEnd, h.shadowEnd, h.shadowStart);
+}
+__device__ __forceinline__ void store_hit_setup(double *q, const HitSetup<double> &h) {
+  reinterpret_cast<double2 *>(q)[0] = make_double2(h.point.x, h.point.y);
+  reinterpret_cast<double2 *>(q)[1] = make_double2(h.point.z, h.thr);
+  reinterpret_cast<double2 *>(q)[2] = make_double2(h.delta, h.aoEnd);
+  reinterpret_cast<double2 *>(q)[3] = make_double2(h.shadowEnd, h.shadowStart);
+}
+__device__ __forceinline__ HitSetup<float> load_hit_setup(const float *q) {
+  const float4 a = reinterpret_cast<const float4 *>(q)[0], b = reinterpret_cast<const float4 *>(q)[1];
+  return HitSetup<float>{{a.x, a.y, a.z}, a.w, b.x, b.y, b.z, b.w};
+}
+__device__ __forceinline__ HitSetup<double> load_hit_setup(const double *q) {
+  const double2 a = reinterpret_cast<const double2 *>(q)[0], b = reinterpret_cast<const double2 *>(q)[1];
+  const double2 c = reinterpret_cast<const double2 *>(q)[2], d = reinterpret_cast<const double2 *>(q)[3];
+  return HitSetup<double>{{a.x, a.y, b.x}, b.y, c.x, c.y, d.x, d.y};
+}
+template <typename T>
+__device__ __forceinline__ HitSetup<T> hit_setup(const ParamsT<T> &p, const FrameCam<T> &c, const WaveBufs<T> &wb,
+                                                 const int64_t ri) {
+  const HitInfo<T> h = hit_info(p, c, wb, ri);
+  HitSetup<T> q;
+  q.point = h.point;
+  q.thr = h.thr;
+  q.delta = h.delta;
+  q.aoEnd = h.delta / c.resolution;
+  q.shadowEnd = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
+  q.shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
+  return q;
+}
+
+// Plain variant: every hit's shadow/AO set-up in hit-list order, so that a job reads its
+// hit's with two coalesced vector loads (the shadow stage claims its jobs in this order).
+template <typename T>
+__global__ void __launch_bounds__(128) hit_setup_kernel(const __grid_constant__ ParamsT<T> p, const WaveBufs<T> wb,
+                                                        const FrameCam<T> *__restrict__ cams, const int ncams) {
+  const unsigned int nh = *(volatile unsigned int *)&wb.ctl[1];
+  for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += gridDim.x * blockDim.x) {
+    const int64_t ri = (int64_t)wb.hit_list[k];
+    const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, pixel_of_ray(wb, ri))];
+    store_hit_setup(wb.hit_setup + (int64_t)8 * k, hit_setup(p, c, wb, ri));
+  }
+}
+
 // Volumetric lights and iteration fog: the step groups of every ray that the volumetric walk
 // lights (records summed far to near until the sum reaches thr x quality,
 // src/shaders.cpp:198-205; group_has_sample), each ray's samples contiguous and in the walk's
@@ -1795,23 +1850,26 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
                                                 const FrameCam<T> *__restrict__ cams, const int ncams,
                                                 const unsigned int nh, const SecondaryJobs &jn,
                                                 const unsigned int job, SecondaryRay<T> &s) {
+  unsigned int k;   // the job's entry of the hit list
   if (job < jn.nShadow) {
     s.kind = 0;
-    s.gp = (int64_t)wb.hit_list[job];
+    k = job;
   } else if (job < jn.nShadow + jn.nAO) {
     const unsigned int q = job - jn.nShadow;
     s.kind = 1;
     s.j = q / nh;
-    s.gp = (int64_t)wb.hit_list[q % nh];
+    k = q - s.j * nh;
   } else {
     const unsigned int q = job - jn.nShadow - jn.nAO;
     s.kind = 2;
     s.j = q / nh;
-    s.gp = (int64_t)wb.hit_list[q % nh];
+    k = q - s.j * nh;
   }
+  s.gp = (int64_t)wb.hit_list[k];
   const int64_t px = pixel_of_ray(wb, s.gp);
   const FrameCam<T> &c = cams[frame_of_pixel(cams, ncams, px)];
-  const HitInfo<T> h = hit_info(p, c, wb, s.gp);
+  // the hit's set-up, formed once per hit by hit_setup_kernel where the launch has it
+  const HitSetup<T> h = wb.hit_setup ? load_hit_setup(wb.hit_setup + (int64_t)8 * k) : hit_setup(p, c, wb, s.gp);
   s.point = h.point;
   s.fpar = c.fparam;
   // MainShadow, AmbientOcclusion and AuxShadow compare with the threshold stored in a float
@@ -1819,20 +1877,18 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
   s.sh = T(1);
   s.maxSoft = T(0);
   s.guard = 0;
-  const T factor = p.penetrating ? h.delta / c.resolution : p.viewDistanceMax;
-  const T shadowStart = p.f.interiorMode ? h.thr * p.DE_factor : h.thr;
   if (s.kind == 0) {
     s.dir = {c.lightVect[0], c.lightVect[1], c.lightVect[2]};
-    s.end = factor;
-    s.r = shadowStart;
+    s.end = h.shadowEnd;
+    s.r = h.shadowStart;
     s.detail = s.thr;
     s.stepMul = p.DE_factor;
   } else {
     // detailSize after MainShadow: the float threshold if its loop ran at least once
-    s.detail = (p.shadow && shadowStart < factor) ? s.thr : h.thr;
+    s.detail = (p.shadow && h.shadowStart < h.shadowEnd) ? s.thr : h.thr;
     if (s.kind == 1) {
       s.dir = {__ldg(&p.aoVec[3 * s.j + 0]), __ldg(&p.aoVec[3 * s.j + 1]), __ldg(&p.aoVec[3 * s.j + 2])};
-      s.end = h.delta / c.resolution;
+      s.end = h.aoEnd;
       s.r = h.delta;
       s.stepMul = T(2);
     }
@@ -2199,24 +2255,30 @@ __device__ __forceinline__ void volumetric_pool(const ParamsT<T> &p, const PoolR
     }
     return (int64_t)chunk * kChunk + (at - chunkBase);
   };
-  T curDist = T(0), curThr = T(0);   // narrow records: record `index`, read the turn before
-  if (!EFX && stepCount > 1) load_record_narrow(pr.rec + 2 * seek(stepCount - 1), curDist, curThr);
+  // narrow records: records `index` and index - 1 are read ahead, one turn apart, so that
+  // each turn's load (of index - 2) overlaps the turn's arithmetic
+  T curDist = T(0), curThr = T(0), prevDist = T(0), prevThr = T(0);
+  if (!EFX && stepCount > 1) {
+    load_record_narrow(pr.rec + 2 * seek(stepCount - 1), curDist, curThr);
+    load_record_narrow(pr.rec + 2 * seek(stepCount - 2), prevDist, prevThr);
+  }
   for (int index = stepCount - 1; index > 0; index--) {
     T distance, dist_thresh, step;
-    int64_t rec;
+    int64_t rec = 0;
     if constexpr (EFX) {
       rec = seek(index);
       load_record(pr.rec + 4 * rec, distance, dist_thresh, step);
     } else {
+      T nextDist = T(0), nextThr = T(0);
+      if (index >= 2) load_record_narrow(pr.rec + 2 * seek(index - 2), nextDist, nextThr);
       // the step that reached record `index` is the march's step after record index - 1
-      rec = seek(index - 1);
-      T prevDist, prevThr;
-      load_record_narrow(pr.rec + 2 * rec, prevDist, prevThr);
       step = march_step(p, prevDist, prevThr, stepFrac, pixel, (uint32_t)(index - 1));
       distance = curDist;
       dist_thresh = curThr;
       curDist = prevDist;
       curThr = prevThr;
+      prevDist = nextDist;
+      prevThr = nextThr;
     }
     totalStep += step;
     if (totalStep < dist_thresh * p.quality) continue;

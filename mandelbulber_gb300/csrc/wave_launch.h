@@ -81,6 +81,10 @@ struct WaveBufs {
   uint32_t *seg_count;                   // [segments][kHitSegWarps] hits per warp of each segment
                                          // of kHitSeg primary jobs (hit list in tile order; null =
                                          // kept in completion order)
+  T *hit_setup;                          // [k][8] the shadow/AO set-up of hit-list entry k (plain
+                                         // variant): point, thr, delta, AO end, shadow end and
+                                         // start (hit_setup_kernel); null with one ray per pixel
+                                         // not given
 };
 
 constexpr int kHitSegWarps = 4;          // warps per segment of the hit-list compaction

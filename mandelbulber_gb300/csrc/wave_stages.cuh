@@ -63,6 +63,9 @@ cudaError_t run_stages(const WaveLaunch<T> &L, cudaStream_t s) {
   // auxiliary lights: the hit normals, which the AuxShadow jobs test (counted with composition)
   if (L.wb.normal)
     dev::normal_kernel<T, F, FAST><<<L.polish_grid, L.block, 0, s>>>(L.p, stage_io(L.io, 3), L.wb, L.cams, L.ncams);
+  // the plain variant's per-hit set-up of the shadow and AO jobs
+  if (L.wb.hit_setup && !efx)
+    dev::hit_setup_kernel<T><<<L.polish_grid, L.block, 0, s>>>(L.p, L.wb, L.cams, L.ncams);
   bool pair = false;
   if constexpr (sizeof(T) == 4 && F == 8 && FAST) pair = L.wb.pair_rays && L.wb.orbit_refill <= 0 && !efx;
   if constexpr (sizeof(T) == 4 && F == 8 && FAST) {

@@ -35,9 +35,9 @@ def test_flight_batch_equals_single_frames(gpu_ctx, flight_small):
     st = gpu_ctx.stats()
     assert st.frames == 64
     assert st.pixels == sum(f.image_width * f.image_height for f in flight_small)
-    # one launch sequence: primary, polish, secondary, compose, and from 2^20 pixels on the
-    # three launches that put the hit list in tile order
-    assert st.launches == 4 + (3 if st.pixels >= 1 << 20 else 0), st.launches
+    # one launch sequence: primary, polish, the hits' shadow set-up, secondary, compose, and
+    # from 2^20 pixels on the three launches that put the hit list in tile order
+    assert st.launches == 5 + (3 if st.pixels >= 1 << 20 else 0), st.launches
     for i in (0, 1, 7, 8, 31, 63):
         single = gpu_ctx.render(flight_small[i])
         _same(batch[i], single, f"frame {i}")
@@ -168,12 +168,12 @@ def test_per_frame_fractal_parameter(gpu_ctx):
     # sequence: the parameter travels in the frame table
     bulbs = [W.workload("mandelbulb_640x480", 64, 48, power=pw) for pw in (6.5, 7.0, 9.25)]
     batch = gpu_ctx.render_batch(bulbs)
-    assert gpu_ctx.stats().launches == 4
+    assert gpu_ctx.stats().launches == 5   # primary, polish, shadow set-up, secondary, compose
     for i, f in enumerate(bulbs):
         _same(batch[i], gpu_ctx.render(f), f"power frame {i}")
     boxes = [W.workload("mandelbox_1080p", 96, 54, mandelbox_scale=sc) for sc in (2.0, 2.2, -1.5)]
     batch = gpu_ctx.render_batch(boxes)
-    assert gpu_ctx.stats().launches == 5   # + the overflow pass of the volumetric records
+    assert gpu_ctx.stats().launches == 6   # + the overflow pass of the volumetric records
     for i, f in enumerate(boxes):
         _same(batch[i], gpu_ctx.render(f), f"scale frame {i}")
     batch = gpu_ctx.render_batch(boxes, precision=mb.PREC_FP64)
