@@ -72,8 +72,25 @@ struct LeanOrbit<8> {
       dist = 0.0f;
       return true;
     }
+    if (L <= N - kUnroll) {   // a whole block: the count is tested once, after it
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) {
+      for (int u = 0; u < kUnroll; u++) {
+        const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
+        if (r2 > 1048576.0f) {
+          L += u;
+          dist = box_bailout_dist(r2, dr);
+          return true;
+        }
+      }
+      L += kUnroll;
+      if (L == N) {
+        dist = 0.0f;
+        return true;
+      }
+      return false;
+    }
+#pragma unroll 1
+    for (;;) {
       const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
       if (r2 > 1048576.0f) {
         dist = box_bailout_dist(r2, dr);
@@ -84,7 +101,6 @@ struct LeanOrbit<8> {
         return true;
       }
     }
-    return false;
   }
 };
 
