@@ -40,10 +40,11 @@ WORKLOAD = "mandelbox_1080p"
 # plus sqrt and divide of each DE evaluation
 FLOPS_PER_ITER = {8: 21, 2: 27}
 # dram__bytes_read.sum + dram__bytes_write.sum of secondary_kernel in one full 1920x1080
-# launch of this workload (a one-pass ncu capture of `bench.py --once 1920x1080`): 45.0 MB
-# read + 169.3 MB written, mostly the per-direction AO result slots, which outgrow L2 at
-# this size (at 480x270 they stay in L2, and a small capture sees almost no DRAM traffic)
-DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 214.3e6}
+# launch of this workload (a one-pass ncu capture of `bench.py --once 1920x1080`): 124.8 MB
+# read (the per-hit set-up records and hit list, once per block of 4096 hits) + 157.6 MB
+# written (the per-direction AO result slots that leave L2); at 480x270 both stay in L2, and
+# a small capture sees almost no DRAM traffic
+DRAM_BYTES_PER_LAUNCH = {"mandelbox_1080p": 282.4e6}
 FLOPS_PER_DE = {8: 2, 2: 4}
 PRECISION = "fp32 march/orbit/shading + fp64 ray origin and binary hit refinement"
 # the single-frame workloads bench.py times (the scenes are built by mandelbulber_gb300.workloads;

@@ -1657,6 +1657,9 @@ __device__ __forceinline__ SecondaryJobs secondary_jobs(const ParamsT<T> &p, con
   return j;
 }
 
+// Hits per block of the plain variant's AO job order (a power of two).
+constexpr unsigned int kAoBlock = 4096;
+
 // State of one shadow (kind 0), AO (kind 1) or auxiliary-light shadow (kind 2) ray.
 template <typename T>
 struct SecondaryRay {
@@ -1871,10 +1874,21 @@ __device__ __forceinline__ bool secondary_begin(const ParamsT<T> &p, const WaveB
     s.kind = 0;
     k = job;
   } else if (job < jn.nShadow + jn.nAO) {
+    // AO jobs in blocks of kAoBlock hits, every direction of a block before the next block,
+    // so that the block's set-up records stay in cache over its aoCount sweeps; a warp's jobs
+    // are still consecutive hits (one tile) in one direction
     const unsigned int q = job - jn.nShadow;
+    const unsigned int perBlock = kAoBlock * (unsigned int)p.aoCount;
+    const unsigned int b = q / perBlock, r = q - b * perBlock, base = b * kAoBlock;
     s.kind = 1;
-    s.j = q / nh;
-    k = q - s.j * nh;
+    if (nh - base >= kAoBlock) {
+      s.j = r / kAoBlock;
+      k = base + r % kAoBlock;
+    } else {   // the last, partial block
+      const unsigned int g = nh - base;
+      s.j = r / g;
+      k = base + (r - s.j * g);
+    }
   } else {
     const unsigned int q = job - jn.nShadow - jn.nAO;
     s.kind = 2;
