@@ -283,7 +283,10 @@ __device__ __forceinline__ float bulb8_iteration(float &x, float &y, float &z, c
 
 // Mandelbulb power 8 orbit. MODE 0 returns the distance estimate 0.5*r*ln(r)/dr at the
 // bailout r > 100 (or the scene's bailoutRadius: r^2 > FractalT::bailout2); MODE 1 returns
-// the colouring value (min |z| until |z| > 1e15, times 5000).
+// the colouring value (min |z| until |z| > 1e15, times 5000). The iterations run in blocks of
+// kBulbBlock with the end test after each and the count test once per block (a remainder
+// loop takes N mod kBulbBlock), as the lean Mandelbox orbit's box_orbit does.
+constexpr int kBulbBlock = 4;
 template <int MODE>
 __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, const float px, const float py,
                                                   const float pz, const int N, int &Lout, Counters &cnt) {
@@ -297,19 +300,36 @@ __device__ __forceinline__ float mandelbulb8_fast(const FractalT<float> &f, cons
   float r2 = norm2_rn(x, y, z);
   float minr2 = __int_as_float(0x7f800000);
   const float bail2 = f.bailout2;
-  int L;
-  for (L = 0; L < N; L++) {
+  // one iteration; true when the orbit ends at it
+  auto step = [&]() -> bool {
     r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
-    if (MODE == 0) {
-      if (r2 > bail2) {
-        const float r = sqrtf(r2);
-        dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
+    if (MODE == 0) return r2 > bail2;
+    if (r2 < minr2) minr2 = r2;
+    return r2 > 1.0e30f;
+  };
+  int L = 0;
+  bool ended = false;
+  while (!ended && L <= N - kBulbBlock) {
+#pragma unroll
+    for (int u = 0; u < kBulbBlock; u++) {
+      if (step()) {
+        L += u;
+        ended = true;
         break;
       }
-    } else {
-      if (r2 < minr2) minr2 = r2;
-      if (r2 > 1.0e30f) break;
     }
+    if (!ended) L += kBulbBlock;
+  }
+#pragma unroll 1
+  for (; !ended && L < N; L++) {
+    if (step()) {
+      ended = true;
+      break;
+    }
+  }
+  if (MODE == 0 && ended) {
+    const float r = sqrtf(r2);
+    dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
   }
   cnt.orbit += (unsigned long long)(L + 1);
   cnt.calls += 1;

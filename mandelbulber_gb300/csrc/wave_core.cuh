@@ -138,8 +138,26 @@ struct LeanOrbit<2> {
       dist = 0.0f;
       return true;
     }
+    if (L <= N - kUnroll) {   // a whole block: the count is tested once, after it
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) {
+      for (int u = 0; u < kUnroll; u++) {
+        r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
+        if (r2 > bail2) {
+          L += u;
+          const float r = sqrtf(r2);
+          dist = __fmul_rn(__fmul_rn(0.5f, r), __logf(r)) / r_dz;
+          return true;
+        }
+      }
+      L += kUnroll;
+      if (L == N) {
+        dist = 0.0f;
+        return true;
+      }
+      return false;
+    }
+#pragma unroll 1
+    for (;;) {
       r2 = bulb8_iteration(x, y, z, r2, r_dz, cx, cy, cz);
       if (r2 > bail2) {
         const float r = sqrtf(r2);
@@ -151,7 +169,6 @@ struct LeanOrbit<2> {
         return true;
       }
     }
-    return false;
   }
 };
 
