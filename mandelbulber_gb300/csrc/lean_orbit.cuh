@@ -61,41 +61,6 @@ __device__ __forceinline__ float box_iteration(const LeanBoxK &k, const float s,
   return norm2_rn(x, y, z);
 }
 
-// The lean Mandelbox orbit of (x, y, z) with constant c, at most N iterations: returns the
-// distance estimate r / |dr| at the first iteration whose radius passes the bailout
-// (r^2 > 1024^2), with that iteration's index in L, or 0 with L = N when the orbit stays
-// bounded. The iterations run in blocks of kBoxBlock, each followed by its bailout test,
-// and the iteration count is tested once per block (a remainder loop takes N mod
-// kBoxBlock), so the loop spends no instructions on the count inside a block.
-constexpr int kBoxBlock = 5;
-
-__device__ __forceinline__ float box_orbit(const LeanBoxK &k, const float s, const float skm1, float x, float y,
-                                           float z, const float cx, const float cy, const float cz, const int N,
-                                           int &L) {
-  float dr = 1.0f;
-  int l = 0;
-  for (; l <= N - kBoxBlock; l += kBoxBlock) {
-#pragma unroll
-    for (int u = 0; u < kBoxBlock; u++) {
-      const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
-      if (r2 > 1048576.0f) {
-        L = l + u;
-        return box_bailout_dist(r2, dr);
-      }
-    }
-  }
-#pragma unroll 1
-  for (; l < N; l++) {
-    const float r2 = box_iteration(k, s, skm1, x, y, z, dr, cx, cy, cz);
-    if (r2 > 1048576.0f) {
-      L = l;
-      return box_bailout_dist(r2, dr);
-    }
-  }
-  L = N;
-  return 0.0f;
-}
-
 // ---- Packed FP32 (f32x2): two orbits per thread ----
 // A pair of floats in one 64-bit register pair: low half = ray A, high half = ray B. The
 // f32x2 add / mul / fma each round both halves exactly as the scalar .rn instructions do,
@@ -179,6 +144,65 @@ __device__ __forceinline__ f2 box_iteration_x2(const LeanBoxK &k, BoxPair &o) {
   o.nz = f2_fma(z, nks, o.ncz);
   o.dr = f2_fma(o.dr, aks, one);
   return f2_fma(o.nz, o.nz, f2_fma(o.ny, o.ny, f2_mul(o.nx, o.nx)));
+}
+
+// One Mandelbox iteration (box_iteration) with x and y in one f32x2 pair, kept NEGATED
+// (nxy = (-x, -y), ncxy = (-cx, -cy)), and z scalar. The box fold of x and y is one packed FMA,
+// fma(clamp(-x), -2, -x) = round(2 clamp(x) - x) (the clamp interval is symmetric), which
+// leaves the folded pair positive; the scale of the pair is another, fma(fx, -ks, -cx) =
+// -round(fx ks + cx), with -ks = fma(t, -s(k1 - 1), -s) formed as box_iteration forms ks.
+// Every lane rounds as box_iteration's scalar FMAs do, so the orbit is the same bit for bit.
+__device__ __forceinline__ float box_iteration_xy(const LeanBoxK &k, const float ns, const float nskm1, f2 &nxy,
+                                                  float &z, float &dr, const f2 ncxy, const float cz) {
+  const float fl = k.fl;
+  const f2 cl = f2_pack(fminf(fmaxf(f2_lo(nxy), -fl), fl), fminf(fmaxf(f2_hi(nxy), -fl), fl));
+  const f2 fxy = f2_fma(cl, f2_pack(-2.0f, -2.0f), nxy);
+  z = fmaf(fminf(fmaxf(z, -fl), fl), 2.0f, -z);
+  const float r2 = norm2_rn(f2_lo(fxy), f2_hi(fxy), z);
+  const float nks = fmaf(__saturatef(fmaf(k.sa, rcp_approx(r2), -k.sb)), nskm1, ns);
+  nxy = f2_fma(fxy, f2_pack(nks, nks), ncxy);
+  z = fmaf(z, -nks, cz);
+  dr = fmaf(dr, fabsf(nks), 1.0f);
+  return norm2_rn(f2_lo(nxy), f2_hi(nxy), z);
+}
+
+// The lean Mandelbox orbit of (x, y, z) with constant c, at most N iterations: returns the
+// distance estimate r / |dr| at the first iteration whose radius passes the bailout
+// (r^2 > 1024^2), with that iteration's index in L, or 0 with L = N when the orbit stays
+// bounded. The iterations run in blocks of kBoxBlock, each followed by its bailout test,
+// and the iteration count is tested once per block (a remainder loop takes N mod
+// kBoxBlock), so the loop spends no instructions on the count inside a block. The iteration
+// is box_iteration_xy, box_iteration's values with x and y in one packed pair.
+constexpr int kBoxBlock = 5;
+
+__device__ __forceinline__ float box_orbit(const LeanBoxK &k, const float s, const float skm1, float x, float y,
+                                           float z, const float cx, const float cy, const float cz, const int N,
+                                           int &L) {
+  float dr = 1.0f;
+  f2 nxy = f2_pack(-x, -y);
+  const f2 ncxy = f2_pack(-cx, -cy);
+  const float ns = -s, nskm1 = -skm1;
+  int l = 0;
+  for (; l <= N - kBoxBlock; l += kBoxBlock) {
+#pragma unroll
+    for (int u = 0; u < kBoxBlock; u++) {
+      const float r2 = box_iteration_xy(k, ns, nskm1, nxy, z, dr, ncxy, cz);
+      if (r2 > 1048576.0f) {
+        L = l + u;
+        return box_bailout_dist(r2, dr);
+      }
+    }
+  }
+#pragma unroll 1
+  for (; l < N; l++) {
+    const float r2 = box_iteration_xy(k, ns, nskm1, nxy, z, dr, ncxy, cz);
+    if (r2 > 1048576.0f) {
+      L = l;
+      return box_bailout_dist(r2, dr);
+    }
+  }
+  L = N;
+  return 0.0f;
 }
 
 }  // namespace dev
