@@ -38,7 +38,7 @@ typedef enum mbgb_status {
   MBGB_ERR_OOM = 2,         /* device or host allocation failed */
   MBGB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
   MBGB_ERR_TIMEOUT = 4,     /* a kernel hit its device-side deadline and stopped early */
-  MBGB_ERR_UNSUPPORTED = 5, /* the scene uses a feature this build does not render */
+  MBGB_ERR_UNSUPPORTED = 5, /* the scene uses a feature the library does not render */
   MBGB_ERR_IO = 6,          /* settings file could not be read / image could not be written */
   MBGB_ERR_NO_DEVICE = 7    /* no CUDA device visible */
 } mbgb_status;

@@ -10,7 +10,7 @@
 //     -res WIDTHxHEIGHT      override image_width / image_height
 //     -fpk N                 override frames_per_keyframe
 //     -o key=value           override one setting
-//   options of this build:
+//   options of mbgb_cli only:
 //     -defaults FILE         settings read before the settings file (default: none)
 //     -precision fp64|fp32|auto    render policy (default fp32: FP32 with FP64 refinement)
 //     -batch N               frames rendered per launch sequence (default 16)
@@ -21,8 +21,8 @@
 // to 16 bits (CompileImage), post-processed with SSAO when post_SSAO_enabled is set and with
 // the depth of field when post_DOF_enabled is set, and
 // written as IndexFilename(file_destination, ext, frame) = destination%05d.ext.
-// JPEG needs libjpeg, which this build does not carry: -format jpg writes an 8-bit PNG.
-// Network rendering (-ip, -port) and tiled output are not part of this build.
+// JPEG needs libjpeg, which mbgb_cli does not link: -format jpg writes an 8-bit PNG.
+// Network rendering (-ip, -port) and tiled output are not supported by mbgb_cli.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -136,7 +136,7 @@ bool parse(int argc, char **argv, Args &a) {
       continue;
     }
     if (s == "-ip" || s == "-port") {
-      printf("commandline: network rendering is not part of this build\n");
+      printf("commandline: network rendering is not supported by mbgb_cli\n");
       return false;
     }
     if (s == "-help" || i < argc - 1) return false;
@@ -224,7 +224,7 @@ bool render_jobs(mbgb_context *ctx, const std::vector<Job> &jobs, const Args &a)
     ok = mbgb_compile_image16_device(ctx, &sc, outs[i].image_float, w, h, img16[i]) == MBGB_OK;
     if (ok && sc.SSAOEnabled) ok = mbgb_ssao_device(ctx, &sc, &outs[i], img16[i]) == MBGB_OK;
     // the DOF shuffle draws from rand(); the reference continues its process's stream there,
-    // this build seeds it with the scene's colouring seed
+    // mbgb_cli seeds it with the scene's colouring seed
     if (ok && sc.DOFEnabled) ok = mbgb_dof_device(ctx, &sc, &outs[i], img16[i], (uint32_t)sc.coloring_seed) == MBGB_OK;
     if (!ok) {
       fprintf(stderr, "mbgb_cli: post-processing: %s\n", mbgb_last_error());
@@ -281,7 +281,7 @@ int main(int argc, char **argv) {
     return 1;
   }
   if (scene.noOfTiles > 1) {
-    fprintf(stderr, "mbgb_cli: tiled output is not part of this build\n");
+    fprintf(stderr, "mbgb_cli: tiled output is not supported\n");
     return 1;
   }
   char buf[1000];
@@ -291,7 +291,7 @@ int main(int argc, char **argv) {
     dest = buf;
   const char *ext = a.format == kJPG ? "jpg" : "png";
   if (a.format == kJPG) {
-    printf("mbgb_cli: no JPEG writer in this build; writing 8-bit PNG files\n");
+    printf("mbgb_cli: no JPEG writer; writing 8-bit PNG files\n");
     ext = "png";
   }
   mbgb_context *ctx = nullptr;

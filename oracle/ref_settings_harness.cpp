@@ -14,7 +14,7 @@
 //     the rotation matrices of RecalculateIFSParams (src/callbacks.cpp:1538-1556) are
 //     computed with the reference's own CRotationMatrix and CVector3::Normalize.
 // The resulting sParamRender is copied field by field into an mbgb_scene (names follow
-// the reference's fields), so tests can compare this build's settings reader with the
+// the reference's fields), so tests can compare the library's settings reader with the
 // reference's byte for byte. Used only by tests/golden/make_golden.py and the settings
 // tests; nothing in the product loads it.
 #include <cstdio>

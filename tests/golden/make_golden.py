@@ -24,7 +24,7 @@ the tests rebuild the exact input without the reference tree.
 
 Every scene is read by the reference's own settings code (src/settings.cpp compiled in
 place into oracle/_ref/libmbref_settings.so) and the -nogui derivations, never by this
-build's reader: the parity tests then inherit no parsing of this build. The reference tree
+library's reader: the parity tests then inherit nothing from the library's parsing. The reference tree
 is found through oracle/Makefile (MBGB_REF_TREE).
 """
 from __future__ import annotations
@@ -111,9 +111,9 @@ FORMULA_DE = (("trigde", "mandelbulb_640x480", {"formula": 1}, 1.6),
               ("vary4d", "mandelbox_1080p", {**W.VARY4D, "mandelbox_scale": 2.0}, 4.0))
 
 
-# Example scenes of the reference (share/examples/*.fract, read through this build's settings
-# loader after share/defaults) at 48 x 32 with SSAO off; a few get one feature switched off
-# that this build does not render (the override is recorded in the fixture). The fixture
+# Example scenes of the reference (share/examples/*.fract, read by the reference's own settings
+# code after share/defaults) at 48 x 32 with SSAO off; a few get one feature switched off
+# that the library does not render (the override is recorded in the fixture). The fixture
 # stores the loaded scene as bytes, so the tests need neither the reference tree nor the files.
 EXAMPLES = {
     "ifs_sierpinski": ("IFS Sierpinski.fract", {}),
