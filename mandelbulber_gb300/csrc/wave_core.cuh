@@ -355,8 +355,8 @@ __device__ __forceinline__ void load_record_narrow(const double *r, double &dist
 }
 
 // The march's next step after the estimate `dist` at threshold `thr` of march step i
-// (src/Render3D.cpp:129-137): the distance clamped at 3, less stepFrac thresholds, times the
-// DE factor, with the step jitter when it is on. One function for the march and for the
+// (src/Render3D.cpp:117, 127-134): the distance clamped at 3, less stepFrac thresholds, times
+// the DE factor, with the step jitter when it is on. One function for the march and for the
 // volumetric walk's recomputation, so that both round alike (the FP32 form spells out its
 // multiply-add).
 template <typename T>
