@@ -552,8 +552,6 @@ static void fill_params(const mbgb_scene &s, ParamsT<T> &p, const mbgb_opts &o, 
   p.fogInvVisibility = (T)(1.0 / (double)p.fogVisibility);
   p.fogDistFactor2 = p.fogDistFactor * p.fogDistFactor;
   for (int c = 0; c < 3; c++) {
-    p.glowCol1[c] = (T)p.glow1[c] / (T)65536;
-    p.glowCol2[c] = (T)p.glow2[c] / (T)65536;
     p.fogColorS[c] = (T)p.fogColor[c] / (T)65536;
     p.fogCol1S[c] = (T)p.fogCol1[c] / (T)65536;
     p.fogCol2S[c] = (T)p.fogCol2[c] / (T)65536;

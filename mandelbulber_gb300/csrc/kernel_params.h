@@ -166,7 +166,7 @@ struct ParamsT {
   // distances and of the post-fog visibility, fogDistFactor^2, and every colour divided by
   // 65536 (exact)
   T fogInvC1Dist, fogInvC2Dist, fogInvVisibility, fogDistFactor2;
-  T glowCol1[3], glowCol2[3], fogColorS[3], fogCol1S[3], fogCol2S[3], fogCol3S[3];
+  T fogColorS[3], fogCol1S[3], fogCol2S[3], fogCol3S[3];
   // auxiliary lights (AuxLightsShader / LightShading / AuxShadow, src/shaders.cpp:997-1132)
   int auxLightNumber;      // random lights; the shaders also read lights 0-3 when enabled
   int numberOfLights;      // max(auxLightNumber, 4), 0 when the scene has no aux lights
